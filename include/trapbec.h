@@ -1,0 +1,268 @@
+/*
+ * trapbec.h -- C ABI of the GB300 time-stepping engine for the TrapBEC
+ * Gross-Pitaevskii solver.
+ *
+ * The reference program (Fortran 90 + MPI) has no library interface: its hot
+ * path is a set of argument-less module procedures acting on module globals
+ * (get_rhs, ghost_comm, Psi_norm, Psi_info) and inline loops in `program run`.
+ * Each entry point below replaces one of those pieces; the comment on each
+ * names the reference lines it stands in for (paths relative to the
+ * reference project root).
+ *
+ * Conventions
+ *  - Every function returns an int status: 0 (TRAPBEC_OK) on success, a
+ *    positive TRAPBEC_ERR_* code otherwise.  Nothing throws or exits across
+ *    the ABI.  trapbec_strerror() maps a code to text; trapbec_last_error()
+ *    gives the detail of the last failure on the calling thread.
+ *  - Host arrays are owned by the caller and copied at set/get time.  Device
+ *    buffers are owned by the context.
+ *  - Complex arrays are interleaved (re, im) pairs, layout-compatible with
+ *    Fortran complex(c_float_complex) / complex(c_double_complex) and C99
+ *    float _Complex / double _Complex.  Their element type is the context's
+ *    precision (TRAPBEC_FP32 -> float pairs, TRAPBEC_FP64 -> double pairs).
+ *  - Array order is the reference's Psi(k,j,i): z fastest, then y, then x.
+ *  - One host thread per context; each context owns one CUDA stream and all
+ *    of its calls are ordered on it.  get/diag calls synchronise.
+ *  - All quantities are in the reference's units (healing-length units with
+ *    g = mu = 1/2 folded into the equation, finite_diff.f90:23-27,128-132).
+ */
+#ifndef TRAPBEC_H
+#define TRAPBEC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TRAPBEC_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------ */
+enum trapbec_status {
+  TRAPBEC_OK = 0,
+  TRAPBEC_ERR_ARG = 1,         /* bad argument / parameter combination      */
+  TRAPBEC_ERR_CUDA = 2,        /* a CUDA runtime or driver call failed      */
+  TRAPBEC_ERR_NOMEM = 3,       /* device or host allocation failed          */
+  TRAPBEC_ERR_STATE = 4,       /* call not valid in the current state       */
+  TRAPBEC_ERR_TIMEOUT = 5,     /* a bounded device-side wait gave up        */
+  TRAPBEC_ERR_NONFINITE = 6,   /* NaN/Inf detected in psi by a reduction    */
+  TRAPBEC_ERR_IO = 7,          /* file could not be read or written         */
+  TRAPBEC_ERR_UNSUPPORTED = 8, /* option not built for this configuration   */
+  TRAPBEC_ERR_PARSE = 9,       /* cparam.local text could not be parsed     */
+  TRAPBEC_ERR_NODEVICE = 10    /* no CUDA device / driver available         */
+};
+
+/* ---- enumerations mirroring the cparam.local string parameters ---------- */
+enum trapbec_boundaries {      /* cparam.local `boundaries`, ghost.f90:53-60 */
+  TRAPBEC_BC_ZERO = 0,
+  TRAPBEC_BC_SOLID = 1,
+  TRAPBEC_BC_PERIODIC = 2
+};
+
+enum trapbec_potential {       /* cparam.local `potential`, finite_diff.f90:29-124 */
+  TRAPBEC_POT_ZERO = 0,
+  TRAPBEC_POT_HARMONIC = 1,
+  TRAPBEC_POT_HARMONIC_RING = 2,
+  TRAPBEC_POT_HARMONIC_RING2 = 3,
+  TRAPBEC_POT_BARRIER = 4,
+  TRAPBEC_POT_BOX_TRAP = 5,
+  TRAPBEC_POT_CHANNEL = 6,
+  TRAPBEC_POT_QUARTIC = 7,
+  TRAPBEC_POT_SPHERE = 8,
+  TRAPBEC_POT_MOBIUS = 9,      /* reads the Trap array (trapbec_set_trap) + marker */
+  TRAPBEC_POT_ARRAY = 10       /* plain Trap array, no marker (new)            */
+};
+
+enum trapbec_precision { TRAPBEC_FP32 = 0, TRAPBEC_FP64 = 1 };
+
+enum trapbec_layout {
+  TRAPBEC_LAYOUT_INTERIOR = 0, /* Psi(1:nz,1:ny,1:nx)                         */
+  TRAPBEC_LAYOUT_GHOSTED = 1   /* Psi(-2:nz+3,-2:ny+3,-2:nx+3), initial.f90:16 */
+};
+
+enum trapbec_imag_variant {
+  TRAPBEC_IMAG_REF_EULER = 0,  /* Psi = Psi + dt*0.5*rhs, no renorm, run.f90:19-35 */
+  TRAPBEC_IMAG_RK3_RENORM = 1  /* low-storage RK3 in imaginary time + FP64
+                                  renormalisation + |dE| stop (new)           */
+};
+
+enum trapbec_scalar {          /* run-time changeable scalars (trapbec_set_scalar) */
+  TRAPBEC_SCALAR_OMEGA_Z = 0,
+  TRAPBEC_SCALAR_DT_RE = 1,
+  TRAPBEC_SCALAR_DT_IM = 2,
+  TRAPBEC_SCALAR_GAMMA = 3,
+  TRAPBEC_SCALAR_T = 4,
+  TRAPBEC_SCALAR_ADVECTIVE_VX = 5,
+  TRAPBEC_SCALAR_NORM_TARGET = 6
+};
+
+/* ---- parameters: the hot-path subset of cparam.local ------------------- */
+/* cparam.local:2-44 and mpi_var.f90:147-156.  Field names follow the
+ * Fortran parameter names.  nprocx/nprocy do not split the device domain
+ * (one GPU holds the whole grid); they only reproduce the coordinate
+ * arithmetic of an MPI run on an nprocx x nprocy process grid
+ * (initial.f90:34-42), so results can be compared with such a run.        */
+typedef struct trapbec_params {
+  int32_t nx, ny, nz;          /* Nx, Ny, Nz: global grid                     */
+  int32_t nprocx, nprocy;      /* virtual process grid (default 1,1)          */
+  int32_t precision;           /* trapbec_precision                           */
+  int32_t boundaries;          /* trapbec_boundaries                          */
+  int32_t periodicz;           /* logical periodicz                           */
+  int32_t two_dim;             /* logical two_dim                             */
+  int32_t potential;           /* trapbec_potential                           */
+  int32_t lbeam;               /* logical lbeam                               */
+  int32_t winding_number;      /* integer winding_number                      */
+  double lx, ly, lz;           /* Lx, Ly, Lz                                  */
+  double dt_re, dt_im;         /* complex dt                                  */
+  double gamma;                /* dissipation, applied as dt*(1-i*gamma)      */
+  double harm_wx, harm_wy, harm_wz;
+  double potential_off;        /* pot = 0 once t > potential_off              */
+  double wbeam;                /* laser width                                 */
+  double advective_vx;         /* moving frame velocity                       */
+  double omega_z;              /* rotating frame angular velocity             */
+  double t_spindown;           /* rotation switched off once t >= t_spindown  */
+  double ring_rad;             /* vortex ring radius (initial states)         */
+  int32_t vor_ring_count;      /* number of random rings (initial states)     */
+  int32_t reserved[7];         /* zero                                        */
+} trapbec_params;
+
+/* Fill *p with the defaults of the shipped cparam.local (cparam.local:2-44)
+ * but precision FP64, 64^3, 'zero' boundaries, 'harmonic' potential.       */
+int trapbec_params_default(trapbec_params* p);
+
+/* Parse cparam.local text (Fortran declarations `type :: name=value, ...`)
+ * into *p, starting from the current contents of *p.  Unknown names that
+ * the hot path needs are errors; names the hot path ignores are accepted.
+ * errbuf (may be NULL) receives a one-line message on failure.
+ * Replaces the compile-time include of cparam.local (cdata.f90:3).        */
+int trapbec_params_parse(const char* text, trapbec_params* p, char* errbuf, size_t errlen);
+
+/* ---- context ------------------------------------------------------------ */
+typedef struct trapbec_ctx trapbec_ctx;
+
+/* Allocate device state for one grid on the current CUDA device.
+ * Replaces mpi_setup + mesh_init's allocations and coordinates
+ * (mpi_var.f90:14-43, initial.f90:16-42) and ghost_init (ghost.f90:16-26). */
+int trapbec_create(const trapbec_params* p, trapbec_ctx** out);
+void trapbec_destroy(trapbec_ctx* ctx);
+
+/* Copy psi host->device / device->host.  layout: trapbec_layout.  For the
+ * GHOSTED layout only the interior is read on set; on get the ghost cells
+ * are filled the way ghost_comm leaves them (ghost.f90:27-192).            */
+int trapbec_set_psi(trapbec_ctx* ctx, const void* psi, int layout);
+int trapbec_get_psi(trapbec_ctx* ctx, void* psi, int layout);
+
+/* Set the Trap(1:nz,1:ny,1:nx) array (cdata.f90:10) used by the 'mobius' and
+ * 'array' potentials; values are FP64 and converted to the context precision. */
+int trapbec_set_trap(trapbec_ctx* ctx, const double* trap);
+
+/* Fill psi with one of the reference's initial states (initial.f90:58-157
+ * and the helpers :202-870), evaluated on the device.  Random draws use a
+ * seeded counter-based generator instead of the clock-seeded Fortran RNG
+ * (mpi_var.f90:183-209).  Also accepts the states of the workload set:
+ * "tf_vortex_line", "tf_vortex_ring" (see trapbec_init_args).              */
+typedef struct trapbec_init_args {
+  uint64_t seed;               /* RNG seed                                    */
+  double amp;                  /* overall amplitude (new states)              */
+  double r_tf2[3];             /* TF inverse radii^2 per axis (new states)    */
+  double ring_radius;          /* ring radius (tf_vortex_ring)                */
+  double core2;                /* Pade core parameter (rho^2 + core2)         */
+  double noise_amp;            /* phase-noise amplitude (tf_vortex_ring)      */
+  double reserved[4];
+} trapbec_init_args;
+int trapbec_init_state(trapbec_ctx* ctx, const char* init_cond, const trapbec_init_args* args);
+
+/* Evaluate rhs = get_rhs(psi) for the current psi without stepping and copy
+ * it to host memory (interior layout).  Replaces finite_diff.f90:8-136.    */
+int trapbec_get_rhs(trapbec_ctx* ctx, void* rhs_out);
+
+/* Advance nsteps real-time low-storage RK3 steps with dt*(1-i*gamma).
+ * *t_inout is the simulation time t (cdata.f90:18), advanced by Re(dt) per
+ * step.  Replaces run.f90:42-57 (one call per `shots` block).            */
+int trapbec_step_rt(trapbec_ctx* ctx, int nsteps, double* t_inout);
+
+/* Imaginary-time relaxation.
+ *  REF_EULER : nsteps of Psi = Psi + dt*0.5*rhs (run.f90:19-35); *stat_out
+ *              receives the last norm ratio intPsi2/intPsi2_old (run.f90:23).
+ *  RK3_RENORM: up to nsteps RK3 steps with real step Re(dt); after each step
+ *              psi is renormalised to the norm target (FP64) and the FP64
+ *              energy is formed; stops when |E_n - E_{n-1}| <= tol*|E_n|.
+ *              *stat_out receives the last |dE|/|E|.
+ * *steps_done receives the number of steps taken.                          */
+int trapbec_step_imag(trapbec_ctx* ctx, int nsteps, int variant, double tol,
+                      int* steps_done, double* stat_out);
+
+/* Diagnostics of the current psi.  intpsi2/maxpsi/minpsi/meanpsi follow
+ * Psi_norm and Psi_info (diagnostic.f90:7-25) but are summed in FP64 with
+ * compensation.  The rest are new (FP64): energy, chemical potential and
+ * their pieces, in reference units with the cell volume dV = hx*hy*hz.     */
+typedef struct trapbec_diag_out {
+  double intpsi2;              /* sum |psi|^2 (no dV), Psi_norm               */
+  double maxpsi, minpsi, meanpsi; /* Psi_info                                 */
+  double norm;                 /* dV * sum |psi|^2                            */
+  double energy;               /* dV * sum[-1/2 Re psi* lap + 1/2 pot|psi|^2
+                                         + 1/4 |psi|^4 - 1/2 Re psi* rot]     */
+  double mu;                   /* <psi|H|psi>/<psi|psi> without the -1/2 shift */
+  double kinetic, potential, interaction, rotation; /* raw sums (no dV)       */
+  int32_t nonfinite;           /* 1 if any NaN/Inf was seen                    */
+  int32_t reserved;
+} trapbec_diag_out;
+int trapbec_diag(trapbec_ctx* ctx, trapbec_diag_out* out);
+
+/* Change a scalar between calls (trapbec_scalar), e.g. an Omega ramp.     */
+int trapbec_set_scalar(trapbec_ctx* ctx, int which, double value);
+int trapbec_get_scalar(trapbec_ctx* ctx, int which, double* value);
+
+/* Select the stage kernel: 0 = automatic (tiled TMA kernel where the grid
+ * allows it), 1 = simple per-cell kernel, 2 = tiled kernel (error if the
+ * grid does not allow it).  tile_z/tile_y = 0 lets the autotuner choose.   */
+int trapbec_set_kernel(trapbec_ctx* ctx, int kind, int tile_z, int tile_y);
+
+/* Kernels launched by this context since creation (for launch accounting). */
+int trapbec_launch_count(trapbec_ctx* ctx, int64_t* count);
+
+/* Device time of the stage kernels of the last trapbec_step_* call, ms,
+ * measured with events on the context stream around the kernels.          */
+int trapbec_last_kernel_ms(trapbec_ctx* ctx, double* ms);
+
+/* ---- output / restart layout (output.f90:48-118, initial.f90:796-818) --- */
+/* Write data/proc000/var####.dat (one unformatted record: coords(2) int32,
+ * Lx, Ly, Lz, t, Psi interior) or imag_var####.dat, and the 3-record restart
+ * file var.dat (itime+1, t, Psi).  Real kind follows the precision.        */
+int trapbec_write_var(trapbec_ctx* ctx, const char* datadir, int itime, int shots,
+                      double t, int imaginary);
+int trapbec_write_restart(trapbec_ctx* ctx, const char* datadir, int itime, double t);
+/* Read var.dat (proc000, or proc00 as the reference reader expects).        */
+int trapbec_read_restart(trapbec_ctx* ctx, const char* datadir, int* nstart, double* t);
+int trapbec_write_dims(const trapbec_params* p, const char* datadir);
+int trapbec_write_timing(const trapbec_params* p, const char* datadir,
+                         double time_per_timestep, double tot_comm_time);
+
+/* ---- batched imaginary-time ground states (new) ------------------------- */
+/* Many independent instances (own grid size, trap, g via units, Omega) are
+ * relaxed together: each RK3 stage is one persistent launch over the work
+ * of all unconverged instances; the step loop is captured in a CUDA graph. */
+typedef struct trapbec_batch trapbec_batch;
+int trapbec_batch_create(int ninst, const trapbec_params* params, trapbec_batch** out);
+void trapbec_batch_destroy(trapbec_batch* b);
+int trapbec_batch_set_psi(trapbec_batch* b, int inst, const void* psi);
+int trapbec_batch_get_psi(trapbec_batch* b, int inst, void* psi);
+/* Relax all instances: up to max_steps steps each, convergence when
+ * |dE|/|E| <= tol.  check_every = steps per graph replay between host checks.
+ * steps_out[ninst], energy_out[ninst], mu_out[ninst] (may be NULL).        */
+int trapbec_batch_solve_imag(trapbec_batch* b, int max_steps, double tol, int check_every,
+                             int* steps_out, double* energy_out, double* mu_out);
+
+/* ---- errors ------------------------------------------------------------- */
+const char* trapbec_strerror(int code);
+const char* trapbec_last_error(void);
+int trapbec_abi_version(void);
+/* sizeof of the ABI structs (0: trapbec_params, 1: trapbec_diag_out,
+ * 2: trapbec_init_args), so bindings can check their mirrors.            */
+int trapbec_abi_struct_size(int which);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TRAPBEC_H */

@@ -1,0 +1,913 @@
+// trapbec_oracle.cpp -- CPU restatement of TrapBEC's time-stepping hot path.
+//
+// TEST INFRASTRUCTURE ONLY.  This file is the checker: tests, the smoke check
+// and the CPU-baseline leg of the benchmark call it to produce the answers the
+// CUDA path must reproduce.  Nothing in the shipped library links, loads or
+// calls it.
+//
+// Parity status: the reference is Fortran 90 + MPI and no Fortran compiler or
+// MPI exists in the build or GPU images, so the reference binary cannot be run
+// and the reference ships no golden vectors.  This restatement is therefore
+// pinned by known-answer tests derived from mathematics (stencil exactness on
+// polynomials, convergence order, the RK3 amplification polynomial, the Lz
+// eigenvalue, norm conservation, the harmonic-oscillator ground state) and not
+// by reference outputs ("parity unpinned" against the reference binary).
+//
+// It follows the reference statement by statement, in the same evaluation
+// order, with T = float for the shipped single-precision build and
+// T = double for the -fdefault-real-8 build:
+//   coordinates        initial.f90:26,34-42
+//   ghost fill         ghost.f90:27-192 (local fills + the face exchange of
+//                      an nprocx x nprocy process grid, done in-process)
+//   stencils           deriv.f90:12-25
+//   get_rhs            finite_diff.f90:8-136
+//   RK3 / imag Euler   run.f90:19-57
+//   Psi_info/Psi_norm  diagnostic.f90:7-25
+//   initial states     initial.f90:58-157,202-870
+// and adds the FP64 energy / chemical potential and the RK3 imaginary-time
+// relaxation with renormalisation, which the reference does not have.
+// Complex arithmetic is written out in real arithmetic so the operation order
+// is explicit; operations gfortran lowers component-wise (complex * real,
+// complex / real) are component-wise here too.  Build with -ffp-contract=off.
+
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+#include <limits>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "../include/trapbec.h"
+
+namespace {
+
+template <typename T> struct C {  // complex value, explicit arithmetic
+  T re, im;
+};
+template <typename T> inline C<T> cadd(C<T> a, C<T> b) { return {a.re + b.re, a.im + b.im}; }
+template <typename T> inline C<T> csub(C<T> a, C<T> b) { return {a.re - b.re, a.im - b.im}; }
+template <typename T> inline C<T> cscale(T s, C<T> a) { return {s * a.re, s * a.im}; }
+template <typename T> inline C<T> cdivr(C<T> a, T d) { return {a.re / d, a.im / d}; }
+template <typename T> inline C<T> cmul(C<T> a, C<T> b) {
+  return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
+}
+template <typename T> inline T cabs_(C<T> a) { return std::hypot(a.re, a.im); }
+
+// ---------------------------------------------------------------- RNG ----
+// Seeded replacement for the clock-seeded Fortran RNG (mpi_var.f90:183-209,
+// statistics.f90:29-35).  splitmix64: host draws are a sequence, per-cell
+// draws are a keyed hash of (seed, global cell index), so results do not
+// depend on the decomposition.
+inline uint64_t mix64(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+  return z ^ (z >> 31);
+}
+struct Rng {
+  uint64_t s;
+  double next() {  // U[0,1)
+    s += 0x9e3779b97f4a7c15ULL;
+    return (double)(mix64(s) >> 11) * (1.0 / 9007199254740992.0);
+  }
+};
+inline double cell_uniform(uint64_t seed, uint64_t idx, uint64_t stream) {
+  uint64_t h = mix64(seed ^ mix64(idx * 2ULL + stream + 0x632be59bd9b4e019ULL));
+  return (double)(h >> 11) * (1.0 / 9007199254740992.0);
+}
+
+// --------------------------------------------------------- one "rank" ----
+template <typename T> struct Rank {
+  int cx, cy;                 // coords(1), coords(2)
+  int nmx, nmy, nmz;          // nmeshx, nmeshy, nmeshz
+  int left, right, top, bot;  // neighbour ranks, -1 = MPI_PROC_NULL
+  std::vector<T> xx, yy, zz;  // 1-based storage: index 0 unused
+  std::vector<C<T>> psi;      // (-2:nmz+3, -2:nmy+3, -2:nmx+3)
+  std::vector<C<T>> rhs, w;   // (1:nmz, 1:nmy, 1:nmx)
+  std::vector<T> trap;        // (1:nmz, 1:nmy, 1:nmx)
+  size_t gz, gy;              // ghosted extents in z and y
+  inline size_t g(int k, int j, int i) const {  // Psi(k,j,i), ghosted
+    return ((size_t)(i + 2) * gy + (size_t)(j + 2)) * gz + (size_t)(k + 2);
+  }
+  inline size_t in(int k, int j, int i) const {  // interior arrays, 1-based
+    return ((size_t)(i - 1) * nmy + (size_t)(j - 1)) * nmz + (size_t)(k - 1);
+  }
+};
+
+template <typename T> struct Oracle {
+  trapbec_params p;
+  int px, py;
+  T Lx, Ly, Lz, hx, hy, hz;
+  C<T> dt;      // current complex dt (run.f90:42 multiplies it once)
+  T t;          // simulation time
+  T pi;
+  T eps;        // epsilon(0.)
+  std::vector<Rank<T>> ranks;
+  double norm_target = -1.0;
+  double e_prev = std::numeric_limits<double>::quiet_NaN();
+  double intpsi2_old = 1.0;
+
+  explicit Oracle(const trapbec_params& pp) : p(pp) {
+    px = p.nprocx > 0 ? p.nprocx : 1;
+    py = p.nprocy > 0 ? p.nprocy : 1;
+    Lx = (T)p.lx; Ly = (T)p.ly; Lz = (T)p.lz;
+    hx = Lx / (T)p.nx; hy = Ly / (T)p.ny; hz = Lz / (T)p.nz;   // initial.f90:26
+    dt = {(T)p.dt_re, (T)p.dt_im};
+    t = 0;
+    pi = (T)3.14159265359;                                         // cdata.f90:13
+    eps = std::numeric_limits<T>::epsilon();
+    int nmx = p.nx / px, nmy = p.ny / py, nmz = p.nz;              // mpi_var.f90:156
+    bool per = p.boundaries == TRAPBEC_BC_PERIODIC;
+    ranks.resize((size_t)px * py);
+    for (int r = 0; r < px * py; ++r) {
+      Rank<T>& R = ranks[r];
+      R.cx = r / py; R.cy = r % py;   // MPI_Cart_create row-major ordering
+      R.nmx = nmx; R.nmy = nmy; R.nmz = nmz;
+      auto rk = [&](int cx, int cy) -> int {
+        if (per) { cx = (cx + px) % px; cy = (cy + py) % py; }
+        if (cx < 0 || cx >= px || cy < 0 || cy >= py) return -1;
+        return cx * py + cy;
+      };
+      R.left = rk(R.cx - 1, R.cy); R.right = rk(R.cx + 1, R.cy);
+      R.top = rk(R.cx, R.cy - 1); R.bot = rk(R.cx, R.cy + 1);
+      R.gz = (size_t)nmz + 6; R.gy = (size_t)nmy + 6;
+      R.psi.assign(R.gz * R.gy * ((size_t)nmx + 6), C<T>{0, 0});
+      R.rhs.assign((size_t)nmx * nmy * nmz, C<T>{0, 0});
+      R.w.assign((size_t)nmx * nmy * nmz, C<T>{0, 0});
+      R.trap.assign((size_t)nmx * nmy * nmz, (T)0);
+      R.xx.assign(nmx + 1, 0); R.yy.assign(nmy + 1, 0); R.zz.assign(nmz + 1, 0);
+      // initial.f90:34-42
+      for (int k = 1; k <= nmz; ++k)
+        R.zz[k] = (T)(2 * k - 1) / ((T)2 * (T)nmz) * Lz - Lz / (T)2;
+      for (int j = 1; j <= nmy; ++j)
+        R.yy[j] = (T)(2 * j - 1) / ((T)2 * (T)nmy) * Ly / (T)py + (T)R.cy * Ly / (T)py - Ly / (T)2;
+      for (int i = 1; i <= nmx; ++i)
+        R.xx[i] = (T)(2 * i - 1) / ((T)2 * (T)nmx) * Lx / (T)px + (T)R.cx * Lx / (T)px - Lx / (T)2;
+    }
+  }
+
+  // global interior index (z fastest) <-> (rank, local)
+  size_t gidx(int K, int J, int I) const {  // 0-based global
+    return ((size_t)I * p.ny + J) * p.nz + K;
+  }
+
+  // ---------------------------------------------------------- ghost.f90 --
+  void ghost_comm() {
+    // Face exchange of the process grid, then the boundary fills where a
+    // side has no neighbour.  x faces first, then y faces, then z
+    // (ghost.f90:29-94, 96-160, 163-191).  Corners are never read.
+    for (auto& R : ranks) {
+      int nmx = R.nmx, nmy = R.nmy, nmz = R.nmz;
+      // ghost planes from the right neighbour (its first planes 1..3)
+      if (R.right >= 0) {
+        Rank<T>& N = ranks[R.right];
+        for (int m = 1; m <= 3; ++m)
+          for (int j = 1; j <= nmy; ++j)
+            for (int k = 1; k <= nmz; ++k) R.psi[R.g(k, j, nmx + m)] = N.psi[N.g(k, j, m)];
+      } else {
+        for (int m = 1; m <= 3; ++m)
+          for (int j = 1; j <= nmy; ++j)
+            for (int k = 1; k <= nmz; ++k)
+              R.psi[R.g(k, j, nmx + m)] = p.boundaries == TRAPBEC_BC_SOLID
+                                              ? R.psi[R.g(k, j, nmx - m)] : C<T>{0, 0};
+      }
+      if (R.left >= 0) {
+        Rank<T>& N = ranks[R.left];
+        for (int m = 0; m <= 2; ++m)
+          for (int j = 1; j <= nmy; ++j)
+            for (int k = 1; k <= nmz; ++k) R.psi[R.g(k, j, -m)] = N.psi[N.g(k, j, N.nmx - m)];
+      } else {
+        for (int m = 0; m <= 2; ++m)
+          for (int j = 1; j <= nmy; ++j)
+            for (int k = 1; k <= nmz; ++k)
+              R.psi[R.g(k, j, -m)] = p.boundaries == TRAPBEC_BC_SOLID
+                                         ? R.psi[R.g(k, j, 2 + m)] : C<T>{0, 0};
+      }
+    }
+    for (auto& R : ranks) {
+      int nmx = R.nmx, nmy = R.nmy, nmz = R.nmz;
+      if (R.bot >= 0) {
+        Rank<T>& N = ranks[R.bot];
+        for (int i = 1; i <= nmx; ++i)
+          for (int m = 1; m <= 3; ++m)
+            for (int k = 1; k <= nmz; ++k) R.psi[R.g(k, nmy + m, i)] = N.psi[N.g(k, m, i)];
+      } else {
+        for (int i = 1; i <= nmx; ++i)
+          for (int m = 1; m <= 3; ++m)
+            for (int k = 1; k <= nmz; ++k)
+              R.psi[R.g(k, nmy + m, i)] = p.boundaries == TRAPBEC_BC_SOLID
+                                              ? R.psi[R.g(k, nmy - m, i)] : C<T>{0, 0};
+      }
+      if (R.top >= 0) {
+        Rank<T>& N = ranks[R.top];
+        for (int i = 1; i <= nmx; ++i)
+          for (int m = 0; m <= 2; ++m)
+            for (int k = 1; k <= nmz; ++k) R.psi[R.g(k, -m, i)] = N.psi[N.g(k, N.nmy - m, i)];
+      } else {
+        for (int i = 1; i <= nmx; ++i)
+          for (int m = 0; m <= 2; ++m)
+            for (int k = 1; k <= nmz; ++k)
+              R.psi[R.g(k, -m, i)] = p.boundaries == TRAPBEC_BC_SOLID
+                                         ? R.psi[R.g(k, 2 + m, i)] : C<T>{0, 0};
+      }
+    }
+    for (auto& R : ranks) {
+      int nmx = R.nmx, nmy = R.nmy, nmz = R.nmz;
+      bool zper = p.periodicz || p.boundaries == TRAPBEC_BC_PERIODIC;
+      for (int i = 1; i <= nmx; ++i)
+        for (int j = 1; j <= nmy; ++j)
+          for (int m = 1; m <= 3; ++m) {
+            C<T> hi, lo;
+            if (zper) {
+              hi = R.psi[R.g(m, j, i)];
+              lo = R.psi[R.g(nmz + 1 - m, j, i)];
+            } else if (p.boundaries == TRAPBEC_BC_SOLID) {
+              hi = R.psi[R.g(nmz - m, j, i)];
+              lo = R.psi[R.g(1 + m, j, i)];
+            } else {
+              hi = lo = C<T>{0, 0};
+            }
+            R.psi[R.g(nmz + m, j, i)] = hi;
+            R.psi[R.g(1 - m, j, i)] = lo;
+          }
+    }
+  }
+
+  // ---------------------------------------------------------- deriv.f90 --
+  static inline C<T> second_deriv(const C<T>* v, ptrdiff_t s, T h) {  // deriv.f90:19-25
+    C<T> a = cscale((T)2, v[-3 * s]);
+    a = csub(a, cscale((T)27, v[-2 * s]));
+    a = cadd(a, cscale((T)270, v[-1 * s]));
+    a = csub(a, cscale((T)490, v[0]));
+    a = cadd(a, cscale((T)270, v[1 * s]));
+    a = csub(a, cscale((T)27, v[2 * s]));
+    a = cadd(a, cscale((T)2, v[3 * s]));
+    return cdivr(a, (T)180 * (h * h));
+  }
+  static inline C<T> first_deriv(const C<T>* v, ptrdiff_t s, T h) {  // deriv.f90:12-18
+    C<T> a = {-v[-3 * s].re, -v[-3 * s].im};
+    a = cadd(a, cscale((T)9, v[-2 * s]));
+    a = csub(a, cscale((T)45, v[-1 * s]));
+    a = cadd(a, cscale((T)45, v[1 * s]));
+    a = csub(a, cscale((T)9, v[2 * s]));
+    a = cadd(a, v[3 * s]);
+    return cdivr(a, (T)60 * h);
+  }
+
+  // ------------------------------------------------ potential (per cell) --
+  T potential(const Rank<T>& R, int k, int j, int i) const {  // finite_diff.f90:29-124
+    const T x = R.xx[i], y = R.yy[j], z = R.zz[k];
+    T pot = 0, r, r1, r2;
+    switch (p.potential) {
+      case TRAPBEC_POT_ZERO: break;
+      case TRAPBEC_POT_HARMONIC: {
+        T a = x / Lx, b = y / Ly, c = z / Lz;
+        pot = (T)p.harm_wx * (a * a) + (T)p.harm_wy * (b * b) + (T)p.harm_wz * (c * c);
+      } break;
+      case TRAPBEC_POT_HARMONIC_RING: {
+        T a = x / Lx, b = y / Lx;
+        r = std::sqrt(a * a + b * b);
+        T d = r - (T)0.3;
+        pot = (T)p.harm_wx * (d * d);
+        if (std::fabs(r - (T)0.3) < (T)0.01) pot = std::max((T)0, (T)5 - (T)0.1 * t);
+      } break;
+      case TRAPBEC_POT_HARMONIC_RING2: {
+        T pw = 6;
+        r1 = std::pow(std::fabs(std::pow((T)0.25, pw) - (T)0.15 * std::pow(x / Lx, pw) -
+                                (T)4 * std::pow(y / Ly - (T)0.2, pw)), (T)1 / pw);
+        r2 = std::pow(std::fabs(std::pow((T)0.25, pw) - (T)0.15 * std::pow(x / Lx, pw) -
+                                (T)4 * std::pow(y / Ly + (T)0.2, pw)), (T)1 / pw);
+        r1 = (r1 < (T)0.2495) ? (T)0 : (T)5;
+        r2 = (r2 < (T)0.2495) ? (T)0 : (T)5;
+        pot = r1 * r2;
+        if (pot < (T)0) pot = 0;
+        if (std::fabs(y / Ly) < (T)0.01 && pot < (T)0.01) pot = std::max((T)0, (T)5 - (T)0.1 * t);
+      } break;
+      case TRAPBEC_POT_BARRIER:
+        pot = 0;
+        if (std::fabs(y / Ly) > (T)0.3) pot = 5;
+        if (std::fabs(y / Ly) < (T)0.01) pot = std::max((T)0, (T)5 - (T)0.1 * t);
+        break;
+      case TRAPBEC_POT_BOX_TRAP:
+        pot = 10;
+        r = std::sqrt(x * x + y * y);
+        if (r < Lx / (T)3 && std::fabs(z) < Lz / (T)2.5) pot = 0;
+        pot = pot + (T)5 * std::sin((T)0.1 * t) * z / Lz;
+        break;
+      case TRAPBEC_POT_CHANNEL:
+        pot = 0;
+        if (std::fabs(y) > (T)0.75 * Ly / (T)2 || std::fabs(z) > (T)0.75 * Lz / (T)2) pot = 5;
+        for (int l1 = -1; l1 <= 1; ++l1)
+          if (std::fabs(x) < Lx / (T)p.nx && std::fabs(y - (T)l1 * Ly / (T)5) < Ly / (T)p.ny) pot = (T)7.5;
+        for (int l1 = -1; l1 <= 1; ++l1)
+          if (std::fabs(x) < Lx / (T)p.nx && std::fabs(z - (T)l1 * Lz / (T)5) < Ly / (T)p.ny) pot = (T)7.5;
+        break;
+      case TRAPBEC_POT_QUARTIC: {
+        T a = x / Lx, b = y / Ly;
+        r = std::sqrt(a * a + b * b);
+        T r2_ = r * r, r4 = r2_ * r2_;
+        pot = (T)p.harm_wx * (r4 * r4);
+      } break;
+      case TRAPBEC_POT_SPHERE: {
+        T theta = std::atan2(y, x);
+        T a = x / Lx, b = y / Ly, c = z / Lz;
+        r1 = std::sqrt(a * a + b * b + c * c);
+        T phi = std::acos((z / Lz) / r1);
+        pot = (r1 < (T)0.2 + (T)0.01 * std::sin((T)20 * phi) + (T)0.01 * std::cos((T)30 * theta + (T)0.03))
+                  ? (T)10 : (T)0;
+      } break;
+      case TRAPBEC_POT_MOBIUS:
+        pot = R.trap[R.in(k, j, i)];
+        if (std::fabs(y) < (T)1 && std::fabs(x - (T)25) < (T)1) pot = pot + 10;
+        break;
+      case TRAPBEC_POT_ARRAY:
+        pot = R.trap[R.in(k, j, i)];
+        break;
+    }
+    if (p.lbeam) {  // finite_diff.f90:118-123, las_freq = 0
+      T las_freq = 0;
+      T las_x = (T)70 * std::cos(las_freq * t) * ((T)1 - std::sin(las_freq * t));
+      T las_y = (T)30 * std::sin(las_freq * t) * std::cos(las_freq * t);
+      T a = (x - las_x) / (T)p.wbeam, b = (y - las_y) / (T)p.wbeam;
+      pot = pot + (T)20 * std::exp(-(a * a) - (b * b));
+    }
+    if (t > (T)p.potential_off) pot = 0;  // finite_diff.f90:124
+    return pot;
+  }
+
+  // Rotation / advective term of get_rhs (finite_diff.f90:126-131), or zero.
+  inline C<T> frame_term(const Rank<T>& R, const C<T>* c, ptrdiff_t sx, ptrdiff_t sy,
+                         int j, int i, bool* active) const {
+    *active = false;
+    if (std::fabs((T)p.advective_vx) > eps) {
+      *active = true;
+      C<T> d = first_deriv(c, sx, hx);
+      T s = (T)2 * (T)p.advective_vx;   // (2*eye*vx) = (0, 2vx)
+      return {-s * d.im, s * d.re};
+    } else if (std::fabs((T)p.omega_z) > eps && t < (T)p.t_spindown) {
+      *active = true;
+      C<T> dy = first_deriv(c, sy, hy), dx = first_deriv(c, sx, hx);
+      C<T> zc = csub(cscale(R.xx[i], dy), cscale(R.yy[j], dx));
+      T om = (T)p.omega_z;              // (omega_z*eye) = (0, omega)
+      return {-om * zc.im, om * zc.re};
+    }
+    return {0, 0};
+  }
+
+  // --------------------------------------------------- finite_diff.f90 --
+  void get_rhs() {
+    ghost_comm();
+    const bool two = p.two_dim != 0;
+    for (auto& R : ranks) {
+      const ptrdiff_t sx = (ptrdiff_t)(R.gz * R.gy), sy = (ptrdiff_t)R.gz;
+#pragma omp parallel for schedule(static)
+      for (int i = 1; i <= R.nmx; ++i)
+        for (int j = 1; j <= R.nmy; ++j)
+          for (int k = 1; k <= R.nmz; ++k) {
+            const C<T>* c = &R.psi[R.g(k, j, i)];
+            C<T> rhs = second_deriv(c, sx, hx);
+            rhs = cadd(rhs, second_deriv(c, sy, hy));
+            if (!two) rhs = cadd(rhs, second_deriv(c, 1, hz));
+            T pot = potential(R, k, j, i);
+            bool act;
+            C<T> fr = frame_term(R, c, sx, sy, j, i, &act);
+            if (act) rhs = cadd(rhs, fr);
+            T rho = (T)1 - cabs_(cmul(*c, *c)) - pot;   // abs(Psi**2)
+            rhs = cadd(rhs, cscale(rho, *c));
+            R.rhs[R.in(k, j, i)] = rhs;
+          }
+    }
+  }
+
+  // ------------------------------------------------------------ run.f90 --
+  template <typename F> void for_interior(F f) {
+    for (auto& R : ranks) {
+#pragma omp parallel for schedule(static)
+      for (int i = 1; i <= R.nmx; ++i)
+        for (int j = 1; j <= R.nmy; ++j)
+          for (int k = 1; k <= R.nmz; ++k) f(R, k, j, i);
+    }
+  }
+
+  void apply_damping() {  // run.f90:42, dt=dt*(1.-gamma*eye)
+    C<T> f = {(T)1, -(T)p.gamma};
+    dt = cmul(dt, f);
+  }
+
+  void rk3_step() {  // run.f90:44-55
+    // eye*0.5*dt: (0, 0.5) * dt
+    const C<T> cf = {-(T)0.5 * dt.im, (T)0.5 * dt.re};
+    get_rhs();
+    for_interior([&](Rank<T>& R, int k, int j, int i) {
+      size_t q = R.in(k, j, i);
+      C<T> w = cmul(cf, R.rhs[q]);
+      R.w[q] = w;
+      C<T>& ps = R.psi[R.g(k, j, i)];
+      ps = cadd(ps, cdivr(w, (T)3));
+    });
+    get_rhs();
+    const T a2 = (T)(-2.) / (T)3.;
+    for_interior([&](Rank<T>& R, int k, int j, int i) {
+      size_t q = R.in(k, j, i);
+      C<T> w = cadd(cscale(a2, R.w[q]), cmul(cf, R.rhs[q]));
+      R.w[q] = w;
+      C<T>& ps = R.psi[R.g(k, j, i)];
+      ps = cadd(ps, w);
+    });
+    get_rhs();
+    for_interior([&](Rank<T>& R, int k, int j, int i) {
+      size_t q = R.in(k, j, i);
+      C<T> w = cadd(C<T>{-R.w[q].re, -R.w[q].im}, cmul(cf, R.rhs[q]));
+      R.w[q] = w;
+      C<T>& ps = R.psi[R.g(k, j, i)];
+      ps = cadd(ps, cscale((T)0.5, w));
+    });
+    t = t + dt.re;  // run.f90:55, t real
+  }
+
+  void imag_euler_step() {  // run.f90:21-23
+    const C<T> cf = {dt.re * (T)0.5, dt.im * (T)0.5};
+    get_rhs();
+    for_interior([&](Rank<T>& R, int k, int j, int i) {
+      C<T>& ps = R.psi[R.g(k, j, i)];
+      ps = cadd(ps, cmul(cf, R.rhs[R.in(k, j, i)]));
+    });
+  }
+
+  // Reference Psi_norm: sum(abs(Psi)**2) in T per rank, then rank-order sum.
+  T psi_norm_ref() {
+    T tot = 0;
+    for (auto& R : ranks) {
+      T s = 0;
+      for (int i = 1; i <= R.nmx; ++i)
+        for (int j = 1; j <= R.nmy; ++j)
+          for (int k = 1; k <= R.nmz; ++k) {
+            T a = cabs_(R.psi[R.g(k, j, i)]);
+            s = s + a * a;
+          }
+      tot = tot + s;
+    }
+    return tot;
+  }
+
+  // ------------------------------------------------ FP64 diagnostics (new) --
+  struct Acc {  // Neumaier-compensated FP64 sum
+    double s = 0, c = 0;
+    void add(double v) {
+      double tt = s + v;
+      if (std::fabs(s) >= std::fabs(v)) c += (s - tt) + v; else c += (v - tt) + s;
+      s = tt;
+    }
+    double val() const { return s + c; }
+  };
+
+  void diag(trapbec_diag_out* o) {
+    ghost_comm();
+    const bool two = p.two_dim != 0;
+    Acc n, K, P, Q, Rr, sa;
+    double mx = -1, mn = std::numeric_limits<double>::infinity();
+    int nonfinite = 0;
+    for (auto& R : ranks) {
+      const ptrdiff_t sx = (ptrdiff_t)(R.gz * R.gy), sy = (ptrdiff_t)R.gz;
+      for (int i = 1; i <= R.nmx; ++i)
+        for (int j = 1; j <= R.nmy; ++j)
+          for (int k = 1; k <= R.nmz; ++k) {
+            const C<T>* c = &R.psi[R.g(k, j, i)];
+            C<T> lap = second_deriv(c, sx, hx);
+            lap = cadd(lap, second_deriv(c, sy, hy));
+            if (!two) lap = cadd(lap, second_deriv(c, 1, hz));
+            bool act;
+            C<T> fr = frame_term(R, c, sx, sy, j, i, &act);
+            double re = c->re, im = c->im;
+            double a2 = re * re + im * im;
+            if (!std::isfinite(a2)) nonfinite = 1;
+            double pot = potential(R, k, j, i);
+            n.add(a2);
+            K.add(re * (double)lap.re + im * (double)lap.im);
+            P.add(pot * a2);
+            Q.add(a2 * a2);
+            Rr.add(re * (double)fr.re + im * (double)fr.im);
+            double a = std::sqrt(a2);
+            sa.add(a);
+            mx = std::max(mx, a); mn = std::min(mn, a);
+          }
+    }
+    double dV = (double)hx * (double)hy * (p.two_dim ? 1.0 : (double)hz);
+    o->intpsi2 = n.val();
+    o->maxpsi = mx; o->minpsi = mn;
+    o->meanpsi = sa.val() / ((double)p.nx * p.ny * p.nz);
+    o->norm = dV * n.val();
+    o->kinetic = K.val(); o->potential = P.val(); o->interaction = Q.val(); o->rotation = Rr.val();
+    o->energy = dV * (-0.5 * K.val() + 0.5 * P.val() + 0.25 * Q.val() - 0.5 * Rr.val());
+    o->mu = (-0.5 * K.val() + 0.5 * P.val() + 0.5 * Q.val() - 0.5 * Rr.val()) / n.val();
+    o->nonfinite = nonfinite;
+    o->reserved = 0;
+  }
+
+  // ---------------------------- imaginary-time RK3 with renormalisation (new) --
+  // d psi / d tau = rhs / 2 (the real-time operator i*0.5*dt replaced by the
+  // real 0.5*dtau), same 2N-storage coefficients as run.f90:46-54, then
+  // psi <- psi * sqrt(N0/N) in FP64, then E in FP64.
+  int imag_rk3(int nsteps, double tol, int* steps_done, double* rel_de) {
+    const T cf = (T)0.5 * dt.re;
+    trapbec_diag_out d;
+    if (norm_target <= 0) { diag(&d); norm_target = d.norm; }
+    diag(&d);            // energy of the incoming state: the first test is after step 1
+    e_prev = d.energy;
+    int s = 0;
+    double rel = std::numeric_limits<double>::infinity();
+    const T a2 = (T)(-2.) / (T)3.;
+    for (s = 1; s <= nsteps; ++s) {
+      get_rhs();
+      for_interior([&](Rank<T>& R, int k, int j, int i) {
+        size_t q = R.in(k, j, i);
+        C<T> w = cscale(cf, R.rhs[q]);
+        R.w[q] = w;
+        C<T>& ps = R.psi[R.g(k, j, i)];
+        ps = cadd(ps, cdivr(w, (T)3));
+      });
+      get_rhs();
+      for_interior([&](Rank<T>& R, int k, int j, int i) {
+        size_t q = R.in(k, j, i);
+        C<T> w = cadd(cscale(a2, R.w[q]), cscale(cf, R.rhs[q]));
+        R.w[q] = w;
+        C<T>& ps = R.psi[R.g(k, j, i)];
+        ps = cadd(ps, w);
+      });
+      get_rhs();
+      for_interior([&](Rank<T>& R, int k, int j, int i) {
+        size_t q = R.in(k, j, i);
+        C<T> w = cadd(C<T>{-R.w[q].re, -R.w[q].im}, cscale(cf, R.rhs[q]));
+        R.w[q] = w;
+        C<T>& ps = R.psi[R.g(k, j, i)];
+        ps = cadd(ps, cscale((T)0.5, w));
+      });
+      // renormalise (FP64 norm, scale rounded to T)
+      Acc n;
+      for (auto& R : ranks)
+        for (int i = 1; i <= R.nmx; ++i)
+          for (int j = 1; j <= R.nmy; ++j)
+            for (int k = 1; k <= R.nmz; ++k) {
+              const C<T>& c = R.psi[R.g(k, j, i)];
+              n.add((double)c.re * c.re + (double)c.im * c.im);
+            }
+      double dV = (double)hx * (double)hy * (p.two_dim ? 1.0 : (double)hz);
+      double N = dV * n.val();
+      if (!(N > 0) || !std::isfinite(N)) { *steps_done = s; *rel_de = NAN; return TRAPBEC_ERR_NONFINITE; }
+      const T sc = (T)std::sqrt(norm_target / N);
+      for_interior([&](Rank<T>& R, int k, int j, int i) {
+        C<T>& ps = R.psi[R.g(k, j, i)];
+        ps = cscale(sc, ps);
+      });
+      diag(&d);
+      rel = std::fabs(d.energy - e_prev) / std::fabs(d.energy);
+      e_prev = d.energy;
+      if (rel <= tol) break;
+    }
+    if (s > nsteps) s = nsteps;
+    *steps_done = s;
+    *rel_de = rel;
+    return TRAPBEC_OK;
+  }
+
+  // ------------------------------------------------------ initial states --
+  T ring_density(T r) const {  // initial.f90:628-635
+    T c1 = (T)11 / (T)32;
+    T c3 = ((T)5 - (T)32 * c1) / ((T)48 - (T)192 * c1);
+    T c2 = c1 * (c3 - (T)0.25);
+    T r2 = r * r;
+    return std::sqrt(r2 * (c1 + c2 * r2) / ((T)1 + c3 * r2 + c2 * (r2 * r2)));
+  }
+  static C<T> cexpi(T th) { return {std::cos(th), std::sin(th)}; }
+  T vortex_func(T r) const { return (T)1 - std::exp((T)(-0.7) * std::pow(r, (T)1.15)); }
+
+  void set_cell(Rank<T>& R, int k, int j, int i, C<T> v) { R.psi[R.g(k, j, i)] = v; }
+  C<T>& cell(Rank<T>& R, int k, int j, int i) { return R.psi[R.g(k, j, i)]; }
+
+  T tf_dense(const Rank<T>& R, int k, int j, int i) const {  // initial.f90:644
+    T a = R.xx[i] / Lx, b = R.yy[j] / Ly, c = R.zz[k] / Lz;
+    return (T)1 - (T)p.harm_wx * (a * a) - (T)p.harm_wy * (b * b) - (T)p.harm_wz * (c * c);
+  }
+
+  int init_state(const char* name, const trapbec_init_args* a) {
+    std::string nm(name);
+    Rng rng{a ? a->seed : 0};
+    auto runif = [&](T lo, T hi) { T u = (T)rng.next(); return lo + u * (hi - lo); };
+    for (auto& R : ranks) std::fill(R.psi.begin(), R.psi.end(), C<T>{0, 0});
+    const T ring_rad = (T)p.ring_rad;
+    const int wn = p.winding_number;
+    if (nm == "constant") {
+      T v = (T)1 / std::sqrt((T)2);
+      for_interior([&](Rank<T>& R, int k, int j, int i) { set_cell(R, k, j, i, {v, v}); });
+    } else if (nm == "thomas_fermi" || nm == "soliton") {  // initial.f90:637-652, 67-80
+      for_interior([&](Rank<T>& R, int k, int j, int i) {
+        T d = tf_dense(R, k, j, i);
+        d = d / std::sqrt((T)2);
+        if (d < (T)0) d = 0;
+        set_cell(R, k, j, i, {d, d});
+      });
+      if (nm == "soliton") {
+        for_interior([&](Rank<T>& R, int k, int j, int i) {
+          T ld = cabs_(cell(R, k, j, i));
+          C<T> e = R.xx[i] < (T)0 ? cexpi((T)0) : cexpi(pi);
+          set_cell(R, k, j, i, cscale(ld, e));
+        });
+      }
+    } else if (nm == "single_vortex") {  // initial.f90:109-121
+      for_interior([&](Rank<T>& R, int k, int j, int i) {
+        T dx = R.xx[i], dy = R.yy[j];
+        T r = std::sqrt(dx * dx + dy * dy);
+        T th = std::atan2(dy, dx);
+        T f = vortex_func(r);
+        set_cell(R, k, j, i, cscale(f, cexpi((T)wn * th)));
+      });
+    } else if (nm == "sausage") {  // initial.f90:122-138
+      for_interior([&](Rank<T>& R, int k, int j, int i) {
+        T dx = R.xx[i], dy = R.yy[j];
+        T r = std::sqrt(dx * dx + dy * dy);
+        T th = std::atan2(dy, dx);
+        T f = std::fabs(R.zz[k]) < (T)4 ? (T)1 - std::exp((T)(-0.1) * std::pow(r, (T)1.15)) : vortex_func(r);
+        set_cell(R, k, j, i, cscale(f, cexpi(th)));
+      });
+    } else if (nm == "crow") {  // initial.f90:90-108
+      for_interior([&](Rank<T>& R, int k, int j, int i) {
+        T vy = -Ly / (T)4;
+        T vx1 = (T)(-4) + std::cos(pi * R.zz[k] / Lz);
+        T dx = R.xx[i] - vx1, dy = R.yy[j] - vy;
+        C<T> a = cscale(vortex_func(std::sqrt(dx * dx + dy * dy)), cexpi(std::atan2(dy, dx)));
+        T vx2 = (T)4 - std::cos(pi * R.zz[k] / Lz);
+        dx = R.xx[i] - vx2;
+        C<T> b = cscale(vortex_func(std::sqrt(dx * dx + dy * dy)), cexpi(-std::atan2(dy, dx)));
+        set_cell(R, k, j, i, cmul(a, b));
+      });
+    } else if (nm == "random_points" || nm == "leap_frog") {  // initial.f90:268-344
+      for_interior([&](Rank<T>& R, int k, int j, int i) { set_cell(R, k, j, i, {(T)0.7071, (T)0.7071}); });
+      int nv = nm == "random_points" ? 20 : 4;
+      for (int v = 1; v <= nv; ++v) {
+        T vx, vy, dir;
+        if (nm == "random_points") {
+          vx = runif(-Lx / (T)5, Lx / (T)5);
+          vy = runif(-Ly / (T)5, Ly / (T)5);
+          dir = runif((T)0.9, (T)1);
+          dir = dir < (T)0.5 ? (T)(-1) : (T)1;
+        } else {
+          const T sh = 3, s1 = 3, s2 = 12;
+          if (v == 1) { vx = -sh; vy = s1; dir = 1; }
+          else if (v == 2) { vx = sh; vy = s2; dir = 1; }
+          else if (v == 3) { vx = -sh; vy = -s1; dir = -1; }
+          else { vx = sh; vy = -s2; dir = -1; }
+        }
+        for_interior([&](Rank<T>& R, int k, int j, int i) {
+          T dx = R.xx[i] - vx, dy = R.yy[j] - vy;
+          C<T> tmp = cscale(vortex_func(std::sqrt(dx * dx + dy * dy)), cexpi(dir * std::atan2(dy, dx)));
+          cell(R, k, j, i) = cmul(cell(R, k, j, i), tmp);
+        });
+      }
+    } else if (nm == "vortex_rings") {  // initial.f90:202-266
+      for_interior([&](Rank<T>& R, int k, int j, int i) { set_cell(R, k, j, i, {(T)1, (T)0}); });
+      for (int v = 1; v <= p.vor_ring_count; ++v) {
+        T ax = runif(0, 0), ay = runif(0, (T)2 * pi), az = runif(0, (T)2 * pi);
+        T tu = runif(-1, 1), tth = runif(0, (T)2 * pi), tr = runif(0, Lx / (T)6);
+        T tx = tr * std::sqrt((T)1 - tu * tu) * std::cos(tth);
+        T ty = tr * std::sqrt((T)1 - tu * tu) * std::sin(tth);
+        T tz = tr * tu;
+        for_interior([&](Rank<T>& R, int k, int j, int i) {
+          T x = R.xx[i], y = R.yy[j], z = R.zz[k];
+          T X = std::cos(ay) * std::cos(az) * x +
+                (std::cos(ax) * std::sin(az) + std::sin(ax) * std::sin(ay) * std::cos(az)) * y +
+                (std::sin(ax) * std::sin(az) - std::cos(ax) * std::sin(ay) * std::cos(az)) * z;
+          T Y = -std::cos(ay) * std::sin(az) * x +
+                (std::cos(ax) * std::cos(az) - std::sin(ax) * std::sin(ay) * std::sin(az)) * y +
+                (std::sin(ax) * std::cos(ay) + std::cos(ax) * std::sin(ay) * std::sin(az)) * z;
+          T Z = std::sin(ay) * x - std::sin(ax) * std::cos(ay) * y + std::cos(ax) * std::cos(ay) * z;
+          T s = std::sqrt((Y - ty) * (Y - ty) + (Z - tz) * (Z - tz));
+          T r = std::sqrt((X - tx) * (X - tx) + (s + ring_rad) * (s + ring_rad));
+          T th = std::atan2(Z - tz, Y - ty);
+          auto pade = [&](T rr) {
+            T r2 = rr * rr;
+            return std::sqrt(r2 * ((T)0.347 + (T)0.0286 * r2) / ((T)1 + (T)0.3333 * r2 + (T)0.0286 * (r2 * r2)));
+          };
+          C<T> p1 = cscale(pade(r), cexpi(th));
+          r = std::sqrt((X - tx) * (X - tx) + (s - ring_rad) * (s - ring_rad));
+          C<T> p2 = cscale(pade(r), cexpi(th));
+          C<T> tmp = cmul(p1, C<T>{p2.re, -p2.im});
+          cell(R, k, j, i) = cmul(cell(R, k, j, i), tmp);
+        });
+      }
+    } else if (nm == "tf_vortex_line" || nm == "tf_vortex_ring" || nm == "tf_noise") {
+      // States of the workload set (not reference init_cond cases), in the
+      // reference's units, evaluated in FP64 and rounded to T:
+      //   tf_vortex_line: amp*sqrt(max(0,1-sum x_a^2 r_tf2_a)) * rho/sqrt(rho^2+core2) * e^{i theta}
+      //   tf_vortex_ring: TF * Pade ring of radius ring_radius in z=0 (axis z)
+      //                   * e^{i noise_amp (2u-1)}
+      //   tf_noise      : TF + noise_amp*(eta1 + i eta2), eta in U[-1,1]
+      if (!a) return TRAPBEC_ERR_ARG;
+      for_interior([&](Rank<T>& R, int k, int j, int i) {
+        double x = R.xx[i], y = R.yy[j], z = R.zz[k];
+        double q = 1.0 - x * x * a->r_tf2[0] - y * y * a->r_tf2[1] - z * z * a->r_tf2[2];
+        double tf = a->amp * std::sqrt(q > 0 ? q : 0.0);
+        int I = R.cx * R.nmx + (i - 1), J = R.cy * R.nmy + (j - 1), K = k - 1;
+        uint64_t gi = ((uint64_t)I * p.ny + J) * p.nz + K;
+        double re, im;
+        if (nm == "tf_vortex_line") {
+          double rho2 = x * x + y * y;
+          double f = std::sqrt(rho2) / std::sqrt(rho2 + a->core2);
+          double th = std::atan2(y, x);
+          re = tf * f * std::cos(th); im = tf * f * std::sin(th);
+        } else if (nm == "tf_vortex_ring") {
+          double s = std::sqrt(x * x + y * y);
+          double th1 = std::atan2(z, s + a->ring_radius);
+          double r1 = std::sqrt(z * z + (s + a->ring_radius) * (s + a->ring_radius));
+          double th2 = std::atan2(z, s - a->ring_radius);
+          double r2 = std::sqrt(z * z + (s - a->ring_radius) * (s - a->ring_radius));
+          auto pade = [](double r) {
+            double c1 = 11.0 / 32.0, c3 = (5.0 - 32.0 * c1) / (48.0 - 192.0 * c1), c2 = c1 * (c3 - 0.25);
+            double rr = r * r;
+            return std::sqrt(rr * (c1 + c2 * rr) / (1.0 + c3 * rr + c2 * rr * rr));
+          };
+          double amp = tf * pade(r1) * pade(r2);
+          double ph = th1 - th2 + a->noise_amp * (2.0 * cell_uniform(a->seed, gi, 0) - 1.0);
+          re = amp * std::cos(ph); im = amp * std::sin(ph);
+        } else {
+          re = tf + a->noise_amp * (2.0 * cell_uniform(a->seed, gi, 0) - 1.0);
+          im = a->noise_amp * (2.0 * cell_uniform(a->seed, gi, 1) - 1.0);
+        }
+        set_cell(R, k, j, i, {(T)re, (T)im});
+      });
+    } else {
+      return TRAPBEC_ERR_ARG;
+    }
+    return TRAPBEC_OK;
+  }
+
+  // ------------------------------------------------------------ host I/O --
+  void set_psi(const T* src) {  // interior, global, z fastest
+    for_interior([&](Rank<T>& R, int k, int j, int i) {
+      int I = R.cx * R.nmx + (i - 1), J = R.cy * R.nmy + (j - 1);
+      size_t q = gidx(k - 1, J, I);
+      R.psi[R.g(k, j, i)] = {src[2 * q], src[2 * q + 1]};
+    });
+  }
+  void get_psi(T* dst) {
+    for_interior([&](Rank<T>& R, int k, int j, int i) {
+      int I = R.cx * R.nmx + (i - 1), J = R.cy * R.nmy + (j - 1);
+      size_t q = gidx(k - 1, J, I);
+      const C<T>& c = R.psi[R.g(k, j, i)];
+      dst[2 * q] = c.re; dst[2 * q + 1] = c.im;
+    });
+  }
+  void get_rhs_out(T* dst) {
+    get_rhs();
+    for_interior([&](Rank<T>& R, int k, int j, int i) {
+      int I = R.cx * R.nmx + (i - 1), J = R.cy * R.nmy + (j - 1);
+      size_t q = gidx(k - 1, J, I);
+      const C<T>& c = R.rhs[R.in(k, j, i)];
+      dst[2 * q] = c.re; dst[2 * q + 1] = c.im;
+    });
+  }
+  void get_ghosted(T* dst) {  // single rank only: Psi(-2:nz+3,-2:ny+3,-2:nx+3)
+    ghost_comm();
+    const Rank<T>& R = ranks[0];
+    for (size_t q = 0; q < R.psi.size(); ++q) { dst[2 * q] = R.psi[q].re; dst[2 * q + 1] = R.psi[q].im; }
+  }
+  void set_trap(const double* tr) {
+    for_interior([&](Rank<T>& R, int k, int j, int i) {
+      int I = R.cx * R.nmx + (i - 1), J = R.cy * R.nmy + (j - 1);
+      R.trap[R.in(k, j, i)] = (T)tr[gidx(k - 1, J, I)];
+    });
+  }
+};
+
+struct Handle {
+  int prec;
+  void* o;
+};
+
+template <typename F> int dispatch(Handle* h, F f) {
+  if (!h) return TRAPBEC_ERR_ARG;
+  if (h->prec == TRAPBEC_FP64) return f(*static_cast<Oracle<double>*>(h->o));
+  return f(*static_cast<Oracle<float>*>(h->o));
+}
+
+}  // namespace
+
+extern "C" {
+
+void* orc_create(const trapbec_params* p) {
+  if (!p || p->nx <= 0 || p->ny <= 0 || p->nz <= 0) return nullptr;
+  int px = p->nprocx > 0 ? p->nprocx : 1, py = p->nprocy > 0 ? p->nprocy : 1;
+  if (p->nx % px || p->ny % py) return nullptr;  // mpi_var.f90:157-160
+  Handle* h = new Handle;
+  h->prec = p->precision;
+  if (p->precision == TRAPBEC_FP64) h->o = new Oracle<double>(*p);
+  else h->o = new Oracle<float>(*p);
+  return h;
+}
+void orc_destroy(void* hv) {
+  Handle* h = (Handle*)hv;
+  if (!h) return;
+  if (h->prec == TRAPBEC_FP64) delete (Oracle<double>*)h->o; else delete (Oracle<float>*)h->o;
+  delete h;
+}
+void orc_set_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+#else
+  (void)n;
+#endif
+}
+int orc_max_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+int orc_set_psi(void* h, const void* psi) {
+  return dispatch((Handle*)h, [&](auto& o) {
+    using T = std::remove_reference_t<decltype(o.t)>;
+    o.set_psi((const T*)psi); return 0; });
+}
+int orc_get_psi(void* h, void* psi) {
+  return dispatch((Handle*)h, [&](auto& o) {
+    using T = std::remove_reference_t<decltype(o.t)>;
+    o.get_psi((T*)psi); return 0; });
+}
+int orc_get_psi_ghosted(void* h, void* out) {
+  return dispatch((Handle*)h, [&](auto& o) {
+    using T = std::remove_reference_t<decltype(o.t)>;
+    if (o.ranks.size() != 1) return (int)TRAPBEC_ERR_ARG;
+    o.get_ghosted((T*)out); return 0; });
+}
+int orc_get_rhs(void* h, void* out) {
+  return dispatch((Handle*)h, [&](auto& o) {
+    using T = std::remove_reference_t<decltype(o.t)>;
+    o.get_rhs_out((T*)out); return 0; });
+}
+int orc_set_trap(void* h, const double* tr) {
+  return dispatch((Handle*)h, [&](auto& o) { o.set_trap(tr); return 0; });
+}
+int orc_coords(void* h, double* xx, double* yy, double* zz) {  // global arrays
+  return dispatch((Handle*)h, [&](auto& o) {
+    for (auto& R : o.ranks) {
+      for (int i = 1; i <= R.nmx; ++i) xx[R.cx * R.nmx + i - 1] = R.xx[i];
+      for (int j = 1; j <= R.nmy; ++j) yy[R.cy * R.nmy + j - 1] = R.yy[j];
+      for (int k = 1; k <= R.nmz; ++k) zz[k - 1] = R.zz[k];
+    }
+    return 0; });
+}
+int orc_apply_damping(void* h) {
+  return dispatch((Handle*)h, [&](auto& o) { o.apply_damping(); return 0; });
+}
+int orc_step_rt(void* h, int nsteps, double* t) {
+  return dispatch((Handle*)h, [&](auto& o) {
+    using T = std::remove_reference_t<decltype(o.t)>;
+    o.t = (T)*t;
+    for (int s = 0; s < nsteps; ++s) o.rk3_step();
+    *t = (double)o.t; return 0; });
+}
+int orc_step_imag_euler(void* h, int nsteps, double* ratio) {
+  return dispatch((Handle*)h, [&](auto& o) {
+    double r = 0;
+    for (int s = 0; s < nsteps; ++s) {
+      o.imag_euler_step();
+      double n = (double)o.psi_norm_ref();
+      r = n / o.intpsi2_old;   // run.f90:23
+      o.intpsi2_old = n;
+    }
+    *ratio = r; return 0; });
+}
+int orc_step_imag_rk3(void* h, int nsteps, double tol, int* steps_done, double* rel) {
+  return dispatch((Handle*)h, [&](auto& o) { return o.imag_rk3(nsteps, tol, steps_done, rel); });
+}
+int orc_set_norm_target(void* h, double n0) {
+  return dispatch((Handle*)h, [&](auto& o) { o.norm_target = n0; return 0; });
+}
+int orc_set_omega(void* h, double om) {
+  return dispatch((Handle*)h, [&](auto& o) { o.p.omega_z = om; return 0; });
+}
+int orc_set_t(void* h, double t) {
+  return dispatch((Handle*)h, [&](auto& o) {
+    using T = std::remove_reference_t<decltype(o.t)>;
+    o.t = (T)t; return 0; });
+}
+int orc_diag(void* h, trapbec_diag_out* out) {
+  return dispatch((Handle*)h, [&](auto& o) { o.diag(out); return 0; });
+}
+double orc_psi_norm_ref(void* h) {
+  Handle* hh = (Handle*)h;
+  if (hh->prec == TRAPBEC_FP64) return ((Oracle<double>*)hh->o)->psi_norm_ref();
+  return (double)((Oracle<float>*)hh->o)->psi_norm_ref();
+}
+int orc_init_state(void* h, const char* name, const trapbec_init_args* a) {
+  return dispatch((Handle*)h, [&](auto& o) { return o.init_state(name, a); });
+}
+double orc_cell_uniform(uint64_t seed, uint64_t idx, uint64_t stream) {
+  return cell_uniform(seed, idx, stream);
+}
+
+}  // extern "C"

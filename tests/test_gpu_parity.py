@@ -1,0 +1,275 @@
+"""GPU parity: the CUDA path (through the C ABI) against the CPU oracle.
+
+Tolerances: FP64 results must match the oracle to 1e-12 relative (psi, norm,
+energy) after N steps; the kernels reorder the stencil sums and use fused
+multiply-adds, so bitwise equality is not expected.  FP32 results are
+compared with the FP32 oracle at FP32 rounding levels and their drift
+against FP64 is reported by the benchmark.
+"""
+import numpy as np
+import pytest
+
+from oracle.pyoracle import Oracle
+from trapbec_gb300 import Solver, abi, units
+from trapbec_gb300.abi import InitArgs
+from tests.helpers import params, smooth_state, rel_err
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-12
+
+
+def _init_args(init):
+    a = InitArgs()
+    a.seed = int(init.get("seed", 0))
+    a.amp = float(init.get("amp", 1.0))
+    for i, v in enumerate(init.get("r_tf2", (0, 0, 0))):
+        a.r_tf2[i] = v
+    a.ring_radius = float(init.get("ring_radius", 0.0))
+    a.core2 = float(init.get("core2", 0.0))
+    a.noise_amp = float(init.get("noise_amp", 0.0))
+    return a
+
+
+def _solver_init(s, init):
+    s.init_state(init["name"], seed=init.get("seed", 0), amp=init.get("amp", 1.0), r_tf2=init.get("r_tf2", (0, 0, 0)),
+                 ring_radius=init.get("ring_radius", 0.0), core2=init.get("core2", 0.0),
+                 noise_amp=init.get("noise_amp", 0.0))
+
+
+@pytest.mark.parametrize("nproc", [(1, 1), (2, 2)])
+def test_vortex_line_64_fp64_200_steps(nproc):
+    """64^3 FP64 vortex line, 200 RK3 steps: psi, norm and energy to 1e-12."""
+    prob, init = units.vortex_line_64(abi.FP64, nproc=nproc)
+    p = prob.to_params()
+    s = Solver(p)
+    _solver_init(s, init)
+    o = Oracle(p)
+    o.init_state(init["name"], _init_args(init))
+    assert rel_err(s.get_psi(), o.get_psi()) < 1e-14
+    o.set_psi(s.get_psi())
+    d0 = o.diag()
+    s.step_rt(init["steps"])
+    o.step_rt(init["steps"])
+    a, b = s.get_psi(), o.get_psi()
+    assert rel_err(a, b) < FP64_TOL
+    assert np.linalg.norm(a - b) / np.linalg.norm(b) < FP64_TOL
+    dg, do = s.diag(), o.diag()
+    for k in ("norm", "energy", "mu", "intpsi2", "maxpsi", "meanpsi"):
+        assert abs(dg[k] - do[k]) <= FP64_TOL * abs(do[k]), (k, dg[k], do[k])
+    assert abs(s.t - o.t) < 1e-14
+    # the run itself conserves norm and energy to RK3 accuracy
+    assert abs(do["norm"] / d0["norm"] - 1) < 1e-6
+
+
+RHS_CASES = [
+    dict(bc=abi.BC_ZERO, pot="harmonic", omega=0.3),
+    dict(bc=abi.BC_SOLID, pot="harmonic", omega=0.3),
+    dict(bc=abi.BC_PERIODIC, pot="zero"),
+    dict(bc=abi.BC_ZERO, pot="zero", periodicz=1, vx=0.2),
+    dict(bc=abi.BC_SOLID, pot="barrier"),
+    dict(bc=abi.BC_ZERO, pot="quartic", harm=(900.0, 8.0, 6.0)),
+    dict(bc=abi.BC_ZERO, pot="sphere"),
+    dict(bc=abi.BC_ZERO, pot="harmonic_ring", harm=(50.0, 0, 0)),
+    dict(bc=abi.BC_ZERO, pot="box_trap"),
+    dict(bc=abi.BC_ZERO, pot="channel"),
+    dict(bc=abi.BC_ZERO, pot="harmonic", lbeam=1, harm=(3.0, 4.0, 5.0)),
+    dict(bc=abi.BC_PERIODIC, pot="zero", two_dim=1),
+]
+
+
+@pytest.mark.parametrize("case", RHS_CASES, ids=lambda c: "-".join(f"{k}{v}" for k, v in c.items()))
+def test_get_rhs_parity(case):
+    case = dict(case)
+    harm = case.pop("harm", (4.0, 5.0, 6.0))
+    n = (16, 14, 1 if case.get("two_dim") else 12)
+    p = params(n=n, L=(80.0, 70.0, 1.0 if case.get("two_dim") else 60.0), harm=harm, **case)
+    psi = smooth_state(p, seed=11)
+    s = Solver(p)
+    s.set_psi(psi)
+    o = Oracle(p)
+    o.set_psi(psi)
+    assert rel_err(s.get_rhs(), o.get_rhs()) < 1e-13
+
+
+def test_array_and_mobius_potential():
+    p = params(n=(16, 16, 16), L=(60.0, 60.0, 20.0), pot="array", omega=0.1)
+    rng = np.random.default_rng(0)
+    trap = rng.uniform(0, 2, size=(16, 16, 16))
+    psi = smooth_state(p, seed=3)
+    for kind in ("array", "mobius"):
+        p.potential = abi.POTENTIALS[kind]
+        s, o = Solver(p), Oracle(p)
+        s.set_trap(trap)
+        o.set_trap(trap)
+        s.set_psi(psi)
+        o.set_psi(psi)
+        assert rel_err(s.get_rhs(), o.get_rhs()) < 1e-13
+        s.step_rt(3)
+        o.step_rt(3)
+        assert rel_err(s.get_psi(), o.get_psi()) < FP64_TOL
+
+
+def test_time_dependent_potential_and_damping():
+    """'barrier' depends on t; gamma > 0 damps dt once (run.f90:42)."""
+    p = params(n=(16, 16, 12), L=(40.0, 40.0, 30.0), pot="barrier", gamma=0.01, dt=0.02)
+    psi = smooth_state(p, seed=8)
+    s, o = Solver(p), Oracle(p)
+    s.set_psi(psi)
+    o.set_psi(psi)
+    o.apply_damping()
+    s.step_rt(15)
+    o.step_rt(15)
+    assert rel_err(s.get_psi(), o.get_psi()) < FP64_TOL
+    assert abs(s.t - o.t) < 1e-14
+
+
+def test_fp32_against_fp32_oracle():
+    prob, init = units.vortex_line_64(abi.FP32)
+    p = prob.to_params()
+    p.nx = p.ny = p.nz = 32
+    p.lx = p.ly = p.lz = p.lx / 2
+    s = Solver(p)
+    _solver_init(s, init)
+    o = Oracle(p)
+    o.set_psi(s.get_psi())
+    s.step_rt(20)
+    o.step_rt(20)
+    a, b = s.get_psi().astype(np.complex128), o.get_psi().astype(np.complex128)
+    assert np.linalg.norm(a - b) / np.linalg.norm(b) < 2e-6
+    dg, do = s.diag(), o.diag()
+    assert abs(dg["norm"] / do["norm"] - 1) < 1e-6
+    assert abs(dg["energy"] / do["energy"] - 1) < 1e-5
+
+
+def test_imag_euler_matches_reference_loop():
+    p = params(n=(16, 16, 16), L=(8.0, 8.0, 8.0), pot="harmonic", harm=(6.0, 6.0, 6.0), dt=0.005)
+    psi = smooth_state(p, seed=9)
+    s, o = Solver(p), Oracle(p)
+    s.set_psi(psi)
+    o.set_psi(psi)
+    sd, ratio = s.step_imag(7, abi.IMAG_REF_EULER)
+    r_o = o.step_imag_euler(7)
+    assert sd == 7
+    assert rel_err(s.get_psi(), o.get_psi()) < FP64_TOL
+    assert abs(ratio - r_o) < 1e-12 * abs(r_o)
+
+
+def test_imag_rk3_renorm_matches_oracle():
+    p = params(n=(20, 20, 20), L=(10.0, 10.0, 10.0), pot="harmonic", harm=(100.0, 120.0, 90.0), dt=0.01,
+               omega=0.2)
+    psi = smooth_state(p, seed=12)
+    s, o = Solver(p), Oracle(p)
+    s.set_psi(psi)
+    o.set_psi(psi)
+    sg, rg = s.step_imag(150, abi.IMAG_RK3_RENORM, 0.0)      # fixed number of steps
+    so, ro = o.step_imag_rk3(150, 0.0)
+    assert sg == so == 150
+    assert rel_err(s.get_psi(), o.get_psi()) < 1e-11
+    dg, do = s.diag(), o.diag()
+    assert abs(dg["energy"] - do["energy"]) < 1e-12 * abs(do["energy"])
+    assert abs(dg["norm"] - do["norm"]) < 1e-12 * do["norm"]
+    # now to convergence: same stopping step (or one apart at the threshold)
+    sg2, rg2 = s.step_imag(5000, abi.IMAG_RK3_RENORM, 1e-10)
+    so2, ro2 = o.step_imag_rk3(5000, 1e-10)
+    assert abs(sg2 - so2) <= 1 and rg2 <= 1e-10 and ro2 <= 1e-10
+    assert rel_err(s.get_psi(), o.get_psi()) < 1e-8
+
+
+INIT_STATES = ["constant", "thomas_fermi", "soliton", "single_vortex", "sausage", "crow", "random_points",
+               "leap_frog", "vortex_rings"]
+
+
+@pytest.mark.parametrize("name", INIT_STATES)
+def test_initial_states(name):
+    p = params(n=(24, 24, 16), L=(40.0, 40.0, 30.0), harm=(3.0, 4.0, 5.0))
+    p.winding_number = 2
+    p.vor_ring_count = 2
+    p.ring_rad = 6.0
+    s, o = Solver(p), Oracle(p)
+    a = InitArgs()
+    a.seed = 77
+    s.init_state(name, seed=77)
+    o.init_state(name, a)
+    assert rel_err(s.get_psi(), o.get_psi()) < 1e-13
+
+
+@pytest.mark.parametrize("name", ["tf_vortex_line", "tf_vortex_ring", "tf_noise"])
+def test_workload_states(name):
+    p = params(n=(24, 24, 20), L=(40.0, 40.0, 30.0))
+    init = dict(name=name, amp=1.3, r_tf2=(1 / 150.0, 1 / 140.0, 1 / 90.0), core2=2.5, ring_radius=6.0,
+                noise_amp=1e-2, seed=5)
+    s, o = Solver(p), Oracle(p)
+    _solver_init(s, init)
+    o.init_state(name, _init_args(init))
+    assert rel_err(s.get_psi(), o.get_psi()) < 1e-13
+
+
+def test_ghosted_layout_roundtrip():
+    p = params(n=(10, 12, 8), L=(5.0, 6.0, 4.0), bc=abi.BC_SOLID, periodicz=1)
+    psi = smooth_state(p, seed=6)
+    s, o = Solver(p), Oracle(p)
+    o.set_psi(psi)
+    g = o.get_psi_ghosted()
+    s.set_psi(g, abi.LAYOUT_GHOSTED)
+    assert np.array_equal(s.get_psi(), psi)
+    gs = s.get_psi(abi.LAYOUT_GHOSTED)
+    # faces as ghost_comm leaves them; edges/corners are never written (zero)
+    m = np.zeros(g.shape, bool)
+    m[3:-3, 3:-3, :] = True
+    m[3:-3, :, 3:-3] = True
+    m[:, 3:-3, 3:-3] = True
+    assert np.array_equal(gs[m], g[m])
+
+
+def test_launch_count_and_timing():
+    p = params(n=(16, 16, 16), L=(8.0, 8.0, 8.0), pot="harmonic", harm=(3.0, 3.0, 3.0))
+    s = Solver(p)
+    s.set_psi(smooth_state(p, seed=1))
+    n0 = s.launch_count()
+    s.step_rt(4)
+    assert s.launch_count() - n0 == 12  # three fused stage kernels per RK3 step
+    assert s.last_kernel_ms() > 0
+
+
+def _read_fortran_record(f):
+    import struct
+    out = b""
+    while True:
+        (lead,) = struct.unpack("<i", f.read(4))
+        n = abs(lead)
+        out += f.read(n)
+        f.read(4)
+        if lead >= 0:
+            return out
+
+
+def test_var_and_restart_files(tmp_path):
+    """var####.dat follows output.f90:75-78 and bin/gather.m:13-28; var.dat has
+    the 3 records of output.f90:103-108; reading it back restores psi."""
+    import struct
+    for prec in (abi.FP32, abi.FP64):
+        p = params(n=(8, 10, 6), L=(4.0, 5.0, 3.0), prec=prec)
+        s = Solver(p)
+        psi = smooth_state(p, seed=2).astype(s.cdtype)
+        s.set_psi(psi)
+        s.set_scalar(abi.SCALAR_T, 1.25)
+        d = str(tmp_path / f"data{prec}")
+        s.write_var(d, itime=200, shots=100)
+        rs = 8 if prec == abi.FP64 else 4
+        with open(f"{d}/proc000/var0002.dat", "rb") as f:
+            rec = _read_fortran_record(f)
+        cx, cy = struct.unpack("<2i", rec[:8])
+        fmt = "<4d" if rs == 8 else "<4f"
+        Lx, Ly, Lz, t = struct.unpack(fmt, rec[8:8 + 4 * rs])
+        arr = np.frombuffer(rec[8 + 4 * rs:], dtype=s.cdtype).reshape(8, 10, 6)
+        assert (cx, cy) == (0, 0) and (Lx, Ly, Lz) == (4.0, 5.0, 3.0) and t == 1.25
+        assert np.array_equal(arr, psi)
+        s.write_restart(d, itime=300)
+        with open(f"{d}/proc000/var.dat", "rb") as f:
+            r1, r2, r3 = (_read_fortran_record(f) for _ in range(3))
+        assert struct.unpack("<i", r1)[0] == 301 and len(r2) == rs
+        s2 = Solver(p)
+        nstart = s2.read_restart(d)
+        assert nstart == 301 and s2.t == 1.25
+        assert np.array_equal(s2.get_psi(), psi)

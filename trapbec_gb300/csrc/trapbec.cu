@@ -1,0 +1,978 @@
+// trapbec.cu -- context, orchestration and the C ABI of libtrapbec.
+//
+// One context = one grid on one GPU, one CUDA stream.  Device layout: psi,
+// w and the potential are interior-only arrays in the reference's order
+// Psi(k,j,i) (z fastest); the ghost planes of the reference (initial.f90:16,
+// ghost.f90) are not stored: the stage kernels produce ghost values by index
+// mapping (per-cell kernel) or by TMA out-of-bounds fill plus a fix-up of
+// the boundary tiles (tiled kernel).  psi is double-buffered because a fused
+// stage reads neighbours of psi while writing the updated psi.
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/trapbec.h"
+#include "common.cuh"
+#include "host_util.h"
+#include "kernels_init.cuh"
+#include "kernels_simple.cuh"
+#include "kernels_tiled.cuh"
+#include "imag_ctrl.cuh"
+
+using namespace tb;
+
+// ---------------------------------------------------------------- errors --
+namespace tbh {
+static thread_local std::string g_err;
+void set_error(const std::string& m) { g_err = m; }
+const char* get_error() { return g_err.c_str(); }
+}  // namespace tbh
+using tbh::set_error;
+
+#define CK(call)                                                                          \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess) {                                                              \
+      set_error(std::string(#call) + ": " + cudaGetErrorString(e_));                      \
+      return (e_ == cudaErrorNoDevice || e_ == cudaErrorInsufficientDriver)               \
+                 ? TRAPBEC_ERR_NODEVICE                                                   \
+                 : (e_ == cudaErrorMemoryAllocation ? TRAPBEC_ERR_NOMEM : TRAPBEC_ERR_CUDA); \
+    }                                                                                     \
+  } while (0)
+
+#define CKL()                                                                             \
+  do {                                                                                    \
+    cudaError_t e_ = cudaGetLastError();                                                  \
+    if (e_ != cudaSuccess) {                                                              \
+      set_error(std::string("kernel launch: ") + cudaGetErrorString(e_));                 \
+      return TRAPBEC_ERR_CUDA;                                                            \
+    }                                                                                     \
+  } while (0)
+
+// ---------------------------------------------------------------- context --
+struct trapbec_ctx {
+  trapbec_params p;
+  int prec = TRAPBEC_FP64;
+  size_t n = 0, esz = 0, rsz = 0;   // cells, complex and real element sizes
+  int dev = 0, nsm = 0;
+  cudaStream_t st = nullptr;
+  void* psi[2] = {nullptr, nullptr};
+  int cur = 0;
+  void* w = nullptr;
+  void *xx = nullptr, *yy = nullptr, *zz = nullptr, *px = nullptr, *py = nullptr, *pz = nullptr;
+  void* trap_user = nullptr;   // Trap array set by the caller (context precision)
+  void* trap_eff = nullptr;    // evaluated potential (POT_ARR)
+  bool pot_valid = false;
+  double pot_t = -1.0;
+  double* red = nullptr;       // [NRED][red_cap] block partials
+  int red_cap = 0;
+  double* red_out = nullptr;   // NRED finalised values
+  double* host_red = nullptr;  // pinned NRED
+  ImagCtrl* ctrl = nullptr;    // device control block of the imaginary-time loop
+  ImagCtrl* host_ctrl = nullptr;
+  double t = 0.0;
+  double dt_re = 0, dt_im = 0, gamma = 0, omega = 0, vx = 0;
+  double norm_target = -1.0;
+  double intpsi2_old = 1.0;    // run.f90:23 ratio state
+  bool ctrl_init = false;
+  int kernel_kind = 0, tile_z = 0, tile_y = 0;
+  int64_t launches = 0;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  double last_ms = 0.0;
+  std::vector<double> hxx, hyy, hzz;   // coordinates as double (exact copies of T values)
+  TiledPlan plan;                      // tiled-kernel plan (tensor maps, tile shape)
+  bool plan_valid = false;
+};
+
+namespace {
+
+int g_nsm_cache = 0;
+
+template <typename T> T eps_of() { return std::numeric_limits<T>::epsilon(); }
+
+// Coordinates as the reference computes them on an nprocx x nprocy grid
+// (initial.f90:34-42), in the reference precision.
+template <typename T>
+void make_coords(const trapbec_params& p, std::vector<T>& xx, std::vector<T>& yy, std::vector<T>& zz) {
+  int px = p.nprocx > 0 ? p.nprocx : 1, py = p.nprocy > 0 ? p.nprocy : 1;
+  int nmx = p.nx / px, nmy = p.ny / py, nmz = p.nz;
+  T Lx = (T)p.lx, Ly = (T)p.ly, Lz = (T)p.lz;
+  xx.resize(p.nx); yy.resize(p.ny); zz.resize(p.nz);
+  for (int k = 1; k <= nmz; ++k) zz[k - 1] = (T)(2 * k - 1) / ((T)2 * (T)nmz) * Lz - Lz / (T)2;
+  for (int cy = 0; cy < py; ++cy)
+    for (int j = 1; j <= nmy; ++j)
+      yy[cy * nmy + j - 1] = (T)(2 * j - 1) / ((T)2 * (T)nmy) * Ly / (T)py + (T)cy * Ly / (T)py - Ly / (T)2;
+  for (int cx = 0; cx < px; ++cx)
+    for (int i = 1; i <= nmx; ++i)
+      xx[cx * nmx + i - 1] = (T)(2 * i - 1) / ((T)2 * (T)nmx) * Lx / (T)px + (T)cx * Lx / (T)px - Lx / (T)2;
+}
+
+template <typename T> int setup_tables(trapbec_ctx* c) {
+  const trapbec_params& p = c->p;
+  std::vector<T> xx, yy, zz;
+  make_coords<T>(p, xx, yy, zz);
+  std::vector<T> px(p.nx), py(p.ny), pz(p.nz);
+  T Lx = (T)p.lx, Ly = (T)p.ly, Lz = (T)p.lz;
+  // finite_diff.f90:34: harm_wx*((xx(i))/Lx)**2 + harm_wy*... + harm_wz*...
+  for (int i = 0; i < p.nx; ++i) { T a = xx[i] / Lx; px[i] = (T)p.harm_wx * (a * a); }
+  for (int j = 0; j < p.ny; ++j) { T a = yy[j] / Ly; py[j] = (T)p.harm_wy * (a * a); }
+  for (int k = 0; k < p.nz; ++k) { T a = zz[k] / Lz; pz[k] = (T)p.harm_wz * (a * a); }
+  CK(cudaMemcpyAsync(c->xx, xx.data(), sizeof(T) * p.nx, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(c->yy, yy.data(), sizeof(T) * p.ny, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(c->zz, zz.data(), sizeof(T) * p.nz, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(c->px, px.data(), sizeof(T) * p.nx, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(c->py, py.data(), sizeof(T) * p.ny, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(c->pz, pz.data(), sizeof(T) * p.nz, cudaMemcpyHostToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  c->hxx.assign(xx.begin(), xx.end());
+  c->hyy.assign(yy.begin(), yy.end());
+  c->hzz.assign(zz.begin(), zz.end());
+  return TRAPBEC_OK;
+}
+
+int simple_grid(const trapbec_ctx* c) {
+  size_t want = (c->n + SIMPLE_THREADS - 1) / SIMPLE_THREADS;
+  size_t cap = (size_t)std::max(1, c->nsm) * 8;
+  return (int)std::max<size_t>(1, std::min(want, cap));
+}
+
+bool pot_time_dependent(int kind) {
+  return kind == TRAPBEC_POT_HARMONIC_RING || kind == TRAPBEC_POT_HARMONIC_RING2 ||
+         kind == TRAPBEC_POT_BARRIER || kind == TRAPBEC_POT_BOX_TRAP;
+}
+
+// Which potential path the stage kernels use at time t.
+template <typename T> int pot_mode_at(trapbec_ctx* c, double t) {
+  const trapbec_params& p = c->p;
+  if ((T)t > (T)p.potential_off) return POT_NONE;  // finite_diff.f90:124
+  if (!p.lbeam && p.potential == TRAPBEC_POT_ZERO) return POT_NONE;
+  if (!p.lbeam && p.potential == TRAPBEC_POT_HARMONIC) return POT_HARM;
+  return POT_ARR;
+}
+
+template <typename T> int ensure_potential(trapbec_ctx* c, double t) {
+  if (pot_mode_at<T>(c, t) != POT_ARR) return TRAPBEC_OK;
+  const trapbec_params& p = c->p;
+  bool tdep = pot_time_dependent(p.potential);
+  if (c->pot_valid && (!tdep || c->pot_t == t)) return TRAPBEC_OK;
+  if ((p.potential == TRAPBEC_POT_MOBIUS || p.potential == TRAPBEC_POT_ARRAY) && !c->trap_user) {
+    set_error("potential needs a Trap array: call trapbec_set_trap first");
+    return TRAPBEC_ERR_STATE;
+  }
+  if (!c->trap_eff) CK(cudaMalloc(&c->trap_eff, c->n * sizeof(T)));
+  PotArgs<T> a;
+  a.trap_out = (T*)c->trap_eff;
+  a.trap_in = (const T*)c->trap_user;
+  a.xx = (const T*)c->xx; a.yy = (const T*)c->yy; a.zz = (const T*)c->zz;
+  a.nx = p.nx; a.ny = p.ny; a.nz = p.nz;
+  a.kind = p.potential;
+  a.lbeam = p.lbeam;
+  a.Lx = (T)p.lx; a.Ly = (T)p.ly; a.Lz = (T)p.lz; a.t = (T)t;
+  a.harm_wx = (T)p.harm_wx; a.harm_wy = (T)p.harm_wy; a.harm_wz = (T)p.harm_wz; a.wbeam = (T)p.wbeam;
+  fill_potential_kernel<T><<<simple_grid(c), SIMPLE_THREADS, 0, c->st>>>(a);
+  CKL();
+  c->launches++;
+  c->pot_valid = true;
+  c->pot_t = t;
+  return TRAPBEC_OK;
+}
+
+// Fill the parts of StageArgs that do not depend on the stage.
+template <typename T> StageArgs<T> base_args(trapbec_ctx* c, double t) {
+  const trapbec_params& p = c->p;
+  StageArgs<T> a;
+  std::memset(&a, 0, sizeof(a));
+  a.xx = (const T*)c->xx; a.yy = (const T*)c->yy; a.zz = (const T*)c->zz;
+  a.px = (const T*)c->px; a.py = (const T*)c->py; a.pz = (const T*)c->pz;
+  a.trap = (const T*)c->trap_eff;
+  a.nx = p.nx; a.ny = p.ny; a.nz = p.nz;
+  a.bc = p.boundaries;
+  a.zper = (p.periodicz || p.boundaries == TRAPBEC_BC_PERIODIC) ? 1 : 0;
+  a.two_dim = p.two_dim ? 1 : 0;
+  a.pot_mode = pot_mode_at<T>(c, t);
+  T hx = (T)p.lx / (T)p.nx, hy = (T)p.ly / (T)p.ny, hz = (T)p.lz / (T)p.nz;  // initial.f90:26
+  a.ix2 = (T)1 / ((T)180 * (hx * hx));
+  a.iy2 = (T)1 / ((T)180 * (hy * hy));
+  a.iz2 = (T)1 / ((T)180 * (hz * hz));
+  a.ix1 = (T)1 / ((T)60 * hx);
+  a.iy1 = (T)1 / ((T)60 * hy);
+  // finite_diff.f90:126-131: advective term takes precedence over rotation.
+  if (std::fabs((T)c->vx) > eps_of<T>()) {
+    a.frame_mode = FRAME_ADV;
+    a.omega = (T)2 * (T)c->vx;
+  } else if (std::fabs((T)c->omega) > eps_of<T>() && (T)t < (T)p.t_spindown) {
+    a.frame_mode = FRAME_ROT;
+    a.omega = (T)c->omega;
+  } else {
+    a.frame_mode = FRAME_NONE;
+    a.omega = 0;
+  }
+  a.scale = (T)1;
+  return a;
+}
+
+template <typename T> bool use_tiled(trapbec_ctx* c) {
+  if (c->kernel_kind == 1) return false;
+  return c->plan_valid;
+}
+
+// Launch one stage.  kind: StageKind or 4 (diagnostics).  Returns status.
+template <typename T>
+int launch_stage(trapbec_ctx* c, int kind, StageArgs<T>& a, int* nblk_out) {
+  if (use_tiled<T>(c) && kind != 4) {
+    int rc = launch_tiled<T>(c->plan, kind, a, c->st, c->red, c->red_cap, nblk_out);
+    if (rc) { set_error("tiled stage launch failed"); return rc; }
+    CKL();
+    c->launches++;
+    return TRAPBEC_OK;
+  }
+  int g = simple_grid(c);
+  if (a.red && g > c->red_cap) g = c->red_cap;
+  switch (kind) {
+    case ST_S1: stage_simple_kernel<T, ST_S1><<<g, SIMPLE_THREADS, 0, c->st>>>(a); break;
+    case ST_S2: stage_simple_kernel<T, ST_S2><<<g, SIMPLE_THREADS, 0, c->st>>>(a); break;
+    case ST_S3: stage_simple_kernel<T, ST_S3><<<g, SIMPLE_THREADS, 0, c->st>>>(a); break;
+    case ST_EU: stage_simple_kernel<T, ST_EU><<<g, SIMPLE_THREADS, 0, c->st>>>(a); break;
+    default: stage_simple_kernel<T, 4><<<g, SIMPLE_THREADS, 0, c->st>>>(a); break;
+  }
+  CKL();
+  c->launches++;
+  if (nblk_out) *nblk_out = g;
+  return TRAPBEC_OK;
+}
+
+template <typename T> int apply_pending_scale(trapbec_ctx* c) {
+  if (!c->ctrl_init) return TRAPBEC_OK;
+  CK(cudaMemcpyAsync(c->host_ctrl, c->ctrl, sizeof(ImagCtrl), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  double s = c->host_ctrl->scale;
+  if (s != 1.0) {
+    scale_kernel<T><<<simple_grid(c), SIMPLE_THREADS, 0, c->st>>>((c_t<T>*)c->psi[c->cur], c->n, (T)s);
+    CKL();
+    c->launches++;
+    c->host_ctrl->scale = 1.0;
+    CK(cudaMemcpyAsync(c->ctrl, c->host_ctrl, sizeof(ImagCtrl), cudaMemcpyHostToDevice, c->st));
+    CK(cudaStreamSynchronize(c->st));
+  }
+  return TRAPBEC_OK;
+}
+
+// Diagnostics reduction of the current psi into c->host_red[NRED].
+template <typename T> int run_diag(trapbec_ctx* c) {
+  int rc = ensure_potential<T>(c, c->t);
+  if (rc) return rc;
+  StageArgs<T> a = base_args<T>(c, c->t);
+  a.psi_in = (const c_t<T>*)c->psi[c->cur];
+  a.red = c->red;
+  a.reduce = 2;
+  int nblk = 0;
+  rc = launch_stage<T>(c, 4, a, &nblk);
+  if (rc) return rc;
+  reduce_finalize_kernel<<<1, FIN_THREADS, 0, c->st>>>(c->red, nblk, c->red_out);
+  CKL();
+  c->launches++;
+  CK(cudaMemcpyAsync(c->host_red, c->red_out, sizeof(double) * NRED, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return TRAPBEC_OK;
+}
+
+template <typename T> double cell_volume(const trapbec_ctx* c) {
+  const trapbec_params& p = c->p;
+  double hx = (double)((T)p.lx / (T)p.nx), hy = (double)((T)p.ly / (T)p.ny), hz = (double)((T)p.lz / (T)p.nz);
+  return hx * hy * (p.two_dim ? 1.0 : hz);
+}
+
+template <typename T> void fill_diag(trapbec_ctx* c, trapbec_diag_out* o) {
+  const double* r = c->host_red;
+  const trapbec_params& p = c->p;
+  double dV = cell_volume<T>(c);
+  o->intpsi2 = r[0];
+  o->maxpsi = r[6];
+  o->minpsi = r[7];
+  o->meanpsi = r[5] / ((double)p.nx * p.ny * p.nz);
+  o->norm = dV * r[0];
+  o->kinetic = r[1];
+  o->potential = r[2];
+  o->interaction = r[3];
+  o->rotation = r[4];
+  o->energy = dV * (-0.5 * r[1] + 0.5 * r[2] + 0.25 * r[3] - 0.5 * r[4]);
+  o->mu = (-0.5 * r[1] + 0.5 * r[2] + 0.5 * r[3] - 0.5 * r[4]) / r[0];
+  o->nonfinite = r[8] != 0.0 ? 1 : 0;
+  o->reserved = 0;
+}
+
+// ---------------------------------------------------------------- steps --
+template <typename T> int do_step_rt(trapbec_ctx* c, int nsteps) {
+  int rc = apply_pending_scale<T>(c);
+  if (rc) return rc;
+  // run.f90:42: dt = dt*(1 - i*gamma), formed in the reference precision
+  T dr = (T)c->dt_re, di = (T)c->dt_im, g = (T)c->gamma;
+  T dcr = dr * (T)1 - di * (-g);
+  T dci = dr * (-g) + di * (T)1;
+  // eye*0.5*dt = (0, 0.5)*dt = (-0.5*Im dt, 0.5*Re dt)  (run.f90:47)
+  T cre = -(T)0.5 * dci, cim = (T)0.5 * dcr;
+  const T a2 = (T)(-2.) / (T)3.;
+  CK(cudaEventRecord(c->e0, c->st));
+  for (int s = 0; s < nsteps; ++s) {
+    rc = ensure_potential<T>(c, c->t);
+    if (rc) return rc;
+    StageArgs<T> a = base_args<T>(c, c->t);
+    a.c_re = cre; a.c_im = cim;
+    a.w = (c_t<T>*)c->w;
+    // stage 1: w = c rhs; psi += w/3
+    a.psi_in = (const c_t<T>*)c->psi[c->cur]; a.psi_out = (c_t<T>*)c->psi[c->cur ^ 1];
+    a.A = 0; a.B = (T)1 / (T)3;
+    if ((rc = launch_stage<T>(c, ST_S1, a, nullptr))) return rc;
+    // stage 2: w = -2/3 w + c rhs; psi += w
+    a.psi_in = (const c_t<T>*)c->psi[c->cur ^ 1]; a.psi_out = (c_t<T>*)c->psi[c->cur];
+    a.A = a2; a.B = (T)1;
+    if ((rc = launch_stage<T>(c, ST_S2, a, nullptr))) return rc;
+    // stage 3: w = -w + c rhs; psi += w/2
+    a.psi_in = (const c_t<T>*)c->psi[c->cur]; a.psi_out = (c_t<T>*)c->psi[c->cur ^ 1];
+    a.A = (T)(-1); a.B = (T)0.5;
+    if ((rc = launch_stage<T>(c, ST_S3, a, nullptr))) return rc;
+    c->cur ^= 1;
+    c->t = (double)((T)c->t + dcr);   // run.f90:55, t real
+  }
+  CK(cudaEventRecord(c->e1, c->st));
+  CK(cudaEventSynchronize(c->e1));
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, c->e0, c->e1));
+  c->last_ms = ms;
+  return TRAPBEC_OK;
+}
+
+template <typename T> int do_imag_euler(trapbec_ctx* c, int nsteps, int* steps_done, double* ratio) {
+  int rc = apply_pending_scale<T>(c);
+  if (rc) return rc;
+  // run.f90:22: Psi = Psi + dt*0.5*rhs, with dt before the damping of run.f90:42
+  T cre = (T)c->dt_re * (T)0.5, cim = (T)c->dt_im * (T)0.5;
+  double r = 0.0;
+  for (int s = 0; s < nsteps; ++s) {
+    if ((rc = ensure_potential<T>(c, c->t))) return rc;
+    StageArgs<T> a = base_args<T>(c, c->t);
+    a.c_re = cre; a.c_im = cim;
+    a.psi_in = (const c_t<T>*)c->psi[c->cur]; a.psi_out = (c_t<T>*)c->psi[c->cur ^ 1];
+    if ((rc = launch_stage<T>(c, ST_EU, a, nullptr))) return rc;
+    c->cur ^= 1;
+    if ((rc = run_diag<T>(c))) return rc;   // Psi_norm (run.f90:23)
+    double nrm = c->host_red[0];
+    r = nrm / c->intpsi2_old;
+    c->intpsi2_old = nrm;
+  }
+  *steps_done = nsteps;
+  *ratio = r;
+  return TRAPBEC_OK;
+}
+
+template <typename T> int do_imag_rk3(trapbec_ctx* c, int nsteps, double tol, int* steps_done, double* rel_out) {
+  int rc = apply_pending_scale<T>(c);
+  if (rc) return rc;
+  double dV = cell_volume<T>(c);
+  if (c->norm_target <= 0) {
+    if ((rc = run_diag<T>(c))) return rc;
+    c->norm_target = dV * c->host_red[0];
+  }
+  if (!c->ctrl_init) {
+    std::memset(c->host_ctrl, 0, sizeof(ImagCtrl));
+    c->host_ctrl->scale = 1.0;
+    c->ctrl_init = true;
+  } else {
+    CK(cudaMemcpyAsync(c->host_ctrl, c->ctrl, sizeof(ImagCtrl), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+  }
+  c->host_ctrl->n0 = c->norm_target;
+  c->host_ctrl->tol = tol;
+  c->host_ctrl->dV = dV;
+  c->host_ctrl->converged = 0;
+  c->host_ctrl->step = 0;
+  c->host_ctrl->nonfinite = 0;
+  c->host_ctrl->have_prev = 0;   // the first comparison is after the first step
+  CK(cudaMemcpyAsync(c->ctrl, c->host_ctrl, sizeof(ImagCtrl), cudaMemcpyHostToDevice, c->st));
+  const T cf = (T)0.5 * (T)c->dt_re;
+  const T a2 = (T)(-2.) / (T)3.;
+  const int start_cur = c->cur;
+  CK(cudaEventRecord(c->e0, c->st));
+  int nblk = 0;
+  for (int s = 0; s < nsteps; ++s) {
+    if ((rc = ensure_potential<T>(c, c->t))) return rc;
+    StageArgs<T> a = base_args<T>(c, c->t);
+    a.c_re = cf; a.c_im = 0;
+    a.w = (c_t<T>*)c->w;
+    a.ctrl = c->ctrl;
+    int par = (start_cur + s) & 1;
+    // stage 1 (+ energy of the incoming, renormalised state)
+    a.psi_in = (const c_t<T>*)c->psi[par]; a.psi_out = (c_t<T>*)c->psi[par ^ 1];
+    a.A = 0; a.B = (T)1 / (T)3;
+    a.red = c->red; a.reduce = 2; a.use_ctrl_scale = 1;
+    if ((rc = launch_stage<T>(c, ST_S1, a, &nblk))) return rc;
+    imag_fin_energy_kernel<<<1, FIN_THREADS, 0, c->st>>>(c->red, nblk, c->ctrl);
+    CKL();
+    c->launches++;
+    a.reduce = 0; a.red = nullptr; a.use_ctrl_scale = 0;
+    a.psi_in = (const c_t<T>*)c->psi[par ^ 1]; a.psi_out = (c_t<T>*)c->psi[par];
+    a.A = a2; a.B = (T)1;
+    if ((rc = launch_stage<T>(c, ST_S2, a, nullptr))) return rc;
+    a.psi_in = (const c_t<T>*)c->psi[par]; a.psi_out = (c_t<T>*)c->psi[par ^ 1];
+    a.A = (T)(-1); a.B = (T)0.5;
+    a.red = c->red; a.reduce = 1;
+    if ((rc = launch_stage<T>(c, ST_S3, a, &nblk))) return rc;
+    imag_fin_norm_kernel<<<1, FIN_THREADS, 0, c->st>>>(c->red, nblk, c->ctrl);
+    CKL();
+    c->launches++;
+    if ((s + 1) % 64 == 0 || s + 1 == nsteps) {
+      CK(cudaMemcpyAsync(c->host_ctrl, c->ctrl, sizeof(ImagCtrl), cudaMemcpyDeviceToHost, c->st));
+      CK(cudaStreamSynchronize(c->st));
+      if (c->host_ctrl->converged || c->host_ctrl->nonfinite) break;
+    }
+  }
+  CK(cudaEventRecord(c->e1, c->st));
+  CK(cudaMemcpyAsync(c->host_ctrl, c->ctrl, sizeof(ImagCtrl), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, c->e0, c->e1));
+  c->last_ms = ms;
+  ImagCtrl& h = *c->host_ctrl;
+  int done = h.step;
+  c->cur = (start_cur + done) & 1;
+  if (h.nonfinite) {
+    *steps_done = done;
+    *rel_out = NAN;
+    set_error("non-finite norm in imaginary-time relaxation");
+    return TRAPBEC_ERR_NONFINITE;
+  }
+  if (!h.converged) {
+    // Energy of the final state (the loop forms E_n in the next step's stage 1).
+    if ((rc = apply_pending_scale<T>(c))) return rc;
+    if ((rc = run_diag<T>(c))) return rc;
+    trapbec_diag_out d;
+    fill_diag<T>(c, &d);
+    double rel = h.have_prev ? std::fabs(d.energy - h.e_prev) / std::fabs(d.energy) : INFINITY;
+    h.e_prev = d.energy;
+    h.have_prev = 1;
+    h.rel = rel;
+    h.energy = d.energy;
+    h.mu = d.mu;
+    CK(cudaMemcpyAsync(c->ctrl, c->host_ctrl, sizeof(ImagCtrl), cudaMemcpyHostToDevice, c->st));
+    CK(cudaStreamSynchronize(c->st));
+  } else {
+    if ((rc = apply_pending_scale<T>(c))) return rc;
+  }
+  *steps_done = done;
+  *rel_out = h.rel;
+  return TRAPBEC_OK;
+}
+
+template <typename T> int init_state_impl(trapbec_ctx* c, const char* name, const trapbec_init_args* ia) {
+  const trapbec_params& p = c->p;
+  std::string nm(name);
+  InitArgsDev<T> a;
+  std::memset(&a, 0, sizeof(a));
+  a.psi = (c_t<T>*)c->psi[c->cur];
+  a.xx = (const T*)c->xx; a.yy = (const T*)c->yy; a.zz = (const T*)c->zz;
+  a.nx = p.nx; a.ny = p.ny; a.nz = p.nz;
+  a.wn = p.winding_number;
+  a.Lx = (T)p.lx; a.Ly = (T)p.ly; a.Lz = (T)p.lz;
+  a.pi = (T)3.14159265359;   // cdata.f90:13
+  a.harm_wx = (T)p.harm_wx; a.harm_wy = (T)p.harm_wy; a.harm_wz = (T)p.harm_wz;
+  tbh::Rng rng{ia ? ia->seed : 0};
+  auto runif = [&](T lo, T hi) { T u = (T)rng.next(); return lo + u * (hi - lo); };
+  auto go = [&](int kind) -> int {
+    a.kind = kind;
+    init_state_kernel<T><<<simple_grid(c), SIMPLE_THREADS, 0, c->st>>>(a);
+    CKL();
+    c->launches++;
+    return TRAPBEC_OK;
+  };
+  int rc = TRAPBEC_OK;
+  const T pi = a.pi;
+  if (nm == "constant") {
+    a.v[0] = a.v[1] = (T)1 / std::sqrt((T)2);
+    rc = go(IK_CONST);
+  } else if (nm == "thomas_fermi") {
+    rc = go(IK_TF);
+  } else if (nm == "soliton") {
+    if (!(rc = go(IK_TF))) rc = go(IK_SOLITON_PHASE);
+  } else if (nm == "single_vortex") {
+    rc = go(IK_SINGLE);
+  } else if (nm == "sausage") {
+    rc = go(IK_SAUSAGE);
+  } else if (nm == "crow") {
+    rc = go(IK_CROW);
+  } else if (nm == "random_points" || nm == "leap_frog") {
+    a.v[0] = a.v[1] = (T)0.7071;
+    if ((rc = go(IK_SET))) return rc;
+    int nv = nm == "random_points" ? 20 : 4;
+    for (int v = 1; v <= nv; ++v) {
+      T vx, vy, dir;
+      if (nm == "random_points") {
+        vx = runif(-(T)p.lx / (T)5, (T)p.lx / (T)5);
+        vy = runif(-(T)p.ly / (T)5, (T)p.ly / (T)5);
+        dir = runif((T)0.9, (T)1);
+        dir = dir < (T)0.5 ? (T)(-1) : (T)1;
+      } else {
+        const T sh = 3, s1 = 3, s2 = 12;
+        if (v == 1) { vx = -sh; vy = s1; dir = 1; }
+        else if (v == 2) { vx = sh; vy = s2; dir = 1; }
+        else if (v == 3) { vx = -sh; vy = -s1; dir = -1; }
+        else { vx = sh; vy = -s2; dir = -1; }
+      }
+      a.v[0] = vx; a.v[1] = vy; a.v[2] = dir;
+      if ((rc = go(IK_VORTEX_MUL))) return rc;
+    }
+  } else if (nm == "vortex_rings") {
+    a.v[0] = 1; a.v[1] = 0;
+    if ((rc = go(IK_SET))) return rc;
+    for (int v = 1; v <= p.vor_ring_count; ++v) {
+      T ax = runif(0, 0), ay = runif(0, (T)2 * pi), az = runif(0, (T)2 * pi);
+      T tu = runif(-1, 1), tth = runif(0, (T)2 * pi), tr = runif(0, (T)p.lx / (T)6);
+      T tx = tr * std::sqrt((T)1 - tu * tu) * std::cos(tth);
+      T ty = tr * std::sqrt((T)1 - tu * tu) * std::sin(tth);
+      T tz = tr * tu;
+      a.v[0] = ax; a.v[1] = ay; a.v[2] = az; a.v[3] = tx; a.v[4] = ty; a.v[5] = tz; a.v[6] = (T)p.ring_rad;
+      if ((rc = go(IK_RING_MUL))) return rc;
+    }
+  } else if (nm == "tf_vortex_line" || nm == "tf_vortex_ring" || nm == "tf_noise") {
+    if (!ia) { set_error("init_state: workload states need trapbec_init_args"); return TRAPBEC_ERR_ARG; }
+    a.d[0] = ia->amp; a.d[1] = ia->r_tf2[0]; a.d[2] = ia->r_tf2[1]; a.d[3] = ia->r_tf2[2];
+    a.d[4] = ia->ring_radius; a.d[5] = ia->core2; a.d[6] = ia->noise_amp;
+    a.seed = ia->seed;
+    rc = go(nm == "tf_vortex_line" ? IK_TF_LINE : (nm == "tf_vortex_ring" ? IK_TF_RING : IK_TF_NOISE));
+  } else {
+    set_error("unknown initial state: " + nm);   // initial.f90:155-156
+    return TRAPBEC_ERR_ARG;
+  }
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(c->st));
+  return TRAPBEC_OK;
+}
+
+template <typename T> int create_impl(trapbec_ctx* c) {
+  const trapbec_params& p = c->p;
+  size_t n = c->n;
+  CK(cudaMalloc(&c->psi[0], n * c->esz));
+  CK(cudaMalloc(&c->psi[1], n * c->esz));
+  CK(cudaMalloc(&c->w, n * c->esz));
+  CK(cudaMemsetAsync(c->psi[0], 0, n * c->esz, c->st));
+  CK(cudaMemsetAsync(c->psi[1], 0, n * c->esz, c->st));
+  CK(cudaMemsetAsync(c->w, 0, n * c->esz, c->st));
+  CK(cudaMalloc(&c->xx, sizeof(T) * p.nx));
+  CK(cudaMalloc(&c->yy, sizeof(T) * p.ny));
+  CK(cudaMalloc(&c->zz, sizeof(T) * p.nz));
+  CK(cudaMalloc(&c->px, sizeof(T) * p.nx));
+  CK(cudaMalloc(&c->py, sizeof(T) * p.ny));
+  CK(cudaMalloc(&c->pz, sizeof(T) * p.nz));
+  c->red_cap = std::max(4096, c->nsm * 16);
+  CK(cudaMalloc(&c->red, sizeof(double) * NRED * (size_t)c->red_cap));
+  CK(cudaMalloc(&c->red_out, sizeof(double) * NRED));
+  CK(cudaMallocHost(&c->host_red, sizeof(double) * NRED));
+  CK(cudaMalloc(&c->ctrl, sizeof(ImagCtrl)));
+  CK(cudaMallocHost(&c->host_ctrl, sizeof(ImagCtrl)));
+  CK(cudaMemsetAsync(c->ctrl, 0, sizeof(ImagCtrl), c->st));
+  int rc = setup_tables<T>(c);
+  if (rc) return rc;
+  c->plan_valid = (plan_tiled<T>(c->p, c->xx, c->psi, c->w, c->nsm, c->tile_z, c->tile_y, &c->plan) == 0);
+  return TRAPBEC_OK;
+}
+
+void free_ctx(trapbec_ctx* c) {
+  if (!c) return;
+  void* bufs[] = {c->psi[0], c->psi[1], c->w, c->xx, c->yy, c->zz, c->px, c->py, c->pz,
+                  c->trap_user, c->trap_eff, c->red, c->red_out, c->ctrl};
+  for (void* b : bufs) if (b) cudaFree(b);
+  if (c->host_red) cudaFreeHost(c->host_red);
+  if (c->host_ctrl) cudaFreeHost(c->host_ctrl);
+  if (c->e0) cudaEventDestroy(c->e0);
+  if (c->e1) cudaEventDestroy(c->e1);
+  if (c->st) cudaStreamDestroy(c->st);
+  delete c;
+}
+
+int validate(const trapbec_params* p) {
+  if (!p) { set_error("null params"); return TRAPBEC_ERR_ARG; }
+  if (p->nx <= 0 || p->ny <= 0 || p->nz <= 0) { set_error("grid sizes must be positive"); return TRAPBEC_ERR_ARG; }
+  if (p->precision != TRAPBEC_FP32 && p->precision != TRAPBEC_FP64) { set_error("bad precision"); return TRAPBEC_ERR_ARG; }
+  if (p->boundaries < 0 || p->boundaries > 2) { set_error("wrong boundaries set"); return TRAPBEC_ERR_ARG; }
+  if (p->potential < 0 || p->potential > 10) { set_error("error incorrect potential set"); return TRAPBEC_ERR_ARG; }
+  int px = p->nprocx > 0 ? p->nprocx : 1, py = p->nprocy > 0 ? p->nprocy : 1;
+  if (p->nx % px || p->ny % py) {  // mpi_var.f90:157-160
+    set_error("unable to evenly subdivide grid check meshsize and number of processors");
+    return TRAPBEC_ERR_ARG;
+  }
+  // Ghost fills reach 3 cells in: solid and periodic boundaries need n >= 4
+  // on every axis whose derivatives are used (ghost.f90 mirrors Psi(2..4)).
+  bool needz = !p->two_dim;
+  if (p->nx < 4 || p->ny < 4 || (needz && p->nz < 4)) {
+    set_error("grid must have at least 4 cells per differentiated axis");
+    return TRAPBEC_ERR_ARG;
+  }
+  if (p->lx <= 0 || p->ly <= 0 || p->lz <= 0) { set_error("box lengths must be positive"); return TRAPBEC_ERR_ARG; }
+  return TRAPBEC_OK;
+}
+
+#define DISPATCH(ctx, fn, ...) ((ctx)->prec == TRAPBEC_FP64 ? fn<double>(__VA_ARGS__) : fn<float>(__VA_ARGS__))
+
+// Interior <-> ghosted host layouts: Psi(-2:nz+3,-2:ny+3,-2:nx+3).
+void to_ghosted(const trapbec_params& p, const char* in, char* out, size_t esz) {
+  size_t gz = p.nz + 6, gy = p.ny + 6, gx = p.nx + 6;
+  std::memset(out, 0, gz * gy * gx * esz);
+  for (int i = 0; i < p.nx; ++i)
+    for (int j = 0; j < p.ny; ++j)
+      std::memcpy(out + (((size_t)(i + 3) * gy + (j + 3)) * gz + 3) * esz,
+                  in + (((size_t)i * p.ny + j) * p.nz) * esz, (size_t)p.nz * esz);
+}
+void from_ghosted(const trapbec_params& p, const char* in, char* out, size_t esz) {
+  size_t gz = p.nz + 6, gy = p.ny + 6;
+  for (int i = 0; i < p.nx; ++i)
+    for (int j = 0; j < p.ny; ++j)
+      std::memcpy(out + (((size_t)i * p.ny + j) * p.nz) * esz,
+                  in + (((size_t)(i + 3) * gy + (j + 3)) * gz + 3) * esz, (size_t)p.nz * esz);
+}
+// Fill the ghost shell the way ghost_comm leaves it on one rank (faces only;
+// edges and corners stay zero as the reference never writes them).
+void ghost_fill_host(const trapbec_params& p, char* g, size_t esz) {
+  const int nx = p.nx, ny = p.ny, nz = p.nz;
+  size_t gz = nz + 6, gy = ny + 6;
+  auto at = [&](int k, int j, int i) { return g + (((size_t)(i + 2) * gy + (j + 2)) * gz + (k + 2)) * esz; };
+  auto cp = [&](char* dst, const char* src) { std::memcpy(dst, src, esz); };
+  auto zero = [&](char* dst) { std::memset(dst, 0, esz); };
+  // 1-based Fortran indices below (ghost.f90:27-192)
+  for (int m = 1; m <= 3; ++m)
+    for (int j = 1; j <= ny; ++j)
+      for (int k = 1; k <= nz; ++k) {
+        char* hi = at(k, j, nx + m); char* lo = at(k, j, 1 - m);
+        if (p.boundaries == TRAPBEC_BC_PERIODIC) { cp(hi, at(k, j, m)); cp(lo, at(k, j, nx + 1 - m)); }
+        else if (p.boundaries == TRAPBEC_BC_SOLID) { cp(hi, at(k, j, nx - m)); cp(lo, at(k, j, 1 + m)); }
+        else { zero(hi); zero(lo); }
+      }
+  for (int i = 1; i <= nx; ++i)
+    for (int m = 1; m <= 3; ++m)
+      for (int k = 1; k <= nz; ++k) {
+        char* hi = at(k, ny + m, i); char* lo = at(k, 1 - m, i);
+        if (p.boundaries == TRAPBEC_BC_PERIODIC) { cp(hi, at(k, m, i)); cp(lo, at(k, ny + 1 - m, i)); }
+        else if (p.boundaries == TRAPBEC_BC_SOLID) { cp(hi, at(k, ny - m, i)); cp(lo, at(k, 1 + m, i)); }
+        else { zero(hi); zero(lo); }
+      }
+  bool zper = p.periodicz || p.boundaries == TRAPBEC_BC_PERIODIC;
+  for (int i = 1; i <= nx; ++i)
+    for (int j = 1; j <= ny; ++j)
+      for (int m = 1; m <= 3; ++m) {
+        char* hi = at(nz + m, j, i); char* lo = at(1 - m, j, i);
+        if (zper) { cp(hi, at(m, j, i)); cp(lo, at(nz + 1 - m, j, i)); }
+        else if (p.boundaries == TRAPBEC_BC_SOLID) { cp(hi, at(nz - m, j, i)); cp(lo, at(1 + m, j, i)); }
+        else { zero(hi); zero(lo); }
+      }
+}
+
+}  // namespace
+
+// ================================================================== C ABI ==
+extern "C" {
+
+int trapbec_abi_version(void) { return TRAPBEC_ABI_VERSION; }
+
+int trapbec_abi_struct_size(int which) {
+  switch (which) {
+    case 0: return (int)sizeof(trapbec_params);
+    case 1: return (int)sizeof(trapbec_diag_out);
+    case 2: return (int)sizeof(trapbec_init_args);
+  }
+  return -1;
+}
+
+const char* trapbec_strerror(int code) {
+  switch (code) {
+    case TRAPBEC_OK: return "ok";
+    case TRAPBEC_ERR_ARG: return "invalid argument";
+    case TRAPBEC_ERR_CUDA: return "CUDA error";
+    case TRAPBEC_ERR_NOMEM: return "out of memory";
+    case TRAPBEC_ERR_STATE: return "invalid state";
+    case TRAPBEC_ERR_TIMEOUT: return "device wait timed out";
+    case TRAPBEC_ERR_NONFINITE: return "non-finite values in psi";
+    case TRAPBEC_ERR_IO: return "I/O error";
+    case TRAPBEC_ERR_UNSUPPORTED: return "unsupported";
+    case TRAPBEC_ERR_PARSE: return "parse error";
+    case TRAPBEC_ERR_NODEVICE: return "no CUDA device";
+  }
+  return "unknown error";
+}
+
+const char* trapbec_last_error(void) { return tbh::get_error(); }
+
+int trapbec_create(const trapbec_params* p, trapbec_ctx** out) {
+  if (!out) return TRAPBEC_ERR_ARG;
+  *out = nullptr;
+  int rc = validate(p);
+  if (rc) return rc;
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0) {
+    set_error(std::string("no CUDA device: ") + cudaGetErrorString(e));
+    return TRAPBEC_ERR_NODEVICE;
+  }
+  trapbec_ctx* c = new trapbec_ctx;
+  c->p = *p;
+  c->prec = p->precision;
+  c->n = (size_t)p->nx * p->ny * p->nz;
+  c->rsz = p->precision == TRAPBEC_FP64 ? 8 : 4;
+  c->esz = 2 * c->rsz;
+  c->dt_re = p->dt_re; c->dt_im = p->dt_im; c->gamma = p->gamma;
+  c->omega = p->omega_z; c->vx = p->advective_vx;
+  cudaGetDevice(&c->dev);
+  cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, c->dev);
+  g_nsm_cache = c->nsm;
+  auto bail = [&](int code) { free_ctx(c); return code; };
+  if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess) {
+    set_error("cudaStreamCreate failed");
+    return bail(TRAPBEC_ERR_CUDA);
+  }
+  cudaEventCreate(&c->e0);
+  cudaEventCreate(&c->e1);
+  rc = DISPATCH(c, create_impl, c);
+  if (rc) return bail(rc);
+  *out = c;
+  return TRAPBEC_OK;
+}
+
+void trapbec_destroy(trapbec_ctx* c) {
+  if (c && c->st) cudaStreamSynchronize(c->st);
+  free_ctx(c);
+}
+
+int trapbec_set_psi(trapbec_ctx* c, const void* psi, int layout) {
+  if (!c || !psi) return TRAPBEC_ERR_ARG;
+  if (layout == TRAPBEC_LAYOUT_INTERIOR) {
+    CK(cudaMemcpyAsync(c->psi[c->cur], psi, c->n * c->esz, cudaMemcpyHostToDevice, c->st));
+  } else if (layout == TRAPBEC_LAYOUT_GHOSTED) {
+    std::vector<char> tmp(c->n * c->esz);
+    from_ghosted(c->p, (const char*)psi, tmp.data(), c->esz);
+    CK(cudaMemcpyAsync(c->psi[c->cur], tmp.data(), c->n * c->esz, cudaMemcpyHostToDevice, c->st));
+    CK(cudaStreamSynchronize(c->st));
+  } else {
+    set_error("bad layout");
+    return TRAPBEC_ERR_ARG;
+  }
+  if (c->ctrl_init) {  // a new state cancels any pending renormalisation
+    c->host_ctrl->scale = 1.0;
+    c->host_ctrl->have_prev = 0;
+    CK(cudaMemcpyAsync(c->ctrl, c->host_ctrl, sizeof(ImagCtrl), cudaMemcpyHostToDevice, c->st));
+  }
+  CK(cudaStreamSynchronize(c->st));
+  return TRAPBEC_OK;
+}
+
+int trapbec_get_psi(trapbec_ctx* c, void* psi, int layout) {
+  if (!c || !psi) return TRAPBEC_ERR_ARG;
+  int rc = DISPATCH(c, apply_pending_scale, c);
+  if (rc) return rc;
+  if (layout == TRAPBEC_LAYOUT_INTERIOR) {
+    CK(cudaMemcpyAsync(psi, c->psi[c->cur], c->n * c->esz, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+  } else if (layout == TRAPBEC_LAYOUT_GHOSTED) {
+    std::vector<char> tmp(c->n * c->esz);
+    CK(cudaMemcpyAsync(tmp.data(), c->psi[c->cur], c->n * c->esz, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    to_ghosted(c->p, tmp.data(), (char*)psi, c->esz);
+    ghost_fill_host(c->p, (char*)psi, c->esz);
+  } else {
+    set_error("bad layout");
+    return TRAPBEC_ERR_ARG;
+  }
+  return TRAPBEC_OK;
+}
+
+int trapbec_set_trap(trapbec_ctx* c, const double* trap) {
+  if (!c || !trap) return TRAPBEC_ERR_ARG;
+  if (!c->trap_user) CK(cudaMalloc(&c->trap_user, c->n * c->rsz));
+  if (c->prec == TRAPBEC_FP64) {
+    CK(cudaMemcpyAsync(c->trap_user, trap, c->n * 8, cudaMemcpyHostToDevice, c->st));
+    CK(cudaStreamSynchronize(c->st));
+  } else {
+    std::vector<float> f(c->n);
+    for (size_t i = 0; i < c->n; ++i) f[i] = (float)trap[i];
+    CK(cudaMemcpyAsync(c->trap_user, f.data(), c->n * 4, cudaMemcpyHostToDevice, c->st));
+    CK(cudaStreamSynchronize(c->st));
+  }
+  c->pot_valid = false;
+  return TRAPBEC_OK;
+}
+
+int trapbec_init_state(trapbec_ctx* c, const char* name, const trapbec_init_args* args) {
+  if (!c || !name) return TRAPBEC_ERR_ARG;
+  int rc = DISPATCH(c, init_state_impl, c, name, args);
+  if (rc) return rc;
+  if (c->ctrl_init) {
+    c->host_ctrl->scale = 1.0;
+    c->host_ctrl->have_prev = 0;
+    CK(cudaMemcpyAsync(c->ctrl, c->host_ctrl, sizeof(ImagCtrl), cudaMemcpyHostToDevice, c->st));
+    CK(cudaStreamSynchronize(c->st));
+  }
+  return TRAPBEC_OK;
+}
+
+}  // extern "C"
+namespace {
+template <typename T> int get_rhs_impl(trapbec_ctx* c, void* out) {
+  int rc = apply_pending_scale<T>(c);
+  if (rc) return rc;
+  if ((rc = ensure_potential<T>(c, c->t))) return rc;
+  StageArgs<T> a = base_args<T>(c, c->t);
+  a.c_re = 1; a.c_im = 0; a.A = 0; a.B = 0;   // w = 1*rhs exactly
+  a.w = (c_t<T>*)c->w;
+  a.psi_in = (const c_t<T>*)c->psi[c->cur];
+  a.psi_out = (c_t<T>*)c->psi[c->cur ^ 1];     // spare buffer, discarded
+  if ((rc = launch_stage<T>(c, ST_S1, a, nullptr))) return rc;
+  CK(cudaMemcpyAsync(out, c->w, c->n * c->esz, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return TRAPBEC_OK;
+}
+}  // namespace
+extern "C" {
+
+int trapbec_get_rhs(trapbec_ctx* c, void* rhs_out) {
+  if (!c || !rhs_out) return TRAPBEC_ERR_ARG;
+  return DISPATCH(c, get_rhs_impl, c, rhs_out);
+}
+
+int trapbec_step_rt(trapbec_ctx* c, int nsteps, double* t_inout) {
+  if (!c || nsteps < 0) return TRAPBEC_ERR_ARG;
+  if (t_inout) c->t = *t_inout;
+  int rc = DISPATCH(c, do_step_rt, c, nsteps);
+  if (t_inout) *t_inout = c->t;
+  return rc;
+}
+
+int trapbec_step_imag(trapbec_ctx* c, int nsteps, int variant, double tol, int* steps_done, double* stat_out) {
+  if (!c || nsteps < 0) return TRAPBEC_ERR_ARG;
+  int sd = 0;
+  double st = 0;
+  int rc;
+  if (variant == TRAPBEC_IMAG_REF_EULER) rc = DISPATCH(c, do_imag_euler, c, nsteps, &sd, &st);
+  else if (variant == TRAPBEC_IMAG_RK3_RENORM) rc = DISPATCH(c, do_imag_rk3, c, nsteps, tol, &sd, &st);
+  else { set_error("bad imaginary-time variant"); return TRAPBEC_ERR_ARG; }
+  if (steps_done) *steps_done = sd;
+  if (stat_out) *stat_out = st;
+  return rc;
+}
+
+}  // extern "C"
+namespace {
+template <typename T> int diag_impl(trapbec_ctx* c, trapbec_diag_out* o) {
+  int rc = apply_pending_scale<T>(c);
+  if (rc) return rc;
+  if ((rc = run_diag<T>(c))) return rc;
+  fill_diag<T>(c, o);
+  return TRAPBEC_OK;
+}
+}  // namespace
+extern "C" {
+
+int trapbec_diag(trapbec_ctx* c, trapbec_diag_out* out) {
+  if (!c || !out) return TRAPBEC_ERR_ARG;
+  return DISPATCH(c, diag_impl, c, out);
+}
+
+int trapbec_set_scalar(trapbec_ctx* c, int which, double v) {
+  if (!c) return TRAPBEC_ERR_ARG;
+  switch (which) {
+    case TRAPBEC_SCALAR_OMEGA_Z: c->omega = v; c->p.omega_z = v; break;
+    case TRAPBEC_SCALAR_DT_RE: c->dt_re = v; break;
+    case TRAPBEC_SCALAR_DT_IM: c->dt_im = v; break;
+    case TRAPBEC_SCALAR_GAMMA: c->gamma = v; break;
+    case TRAPBEC_SCALAR_T: c->t = v; break;
+    case TRAPBEC_SCALAR_ADVECTIVE_VX: c->vx = v; c->p.advective_vx = v; break;
+    case TRAPBEC_SCALAR_NORM_TARGET: c->norm_target = v; break;
+    default: set_error("unknown scalar"); return TRAPBEC_ERR_ARG;
+  }
+  return TRAPBEC_OK;
+}
+
+int trapbec_get_scalar(trapbec_ctx* c, int which, double* v) {
+  if (!c || !v) return TRAPBEC_ERR_ARG;
+  switch (which) {
+    case TRAPBEC_SCALAR_OMEGA_Z: *v = c->omega; break;
+    case TRAPBEC_SCALAR_DT_RE: *v = c->dt_re; break;
+    case TRAPBEC_SCALAR_DT_IM: *v = c->dt_im; break;
+    case TRAPBEC_SCALAR_GAMMA: *v = c->gamma; break;
+    case TRAPBEC_SCALAR_T: *v = c->t; break;
+    case TRAPBEC_SCALAR_ADVECTIVE_VX: *v = c->vx; break;
+    case TRAPBEC_SCALAR_NORM_TARGET: *v = c->norm_target; break;
+    default: set_error("unknown scalar"); return TRAPBEC_ERR_ARG;
+  }
+  return TRAPBEC_OK;
+}
+
+int trapbec_set_kernel(trapbec_ctx* c, int kind, int tile_z, int tile_y) {
+  if (!c || kind < 0 || kind > 2) return TRAPBEC_ERR_ARG;
+  c->kernel_kind = kind;
+  if (kind == 1) return TRAPBEC_OK;
+  if (tile_z != c->tile_z || tile_y != c->tile_y || !c->plan_valid) {
+    c->tile_z = tile_z;
+    c->tile_y = tile_y;
+    int rc = c->prec == TRAPBEC_FP64
+                 ? plan_tiled<double>(c->p, c->xx, c->psi, c->w, c->nsm, tile_z, tile_y, &c->plan)
+                 : plan_tiled<float>(c->p, c->xx, c->psi, c->w, c->nsm, tile_z, tile_y, &c->plan);
+    c->plan_valid = (rc == 0);
+  }
+  if (kind == 2 && !c->plan_valid) {
+    set_error("tiled kernel not available for this grid / tile shape");
+    return TRAPBEC_ERR_UNSUPPORTED;
+  }
+  return TRAPBEC_OK;
+}
+
+int trapbec_launch_count(trapbec_ctx* c, int64_t* count) {
+  if (!c || !count) return TRAPBEC_ERR_ARG;
+  *count = c->launches;
+  return TRAPBEC_OK;
+}
+
+int trapbec_last_kernel_ms(trapbec_ctx* c, double* ms) {
+  if (!c || !ms) return TRAPBEC_ERR_ARG;
+  *ms = c->last_ms;
+  return TRAPBEC_OK;
+}
+
+// ------------------------------------------------------------------ I/O ---
+int trapbec_write_var(trapbec_ctx* c, const char* datadir, int itime, int shots, double t, int imaginary) {
+  if (!c || !datadir || shots <= 0) return TRAPBEC_ERR_ARG;
+  std::vector<char> buf(c->n * c->esz);
+  int rc = trapbec_get_psi(c, buf.data(), TRAPBEC_LAYOUT_INTERIOR);
+  if (rc) return rc;
+  char name[64];
+  // output.f90:65,75: "./data/proc%03d/var%04d.dat" with itime/shots
+  std::snprintf(name, sizeof(name), "/proc%03d/%s%04d.dat", 0, imaginary ? "imag_var" : "var", itime / shots);
+  return tbh::write_var_file(std::string(datadir) + name, &c->p, t, buf.data(), buf.size());
+}
+
+int trapbec_write_restart(trapbec_ctx* c, const char* datadir, int itime, double t) {
+  if (!c || !datadir) return TRAPBEC_ERR_ARG;
+  std::vector<char> buf(c->n * c->esz);
+  int rc = trapbec_get_psi(c, buf.data(), TRAPBEC_LAYOUT_INTERIOR);
+  if (rc) return rc;
+  return tbh::write_restart_file(std::string(datadir) + "/proc000/var.dat", &c->p, itime, t, buf.data(),
+                                 buf.size());
+}
+
+int trapbec_read_restart(trapbec_ctx* c, const char* datadir, int* nstart, double* t) {
+  if (!c || !datadir || !nstart || !t) return TRAPBEC_ERR_ARG;
+  // The reference reader looks in proc%02d (initial.f90:44,800) while the
+  // writer uses proc%03d (output.f90:103); accept both, proc000 first.
+  std::vector<char> buf(c->n * c->esz);
+  std::string d(datadir);
+  int rc = tbh::read_restart_file(d + "/proc000/var.dat", &c->p, nstart, t, buf.data(), buf.size());
+  if (rc) rc = tbh::read_restart_file(d + "/proc00/var.dat", &c->p, nstart, t, buf.data(), buf.size());
+  if (rc) return rc;
+  c->t = *t;
+  return trapbec_set_psi(c, buf.data(), TRAPBEC_LAYOUT_INTERIOR);
+}
+
+}  // extern "C"

@@ -1,0 +1,167 @@
+"""Host-side mirror of the reference's hot-path operators over libtrapbec.
+
+The reference exposes its time stepping as module procedures on globals
+(finite_diff.f90 get_rhs, diagnostic.f90 Psi_norm / Psi_info, the RK3 and
+Euler loops of run.f90).  `Solver` gives the same operations, with the same
+meaning and units, on one GPU grid.  Arrays are numpy arrays of shape
+(Nx, Ny, Nz) in C order, which is the memory order of the Fortran Psi(k,j,i).
+There is no CPU fallback: every call goes through the CUDA library.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+from .abi import check, DiagOut, InitArgs, Params
+
+
+class Solver:
+    def __init__(self, params: Params):
+        self.lib = abi.load()
+        self.params = params.copy()
+        self.ctx = C.c_void_p()
+        check(self.lib.trapbec_create(C.byref(self.params), C.byref(self.ctx)), "trapbec_create")
+        fp64 = params.precision == abi.FP64
+        self.cdtype = np.complex128 if fp64 else np.complex64
+        self.rdtype = np.float64 if fp64 else np.float32
+        self.shape = (params.nx, params.ny, params.nz)
+        self.t = 0.0
+
+    # -- lifetime --------------------------------------------------------
+    def close(self) -> None:
+        if getattr(self, "ctx", None) and self.ctx.value:
+            self.lib.trapbec_destroy(self.ctx)
+            self.ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- state -----------------------------------------------------------
+    def set_psi(self, psi: np.ndarray, layout: int = abi.LAYOUT_INTERIOR) -> None:
+        a = np.ascontiguousarray(psi, dtype=self.cdtype)
+        want = self.shape if layout == abi.LAYOUT_INTERIOR else tuple(s + 6 for s in self.shape)
+        if a.shape != want:
+            a = a.reshape(want)
+        check(self.lib.trapbec_set_psi(self.ctx, a.ctypes.data, layout), "trapbec_set_psi")
+
+    def get_psi(self, layout: int = abi.LAYOUT_INTERIOR) -> np.ndarray:
+        shp = self.shape if layout == abi.LAYOUT_INTERIOR else tuple(s + 6 for s in self.shape)
+        a = np.empty(shp, dtype=self.cdtype)
+        check(self.lib.trapbec_get_psi(self.ctx, a.ctypes.data, layout), "trapbec_get_psi")
+        return a
+
+    def set_trap(self, trap: np.ndarray) -> None:
+        a = np.ascontiguousarray(trap.reshape(self.shape), dtype=np.float64)
+        check(self.lib.trapbec_set_trap(self.ctx, a.ctypes.data_as(C.POINTER(C.c_double))),
+              "trapbec_set_trap")
+
+    def init_state(self, name: str, seed: int = 0, amp: float = 1.0, r_tf2=(0.0, 0.0, 0.0),
+                   ring_radius: float = 0.0, core2: float = 0.0, noise_amp: float = 0.0) -> None:
+        a = InitArgs()
+        a.seed = int(seed)
+        a.amp = float(amp)
+        for i in range(3):
+            a.r_tf2[i] = float(r_tf2[i])
+        a.ring_radius = float(ring_radius)
+        a.core2 = float(core2)
+        a.noise_amp = float(noise_amp)
+        check(self.lib.trapbec_init_state(self.ctx, name.encode(), C.byref(a)), "trapbec_init_state")
+
+    # -- the hot path ----------------------------------------------------------
+    def get_rhs(self) -> np.ndarray:
+        """rhs = get_rhs(psi) (finite_diff.f90:8-136) of the current state."""
+        a = np.empty(self.shape, dtype=self.cdtype)
+        check(self.lib.trapbec_get_rhs(self.ctx, a.ctypes.data), "trapbec_get_rhs")
+        return a
+
+    def step_rt(self, nsteps: int) -> float:
+        """nsteps low-storage RK3 steps (run.f90:42-57); returns t."""
+        t = C.c_double(self.t)
+        check(self.lib.trapbec_step_rt(self.ctx, int(nsteps), C.byref(t)), "trapbec_step_rt")
+        self.t = t.value
+        return self.t
+
+    def step_imag(self, nsteps: int, variant: int = abi.IMAG_RK3_RENORM, tol: float = 0.0):
+        """Imaginary-time relaxation; returns (steps_done, stat)."""
+        s, st = C.c_int(0), C.c_double(0)
+        check(self.lib.trapbec_step_imag(self.ctx, int(nsteps), int(variant), float(tol),
+                                         C.byref(s), C.byref(st)), "trapbec_step_imag")
+        return s.value, st.value
+
+    def diag(self) -> dict:
+        d = DiagOut()
+        check(self.lib.trapbec_diag(self.ctx, C.byref(d)), "trapbec_diag")
+        return d.as_dict()
+
+    def psi_norm(self) -> float:
+        """intPsi2 of Psi_norm (diagnostic.f90:19-25), summed in FP64."""
+        return self.diag()["intpsi2"]
+
+    def psi_info(self) -> tuple[float, float, float]:
+        """(maxPsi, minPsi, meanPsi) of Psi_info (diagnostic.f90:7-17)."""
+        d = self.diag()
+        return d["maxpsi"], d["minpsi"], d["meanpsi"]
+
+    # -- controls ----------------------------------------------------------------
+    def set_scalar(self, which: int, value: float) -> None:
+        check(self.lib.trapbec_set_scalar(self.ctx, int(which), float(value)), "trapbec_set_scalar")
+        if which == abi.SCALAR_T:
+            self.t = float(value)
+
+    def get_scalar(self, which: int) -> float:
+        v = C.c_double(0)
+        check(self.lib.trapbec_get_scalar(self.ctx, int(which), C.byref(v)), "trapbec_get_scalar")
+        return v.value
+
+    def set_kernel(self, kind: int, tile_z: int = 0, tile_y: int = 0) -> None:
+        check(self.lib.trapbec_set_kernel(self.ctx, int(kind), int(tile_z), int(tile_y)),
+              "trapbec_set_kernel")
+
+    def launch_count(self) -> int:
+        v = C.c_int64(0)
+        check(self.lib.trapbec_launch_count(self.ctx, C.byref(v)), "trapbec_launch_count")
+        return v.value
+
+    def last_kernel_ms(self) -> float:
+        v = C.c_double(0)
+        check(self.lib.trapbec_last_kernel_ms(self.ctx, C.byref(v)), "trapbec_last_kernel_ms")
+        return v.value
+
+    # -- output layout -------------------------------------------------------------
+    def write_var(self, datadir: str, itime: int, shots: int, imaginary: bool = False) -> None:
+        check(self.lib.trapbec_write_var(self.ctx, datadir.encode(), int(itime), int(shots),
+                                         float(self.t), int(imaginary)), "trapbec_write_var")
+
+    def write_restart(self, datadir: str, itime: int) -> None:
+        check(self.lib.trapbec_write_restart(self.ctx, datadir.encode(), int(itime), float(self.t)),
+              "trapbec_write_restart")
+
+    def read_restart(self, datadir: str) -> int:
+        n, t = C.c_int(0), C.c_double(0)
+        check(self.lib.trapbec_read_restart(self.ctx, datadir.encode(), C.byref(n), C.byref(t)),
+              "trapbec_read_restart")
+        self.t = t.value
+        return n.value
+
+
+def parse_cparam(text: str, base: Params | None = None) -> Params:
+    """Parse cparam.local text (the reference's compile-time parameters) with
+    the library's parser into a Params, starting from `base` or the defaults."""
+    lib = abi.load()
+    p = base.copy() if base is not None else Params()
+    if base is None:
+        check(lib.trapbec_params_default(C.byref(p)), "trapbec_params_default")
+    err = C.create_string_buffer(256)
+    check(lib.trapbec_params_parse(text.encode(), C.byref(p), err, 256), "trapbec_params_parse")
+    return p
