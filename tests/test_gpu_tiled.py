@@ -1,0 +1,105 @@
+"""The tiled (TMA) stage kernel against the CPU oracle and the per-cell kernel,
+for every instantiated tile shape and boundary type, including partial tiles."""
+import numpy as np
+import pytest
+
+from oracle.pyoracle import Oracle
+from trapbec_gb300 import Solver, abi
+from tests.helpers import params, smooth_state, rel_err
+
+pytestmark = pytest.mark.gpu
+
+SHAPES = {abi.FP32: [(64, 8), (32, 16), (128, 8)], abi.FP64: [(32, 8), (64, 8)]}
+
+
+def _grid_for(tz, ty, bc, zper):
+    # full tiles where the boundary needs fix-ups, two tiles per axis
+    return (12, 2 * ty, 2 * tz)
+
+
+CASES = [(prec, shp, bc, zper) for prec in (abi.FP64, abi.FP32) for shp in SHAPES[prec]
+         for bc, zper in ((abi.BC_ZERO, 0), (abi.BC_SOLID, 0), (abi.BC_PERIODIC, 0), (abi.BC_ZERO, 1))]
+
+
+@pytest.mark.parametrize("prec,shape,bc,zper", CASES, ids=lambda v: str(v))
+def test_tiled_matches_oracle(prec, shape, bc, zper):
+    tz, ty = shape
+    n = _grid_for(tz, ty, bc, zper)
+    p = params(n=n, L=(0.5 * n[0], 0.5 * n[1], 0.5 * n[2]), prec=prec, bc=bc, periodicz=zper, pot="harmonic",
+               harm=(40.0, 50.0, 60.0), omega=0.35, dt=0.01)
+    psi = smooth_state(p, seed=21)
+    s = Solver(p)
+    s.set_kernel(2, tz, ty)
+    s.set_psi(psi)
+    o = Oracle(p)
+    o.set_psi(s.get_psi())
+    tol_rhs = 1e-13 if prec == abi.FP64 else 3e-6
+    assert rel_err(s.get_rhs(), o.get_rhs()) < tol_rhs
+    s.step_rt(6)
+    o.step_rt(6)
+    a = s.get_psi().astype(np.complex128)
+    b = o.get_psi().astype(np.complex128)
+    if prec == abi.FP64:
+        assert rel_err(a, b) < 1e-12
+    else:
+        assert np.linalg.norm(a - b) / np.linalg.norm(b) < 2e-6
+    d, do = s.diag(), o.diag()
+    tol = 1e-12 if prec == abi.FP64 else 2e-6
+    for k in ("norm", "energy", "maxpsi", "intpsi2"):
+        assert abs(d[k] - do[k]) <= tol * abs(do[k]), (k, d[k], do[k])
+
+
+@pytest.mark.parametrize("prec", [abi.FP32, abi.FP64])
+def test_tiled_partial_tiles_zero_ghosts(prec):
+    """Grids that are not a multiple of the tile: zero ghosts come from the
+    TMA out-of-bounds fill, outputs beyond the grid are masked."""
+    n = (9, 13, 70)
+    p = params(n=n, L=(4.5, 6.5, 35.0), prec=prec, pot="harmonic", harm=(3.0, 4.0, 5.0), omega=0.2, dt=0.01)
+    psi = smooth_state(p, seed=4)
+    s, o = Solver(p), Oracle(p)
+    s.set_kernel(2)
+    s.set_psi(psi)
+    o.set_psi(s.get_psi())
+    s.step_rt(5)
+    o.step_rt(5)
+    a, b = s.get_psi().astype(np.complex128), o.get_psi().astype(np.complex128)
+    assert np.linalg.norm(a - b) / np.linalg.norm(b) < (1e-13 if prec == abi.FP64 else 2e-6)
+
+
+def test_tiled_equals_simple_fp32_array_potential():
+    n = (10, 16, 64)
+    p = params(n=n, L=(10.0, 16.0, 64.0), prec=abi.FP32, pot="array", vx=0.1, dt=0.01)
+    trap = np.random.default_rng(2).uniform(0, 1, size=n)
+    psi = smooth_state(p, seed=5)
+    out = []
+    for kind in (1, 2):
+        s = Solver(p)
+        s.set_kernel(kind)
+        s.set_trap(trap)
+        s.set_psi(psi)
+        s.step_rt(4)
+        out.append(s.get_psi().astype(np.complex128))
+    assert np.linalg.norm(out[0] - out[1]) / np.linalg.norm(out[1]) < 1e-6
+
+
+@pytest.mark.parametrize("prec", [abi.FP64, abi.FP32])
+def test_tiled_imag_rk3(prec):
+    n = (16, 16, 64)
+    p = params(n=n, L=(8.0, 8.0, 16.0), prec=prec, pot="harmonic", harm=(64.0, 64.0, 256.0), omega=0.3, dt=0.005)
+    psi = smooth_state(p, seed=8)
+    s, o = Solver(p), Oracle(p)
+    s.set_kernel(2)
+    s.set_psi(psi)
+    o.set_psi(s.get_psi())
+    sg, _ = s.step_imag(60, abi.IMAG_RK3_RENORM, 0.0)
+    so, _ = o.step_imag_rk3(60, 0.0)
+    assert sg == so == 60
+    a, b = s.get_psi().astype(np.complex128), o.get_psi().astype(np.complex128)
+    d, do = s.diag(), o.diag()
+    if prec == abi.FP64:
+        assert rel_err(a, b) < 1e-11
+        assert abs(d["energy"] - do["energy"]) < 1e-12 * abs(do["energy"])
+    else:
+        assert np.linalg.norm(a - b) / np.linalg.norm(b) < 1e-5
+        assert abs(d["energy"] - do["energy"]) < 1e-5 * abs(do["energy"])
+    assert abs(d["norm"] / do["norm"] - 1) < (1e-12 if prec == abi.FP64 else 1e-6)

@@ -25,7 +25,8 @@ enum FrameMode : int { FRAME_NONE = 0, FRAME_ROT = 1, FRAME_ADV = 2 };
 //   S2: w = A*w + c*rhs,      psi' = psi + B*w, w stored     (run.f90:49-51)
 //   S3: w = A*w + c*rhs,      psi' = psi + B*w, w not stored (run.f90:52-54)
 //   EU: psi' = psi + c*rhs,   no w                           (run.f90:22)
-enum StageKind : int { ST_S1 = 0, ST_S2 = 1, ST_S3 = 2, ST_EU = 3 };
+//   DIAG: no update, no writes; reductions of the energy set only
+enum StageKind : int { ST_S1 = 0, ST_S2 = 1, ST_S3 = 2, ST_EU = 3, ST_DIAG = 4 };
 
 // Number of FP64 quantities a stage kernel may reduce (fused reductions).
 //   0: sum|psi|^2  1: sum Re psi* lap  2: sum pot|psi|^2  3: sum |psi|^4

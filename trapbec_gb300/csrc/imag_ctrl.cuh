@@ -36,7 +36,7 @@ __device__ __forceinline__ void imag_norm_update(const double* r, ImagCtrl* c) {
   c->step += 1;
 }
 
-__global__ void __launch_bounds__(FIN_THREADS) imag_fin_energy_kernel(const double* __restrict__ red, int nblk,
+static __global__ void __launch_bounds__(FIN_THREADS) imag_fin_energy_kernel(const double* __restrict__ red, int nblk,
                                                                       ImagCtrl* ctrl) {
   if (ctrl->converged || ctrl->nonfinite) return;
   __shared__ double out[NRED];
@@ -44,7 +44,7 @@ __global__ void __launch_bounds__(FIN_THREADS) imag_fin_energy_kernel(const doub
   if (threadIdx.x == 0) imag_energy_update(out, ctrl);
 }
 
-__global__ void __launch_bounds__(FIN_THREADS) imag_fin_norm_kernel(const double* __restrict__ red, int nblk,
+static __global__ void __launch_bounds__(FIN_THREADS) imag_fin_norm_kernel(const double* __restrict__ red, int nblk,
                                                                     ImagCtrl* ctrl) {
   if (ctrl->converged || ctrl->nonfinite) return;
   __shared__ double out[NRED];

@@ -170,7 +170,7 @@ __device__ __forceinline__ void finalize_partials(const double* __restrict__ red
   }
 }
 
-__global__ void __launch_bounds__(FIN_THREADS) reduce_finalize_kernel(const double* __restrict__ red,
+static __global__ void __launch_bounds__(FIN_THREADS) reduce_finalize_kernel(const double* __restrict__ red,
                                                                       int nblk, double* __restrict__ out) {
   finalize_partials(red, nblk, out);
 }

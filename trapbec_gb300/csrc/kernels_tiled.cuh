@@ -1,26 +1,472 @@
-// kernels_tiled.cuh -- TMA-staged, register-streaming stage kernel (fast path).
+// kernels_tiled.cuh -- TMA-staged, register-streaming fused RK3 stage kernel.
+//
+// One launch performs one stage of the 2N-storage RK3 (run.f90:46-54) over
+// the whole grid: rhs = get_rhs(psi) (finite_diff.f90:19-132) fused with the
+// w / psi updates, so psi is read once and written once per stage.
+//
+// Decomposition: the (y, z) plane is cut into TY x TZ tiles; a work unit is
+// one tile on one x-plane.  The units (tile-major, x-minor) are split evenly
+// over a persistent grid of CTAs, so each CTA streams a contiguous x-range of
+// one or two tiles and the load is balanced to within one plane.
+//
+// Staging: each x-plane of a tile is copied with one TMA box of
+// (TZ + 2*HZ) x (TY + 6) complex values (the 3-deep y/z ghost planes
+// included) into an S-slot shared-memory ring; slots are guarded by
+// mbarriers and refilled S planes ahead.  Out-of-range boxes come back zero,
+// which is the reference's 'zero' ghost fill (ghost.f90:53-55); for 'solid'
+// and periodic sides the x-plane coordinate is remapped before the copy and
+// the y/z ghost cells of boundary tiles are patched from global memory.
+// The x-direction neighbours live in a 7-deep register queue per thread
+// whose rotation is resolved at compile time (the x loop is unrolled by 7).
+// FP32 complex arithmetic uses Blackwell's packed f32x2 add/mul/fma.
+// Every mbarrier wait is bounded: on timeout the kernel records an error
+// code, drains its own copies (also bounded) and returns.
 #pragma once
+#include <cuda.h>
+
 #include "common.cuh"
+#include "kernels_simple.cuh"
+#include "tiled_api.h"
 
 namespace tb {
 
-struct TiledPlan {
-  int valid = 0;
+// ----------------------------------------------------- packed complex ops --
+template <typename T> struct PK;
+template <> struct PK<float> {
+  using V = float2;
+  static __device__ __forceinline__ unsigned long long u(V a) { return *reinterpret_cast<unsigned long long*>(&a); }
+  static __device__ __forceinline__ V v(unsigned long long a) { return *reinterpret_cast<V*>(&a); }
+  static __device__ __forceinline__ V add(V a, V b) {
+    unsigned long long r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(u(a)), "l"(u(b)));
+    return v(r);
+  }
+  static __device__ __forceinline__ V sub(V a, V b) {
+    unsigned long long r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(u(a)), "l"(u(b)));
+    return v(r);
+  }
+  static __device__ __forceinline__ V mul(V a, V b) {
+    unsigned long long r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(u(a)), "l"(u(b)));
+    return v(r);
+  }
+  static __device__ __forceinline__ V fma(V a, V b, V c) {
+    unsigned long long r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(u(a)), "l"(u(b)), "l"(u(c)));
+    return v(r);
+  }
+};
+template <> struct PK<double> {
+  using V = double2;
+  static __device__ __forceinline__ V add(V a, V b) { return make_double2(a.x + b.x, a.y + b.y); }
+  static __device__ __forceinline__ V sub(V a, V b) { return make_double2(a.x - b.x, a.y - b.y); }
+  static __device__ __forceinline__ V mul(V a, V b) { return make_double2(a.x * b.x, a.y * b.y); }
+  static __device__ __forceinline__ V fma(V a, V b, V c) {
+    return make_double2(::fma(a.x, b.x, c.x), ::fma(a.y, b.y, c.y));
+  }
+};
+template <typename T> __device__ __forceinline__ c_t<T> splat(T s) { return mk<T>(s, s); }
+
+// ------------------------------------------------------------- mbarrier --
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* b, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* b, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* tm, int c0, int c1, int c2, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+      ::"r"(smem_u32(dst)), "l"(tm), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// Error codes written to TiledArgs::err.
+enum TiledErr : int { TERR_NONE = 0, TERR_WAIT_TIMEOUT = 1 };
+constexpr uint32_t WAIT_SPIN_LIMIT = 1u << 24;  // try_wait calls (each may suspend) before giving up
+
+template <typename T> struct TiledArgs {
+  StageArgs<T> s;
+  int ntz, nty;            // tiles along z and y
+  long long units;         // ntz * nty * nx
+  int* err;                // error flag (device)
+  int bcz;                 // boundary type along z (periodic if zper)
+  int fix_y, fix_z;        // ghost fix-up needed on y / z boundary tiles
 };
 
-template <typename T>
-int plan_tiled(const trapbec_params& p, const void* xx, void* const psi[2], void* w, int nsm, int tz, int ty,
-               TiledPlan* plan) {
-  (void)p; (void)xx; (void)psi; (void)w; (void)nsm; (void)tz; (void)ty;
-  plan->valid = 0;
-  return -1;
-}
+// Float-float (FP32) or Neumaier (FP64) running sums for the fused reductions.
+template <typename T> struct RSum;
+template <> struct RSum<float> {
+  float hi, lo;
+  __device__ __forceinline__ void init() { hi = 0.f; lo = 0.f; }
+  __device__ __forceinline__ void add(float b) {  // TwoSum
+    float s = hi + b;
+    float bb = s - hi;
+    float e = (hi - (s - bb)) + (b - bb);
+    hi = s;
+    lo += e;
+  }
+  __device__ __forceinline__ double val() const { return (double)hi + (double)lo; }
+};
+template <> struct RSum<double> {
+  Acc a;
+  __device__ __forceinline__ void init() { a.init(); }
+  __device__ __forceinline__ void add(double b) { a.add(b); }
+  __device__ __forceinline__ double val() const { return a.val(); }
+};
 
-template <typename T>
-int launch_tiled(const TiledPlan& plan, int kind, const StageArgs<T>& a, cudaStream_t st, double* red, int red_cap,
-                 int* nblk_out) {
-  (void)plan; (void)kind; (void)a; (void)st; (void)red; (void)red_cap; (void)nblk_out;
-  return -1;
+template <typename T> constexpr int halo_z() { return sizeof(T) == 4 ? 4 : 3; }
+
+template <typename T, int TZ, int TY, int R> struct TileGeom {
+  static constexpr int HZ = halo_z<T>();
+  static constexpr int TZP = TZ + 2 * HZ;           // row pitch (complex)
+  static constexpr int ROWS = TY + 6;
+  static constexpr int SLOT_ELEMS = ROWS * TZP;
+  static constexpr int SLOT_BYTES = SLOT_ELEMS * (int)sizeof(c_t<T>);   // one TMA box
+  static constexpr int SLOT_STRIDE = (SLOT_BYTES + 127) / 128 * 128;     // 128-B aligned slots
+  static constexpr int SLOT_STRIDE_ELEMS = SLOT_STRIDE / (int)sizeof(c_t<T>);
+  static constexpr int NT = TZ * (TY / R);
+  static constexpr int S = 8;                       // ring slots
+  static constexpr int SMEM = S * SLOT_STRIDE + S * 8;
+};
+
+template <typename T, int TZ, int TY, int R, int KIND>
+__global__ void __launch_bounds__(TileGeom<T, TZ, TY, R>::NT, ((sizeof(T) == 4 && TileGeom<T, TZ, TY, R>::NT < 512) ? 2 : 1))
+stage_tiled_kernel(const __grid_constant__ CUtensorMap tm, TiledArgs<T> ta) {
+  using G = TileGeom<T, TZ, TY, R>;
+  using P = PK<T>;
+  using V = c_t<T>;
+  constexpr int HZ = G::HZ, TZP = G::TZP, S = G::S, NT = G::NT;
+  const StageArgs<T>& a = ta.s;
+
+  T scale;
+  if (stage_skip(a, &scale)) return;
+
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  V* ring = reinterpret_cast<V*>(smem_raw);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + S * G::SLOT_STRIDE);
+
+  const int tid = threadIdx.x;
+  const int lz = tid % TZ;
+  const int yg = tid / TZ;
+  const int nx = a.nx, ny = a.ny, nz = a.nz;
+
+  if (tid == 0) {
+    for (int s = 0; s < S; ++s) mbar_init(&bars[s], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+
+  // packed stencil coefficients with the 1/(180 h^2) and 1/(60 h) folded in
+  const V cx2 = splat<T>((T)2 * a.ix2), cx27 = splat<T>((T)(-27) * a.ix2), cx270 = splat<T>((T)270 * a.ix2);
+  const V cy2 = splat<T>((T)2 * a.iy2), cy27 = splat<T>((T)(-27) * a.iy2), cy270 = splat<T>((T)270 * a.iy2);
+  const V cz2 = splat<T>((T)2 * a.iz2), cz27 = splat<T>((T)(-27) * a.iz2), cz270 = splat<T>((T)270 * a.iz2);
+  const T c490 = (T)(-490) * (a.ix2 + a.iy2 + (a.two_dim ? (T)0 : a.iz2));
+  const V cx1 = splat<T>(a.ix1), cx9 = splat<T>((T)(-9) * a.ix1), cx45 = splat<T>((T)45 * a.ix1);
+  const V cy1 = splat<T>(a.iy1), cy9 = splat<T>((T)(-9) * a.iy1), cy45 = splat<T>((T)45 * a.iy1);
+  const V vscale = splat<T>(scale);
+
+  RSum<T> rN, rK, rP, rQ, rR, rA;
+  rN.init(); rK.init(); rP.init(); rQ.init(); rR.init(); rA.init();
+  double mx = 0.0, mn = 1.0e300, nf = 0.0;
+
+  const long long G0 = (long long)blockIdx.x * ta.units / gridDim.x;
+  const long long G1 = (long long)(blockIdx.x + 1) * ta.units / gridDim.x;
+  uint32_t seq = 0;       // load sequence number of the next plane to wait on
+  uint32_t seq_issue = 0; // next sequence number to issue (thread 0)
+  bool failed = false;
+
+  auto plane_src = [&](int p) -> int {  // x coordinate the TMA reads for plane p
+    if (p >= 0 && p < nx) return p;
+    if (a.bc == TRAPBEC_BC_ZERO) return p;  // out of range -> zero fill
+    return map_ghost(p, nx, a.bc);
+  };
+
+  for (long long u0 = G0; u0 < G1;) {
+    const int tile = (int)(u0 / nx);
+    const int xa = (int)(u0 % nx);
+    long long tile_end = (long long)(tile + 1) * nx;
+    const int xb = (int)((G1 < tile_end ? G1 : tile_end) - (long long)tile * nx);
+    u0 = (long long)tile * nx + xb;
+    const int z0 = (tile % ta.ntz) * TZ;
+    const int y0 = (tile / ta.ntz) * TY;
+    const int gz = z0 + lz;
+    const bool zok = gz < nz;
+    const bool bnd_y = ta.fix_y && (y0 == 0 || y0 + TY >= ny);
+    const bool bnd_z = ta.fix_z && (z0 == 0 || z0 + TZ >= nz);
+    const int plast = xb + 2;   // last plane of this segment
+    const uint32_t base = seq;  // sequence number of plane xa - 3
+
+    // per-thread constants of this tile
+    T pyv[R], yyv[R];
+    bool yok[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int gy = y0 + yg * R + r;
+      yok[r] = gy < ny;
+      pyv[r] = (yok[r] && a.pot_mode == POT_HARM) ? a.py[gy] : (T)0;
+      yyv[r] = yok[r] ? a.yy[gy] : (T)0;
+    }
+    const T pzv = (zok && a.pot_mode == POT_HARM) ? a.pz[gz] : (T)0;
+
+    // issue the first planes of the segment
+    if (tid == 0) {
+      seq_issue = base;
+      for (int p = xa - 3; p <= plast && p < xa - 3 + S; ++p) {
+        const uint32_t sq = seq_issue++;
+        const int sl = sq % S;
+        fence_proxy_async();
+        mbar_expect_tx(&bars[sl], G::SLOT_BYTES);
+        const int c0 = (int)(sizeof(T) == 4 ? (z0 - HZ) : 2 * (z0 - HZ));
+        tma_load_3d(ring + (size_t)sl * G::SLOT_STRIDE_ELEMS, &tm, c0, y0 - 3, plane_src(p), &bars[sl]);
+      }
+    }
+
+    auto wait_plane = [&](uint32_t sq) {
+      const int sl = sq % S;
+      const uint32_t par = (sq / S) & 1u;
+      uint32_t spins = 0;
+      while (!mbar_try_wait(&bars[sl], par)) {
+        if (++spins > WAIT_SPIN_LIMIT) {
+          failed = true;
+          atomicExch(ta.err, (int)TERR_WAIT_TIMEOUT);
+          break;
+        }
+      }
+    };
+
+    // Patch the y/z ghost cells of a boundary tile's slot from global memory
+    // (solid mirror or periodic wrap; zero where map_ghost says so).
+    auto fixup = [&](uint32_t sq, int p) {
+      if (!(bnd_y || bnd_z)) return;
+      V* sl = ring + (size_t)(sq % S) * G::SLOT_STRIDE_ELEMS;
+      const int xp = plane_src(p);
+      if (xp < 0 || xp >= nx) return;  // zero plane
+      const size_t plane = (size_t)xp * ny;
+      if (bnd_y) {
+        for (int e = tid; e < 6 * TZ; e += NT) {
+          const int rr = e / TZ, cz = e % TZ;
+          const int ry = rr < 3 ? rr - 3 : TY + rr - 3;
+          const int gy = y0 + ry, gzz = z0 + cz;
+          if ((gy >= 0 && gy < ny) || gzz >= nz) continue;
+          const int my = map_ghost(gy, ny, a.bc);
+          V v = mk<T>((T)0, (T)0);
+          if (my >= 0) v = a.psi_in[(plane + my) * nz + gzz];
+          sl[(ry + 3) * TZP + cz + HZ] = v;
+        }
+      }
+      if (bnd_z) {
+        for (int e = tid; e < 6 * TY; e += NT) {
+          const int ry = e / 6, m = e % 6;
+          const int cz = m < 3 ? m - 3 : TZ + m - 3;
+          const int gy = y0 + ry, gzz = z0 + cz;
+          if ((gzz >= 0 && gzz < nz) || gy >= ny) continue;
+          const int mz = map_ghost(gzz, nz, ta.bcz);
+          V v = mk<T>((T)0, (T)0);
+          if (mz >= 0) v = a.psi_in[(plane + gy) * nz + mz];
+          sl[(ry + 3) * TZP + cz + HZ] = v;
+        }
+      }
+    };
+
+    V q[7][R];
+    // prologue: planes xa-3 .. xa+2 -> q[0..5]
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+      const uint32_t sq = base + j;
+      wait_plane(sq);
+      if (j >= 3) fixup(sq, xa - 3 + j);
+      const V* sl = ring + (size_t)(sq % S) * G::SLOT_STRIDE_ELEMS;
+#pragma unroll
+      for (int r = 0; r < R; ++r) q[j][r] = sl[(yg * R + r + 3) * TZP + lz + HZ];
+    }
+    __syncthreads();
+    if (tid == 0) {
+      for (int j = 0; j < 3; ++j) {
+        const int p = xa - 3 + j + S;
+        if (p > plast) break;
+        const uint32_t sq = seq_issue++;
+        const int sl = sq % S;
+        fence_proxy_async();
+        mbar_expect_tx(&bars[sl], G::SLOT_BYTES);
+        const int c0 = (int)(sizeof(T) == 4 ? (z0 - HZ) : 2 * (z0 - HZ));
+        tma_load_3d(ring + (size_t)sl * G::SLOT_STRIDE_ELEMS, &tm, c0, y0 - 3, plane_src(p), &bars[sl]);
+      }
+    }
+
+    // one x-plane; OFF = (x - xa) mod 7 resolves the register queue at compile time
+    auto body = [&](auto offc, int x) {
+      constexpr int OFF = decltype(offc)::value;
+      const uint32_t sqx = base + (uint32_t)(x - xa) + 3;      // plane x
+      const uint32_t sq3 = sqx + 3;                             // plane x + 3
+      // prefetch w / potential of this plane
+      const size_t rowbase = ((size_t)x * ny + (y0 + yg * R)) * nz + gz;
+      V wv[R];
+      T tv[R];
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const bool ok = zok && yok[r];
+        const size_t idx = rowbase + (size_t)r * nz;
+        wv[r] = mk<T>((T)0, (T)0);
+        if ((KIND == ST_S2 || KIND == ST_S3) && ok) wv[r] = a.w[idx];
+        tv[r] = (a.pot_mode == POT_ARR && ok) ? a.trap[idx] : (T)0;
+      }
+      wait_plane(sq3);
+      fixup(sq3, x + 3);
+      {
+        const V* sl3 = ring + (size_t)(sq3 % S) * G::SLOT_STRIDE_ELEMS;
+#pragma unroll
+        for (int r = 0; r < R; ++r) q[(OFF + 6) % 7][r] = sl3[(yg * R + r + 3) * TZP + lz + HZ];
+      }
+      const V* sl = ring + (size_t)(sqx % S) * G::SLOT_STRIDE_ELEMS;
+      const V* col = sl + (yg * R + 3) * TZP + lz + HZ;  // row of the first cell
+      // y column: 3 ghost rows above, R centres (from the queue), 3 below
+      V yc[R + 6];
+#pragma unroll
+      for (int j = 0; j < 3; ++j) yc[j] = col[(j - 3) * TZP];
+#pragma unroll
+      for (int r = 0; r < R; ++r) yc[r + 3] = q[(OFF + 3) % 7][r];
+#pragma unroll
+      for (int j = 0; j < 3; ++j) yc[R + 3 + j] = col[(R + j) * TZP];
+      const T xv = a.xx[x];
+      const T pxv = a.pot_mode == POT_HARM ? a.px[x] : (T)0;
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const V craw = q[(OFF + 3) % 7][r];
+        // x line from the queue
+        const V xm3 = q[(OFF + 0) % 7][r], xm2 = q[(OFF + 1) % 7][r], xm1 = q[(OFF + 2) % 7][r];
+        const V xp1 = q[(OFF + 4) % 7][r], xp2 = q[(OFF + 5) % 7][r], xp3 = q[(OFF + 6) % 7][r];
+        const V ym3 = yc[r], ym2 = yc[r + 1], ym1 = yc[r + 2];
+        const V yp1 = yc[r + 4], yp2 = yc[r + 5], yp3 = yc[r + 6];
+        V lap = P::mul(splat<T>(c490), craw);
+        lap = P::fma(cx2, P::add(xm3, xp3), lap);
+        lap = P::fma(cx27, P::add(xm2, xp2), lap);
+        lap = P::fma(cx270, P::add(xm1, xp1), lap);
+        lap = P::fma(cy2, P::add(ym3, yp3), lap);
+        lap = P::fma(cy27, P::add(ym2, yp2), lap);
+        lap = P::fma(cy270, P::add(ym1, yp1), lap);
+        if (!a.two_dim) {
+          const V* zr = col + r * TZP;
+          const V zm3 = zr[-3], zm2 = zr[-2], zm1 = zr[-1];
+          const V zp1 = zr[1], zp2 = zr[2], zp3 = zr[3];
+          lap = P::fma(cz2, P::add(zm3, zp3), lap);
+          lap = P::fma(cz27, P::add(zm2, zp2), lap);
+          lap = P::fma(cz270, P::add(zm1, zp1), lap);
+        }
+        V fr = mk<T>((T)0, (T)0);
+        if (a.frame_mode != FRAME_NONE) {
+          V d1x = P::mul(cx1, P::sub(xp3, xm3));
+          d1x = P::fma(cx9, P::sub(xp2, xm2), d1x);
+          d1x = P::fma(cx45, P::sub(xp1, xm1), d1x);
+          V zc;
+          if (a.frame_mode == FRAME_ROT) {
+            V d1y = P::mul(cy1, P::sub(yp3, ym3));
+            d1y = P::fma(cy9, P::sub(yp2, ym2), d1y);
+            d1y = P::fma(cy45, P::sub(yp1, ym1), d1y);
+            // Z = x*D1y - y*D1x
+            zc = P::fma(splat<T>(-yyv[r]), d1x, P::mul(splat<T>(xv), d1y));
+          } else {
+            zc = d1x;
+          }
+          // (0, omega) * Z = (-omega Z.im, omega Z.re), on the renormalised state
+          const T os = a.omega * scale;
+          fr = mk<T>(-os * zc.y, os * zc.x);
+        }
+        // everything above is linear in psi: apply the load factor once
+        const V c = P::mul(vscale, craw);
+        lap = P::mul(vscale, lap);
+        T pot = (T)0;
+        if (a.pot_mode == POT_HARM) pot = pxv + pyv[r] + pzv;
+        else if (a.pot_mode == POT_ARR) pot = tv[r];
+        const T a2 = c.x * c.x + c.y * c.y;
+        const T rho = (T)1 - a2 - pot;
+        const V rhs = P::fma(splat<T>(rho), c, P::add(lap, fr));
+        // w = A w + c_f * rhs ; psi' = psi + B w  (run.f90:47-54)
+        V cr = P::mul(splat<T>(a.c_re), rhs);
+        cr = P::fma(mk<T>(-a.c_im, a.c_im), mk<T>(rhs.y, rhs.x), cr);
+        V wn, pn;
+        if (KIND == ST_EU) {
+          pn = P::add(c, cr);
+          wn = cr;
+        } else {
+          wn = (KIND == ST_S1) ? cr : P::fma(splat<T>(a.A), wv[r], cr);
+          pn = P::fma(splat<T>(a.B), wn, c);
+        }
+        const bool ok = zok && yok[r];
+        if (ok) {
+          const size_t idx = rowbase + (size_t)r * nz;
+          if (KIND == ST_S1 || KIND == ST_S2) a.w[idx] = wn;
+          if (KIND != ST_DIAG) a.psi_out[idx] = pn;
+          if (a.reduce == 1) rN.add(pn.x * pn.x + pn.y * pn.y);
+          if (KIND == ST_DIAG || a.reduce == 2) {
+            rN.add(a2);
+            rK.add(c.x * lap.x + c.y * lap.y);
+            rP.add(pot * a2);
+            rQ.add(a2 * a2);
+            rR.add(c.x * fr.x + c.y * fr.y);
+            const double am = sqrt((double)a2);
+            rA.add((T)am);
+            mx = fmax(mx, am);
+            mn = fmin(mn, am);
+            if (!isfinite(a2)) nf = 1.0;
+          }
+        }
+      }
+      __syncthreads();
+      if (tid == 0) {
+        const int p = x + S;
+        if (p <= plast) {
+          const uint32_t sq = seq_issue++;
+          const int slx = sq % S;
+          fence_proxy_async();
+          mbar_expect_tx(&bars[slx], G::SLOT_BYTES);
+          const int c0 = (int)(sizeof(T) == 4 ? (z0 - HZ) : 2 * (z0 - HZ));
+          tma_load_3d(ring + (size_t)slx * G::SLOT_STRIDE_ELEMS, &tm, c0, y0 - 3, plane_src(p), &bars[slx]);
+        }
+      }
+    };
+
+    int x = xa;
+    for (; x + 7 <= xb; x += 7) {
+      body(std::integral_constant<int, 0>{}, x);
+      body(std::integral_constant<int, 1>{}, x + 1);
+      body(std::integral_constant<int, 2>{}, x + 2);
+      body(std::integral_constant<int, 3>{}, x + 3);
+      body(std::integral_constant<int, 4>{}, x + 4);
+      body(std::integral_constant<int, 5>{}, x + 5);
+      body(std::integral_constant<int, 6>{}, x + 6);
+    }
+    if (x < xb) body(std::integral_constant<int, 0>{}, x);
+    if (x + 1 < xb) body(std::integral_constant<int, 1>{}, x + 1);
+    if (x + 2 < xb) body(std::integral_constant<int, 2>{}, x + 2);
+    if (x + 3 < xb) body(std::integral_constant<int, 3>{}, x + 3);
+    if (x + 4 < xb) body(std::integral_constant<int, 4>{}, x + 4);
+    if (x + 5 < xb) body(std::integral_constant<int, 5>{}, x + 5);
+    seq = base + (uint32_t)(xb - xa) + 6;
+    failed = __syncthreads_or(failed) != 0;
+    if (failed) break;
+  }
+
+  if (a.red != nullptr) {
+    double acc[NRED];
+    acc[0] = rN.val(); acc[1] = rK.val(); acc[2] = rP.val(); acc[3] = rQ.val();
+    acc[4] = rR.val(); acc[5] = rA.val(); acc[6] = mx; acc[7] = mn; acc[8] = nf;
+    block_reduce_store<NT>(acc, a.red, blockIdx.x, gridDim.x);
+  }
 }
 
 }  // namespace tb

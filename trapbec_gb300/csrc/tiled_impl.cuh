@@ -1,0 +1,115 @@
+// tiled_impl.cuh -- plan and launch of the tiled stage kernel, instantiated
+// per precision by tiled_f32.cu and tiled_f64.cu.
+#pragma once
+#include <cudaTypedefs.h>
+
+#include <cstring>
+
+#include "kernels_tiled.cuh"
+
+namespace tb {
+
+inline PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (PFN_cuTensorMapEncodeTiled_v12000)f;
+  }
+  return fn;
+}
+
+template <typename T, int TZ, int TY, int R>
+int plan_shape(const trapbec_params& p, void* const psi[2], int nsm, int* err_flag, TiledPlan* plan) {
+  using G = TileGeom<T, TZ, TY, R>;
+  if (p.two_dim || p.nx < 4 || p.ny < 4 || p.nz < 8) return 1;
+  if (sizeof(T) == 4 && (p.nz % 2)) return 1;  // TMA strides must be multiples of 16 bytes
+  const int bcz = (p.periodicz || p.boundaries == TRAPBEC_BC_PERIODIC) ? TRAPBEC_BC_PERIODIC : p.boundaries;
+  const int fix_y = p.boundaries != TRAPBEC_BC_ZERO;
+  const int fix_z = bcz != TRAPBEC_BC_ZERO;
+  // ghost fix-ups address the tile edges: partial tiles only with zero ghosts
+  if (fix_y && (p.ny % TY)) return 1;
+  if (fix_z && (p.nz % TZ)) return 1;
+  auto enc = tensor_map_encoder();
+  if (!enc) return 2;
+  TiledPlan q;
+  for (int b = 0; b < 2; ++b) {
+    cuuint64_t dims[3], strides[2];
+    cuuint32_t box[3], es[3] = {1, 1, 1};
+    if (sizeof(T) == 4) {  // one 8-byte element = one complex float
+      dims[0] = (cuuint64_t)p.nz;
+      box[0] = G::TZP;
+    } else {               // complex double as two doubles
+      dims[0] = (cuuint64_t)p.nz * 2;
+      box[0] = 2 * G::TZP;
+    }
+    dims[1] = (cuuint64_t)p.ny;
+    dims[2] = (cuuint64_t)p.nx;
+    strides[0] = (cuuint64_t)p.nz * sizeof(c_t<T>);
+    strides[1] = (cuuint64_t)p.ny * p.nz * sizeof(c_t<T>);
+    box[1] = G::ROWS;
+    box[2] = 1;
+    CUresult r = enc(&q.tm[b], CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, psi[b], dims, strides, box, es,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return 3;
+    q.psi_base[b] = psi[b];
+  }
+  auto k1 = stage_tiled_kernel<T, TZ, TY, R, ST_S1>;
+  auto k2 = stage_tiled_kernel<T, TZ, TY, R, ST_S2>;
+  auto k3 = stage_tiled_kernel<T, TZ, TY, R, ST_S3>;
+  auto k4 = stage_tiled_kernel<T, TZ, TY, R, ST_EU>;
+  auto k5 = stage_tiled_kernel<T, TZ, TY, R, ST_DIAG>;
+  for (auto k : {k1, k2, k3, k4, k5})
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM) != cudaSuccess) return 4;
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k2, G::NT, G::SMEM) != cudaSuccess || nb < 1) return 5;
+  q.ntz = (p.nz + TZ - 1) / TZ;
+  q.nty = (p.ny + TY - 1) / TY;
+  q.units = (long long)q.ntz * q.nty * p.nx;
+  long long g = (long long)nb * nsm;
+  q.grid = (int)(g < q.units ? g : q.units);
+  q.smem = G::SMEM;
+  q.nt = G::NT;
+  q.tz = TZ; q.ty = TY; q.r = R;
+  q.fix_y = fix_y; q.fix_z = fix_z; q.bcz = bcz;
+  q.err = err_flag;
+  q.valid = 1;
+  *plan = q;
+  return 0;
+}
+
+template <typename T, int TZ, int TY, int R>
+int launch_shape(const TiledPlan& plan, int kind, const StageArgs<T>& a, cudaStream_t st, int red_cap, int* nblk) {
+  using G = TileGeom<T, TZ, TY, R>;
+  TiledArgs<T> ta;
+  ta.s = a;
+  ta.ntz = plan.ntz;
+  ta.nty = plan.nty;
+  ta.units = plan.units;
+  ta.err = plan.err;
+  ta.bcz = plan.bcz;
+  ta.fix_y = plan.fix_y;
+  ta.fix_z = plan.fix_z;
+  const CUtensorMap* tm = nullptr;
+  if ((const void*)a.psi_in == plan.psi_base[0]) tm = &plan.tm[0];
+  else if ((const void*)a.psi_in == plan.psi_base[1]) tm = &plan.tm[1];
+  if (!tm) return 6;
+  int grid = plan.grid;
+  if (a.red && grid > red_cap) grid = red_cap;
+  switch (kind) {
+    case ST_S1: stage_tiled_kernel<T, TZ, TY, R, ST_S1><<<grid, G::NT, G::SMEM, st>>>(*tm, ta); break;
+    case ST_S2: stage_tiled_kernel<T, TZ, TY, R, ST_S2><<<grid, G::NT, G::SMEM, st>>>(*tm, ta); break;
+    case ST_S3: stage_tiled_kernel<T, TZ, TY, R, ST_S3><<<grid, G::NT, G::SMEM, st>>>(*tm, ta); break;
+    case ST_EU: stage_tiled_kernel<T, TZ, TY, R, ST_EU><<<grid, G::NT, G::SMEM, st>>>(*tm, ta); break;
+    case ST_DIAG: stage_tiled_kernel<T, TZ, TY, R, ST_DIAG><<<grid, G::NT, G::SMEM, st>>>(*tm, ta); break;
+    default: return 7;
+  }
+  if (nblk) *nblk = grid;
+  return cudaGetLastError() == cudaSuccess ? 0 : 8;
+}
+
+}  // namespace tb

@@ -24,7 +24,7 @@
 #include "host_util.h"
 #include "kernels_init.cuh"
 #include "kernels_simple.cuh"
-#include "kernels_tiled.cuh"
+#include "tiled_api.h"
 #include "imag_ctrl.cuh"
 
 using namespace tb;
@@ -90,6 +90,9 @@ struct trapbec_ctx {
   std::vector<double> hxx, hyy, hzz;   // coordinates as double (exact copies of T values)
   TiledPlan plan;                      // tiled-kernel plan (tensor maps, tile shape)
   bool plan_valid = false;
+  int shape = 0;                       // tiled-kernel shape index
+  int* d_err = nullptr;                // device error flag of the tiled kernel
+  int* h_err = nullptr;                // pinned copy
 };
 
 namespace {
@@ -224,12 +227,27 @@ template <typename T> bool use_tiled(trapbec_ctx* c) {
   return c->plan_valid;
 }
 
+// Read and clear the device error flag of the tiled kernel.
+int check_device_error(trapbec_ctx* c) {
+  CK(cudaMemcpyAsync(c->h_err, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  if (*c->h_err != 0) {
+    int code = *c->h_err;
+    *c->h_err = 0;
+    CK(cudaMemsetAsync(c->d_err, 0, sizeof(int), c->st));
+    CK(cudaStreamSynchronize(c->st));
+    set_error("device-side wait timed out in the tiled stage kernel (code " + std::to_string(code) + ")");
+    return TRAPBEC_ERR_TIMEOUT;
+  }
+  return TRAPBEC_OK;
+}
+
 // Launch one stage.  kind: StageKind or 4 (diagnostics).  Returns status.
 template <typename T>
 int launch_stage(trapbec_ctx* c, int kind, StageArgs<T>& a, int* nblk_out) {
-  if (use_tiled<T>(c) && kind != 4) {
-    int rc = launch_tiled<T>(c->plan, kind, a, c->st, c->red, c->red_cap, nblk_out);
-    if (rc) { set_error("tiled stage launch failed"); return rc; }
+  if (use_tiled<T>(c)) {
+    int rc = launch_tiled<T>(c->plan, kind, a, c->st, c->red_cap, nblk_out);
+    if (rc) { set_error("tiled stage launch failed (" + std::to_string(rc) + ")"); return TRAPBEC_ERR_CUDA; }
     CKL();
     c->launches++;
     return TRAPBEC_OK;
@@ -347,7 +365,7 @@ template <typename T> int do_step_rt(trapbec_ctx* c, int nsteps) {
   float ms = 0;
   CK(cudaEventElapsedTime(&ms, c->e0, c->e1));
   c->last_ms = ms;
-  return TRAPBEC_OK;
+  return check_device_error(c);
 }
 
 template <typename T> int do_imag_euler(trapbec_ctx* c, int nsteps, int* steps_done, double* ratio) {
@@ -577,18 +595,23 @@ template <typename T> int create_impl(trapbec_ctx* c) {
   CK(cudaMalloc(&c->ctrl, sizeof(ImagCtrl)));
   CK(cudaMallocHost(&c->host_ctrl, sizeof(ImagCtrl)));
   CK(cudaMemsetAsync(c->ctrl, 0, sizeof(ImagCtrl), c->st));
+  CK(cudaMalloc(&c->d_err, sizeof(int)));
+  CK(cudaMallocHost(&c->h_err, sizeof(int)));
+  CK(cudaMemsetAsync(c->d_err, 0, sizeof(int), c->st));
+  *c->h_err = 0;
   int rc = setup_tables<T>(c);
   if (rc) return rc;
-  c->plan_valid = (plan_tiled<T>(c->p, c->xx, c->psi, c->w, c->nsm, c->tile_z, c->tile_y, &c->plan) == 0);
+  c->plan_valid = (plan_tiled<T>(c->p, c->psi, c->nsm, 0, c->d_err, &c->plan) == 0);
   return TRAPBEC_OK;
 }
 
 void free_ctx(trapbec_ctx* c) {
   if (!c) return;
   void* bufs[] = {c->psi[0], c->psi[1], c->w, c->xx, c->yy, c->zz, c->px, c->py, c->pz,
-                  c->trap_user, c->trap_eff, c->red, c->red_out, c->ctrl};
+                  c->trap_user, c->trap_eff, c->red, c->red_out, c->ctrl, c->d_err};
   for (void* b : bufs) if (b) cudaFree(b);
   if (c->host_red) cudaFreeHost(c->host_red);
+  if (c->h_err) cudaFreeHost(c->h_err);
   if (c->host_ctrl) cudaFreeHost(c->host_ctrl);
   if (c->e0) cudaEventDestroy(c->e0);
   if (c->e1) cudaEventDestroy(c->e1);
@@ -914,12 +937,25 @@ int trapbec_set_kernel(trapbec_ctx* c, int kind, int tile_z, int tile_y) {
   if (!c || kind < 0 || kind > 2) return TRAPBEC_ERR_ARG;
   c->kernel_kind = kind;
   if (kind == 1) return TRAPBEC_OK;
-  if (tile_z != c->tile_z || tile_y != c->tile_y || !c->plan_valid) {
+  int shape = 0;
+  if (tile_z || tile_y) {
+    shape = -1;
+    int ns = c->prec == TRAPBEC_FP64 ? tiled_nshapes<double>() : tiled_nshapes<float>();
+    for (int i = 0; i < ns; ++i) {
+      Shape sh = c->prec == TRAPBEC_FP64 ? tiled_shape<double>(i) : tiled_shape<float>(i);
+      if (sh.tz == tile_z && sh.ty == tile_y) shape = i;
+    }
+    if (shape < 0) {
+      set_error("no tiled kernel is built for this tile shape");
+      return TRAPBEC_ERR_UNSUPPORTED;
+    }
+  }
+  if (shape != c->shape || !c->plan_valid) {
+    c->shape = shape;
     c->tile_z = tile_z;
     c->tile_y = tile_y;
-    int rc = c->prec == TRAPBEC_FP64
-                 ? plan_tiled<double>(c->p, c->xx, c->psi, c->w, c->nsm, tile_z, tile_y, &c->plan)
-                 : plan_tiled<float>(c->p, c->xx, c->psi, c->w, c->nsm, tile_z, tile_y, &c->plan);
+    int rc = c->prec == TRAPBEC_FP64 ? plan_tiled<double>(c->p, c->psi, c->nsm, shape, c->d_err, &c->plan)
+                                     : plan_tiled<float>(c->p, c->psi, c->nsm, shape, c->d_err, &c->plan);
     c->plan_valid = (rc == 0);
   }
   if (kind == 2 && !c->plan_valid) {
