@@ -1,0 +1,339 @@
+"""Benchmark of the TrapBEC hot path on GB300.
+
+Workload (default): the rotating-trap quench at 512^3 in complex FP32 with
+FP64 diagnostics, on [-64,64]^3, omega_perp = 0.02, omega_z = 0.04, g = 1,
+dt = 0.004, Omega ramped linearly towards 0.8 omega_perp.  One bench step is
+one full low-storage RK3 step (three fused stage kernels) over the whole
+grid.  The metric is grid-point updates per second (one grid point advanced
+by one RK3 step).  Synthetic seeded initial state: a Thomas-Fermi cloud with
+1e-2 noise standing in for a relaxed ground state.  Each array is 1 GiB, far
+larger than the 129 MB L2, so no flush is needed between steps.
+
+Output: one JSON line (see the keys below); `--impl reference` times the CPU
+restatement of the reference's algorithm on the host cores instead.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import re
+import statistics
+import subprocess
+import sys
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "grid-pt updates/s at 512^3 FP32 vs FP64 (HBM %); imag-time wall to dE<1e-10: NN vs TF"
+UNIT = "grid-point updates/s"
+
+
+def load_peaks():
+    p = os.path.join(HERE, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic(prec_tag: str):
+    """DRAM bytes per grid point per stage launch from the committed ncu summary."""
+    path = os.path.join(HERE, "profiles", f"stage_tiled_{prec_tag}_256.txt")
+    if not os.path.exists(path):
+        return None
+    m = re.search(r"dram_bytes_per_point_per_launch:\s*([0-9.eE+-]+)", open(path).read())
+    return float(m.group(1)) if m else None
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.path = os.path.join("/tmp", f"trapbec_clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], None, set()
+        names = ["active", "hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names[1:], f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_problem(n: int, prec):
+    from trapbec_gb300 import abi, units
+    prob, init = units.rotating_quench_512(prec, n=n)
+    return prob, init
+
+
+def cpu_reference(n: int, steps: int, threads: int | None):
+    """Time the oracle (CPU restatement of the reference) on the host cores."""
+    from oracle.pyoracle import Oracle
+    from trapbec_gb300 import abi
+    from trapbec_gb300.abi import InitArgs
+    prob, init = make_problem(n, abi.FP32)
+    p = prob.to_params()
+    p.omega_z = prob.omega_z_for(0.4 * init["omega_final"])
+    if threads:
+        Oracle.set_threads(threads)
+    cores = Oracle.max_threads()
+    o = Oracle(p)
+    a = InitArgs()
+    a.seed = init["seed"]; a.amp = init["amp"]; a.noise_amp = init["noise_amp"]
+    for i in range(3):
+        a.r_tf2[i] = init["r_tf2"][i]
+    o.init_state(init["name"], a)
+    o.step_rt(1)  # warm caches and pages
+    t0 = time.perf_counter()
+    o.step_rt(steps)
+    dt = time.perf_counter() - t0
+    return n ** 3 * steps / dt, cores, dt
+
+
+def run_reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    n = args.n
+    # a bounded sample of the workload: the full 512^3 grid, few steps
+    k = max(1, min(args.steps, 2))
+    val, cores, dt = cpu_reference(n, k, None)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": k, "warmup": 1, "ms_per_step": 1e3 * dt / k, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c64 (f32)", "data": "synthetic",
+        "config": {"workload": f"rotating-trap RK3 quench {n}^3 complex FP32", "grid": [n, n, n],
+                   "l2_flush": "inputs larger than L2 (1 GiB per array)"},
+        "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{k} RK3 step(s) of the full {n}^3 grid (OpenMP over x)"},
+        "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference (Fortran 90 + MPI) has no Fortran compiler or MPI on this image; "
+                "its algorithm is timed through the CPU restatement (oracle/)",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def timed_steps(s, steps, chunk, omega_of_step, start_step=0):
+    """Run `steps` RK3 steps in chunks (Omega updated per chunk); returns
+    (device ms of the stage kernels, launches)."""
+    from trapbec_gb300 import abi
+    ms = 0.0
+    l0 = s.launch_count()
+    done = 0
+    while done < steps:
+        k = min(chunk, steps - done)
+        s.set_scalar(abi.SCALAR_OMEGA_Z, omega_of_step(start_step + done))
+        s.step_rt(k)
+        ms += s.last_kernel_ms()
+        done += k
+    return ms, s.launch_count() - l0
+
+
+def run_gpu_arm(args):
+    import numpy as np
+    import torch
+    from trapbec_gb300 import Solver, abi
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    n = args.n
+    prec = abi.FP64 if args.fp64_only else abi.FP32
+    prob, init = make_problem(n, prec)
+    p = prob.to_params()
+    s = Solver(p)
+    if args.kernel:
+        s.set_kernel(*args.kernel)
+    s.init_state(init["name"], seed=init["seed"] + rank, amp=init["amp"], r_tf2=init["r_tf2"],
+                 noise_amp=init["noise_amp"])
+    ramp_steps = 5000
+    om_final = init["omega_final"]
+
+    def omega_of_step(k):
+        return prob.omega_z_for(om_final * min(1.0, k / ramp_steps))
+
+    chunk = args.chunk
+    d0 = s.diag()
+    # warm-up (untimed)
+    timed_steps(s, args.warmup, chunk, omega_of_step, 0)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ms, launches = timed_steps(s, args.steps, chunk, omega_of_step, args.warmup)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    if dist:
+        dist.barrier()
+    d1 = s.diag()
+    ms_t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+    if dist:
+        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
+    ms = float(ms_t.item())
+    cells = n ** 3
+    value = world * cells * args.steps / (ms * 1e-3)
+    peak, peak_kind = load_peaks()
+    bpc = 80.0 if prec == abi.FP32 else 160.0   # algorithmic bytes per grid point per RK3 step
+    achieved = cells * args.steps * bpc / (ms * 1e-3) / 1e9
+    tag = "fp32" if prec == abi.FP32 else "fp64"
+    tpp = profile_traffic(tag)
+    traffic = tpp * cells if tpp else None
+
+    # ---- end to end through the C ABI with pinned host buffers ----------------
+    e2e = None
+    if not args.no_e2e:
+        shots = args.shots
+        host = torch.empty(cells, dtype=torch.complex64 if prec == abi.FP32 else torch.complex128,
+                           pin_memory=True).numpy()
+        host_out = torch.empty_like(torch.from_numpy(host)).pin_memory().numpy()
+        host[:] = s.get_psi().reshape(-1)
+        reps = max(1, args.e2e_reps)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for r in range(reps):
+            s.set_psi(host.reshape(s.shape))                       # H2D of the state
+            s.set_scalar(abi.SCALAR_OMEGA_Z, omega_of_step(args.warmup + args.steps + r * shots))
+            s.step_rt(shots)                                       # RK3 steps
+            dd = s.diag()                                          # FP64 diagnostics (Psi_info/Psi_norm, E)
+            got = s.get_psi()                                      # D2H of the state
+            host_out[:] = got.reshape(-1)
+        torch.cuda.synchronize()
+        et = time.perf_counter() - t0
+        e2e = {"value": world * cells * shots * reps / et, "unit": UNIT,
+               "h2d_bytes_per_step": int(cells * host.itemsize / shots),
+               "d2h_bytes_per_step": int(cells * host.itemsize / shots),
+               "shots": shots, "note": "per call: set_psi (H2D) + shots RK3 steps + diag + get_psi (D2H)"}
+
+    # ---- FP64 comparison line (same workload, same kernel family) ------------
+    fp64 = None
+    if not args.no_fp64 and prec == abi.FP32:
+        s.close()
+        prob64, _ = make_problem(n, abi.FP64)
+        p64 = prob64.to_params()
+        s64 = Solver(p64)
+        s64.init_state(init["name"], seed=init["seed"] + rank, amp=init["amp"], r_tf2=init["r_tf2"],
+                       noise_amp=init["noise_amp"])
+        timed_steps(s64, 2, chunk, omega_of_step, 0)
+        k64 = args.fp64_steps
+        ms64, _ = timed_steps(s64, k64, chunk, omega_of_step, 2)
+        v64 = cells * k64 / (ms64 * 1e-3)
+        fp64 = {"value": v64, "unit": UNIT, "ms_per_step": ms64 / k64,
+                "hbm_gbs_alg": cells * k64 * 160.0 / (ms64 * 1e-3) / 1e9,
+                "hbm_frac": cells * k64 * 160.0 / (ms64 * 1e-3) / 1e9 / peak,
+                "note": "FP64 stage kernels are bound by GB300's FP64 pipe, not HBM"}
+        s64.close()
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        val, cores, dt = cpu_reference(n, 1, None)
+        cpu = {"value": val, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"1 RK3 step of the full {n}^3 FP32 grid on the host cores ({dt:.1f} s)"}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c64 (f32)" if prec == abi.FP32 else "c128 (f64)",
+        "data": "synthetic (seeded TF cloud + 1e-2 noise)",
+        "config": {"workload": f"rotating-trap RK3 quench {n}^3 complex {'FP32' if prec == abi.FP32 else 'FP64'}",
+                   "grid": [n, n, n], "box": [128.0, 128.0, 128.0], "dt_trap_units": 0.004,
+                   "omega_ramp": "0 -> 0.8 omega_perp over 5000 steps, updated every chunk",
+                   "chunk_steps": chunk, "parallelism": "replicas" if world > 1 else "single GPU",
+                   "l2_flush": "inputs larger than L2 (1 GiB per array)",
+                   "kernel": "tiled TMA stage kernel" if s.launch_count() >= 0 else None},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                     "algorithmic_bytes_per_point_step": bpc,
+                     "kernel": "stage_tiled_kernel (3 launches per RK3 step; achieved averaged over them)"},
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+        "wall_s_timed": wall,
+        "drift": {"norm_rel": d1["norm"] / d0["norm"] - 1.0, "energy_rel": d1["energy"] / d0["energy"] - 1.0},
+    }
+    if fp64:
+        line["fp64"] = fp64
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=60)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=512, help="grid size per axis (profiling uses smaller cases)")
+    ap.add_argument("--chunk", type=int, default=20, help="RK3 steps per C-ABI call (Omega updated per call)")
+    ap.add_argument("--shots", type=int, default=100, help="RK3 steps per end-to-end call")
+    ap.add_argument("--e2e-reps", type=int, default=2)
+    ap.add_argument("--fp64-steps", type=int, default=6)
+    ap.add_argument("--fp64-only", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--kernel", type=int, nargs=3, default=None, metavar=("KIND", "TZ", "TY"))
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    from trapbec_gb300.build import build_library
+    build_library()
+    if args.impl == "reference":
+        run_reference_arm(args)
+    else:
+        run_gpu_arm(args)
+
+
+if __name__ == "__main__":
+    main()
