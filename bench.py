@@ -228,6 +228,8 @@ def run_gpu_arm(args):
     tpp = profile_traffic(tag)
     traffic = tpp * cells if tpp else None
 
+    kernel_name = "tiled TMA stage kernel" if args.kernel is None or args.kernel[0] != 1 else "per-cell stage kernel"
+
     # ---- end to end through the C ABI with pinned host buffers ----------------
     e2e = None
     if not args.no_e2e:
@@ -288,7 +290,7 @@ def run_gpu_arm(args):
                    "omega_ramp": "0 -> 0.8 omega_perp over 5000 steps, updated every chunk",
                    "chunk_steps": chunk, "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2_flush": "inputs larger than L2 (1 GiB per array)",
-                   "kernel": "tiled TMA stage kernel" if s.launch_count() >= 0 else None},
+                   "kernel": kernel_name},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                      "algorithmic_bytes_per_point_step": bpc,
