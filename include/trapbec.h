@@ -219,6 +219,18 @@ int trapbec_get_scalar(trapbec_ctx* ctx, int which, double* value);
  * grid does not allow it).  tile_z/tile_y = 0 lets the autotuner choose.   */
 int trapbec_set_kernel(trapbec_ctx* ctx, int kind, int tile_z, int tile_y);
 
+/* Work order of the tiled kernel: x-planes per chunk (0 = automatic).  Tiles
+ * adjacent in y are processed chunk by chunk so their shared ghost rows are
+ * served from L2.                                                          */
+int trapbec_set_chunk(trapbec_ctx* ctx, int chunk);
+
+/* Autotune the tiled kernel for this grid: time every built tile shape and a
+ * few chunk lengths over `steps` RK3 steps each on the current state (which
+ * is saved and restored), keep the fastest.  *tile_z, *tile_y, *chunk (may
+ * be NULL) receive the choice, *ms_per_step its time.  Results are cached
+ * per process for identical grids.                                         */
+int trapbec_autotune(trapbec_ctx* ctx, int steps, int* tile_z, int* tile_y, int* chunk, double* ms_per_step);
+
 /* Kernels launched by this context since creation (for launch accounting). */
 int trapbec_launch_count(trapbec_ctx* ctx, int64_t* count);
 

@@ -135,6 +135,9 @@ _PROTOS = {
     "trapbec_set_scalar": (C.c_int, [_VP, C.c_int, C.c_double]),
     "trapbec_get_scalar": (C.c_int, [_VP, C.c_int, C.POINTER(C.c_double)]),
     "trapbec_set_kernel": (C.c_int, [_VP, C.c_int, C.c_int, C.c_int]),
+    "trapbec_set_chunk": (C.c_int, [_VP, C.c_int]),
+    "trapbec_autotune": (C.c_int, [_VP, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                   C.POINTER(C.c_double)]),
     "trapbec_launch_count": (C.c_int, [_VP, C.POINTER(C.c_int64)]),
     "trapbec_last_kernel_ms": (C.c_int, [_VP, C.POINTER(C.c_double)]),
     "trapbec_write_var": (C.c_int, [_VP, C.c_char_p, C.c_int, C.c_int, C.c_double, C.c_int]),

@@ -31,42 +31,25 @@
 namespace tb {
 
 // ----------------------------------------------------- packed complex ops --
+// FP32 complex values are float2 register pairs operated on with Blackwell's
+// packed FFMA2/FADD2/FMUL2 (CUDA builtins); FP64 uses scalar pairs.
 template <typename T> struct PK;
 template <> struct PK<float> {
   using V = float2;
-  static __device__ __forceinline__ unsigned long long u(V a) { return *reinterpret_cast<unsigned long long*>(&a); }
-  static __device__ __forceinline__ V v(unsigned long long a) { return *reinterpret_cast<V*>(&a); }
-  static __device__ __forceinline__ V add(V a, V b) {
-    unsigned long long r;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(u(a)), "l"(u(b)));
-    return v(r);
-  }
-  static __device__ __forceinline__ V sub(V a, V b) {
-    unsigned long long r;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(u(a)), "l"(u(b)));
-    return v(r);
-  }
-  static __device__ __forceinline__ V mul(V a, V b) {
-    unsigned long long r;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(u(a)), "l"(u(b)));
-    return v(r);
-  }
-  static __device__ __forceinline__ V fma(V a, V b, V c) {
-    unsigned long long r;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(u(a)), "l"(u(b)), "l"(u(c)));
-    return v(r);
-  }
+  static __device__ __forceinline__ V add(V a, V b) { return __fadd2_rn(a, b); }
+  static __device__ __forceinline__ V mul(V a, V b) { return __fmul2_rn(a, b); }
+  static __device__ __forceinline__ V fma(V a, V b, V c) { return __ffma2_rn(a, b, c); }
 };
 template <> struct PK<double> {
   using V = double2;
   static __device__ __forceinline__ V add(V a, V b) { return make_double2(a.x + b.x, a.y + b.y); }
-  static __device__ __forceinline__ V sub(V a, V b) { return make_double2(a.x - b.x, a.y - b.y); }
   static __device__ __forceinline__ V mul(V a, V b) { return make_double2(a.x * b.x, a.y * b.y); }
   static __device__ __forceinline__ V fma(V a, V b, V c) {
     return make_double2(::fma(a.x, b.x, c.x), ::fma(a.y, b.y, c.y));
   }
 };
 template <typename T> __device__ __forceinline__ c_t<T> splat(T s) { return mk<T>(s, s); }
+template <typename T> __device__ __forceinline__ T neg(T v) { v.x = -v.x; v.y = -v.y; return v; }
 
 // ------------------------------------------------------------- mbarrier --
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -106,6 +89,12 @@ template <typename T> struct TiledArgs {
   int* err;                // error flag (device)
   int bcz;                 // boundary type along z (periodic if zper)
   int fix_y, fix_z;        // ghost fix-up needed on y / z boundary tiles
+  int chunk;               // x-chunk length of the work order
+  // Packed coefficients, formed on the host so the kernel can take them from
+  // the parameter (constant) bank instead of holding them in registers:
+  // 0-2: (2,-27,270)/(180 hx^2), 3-5: y, 6-8: z, 9: -490*sum(1/(180 h^2)),
+  // 10: -9, 11: 45, 12: (c_re, c_re), 13: (-c_im, c_im), 14: (A, A), 15: (B, B)
+  c_t<T> k[16];
 };
 
 // Float-float (FP32) or Neumaier (FP64) running sums for the fused reductions.
@@ -164,6 +153,7 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm, TiledArgs<T> ta) {
   const int lz = tid % TZ;
   const int yg = tid / TZ;
   const int nx = a.nx, ny = a.ny, nz = a.nz;
+  const int L = ta.chunk;
 
   if (tid == 0) {
     for (int s = 0; s < S; ++s) mbar_init(&bars[s], 1);
@@ -171,14 +161,8 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm, TiledArgs<T> ta) {
   }
   __syncthreads();
 
-  // packed stencil coefficients with the 1/(180 h^2) and 1/(60 h) folded in
-  const V cx2 = splat<T>((T)2 * a.ix2), cx27 = splat<T>((T)(-27) * a.ix2), cx270 = splat<T>((T)270 * a.ix2);
-  const V cy2 = splat<T>((T)2 * a.iy2), cy27 = splat<T>((T)(-27) * a.iy2), cy270 = splat<T>((T)270 * a.iy2);
-  const V cz2 = splat<T>((T)2 * a.iz2), cz27 = splat<T>((T)(-27) * a.iz2), cz270 = splat<T>((T)270 * a.iz2);
-  const T c490 = (T)(-490) * (a.ix2 + a.iy2 + (a.two_dim ? (T)0 : a.iz2));
-  const V cx1 = splat<T>(a.ix1), cx9 = splat<T>((T)(-9) * a.ix1), cx45 = splat<T>((T)45 * a.ix1);
-  const V cy1 = splat<T>(a.iy1), cy9 = splat<T>((T)(-9) * a.iy1), cy45 = splat<T>((T)45 * a.iy1);
   const V vscale = splat<T>(scale);
+  const T oms = a.omega * scale;
 
   RSum<T> rN, rK, rP, rQ, rR, rA;
   rN.init(); rK.init(); rP.init(); rQ.init(); rR.init(); rA.init();
@@ -186,7 +170,7 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm, TiledArgs<T> ta) {
 
   const long long G0 = (long long)blockIdx.x * ta.units / gridDim.x;
   const long long G1 = (long long)(blockIdx.x + 1) * ta.units / gridDim.x;
-  uint32_t seq = 0;       // load sequence number of the next plane to wait on
+  uint32_t seq = 0;       // load sequence number of the first plane of a segment
   uint32_t seq_issue = 0; // next sequence number to issue (thread 0)
   bool failed = false;
 
@@ -196,44 +180,54 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm, TiledArgs<T> ta) {
     return map_ghost(p, nx, a.bc);
   };
 
+  // Work units are ordered (z-tile, x-chunk, y-tile, x): consecutive units
+  // stream x inside one chunk of L planes, then move to the y-neighbour tile,
+  // so the y ghost rows of a tile were fetched by its neighbour shortly before
+  // and are served from L2.
+  const long long per_tz = (long long)ta.nty * nx;
   for (long long u0 = G0; u0 < G1;) {
-    const int tile = (int)(u0 / nx);
-    const int xa = (int)(u0 % nx);
-    long long tile_end = (long long)(tile + 1) * nx;
-    const int xb = (int)((G1 < tile_end ? G1 : tile_end) - (long long)tile * nx);
-    u0 = (long long)tile * nx + xb;
-    const int z0 = (tile % ta.ntz) * TZ;
-    const int y0 = (tile / ta.ntz) * TY;
+    const int tzi = (int)(u0 / per_tz);
+    const long long rr0 = u0 - (long long)tzi * per_tz;
+    const int xc = (int)(rr0 / ((long long)ta.nty * L));
+    const long long rr1 = rr0 - (long long)xc * ta.nty * L;
+    const int Lc = min(L, nx - xc * L);
+    const int tyi = (int)(rr1 / Lc);
+    const int xa = xc * L + (int)(rr1 - (long long)tyi * Lc);
+    int xb = xc * L + Lc;
+    if (u0 + (xb - xa) > G1) xb = xa + (int)(G1 - u0);
+    u0 += xb - xa;
+    const int z0 = tzi * TZ;
+    const int y0 = tyi * TY;
     const int gz = z0 + lz;
     const bool zok = gz < nz;
     const bool bnd_y = ta.fix_y && (y0 == 0 || y0 + TY >= ny);
     const bool bnd_z = ta.fix_z && (z0 == 0 || z0 + TZ >= nz);
     const int plast = xb + 2;   // last plane of this segment
     const uint32_t base = seq;  // sequence number of plane xa - 3
+    const int c0 = (int)(sizeof(T) == 4 ? (z0 - HZ) : 2 * (z0 - HZ));
 
     // per-thread constants of this tile
-    T pyv[R], yyv[R];
+    T pyv[R], yv1[R];
     bool yok[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) {
       const int gy = y0 + yg * R + r;
       yok[r] = gy < ny;
       pyv[r] = (yok[r] && a.pot_mode == POT_HARM) ? a.py[gy] : (T)0;
-      yyv[r] = yok[r] ? a.yy[gy] : (T)0;
+      yv1[r] = yok[r] ? a.yy[gy] * a.ix1 : (T)0;   // y / (60 hx)
     }
     const T pzv = (zok && a.pot_mode == POT_HARM) ? a.pz[gz] : (T)0;
 
-    // issue the first planes of the segment
+    auto issue = [&](int p) {
+      const uint32_t sq = seq_issue++;
+      const int sl = sq % S;
+      fence_proxy_async();
+      mbar_expect_tx(&bars[sl], G::SLOT_BYTES);
+      tma_load_3d(ring + (size_t)sl * G::SLOT_STRIDE_ELEMS, &tm, c0, y0 - 3, plane_src(p), &bars[sl]);
+    };
     if (tid == 0) {
       seq_issue = base;
-      for (int p = xa - 3; p <= plast && p < xa - 3 + S; ++p) {
-        const uint32_t sq = seq_issue++;
-        const int sl = sq % S;
-        fence_proxy_async();
-        mbar_expect_tx(&bars[sl], G::SLOT_BYTES);
-        const int c0 = (int)(sizeof(T) == 4 ? (z0 - HZ) : 2 * (z0 - HZ));
-        tma_load_3d(ring + (size_t)sl * G::SLOT_STRIDE_ELEMS, &tm, c0, y0 - 3, plane_src(p), &bars[sl]);
-      }
+      for (int p = xa - 3; p <= plast && p < xa - 3 + S; ++p) issue(p);
     }
 
     auto wait_plane = [&](uint32_t sq) {
@@ -252,7 +246,6 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm, TiledArgs<T> ta) {
     // Patch the y/z ghost cells of a boundary tile's slot from global memory
     // (solid mirror or periodic wrap; zero where map_ghost says so).
     auto fixup = [&](uint32_t sq, int p) {
-      if (!(bnd_y || bnd_z)) return;
       V* sl = ring + (size_t)(sq % S) * G::SLOT_STRIDE_ELEMS;
       const int xp = plane_src(p);
       if (xp < 0 || xp >= nx) return;  // zero plane
@@ -283,108 +276,102 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm, TiledArgs<T> ta) {
       }
     };
 
+    // register queue: q[j][r] holds plane x-3+j after the shift of plane x
     V q[7][R];
-    // prologue: planes xa-3 .. xa+2 -> q[0..5]
+    const int qoff = (yg * R + 3) * TZP + lz + HZ;   // first cell of this thread in a slot
 #pragma unroll
     for (int j = 0; j < 6; ++j) {
       const uint32_t sq = base + j;
       wait_plane(sq);
-      if (j >= 3) fixup(sq, xa - 3 + j);
+      if (j >= 3 && (bnd_y || bnd_z)) fixup(sq, xa - 3 + j);
       const V* sl = ring + (size_t)(sq % S) * G::SLOT_STRIDE_ELEMS;
 #pragma unroll
-      for (int r = 0; r < R; ++r) q[j][r] = sl[(yg * R + r + 3) * TZP + lz + HZ];
+      for (int r = 0; r < R; ++r) q[j + 1][r] = sl[qoff + r * TZP];
     }
     __syncthreads();
     if (tid == 0) {
       for (int j = 0; j < 3; ++j) {
         const int p = xa - 3 + j + S;
         if (p > plast) break;
-        const uint32_t sq = seq_issue++;
-        const int sl = sq % S;
-        fence_proxy_async();
-        mbar_expect_tx(&bars[sl], G::SLOT_BYTES);
-        const int c0 = (int)(sizeof(T) == 4 ? (z0 - HZ) : 2 * (z0 - HZ));
-        tma_load_3d(ring + (size_t)sl * G::SLOT_STRIDE_ELEMS, &tm, c0, y0 - 3, plane_src(p), &bars[sl]);
+        issue(p);
       }
     }
 
-    // one x-plane; OFF = (x - xa) mod 7 resolves the register queue at compile time
-    auto body = [&](auto offc, int x) {
-      constexpr int OFF = decltype(offc)::value;
-      const uint32_t sqx = base + (uint32_t)(x - xa) + 3;      // plane x
-      const uint32_t sq3 = sqx + 3;                             // plane x + 3
-      // prefetch w / potential of this plane
-      const size_t rowbase = ((size_t)x * ny + (y0 + yg * R)) * nz + gz;
+    size_t rowbase = ((size_t)xa * ny + (y0 + yg * R)) * nz + gz;
+    const size_t plane_stride = (size_t)ny * nz;
+#pragma unroll 1
+    for (int x = xa; x < xb; ++x, rowbase += plane_stride) {
+      const uint32_t sqx = base + (uint32_t)(x - xa) + 3;   // plane x
+      const uint32_t sq3 = sqx + 3;                          // plane x + 3
+      // w and the potential of this plane: issue the loads before waiting
       V wv[R];
       T tv[R];
 #pragma unroll
       for (int r = 0; r < R; ++r) {
         const bool ok = zok && yok[r];
-        const size_t idx = rowbase + (size_t)r * nz;
         wv[r] = mk<T>((T)0, (T)0);
-        if ((KIND == ST_S2 || KIND == ST_S3) && ok) wv[r] = a.w[idx];
-        tv[r] = (a.pot_mode == POT_ARR && ok) ? a.trap[idx] : (T)0;
+        tv[r] = (T)0;
+        if ((KIND == ST_S2 || KIND == ST_S3) && ok) wv[r] = a.w[rowbase + (size_t)r * nz];
+        if (a.pot_mode == POT_ARR && ok) tv[r] = a.trap[rowbase + (size_t)r * nz];
       }
+      const T xv1 = a.xx[x] * a.iy1;   // x / (60 hy)
+      const T pxv = a.pot_mode == POT_HARM ? a.px[x] : (T)0;
       wait_plane(sq3);
-      fixup(sq3, x + 3);
-      {
-        const V* sl3 = ring + (size_t)(sq3 % S) * G::SLOT_STRIDE_ELEMS;
+      if (bnd_y || bnd_z) fixup(sq3, x + 3);
+      const V* sl3 = ring + (size_t)(sq3 % S) * G::SLOT_STRIDE_ELEMS;
 #pragma unroll
-        for (int r = 0; r < R; ++r) q[(OFF + 6) % 7][r] = sl3[(yg * R + r + 3) * TZP + lz + HZ];
+      for (int r = 0; r < R; ++r) {
+#pragma unroll
+        for (int j = 0; j < 6; ++j) q[j][r] = q[j + 1][r];
+        q[6][r] = sl3[qoff + r * TZP];
       }
-      const V* sl = ring + (size_t)(sqx % S) * G::SLOT_STRIDE_ELEMS;
-      const V* col = sl + (yg * R + 3) * TZP + lz + HZ;  // row of the first cell
+      const V* col = ring + (size_t)(sqx % S) * G::SLOT_STRIDE_ELEMS + qoff;
       // y column: 3 ghost rows above, R centres (from the queue), 3 below
       V yc[R + 6];
 #pragma unroll
       for (int j = 0; j < 3; ++j) yc[j] = col[(j - 3) * TZP];
 #pragma unroll
-      for (int r = 0; r < R; ++r) yc[r + 3] = q[(OFF + 3) % 7][r];
+      for (int r = 0; r < R; ++r) yc[r + 3] = q[3][r];
 #pragma unroll
       for (int j = 0; j < 3; ++j) yc[R + 3 + j] = col[(R + j) * TZP];
-      const T xv = a.xx[x];
-      const T pxv = a.pot_mode == POT_HARM ? a.px[x] : (T)0;
 #pragma unroll
       for (int r = 0; r < R; ++r) {
-        const V craw = q[(OFF + 3) % 7][r];
-        // x line from the queue
-        const V xm3 = q[(OFF + 0) % 7][r], xm2 = q[(OFF + 1) % 7][r], xm1 = q[(OFF + 2) % 7][r];
-        const V xp1 = q[(OFF + 4) % 7][r], xp2 = q[(OFF + 5) % 7][r], xp3 = q[(OFF + 6) % 7][r];
+        const V craw = q[3][r];
+        const V xm3 = q[0][r], xm2 = q[1][r], xm1 = q[2][r];
+        const V xp1 = q[4][r], xp2 = q[5][r], xp3 = q[6][r];
         const V ym3 = yc[r], ym2 = yc[r + 1], ym1 = yc[r + 2];
         const V yp1 = yc[r + 4], yp2 = yc[r + 5], yp3 = yc[r + 6];
-        V lap = P::mul(splat<T>(c490), craw);
-        lap = P::fma(cx2, P::add(xm3, xp3), lap);
-        lap = P::fma(cx27, P::add(xm2, xp2), lap);
-        lap = P::fma(cx270, P::add(xm1, xp1), lap);
-        lap = P::fma(cy2, P::add(ym3, yp3), lap);
-        lap = P::fma(cy27, P::add(ym2, yp2), lap);
-        lap = P::fma(cy270, P::add(ym1, yp1), lap);
+        V lap = P::mul(ta.k[9], craw);
+        lap = P::fma(ta.k[0], P::add(xm3, xp3), lap);
+        lap = P::fma(ta.k[1], P::add(xm2, xp2), lap);
+        lap = P::fma(ta.k[2], P::add(xm1, xp1), lap);
+        lap = P::fma(ta.k[3], P::add(ym3, yp3), lap);
+        lap = P::fma(ta.k[4], P::add(ym2, yp2), lap);
+        lap = P::fma(ta.k[5], P::add(ym1, yp1), lap);
         if (!a.two_dim) {
           const V* zr = col + r * TZP;
-          const V zm3 = zr[-3], zm2 = zr[-2], zm1 = zr[-1];
-          const V zp1 = zr[1], zp2 = zr[2], zp3 = zr[3];
-          lap = P::fma(cz2, P::add(zm3, zp3), lap);
-          lap = P::fma(cz27, P::add(zm2, zp2), lap);
-          lap = P::fma(cz270, P::add(zm1, zp1), lap);
+          lap = P::fma(ta.k[6], P::add(zr[-3], zr[3]), lap);
+          lap = P::fma(ta.k[7], P::add(zr[-2], zr[2]), lap);
+          lap = P::fma(ta.k[8], P::add(zr[-1], zr[1]), lap);
         }
         V fr = mk<T>((T)0, (T)0);
         if (a.frame_mode != FRAME_NONE) {
-          V d1x = P::mul(cx1, P::sub(xp3, xm3));
-          d1x = P::fma(cx9, P::sub(xp2, xm2), d1x);
-          d1x = P::fma(cx45, P::sub(xp1, xm1), d1x);
+          // D1 without 1/(60h): (v3 - v-3) - 9 (v2 - v-2) + 45 (v1 - v-1)
+          V dx = P::add(xp3, neg(xm3));
+          dx = P::fma(ta.k[10], P::add(xp2, neg(xm2)), dx);
+          dx = P::fma(ta.k[11], P::add(xp1, neg(xm1)), dx);
           V zc;
           if (a.frame_mode == FRAME_ROT) {
-            V d1y = P::mul(cy1, P::sub(yp3, ym3));
-            d1y = P::fma(cy9, P::sub(yp2, ym2), d1y);
-            d1y = P::fma(cy45, P::sub(yp1, ym1), d1y);
-            // Z = x*D1y - y*D1x
-            zc = P::fma(splat<T>(-yyv[r]), d1x, P::mul(splat<T>(xv), d1y));
+            V dy = P::add(yp3, neg(ym3));
+            dy = P::fma(ta.k[10], P::add(yp2, neg(ym2)), dy);
+            dy = P::fma(ta.k[11], P::add(yp1, neg(ym1)), dy);
+            // Z = x D1y - y D1x with the 1/(60h) factors folded into x and y
+            zc = P::fma(splat<T>(-yv1[r]), dx, P::mul(splat<T>(xv1), dy));
           } else {
-            zc = d1x;
+            zc = P::mul(splat<T>(a.ix1), dx);
           }
           // (0, omega) * Z = (-omega Z.im, omega Z.re), on the renormalised state
-          const T os = a.omega * scale;
-          fr = mk<T>(-os * zc.y, os * zc.x);
+          fr = mk<T>(-oms * zc.y, oms * zc.x);
         }
         // everything above is linear in psi: apply the load factor once
         const V c = P::mul(vscale, craw);
@@ -396,18 +383,16 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm, TiledArgs<T> ta) {
         const T rho = (T)1 - a2 - pot;
         const V rhs = P::fma(splat<T>(rho), c, P::add(lap, fr));
         // w = A w + c_f * rhs ; psi' = psi + B w  (run.f90:47-54)
-        V cr = P::mul(splat<T>(a.c_re), rhs);
-        cr = P::fma(mk<T>(-a.c_im, a.c_im), mk<T>(rhs.y, rhs.x), cr);
+        const V cr = P::fma(ta.k[13], mk<T>(rhs.y, rhs.x), P::mul(ta.k[12], rhs));
         V wn, pn;
         if (KIND == ST_EU) {
           pn = P::add(c, cr);
           wn = cr;
         } else {
-          wn = (KIND == ST_S1) ? cr : P::fma(splat<T>(a.A), wv[r], cr);
-          pn = P::fma(splat<T>(a.B), wn, c);
+          wn = (KIND == ST_S1) ? cr : P::fma(ta.k[14], wv[r], cr);
+          pn = P::fma(ta.k[15], wn, c);
         }
-        const bool ok = zok && yok[r];
-        if (ok) {
+        if (zok && yok[r]) {
           const size_t idx = rowbase + (size_t)r * nz;
           if (KIND == ST_S1 || KIND == ST_S2) a.w[idx] = wn;
           if (KIND != ST_DIAG) a.psi_out[idx] = pn;
@@ -427,35 +412,8 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm, TiledArgs<T> ta) {
         }
       }
       __syncthreads();
-      if (tid == 0) {
-        const int p = x + S;
-        if (p <= plast) {
-          const uint32_t sq = seq_issue++;
-          const int slx = sq % S;
-          fence_proxy_async();
-          mbar_expect_tx(&bars[slx], G::SLOT_BYTES);
-          const int c0 = (int)(sizeof(T) == 4 ? (z0 - HZ) : 2 * (z0 - HZ));
-          tma_load_3d(ring + (size_t)slx * G::SLOT_STRIDE_ELEMS, &tm, c0, y0 - 3, plane_src(p), &bars[slx]);
-        }
-      }
-    };
-
-    int x = xa;
-    for (; x + 7 <= xb; x += 7) {
-      body(std::integral_constant<int, 0>{}, x);
-      body(std::integral_constant<int, 1>{}, x + 1);
-      body(std::integral_constant<int, 2>{}, x + 2);
-      body(std::integral_constant<int, 3>{}, x + 3);
-      body(std::integral_constant<int, 4>{}, x + 4);
-      body(std::integral_constant<int, 5>{}, x + 5);
-      body(std::integral_constant<int, 6>{}, x + 6);
+      if (tid == 0 && x + S <= plast) issue(x + S);
     }
-    if (x < xb) body(std::integral_constant<int, 0>{}, x);
-    if (x + 1 < xb) body(std::integral_constant<int, 1>{}, x + 1);
-    if (x + 2 < xb) body(std::integral_constant<int, 2>{}, x + 2);
-    if (x + 3 < xb) body(std::integral_constant<int, 3>{}, x + 3);
-    if (x + 4 < xb) body(std::integral_constant<int, 4>{}, x + 4);
-    if (x + 5 < xb) body(std::integral_constant<int, 5>{}, x + 5);
     seq = base + (uint32_t)(xb - xa) + 6;
     failed = __syncthreads_or(failed) != 0;
     if (failed) break;

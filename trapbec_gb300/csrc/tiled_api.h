@@ -17,6 +17,7 @@ struct TiledPlan {
   int ntz = 0, nty = 0;
   long long units = 0;
   int fix_y = 0, fix_z = 0, bcz = 0;
+  int chunk = 0;         // x-chunk length of the work order (nx: tile-major)
   const void* psi_base[2] = {nullptr, nullptr};
   CUtensorMap tm[2];
   int* err = nullptr;    // device error flag (owned by the context)

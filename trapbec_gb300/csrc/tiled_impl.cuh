@@ -76,6 +76,7 @@ int plan_shape(const trapbec_params& p, void* const psi[2], int nsm, int* err_fl
   q.nt = G::NT;
   q.tz = TZ; q.ty = TY; q.r = R;
   q.fix_y = fix_y; q.fix_z = fix_z; q.bcz = bcz;
+  q.chunk = p.nx;   // tile-major order until set_chunk chooses otherwise
   q.err = err_flag;
   q.valid = 1;
   *plan = q;
@@ -94,6 +95,18 @@ int launch_shape(const TiledPlan& plan, int kind, const StageArgs<T>& a, cudaStr
   ta.bcz = plan.bcz;
   ta.fix_y = plan.fix_y;
   ta.fix_z = plan.fix_z;
+  ta.chunk = plan.chunk;
+  {
+    auto pr = [](T v) { return mk<T>(v, v); };
+    const T ix2 = a.ix2, iy2 = a.iy2, iz2 = a.iz2;
+    ta.k[0] = pr((T)2 * ix2); ta.k[1] = pr((T)(-27) * ix2); ta.k[2] = pr((T)270 * ix2);
+    ta.k[3] = pr((T)2 * iy2); ta.k[4] = pr((T)(-27) * iy2); ta.k[5] = pr((T)270 * iy2);
+    ta.k[6] = pr((T)2 * iz2); ta.k[7] = pr((T)(-27) * iz2); ta.k[8] = pr((T)270 * iz2);
+    ta.k[9] = pr((T)(-490) * (ix2 + iy2 + (a.two_dim ? (T)0 : iz2)));
+    ta.k[10] = pr((T)(-9)); ta.k[11] = pr((T)45);
+    ta.k[12] = pr(a.c_re); ta.k[13] = mk<T>(-a.c_im, a.c_im);
+    ta.k[14] = pr(a.A); ta.k[15] = pr(a.B);
+  }
   const CUtensorMap* tm = nullptr;
   if ((const void*)a.psi_in == plan.psi_base[0]) tm = &plan.tm[0];
   else if ((const void*)a.psi_in == plan.psi_base[1]) tm = &plan.tm[1];

@@ -93,6 +93,7 @@ struct trapbec_ctx {
   int shape = 0;                       // tiled-kernel shape index
   int* d_err = nullptr;                // device error flag of the tiled kernel
   int* h_err = nullptr;                // pinned copy
+  int chunk_user = 0;                  // x-chunk requested by the caller (0 = automatic)
 };
 
 namespace {
@@ -220,6 +221,17 @@ template <typename T> StageArgs<T> base_args(trapbec_ctx* c, double t) {
   }
   a.scale = (T)1;
   return a;
+}
+
+// Default x-chunk: keep the boxes fetched by all resident CTAs during one
+// chunk within about half of L2, so a y-neighbour's ghost rows are still there.
+int auto_chunk(const trapbec_ctx* c) {
+  if (c->chunk_user > 0) return std::min(c->chunk_user, c->p.nx);
+  const double half_l2 = 64.0e6;
+  const double box = (double)(c->plan.tz + 8) * (c->plan.ty + 6) * (double)c->esz;
+  int L = (int)(half_l2 / (std::max(1, c->plan.grid) * box));
+  L = std::max(16, std::min(L, c->p.nx));
+  return L;
 }
 
 template <typename T> bool use_tiled(trapbec_ctx* c) {
@@ -602,6 +614,7 @@ template <typename T> int create_impl(trapbec_ctx* c) {
   int rc = setup_tables<T>(c);
   if (rc) return rc;
   c->plan_valid = (plan_tiled<T>(c->p, c->psi, c->nsm, 0, c->d_err, &c->plan) == 0);
+  if (c->plan_valid) c->plan.chunk = auto_chunk(c);
   return TRAPBEC_OK;
 }
 
@@ -957,11 +970,113 @@ int trapbec_set_kernel(trapbec_ctx* c, int kind, int tile_z, int tile_y) {
     int rc = c->prec == TRAPBEC_FP64 ? plan_tiled<double>(c->p, c->psi, c->nsm, shape, c->d_err, &c->plan)
                                      : plan_tiled<float>(c->p, c->psi, c->nsm, shape, c->d_err, &c->plan);
     c->plan_valid = (rc == 0);
+    if (c->plan_valid) c->plan.chunk = auto_chunk(c);
   }
   if (kind == 2 && !c->plan_valid) {
     set_error("tiled kernel not available for this grid / tile shape");
     return TRAPBEC_ERR_UNSUPPORTED;
   }
+  return TRAPBEC_OK;
+}
+
+int trapbec_set_chunk(trapbec_ctx* c, int chunk) {
+  if (!c || chunk < 0) return TRAPBEC_ERR_ARG;
+  c->chunk_user = chunk;
+  if (c->plan_valid) c->plan.chunk = auto_chunk(c);
+  return TRAPBEC_OK;
+}
+
+}  // extern "C"
+namespace {
+struct TuneKey {
+  trapbec_params p;
+  bool operator==(const TuneKey& o) const { return std::memcmp(&p, &o.p, sizeof(p)) == 0; }
+};
+struct TuneVal { int shape, chunk; double ms; };
+std::vector<std::pair<TuneKey, TuneVal>> g_tune_cache;
+std::mutex g_tune_mu;
+
+template <typename T> int autotune_impl(trapbec_ctx* c, int steps, TuneVal* best) {
+  TuneKey key;
+  std::memset(&key.p, 0, sizeof(key.p));
+  key.p.nx = c->p.nx; key.p.ny = c->p.ny; key.p.nz = c->p.nz;
+  key.p.precision = c->p.precision; key.p.boundaries = c->p.boundaries; key.p.periodicz = c->p.periodicz;
+  key.p.potential = c->p.potential;
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    for (auto& kv : g_tune_cache)
+      if (kv.first == key) { *best = kv.second; return TRAPBEC_OK; }
+  }
+  // save the state (both buffers: psi and w) and the time
+  void* save = nullptr;
+  CK(cudaMalloc(&save, c->n * c->esz));
+  CK(cudaMemcpyAsync(save, c->psi[c->cur], c->n * c->esz, cudaMemcpyDeviceToDevice, c->st));
+  const double t_save = c->t;
+  const int cur_save = c->cur;
+  TuneVal bv{-1, 0, 1e300};
+  const int ns = tiled_nshapes<T>();
+  int rc = TRAPBEC_OK;
+  for (int sh = 0; sh < ns && rc == TRAPBEC_OK; ++sh) {
+    TiledPlan plan;
+    if (plan_tiled<T>(c->p, c->psi, c->nsm, sh, c->d_err, &plan) != 0) continue;
+    std::vector<int> chunks = {16, 32, 64, c->p.nx};
+    for (int L : chunks) {
+      if (L > c->p.nx) continue;
+      plan.chunk = L;
+      c->plan = plan;
+      c->plan_valid = true;
+      c->kernel_kind = 2;
+      if ((rc = do_step_rt<T>(c, 1))) break;     // warm-up
+      if ((rc = do_step_rt<T>(c, steps))) break;
+      double ms = c->last_ms / steps;
+      if (ms < bv.ms) bv = TuneVal{sh, L, ms};
+      CK(cudaMemcpyAsync(c->psi[cur_save], save, c->n * c->esz, cudaMemcpyDeviceToDevice, c->st));
+      c->cur = cur_save;
+      c->t = t_save;
+    }
+  }
+  CK(cudaMemcpyAsync(c->psi[cur_save], save, c->n * c->esz, cudaMemcpyDeviceToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  cudaFree(save);
+  c->cur = cur_save;
+  c->t = t_save;
+  c->kernel_kind = 0;
+  if (rc) return rc;
+  if (bv.shape < 0) { set_error("no tiled kernel shape fits this grid"); return TRAPBEC_ERR_UNSUPPORTED; }
+  if (plan_tiled<T>(c->p, c->psi, c->nsm, bv.shape, c->d_err, &c->plan) != 0) return TRAPBEC_ERR_CUDA;
+  c->plan.chunk = bv.chunk;
+  c->plan_valid = true;
+  c->shape = bv.shape;
+  c->chunk_user = bv.chunk;
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune_cache.push_back({key, bv});
+  }
+  *best = bv;
+  return TRAPBEC_OK;
+}
+}  // namespace
+extern "C" {
+
+int trapbec_autotune(trapbec_ctx* c, int steps, int* tile_z, int* tile_y, int* chunk, double* ms_per_step) {
+  if (!c || steps < 1) return TRAPBEC_ERR_ARG;
+  TuneVal bv;
+  int rc = DISPATCH(c, autotune_impl, c, steps, &bv);
+  if (rc) return rc;
+  if (!c->plan_valid || c->plan.shape != bv.shape) {
+    int r2 = c->prec == TRAPBEC_FP64 ? plan_tiled<double>(c->p, c->psi, c->nsm, bv.shape, c->d_err, &c->plan)
+                                     : plan_tiled<float>(c->p, c->psi, c->nsm, bv.shape, c->d_err, &c->plan);
+    if (r2) return TRAPBEC_ERR_CUDA;
+    c->plan_valid = true;
+    c->shape = bv.shape;
+  }
+  c->chunk_user = bv.chunk;
+  c->plan.chunk = bv.chunk;
+  Shape sh = c->prec == TRAPBEC_FP64 ? tiled_shape<double>(bv.shape) : tiled_shape<float>(bv.shape);
+  if (tile_z) *tile_z = sh.tz;
+  if (tile_y) *tile_y = sh.ty;
+  if (chunk) *chunk = bv.chunk;
+  if (ms_per_step) *ms_per_step = bv.ms;
   return TRAPBEC_OK;
 }
 

@@ -128,6 +128,15 @@ class Solver:
         check(self.lib.trapbec_set_kernel(self.ctx, int(kind), int(tile_z), int(tile_y)),
               "trapbec_set_kernel")
 
+    def set_chunk(self, chunk: int) -> None:
+        check(self.lib.trapbec_set_chunk(self.ctx, int(chunk)), "trapbec_set_chunk")
+
+    def autotune(self, steps: int = 3) -> dict:
+        tz, ty, ch, ms = C.c_int(0), C.c_int(0), C.c_int(0), C.c_double(0)
+        check(self.lib.trapbec_autotune(self.ctx, int(steps), C.byref(tz), C.byref(ty), C.byref(ch),
+                                        C.byref(ms)), "trapbec_autotune")
+        return {"tile_z": tz.value, "tile_y": ty.value, "chunk": ch.value, "ms_per_step": ms.value}
+
     def launch_count(self) -> int:
         v = C.c_int64(0)
         check(self.lib.trapbec_launch_count(self.ctx, C.byref(v)), "trapbec_launch_count")
