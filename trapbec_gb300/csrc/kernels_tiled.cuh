@@ -125,9 +125,12 @@ template <typename T, int TZ, int TY, int R> struct TileGeom {
   static constexpr int TZP = TZ + 2 * HZ;           // row pitch (complex)
   static constexpr int ROWS = TY + 6;
   static constexpr int SLOT_ELEMS = ROWS * TZP;
-  static constexpr int SLOT_BYTES = SLOT_ELEMS * (int)sizeof(c_t<T>);   // one TMA box
-  static constexpr int SLOT_STRIDE = (SLOT_BYTES + 127) / 128 * 128;     // 128-B aligned slots
+  static constexpr int SLOT_BYTES = SLOT_ELEMS * (int)sizeof(c_t<T>);   // one psi TMA box
+  static constexpr int W_OFF = (SLOT_BYTES + 127) / 128 * 128;           // w tile after the psi box
+  static constexpr int W_BYTES = TZ * TY * (int)sizeof(c_t<T>);          // one w TMA box (no ghosts)
+  static constexpr int SLOT_STRIDE = (W_OFF + W_BYTES + 127) / 128 * 128; // 128-B aligned slots
   static constexpr int SLOT_STRIDE_ELEMS = SLOT_STRIDE / (int)sizeof(c_t<T>);
+  static constexpr int W_OFF_ELEMS = W_OFF / (int)sizeof(c_t<T>);
   static constexpr int NT = TZ * (TY / R);
   static constexpr int S = 8;                       // ring slots
   static constexpr int SMEM = S * SLOT_STRIDE + S * 8;
@@ -135,7 +138,8 @@ template <typename T, int TZ, int TY, int R> struct TileGeom {
 
 template <typename T, int TZ, int TY, int R, int KIND>
 __global__ void __launch_bounds__(TileGeom<T, TZ, TY, R>::NT, ((sizeof(T) == 4 && TileGeom<T, TZ, TY, R>::NT < 512) ? 2 : 1))
-stage_tiled_kernel(const __grid_constant__ CUtensorMap tm, TiledArgs<T> ta) {
+stage_tiled_kernel(const __grid_constant__ CUtensorMap tm, const __grid_constant__ CUtensorMap tmw,
+                   TiledArgs<T> ta) {
   using G = TileGeom<T, TZ, TY, R>;
   using P = PK<T>;
   using V = c_t<T>;
@@ -218,12 +222,19 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm, TiledArgs<T> ta) {
     }
     const T pzv = (zok && a.pot_mode == POT_HARM) ? a.pz[gz] : (T)0;
 
+    // One ring slot = the psi box of plane p and, for stages that read w,
+    // the w tile of plane p (only planes this segment computes).
+    constexpr bool READS_W = (KIND == ST_S2 || KIND == ST_S3);
+    const int cw = (int)(sizeof(T) == 4 ? z0 : 2 * z0);
     auto issue = [&](int p) {
       const uint32_t sq = seq_issue++;
       const int sl = sq % S;
+      const bool with_w = READS_W && p >= xa && p < xb;
+      V* dst = ring + (size_t)sl * G::SLOT_STRIDE_ELEMS;
       fence_proxy_async();
-      mbar_expect_tx(&bars[sl], G::SLOT_BYTES);
-      tma_load_3d(ring + (size_t)sl * G::SLOT_STRIDE_ELEMS, &tm, c0, y0 - 3, plane_src(p), &bars[sl]);
+      mbar_expect_tx(&bars[sl], G::SLOT_BYTES + (with_w ? G::W_BYTES : 0));
+      tma_load_3d(dst, &tm, c0, y0 - 3, plane_src(p), &bars[sl]);
+      if (with_w) tma_load_3d(dst + G::W_OFF_ELEMS, &tmw, cw, y0, p, &bars[sl]);
     };
     if (tid == 0) {
       seq_issue = base;
@@ -303,16 +314,12 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm, TiledArgs<T> ta) {
     for (int x = xa; x < xb; ++x, rowbase += plane_stride) {
       const uint32_t sqx = base + (uint32_t)(x - xa) + 3;   // plane x
       const uint32_t sq3 = sqx + 3;                          // plane x + 3
-      // w and the potential of this plane: issue the loads before waiting
-      V wv[R];
+      // the potential of this plane (array potentials only): issue before waiting
       T tv[R];
 #pragma unroll
       for (int r = 0; r < R; ++r) {
-        const bool ok = zok && yok[r];
-        wv[r] = mk<T>((T)0, (T)0);
         tv[r] = (T)0;
-        if ((KIND == ST_S2 || KIND == ST_S3) && ok) wv[r] = a.w[rowbase + (size_t)r * nz];
-        if (a.pot_mode == POT_ARR && ok) tv[r] = a.trap[rowbase + (size_t)r * nz];
+        if (a.pot_mode == POT_ARR && zok && yok[r]) tv[r] = a.trap[rowbase + (size_t)r * nz];
       }
       const T xv1 = a.xx[x] * a.iy1;   // x / (60 hy)
       const T pxv = a.pot_mode == POT_HARM ? a.px[x] : (T)0;
@@ -325,7 +332,12 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm, TiledArgs<T> ta) {
         for (int j = 0; j < 6; ++j) q[j][r] = q[j + 1][r];
         q[6][r] = sl3[qoff + r * TZP];
       }
-      const V* col = ring + (size_t)(sqx % S) * G::SLOT_STRIDE_ELEMS + qoff;
+      const V* slx = ring + (size_t)(sqx % S) * G::SLOT_STRIDE_ELEMS;
+      const V* col = slx + qoff;
+      V wv[R];
+#pragma unroll
+      for (int r = 0; r < R; ++r)
+        wv[r] = READS_W ? slx[G::W_OFF_ELEMS + (yg * R + r) * TZ + lz] : mk<T>((T)0, (T)0);
       // y column: 3 ghost rows above, R centres (from the queue), 3 below
       V yc[R + 6];
 #pragma unroll

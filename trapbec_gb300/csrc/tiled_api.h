@@ -20,6 +20,7 @@ struct TiledPlan {
   int chunk = 0;         // x-chunk length of the work order (nx: tile-major)
   const void* psi_base[2] = {nullptr, nullptr};
   CUtensorMap tm[2];
+  CUtensorMap tmw;       // w (read by stages 2 and 3)
   int* err = nullptr;    // device error flag (owned by the context)
 };
 
@@ -36,7 +37,8 @@ template <typename T> inline Shape tiled_shape(int i) { return sizeof(T) == 4 ? 
 // tiled kernel can run this grid with this shape, nonzero otherwise (the
 // caller then uses the per-cell kernel).  Defined in tiled_f32.cu / tiled_f64.cu.
 template <typename T>
-int plan_tiled(const trapbec_params& p, void* const psi[2], int nsm, int shape, int* err_flag, TiledPlan* plan);
+int plan_tiled(const trapbec_params& p, void* const psi[2], void* w, int nsm, int shape, int* err_flag,
+               TiledPlan* plan);
 
 // Launch one stage.  kind: StageKind.  a.psi_in must be one of the two psi
 // buffers of the plan.  *nblk_out receives the grid size (reduction partials).

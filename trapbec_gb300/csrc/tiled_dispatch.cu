@@ -4,11 +4,11 @@
 
 namespace tb {
 
-int plan_f32_s0(const trapbec_params&, void* const[2], int, int*, TiledPlan*);
-int plan_f32_s1(const trapbec_params&, void* const[2], int, int*, TiledPlan*);
-int plan_f32_s2(const trapbec_params&, void* const[2], int, int*, TiledPlan*);
-int plan_f64_s0(const trapbec_params&, void* const[2], int, int*, TiledPlan*);
-int plan_f64_s1(const trapbec_params&, void* const[2], int, int*, TiledPlan*);
+int plan_f32_s0(const trapbec_params&, void* const[2], void*, int, int*, TiledPlan*);
+int plan_f32_s1(const trapbec_params&, void* const[2], void*, int, int*, TiledPlan*);
+int plan_f32_s2(const trapbec_params&, void* const[2], void*, int, int*, TiledPlan*);
+int plan_f64_s0(const trapbec_params&, void* const[2], void*, int, int*, TiledPlan*);
+int plan_f64_s1(const trapbec_params&, void* const[2], void*, int, int*, TiledPlan*);
 int launch_f32_s0(const TiledPlan&, int, const StageArgs<float>&, cudaStream_t, int, int*);
 int launch_f32_s1(const TiledPlan&, int, const StageArgs<float>&, cudaStream_t, int, int*);
 int launch_f32_s2(const TiledPlan&, int, const StageArgs<float>&, cudaStream_t, int, int*);
@@ -16,12 +16,13 @@ int launch_f64_s0(const TiledPlan&, int, const StageArgs<double>&, cudaStream_t,
 int launch_f64_s1(const TiledPlan&, int, const StageArgs<double>&, cudaStream_t, int, int*);
 
 template <>
-int plan_tiled<float>(const trapbec_params& p, void* const psi[2], int nsm, int shape, int* err, TiledPlan* plan) {
+int plan_tiled<float>(const trapbec_params& p, void* const psi[2], void* w, int nsm, int shape, int* err,
+                      TiledPlan* plan) {
   int rc;
   switch (shape) {
-    case 0: rc = plan_f32_s0(p, psi, nsm, err, plan); break;
-    case 1: rc = plan_f32_s1(p, psi, nsm, err, plan); break;
-    case 2: rc = plan_f32_s2(p, psi, nsm, err, plan); break;
+    case 0: rc = plan_f32_s0(p, psi, w, nsm, err, plan); break;
+    case 1: rc = plan_f32_s1(p, psi, w, nsm, err, plan); break;
+    case 2: rc = plan_f32_s2(p, psi, w, nsm, err, plan); break;
     default: return 9;
   }
   if (rc == 0) plan->shape = shape;
@@ -40,11 +41,12 @@ int launch_tiled<float>(const TiledPlan& plan, int kind, const StageArgs<float>&
 }
 
 template <>
-int plan_tiled<double>(const trapbec_params& p, void* const psi[2], int nsm, int shape, int* err, TiledPlan* plan) {
+int plan_tiled<double>(const trapbec_params& p, void* const psi[2], void* w, int nsm, int shape, int* err,
+                       TiledPlan* plan) {
   int rc;
   switch (shape) {
-    case 0: rc = plan_f64_s0(p, psi, nsm, err, plan); break;
-    case 1: rc = plan_f64_s1(p, psi, nsm, err, plan); break;
+    case 0: rc = plan_f64_s0(p, psi, w, nsm, err, plan); break;
+    case 1: rc = plan_f64_s1(p, psi, w, nsm, err, plan); break;
     default: return 9;
   }
   if (rc == 0) plan->shape = shape;

@@ -23,7 +23,7 @@ inline PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
 }
 
 template <typename T, int TZ, int TY, int R>
-int plan_shape(const trapbec_params& p, void* const psi[2], int nsm, int* err_flag, TiledPlan* plan) {
+int plan_shape(const trapbec_params& p, void* const psi[2], void* w, int nsm, int* err_flag, TiledPlan* plan) {
   using G = TileGeom<T, TZ, TY, R>;
   if (p.two_dim || p.nx < 4 || p.ny < 4 || p.nz < 8) return 1;
   if (sizeof(T) == 4 && (p.nz % 2)) return 1;  // TMA strides must be multiples of 16 bytes
@@ -57,6 +57,22 @@ int plan_shape(const trapbec_params& p, void* const psi[2], int nsm, int* err_fl
                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return 3;
     q.psi_base[b] = psi[b];
+  }
+  {  // w: interior tiles only
+    cuuint64_t dims[3], strides[2];
+    cuuint32_t box[3], es[3] = {1, 1, 1};
+    dims[0] = sizeof(T) == 4 ? (cuuint64_t)p.nz : (cuuint64_t)p.nz * 2;
+    box[0] = sizeof(T) == 4 ? TZ : 2 * TZ;
+    dims[1] = (cuuint64_t)p.ny;
+    dims[2] = (cuuint64_t)p.nx;
+    strides[0] = (cuuint64_t)p.nz * sizeof(c_t<T>);
+    strides[1] = (cuuint64_t)p.ny * p.nz * sizeof(c_t<T>);
+    box[1] = TY;
+    box[2] = 1;
+    CUresult r = enc(&q.tmw, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, w, dims, strides, box, es,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return 3;
   }
   auto k1 = stage_tiled_kernel<T, TZ, TY, R, ST_S1>;
   auto k2 = stage_tiled_kernel<T, TZ, TY, R, ST_S2>;
@@ -114,11 +130,11 @@ int launch_shape(const TiledPlan& plan, int kind, const StageArgs<T>& a, cudaStr
   int grid = plan.grid;
   if (a.red && grid > red_cap) grid = red_cap;
   switch (kind) {
-    case ST_S1: stage_tiled_kernel<T, TZ, TY, R, ST_S1><<<grid, G::NT, G::SMEM, st>>>(*tm, ta); break;
-    case ST_S2: stage_tiled_kernel<T, TZ, TY, R, ST_S2><<<grid, G::NT, G::SMEM, st>>>(*tm, ta); break;
-    case ST_S3: stage_tiled_kernel<T, TZ, TY, R, ST_S3><<<grid, G::NT, G::SMEM, st>>>(*tm, ta); break;
-    case ST_EU: stage_tiled_kernel<T, TZ, TY, R, ST_EU><<<grid, G::NT, G::SMEM, st>>>(*tm, ta); break;
-    case ST_DIAG: stage_tiled_kernel<T, TZ, TY, R, ST_DIAG><<<grid, G::NT, G::SMEM, st>>>(*tm, ta); break;
+    case ST_S1: stage_tiled_kernel<T, TZ, TY, R, ST_S1><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta); break;
+    case ST_S2: stage_tiled_kernel<T, TZ, TY, R, ST_S2><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta); break;
+    case ST_S3: stage_tiled_kernel<T, TZ, TY, R, ST_S3><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta); break;
+    case ST_EU: stage_tiled_kernel<T, TZ, TY, R, ST_EU><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta); break;
+    case ST_DIAG: stage_tiled_kernel<T, TZ, TY, R, ST_DIAG><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta); break;
     default: return 7;
   }
   if (nblk) *nblk = grid;

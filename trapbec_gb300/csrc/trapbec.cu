@@ -223,15 +223,10 @@ template <typename T> StageArgs<T> base_args(trapbec_ctx* c, double t) {
   return a;
 }
 
-// Default x-chunk: keep the boxes fetched by all resident CTAs during one
-// chunk within about half of L2, so a y-neighbour's ghost rows are still there.
+// Default x-chunk of the work order (the autotuner may pick another).
 int auto_chunk(const trapbec_ctx* c) {
   if (c->chunk_user > 0) return std::min(c->chunk_user, c->p.nx);
-  const double half_l2 = 64.0e6;
-  const double box = (double)(c->plan.tz + 8) * (c->plan.ty + 6) * (double)c->esz;
-  int L = (int)(half_l2 / (std::max(1, c->plan.grid) * box));
-  L = std::max(16, std::min(L, c->p.nx));
-  return L;
+  return c->p.nx;   // tile-major: measured fastest at 512^3; the autotuner tries shorter chunks
 }
 
 template <typename T> bool use_tiled(trapbec_ctx* c) {
@@ -613,7 +608,7 @@ template <typename T> int create_impl(trapbec_ctx* c) {
   *c->h_err = 0;
   int rc = setup_tables<T>(c);
   if (rc) return rc;
-  c->plan_valid = (plan_tiled<T>(c->p, c->psi, c->nsm, 0, c->d_err, &c->plan) == 0);
+  c->plan_valid = (plan_tiled<T>(c->p, c->psi, c->w, c->nsm, 0, c->d_err, &c->plan) == 0);
   if (c->plan_valid) c->plan.chunk = auto_chunk(c);
   return TRAPBEC_OK;
 }
@@ -967,8 +962,8 @@ int trapbec_set_kernel(trapbec_ctx* c, int kind, int tile_z, int tile_y) {
     c->shape = shape;
     c->tile_z = tile_z;
     c->tile_y = tile_y;
-    int rc = c->prec == TRAPBEC_FP64 ? plan_tiled<double>(c->p, c->psi, c->nsm, shape, c->d_err, &c->plan)
-                                     : plan_tiled<float>(c->p, c->psi, c->nsm, shape, c->d_err, &c->plan);
+    int rc = c->prec == TRAPBEC_FP64 ? plan_tiled<double>(c->p, c->psi, c->w, c->nsm, shape, c->d_err, &c->plan)
+                                     : plan_tiled<float>(c->p, c->psi, c->w, c->nsm, shape, c->d_err, &c->plan);
     c->plan_valid = (rc == 0);
     if (c->plan_valid) c->plan.chunk = auto_chunk(c);
   }
@@ -1018,7 +1013,7 @@ template <typename T> int autotune_impl(trapbec_ctx* c, int steps, TuneVal* best
   int rc = TRAPBEC_OK;
   for (int sh = 0; sh < ns && rc == TRAPBEC_OK; ++sh) {
     TiledPlan plan;
-    if (plan_tiled<T>(c->p, c->psi, c->nsm, sh, c->d_err, &plan) != 0) continue;
+    if (plan_tiled<T>(c->p, c->psi, c->w, c->nsm, sh, c->d_err, &plan) != 0) continue;
     std::vector<int> chunks = {16, 32, 64, c->p.nx};
     for (int L : chunks) {
       if (L > c->p.nx) continue;
@@ -1043,7 +1038,7 @@ template <typename T> int autotune_impl(trapbec_ctx* c, int steps, TuneVal* best
   c->kernel_kind = 0;
   if (rc) return rc;
   if (bv.shape < 0) { set_error("no tiled kernel shape fits this grid"); return TRAPBEC_ERR_UNSUPPORTED; }
-  if (plan_tiled<T>(c->p, c->psi, c->nsm, bv.shape, c->d_err, &c->plan) != 0) return TRAPBEC_ERR_CUDA;
+  if (plan_tiled<T>(c->p, c->psi, c->w, c->nsm, bv.shape, c->d_err, &c->plan) != 0) return TRAPBEC_ERR_CUDA;
   c->plan.chunk = bv.chunk;
   c->plan_valid = true;
   c->shape = bv.shape;
@@ -1064,8 +1059,8 @@ int trapbec_autotune(trapbec_ctx* c, int steps, int* tile_z, int* tile_y, int* c
   int rc = DISPATCH(c, autotune_impl, c, steps, &bv);
   if (rc) return rc;
   if (!c->plan_valid || c->plan.shape != bv.shape) {
-    int r2 = c->prec == TRAPBEC_FP64 ? plan_tiled<double>(c->p, c->psi, c->nsm, bv.shape, c->d_err, &c->plan)
-                                     : plan_tiled<float>(c->p, c->psi, c->nsm, bv.shape, c->d_err, &c->plan);
+    int r2 = c->prec == TRAPBEC_FP64 ? plan_tiled<double>(c->p, c->psi, c->w, c->nsm, bv.shape, c->d_err, &c->plan)
+                                     : plan_tiled<float>(c->p, c->psi, c->w, c->nsm, bv.shape, c->d_err, &c->plan);
     if (r2) return TRAPBEC_ERR_CUDA;
     c->plan_valid = true;
     c->shape = bv.shape;
