@@ -136,7 +136,11 @@ template <typename T, int TZ, int TY, int R> struct TileGeom {
   static constexpr int SMEM = S * SLOT_STRIDE + S * 8;
 };
 
-template <typename T, int TZ, int TY, int R, int KIND>
+// PLAIN: the real-time / get_rhs fast path -- no fused reductions, no load
+// factor, harmonic or no potential, rotation or no frame term (the rotation
+// algebra runs with omega = 0 when the frame is off).  Everything else goes
+// through the general variant (PLAIN = false) with run-time switches.
+template <typename T, int TZ, int TY, int R, int KIND, bool PLAIN>
 __global__ void __launch_bounds__(TileGeom<T, TZ, TY, R>::NT, ((sizeof(T) == 4 && TileGeom<T, TZ, TY, R>::NT < 512) ? 2 : 1))
 stage_tiled_kernel(const __grid_constant__ CUtensorMap tm, const __grid_constant__ CUtensorMap tmw,
                    TiledArgs<T> ta) {
@@ -144,10 +148,11 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm, const __grid_constant
   using P = PK<T>;
   using V = c_t<T>;
   constexpr int HZ = G::HZ, TZP = G::TZP, S = G::S, NT = G::NT;
+  constexpr bool READS_W = (KIND == ST_S2 || KIND == ST_S3);
   const StageArgs<T>& a = ta.s;
 
-  T scale;
-  if (stage_skip(a, &scale)) return;
+  T scale = (T)1;
+  if (!PLAIN && stage_skip(a, &scale)) return;
 
   extern __shared__ __align__(128) unsigned char smem_raw[];
   V* ring = reinterpret_cast<V*>(smem_raw);
@@ -166,7 +171,9 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm, const __grid_constant
   __syncthreads();
 
   const V vscale = splat<T>(scale);
-  const T oms = a.omega * scale;
+  const T oms = (PLAIN && a.frame_mode == FRAME_NONE) ? (T)0 : a.omega * scale;
+  const bool rot = PLAIN || a.frame_mode == FRAME_ROT;
+  const bool harm = a.pot_mode == POT_HARM;
 
   RSum<T> rN, rK, rP, rQ, rR, rA;
   rN.init(); rK.init(); rP.init(); rQ.init(); rR.init(); rA.init();
@@ -184,10 +191,9 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm, const __grid_constant
     return map_ghost(p, nx, a.bc);
   };
 
-  // Work units are ordered (z-tile, x-chunk, y-tile, x): consecutive units
-  // stream x inside one chunk of L planes, then move to the y-neighbour tile,
-  // so the y ghost rows of a tile were fetched by its neighbour shortly before
-  // and are served from L2.
+  // Work units are ordered (z-tile, x-chunk, y-tile, x); with the default
+  // chunk = nx this is tile-major order and each CTA streams a contiguous
+  // x-range of one or two tiles.
   const long long per_tz = (long long)ta.nty * nx;
   for (long long u0 = G0; u0 < G1;) {
     const int tzi = (int)(u0 / per_tz);
@@ -206,26 +212,30 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm, const __grid_constant
     const bool zok = gz < nz;
     const bool bnd_y = ta.fix_y && (y0 == 0 || y0 + TY >= ny);
     const bool bnd_z = ta.fix_z && (z0 == 0 || z0 + TZ >= nz);
-    const int plast = xb + 2;   // last plane of this segment
-    const uint32_t base = seq;  // sequence number of plane xa - 3
+    // the x loop runs in groups of 7 planes (compile-time queue rotation);
+    // planes past xb in the last group are computed but not stored
+    const int nit = (xb - xa + 6) / 7;
+    const int xe = xa + 7 * nit;   // end of the computed range
+    const int plast = xe + 2;      // last plane loaded for this segment
+    const uint32_t base = seq;     // sequence number of plane xa - 3
     const int c0 = (int)(sizeof(T) == 4 ? (z0 - HZ) : 2 * (z0 - HZ));
+    const int cw = (int)(sizeof(T) == 4 ? z0 : 2 * z0);
 
     // per-thread constants of this tile
-    T pyv[R], yv1[R];
+    T pyv[R];
+    V myv1[R];   // (-y/(60 hx), -y/(60 hx)) for the rotation term
     bool yok[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) {
       const int gy = y0 + yg * R + r;
       yok[r] = gy < ny;
-      pyv[r] = (yok[r] && a.pot_mode == POT_HARM) ? a.py[gy] : (T)0;
-      yv1[r] = yok[r] ? a.yy[gy] * a.ix1 : (T)0;   // y / (60 hx)
+      pyv[r] = (yok[r] && harm) ? a.py[gy] : (T)0;
+      myv1[r] = splat<T>(yok[r] ? -a.yy[gy] * a.ix1 : (T)0);
     }
-    const T pzv = (zok && a.pot_mode == POT_HARM) ? a.pz[gz] : (T)0;
+    const T pzv = (zok && harm) ? a.pz[gz] : (T)0;
 
     // One ring slot = the psi box of plane p and, for stages that read w,
-    // the w tile of plane p (only planes this segment computes).
-    constexpr bool READS_W = (KIND == ST_S2 || KIND == ST_S3);
-    const int cw = (int)(sizeof(T) == 4 ? z0 : 2 * z0);
+    // the w tile of plane p (only planes this segment stores).
     auto issue = [&](int p) {
       const uint32_t sq = seq_issue++;
       const int sl = sq % S;
@@ -287,7 +297,7 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm, const __grid_constant
       }
     };
 
-    // register queue: q[j][r] holds plane x-3+j after the shift of plane x
+    // register queue: at plane x, q[(x - xa + j) % 7][r] holds plane x - 3 + j
     V q[7][R];
     const int qoff = (yg * R + 3) * TZP + lz + HZ;   // first cell of this thread in a slot
 #pragma unroll
@@ -297,7 +307,7 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm, const __grid_constant
       if (j >= 3 && (bnd_y || bnd_z)) fixup(sq, xa - 3 + j);
       const V* sl = ring + (size_t)(sq % S) * G::SLOT_STRIDE_ELEMS;
 #pragma unroll
-      for (int r = 0; r < R; ++r) q[j + 1][r] = sl[qoff + r * TZP];
+      for (int r = 0; r < R; ++r) q[j][r] = sl[qoff + r * TZP];
     }
     __syncthreads();
     if (tid == 0) {
@@ -308,51 +318,48 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm, const __grid_constant
       }
     }
 
-    size_t rowbase = ((size_t)xa * ny + (y0 + yg * R)) * nz + gz;
     const size_t plane_stride = (size_t)ny * nz;
-#pragma unroll 1
-    for (int x = xa; x < xb; ++x, rowbase += plane_stride) {
+    size_t rowbase = ((size_t)xa * ny + (y0 + yg * R)) * nz + gz;
+
+    auto body = [&](auto offc, int x) {
+      constexpr int OFF = decltype(offc)::value;
+      const bool store = x < xb;
       const uint32_t sqx = base + (uint32_t)(x - xa) + 3;   // plane x
       const uint32_t sq3 = sqx + 3;                          // plane x + 3
-      // the potential of this plane (array potentials only): issue before waiting
       T tv[R];
 #pragma unroll
       for (int r = 0; r < R; ++r) {
         tv[r] = (T)0;
-        if (a.pot_mode == POT_ARR && zok && yok[r]) tv[r] = a.trap[rowbase + (size_t)r * nz];
+        if (!PLAIN && a.pot_mode == POT_ARR && store && zok && yok[r]) tv[r] = a.trap[rowbase + (size_t)r * nz];
       }
-      const T xv1 = a.xx[x] * a.iy1;   // x / (60 hy)
-      const T pxv = a.pot_mode == POT_HARM ? a.px[x] : (T)0;
+      const int xcl = x < nx ? x : nx - 1;
+      const V xv1 = splat<T>(a.xx[xcl] * a.iy1);   // x / (60 hy)
+      const T pxv = harm ? a.px[xcl] : (T)0;
       wait_plane(sq3);
       if (bnd_y || bnd_z) fixup(sq3, x + 3);
-      const V* sl3 = ring + (size_t)(sq3 % S) * G::SLOT_STRIDE_ELEMS;
+      {
+        const V* sl3 = ring + (size_t)(sq3 % S) * G::SLOT_STRIDE_ELEMS;
 #pragma unroll
-      for (int r = 0; r < R; ++r) {
-#pragma unroll
-        for (int j = 0; j < 6; ++j) q[j][r] = q[j + 1][r];
-        q[6][r] = sl3[qoff + r * TZP];
+        for (int r = 0; r < R; ++r) q[(OFF + 6) % 7][r] = sl3[qoff + r * TZP];
       }
       const V* slx = ring + (size_t)(sqx % S) * G::SLOT_STRIDE_ELEMS;
       const V* col = slx + qoff;
-      V wv[R];
-#pragma unroll
-      for (int r = 0; r < R; ++r)
-        wv[r] = READS_W ? slx[G::W_OFF_ELEMS + (yg * R + r) * TZ + lz] : mk<T>((T)0, (T)0);
       // y column: 3 ghost rows above, R centres (from the queue), 3 below
       V yc[R + 6];
 #pragma unroll
       for (int j = 0; j < 3; ++j) yc[j] = col[(j - 3) * TZP];
 #pragma unroll
-      for (int r = 0; r < R; ++r) yc[r + 3] = q[3][r];
+      for (int r = 0; r < R; ++r) yc[r + 3] = q[(OFF + 3) % 7][r];
 #pragma unroll
       for (int j = 0; j < 3; ++j) yc[R + 3 + j] = col[(R + j) * TZP];
 #pragma unroll
       for (int r = 0; r < R; ++r) {
-        const V craw = q[3][r];
-        const V xm3 = q[0][r], xm2 = q[1][r], xm1 = q[2][r];
-        const V xp1 = q[4][r], xp2 = q[5][r], xp3 = q[6][r];
+        const V craw = q[(OFF + 3) % 7][r];
+        const V xm3 = q[(OFF + 0) % 7][r], xm2 = q[(OFF + 1) % 7][r], xm1 = q[(OFF + 2) % 7][r];
+        const V xp1 = q[(OFF + 4) % 7][r], xp2 = q[(OFF + 5) % 7][r], xp3 = q[(OFF + 6) % 7][r];
         const V ym3 = yc[r], ym2 = yc[r + 1], ym1 = yc[r + 2];
         const V yp1 = yc[r + 4], yp2 = yc[r + 5], yp3 = yc[r + 6];
+        const V* zr = col + r * TZP;
         V lap = P::mul(ta.k[9], craw);
         lap = P::fma(ta.k[0], P::add(xm3, xp3), lap);
         lap = P::fma(ta.k[1], P::add(xm2, xp2), lap);
@@ -360,37 +367,35 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm, const __grid_constant
         lap = P::fma(ta.k[3], P::add(ym3, yp3), lap);
         lap = P::fma(ta.k[4], P::add(ym2, yp2), lap);
         lap = P::fma(ta.k[5], P::add(ym1, yp1), lap);
-        if (!a.two_dim) {
-          const V* zr = col + r * TZP;
-          lap = P::fma(ta.k[6], P::add(zr[-3], zr[3]), lap);
-          lap = P::fma(ta.k[7], P::add(zr[-2], zr[2]), lap);
-          lap = P::fma(ta.k[8], P::add(zr[-1], zr[1]), lap);
-        }
+        lap = P::fma(ta.k[6], P::add(zr[-3], zr[3]), lap);
+        lap = P::fma(ta.k[7], P::add(zr[-2], zr[2]), lap);
+        lap = P::fma(ta.k[8], P::add(zr[-1], zr[1]), lap);
         V fr = mk<T>((T)0, (T)0);
-        if (a.frame_mode != FRAME_NONE) {
+        if (PLAIN || a.frame_mode != FRAME_NONE) {
           // D1 without 1/(60h): (v3 - v-3) - 9 (v2 - v-2) + 45 (v1 - v-1)
           V dx = P::add(xp3, neg(xm3));
           dx = P::fma(ta.k[10], P::add(xp2, neg(xm2)), dx);
           dx = P::fma(ta.k[11], P::add(xp1, neg(xm1)), dx);
           V zc;
-          if (a.frame_mode == FRAME_ROT) {
+          if (rot) {
             V dy = P::add(yp3, neg(ym3));
             dy = P::fma(ta.k[10], P::add(yp2, neg(ym2)), dy);
             dy = P::fma(ta.k[11], P::add(yp1, neg(ym1)), dy);
             // Z = x D1y - y D1x with the 1/(60h) factors folded into x and y
-            zc = P::fma(splat<T>(-yv1[r]), dx, P::mul(splat<T>(xv1), dy));
+            zc = P::fma(myv1[r], dx, P::mul(xv1, dy));
           } else {
             zc = P::mul(splat<T>(a.ix1), dx);
           }
           // (0, omega) * Z = (-omega Z.im, omega Z.re), on the renormalised state
           fr = mk<T>(-oms * zc.y, oms * zc.x);
         }
-        // everything above is linear in psi: apply the load factor once
-        const V c = P::mul(vscale, craw);
-        lap = P::mul(vscale, lap);
-        T pot = (T)0;
-        if (a.pot_mode == POT_HARM) pot = pxv + pyv[r] + pzv;
-        else if (a.pot_mode == POT_ARR) pot = tv[r];
+        V c = craw;
+        if (!PLAIN) {   // everything above is linear in psi: apply the load factor once
+          c = P::mul(vscale, craw);
+          lap = P::mul(vscale, lap);
+        }
+        T pot = pxv + pyv[r] + pzv;
+        if (!PLAIN && a.pot_mode == POT_ARR) pot = tv[r];
         const T a2 = c.x * c.x + c.y * c.y;
         const T rho = (T)1 - a2 - pot;
         const V rhs = P::fma(splat<T>(rho), c, P::add(lap, fr));
@@ -401,37 +406,51 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm, const __grid_constant
           pn = P::add(c, cr);
           wn = cr;
         } else {
-          wn = (KIND == ST_S1) ? cr : P::fma(ta.k[14], wv[r], cr);
+          const V wv = READS_W ? slx[G::W_OFF_ELEMS + (yg * R + r) * TZ + lz] : mk<T>((T)0, (T)0);
+          wn = (KIND == ST_S1) ? cr : P::fma(ta.k[14], wv, cr);
           pn = P::fma(ta.k[15], wn, c);
         }
-        if (zok && yok[r]) {
+        if (store && zok && yok[r]) {
           const size_t idx = rowbase + (size_t)r * nz;
           if (KIND == ST_S1 || KIND == ST_S2) a.w[idx] = wn;
           if (KIND != ST_DIAG) a.psi_out[idx] = pn;
-          if (a.reduce == 1) rN.add(pn.x * pn.x + pn.y * pn.y);
-          if (KIND == ST_DIAG || a.reduce == 2) {
-            rN.add(a2);
-            rK.add(c.x * lap.x + c.y * lap.y);
-            rP.add(pot * a2);
-            rQ.add(a2 * a2);
-            rR.add(c.x * fr.x + c.y * fr.y);
-            const double am = sqrt((double)a2);
-            rA.add((T)am);
-            mx = fmax(mx, am);
-            mn = fmin(mn, am);
-            if (!isfinite(a2)) nf = 1.0;
+          if (!PLAIN) {
+            if (a.reduce == 1) rN.add(pn.x * pn.x + pn.y * pn.y);
+            if (KIND == ST_DIAG || a.reduce == 2) {
+              rN.add(a2);
+              rK.add(c.x * lap.x + c.y * lap.y);
+              rP.add(pot * a2);
+              rQ.add(a2 * a2);
+              rR.add(c.x * fr.x + c.y * fr.y);
+              const double am = sqrt((double)a2);
+              rA.add((T)am);
+              mx = fmax(mx, am);
+              mn = fmin(mn, am);
+              if (!isfinite(a2)) nf = 1.0;
+            }
           }
         }
       }
       __syncthreads();
       if (tid == 0 && x + S <= plast) issue(x + S);
+      rowbase += plane_stride;
+    };
+
+    for (int x = xa; x < xe; x += 7) {
+      body(std::integral_constant<int, 0>{}, x);
+      body(std::integral_constant<int, 1>{}, x + 1);
+      body(std::integral_constant<int, 2>{}, x + 2);
+      body(std::integral_constant<int, 3>{}, x + 3);
+      body(std::integral_constant<int, 4>{}, x + 4);
+      body(std::integral_constant<int, 5>{}, x + 5);
+      body(std::integral_constant<int, 6>{}, x + 6);
     }
-    seq = base + (uint32_t)(xb - xa) + 6;
+    seq = base + (uint32_t)(xe - xa) + 6;
     failed = __syncthreads_or(failed) != 0;
     if (failed) break;
   }
 
-  if (a.red != nullptr) {
+  if (!PLAIN && a.red != nullptr) {
     double acc[NRED];
     acc[0] = rN.val(); acc[1] = rK.val(); acc[2] = rP.val(); acc[3] = rQ.val();
     acc[4] = rR.val(); acc[5] = rA.val(); acc[6] = mx; acc[7] = mn; acc[8] = nf;

@@ -74,12 +74,15 @@ int plan_shape(const trapbec_params& p, void* const psi[2], void* w, int nsm, in
                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return 3;
   }
-  auto k1 = stage_tiled_kernel<T, TZ, TY, R, ST_S1>;
-  auto k2 = stage_tiled_kernel<T, TZ, TY, R, ST_S2>;
-  auto k3 = stage_tiled_kernel<T, TZ, TY, R, ST_S3>;
-  auto k4 = stage_tiled_kernel<T, TZ, TY, R, ST_EU>;
-  auto k5 = stage_tiled_kernel<T, TZ, TY, R, ST_DIAG>;
-  for (auto k : {k1, k2, k3, k4, k5})
+  auto k1 = stage_tiled_kernel<T, TZ, TY, R, ST_S1, false>;
+  auto k2 = stage_tiled_kernel<T, TZ, TY, R, ST_S2, false>;
+  auto k3 = stage_tiled_kernel<T, TZ, TY, R, ST_S3, false>;
+  auto k4 = stage_tiled_kernel<T, TZ, TY, R, ST_EU, false>;
+  auto k5 = stage_tiled_kernel<T, TZ, TY, R, ST_DIAG, false>;
+  auto k6 = stage_tiled_kernel<T, TZ, TY, R, ST_S1, true>;
+  auto k7 = stage_tiled_kernel<T, TZ, TY, R, ST_S2, true>;
+  auto k8 = stage_tiled_kernel<T, TZ, TY, R, ST_S3, true>;
+  for (auto k : {k1, k2, k3, k4, k5, k6, k7, k8})
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM) != cudaSuccess) return 4;
   int nb = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k2, G::NT, G::SMEM) != cudaSuccess || nb < 1) return 5;
@@ -129,13 +132,25 @@ int launch_shape(const TiledPlan& plan, int kind, const StageArgs<T>& a, cudaStr
   if (!tm) return 6;
   int grid = plan.grid;
   if (a.red && grid > red_cap) grid = red_cap;
-  switch (kind) {
-    case ST_S1: stage_tiled_kernel<T, TZ, TY, R, ST_S1><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta); break;
-    case ST_S2: stage_tiled_kernel<T, TZ, TY, R, ST_S2><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta); break;
-    case ST_S3: stage_tiled_kernel<T, TZ, TY, R, ST_S3><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta); break;
-    case ST_EU: stage_tiled_kernel<T, TZ, TY, R, ST_EU><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta); break;
-    case ST_DIAG: stage_tiled_kernel<T, TZ, TY, R, ST_DIAG><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta); break;
-    default: return 7;
+  // the plain variant: no reductions, no load factor, harmonic / no potential,
+  // rotation / no frame term, not from the imaginary-time control block
+  const bool plain = a.red == nullptr && a.reduce == 0 && a.ctrl == nullptr && a.scale == (T)1 &&
+                     a.pot_mode != POT_ARR && a.frame_mode != FRAME_ADV;
+  if (plain && kind == ST_S1) {
+    stage_tiled_kernel<T, TZ, TY, R, ST_S1, true><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta);
+  } else if (plain && kind == ST_S2) {
+    stage_tiled_kernel<T, TZ, TY, R, ST_S2, true><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta);
+  } else if (plain && kind == ST_S3) {
+    stage_tiled_kernel<T, TZ, TY, R, ST_S3, true><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta);
+  } else {
+    switch (kind) {
+      case ST_S1: stage_tiled_kernel<T, TZ, TY, R, ST_S1, false><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta); break;
+      case ST_S2: stage_tiled_kernel<T, TZ, TY, R, ST_S2, false><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta); break;
+      case ST_S3: stage_tiled_kernel<T, TZ, TY, R, ST_S3, false><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta); break;
+      case ST_EU: stage_tiled_kernel<T, TZ, TY, R, ST_EU, false><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta); break;
+      case ST_DIAG: stage_tiled_kernel<T, TZ, TY, R, ST_DIAG, false><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta); break;
+      default: return 7;
+    }
   }
   if (nblk) *nblk = grid;
   return cudaGetLastError() == cudaSuccess ? 0 : 8;
