@@ -216,7 +216,8 @@ int trapbec_get_scalar(trapbec_ctx* ctx, int which, double* value);
 
 /* Select the stage kernel: 0 = automatic (tiled TMA kernel where the grid
  * allows it), 1 = simple per-cell kernel, 2 = tiled kernel (error if the
- * grid does not allow it).  tile_z/tile_y = 0 lets the autotuner choose.   */
+ * grid does not allow it).  tile_z/tile_y pick a built tile shape (0, 0:
+ * the default shape; tile_z = -(i+1): built shape number i).              */
 int trapbec_set_kernel(trapbec_ctx* ctx, int kind, int tile_z, int tile_y);
 
 /* Work order of the tiled kernel: x-planes per chunk (0 = automatic).  Tiles

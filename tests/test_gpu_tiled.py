@@ -9,12 +9,17 @@ from tests.helpers import params, smooth_state, rel_err
 
 pytestmark = pytest.mark.gpu
 
-SHAPES = {abi.FP32: [(64, 8), (32, 16), (128, 8)], abi.FP64: [(32, 8), (64, 8)]}
+# built shapes by index (FP32: (128,8), (64,8), (64,16), (64,8) with 6 slots / 3 CTAs per SM)
+SHAPES = {abi.FP32: [(128, 8, 0), (64, 8, 1), (64, 16, 2), (64, 8, 3)], abi.FP64: [(32, 8, 0), (64, 8, 1)]}
 
 
 def _grid_for(tz, ty, bc, zper):
     # full tiles where the boundary needs fix-ups, two tiles per axis
     return (12, 2 * ty, 2 * tz)
+
+
+def _shape_ids(v):
+    return str(v)
 
 
 CASES = [(prec, shp, bc, zper) for prec in (abi.FP64, abi.FP32) for shp in SHAPES[prec]
@@ -23,13 +28,13 @@ CASES = [(prec, shp, bc, zper) for prec in (abi.FP64, abi.FP32) for shp in SHAPE
 
 @pytest.mark.parametrize("prec,shape,bc,zper", CASES, ids=lambda v: str(v))
 def test_tiled_matches_oracle(prec, shape, bc, zper):
-    tz, ty = shape
+    tz, ty, idx = shape
     n = _grid_for(tz, ty, bc, zper)
     p = params(n=n, L=(0.5 * n[0], 0.5 * n[1], 0.5 * n[2]), prec=prec, bc=bc, periodicz=zper, pot="harmonic",
                harm=(40.0, 50.0, 60.0), omega=0.35, dt=0.01)
     psi = smooth_state(p, seed=21)
     s = Solver(p)
-    s.set_kernel(2, tz, ty)
+    s.set_kernel(2, -(idx + 1), 0)
     s.set_psi(psi)
     o = Oracle(p)
     o.set_psi(s.get_psi())

@@ -120,7 +120,7 @@ template <> struct RSum<double> {
 
 template <typename T> constexpr int halo_z() { return sizeof(T) == 4 ? 4 : 3; }
 
-template <typename T, int TZ, int TY, int R> struct TileGeom {
+template <typename T, int TZ, int TY, int R, int NSLOT = 8, int MINB = 0> struct TileGeom {
   static constexpr int HZ = halo_z<T>();
   static constexpr int TZP = TZ + 2 * HZ;           // row pitch (complex)
   static constexpr int ROWS = TY + 6;
@@ -132,19 +132,21 @@ template <typename T, int TZ, int TY, int R> struct TileGeom {
   static constexpr int SLOT_STRIDE_ELEMS = SLOT_STRIDE / (int)sizeof(c_t<T>);
   static constexpr int W_OFF_ELEMS = W_OFF / (int)sizeof(c_t<T>);
   static constexpr int NT = TZ * (TY / R);
-  static constexpr int S = 8;                       // ring slots
+  static constexpr int S = NSLOT;                   // ring slots
   static constexpr int SMEM = S * SLOT_STRIDE + S * 8;
+  // CTAs per SM the register allocation is sized for
+  static constexpr int MIN_BLOCKS = MINB > 0 ? MINB : ((sizeof(T) == 4 && NT < 512) ? 2 : 1);
 };
 
 // PLAIN: the real-time / get_rhs fast path -- no fused reductions, no load
 // factor, harmonic or no potential, rotation or no frame term (the rotation
 // algebra runs with omega = 0 when the frame is off).  Everything else goes
 // through the general variant (PLAIN = false) with run-time switches.
-template <typename T, int TZ, int TY, int R, int KIND, bool PLAIN>
-__global__ void __launch_bounds__(TileGeom<T, TZ, TY, R>::NT, ((sizeof(T) == 4 && TileGeom<T, TZ, TY, R>::NT < 512) ? 2 : 1))
+template <typename T, int TZ, int TY, int R, int NSLOT, int MINB, int KIND, bool PLAIN>
+__global__ void __launch_bounds__(TileGeom<T, TZ, TY, R, NSLOT, MINB>::NT, TileGeom<T, TZ, TY, R, NSLOT, MINB>::MIN_BLOCKS)
 stage_tiled_kernel(const __grid_constant__ CUtensorMap tm, const __grid_constant__ CUtensorMap tmw,
                    TiledArgs<T> ta) {
-  using G = TileGeom<T, TZ, TY, R>;
+  using G = TileGeom<T, TZ, TY, R, NSLOT, MINB>;
   using P = PK<T>;
   using V = c_t<T>;
   constexpr int HZ = G::HZ, TZP = G::TZP, S = G::S, NT = G::NT;
@@ -320,6 +322,9 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm, const __grid_constant
 
     const size_t plane_stride = (size_t)ny * nz;
     size_t rowbase = ((size_t)xa * ny + (y0 + yg * R)) * nz + gz;
+    // x / (60 hy) and the x part of the trap, loaded one plane ahead
+    T xnext = a.xx[xa] * a.iy1;
+    T pnext = harm ? a.px[xa] : (T)0;
 
     auto body = [&](auto offc, int x) {
       constexpr int OFF = decltype(offc)::value;
@@ -332,9 +337,13 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm, const __grid_constant
         tv[r] = (T)0;
         if (!PLAIN && a.pot_mode == POT_ARR && store && zok && yok[r]) tv[r] = a.trap[rowbase + (size_t)r * nz];
       }
-      const int xcl = x < nx ? x : nx - 1;
-      const V xv1 = splat<T>(a.xx[xcl] * a.iy1);   // x / (60 hy)
-      const T pxv = harm ? a.px[xcl] : (T)0;
+      const V xv1 = splat<T>(xnext);
+      const T pxv = pnext;
+      {
+        const int xn = x + 1 < nx ? x + 1 : nx - 1;
+        xnext = a.xx[xn] * a.iy1;
+        pnext = harm ? a.px[xn] : (T)0;
+      }
       wait_plane(sq3);
       if (bnd_y || bnd_z) fixup(sq3, x + 3);
       {

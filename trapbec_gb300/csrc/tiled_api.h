@@ -24,11 +24,12 @@ struct TiledPlan {
   int* err = nullptr;    // device error flag (owned by the context)
 };
 
-// Tile shapes instantiated per precision: {TZ, TY, R} (R = rows per thread).
-struct Shape { int tz, ty, r; };
-constexpr Shape SHAPES_F32[] = {{64, 8, 2}, {32, 16, 4}, {128, 8, 2}};
-constexpr Shape SHAPES_F64[] = {{32, 8, 2}, {64, 8, 2}};
-constexpr int NSHAPES_F32 = 3, NSHAPES_F64 = 2;
+// Tile shapes instantiated per precision: {TZ, TY, R, ring slots, CTAs/SM}
+// (R = rows per thread; CTAs/SM 0 = chosen from the thread count).
+struct Shape { int tz, ty, r, slots, minb; };
+constexpr Shape SHAPES_F32[] = {{128, 8, 2, 8, 0}, {64, 8, 2, 8, 0}, {64, 16, 2, 8, 0}, {64, 8, 2, 6, 3}};
+constexpr Shape SHAPES_F64[] = {{32, 8, 2, 8, 0}, {64, 8, 2, 8, 0}};
+constexpr int NSHAPES_F32 = 4, NSHAPES_F64 = 2;
 
 template <typename T> inline int tiled_nshapes() { return sizeof(T) == 4 ? NSHAPES_F32 : NSHAPES_F64; }
 template <typename T> inline Shape tiled_shape(int i) { return sizeof(T) == 4 ? SHAPES_F32[i] : SHAPES_F64[i]; }

@@ -22,9 +22,9 @@ inline PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
   return fn;
 }
 
-template <typename T, int TZ, int TY, int R>
+template <typename T, int TZ, int TY, int R, int NS, int MB>
 int plan_shape(const trapbec_params& p, void* const psi[2], void* w, int nsm, int* err_flag, TiledPlan* plan) {
-  using G = TileGeom<T, TZ, TY, R>;
+  using G = TileGeom<T, TZ, TY, R, NS, MB>;
   if (p.two_dim || p.nx < 4 || p.ny < 4 || p.nz < 8) return 1;
   if (sizeof(T) == 4 && (p.nz % 2)) return 1;  // TMA strides must be multiples of 16 bytes
   const int bcz = (p.periodicz || p.boundaries == TRAPBEC_BC_PERIODIC) ? TRAPBEC_BC_PERIODIC : p.boundaries;
@@ -74,14 +74,14 @@ int plan_shape(const trapbec_params& p, void* const psi[2], void* w, int nsm, in
                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return 3;
   }
-  auto k1 = stage_tiled_kernel<T, TZ, TY, R, ST_S1, false>;
-  auto k2 = stage_tiled_kernel<T, TZ, TY, R, ST_S2, false>;
-  auto k3 = stage_tiled_kernel<T, TZ, TY, R, ST_S3, false>;
-  auto k4 = stage_tiled_kernel<T, TZ, TY, R, ST_EU, false>;
-  auto k5 = stage_tiled_kernel<T, TZ, TY, R, ST_DIAG, false>;
-  auto k6 = stage_tiled_kernel<T, TZ, TY, R, ST_S1, true>;
-  auto k7 = stage_tiled_kernel<T, TZ, TY, R, ST_S2, true>;
-  auto k8 = stage_tiled_kernel<T, TZ, TY, R, ST_S3, true>;
+  auto k1 = stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S1, false>;
+  auto k2 = stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S2, false>;
+  auto k3 = stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S3, false>;
+  auto k4 = stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_EU, false>;
+  auto k5 = stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_DIAG, false>;
+  auto k6 = stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S1, true>;
+  auto k7 = stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S2, true>;
+  auto k8 = stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S3, true>;
   for (auto k : {k1, k2, k3, k4, k5, k6, k7, k8})
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM) != cudaSuccess) return 4;
   int nb = 0;
@@ -102,9 +102,9 @@ int plan_shape(const trapbec_params& p, void* const psi[2], void* w, int nsm, in
   return 0;
 }
 
-template <typename T, int TZ, int TY, int R>
+template <typename T, int TZ, int TY, int R, int NS, int MB>
 int launch_shape(const TiledPlan& plan, int kind, const StageArgs<T>& a, cudaStream_t st, int red_cap, int* nblk) {
-  using G = TileGeom<T, TZ, TY, R>;
+  using G = TileGeom<T, TZ, TY, R, NS, MB>;
   TiledArgs<T> ta;
   ta.s = a;
   ta.ntz = plan.ntz;
@@ -137,18 +137,18 @@ int launch_shape(const TiledPlan& plan, int kind, const StageArgs<T>& a, cudaStr
   const bool plain = a.red == nullptr && a.reduce == 0 && a.ctrl == nullptr && a.scale == (T)1 &&
                      a.pot_mode != POT_ARR && a.frame_mode != FRAME_ADV;
   if (plain && kind == ST_S1) {
-    stage_tiled_kernel<T, TZ, TY, R, ST_S1, true><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta);
+    stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S1, true><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta);
   } else if (plain && kind == ST_S2) {
-    stage_tiled_kernel<T, TZ, TY, R, ST_S2, true><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta);
+    stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S2, true><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta);
   } else if (plain && kind == ST_S3) {
-    stage_tiled_kernel<T, TZ, TY, R, ST_S3, true><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta);
+    stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S3, true><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta);
   } else {
     switch (kind) {
-      case ST_S1: stage_tiled_kernel<T, TZ, TY, R, ST_S1, false><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta); break;
-      case ST_S2: stage_tiled_kernel<T, TZ, TY, R, ST_S2, false><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta); break;
-      case ST_S3: stage_tiled_kernel<T, TZ, TY, R, ST_S3, false><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta); break;
-      case ST_EU: stage_tiled_kernel<T, TZ, TY, R, ST_EU, false><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta); break;
-      case ST_DIAG: stage_tiled_kernel<T, TZ, TY, R, ST_DIAG, false><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta); break;
+      case ST_S1: stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S1, false><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta); break;
+      case ST_S2: stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S2, false><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta); break;
+      case ST_S3: stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S3, false><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta); break;
+      case ST_EU: stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_EU, false><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta); break;
+      case ST_DIAG: stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_DIAG, false><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta); break;
       default: return 7;
     }
   }

@@ -946,10 +946,13 @@ int trapbec_set_kernel(trapbec_ctx* c, int kind, int tile_z, int tile_y) {
   c->kernel_kind = kind;
   if (kind == 1) return TRAPBEC_OK;
   int shape = 0;
-  if (tile_z || tile_y) {
+  const int ns = c->prec == TRAPBEC_FP64 ? tiled_nshapes<double>() : tiled_nshapes<float>();
+  if (tile_z < 0) {  // select a built shape by index: tile_z = -(index + 1)
+    shape = -tile_z - 1;
+    if (shape >= ns) { set_error("no tiled kernel shape with this index"); return TRAPBEC_ERR_UNSUPPORTED; }
+  } else if (tile_z || tile_y) {
     shape = -1;
-    int ns = c->prec == TRAPBEC_FP64 ? tiled_nshapes<double>() : tiled_nshapes<float>();
-    for (int i = 0; i < ns; ++i) {
+    for (int i = 0; i < ns && shape < 0; ++i) {
       Shape sh = c->prec == TRAPBEC_FP64 ? tiled_shape<double>(i) : tiled_shape<float>(i);
       if (sh.tz == tile_z && sh.ty == tile_y) shape = i;
     }
