@@ -40,8 +40,9 @@ def load_peaks():
 
 
 def profile_traffic(prec_tag: str):
-    """DRAM bytes per grid point per stage launch from the committed ncu summary."""
-    path = os.path.join(HERE, "profiles", f"stage_tiled_{prec_tag}_256.txt")
+    """DRAM bytes per grid point per stage launch from the committed ncu summary
+    of the full-size launch list (profiles/stage_tiled_<prec>_512.txt)."""
+    path = os.path.join(HERE, "profiles", f"stage_tiled_{prec_tag}_512.txt")
     if not os.path.exists(path):
         return None
     m = re.search(r"dram_bytes_per_point_per_launch:\s*([0-9.eE+-]+)", open(path).read())
@@ -64,7 +65,7 @@ class ClockSampler:
         try:
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=self.f, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
@@ -79,7 +80,7 @@ class ClockSampler:
                 self.proc.kill()
             self.f.close()
 
-    def summary(self):
+    def summary(self):  # noqa: D401
         if self.proc is None or not os.path.exists(self.path):
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         sm, smax, reasons = [], None, set()
@@ -136,8 +137,9 @@ def run_reference_arm(args):
     if rank != 0:
         return
     n = args.n
-    # a bounded sample of the workload: the full 512^3 grid, few steps
-    k = max(1, min(args.steps, 2))
+    # a bounded sample of the workload: the full 512^3 grid, a few steps
+    # (about 10 s on 16 host cores), repeated for each timed bench step
+    k = max(1, min(args.steps, args.cpu_steps))
     val, cores, dt = cpu_reference(n, k, None)
     line = {
         "impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
@@ -276,9 +278,10 @@ def run_gpu_arm(args):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        val, cores, dt = cpu_reference(n, 1, None)
+        k_cpu = max(1, args.cpu_steps)
+        val, cores, dt = cpu_reference(n, k_cpu, None)
         cpu = {"value": val, "unit": UNIT, "cores": cores, "kind": "port",
-               "sample": f"1 RK3 step of the full {n}^3 FP32 grid on the host cores ({dt:.1f} s)"}
+               "sample": f"{k_cpu} RK3 steps of the full {n}^3 FP32 grid on the host cores ({dt:.1f} s)"}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -313,7 +316,7 @@ def run_gpu_arm(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=60)
+    ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=512, help="grid size per axis (profiling uses smaller cases)")
@@ -321,6 +324,7 @@ def main():
     ap.add_argument("--shots", type=int, default=100, help="RK3 steps per end-to-end call")
     ap.add_argument("--e2e-reps", type=int, default=2)
     ap.add_argument("--fp64-steps", type=int, default=6)
+    ap.add_argument("--cpu-steps", type=int, default=12, help="RK3 steps of the CPU baseline sample")
     ap.add_argument("--fp64-only", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")

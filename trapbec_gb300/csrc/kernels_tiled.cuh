@@ -179,7 +179,9 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm, const __grid_constant
 
   RSum<T> rN, rK, rP, rQ, rR, rA;
   rN.init(); rK.init(); rP.init(); rQ.init(); rR.init(); rA.init();
-  double mx = 0.0, mn = 1.0e300, nf = 0.0;
+  // max/min |psi| in the state precision (FP64 operations are slow on GB300)
+  T mx = (T)0, mn = (T)3.0e38;
+  bool nf = false;
 
   const long long G0 = (long long)blockIdx.x * ta.units / gridDim.x;
   const long long G1 = (long long)(blockIdx.x + 1) * ta.units / gridDim.x;
@@ -431,11 +433,11 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm, const __grid_constant
               rP.add(pot * a2);
               rQ.add(a2 * a2);
               rR.add(c.x * fr.x + c.y * fr.y);
-              const double am = sqrt((double)a2);
-              rA.add((T)am);
+              const T am = sqrt(a2);
+              rA.add(am);
               mx = fmax(mx, am);
               mn = fmin(mn, am);
-              if (!isfinite(a2)) nf = 1.0;
+              nf |= !isfinite(a2);
             }
           }
         }
@@ -462,7 +464,7 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm, const __grid_constant
   if (!PLAIN && a.red != nullptr) {
     double acc[NRED];
     acc[0] = rN.val(); acc[1] = rK.val(); acc[2] = rP.val(); acc[3] = rQ.val();
-    acc[4] = rR.val(); acc[5] = rA.val(); acc[6] = mx; acc[7] = mn; acc[8] = nf;
+    acc[4] = rR.val(); acc[5] = rA.val(); acc[6] = (double)mx; acc[7] = (double)mn; acc[8] = nf ? 1.0 : 0.0;
     block_reduce_store<NT>(acc, a.red, blockIdx.x, gridDim.x);
   }
 }
