@@ -252,6 +252,30 @@ int trapbec_write_dims(const trapbec_params* p, const char* datadir);
 int trapbec_write_timing(const trapbec_params* p, const char* datadir,
                          double time_per_timestep, double tot_comm_time);
 
+/* ---- statistics of a device-resident psi without allocating ------------ */
+/* This entry point has no counterpart in the reference.  It returns, for a
+ * psi the caller already holds in device memory, the four values trapbec_diag
+ * reports as intpsi2, maxpsi, minpsi and meanpsi (Psi_norm and Psi_info), and
+ * it allocates nothing: no cudaMalloc, cudaFree or allocating library call.
+ * It is meant for callers that cannot let a library allocate device memory,
+ * such as hosts that reserve a GPU's memory up front in their own pool and
+ * must not have memory taken behind the pool's back or their streams stalled
+ * by the device synchronisation an allocation may cause.
+ *  psi       device pointer to ncells complex values of `precision`
+ *  ncells    1 .. 268435456 (16384 blocks x 16384 cells; larger counts are
+ *            rejected with TRAPBEC_ERR_ARG because the fixed scratch would
+ *            not hold their partial sums)
+ *  stats     device pointer to 4 doubles: intpsi2, maxpsi, minpsi, meanpsi
+ *  stream    cudaStream_t to launch on (NULL: the legacy default stream)
+ * The work is queued on `stream`; read `stats` after synchronising with it.
+ * Scratch space is a 512 KiB array in the library's device memory, present on
+ * every GPU that loads the library until the process exits.  The first call
+ * on a device looks up that array's address on the current device; make that
+ * first call before starting any stream capture.  All calls on a device share
+ * the one array, so calls that overlap on the GPU (different streams, or
+ * different host threads) race and must be serialised by the caller.        */
+int trapbec_psi_stats_noalloc(const void* psi, int64_t ncells, int precision, double* stats, void* stream);
+
 /* ---- batched imaginary-time ground states (new) ------------------------- */
 /* Many independent instances (own grid size, trap, g via units, Omega) are
  * relaxed together: each RK3 stage is one persistent launch over the work

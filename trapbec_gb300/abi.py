@@ -146,6 +146,7 @@ _PROTOS = {
                                        C.POINTER(C.c_double)]),
     "trapbec_write_dims": (C.c_int, [C.POINTER(Params), C.c_char_p]),
     "trapbec_write_timing": (C.c_int, [C.POINTER(Params), C.c_char_p, C.c_double, C.c_double]),
+    "trapbec_psi_stats_noalloc": (C.c_int, [_VP, C.c_int64, C.c_int, _VP, _VP]),
     "trapbec_batch_create": (C.c_int, [C.c_int, C.POINTER(Params), C.POINTER(_VP)]),
     "trapbec_batch_destroy": (None, [_VP]),
     "trapbec_batch_set_psi": (C.c_int, [_VP, C.c_int, _VP]),
