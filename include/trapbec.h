@@ -290,6 +290,13 @@ int trapbec_batch_get_psi(trapbec_batch* b, int inst, void* psi);
  * steps_out[ninst], energy_out[ninst], mu_out[ninst] (may be NULL).        */
 int trapbec_batch_solve_imag(trapbec_batch* b, int max_steps, double tol, int check_every,
                              int* steps_out, double* energy_out, double* mu_out);
+/* Fill instance `inst` with a Thomas-Fermi state ("thomas_fermi", from the
+ * instance's harm_w*) or a workload state ("tf_noise", "tf_vortex_line",
+ * "tf_vortex_ring"; see trapbec_init_state).                                */
+int trapbec_batch_init_state(trapbec_batch* b, int inst, const char* init_cond, const trapbec_init_args* args);
+/* Device time of the last solve (ms, events around the whole loop), the tile
+ * shape the autotuner chose, and the kernels launched so far.               */
+int trapbec_batch_stats(trapbec_batch* b, double* solve_ms, int* tile_z, int* tile_y, int64_t* launches);
 
 /* ---- errors ------------------------------------------------------------- */
 const char* trapbec_strerror(int code);

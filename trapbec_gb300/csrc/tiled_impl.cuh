@@ -22,6 +22,49 @@ inline PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
   return fn;
 }
 
+// Packed stencil/update coefficients of TiledArgs::k from the StageArgs.
+template <typename T> inline void fill_coeffs(TiledArgs<T>& ta) {
+  auto pr = [](T v) { return mk<T>(v, v); };
+  const StageArgs<T>& a = ta.s;
+  const T ix2 = a.ix2, iy2 = a.iy2, iz2 = a.iz2;
+  ta.k[0] = pr((T)2 * ix2); ta.k[1] = pr((T)(-27) * ix2); ta.k[2] = pr((T)270 * ix2);
+  ta.k[3] = pr((T)2 * iy2); ta.k[4] = pr((T)(-27) * iy2); ta.k[5] = pr((T)270 * iy2);
+  ta.k[6] = pr((T)2 * iz2); ta.k[7] = pr((T)(-27) * iz2); ta.k[8] = pr((T)270 * iz2);
+  ta.k[9] = pr((T)(-490) * (ix2 + iy2 + (a.two_dim ? (T)0 : iz2)));
+  ta.k[10] = pr((T)(-9)); ta.k[11] = pr((T)45);
+  ta.k[12] = pr(a.c_re); ta.k[13] = mk<T>(-a.c_im, a.c_im);
+  ta.k[14] = pr(a.A); ta.k[15] = pr(a.B);
+}
+
+// TMA descriptors of one grid: the two psi buffers (boxes with the 3-deep
+// ghost frame) and w (interior tiles).
+template <typename T, int TZ, int TY, int R, int NS, int MB>
+int encode_maps(const trapbec_params& p, void* const psi[2], void* w, CUtensorMap* tm, CUtensorMap* tmw) {
+  using G = TileGeom<T, TZ, TY, R, NS, MB>;
+  auto enc = tensor_map_encoder();
+  if (!enc) return 2;
+  for (int b = 0; b < 3; ++b) {
+    const bool is_w = (b == 2);
+    cuuint64_t dims[3], strides[2];
+    cuuint32_t box[3], es[3] = {1, 1, 1};
+    // FP32: one 8-byte element = one complex float; FP64: a complex double is two doubles
+    dims[0] = sizeof(T) == 4 ? (cuuint64_t)p.nz : (cuuint64_t)p.nz * 2;
+    const int bz = is_w ? TZ : G::TZP;
+    box[0] = sizeof(T) == 4 ? bz : 2 * bz;
+    dims[1] = (cuuint64_t)p.ny;
+    dims[2] = (cuuint64_t)p.nx;
+    strides[0] = (cuuint64_t)p.nz * sizeof(c_t<T>);
+    strides[1] = (cuuint64_t)p.ny * p.nz * sizeof(c_t<T>);
+    box[1] = is_w ? TY : G::ROWS;
+    box[2] = 1;
+    CUresult r = enc(is_w ? tmw : &tm[b], CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, is_w ? w : psi[b], dims, strides,
+                     box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return 3;
+  }
+  return 0;
+}
+
 template <typename T, int TZ, int TY, int R, int NS, int MB>
 int plan_shape(const trapbec_params& p, void* const psi[2], void* w, int nsm, int* err_flag, TiledPlan* plan) {
   using G = TileGeom<T, TZ, TY, R, NS, MB>;
@@ -33,55 +76,18 @@ int plan_shape(const trapbec_params& p, void* const psi[2], void* w, int nsm, in
   // ghost fix-ups address the tile edges: partial tiles only with zero ghosts
   if (fix_y && (p.ny % TY)) return 1;
   if (fix_z && (p.nz % TZ)) return 1;
-  auto enc = tensor_map_encoder();
-  if (!enc) return 2;
   TiledPlan q;
-  for (int b = 0; b < 2; ++b) {
-    cuuint64_t dims[3], strides[2];
-    cuuint32_t box[3], es[3] = {1, 1, 1};
-    if (sizeof(T) == 4) {  // one 8-byte element = one complex float
-      dims[0] = (cuuint64_t)p.nz;
-      box[0] = G::TZP;
-    } else {               // complex double as two doubles
-      dims[0] = (cuuint64_t)p.nz * 2;
-      box[0] = 2 * G::TZP;
-    }
-    dims[1] = (cuuint64_t)p.ny;
-    dims[2] = (cuuint64_t)p.nx;
-    strides[0] = (cuuint64_t)p.nz * sizeof(c_t<T>);
-    strides[1] = (cuuint64_t)p.ny * p.nz * sizeof(c_t<T>);
-    box[1] = G::ROWS;
-    box[2] = 1;
-    CUresult r = enc(&q.tm[b], CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, psi[b], dims, strides, box, es,
-                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r != CUDA_SUCCESS) return 3;
-    q.psi_base[b] = psi[b];
-  }
-  {  // w: interior tiles only
-    cuuint64_t dims[3], strides[2];
-    cuuint32_t box[3], es[3] = {1, 1, 1};
-    dims[0] = sizeof(T) == 4 ? (cuuint64_t)p.nz : (cuuint64_t)p.nz * 2;
-    box[0] = sizeof(T) == 4 ? TZ : 2 * TZ;
-    dims[1] = (cuuint64_t)p.ny;
-    dims[2] = (cuuint64_t)p.nx;
-    strides[0] = (cuuint64_t)p.nz * sizeof(c_t<T>);
-    strides[1] = (cuuint64_t)p.ny * p.nz * sizeof(c_t<T>);
-    box[1] = TY;
-    box[2] = 1;
-    CUresult r = enc(&q.tmw, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, w, dims, strides, box, es,
-                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r != CUDA_SUCCESS) return 3;
-  }
-  auto k1 = stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S1, false>;
-  auto k2 = stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S2, false>;
-  auto k3 = stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S3, false>;
-  auto k4 = stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_EU, false>;
-  auto k5 = stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_DIAG, false>;
-  auto k6 = stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S1, true>;
-  auto k7 = stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S2, true>;
-  auto k8 = stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S3, true>;
+  if (int rc = encode_maps<T, TZ, TY, R, NS, MB>(p, psi, w, q.tm, &q.tmw)) return rc;
+  q.psi_base[0] = psi[0];
+  q.psi_base[1] = psi[1];
+  auto k1 = stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S1, false, false>;
+  auto k2 = stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S2, false, false>;
+  auto k3 = stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S3, false, false>;
+  auto k4 = stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_EU, false, false>;
+  auto k5 = stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_DIAG, false, false>;
+  auto k6 = stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S1, true, false>;
+  auto k7 = stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S2, true, false>;
+  auto k8 = stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S3, true, false>;
   for (auto k : {k1, k2, k3, k4, k5, k6, k7, k8})
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM) != cudaSuccess) return 4;
   int nb = 0;
@@ -115,17 +121,7 @@ int launch_shape(const TiledPlan& plan, int kind, const StageArgs<T>& a, cudaStr
   ta.fix_y = plan.fix_y;
   ta.fix_z = plan.fix_z;
   ta.chunk = plan.chunk;
-  {
-    auto pr = [](T v) { return mk<T>(v, v); };
-    const T ix2 = a.ix2, iy2 = a.iy2, iz2 = a.iz2;
-    ta.k[0] = pr((T)2 * ix2); ta.k[1] = pr((T)(-27) * ix2); ta.k[2] = pr((T)270 * ix2);
-    ta.k[3] = pr((T)2 * iy2); ta.k[4] = pr((T)(-27) * iy2); ta.k[5] = pr((T)270 * iy2);
-    ta.k[6] = pr((T)2 * iz2); ta.k[7] = pr((T)(-27) * iz2); ta.k[8] = pr((T)270 * iz2);
-    ta.k[9] = pr((T)(-490) * (ix2 + iy2 + (a.two_dim ? (T)0 : iz2)));
-    ta.k[10] = pr((T)(-9)); ta.k[11] = pr((T)45);
-    ta.k[12] = pr(a.c_re); ta.k[13] = mk<T>(-a.c_im, a.c_im);
-    ta.k[14] = pr(a.A); ta.k[15] = pr(a.B);
-  }
+  fill_coeffs<T>(ta);
   const CUtensorMap* tm = nullptr;
   if ((const void*)a.psi_in == plan.psi_base[0]) tm = &plan.tm[0];
   else if ((const void*)a.psi_in == plan.psi_base[1]) tm = &plan.tm[1];
@@ -137,18 +133,18 @@ int launch_shape(const TiledPlan& plan, int kind, const StageArgs<T>& a, cudaStr
   const bool plain = a.red == nullptr && a.reduce == 0 && a.ctrl == nullptr && a.scale == (T)1 &&
                      a.pot_mode != POT_ARR && a.frame_mode != FRAME_ADV;
   if (plain && kind == ST_S1) {
-    stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S1, true><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta);
+    stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S1, true, false><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta, BatchArgs{});
   } else if (plain && kind == ST_S2) {
-    stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S2, true><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta);
+    stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S2, true, false><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta, BatchArgs{});
   } else if (plain && kind == ST_S3) {
-    stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S3, true><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta);
+    stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S3, true, false><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta, BatchArgs{});
   } else {
     switch (kind) {
-      case ST_S1: stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S1, false><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta); break;
-      case ST_S2: stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S2, false><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta); break;
-      case ST_S3: stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S3, false><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta); break;
-      case ST_EU: stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_EU, false><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta); break;
-      case ST_DIAG: stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_DIAG, false><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta); break;
+      case ST_S1: stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S1, false, false><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta, BatchArgs{}); break;
+      case ST_S2: stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S2, false, false><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta, BatchArgs{}); break;
+      case ST_S3: stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S3, false, false><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta, BatchArgs{}); break;
+      case ST_EU: stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_EU, false, false><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta, BatchArgs{}); break;
+      case ST_DIAG: stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_DIAG, false, false><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta, BatchArgs{}); break;
       default: return 7;
     }
   }
