@@ -34,8 +34,6 @@ def test_batch_matches_oracle_fixed_steps_fp64():
         so, _ = o.step_imag_rk3(40, 0.0)
         assert so == 40
         assert rel_err(b.get_psi(i), o.get_psi()) < 1e-11, i
-        d = o.diag()
-        assert abs(out["energy"][i] - d["energy"]) < 1e-9 * abs(d["energy"]) or True  # energy of step-40 state is formed at step 41
 
 
 def test_batch_converges_like_single_grid_fp64():
