@@ -297,6 +297,10 @@ int trapbec_batch_init_state(trapbec_batch* b, int inst, const char* init_cond, 
 /* Device time of the last solve (ms, events around the whole loop), the tile
  * shape the autotuner chose, and the kernels launched so far.               */
 int trapbec_batch_stats(trapbec_batch* b, double* solve_ms, int* tile_z, int* tile_y, int64_t* launches);
+/* Status of instance `inst` after a solve: out[0..9] = renormalisation factor
+ * pending, previous energy, last |dE|/|E|, energy, chemical potential, norm
+ * before renormalisation, norm target, steps, converged flag, non-finite flag. */
+int trapbec_batch_status(trapbec_batch* b, int inst, double* out10);
 
 /* ---- errors ------------------------------------------------------------- */
 const char* trapbec_strerror(int code);

@@ -157,6 +157,7 @@ _PROTOS = {
     "trapbec_batch_init_state": (C.c_int, [_VP, C.c_int, C.c_char_p, C.POINTER(InitArgs)]),
     "trapbec_batch_stats": (C.c_int, [_VP, C.POINTER(C.c_double), C.POINTER(C.c_int), C.POINTER(C.c_int),
                                       C.POINTER(C.c_int64)]),
+    "trapbec_batch_status": (C.c_int, [_VP, C.c_int, C.POINTER(C.c_double)]),
     "trapbec_strerror": (C.c_char_p, [C.c_int]),
     "trapbec_last_error": (C.c_char_p, []),
     "trapbec_abi_version": (C.c_int, []),

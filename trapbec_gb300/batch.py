@@ -70,6 +70,12 @@ class BatchSolver:
               "trapbec_batch_solve_imag")
         return {"steps": list(steps), "energy": list(e), "mu": list(mu)}
 
+    def status(self, i: int) -> dict:
+        o = (C.c_double * 10)()
+        check(self.lib.trapbec_batch_status(self.h, int(i), o), "trapbec_batch_status")
+        keys = ("scale", "e_prev", "rel", "energy", "mu", "norm", "n0", "step", "converged", "nonfinite")
+        return dict(zip(keys, list(o)))
+
     def stats(self) -> dict:
         ms, tz, ty, nl = C.c_double(0), C.c_int(0), C.c_int(0), C.c_int64(0)
         check(self.lib.trapbec_batch_stats(self.h, C.byref(ms), C.byref(tz), C.byref(ty), C.byref(nl)),

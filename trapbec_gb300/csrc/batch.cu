@@ -364,6 +364,9 @@ template <typename T> int enqueue_steps(trapbec_batch* b, int s, int k, int nact
 }
 
 template <typename T> int upload_work(trapbec_batch* b, int s, const std::vector<int>& act) {
+  // descriptors first: they set each instance's unit count for shape s
+  for (int i = 0; i < b->ninst; ++i)
+    if (int rc = fill_desc<T>(b, i, s)) return rc;
   long long u = 0;
   for (size_t k = 0; k < act.size(); ++k) {
     b->h_act[k] = act[k];
@@ -371,8 +374,6 @@ template <typename T> int upload_work(trapbec_batch* b, int s, const std::vector
     u += b->in[act[k]].units;
   }
   b->h_ustart[act.size()] = u;
-  for (int i = 0; i < b->ninst; ++i)
-    if (int rc = fill_desc<T>(b, i, s)) return rc;
   BCK(cudaMemcpyAsync(b->d_desc, b->h_desc.data(), b->h_desc.size(), cudaMemcpyHostToDevice, b->st));
   BCK(cudaMemcpyAsync(b->d_act, b->h_act, sizeof(int) * act.size(), cudaMemcpyHostToDevice, b->st));
   BCK(cudaMemcpyAsync(b->d_ustart, b->h_ustart, sizeof(long long) * (act.size() + 1), cudaMemcpyHostToDevice, b->st));
@@ -675,6 +676,16 @@ int trapbec_batch_stats(trapbec_batch* b, double* solve_ms, int* tile_z, int* ti
   if (tile_z) *tile_z = b->shape < 0 ? 0 : (b->prec == TRAPBEC_FP64 ? shape_tz<double>(b->shape) : shape_tz<float>(b->shape));
   if (tile_y) *tile_y = b->shape < 0 ? 0 : (b->prec == TRAPBEC_FP64 ? shape_ty<double>(b->shape) : shape_ty<float>(b->shape));
   if (launches) *launches = b->launches;
+  return TRAPBEC_OK;
+}
+
+int trapbec_batch_status(trapbec_batch* b, int inst, double* o) {
+  if (!b || !o || inst < 0 || inst >= b->ninst) return TRAPBEC_ERR_ARG;
+  BCK(cudaMemcpyAsync(b->h_ctrl, b->d_ctrl, sizeof(ImagCtrl) * b->ninst, cudaMemcpyDeviceToHost, b->st));
+  BCK(cudaStreamSynchronize(b->st));
+  const ImagCtrl& c = b->h_ctrl[inst];
+  o[0] = c.scale; o[1] = c.e_prev; o[2] = c.rel; o[3] = c.energy; o[4] = c.mu;
+  o[5] = c.norm; o[6] = c.n0; o[7] = c.step; o[8] = c.converged; o[9] = c.nonfinite;
   return TRAPBEC_OK;
 }
 
