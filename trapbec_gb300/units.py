@@ -23,6 +23,8 @@ The reference's harmonic potential is the only trap shape the workloads use
 from __future__ import annotations
 
 import math
+
+import numpy as np
 from dataclasses import dataclass, field
 
 from .abi import (Params, default_params, BC_ZERO, POT_HARMONIC, FP32, FP64)
@@ -164,3 +166,35 @@ def rotating_quench_512(precision: int = FP32, n: int = 512, seed: int = 99) -> 
     init = dict(name="tf_noise", amp=1.0, r_tf2=[(a / Ra) ** 2 for Ra in R],
                 noise_amp=1e-2, seed=seed, steps=5000, omega_final=0.8 * wp)
     return prob, init
+
+
+def ground_state_draws(count: int, seed: int, grids=(64, 96, 128), precision: int = FP32,
+                       dtau: float = 0.002, res: float = 1.2) -> list[tuple[TrapProblem, dict]]:
+    """Seeded parameter draws of the batched ground-state workload.
+
+    omega_perp ~ U[0.05, 0.2], omega_z / omega_perp ~ U[0.5, 4], g log-uniform
+    in [1, 1000], Omega ~ U[0, 0.7 omega_perp] (entering as -Omega Lz), grid
+    uniform over `grids` (cubic in cells, box per axis 2.6 x the TF radius).
+    The atom number is set so that the chemical potential keeps the healing
+    length resolved: mu = res-scaled so that dx_perp ~ 1.2 xi.  Initial guess:
+    the Thomas-Fermi profile plus 1e-2 seeded noise.  Step dtau (trap units).
+    """
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        n = int(rng.choice(grids))
+        wp = float(rng.uniform(0.05, 0.2))
+        lam = float(rng.uniform(0.5, 4.0))
+        g = float(10 ** rng.uniform(0.0, 3.0))
+        Om = float(rng.uniform(0.0, 0.7 * wp))
+        w = (wp, wp, lam * wp)
+        # dx_perp / xi = 2.6 R_perp / n * sqrt(2 mu) = 5.2 mu / (w_perp n)
+        mu = res * wp * n / 5.2 * float(rng.uniform(0.6, 1.0))
+        R = [math.sqrt(2 * mu) / wa for wa in w]
+        box = tuple(2.6 * r for r in R)
+        prob = TrapProblem(n=(n, n, n), box=box, omega=w, g=g, mu=mu, dt=dtau, Omega=Om, precision=precision)
+        a = prob.a
+        init = dict(name="tf_noise", amp=1.0, r_tf2=[(a / r) ** 2 for r in R], noise_amp=1e-2,
+                    seed=int(seed * 1000003 + i), g=g, Omega=Om, omega=w, N=tf_norm(w, g, mu))
+        out.append((prob, init))
+    return out
