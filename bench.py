@@ -172,6 +172,33 @@ def timed_steps(s, steps, chunk, omega_of_step, start_step=0):
     return ms, s.launch_count() - l0
 
 
+def imag_leg(args):
+    """Batched imaginary-time ground states from the Thomas-Fermi guess: wall
+    time (device events around the whole graph-replayed loop) until every
+    instance reaches |dE|/|E| <= tol, on a bounded set of draws."""
+    from trapbec_gb300 import abi, units
+    from trapbec_gb300.batch import BatchSolver
+    draws = units.ground_state_draws(args.imag_count, args.imag_seed, grids=tuple(args.imag_grids),
+                                     precision=abi.FP32)
+    b = BatchSolver([p.to_params() for p, _ in draws])
+    for i, (p, ini) in enumerate(draws):
+        b.init_state(i, ini["name"], seed=ini["seed"], amp=ini["amp"], r_tf2=ini["r_tf2"],
+                     noise_amp=ini["noise_amp"])
+    t0 = time.perf_counter()
+    out = b.solve(max_steps=args.imag_max_steps, tol=args.imag_tol, check_every=200)
+    wall = time.perf_counter() - t0
+    st = b.stats()
+    conv = [b.status(i)["converged"] > 0 for i in range(len(draws))]
+    cells = sum(p.n[0] * p.n[1] * p.n[2] for p, _ in draws)
+    b.close()
+    return {"guess": "thomas_fermi+1e-2 noise", "instances": len(draws), "cells": cells,
+            "grids": sorted(set(p.n[0] for p, _ in draws)), "tol_rel_dE": args.imag_tol,
+            "dtau_trap_units": 0.002, "max_steps": args.imag_max_steps,
+            "converged": int(sum(conv)), "steps_median": float(statistics.median(out["steps"])),
+            "steps_max": int(max(out["steps"])), "solve_ms_device": st["solve_ms"], "wall_s": wall,
+            "tile": [st["tile_z"], st["tile_y"]], "precision": "c64 state, FP64 norm/energy/test"}
+
+
 def run_gpu_arm(args):
     import numpy as np
     import torch
@@ -307,6 +334,8 @@ def run_gpu_arm(args):
     }
     if fp64:
         line["fp64"] = fp64
+    if args.imag and rank == 0:
+        line["imag"] = imag_leg(args)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:
@@ -330,6 +359,12 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--kernel", type=int, nargs=3, default=None, metavar=("KIND", "TZ", "TY"))
+    ap.add_argument("--imag", action="store_true", help="add the batched imaginary-time leg")
+    ap.add_argument("--imag-count", type=int, default=16)
+    ap.add_argument("--imag-seed", type=int, default=3)
+    ap.add_argument("--imag-grids", type=int, nargs="+", default=[64, 96, 128])
+    ap.add_argument("--imag-tol", type=float, default=1e-10)
+    ap.add_argument("--imag-max-steps", type=int, default=20000)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
