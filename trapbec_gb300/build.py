@@ -63,7 +63,8 @@ def build_library(force: bool = False, verbose_ptxas: bool = False, jobs: int | 
     out = os.path.join(LIB_DIR, "libtrapbec.so")
     os.makedirs(OBJ_DIR, exist_ok=True)
     srcs = [s for s in CUDA_SOURCES + CXX_SOURCES if os.path.exists(os.path.join(CSRC, s))]
-    if not force and os.path.exists(out) and os.path.getmtime(out) >= _newest_dep():
+    drv = os.path.join(LIB_DIR, "trapbec_run")
+    if not force and os.path.exists(out) and os.path.exists(drv) and os.path.getmtime(out) >= _newest_dep():
         return out
     jobs = jobs or min(len(srcs), os.cpu_count() or 4)
     logs = []
@@ -80,6 +81,13 @@ def build_library(force: bool = False, verbose_ptxas: bool = False, jobs: int | 
     if r.returncode != 0:
         raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, out)
+    # the run.f90-style driver program, linked against the library
+    drv = os.path.join(LIB_DIR, "trapbec_run")
+    cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", os.path.join(CSRC, "trapbec_run.cpp"), "-o", drv,
+           "-L", LIB_DIR, "-ltrapbec", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"driver link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
     if verbose_ptxas:
         sys.stderr.write("\n".join(logs))
     return out
