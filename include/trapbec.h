@@ -210,6 +210,17 @@ typedef struct trapbec_diag_out {
 } trapbec_diag_out;
 int trapbec_diag(trapbec_ctx* ctx, trapbec_diag_out* out);
 
+/* Output-time diagnostics of the current psi, written to host memory as
+ * 3 x (nx*ny*nz) reals of the context precision, component-major
+ * ([3][nx][ny][nz], i.e. Fortran vel(k,j,i,c)):
+ *  velocity : 6th-order first derivative of atan2(Im, Re) along x, y, z
+ *             (get_phase, diagnostic.f90:27-48; no phase unwrapping)
+ *  qpressure: 2nd-order gradient of the 4th-order Laplacian of |psi|
+ *             (get_qpressure, diagnostic.f90:50-84)
+ * Both read the ghosted state as ghost_comm leaves it (edges/corners 0).   */
+int trapbec_get_velocity(trapbec_ctx* ctx, void* vel_out);
+int trapbec_get_qpressure(trapbec_ctx* ctx, void* qp_out);
+
 /* Change a scalar between calls (trapbec_scalar), e.g. an Omega ramp.     */
 int trapbec_set_scalar(trapbec_ctx* ctx, int which, double value);
 int trapbec_get_scalar(trapbec_ctx* ctx, int which, double* value);

@@ -42,7 +42,8 @@ def lib() -> C.CDLL:
         L.orc_set_threads.argtypes = [C.c_int]
         L.orc_set_threads.restype = None
         L.orc_max_threads.restype = C.c_int
-        for n in ("orc_set_psi", "orc_get_psi", "orc_get_psi_ghosted", "orc_get_rhs"):
+        for n in ("orc_set_psi", "orc_get_psi", "orc_get_psi_ghosted", "orc_get_rhs", "orc_velocity",
+                  "orc_qpressure"):
             getattr(L, n).argtypes = [vp, vp]
             getattr(L, n).restype = C.c_int
         L.orc_set_trap.argtypes = [vp, C.POINTER(C.c_double)]
@@ -112,6 +113,18 @@ class Oracle:
     def get_rhs(self) -> np.ndarray:
         a = np.empty(self.shape, dtype=self.cdtype)
         assert lib().orc_get_rhs(self.h, a.ctypes.data) == 0
+        return a
+
+    def velocity(self) -> np.ndarray:
+        """get_phase's vel, shape (3, Nx, Ny, Nz)."""
+        a = np.empty((3,) + self.shape, dtype=self.dtype)
+        assert lib().orc_velocity(self.h, a.ctypes.data) == 0
+        return a
+
+    def qpressure(self) -> np.ndarray:
+        """get_qpressure's qpressure, shape (3, Nx, Ny, Nz)."""
+        a = np.empty((3,) + self.shape, dtype=self.dtype)
+        assert lib().orc_qpressure(self.h, a.ctypes.data) == 0
         return a
 
     def set_trap(self, trap: np.ndarray) -> None:

@@ -597,8 +597,45 @@ template <typename T> struct Oracle {
     std::string nm(name);
     Rng rng{a ? a->seed : 0};
     auto runif = [&](T lo, T hi) { T u = (T)rng.next(); return lo + u * (hi - lo); };
-    for (auto& R : ranks) std::fill(R.psi.begin(), R.psi.end(), C<T>{0, 0});
+    const bool helper = nm == "add_noise" || nm == "add_ring" || nm == "add_dipole" || nm == "phase_imprint" ||
+                        nm == "add_pcurrent";
+    if (!helper)
+      for (auto& R : ranks) std::fill(R.psi.begin(), R.psi.end(), C<T>{0, 0});
     const T ring_rad = (T)p.ring_rad;
+    // psi *= func(r) e^{i dir theta} for a straight vortex in plane pl (0: x-y, 1: x-z, 2: y-z)
+    auto vortex_mul = [&](T p1, T p2, T dir, int pl) {
+      for_interior([&](Rank<T>& R, int k, int j, int i) {
+        T c1 = pl == 2 ? R.yy[j] : R.xx[i], c2 = pl == 0 ? R.yy[j] : R.zz[k];
+        T dx = c1 - p1, dy = c2 - p2;
+        C<T> tmp = cscale(vortex_func(std::sqrt(dx * dx + dy * dy)), cexpi(dir * std::atan2(dy, dx)));
+        cell(R, k, j, i) = cmul(cell(R, k, j, i), tmp);
+      });
+    };
+    // ring_p1 * conjg(ring_p2) of a ring whose axis coordinate is x (axis 0) or
+    // y (axis 1) shifted by sa, radius over the other in-plane coordinate and z - sz
+    auto ringpair = [&](int axis, T sa, T sz, T rr0, bool assign) {
+      for_interior([&](Rank<T>& R, int k, int j, int i) {
+        T u = (axis == 0 ? R.xx[i] : R.yy[j]) - sa;
+        T ww = axis == 0 ? R.yy[j] : R.xx[i];
+        T zq = R.zz[k] - sz;
+        T sq = std::sqrt(ww * ww + zq * zq);
+        T th = std::atan2(u, sq + rr0);
+        T r = std::sqrt(u * u + (sq + rr0) * (sq + rr0));
+        C<T> p1 = cscale(ring_density(r), cexpi(th));
+        th = std::atan2(u, sq - rr0);
+        r = std::sqrt(u * u + (sq - rr0) * (sq - rr0));
+        C<T> p2 = cscale(ring_density(r), cexpi(th));
+        C<T> pr = cmul(p1, C<T>{p2.re, -p2.im});
+        cell(R, k, j, i) = assign ? pr : cmul(cell(R, k, j, i), pr);
+      });
+    };
+    auto tf_mul = [&]() {  // multiply_thomas_fermi, initial.f90:654-667
+      for_interior([&](Rank<T>& R, int k, int j, int i) {
+        T d = tf_dense(R, k, j, i);
+        if (d < (T)0) d = 0;
+        cell(R, k, j, i) = cscale(d, cell(R, k, j, i));
+      });
+    };
     const int wn = p.winding_number;
     if (nm == "constant") {
       T v = (T)1 / std::sqrt((T)2);
@@ -698,6 +735,99 @@ template <typename T> struct Oracle {
           cell(R, k, j, i) = cmul(cell(R, k, j, i), tmp);
         });
       }
+    } else if (nm == "lattice") {  // initial.f90:377-420 (ramp = 0: straight lines)
+      for_interior([&](Rank<T>& R, int k, int j, int i) { set_cell(R, k, j, i, {(T)1, (T)1}); });
+      for (int v1 = 1; v1 <= 10; ++v1)
+        for (int v2 = 1; v2 <= 10; ++v2) {
+          (void)runif(0, (T)2 * pi);
+          (void)runif(0, 1);
+          vortex_mul((T)v1 * (Lx / (T)16) - Lx / (T)3, (T)v2 * (Ly / (T)16) - Ly / (T)3, (T)1, 0);
+        }
+    } else if (nm == "lattice2" || nm == "bundle") {  // initial.f90:422-539
+      for_interior([&](Rank<T>& R, int k, int j, int i) {
+        T d = tf_dense(R, k, j, i) / std::sqrt((T)2);
+        if (d < (T)0) d = 0;
+        set_cell(R, k, j, i, {d, d});
+      });
+      if (nm == "lattice2") {
+        for (int v1 = 1; v1 <= 3; ++v1)
+          for (int v2 = 1; v2 <= 3; ++v2)
+            vortex_mul((T)v1 * (Lx / (T)4) - Lx / (T)2, (T)v2 * (Ly / (T)4) - Ly / (T)2, (T)1, 0);
+        for (int v1 = 1; v1 <= 3; ++v1)
+          for (int v2 = 1; v2 <= 3; ++v2)
+            vortex_mul((T)v1 * (Lx / (T)4) + (T)10 - Lx / (T)2, (T)v2 * (Lz / (T)4) + (T)10 - Lz / (T)2, (T)1, 1);
+      } else {
+        for (int pl = 0; pl < 3; ++pl)
+          for (int v1 = 1; v1 <= 7; ++v1) {
+            T rpos = v1 == 1 ? (T)0 : (T)10;
+            T tpos = v1 == 1 ? (T)0 : (T)(v1 - 2) * (T)2 * pi / (T)6;
+            T c1 = rpos * std::cos(tpos), c2 = rpos * std::sin(tpos);
+            if (pl == 0 || pl == 2) c1 = c1 - (T)30; else c2 = c2 - (T)30;
+            vortex_mul(c1, c2, (T)1, pl);
+          }
+      }
+    } else if (nm == "line_of_lines") {  // initial.f90:541-585
+      T v = (T)1 / std::sqrt((T)2);
+      for_interior([&](Rank<T>& R, int k, int j, int i) { set_cell(R, k, j, i, {v, v}); });
+      ringpair(0, 0, 0, ring_rad, false);
+    } else if (nm == "linked_rings") {  // initial.f90:587-626
+      ringpair(0, 0, 0, ring_rad, true);
+      ringpair(1, 0, ring_rad * (T)1.2, ring_rad, false);
+    } else if (nm == "random_phase") {  // setup_quench, initial.f90:346-375
+      for (int kk = 1; kk <= 20; ++kk) {
+        T k1 = std::floor(runif(-20, 20)), k2 = std::floor(runif(-20, 20)), k3 = std::floor(runif(-20, 20));
+        T a1 = runif((T)(-0.1), (T)0.1), a2 = runif((T)(-0.1), (T)0.1);
+        for_interior([&](Rank<T>& R, int k, int j, int i) {
+          T sarg = R.xx[i] * k1 + R.yy[j] * k2;
+          if (!p.two_dim) sarg = sarg + R.zz[k] * k3;
+          T ph = sarg * (T)2 * pi / Lx;
+          C<T> e = cexpi(ph);
+          cell(R, k, j, i) = cadd(cell(R, k, j, i), cmul(C<T>{a1, a2}, e));
+        });
+      }
+      tf_mul();
+    } else if (nm == "add_noise") {  // initial.f90:741-757, seeded per-cell uniforms
+      uint64_t sd = a ? a->seed : 0;
+      for_interior([&](Rank<T>& R, int k, int j, int i) {
+        int I = R.cx * R.nmx + (i - 1), J = R.cy * R.nmy + (j - 1);
+        uint64_t gi = ((uint64_t)I * p.ny + J) * p.nz + (k - 1);
+        T e1 = (T)cell_uniform(sd, gi, 0) * (T)2 - (T)1, e2 = (T)cell_uniform(sd, gi, 1) * (T)2 - (T)1;
+        cell(R, k, j, i) = cadd(cell(R, k, j, i), C<T>{(T)0.01 * e1, (T)0.01 * e2});
+      });
+    } else if (nm == "add_ring") {  // setup_add_ring option 1, initial.f90:759-794
+      ringpair(0, (T)(-0.25) * Lx, 0, ring_rad, false);
+    } else if (nm == "add_dipole") {  // initial.f90:839-870
+      vortex_mul((T)(-20), (T)5, (T)1, 0);
+      vortex_mul((T)(-20), (T)(-5), (T)(-1), 0);
+    } else if (nm == "phase_imprint") {  // initial.f90:820-836
+      for_interior([&](Rank<T>& R, int k, int j, int i) {
+        T dense = cabs_(cell(R, k, j, i));
+        T th = std::atan2(R.yy[j], R.xx[i]);
+        set_cell(R, k, j, i, cscale(dense, cexpi((T)wn * th)));
+      });
+    } else if (nm == "add_pcurrent") {  // initial.f90:669-739
+      const int pk = p.potential;
+      for_interior([&](Rank<T>& R, int k, int j, int i) {
+        T x = R.xx[i], y = R.yy[j], th = 0, m = 1;
+        if (pk == TRAPBEC_POT_BARRIER) th = y < (T)0 ? x * (T)50 * pi / Lx : (T)20 * pi - x * (T)50 * pi / Lx;
+        else if (pk == TRAPBEC_POT_MOBIUS) th = (T)20 * std::atan2(y, x);
+        else if (pk == TRAPBEC_POT_HARMONIC_RING) {
+          T a1 = x / Lx, b1 = y / Lx;
+          T r = std::sqrt(a1 * a1 + b1 * b1);
+          th = r < (T)0.3 ? std::atan2(y, x) : std::atan2(-y, x);
+          m = 10;
+        } else if (pk == TRAPBEC_POT_HARMONIC_RING2) {
+          th = y < (T)0 ? std::atan2((T)0.5 * (y + Ly / (T)5), x) : std::atan2((T)0.5 * (y - Ly / (T)5), x) - pi;
+          m = 20;
+        } else if (pk == TRAPBEC_POT_CHANNEL) {
+          th = (T)10 * (T)2 * pi * (x + (T)0.5 * Lx) / Lx;
+          m = 2;
+        } else {
+          return;
+        }
+        T ld = cabs_(cell(R, k, j, i));
+        set_cell(R, k, j, i, cscale(ld, cexpi(m * th)));
+      });
     } else if (nm == "tf_vortex_line" || nm == "tf_vortex_ring" || nm == "tf_noise") {
       // States of the workload set (not reference init_cond cases), in the
       // reference's units, evaluated in FP64 and rounded to T:
@@ -774,6 +904,71 @@ template <typename T> struct Oracle {
     const Rank<T>& R = ranks[0];
     for (size_t q = 0; q < R.psi.size(); ++q) { dst[2 * q] = R.psi[q].re; dst[2 * q + 1] = R.psi[q].im; }
   }
+  // ----------------------------------------------------- diagnostic.f90 --
+  // Both diagnostics follow the ghost_comm of run.f90:64 and work per rank on
+  // its ghosted array, whose edge and corner ghosts ghost_comm never writes
+  // (they keep the zeros of initial.f90:27).  Output: [3][nx][ny][nz].
+  static T first_deriv(const T* v, T h) {  // deriv.f90:5-11, v points at vect(0)
+    return (-v[-3] + (T)9 * v[-2] - (T)45 * v[-1] + (T)45 * v[1] - (T)9 * v[2] + v[3]) / ((T)60 * h);
+  }
+  static T real_second_deriv(T m2, T m1, T c, T p1, T p2, T h) {  // deriv.f90:26-32
+    return (-m2 + (T)16 * m1 - (T)30 * c + (T)16 * p1 - p2) / ((T)12 * (h * h));
+  }
+  static T low_first_deriv(T m1, T p1, T h) { return (-m1 + p1) / ((T)2 * h); }  // deriv.f90:33-39
+
+  // get_phase (diagnostic.f90:27-48)
+  void velocity(T* out) {
+    ghost_comm();
+    const size_t n = (size_t)p.nx * p.ny * p.nz;
+    for (auto& R : ranks) {
+      std::vector<T> ph(R.psi.size());
+      for (size_t q = 0; q < ph.size(); ++q) ph[q] = std::atan2(R.psi[q].im, R.psi[q].re);
+      std::vector<T> lx(7), ly(7);
+      for (int i = 1; i <= R.nmx; ++i)
+        for (int j = 1; j <= R.nmy; ++j)
+          for (int k = 1; k <= R.nmz; ++k) {
+            for (int m = -3; m <= 3; ++m) {
+              lx[m + 3] = ph[R.g(k, j, i + m)];
+              ly[m + 3] = ph[R.g(k, j + m, i)];
+            }
+            const size_t q = gidx(k - 1, R.cy * R.nmy + j - 1, R.cx * R.nmx + i - 1);
+            out[q] = first_deriv(&lx[3], hx);
+            out[n + q] = first_deriv(&ly[3], hy);
+            out[2 * n + q] = first_deriv(&ph[R.g(k, j, i)], hz);   // z is contiguous
+          }
+    }
+  }
+
+  // get_qpressure (diagnostic.f90:50-84)
+  void qpressure(T* out) {
+    ghost_comm();
+    const size_t n = (size_t)p.nx * p.ny * p.nz;
+    for (auto& R : ranks) {
+      std::vector<T> den(R.psi.size());
+      for (size_t q = 0; q < den.size(); ++q) den[q] = std::hypot(R.psi[q].re, R.psi[q].im);
+      const int ex = R.nmx + 2, ey = R.nmy + 2, ez = R.nmz + 2;   // laplace_rho(0:nmz+1, 0:nmy+1, 0:nmx+1)
+      std::vector<T> lap((size_t)ex * ey * ez);
+      auto L = [&](int k, int j, int i) -> T& { return lap[((size_t)i * ey + j) * ez + k]; };
+      auto d = [&](int k, int j, int i) { return den[R.g(k, j, i)]; };
+      for (int i = 0; i <= R.nmx + 1; ++i)
+        for (int j = 0; j <= R.nmy + 1; ++j)
+          for (int k = 0; k <= R.nmz + 1; ++k) {
+            T v = real_second_deriv(d(k, j, i - 2), d(k, j, i - 1), d(k, j, i), d(k, j, i + 1), d(k, j, i + 2), hx);
+            v = v + real_second_deriv(d(k, j - 2, i), d(k, j - 1, i), d(k, j, i), d(k, j + 1, i), d(k, j + 2, i), hy);
+            v = v + real_second_deriv(d(k - 2, j, i), d(k - 1, j, i), d(k, j, i), d(k + 1, j, i), d(k + 2, j, i), hz);
+            L(k, j, i) = v;
+          }
+      for (int i = 1; i <= R.nmx; ++i)
+        for (int j = 1; j <= R.nmy; ++j)
+          for (int k = 1; k <= R.nmz; ++k) {
+            const size_t q = gidx(k - 1, R.cy * R.nmy + j - 1, R.cx * R.nmx + i - 1);
+            out[q] = low_first_deriv(L(k, j, i - 1), L(k, j, i + 1), hx);
+            out[n + q] = low_first_deriv(L(k, j - 1, i), L(k, j + 1, i), hy);
+            out[2 * n + q] = low_first_deriv(L(k - 1, j, i), L(k + 1, j, i), hz);
+          }
+    }
+  }
+
   void set_trap(const double* tr) {
     for_interior([&](Rank<T>& R, int k, int j, int i) {
       int I = R.cx * R.nmx + (i - 1), J = R.cy * R.nmy + (j - 1);
@@ -847,6 +1042,16 @@ int orc_get_rhs(void* h, void* out) {
   return dispatch((Handle*)h, [&](auto& o) {
     using T = std::remove_reference_t<decltype(o.t)>;
     o.get_rhs_out((T*)out); return 0; });
+}
+int orc_velocity(void* h, void* out) {
+  return dispatch((Handle*)h, [&](auto& o) {
+    using T = std::remove_reference_t<decltype(o.t)>;
+    o.velocity((T*)out); return 0; });
+}
+int orc_qpressure(void* h, void* out) {
+  return dispatch((Handle*)h, [&](auto& o) {
+    using T = std::remove_reference_t<decltype(o.t)>;
+    o.qpressure((T*)out); return 0; });
 }
 int orc_set_trap(void* h, const double* tr) {
   return dispatch((Handle*)h, [&](auto& o) { o.set_trap(tr); return 0; });

@@ -177,7 +177,27 @@ def test_imag_rk3_renorm_matches_oracle():
 
 
 INIT_STATES = ["constant", "thomas_fermi", "soliton", "single_vortex", "sausage", "crow", "random_points",
-               "leap_frog", "vortex_rings"]
+               "leap_frog", "vortex_rings", "lattice", "lattice2", "bundle", "line_of_lines", "linked_rings",
+               "random_phase"]
+
+
+@pytest.mark.parametrize("helper,pot", [("add_noise", "harmonic"), ("add_ring", "harmonic"),
+                                        ("add_dipole", "harmonic"), ("phase_imprint", "harmonic"),
+                                        ("add_pcurrent", "barrier"), ("add_pcurrent", "channel"),
+                                        ("add_pcurrent", "harmonic_ring")])
+def test_state_helpers(helper, pot):
+    """Helpers act on the current state (initial.f90:669-870)."""
+    p = params(n=(24, 24, 16), L=(60.0, 60.0, 30.0), harm=(3.0, 4.0, 5.0), pot=pot)
+    p.winding_number = 3
+    p.ring_rad = 6.0
+    s, o = Solver(p), Oracle(p)
+    a = InitArgs()
+    a.seed = 5
+    s.init_state("thomas_fermi")
+    o.init_state("thomas_fermi", a)
+    s.init_state(helper, seed=5)
+    o.init_state(helper, a)
+    assert rel_err(s.get_psi(), o.get_psi()) < 1e-13
 
 
 @pytest.mark.parametrize("name", INIT_STATES)
@@ -273,3 +293,31 @@ def test_var_and_restart_files(tmp_path):
         nstart = s2.read_restart(d)
         assert nstart == 301 and s2.t == 1.25
         assert np.array_equal(s2.get_psi(), psi)
+
+
+DIAG_CASES = [(abi.FP64, abi.BC_ZERO, 0, (1, 1)), (abi.FP64, abi.BC_ZERO, 0, (2, 2)),
+              (abi.FP64, abi.BC_PERIODIC, 0, (1, 2)), (abi.FP64, abi.BC_SOLID, 1, (2, 1)),
+              (abi.FP32, abi.BC_ZERO, 0, (1, 1)), (abi.FP32, abi.BC_PERIODIC, 0, (2, 2))]
+
+
+@pytest.mark.parametrize("prec,bc,pz,nproc", DIAG_CASES)
+def test_velocity_and_qpressure(prec, bc, pz, nproc):
+    """get_phase velocity and get_qpressure (diagnostic.f90:27-84), after a few
+    RK3 steps, against the oracle: FP64 to 1e-12 of the field's maximum,
+    FP32 to 2e-5 (atan2/hypot of the two libraries differ by an ulp or two;
+    a vortex-free smooth state keeps the phase away from the branch cut's
+    sign ambiguity)."""
+    p = params(n=(24, 32, 20), L=(6.0, 8.0, 5.0), prec=prec, bc=bc, periodicz=pz, nproc=nproc, omega=0.2)
+    rng = np.random.default_rng(17)
+    psi = smooth_state(p, seed=9) + 0.02 * (rng.normal(size=(24, 32, 20)) + 1j * rng.normal(size=(24, 32, 20)))
+    s = Solver(p)
+    s.set_psi(psi)
+    s.step_rt(3)
+    o = Oracle(p)
+    o.set_psi(s.get_psi())
+    tol = FP64_TOL if prec == abi.FP64 else 2e-5
+    for got, want in ((s.velocity(), o.velocity()), (s.qpressure(), o.qpressure())):
+        assert got.shape == (3, 24, 32, 20)
+        assert np.all(np.isfinite(got))
+        err = np.abs(got.astype(np.float64) - want.astype(np.float64))
+        assert err.max() <= tol * np.abs(want).max(), err.max()

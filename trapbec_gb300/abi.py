@@ -132,6 +132,8 @@ _PROTOS = {
     "trapbec_step_imag": (C.c_int, [_VP, C.c_int, C.c_int, C.c_double,
                                     C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     "trapbec_diag": (C.c_int, [_VP, C.POINTER(DiagOut)]),
+    "trapbec_get_velocity": (C.c_int, [_VP, _VP]),
+    "trapbec_get_qpressure": (C.c_int, [_VP, _VP]),
     "trapbec_set_scalar": (C.c_int, [_VP, C.c_int, C.c_double]),
     "trapbec_get_scalar": (C.c_int, [_VP, C.c_int, C.POINTER(C.c_double)]),
     "trapbec_set_kernel": (C.c_int, [_VP, C.c_int, C.c_int, C.c_int]),

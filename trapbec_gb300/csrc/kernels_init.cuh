@@ -125,7 +125,8 @@ __global__ void fill_potential_kernel(PotArgs<T> a) {
 enum InitKind : int {
   IK_CONST = 0, IK_TF = 1, IK_SOLITON_PHASE = 2, IK_VORTEX_MUL = 3, IK_SINGLE = 4,
   IK_SAUSAGE = 5, IK_CROW = 6, IK_RING_MUL = 7, IK_TF_LINE = 8, IK_TF_RING = 9, IK_TF_NOISE = 10,
-  IK_SET = 11
+  IK_SET = 11, IK_TF_MUL = 12, IK_RINGPAIR_MUL = 13, IK_QUENCH_ADD = 14, IK_PHASE_IMPRINT = 15,
+  IK_NOISE_ADD = 16, IK_PCURRENT = 17
 };
 
 template <typename T> struct InitArgsDev {
@@ -199,11 +200,89 @@ __global__ void init_state_kernel(InitArgsDev<T> a) {
         c_t<T> p2 = mk<T>(f * cos(th), f * sin(th));
         out = cmul_<T>(p1, p2);
       } break;
-      case IK_VORTEX_MUL: {  // psi *= func(r) e^{i dir theta}, v = (vx, vy, dir)
-        T dx = x - a.v[0], dy = y - a.v[1];
+      case IK_VORTEX_MUL: {  // psi *= func(r) e^{i dir theta}; v = (p1, p2, dir, plane)
+        // plane 0: (x, y), 1: (x, z), 2: (y, z)  (initial.f90:109-121, 455-457, 530-531)
+        const int pl = (int)a.v[3];
+        const T c1 = pl == 2 ? y : x, c2 = pl == 0 ? y : z;
+        T dx = c1 - a.v[0], dy = c2 - a.v[1];
         T f = vortex_func(sqrt(dx * dx + dy * dy));
         T th = a.v[2] * atan2(dy, dx);
         out = cmul_<T>(out, mk<T>(f * cos(th), f * sin(th)));
+      } break;
+      case IK_TF_MUL: {  // multiply_thomas_fermi, initial.f90:654-667
+        T p = x / a.Lx, q = y / a.Ly, s = z / a.Lz;
+        T d = (T)1 - a.harm_wx * (p * p) - a.harm_wy * (q * q) - a.harm_wz * (s * s);
+        if (d < (T)0) d = 0;
+        out = mk<T>(out.x * d, out.y * d);
+      } break;
+      case IK_RINGPAIR_MUL: {
+        // Pade vortex pair of a ring (ring_density, initial.f90:628-635): axis
+        // coordinate u (x if v[0] = 0, y if 1) shifted by v[1]; in-plane radius
+        // sqrt(w^2 + (z - v[2])^2) with w the other of x, y; radius v[3]
+        // (initial.f90:575-581, 602-622, 775-781).  v[4] = 1: assign instead of multiply.
+        const T u = (a.v[0] == (T)0 ? x : y) - a.v[1];
+        const T ww = a.v[0] == (T)0 ? y : x;
+        const T zz2 = z - a.v[2];
+        const T s = sqrt(ww * ww + zz2 * zz2);
+        const T R0 = a.v[3];
+        const T c1 = (T)11 / (T)32;
+        const T c3 = ((T)5 - (T)32 * c1) / ((T)48 - (T)192 * c1);
+        const T c2 = c1 * (c3 - (T)0.25);
+        auto rd = [&](T r) {
+          T r2 = r * r;
+          return sqrt(r2 * (c1 + c2 * r2) / ((T)1 + c3 * r2 + c2 * (r2 * r2)));
+        };
+        T th = atan2(u, s + R0);
+        T r = sqrt(u * u + (s + R0) * (s + R0));
+        const c_t<T> p1 = mk<T>(rd(r) * cos(th), rd(r) * sin(th));
+        th = atan2(u, s - R0);
+        r = sqrt(u * u + (s - R0) * (s - R0));
+        const c_t<T> p2 = mk<T>(rd(r) * cos(th), -(rd(r) * sin(th)));
+        const c_t<T> pr = cmul_<T>(p1, p2);
+        out = a.v[4] != (T)0 ? pr : cmul_<T>(out, pr);
+      } break;
+      case IK_QUENCH_ADD: {  // setup_quench wave, initial.f90:362-372; v = (k1, k2, k3, ra1, ra2)
+        T sarg = x * a.v[0] + y * a.v[1];
+        if (!a.wn) sarg = sarg + z * a.v[2];   // wn carries two_dim here
+        const T ph = sarg * (T)2 * a.pi / a.Lx;
+        const c_t<T> e = mk<T>(cos(ph), sin(ph));
+        out = mk<T>(out.x + (a.v[3] * e.x - a.v[4] * e.y), out.y + (a.v[3] * e.y + a.v[4] * e.x));
+      } break;
+      case IK_PHASE_IMPRINT: {  // initial.f90:820-836
+        const T dense = hypot(out.x, out.y);
+        const T th = atan2(y, x);
+        const T ph = (T)a.wn * th;
+        out = mk<T>(dense * cos(ph), dense * sin(ph));
+      } break;
+      case IK_NOISE_ADD: {  // add_noise, initial.f90:741-757, per-cell seeded uniforms
+        const T e1 = (T)cell_uniform(a.seed, (uint64_t)idx, 0) * (T)2 - (T)1;
+        const T e2 = (T)cell_uniform(a.seed, (uint64_t)idx, 1) * (T)2 - (T)1;
+        out = mk<T>(out.x + (T)0.01 * e1, out.y + (T)0.01 * e2);
+      } break;
+      case IK_PCURRENT: {  // setup_pcurrent, initial.f90:669-739; v[0] = potential kind
+        const int pk = (int)a.v[0];
+        T th = 0, m = 1;
+        if (pk == TRAPBEC_POT_BARRIER) {
+          th = y < (T)0 ? x * (T)50 * a.pi / a.Lx : (T)20 * a.pi - x * (T)50 * a.pi / a.Lx;
+        } else if (pk == TRAPBEC_POT_MOBIUS) {
+          th = (T)20 * atan2(y, x);
+        } else if (pk == TRAPBEC_POT_HARMONIC_RING) {
+          const T p = x / a.Lx, q = y / a.Lx;
+          const T r = sqrt(p * p + q * q);
+          th = r < (T)0.3 ? atan2(y, x) : atan2(-y, x);
+          m = 10;
+        } else if (pk == TRAPBEC_POT_HARMONIC_RING2) {
+          th = y < (T)0 ? atan2((T)0.5 * (y + a.Ly / (T)5), x) : atan2((T)0.5 * (y - a.Ly / (T)5), x) - a.pi;
+          m = 20;
+        } else if (pk == TRAPBEC_POT_CHANNEL) {
+          th = (T)10 * (T)2 * a.pi * (x + (T)0.5 * a.Lx) / a.Lx;
+          m = 2;
+        } else {
+          break;
+        }
+        const T ld = hypot(out.x, out.y);
+        const T ph = m * th;
+        out = mk<T>(ld * cos(ph), ld * sin(ph));
       } break;
       case IK_RING_MUL: {  // setup_vortex_rings body, initial.f90:239-254
         const T ax = a.v[0], ay = a.v[1], az = a.v[2], tx = a.v[3], ty = a.v[4], tz = a.v[5], rr0 = a.v[6];

@@ -27,6 +27,7 @@
 #include "kernels_simple.cuh"
 #include "tiled_api.h"
 #include "imag_ctrl.cuh"
+#include "kernels_diag.cuh"
 
 using namespace tb;
 
@@ -178,7 +179,7 @@ template <typename T> StageArgs<T> base_args(trapbec_ctx* c, double t) {
   a.trap = (const T*)c->trap_eff;
   a.nx = p.nx; a.ny = p.ny; a.nz = p.nz;
   a.bc = p.boundaries;
-  a.zper = (p.periodicz || p.boundaries == TRAPBEC_BC_PERIODIC) ? 1 : 0;
+  a.zper =(p.periodicz || p.boundaries == TRAPBEC_BC_PERIODIC) ? 1 : 0;
   a.two_dim = p.two_dim ? 1 : 0;
   a.pot_mode = pot_mode_at<T>(c, t);
   T hx = (T)p.lx / (T)p.nx, hy = (T)p.ly / (T)p.ny, hz = (T)p.lz / (T)p.nz;  // initial.f90:26
@@ -529,9 +530,72 @@ template <typename T> int init_state_impl(trapbec_ctx* c, const char* name, cons
         else if (v == 3) { vx = -sh; vy = -s1; dir = -1; }
         else { vx = sh; vy = -s2; dir = -1; }
       }
-      a.v[0] = vx; a.v[1] = vy; a.v[2] = dir;
+      a.v[0] = vx; a.v[1] = vy; a.v[2] = dir; a.v[3] = 0;
       if ((rc = go(IK_VORTEX_MUL))) return rc;
     }
+  } else if (nm == "lattice") {  // initial.f90:377-420 (ramp = 0: straight lines)
+    a.v[0] = 1; a.v[1] = 1;
+    if ((rc = go(IK_SET))) return rc;
+    for (int v1 = 1; v1 <= 10; ++v1)
+      for (int v2 = 1; v2 <= 10; ++v2) {
+        (void)runif(0, (T)2 * pi);   // rphase
+        (void)runif(0, 1);           // rdir
+        a.v[0] = (T)v1 * ((T)p.lx / (T)16) - (T)p.lx / (T)3;
+        a.v[1] = (T)v2 * ((T)p.ly / (T)16) - (T)p.ly / (T)3;
+        a.v[2] = 1; a.v[3] = 0;
+        if ((rc = go(IK_VORTEX_MUL))) return rc;
+      }
+  } else if (nm == "lattice2" || nm == "bundle") {  // initial.f90:422-539
+    if ((rc = go(IK_TF))) return rc;
+    if (nm == "lattice2") {
+      for (int pl = 0; pl < 2; ++pl)
+        for (int v1 = 1; v1 <= 3; ++v1)
+          for (int v2 = 1; v2 <= 3; ++v2) {
+            if (pl == 0) {
+              a.v[0] = (T)v1 * ((T)p.lx / (T)4) - (T)p.lx / (T)2;
+              a.v[1] = (T)v2 * ((T)p.ly / (T)4) - (T)p.ly / (T)2;
+            } else {
+              a.v[0] = (T)v1 * ((T)p.lx / (T)4) + (T)10 - (T)p.lx / (T)2;
+              a.v[1] = (T)v2 * ((T)p.lz / (T)4) + (T)10 - (T)p.lz / (T)2;
+            }
+            a.v[2] = 1; a.v[3] = (T)pl;
+            if ((rc = go(IK_VORTEX_MUL))) return rc;
+          }
+    } else {
+      for (int pl = 0; pl < 3; ++pl)
+        for (int v1 = 1; v1 <= 7; ++v1) {
+          T rpos = v1 == 1 ? (T)0 : (T)10;
+          T tpos = v1 == 1 ? (T)0 : (T)(v1 - 2) * (T)2 * pi / (T)6;
+          T c1 = rpos * std::cos(tpos), c2 = rpos * std::sin(tpos);
+          if (pl == 0 || pl == 2) c1 = c1 - (T)30; else c2 = c2 - (T)30;
+          a.v[0] = c1; a.v[1] = c2; a.v[2] = 1; a.v[3] = (T)pl;
+          if ((rc = go(IK_VORTEX_MUL))) return rc;
+        }
+    }
+  } else if (nm == "line_of_lines") {  // initial.f90:541-585
+    a.v[0] = a.v[1] = (T)1 / std::sqrt((T)2);
+    if ((rc = go(IK_SET))) return rc;
+    a.v[0] = 0; a.v[1] = 0; a.v[2] = 0; a.v[3] = (T)p.ring_rad; a.v[4] = 0;
+    rc = go(IK_RINGPAIR_MUL);
+  } else if (nm == "linked_rings") {  // initial.f90:587-626
+    a.v[0] = 0; a.v[1] = 0; a.v[2] = 0; a.v[3] = (T)p.ring_rad; a.v[4] = 1;
+    if ((rc = go(IK_RINGPAIR_MUL))) return rc;
+    a.v[0] = 1; a.v[1] = 0; a.v[2] = (T)p.ring_rad * (T)1.2; a.v[3] = (T)p.ring_rad; a.v[4] = 0;
+    rc = go(IK_RINGPAIR_MUL);
+  } else if (nm == "random_phase") {  // setup_quench, initial.f90:346-375
+    a.v[0] = 0; a.v[1] = 0;
+    if ((rc = go(IK_SET))) return rc;
+    a.wn = p.two_dim ? 1 : 0;
+    for (int kk = 1; kk <= 20; ++kk) {
+      a.v[0] = std::floor(runif(-20, 20));
+      a.v[1] = std::floor(runif(-20, 20));
+      a.v[2] = std::floor(runif(-20, 20));
+      a.v[3] = runif((T)(-0.1), (T)0.1);
+      a.v[4] = runif((T)(-0.1), (T)0.1);
+      if ((rc = go(IK_QUENCH_ADD))) return rc;
+    }
+    a.wn = p.winding_number;
+    rc = go(IK_TF_MUL);
   } else if (nm == "vortex_rings") {
     a.v[0] = 1; a.v[1] = 0;
     if ((rc = go(IK_SET))) return rc;
@@ -550,6 +614,22 @@ template <typename T> int init_state_impl(trapbec_ctx* c, const char* name, cons
     a.d[4] = ia->ring_radius; a.d[5] = ia->core2; a.d[6] = ia->noise_amp;
     a.seed = ia->seed;
     rc = go(nm == "tf_vortex_line" ? IK_TF_LINE : (nm == "tf_vortex_ring" ? IK_TF_RING : IK_TF_NOISE));
+  } else if (nm == "add_noise") {  // helpers applied to the current state
+    a.seed = ia ? ia->seed : 0;
+    rc = go(IK_NOISE_ADD);
+  } else if (nm == "add_ring") {  // setup_add_ring option 1, initial.f90:759-794
+    a.v[0] = 0; a.v[1] = (T)(-0.25) * (T)p.lx; a.v[2] = 0; a.v[3] = (T)p.ring_rad; a.v[4] = 0;
+    rc = go(IK_RINGPAIR_MUL);
+  } else if (nm == "add_dipole") {  // setup_add_dipole, initial.f90:839-870
+    for (int v = 1; v <= 2; ++v) {
+      a.v[0] = -20; a.v[1] = v == 1 ? (T)5 : (T)(-5); a.v[2] = v == 1 ? (T)1 : (T)(-1); a.v[3] = 0;
+      if ((rc = go(IK_VORTEX_MUL))) return rc;
+    }
+  } else if (nm == "phase_imprint") {  // initial.f90:820-836
+    rc = go(IK_PHASE_IMPRINT);
+  } else if (nm == "add_pcurrent") {  // setup_pcurrent, initial.f90:669-739
+    a.v[0] = (T)p.potential;
+    rc = go(IK_PCURRENT);
   } else {
     set_error("unknown initial state: " + nm);   // initial.f90:155-156
     return TRAPBEC_ERR_ARG;
@@ -888,6 +968,46 @@ extern "C" {
 int trapbec_diag(trapbec_ctx* c, trapbec_diag_out* out) {
   if (!c || !out) return TRAPBEC_ERR_ARG;
   return DISPATCH(c, diag_impl, c, out);
+}
+
+}  // extern "C"
+namespace {
+template <typename T> int field_diag_impl(trapbec_ctx* c, void* out, int which) {
+  int rc = apply_pending_scale<T>(c);
+  if (rc) return rc;
+  const trapbec_params& p = c->p;
+  DiagFieldArgs<T> a;
+  a.psi = (const c_t<T>*)c->psi[c->cur];
+  a.nx = p.nx; a.ny = p.ny; a.nz = p.nz;
+  a.nmx = p.nx / (p.nprocx > 0 ? p.nprocx : 1);
+  a.nmy = p.ny / (p.nprocy > 0 ? p.nprocy : 1);
+  a.bc = p.boundaries;
+  a.bcz = (p.periodicz || p.boundaries == TRAPBEC_BC_PERIODIC) ? TRAPBEC_BC_PERIODIC : p.boundaries;
+  a.hx = (T)p.lx / (T)p.nx; a.hy = (T)p.ly / (T)p.ny; a.hz = (T)p.lz / (T)p.nz;   // initial.f90:26
+  void* buf = nullptr;
+  CK(cudaMalloc(&buf, 3 * c->n * sizeof(T)));
+  a.out = (T*)buf;
+  if (which == 0) velocity_kernel<T><<<simple_grid(c), SIMPLE_THREADS, 0, c->st>>>(a);
+  else qpressure_kernel<T><<<simple_grid(c), SIMPLE_THREADS, 0, c->st>>>(a);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out, buf, 3 * c->n * sizeof(T), cudaMemcpyDeviceToHost, c->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+  cudaFree(buf);
+  c->launches++;
+  if (e != cudaSuccess) { set_error(std::string("diagnostic field: ") + cudaGetErrorString(e)); return TRAPBEC_ERR_CUDA; }
+  return TRAPBEC_OK;
+}
+}  // namespace
+extern "C" {
+
+int trapbec_get_velocity(trapbec_ctx* c, void* vel_out) {
+  if (!c || !vel_out) return TRAPBEC_ERR_ARG;
+  return DISPATCH(c, field_diag_impl, c, vel_out, 0);
+}
+
+int trapbec_get_qpressure(trapbec_ctx* c, void* qp_out) {
+  if (!c || !qp_out) return TRAPBEC_ERR_ARG;
+  return DISPATCH(c, field_diag_impl, c, qp_out, 1);
 }
 
 int trapbec_set_scalar(trapbec_ctx* c, int which, double v) {

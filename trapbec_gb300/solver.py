@@ -104,6 +104,18 @@ class Solver:
         check(self.lib.trapbec_diag(self.ctx, C.byref(d)), "trapbec_diag")
         return d.as_dict()
 
+    def velocity(self) -> np.ndarray:
+        """vel of get_phase (diagnostic.f90:27-48), shape (3, Nx, Ny, Nz)."""
+        a = np.empty((3,) + self.shape, dtype=self.rdtype)
+        check(self.lib.trapbec_get_velocity(self.ctx, a.ctypes.data), "trapbec_get_velocity")
+        return a
+
+    def qpressure(self) -> np.ndarray:
+        """qpressure of get_qpressure (diagnostic.f90:50-84), shape (3, Nx, Ny, Nz)."""
+        a = np.empty((3,) + self.shape, dtype=self.rdtype)
+        check(self.lib.trapbec_get_qpressure(self.ctx, a.ctypes.data), "trapbec_get_qpressure")
+        return a
+
     def psi_norm(self) -> float:
         """intPsi2 of Psi_norm (diagnostic.f90:19-25), summed in FP64."""
         return self.diag()["intpsi2"]
