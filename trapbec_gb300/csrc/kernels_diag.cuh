@@ -39,7 +39,9 @@ __device__ __forceinline__ c_t<T> ghosted(const DiagFieldArgs<T>& a, RankBox rb,
   const int ok = (k < 0 || k >= a.nz);
   if (oi + oj + ok > 1) return mk<T>((T)0, (T)0);   // edge / corner ghost: never written
   const int ii = map_ghost(i, a.nx, a.bc), jj = map_ghost(j, a.ny, a.bc), kk = map_ghost(k, a.nz, a.bcz);
-  if ((ii | jj | kk) < 0) return mk<T>((T)0, (T)0);
+  // zero-rule ghosts map to -1; tiny extents (nz = 1 in 2D runs) can map
+  // past the far end: both read as zero instead of leaving the array
+  if ((ii | jj | kk) < 0 || ii >= a.nx || jj >= a.ny || kk >= a.nz) return mk<T>((T)0, (T)0);
   return a.psi[((size_t)ii * a.ny + jj) * a.nz + kk];
 }
 
