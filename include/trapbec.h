@@ -81,6 +81,11 @@ enum trapbec_layout {
   TRAPBEC_LAYOUT_GHOSTED = 1   /* Psi(-2:nz+3,-2:ny+3,-2:nx+3), initial.f90:16 */
 };
 
+enum trapbec_field {           /* output-time diagnostic fields               */
+  TRAPBEC_FIELD_VELOCITY = 0,  /* vel of get_phase, diagnostic.f90:27-48       */
+  TRAPBEC_FIELD_QPRESSURE = 1  /* qpressure of get_qpressure, diagnostic.f90:50-84 */
+};
+
 enum trapbec_imag_variant {
   TRAPBEC_IMAG_REF_EULER = 0,  /* Psi = Psi + dt*0.5*rhs, no renorm, run.f90:19-35 */
   TRAPBEC_IMAG_RK3_RENORM = 1  /* low-storage RK3 in imaginary time + FP64
@@ -257,6 +262,10 @@ int trapbec_last_kernel_ms(trapbec_ctx* ctx, double* ms);
 int trapbec_write_var(trapbec_ctx* ctx, const char* datadir, int itime, int shots,
                       double t, int imaginary);
 int trapbec_write_restart(trapbec_ctx* ctx, const char* datadir, int itime, double t);
+/* Write data/proc000/vel##.dat or qpress##.dat (one record: coords(2) int32,
+ * the field as vel(1:nz,1:ny,1:nx,3)), as var_print does when vel_print /
+ * qpress_print are set (output.f90:80-91); ## is itime/shots in i2.2.      */
+int trapbec_write_field(trapbec_ctx* ctx, const char* datadir, int itime, int shots, int which);
 /* Read var.dat (proc000, or proc00 as the reference reader expects).        */
 int trapbec_read_restart(trapbec_ctx* ctx, const char* datadir, int* nstart, double* t);
 int trapbec_write_dims(const trapbec_params* p, const char* datadir);

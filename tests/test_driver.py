@@ -84,3 +84,25 @@ def test_driver_run_restart_matches_api(tmp_path):
     assert np.array_equal(s.get_psi(), psi50)
     timing = (tmp_path / "data" / "timing.log").read_text().split()
     assert int(timing[0]) == 16 ** 3 and float(timing[2]) > 0
+
+
+@pytest.mark.gpu
+def test_driver_vel_and_qpress_files(tmp_path):
+    """vel_print / qpress_print: vel##.dat and qpress##.dat after each block
+    (run.f90:64-66, output.f90:80-91), equal to the API's fields."""
+    from trapbec_gb300 import Solver, parse_cparam
+    text = CPARAM.format(nsteps=20) + "logical, parameter :: vel_print=.true.\nlogical, parameter :: qpress_print=.true.\n"
+    r = _run(tmp_path, text)
+    assert r.returncode == 0, r.stdout + r.stderr
+    p = parse_cparam(text)
+    p.precision = abi.FP32
+    s = Solver(p)
+    s.init_state("single_vortex")
+    s.step_rt(20)
+    for name, want in (("vel02.dat", s.velocity()), ("qpress02.dat", s.qpressure())):
+        raw = (tmp_path / "data" / "proc000" / name).read_bytes()
+        n = struct.unpack("<i", raw[:4])[0]
+        assert n == 8 + 4 * want.size and struct.unpack("<i", raw[-4:])[0] == n
+        assert struct.unpack("<2i", raw[4:12]) == (0, 0)
+        got = np.frombuffer(raw[12:12 + 4 * want.size], dtype=np.float32).reshape(want.shape)
+        assert np.array_equal(got, want)

@@ -31,6 +31,7 @@ POT_ZERO, POT_HARMONIC, POT_MOBIUS, POT_ARRAY = 0, 1, 9, 10
 
 FP32, FP64 = 0, 1
 LAYOUT_INTERIOR, LAYOUT_GHOSTED = 0, 1
+FIELD_VELOCITY, FIELD_QPRESSURE = 0, 1
 IMAG_REF_EULER, IMAG_RK3_RENORM = 0, 1
 
 SCALAR_OMEGA_Z, SCALAR_DT_RE, SCALAR_DT_IM, SCALAR_GAMMA = 0, 1, 2, 3
@@ -144,6 +145,7 @@ _PROTOS = {
     "trapbec_last_kernel_ms": (C.c_int, [_VP, C.POINTER(C.c_double)]),
     "trapbec_write_var": (C.c_int, [_VP, C.c_char_p, C.c_int, C.c_int, C.c_double, C.c_int]),
     "trapbec_write_restart": (C.c_int, [_VP, C.c_char_p, C.c_int, C.c_double]),
+    "trapbec_write_field": (C.c_int, [_VP, C.c_char_p, C.c_int, C.c_int, C.c_int]),
     "trapbec_read_restart": (C.c_int, [_VP, C.c_char_p, C.POINTER(C.c_int),
                                        C.POINTER(C.c_double)]),
     "trapbec_write_dims": (C.c_int, [C.POINTER(Params), C.c_char_p]),

@@ -30,6 +30,7 @@ struct Rng {
 int parse_cparam_text(const char* text, trapbec_params* p,
                       std::vector<std::pair<std::string, std::string>>* rest, char* errbuf, size_t errlen);
 bool mkdirs(const std::string& d);
+int write_field_file(const std::string& path, const void* data, size_t bytes);
 int write_var_file(const std::string& path, const trapbec_params* p, double t, const void* psi,
                    size_t psi_bytes);
 int write_restart_file(const std::string& path, const trapbec_params* p, int itime, double t,

@@ -301,6 +301,18 @@ int write_var_file(const std::string& path, const trapbec_params* p, double t, c
   return TRAPBEC_OK;
 }
 
+int write_field_file(const std::string& path, const void* data, size_t bytes) {
+  size_t sl = path.find_last_of('/');
+  if (sl != std::string::npos && !mkdirs(path.substr(0, sl))) { set_error("cannot create " + path); return TRAPBEC_ERR_IO; }
+  FILE* f = std::fopen(path.c_str(), "wb");
+  if (!f) { set_error("cannot open " + path); return TRAPBEC_ERR_IO; }
+  int32_t coords[2] = {0, 0};
+  bool ok = write_record(f, {{coords, 8}, {data, bytes}});   // output.f90:83,89: coords, field
+  ok = (std::fclose(f) == 0) && ok;
+  if (!ok) { set_error("write failed: " + path); return TRAPBEC_ERR_IO; }
+  return TRAPBEC_OK;
+}
+
 int write_restart_file(const std::string& path, const trapbec_params* p, int itime, double t,
                        const void* psi, size_t psi_bytes) {
   size_t sl = path.find_last_of('/');

@@ -1201,6 +1201,24 @@ int trapbec_write_var(trapbec_ctx* c, const char* datadir, int itime, int shots,
   return tbh::write_var_file(std::string(datadir) + name, &c->p, t, buf.data(), buf.size());
 }
 
+int trapbec_write_field(trapbec_ctx* c, const char* datadir, int itime, int shots, int which) {
+  if (!c || !datadir || shots <= 0 || (which != TRAPBEC_FIELD_VELOCITY && which != TRAPBEC_FIELD_QPRESSURE))
+    return TRAPBEC_ERR_ARG;
+  const size_t rsz = c->p.precision == TRAPBEC_FP64 ? 8 : 4;
+  std::vector<char> buf(3 * c->n * rsz);
+  int rc = which == TRAPBEC_FIELD_VELOCITY ? trapbec_get_velocity(c, buf.data()) : trapbec_get_qpressure(c, buf.data());
+  if (rc) return rc;
+  // output.f90:81,87 name the files with an i2.2 edit descriptor, which
+  // prints "**" once itime/shots passes 99
+  const int q = itime / shots;
+  char num[8];
+  if (q >= 0 && q <= 99) std::snprintf(num, sizeof(num), "%02d", q);
+  else std::snprintf(num, sizeof(num), "**");
+  const std::string name = std::string(datadir) + "/proc000/" +
+                           (which == TRAPBEC_FIELD_VELOCITY ? "vel" : "qpress") + num + ".dat";
+  return tbh::write_field_file(name, buf.data(), buf.size());
+}
+
 int trapbec_write_restart(trapbec_ctx* c, const char* datadir, int itime, double t) {
   if (!c || !datadir) return TRAPBEC_ERR_ARG;
   std::vector<char> buf(c->n * c->esz);

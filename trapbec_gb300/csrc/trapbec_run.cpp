@@ -53,6 +53,7 @@ struct RunControl {  // the run-control names of cparam.local (cparam.local:5-44
   int imag_nsteps = 0;
   bool full_binary_output = true;
   bool imaginary_output = false;
+  bool vel_print = false, qpress_print = false;
   bool add_pcurrent = false, add_ring = false, add_dipole = false, forcing = false;
 };
 
@@ -97,6 +98,8 @@ int main(int argc, char** argv) {
     else if (k == "imag_nsteps") rc.imag_nsteps = std::atoi(v.c_str());
     else if (k == "full_binary_output") rc.full_binary_output = as_bool(v);
     else if (k == "imaginary_output") rc.imaginary_output = as_bool(v);
+    else if (k == "vel_print") rc.vel_print = as_bool(v);
+    else if (k == "qpress_print") rc.qpress_print = as_bool(v);
     else if (k == "add_pcurrent") rc.add_pcurrent = as_bool(v);
     else if (k == "add_ring") rc.add_ring = as_bool(v);
     else if (k == "add_dipole") rc.add_dipole = as_bool(v);
@@ -171,7 +174,12 @@ int main(int argc, char** argv) {
       std::printf(" %12d %16.8E %16.8E %16.8E %16.8E %16.8E\n", last / rc.shots, t, d.maxpsi, d.minpsi, d.meanpsi,
                   d.intpsi2);
       if (d.nonfinite) emergency_stop("non-finite values in Psi");
+      // run.f90:64-66 computes the diagnostics, output.f90:73-91 writes them
       if (rc.full_binary_output) check(trapbec_write_var(ctx, datadir.c_str(), last, rc.shots, t, 0), "var_print");
+      if (rc.vel_print)
+        check(trapbec_write_field(ctx, datadir.c_str(), last, rc.shots, TRAPBEC_FIELD_VELOCITY), "get_phase");
+      if (rc.qpress_print)
+        check(trapbec_write_field(ctx, datadir.c_str(), last, rc.shots, TRAPBEC_FIELD_QPRESSURE), "get_qpressure");
       check(trapbec_write_restart(ctx, datadir.c_str(), last, t), "var_print: var.dat");
     }
   }

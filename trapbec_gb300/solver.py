@@ -164,6 +164,11 @@ class Solver:
         check(self.lib.trapbec_write_var(self.ctx, datadir.encode(), int(itime), int(shots),
                                          float(self.t), int(imaginary)), "trapbec_write_var")
 
+    def write_field(self, datadir: str, itime: int, shots: int, which: int) -> None:
+        """vel##.dat / qpress##.dat of var_print (output.f90:80-91)."""
+        check(self.lib.trapbec_write_field(self.ctx, datadir.encode(), int(itime), int(shots), int(which)),
+              "trapbec_write_field")
+
     def write_restart(self, datadir: str, itime: int) -> None:
         check(self.lib.trapbec_write_restart(self.ctx, datadir.encode(), int(itime), float(self.t)),
               "trapbec_write_restart")
