@@ -215,6 +215,18 @@ typedef struct trapbec_diag_out {
 } trapbec_diag_out;
 int trapbec_diag(trapbec_ctx* ctx, trapbec_diag_out* out);
 
+/* Forcing (force_random_points, force.f90:12-54): multiply psi by a Pade
+ * vortex sqrt(r^2 (c1 + c2 r^2) / (1 + c3 r^2 + c2 r^4)) e^{i dir theta},
+ * straight along z through (x0, y0); dir = +1 or -1.
+ * trapbec_force_vortex takes the position and sign; trapbec_force_random_points
+ * draws them as the reference does (x0 ~ U[-Lx/4, Lx/4], y0 ~ U[-Ly/4, Ly/4],
+ * dir = -1 if U[0,1] < 0.5 else +1) from a counter-based stream: draw number
+ * `draw` of `seed` is reproducible on its own (the reference's draws come from
+ * gfortran's random_number and cannot be reproduced).  drawn[3] (optional)
+ * receives (x0, y0, dir).                                                   */
+int trapbec_force_vortex(trapbec_ctx* ctx, double x0, double y0, double dir);
+int trapbec_force_random_points(trapbec_ctx* ctx, uint64_t seed, uint64_t draw, double drawn[3]);
+
 /* Output-time diagnostics of the current psi, written to host memory as
  * 3 x (nx*ny*nz) reals of the context precision, component-major
  * ([3][nx][ny][nz], i.e. Fortran vel(k,j,i,c)):

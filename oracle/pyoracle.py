@@ -46,6 +46,7 @@ def lib() -> C.CDLL:
                   "orc_qpressure"):
             getattr(L, n).argtypes = [vp, vp]
             getattr(L, n).restype = C.c_int
+        L.orc_force_vortex.argtypes = [vp, C.c_double, C.c_double, C.c_double]
         L.orc_set_trap.argtypes = [vp, C.POINTER(C.c_double)]
         L.orc_coords.argtypes = [vp] + [C.POINTER(C.c_double)] * 3
         L.orc_apply_damping.argtypes = [vp]
@@ -114,6 +115,9 @@ class Oracle:
         a = np.empty(self.shape, dtype=self.cdtype)
         assert lib().orc_get_rhs(self.h, a.ctypes.data) == 0
         return a
+
+    def force_vortex(self, x0: float, y0: float, direction: float) -> None:
+        assert lib().orc_force_vortex(self.h, float(x0), float(y0), float(direction)) == 0
 
     def velocity(self) -> np.ndarray:
         """get_phase's vel, shape (3, Nx, Ny, Nz)."""

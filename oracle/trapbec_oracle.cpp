@@ -904,6 +904,25 @@ template <typename T> struct Oracle {
     const Rank<T>& R = ranks[0];
     for (size_t q = 0; q < R.psi.size(); ++q) { dst[2 * q] = R.psi[q].re; dst[2 * q + 1] = R.psi[q].im; }
   }
+  // ---------------------------------------------------------- force.f90 --
+  static T pade_density(T r) {  // force.f90:46-54
+    const T c1 = (T)11 / (T)32;
+    const T c3 = ((T)5 - (T)32 * c1) / ((T)48 - (T)192 * c1);
+    const T c2 = c1 * (c3 - (T)0.25);
+    return std::sqrt((r * r) * (c1 + c2 * (r * r)) / ((T)1 + c3 * (r * r) + c2 * (r * r * r * r)));
+  }
+  // force_random_points body (force.f90:33-44) at a given position and sign
+  void force_vortex(T x0, T y0, T dir) {
+    for_interior([&](Rank<T>& R, int k, int j, int i) {
+      const T r = std::sqrt((R.xx[i] - x0) * (R.xx[i] - x0) + (R.yy[j] - y0) * (R.yy[j] - y0));
+      const T theta = std::atan2(R.yy[j] - y0, R.xx[i] - x0);
+      const T func = pade_density(r);
+      const C<T> f = {func * std::cos(dir * theta), func * std::sin(dir * theta)};
+      C<T>& ps = R.psi[R.g(k, j, i)];
+      ps = cmul(ps, f);
+    });
+  }
+
   // ----------------------------------------------------- diagnostic.f90 --
   // Both diagnostics follow the ghost_comm of run.f90:64 and work per rank on
   // its ghosted array, whose edge and corner ghosts ghost_comm never writes
@@ -1042,6 +1061,11 @@ int orc_get_rhs(void* h, void* out) {
   return dispatch((Handle*)h, [&](auto& o) {
     using T = std::remove_reference_t<decltype(o.t)>;
     o.get_rhs_out((T*)out); return 0; });
+}
+int orc_force_vortex(void* h, double x0, double y0, double dir) {
+  return dispatch((Handle*)h, [&](auto& o) {
+    using T = std::remove_reference_t<decltype(o.t)>;
+    o.force_vortex((T)x0, (T)y0, (T)dir); return 0; });
 }
 int orc_velocity(void* h, void* out) {
   return dispatch((Handle*)h, [&](auto& o) {

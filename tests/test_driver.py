@@ -106,3 +106,34 @@ def test_driver_vel_and_qpress_files(tmp_path):
         assert struct.unpack("<2i", raw[4:12]) == (0, 0)
         got = np.frombuffer(raw[12:12 + 4 * want.size], dtype=np.float32).reshape(want.shape)
         assert np.array_equal(got, want)
+
+
+@pytest.mark.gpu
+def test_driver_forcing_helpers_and_slice(tmp_path):
+    """forcing every force_freq steps after the output (run.f90:69-74), the
+    add_ring / add_dipole helpers at the start (run.f90:37-40) and the
+    2D_slice##.log output, replayed through the API."""
+    from trapbec_gb300 import Solver, parse_cparam
+    text = (CPARAM.format(nsteps=20) + "logical, parameter :: forcing=.true.\ninteger, parameter :: force_freq=5\n"
+            "logical, parameter :: add_ring=.true.\nlogical, parameter :: add_dipole=.true.\n"
+            "logical, parameter :: gnuplot_2D_print=.true.\n")
+    r = _run(tmp_path, text, env={"TRAPBEC_FORCE_SEED": "42"})
+    assert r.returncode == 0, r.stdout + r.stderr
+    p = parse_cparam(text)
+    p.precision = abi.FP32
+    s = Solver(p)
+    s.init_state("single_vortex")
+    s.init_state("add_ring")
+    s.init_state("add_dipole")
+    for blk in range(1, 5):
+        s.step_rt(5)
+        if blk == 4:
+            break
+        s.force_random_points(seed=42, draw=blk)
+    psi20, _ = _read_var(tmp_path / "data" / "proc000" / "var0002.dat", np.complex64, (16, 16, 16))
+    assert np.array_equal(s.get_psi(), psi20)
+    rows = [l.split() for l in (tmp_path / "data" / "proc000" / "2D_slice02.log").read_text().splitlines()]
+    vals = np.array([[float(v) for v in row] for row in rows if row])
+    assert vals.shape == (16 * 16, 3)
+    want = np.abs(psi20[:, :, 0].reshape(-1)) ** 2
+    assert np.allclose(vals[:, 2], want, rtol=1e-6, atol=1e-12)

@@ -321,3 +321,28 @@ def test_velocity_and_qpressure(prec, bc, pz, nproc):
         assert np.all(np.isfinite(got))
         err = np.abs(got.astype(np.float64) - want.astype(np.float64))
         assert err.max() <= tol * np.abs(want).max(), err.max()
+
+
+@pytest.mark.parametrize("prec", [abi.FP64, abi.FP32])
+def test_forcing_random_points(prec):
+    """force_random_points (force.f90:12-54): the draws lie in
+    [-Lx/4, Lx/4] x [-Ly/4, Ly/4] with dir = +-1, are reproducible per
+    (seed, draw) and differ between draws; the forced state matches the
+    oracle's force_vortex at the drawn point."""
+    p = params(n=(32, 24, 16), L=(16.0, 12.0, 8.0), prec=prec, nproc=(2, 2))
+    psi = smooth_state(p, seed=3) + 0.3
+    s = Solver(p)
+    s.set_psi(psi)
+    o = Oracle(p)
+    o.set_psi(s.get_psi())
+    seen = set()
+    for draw in range(6):
+        x0, y0, d = s.force_random_points(seed=7, draw=draw)
+        assert -4.0 <= x0 <= 4.0 and -3.0 <= y0 <= 3.0 and d in (-1.0, 1.0)
+        seen.add((x0, y0))
+        o.force_vortex(x0, y0, d)
+    assert len(seen) == 6
+    s2 = Solver(p)
+    assert s2.force_random_points(seed=7, draw=3) == Solver.force_random_points(s2, seed=7, draw=3)
+    tol = FP64_TOL if prec == abi.FP64 else 1e-5   # six FP32 multiplications by sin/cos/atan2 values
+    assert rel_err(s.get_psi(), o.get_psi()) < tol

@@ -166,3 +166,33 @@ def test_qpressure_depends_on_process_grid():
     # the difference lives within one cell of rank boundaries in x and y together
     far = dq[:, 2:4, 2:4, :]
     assert far.max() <= 1e-12
+
+
+# ---- forcing (force.f90) ---------------------------------------------------
+
+def test_force_vortex_oracle_known_answers():
+    """psi = 1 forced at (x0, y0): |psi| = pade_density(r), which vanishes on
+    the axis and tends to 1 far away; the phase winds by 2 pi dir around it;
+    forcing +1 then -1 at the same point leaves pade_density(r)^2, real."""
+    p = params(n=(48, 48, 4), L=(24.0, 24.0, 2.0), bc=abi.BC_PERIODIC, periodicz=1)
+    x, y, _ = coords(p)
+    x0, y0 = 0.37, -0.81
+    for d in (1, -1):
+        o = Oracle(p)
+        o.set_psi(np.ones((48, 48, 4), dtype=np.complex128))
+        o.force_vortex(x0, y0, d)
+        ps = o.get_psi()[:, :, 0]
+        r = np.hypot(x[:, None] - x0, y[None, :] - y0)
+        assert np.abs(ps).min() < 0.3 and np.abs(np.abs(ps) - 1)[r > 10].max() < 1e-2
+        # circulation along the square loop of cells 12..36
+        loop = np.r_[ps[12:36, 12], ps[36, 12:36], ps[36:12:-1, 36], ps[12, 36:12:-1], ps[12, 12]]
+        dphi = np.angle(loop[1:] / loop[:-1])
+        assert abs(dphi.sum() - 2 * np.pi * d) < 1e-9
+    o = Oracle(p)
+    o.set_psi(np.ones((48, 48, 4), dtype=np.complex128))
+    o.force_vortex(x0, y0, 1)
+    a = o.get_psi().copy()
+    o.force_vortex(x0, y0, -1)
+    b = o.get_psi()
+    assert np.abs(b.imag).max() < 1e-15
+    assert np.allclose(b.real, np.abs(a) ** 2, rtol=0, atol=1e-14)

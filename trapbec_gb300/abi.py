@@ -133,6 +133,8 @@ _PROTOS = {
     "trapbec_step_imag": (C.c_int, [_VP, C.c_int, C.c_int, C.c_double,
                                     C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     "trapbec_diag": (C.c_int, [_VP, C.POINTER(DiagOut)]),
+    "trapbec_force_vortex": (C.c_int, [_VP, C.c_double, C.c_double, C.c_double]),
+    "trapbec_force_random_points": (C.c_int, [_VP, C.c_uint64, C.c_uint64, C.POINTER(C.c_double)]),
     "trapbec_get_velocity": (C.c_int, [_VP, _VP]),
     "trapbec_get_qpressure": (C.c_int, [_VP, _VP]),
     "trapbec_set_scalar": (C.c_int, [_VP, C.c_int, C.c_double]),

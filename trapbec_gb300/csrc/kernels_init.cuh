@@ -126,7 +126,7 @@ enum InitKind : int {
   IK_CONST = 0, IK_TF = 1, IK_SOLITON_PHASE = 2, IK_VORTEX_MUL = 3, IK_SINGLE = 4,
   IK_SAUSAGE = 5, IK_CROW = 6, IK_RING_MUL = 7, IK_TF_LINE = 8, IK_TF_RING = 9, IK_TF_NOISE = 10,
   IK_SET = 11, IK_TF_MUL = 12, IK_RINGPAIR_MUL = 13, IK_QUENCH_ADD = 14, IK_PHASE_IMPRINT = 15,
-  IK_NOISE_ADD = 16, IK_PCURRENT = 17
+  IK_NOISE_ADD = 16, IK_PCURRENT = 17, IK_FORCE_VORTEX = 18
 };
 
 template <typename T> struct InitArgsDev {
@@ -144,6 +144,14 @@ template <typename T> struct InitArgsDev {
 
 template <typename T> __device__ inline T vortex_func(T r) {  // initial.f90:117
   return (T)1 - exp((T)(-0.7) * pow(r, (T)1.15));
+}
+// Pade vortex density, ring_density (initial.f90:628-635) = pade_density (force.f90:46-54)
+template <typename T> __device__ inline T pade_density(T r) {
+  const T c1 = (T)11 / (T)32;
+  const T c3 = ((T)5 - (T)32 * c1) / ((T)48 - (T)192 * c1);
+  const T c2 = c1 * (c3 - (T)0.25);
+  const T r2 = r * r;
+  return sqrt(r2 * (c1 + c2 * r2) / ((T)1 + c3 * r2 + c2 * (r2 * r2)));
 }
 template <typename T> __device__ inline c_t<T> cmul_(c_t<T> a, c_t<T> b) {
   return mk<T>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
@@ -225,13 +233,7 @@ __global__ void init_state_kernel(InitArgsDev<T> a) {
         const T zz2 = z - a.v[2];
         const T s = sqrt(ww * ww + zz2 * zz2);
         const T R0 = a.v[3];
-        const T c1 = (T)11 / (T)32;
-        const T c3 = ((T)5 - (T)32 * c1) / ((T)48 - (T)192 * c1);
-        const T c2 = c1 * (c3 - (T)0.25);
-        auto rd = [&](T r) {
-          T r2 = r * r;
-          return sqrt(r2 * (c1 + c2 * r2) / ((T)1 + c3 * r2 + c2 * (r2 * r2)));
-        };
+        auto rd = [](T r) { return pade_density(r); };
         T th = atan2(u, s + R0);
         T r = sqrt(u * u + (s + R0) * (s + R0));
         const c_t<T> p1 = mk<T>(rd(r) * cos(th), rd(r) * sin(th));
@@ -258,6 +260,12 @@ __global__ void init_state_kernel(InitArgsDev<T> a) {
         const T e1 = (T)cell_uniform(a.seed, (uint64_t)idx, 0) * (T)2 - (T)1;
         const T e2 = (T)cell_uniform(a.seed, (uint64_t)idx, 1) * (T)2 - (T)1;
         out = mk<T>(out.x + (T)0.01 * e1, out.y + (T)0.01 * e2);
+      } break;
+      case IK_FORCE_VORTEX: {  // force_random_points body, force.f90:33-44; v = (x0, y0, dir)
+        const T dx = x - a.v[0], dy = y - a.v[1];
+        const T f = pade_density(sqrt(dx * dx + dy * dy));
+        const T th = a.v[2] * atan2(dy, dx);
+        out = cmul_<T>(out, mk<T>(f * cos(th), f * sin(th)));
       } break;
       case IK_PCURRENT: {  // setup_pcurrent, initial.f90:669-739; v[0] = potential kind
         const int pk = (int)a.v[0];

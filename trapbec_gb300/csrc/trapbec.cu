@@ -69,6 +69,7 @@ struct trapbec_ctx {
   void* psi[2] = {nullptr, nullptr};
   int cur = 0;
   void* w = nullptr;
+  double force_args[3] = {0.0, 0.0, 1.0};   // (x0, y0, dir) of the next forced vortex
   void *xx = nullptr, *yy = nullptr, *zz = nullptr, *px = nullptr, *py = nullptr, *pz = nullptr;
   void* trap_user = nullptr;   // Trap array set by the caller (context precision)
   void* trap_eff = nullptr;    // evaluated potential (POT_ARR)
@@ -630,6 +631,9 @@ template <typename T> int init_state_impl(trapbec_ctx* c, const char* name, cons
   } else if (nm == "add_pcurrent") {  // setup_pcurrent, initial.f90:669-739
     a.v[0] = (T)p.potential;
     rc = go(IK_PCURRENT);
+  } else if (nm == "force_vortex") {  // force.f90:33-44 at (x0, y0) with dir, from force_args
+    a.v[0] = (T)c->force_args[0]; a.v[1] = (T)c->force_args[1]; a.v[2] = (T)c->force_args[2];
+    rc = go(IK_FORCE_VORTEX);
   } else {
     set_error("unknown initial state: " + nm);   // initial.f90:155-156
     return TRAPBEC_ERR_ARG;
@@ -999,6 +1003,32 @@ template <typename T> int field_diag_impl(trapbec_ctx* c, void* out, int which) 
 }
 }  // namespace
 extern "C" {
+
+int trapbec_force_vortex(trapbec_ctx* c, double x0, double y0, double dir) {
+  if (!c) return TRAPBEC_ERR_ARG;
+  if (dir != 1.0 && dir != -1.0) { set_error("force_vortex: dir must be +1 or -1"); return TRAPBEC_ERR_ARG; }
+  c->force_args[0] = x0; c->force_args[1] = y0; c->force_args[2] = dir;
+  return trapbec_init_state(c, "force_vortex", nullptr);
+}
+
+int trapbec_force_random_points(trapbec_ctx* c, uint64_t seed, uint64_t draw, double drawn[3]) {
+  if (!c) return TRAPBEC_ERR_ARG;
+  // runif draws of force.f90:20-28 in the context precision, from a
+  // counter-based stream: draw d of seed s is reproducible on its own
+  tbh::Rng rng{tbh::Rng::mix(seed ^ tbh::Rng::mix(draw + 0x632be59bd9b4e019ULL))};
+  const bool f64 = c->p.precision == TRAPBEC_FP64;
+  auto runif = [&](double lo, double hi) {
+    if (f64) return lo + rng.next() * (hi - lo);
+    const float u = (float)rng.next();
+    return (double)((float)lo + u * ((float)hi - (float)lo));
+  };
+  const double lx = f64 ? c->p.lx : (double)(float)c->p.lx, ly = f64 ? c->p.ly : (double)(float)c->p.ly;
+  const double x0 = runif(-lx / 4.0, lx / 4.0);
+  const double y0 = runif(-ly / 4.0, ly / 4.0);
+  const double dir = runif(0.0, 1.0) < 0.5 ? -1.0 : 1.0;
+  if (drawn) { drawn[0] = x0; drawn[1] = y0; drawn[2] = dir; }
+  return trapbec_force_vortex(c, x0, y0, dir);
+}
 
 int trapbec_get_velocity(trapbec_ctx* c, void* vel_out) {
   if (!c || !vel_out) return TRAPBEC_ERR_ARG;

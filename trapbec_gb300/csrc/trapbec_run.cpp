@@ -53,8 +53,10 @@ struct RunControl {  // the run-control names of cparam.local (cparam.local:5-44
   int imag_nsteps = 0;
   bool full_binary_output = true;
   bool imaginary_output = false;
-  bool vel_print = false, qpress_print = false;
+  bool vel_print = false, qpress_print = false, gnuplot_2d_print = false;
   bool add_pcurrent = false, add_ring = false, add_dipole = false, forcing = false;
+  bool phase_imprint_on = false;
+  int force_freq = 10;
 };
 
 bool as_bool(const std::string& v) {
@@ -70,6 +72,39 @@ std::string unquote(const std::string& v) {
 bool file_exists(const std::string& p) {
   struct stat st;
   return ::stat(p.c_str(), &st) == 0;
+}
+
+// 2D_slice##.log of var_print (output.f90:92-101): x, y, |Psi(z=1)|^2 per
+// line, a blank line after each x; list-directed output written as %16.8E.
+void write_2d_slice(trapbec_ctx* ctx, const trapbec_params& p, const std::string& datadir, int q) {
+  const bool f64 = p.precision == TRAPBEC_FP64;
+  const size_t n = (size_t)p.nx * p.ny * p.nz;
+  std::vector<double> psi(2 * n);
+  std::vector<float> psif;
+  if (f64) {
+    check(trapbec_get_psi(ctx, psi.data(), TRAPBEC_LAYOUT_INTERIOR), "gnuplot_2D_print");
+  } else {
+    psif.resize(2 * n);
+    check(trapbec_get_psi(ctx, psif.data(), TRAPBEC_LAYOUT_INTERIOR), "gnuplot_2D_print");
+    for (size_t i = 0; i < 2 * n; ++i) psi[i] = psif[i];
+  }
+  char num[8];
+  if (q >= 0 && q <= 99) std::snprintf(num, sizeof(num), "%02d", q);
+  else std::snprintf(num, sizeof(num), "**");
+  const std::string path = datadir + "/proc000/2D_slice" + num + ".log";
+  FILE* f = std::fopen(path.c_str(), "w");
+  if (!f) emergency_stop("cannot open " + path);
+  for (int i = 0; i < p.nx; ++i) {
+    const double x = (2.0 * (i + 1) - 1) / (2.0 * p.nx) * p.lx - p.lx / 2.0;   // initial.f90:40-42
+    for (int j = 0; j < p.ny; ++j) {
+      const double y = (2.0 * (j + 1) - 1) / (2.0 * p.ny) * p.ly - p.ly / 2.0;
+      const size_t c = ((size_t)i * p.ny + j) * p.nz;   // k = 1
+      const double a2 = psi[2 * c] * psi[2 * c] + psi[2 * c + 1] * psi[2 * c + 1];
+      std::fprintf(f, " %16.8E %16.8E %16.8E\n", x, y, a2);
+    }
+    std::fprintf(f, "\n");
+  }
+  std::fclose(f);
 }
 
 }  // namespace
@@ -104,8 +139,12 @@ int main(int argc, char** argv) {
     else if (k == "add_ring") rc.add_ring = as_bool(v);
     else if (k == "add_dipole") rc.add_dipole = as_bool(v);
     else if (k == "forcing") rc.forcing = as_bool(v);
+    else if (k == "force_freq") rc.force_freq = std::atoi(v.c_str());
+    else if (k == "phase_imprint_on") rc.phase_imprint_on = as_bool(v);
+    else if (k == "gnuplot_2d_print") rc.gnuplot_2d_print = as_bool(v);
   }
   if (rc.shots <= 0) emergency_stop("shots must be positive");
+  if (rc.forcing && rc.force_freq <= 0) emergency_stop("force_freq must be positive");
   if (const char* prec = std::getenv("TRAPBEC_PRECISION")) p.precision = std::atoi(prec) ? TRAPBEC_FP64 : TRAPBEC_FP32;
 
   tbh::mkdirs(datadir + "/proc000");
@@ -121,8 +160,6 @@ int main(int argc, char** argv) {
   std::printf(" Dissipation, gamma= %g\n", p.gamma);
   if (p.advective_vx != 0.0) std::printf(" Moving frame, vx= %g\n", p.advective_vx);
   else if (p.omega_z != 0.0) std::printf(" Rotating frame, Omega= %g\n", p.omega_z);
-  if (rc.add_pcurrent || rc.add_ring || rc.add_dipole || rc.forcing)
-    std::printf(" note: add_pcurrent/add_ring/add_dipole/forcing are not applied by this driver\n");
 
   trapbec_ctx* ctx = nullptr;
   check(trapbec_create(&p, &ctx), "mesh_init");
@@ -141,10 +178,12 @@ int main(int argc, char** argv) {
   if (!restarted && rc.imaginary_time) {  // run.f90:19-35
     for (int itime = 1; itime <= rc.imag_nsteps;) {
       const int m = (itime + rc.shots - 1) / rc.shots * rc.shots;   // next output step
-      const int k = std::min(m - itime + 1, rc.imag_nsteps - itime + 1);
+      // phase_imprint follows every imaginary step (run.f90:25)
+      const int k = rc.phase_imprint_on ? 1 : std::min(m - itime + 1, rc.imag_nsteps - itime + 1);
       int done = 0;
       double ratio = 0;
       check(trapbec_step_imag(ctx, k, TRAPBEC_IMAG_REF_EULER, 0.0, &done, &ratio), "imaginary time");
+      if (rc.phase_imprint_on) check(trapbec_init_state(ctx, "phase_imprint", nullptr), "phase_imprint");
       itime += k;
       const int last = itime - 1;
       if (last % rc.shots == 0) {
@@ -156,10 +195,18 @@ int main(int argc, char** argv) {
     std::printf(" finished imaginary time propagation\n");
   }
 
+  // run.f90:37-40, after a restart too
+  if (rc.add_pcurrent) check(trapbec_init_state(ctx, "add_pcurrent", nullptr), "setup_pcurrent");
+  if (rc.add_ring) check(trapbec_init_state(ctx, "add_ring", nullptr), "setup_add_ring");
+  if (rc.add_dipole) check(trapbec_init_state(ctx, "add_dipole", nullptr), "setup_add_dipole");
+
+  // forcing draws: TRAPBEC_FORCE_SEED (default 1), draw number itime/force_freq
+  const uint64_t force_seed = std::getenv("TRAPBEC_FORCE_SEED") ? std::strtoull(std::getenv("TRAPBEC_FORCE_SEED"), nullptr, 10) : 1;
   double tot_ms = 0.0;
   int timed_steps = 0;
   for (int itime = nstart; itime <= rc.nsteps;) {   // run.f90:43-76
-    const int m = (itime + rc.shots - 1) / rc.shots * rc.shots;   // next output step
+    int m = (itime + rc.shots - 1) / rc.shots * rc.shots;   // next output step
+    if (rc.forcing) m = std::min(m, (itime + rc.force_freq - 1) / rc.force_freq * rc.force_freq);
     const int k = std::min(m - itime + 1, rc.nsteps - itime + 1);
     check(trapbec_step_rt(ctx, k, &t), "RK3 step");
     double ms = 0;
@@ -180,8 +227,12 @@ int main(int argc, char** argv) {
         check(trapbec_write_field(ctx, datadir.c_str(), last, rc.shots, TRAPBEC_FIELD_VELOCITY), "get_phase");
       if (rc.qpress_print)
         check(trapbec_write_field(ctx, datadir.c_str(), last, rc.shots, TRAPBEC_FIELD_QPRESSURE), "get_qpressure");
+      if (rc.gnuplot_2d_print) write_2d_slice(ctx, p, datadir, last / rc.shots);
       check(trapbec_write_restart(ctx, datadir.c_str(), last, t), "var_print: var.dat");
     }
+    if (rc.forcing && last % rc.force_freq == 0)   // run.f90:70-74
+      check(trapbec_force_random_points(ctx, force_seed, (uint64_t)(last / rc.force_freq), nullptr),
+            "force_random_points");
   }
   const double tpt = timed_steps ? tot_ms * 1e-3 / timed_steps : 0.0;
   check(trapbec_write_timing(&p, datadir.c_str(), tpt, 0.0), "print_timing");

@@ -104,6 +104,18 @@ class Solver:
         check(self.lib.trapbec_diag(self.ctx, C.byref(d)), "trapbec_diag")
         return d.as_dict()
 
+    def force_vortex(self, x0: float, y0: float, direction: int) -> None:
+        """psi *= pade_density(r) e^{i dir theta} about (x0, y0) (force.f90:33-44)."""
+        check(self.lib.trapbec_force_vortex(self.ctx, float(x0), float(y0), float(direction)),
+              "trapbec_force_vortex")
+
+    def force_random_points(self, seed: int, draw: int) -> tuple[float, float, float]:
+        """force_random_points with draw number `draw` of `seed`; returns (x0, y0, dir)."""
+        out = (C.c_double * 3)()
+        check(self.lib.trapbec_force_random_points(self.ctx, int(seed), int(draw), out),
+              "trapbec_force_random_points")
+        return out[0], out[1], out[2]
+
     def velocity(self) -> np.ndarray:
         """vel of get_phase (diagnostic.f90:27-48), shape (3, Nx, Ny, Nz)."""
         a = np.empty((3,) + self.shape, dtype=self.rdtype)
