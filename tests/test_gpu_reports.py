@@ -9,8 +9,11 @@ pytestmark = pytest.mark.gpu
 
 def test_ring_fp32_drift_and_l2():
     r = reports.fp32_vs_fp64(n=64, steps=200, chunk=50)
+    # RK3 is not norm-preserving (|P(i lambda dt)| < 1): the FP64 run drifts by
+    # the scheme's own amount; FP32 must add less than 1e-6 to it
+    assert abs(r["fp64"]["norm_drift"]) < 1e-6
     assert abs(r["fp32"]["norm_drift"]) < 1e-6
-    assert abs(r["fp64"]["norm_drift"]) < 1e-9
+    assert abs(r["fp32_vs_fp64"]["norm_rel"]) < 1e-6
     assert r["fp32_vs_fp64"]["l2_rel_psi"] < 1e-4
     assert len(r["fp32_vs_fp64"]["checkpoints"]) == 4
 
