@@ -1,0 +1,88 @@
+/* trapbec_surrogate.h -- kernels of the learned warm start for imaginary time.
+ *
+ * None of these entry points has a counterpart in the reference: the
+ * reference starts imaginary-time relaxation from its analytic initial
+ * states only (initial.f90).  The surrogate is a 3D convolutional
+ * encoder-decoder that predicts the ground-state amplitude from the trap
+ * potential and the instance parameters; its prediction is only ever used as
+ * the initial guess of trapbec_step_imag / trapbec_batch_solve_imag, and the
+ * Thomas-Fermi guess remains both the fallback and the judge.
+ *
+ * Conventions: all pointers are device pointers; activations are BF16,
+ * channels-last [batch][D][H][W][C] with C a multiple of 16; gradients of
+ * activations are FP32 in the same layout; weights of a 3x3x3 convolution
+ * are [27][Cout][Cin] (tap = (kd*3 + kh)*3 + kw, offsets -1..1), FP32 master
+ * copies and BF16 working copies.  `stream` is a cudaStream_t (NULL = the
+ * legacy default stream).  Calls are asynchronous on that stream and return
+ * TBSG_OK or an error code; nothing allocates device memory.
+ */
+#ifndef TRAPBEC_SURROGATE_H
+#define TRAPBEC_SURROGATE_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum tbsg_status { TBSG_OK = 0, TBSG_ERR_ARG = 1, TBSG_ERR_SHAPE = 2, TBSG_ERR_CUDA = 3 };
+
+/* 3x3x3 convolution, stride 1, zero padding, on the BF16 tensor cores with
+ * FP32 accumulation.  (Cin, Cout) in {(16,16),(16,32),(32,16),(32,32),(32,64),
+ * (64,32),(64,64),(64,128),(128,64),(128,128)}.
+ *  y != NULL:  y = act(conv(x, w) + bias + skip) in BF16 (bias, skip optional;
+ *              act = 1: leaky ReLU with `slope`, 0: none)
+ *  yf != NULL: yf = conv(x, w) (yf_accumulate = 0) or yf += conv(x, w), FP32;
+ *              with the flipped, transposed kernel this is the input gradient. */
+int tbsg_conv3_fwd(const void* x, int cin, const void* w, const float* bias, const void* skip, void* y,
+                   float* yf, int yf_accumulate, int cout, int batch, int D, int H, int W, int act, float slope,
+                   void* stream);
+
+/* Weight and bias gradients of a 3x3x3 convolution:
+ *  dw[tap][co][ci] = sum_{b,v} dz[b][v][co] x[b][v + tap][ci],  db[co] = sum dz[.][co]
+ * (db optional).  Deterministic: per-chunk partials in `scratch` (at least
+ * tbsg_conv3_wgrad_scratch_bytes bytes) reduced in a fixed order.           */
+size_t tbsg_conv3_wgrad_scratch_bytes(int cin, int cout, int batch, int D, int H, int W);
+int tbsg_conv3_wgrad(const void* x, int cin, const void* dz, int cout, int batch, int D, int H, int W,
+                     float* dw, float* db, void* scratch, size_t scratch_bytes, void* stream);
+
+/* FP32 master weights [27][Cout][Cin] -> BF16 working copy w and the BF16
+ * flipped, transposed copy wt[26 - tap][ci][co] used for input gradients.  */
+int tbsg_weight_prep(const float* w32, void* w, void* wt, int cin, int cout, void* stream);
+
+/* dz = dy * act'(y) in BF16 for the leaky ReLU (y is the activation's output);
+ * if dskip != NULL also dskip += dz (gradient of a skip added before act). */
+int tbsg_act_bwd(const float* dy, const void* y, void* dz, float* dskip, size_t n, float slope, void* stream);
+
+/* 2x2x2 mean pooling (D, H, W of the fine grid, all even) and its gradient
+ * (dx_fine += dy_coarse / 8); nearest-neighbour 2x upsampling (D, H, W of the
+ * coarse grid) and its gradient (dx_coarse = sum of the 8 fine gradients). */
+int tbsg_pool2_fwd(const void* x, void* y, int c, int batch, int D, int H, int W, void* stream);
+int tbsg_pool2_bwd(const float* dy, float* dx, int c, int batch, int D, int H, int W, void* stream);
+int tbsg_up2_fwd(const void* x, void* y, int c, int batch, int D, int H, int W, void* stream);
+int tbsg_up2_bwd(const float* dy, float* dx, int c, int batch, int D, int H, int W, void* stream);
+
+/* Output head (FP32): amp[v] = base[v] + bh + sum_c feat[v][c] wh[c].
+ * tbsg_head_fwd writes amp.  tbsg_head_loss also takes the target amplitude
+ * and returns, for loss = mean_v (amp - target)^2:
+ *  dfeat = d loss / d feat (FP32, overwritten) and out[0] = loss,
+ *  out[1..c] = d loss / d wh, out[c+1] = d loss / d bh, reduced in a fixed
+ *  order through `partials` (at least tbsg_head_partials(nvox, c) floats). */
+int tbsg_head_fwd(const void* feat, int c, const float* wh, const float* bh, const float* base, float* amp,
+                  size_t nvox, void* stream);
+size_t tbsg_head_partials(size_t nvox, int c);
+int tbsg_head_loss(const void* feat, int c, const float* wh, const float* bh, const float* base,
+                   const float* target, size_t nvox, float* dfeat, float* partials, float* out, void* stream);
+
+/* Adam with decoupled weight decay on FP32 parameters (step t >= 1).       */
+int tbsg_adam(float* p, const float* g, float* m, float* v, size_t n, float lr, float beta1, float beta2,
+              float eps, float weight_decay, int t, void* stream);
+
+/* FP32 -> BF16 conversion (inputs of the first layer).                     */
+int tbsg_f32_to_bf16(const float* x, void* y, size_t n, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TRAPBEC_SURROGATE_H */

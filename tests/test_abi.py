@@ -1,5 +1,5 @@
 """C ABI checks that need no GPU: the library loads, exports every function
-include/trapbec.h declares, its structs match the Python mirrors, and the
+include/trapbec.h and include/trapbec_surrogate.h declare, its structs match the Python mirrors, and the
 host-only entry points (defaults, cparam.local parser, dims/timing writers)
 behave like the reference."""
 import ctypes as C
@@ -15,9 +15,11 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def declared_functions():
-    src = open(os.path.join(ROOT, "include", "trapbec.h")).read()
-    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    names = set(re.findall(r"\b(trapbec_[a-z0-9_]+)\s*\(", src))
+    names = set()
+    for h in ("trapbec.h", "trapbec_surrogate.h"):
+        src = open(os.path.join(ROOT, "include", h)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        names |= set(re.findall(r"\b((?:trapbec|tbsg)_[a-z0-9_]+)\s*\(", src))
     return sorted(names)
 
 

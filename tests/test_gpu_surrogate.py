@@ -1,0 +1,208 @@
+"""The warm-start surrogate's kernels against the CPU oracle (float64
+PyTorch on the CPU, fed the same BF16-rounded operands).
+
+Tolerances: FP32-output convolutions and weight gradients accumulate exact
+BF16 products in FP32 -> 1e-5 relative to the largest value; BF16 outputs
+-> one BF16 rounding (2^-8 relative); the whole network runs BF16
+activations, so its loss matches to 1e-2 and each layer's gradient to 6e-2
+(relative Frobenius norm)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from oracle import nn_oracle
+from trapbec_gb300 import abi
+from trapbec_gb300.surrogate import LAYERS, NFEAT, Surrogate, n_params, train
+
+pytestmark = pytest.mark.gpu
+
+PAIRS = [(16, 16), (16, 32), (32, 16), (32, 32), (32, 64), (64, 32), (64, 64), (64, 128), (128, 64), (128, 128)]
+
+
+def _p(t):
+    return C.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def _bf(a, dev="cuda"):
+    return torch.tensor(a, dtype=torch.float32).to(torch.bfloat16).to(dev)
+
+
+@pytest.mark.parametrize("cin,cout", PAIRS)
+def test_conv3_forward_and_gradients(cin, cout):
+    lib = abi.load()
+    rng = np.random.default_rng(cin * 1000 + cout)
+    B, D, H, W = 2, 3, 10, 12          # partial bricks in every direction
+    xb = _bf(rng.normal(size=(B, D, H, W, cin)))
+    wb = _bf(rng.normal(size=(27, cout, cin)) / np.sqrt(27 * cin))
+    dzb = _bf(rng.normal(size=(B, D, H, W, cout)))
+    x64, w64, dz64 = (t.double().cpu() for t in (xb, wb, dzb))
+    bias = torch.tensor(rng.normal(size=cout), dtype=torch.float32, device="cuda")
+    skip = _bf(rng.normal(size=(B, D, H, W, cout)))
+    st = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    # FP32 output
+    yf = torch.empty((B, D, H, W, cout), dtype=torch.float32, device="cuda")
+    assert lib.tbsg_conv3_fwd(_p(xb), cin, _p(wb), None, None, None, _p(yf), 0, cout, B, D, H, W, 0, 0.0, st) == 0
+    ref = nn_oracle.conv3(x64, w64)
+    assert (yf.double().cpu() - ref).abs().max() <= 1e-5 * ref.abs().max()
+    # accumulate mode adds
+    assert lib.tbsg_conv3_fwd(_p(xb), cin, _p(wb), None, None, None, _p(yf), 1, cout, B, D, H, W, 0, 0.0, st) == 0
+    assert (yf.double().cpu() - 2 * ref).abs().max() <= 2e-5 * ref.abs().max()
+    # BF16 output with bias, skip and the leaky ReLU
+    y = torch.empty((B, D, H, W, cout), dtype=torch.bfloat16, device="cuda")
+    assert lib.tbsg_conv3_fwd(_p(xb), cin, _p(wb), _p(bias), _p(skip), _p(y), None, 0, cout, B, D, H, W, 1, 0.05,
+                              st) == 0
+    ref2 = nn_oracle.act(ref + bias.double().cpu() + skip.double().cpu())
+    assert (y.double().cpu() - ref2).abs().max() <= 2 ** -7 * ref2.abs().max()
+    # input gradient: the forward pass of the flipped, transposed kernel
+    w32 = wb.float()
+    wk = torch.empty_like(wb)
+    wt = torch.empty_like(wb)
+    assert lib.tbsg_weight_prep(_p(w32), _p(wk), _p(wt), cin, cout, st) == 0
+    assert torch.equal(wk, wb)
+    gx = torch.empty((B, D, H, W, cin), dtype=torch.float32, device="cuda")
+    assert lib.tbsg_conv3_fwd(_p(dzb), cout, _p(wt), None, None, None, _p(gx), 0, cin, B, D, H, W, 0, 0.0, st) == 0
+    xr = x64.clone().requires_grad_(True)
+    wr = w64.clone().requires_grad_(True)
+    out = nn_oracle.conv3(xr, wr, torch.zeros(cout, dtype=torch.float64, requires_grad=True))
+    (out * dz64).sum().backward()
+    assert (gx.double().cpu() - xr.grad).abs().max() <= 1e-5 * xr.grad.abs().max()
+    # weight and bias gradients
+    dw = torch.empty((27, cout, cin), dtype=torch.float32, device="cuda")
+    db = torch.empty(cout, dtype=torch.float32, device="cuda")
+    sb = lib.tbsg_conv3_wgrad_scratch_bytes(cin, cout, B, D, H, W)
+    scr = torch.empty(sb // 4 + 1, dtype=torch.float32, device="cuda")
+    assert lib.tbsg_conv3_wgrad(_p(xb), cin, _p(dzb), cout, B, D, H, W, _p(dw), _p(db), _p(scr), sb, st) == 0
+    assert (dw.double().cpu() - wr.grad).abs().max() <= 1e-5 * wr.grad.abs().max()
+    assert (db.double().cpu() - dz64.sum(dim=(0, 1, 2, 3))).abs().max() <= 1e-5 * dz64.abs().sum(dim=(0, 1, 2, 3)).max()
+    # deterministic
+    dw2 = torch.empty_like(dw)
+    assert lib.tbsg_conv3_wgrad(_p(xb), cin, _p(dzb), cout, B, D, H, W, _p(dw2), None, _p(scr), sb, st) == 0
+    assert torch.equal(dw, dw2)
+
+
+def test_unsupported_pair_is_an_error():
+    lib = abi.load()
+    x = torch.zeros(16 * 8, dtype=torch.bfloat16, device="cuda")
+    assert lib.tbsg_conv3_fwd(_p(x), 16, _p(x), None, None, _p(x), None, 0, 48, 1, 2, 2, 2, 0, 0.0, None) == 2
+
+
+def test_pool_up_act_head_adam():
+    lib = abi.load()
+    rng = np.random.default_rng(5)
+    st = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    B, D, c = 2, 6, 32
+    x = _bf(rng.normal(size=(B, D, D, D, c)))
+    y = torch.empty((B, D // 2, D // 2, D // 2, c), dtype=torch.bfloat16, device="cuda")
+    assert lib.tbsg_pool2_fwd(_p(x), _p(y), c, B, D, D, D, st) == 0
+    ref = nn_oracle.pool2(x.double().cpu())
+    assert (y.double().cpu() - ref).abs().max() <= 2 ** -8 * ref.abs().max()
+    u = torch.empty_like(x)
+    assert lib.tbsg_up2_fwd(_p(y), _p(u), c, B, D // 2, D // 2, D // 2, st) == 0
+    assert torch.equal(u, nn_oracle.up2(y.cpu()).cuda())
+    g = torch.tensor(rng.normal(size=(B, D, D, D, c)), dtype=torch.float32, device="cuda")
+    gc = torch.empty((B, D // 2, D // 2, D // 2, c), dtype=torch.float32, device="cuda")
+    assert lib.tbsg_up2_bwd(_p(g), _p(gc), c, B, D // 2, D // 2, D // 2, st) == 0
+    want = g.double().cpu().reshape(B, D // 2, 2, D // 2, 2, D // 2, 2, c).sum(dim=(2, 4, 6))
+    assert (gc.double().cpu() - want).abs().max() <= 1e-5 * want.abs().max()
+    acc = torch.ones_like(g)
+    assert lib.tbsg_pool2_bwd(_p(gc), _p(acc), c, B, D, D, D, st) == 0
+    want = 1.0 + nn_oracle.up2(gc.double().cpu()) / 8
+    assert (acc.double().cpu() - want).abs().max() <= 1e-6 * want.abs().max()
+    # activation gradient with the skip accumulation
+    yb = _bf(rng.normal(size=1000))
+    dy = torch.tensor(rng.normal(size=1000), dtype=torch.float32, device="cuda")
+    dz = torch.empty(1000, dtype=torch.bfloat16, device="cuda")
+    sk = torch.ones(1000, dtype=torch.float32, device="cuda")
+    assert lib.tbsg_act_bwd(_p(dy), _p(yb), _p(dz), _p(sk), 1000, 0.05, st) == 0
+    wantg = dy.double().cpu() * torch.where(yb.double().cpu() > 0, 1.0, 0.05)
+    assert (dz.double().cpu() - wantg).abs().max() <= 2 ** -8 * wantg.abs().max()
+    assert (sk.double().cpu() - 1 - wantg).abs().max() <= 1e-6 * wantg.abs().max()
+    # head and loss
+    n = 5000
+    feat = _bf(rng.normal(size=(n, NFEAT)))
+    wh = torch.tensor(rng.normal(size=NFEAT), dtype=torch.float32, device="cuda")
+    bh = torch.tensor([0.3], dtype=torch.float32, device="cuda")
+    base = torch.tensor(rng.uniform(size=n), dtype=torch.float32, device="cuda")
+    tgt = torch.tensor(rng.uniform(size=n), dtype=torch.float32, device="cuda")
+    dfeat = torch.empty((n, NFEAT), dtype=torch.float32, device="cuda")
+    part = torch.empty(lib.tbsg_head_partials(n, NFEAT), dtype=torch.float32, device="cuda")
+    out = torch.empty(NFEAT + 2, dtype=torch.float32, device="cuda")
+    assert lib.tbsg_head_loss(_p(feat), NFEAT, _p(wh), _p(bh), _p(base), _p(tgt), n, _p(dfeat), _p(part), _p(out),
+                              st) == 0
+    f64 = feat.double().cpu()
+    whr = wh.double().cpu().requires_grad_(True)
+    bhr = bh.double().cpu().requires_grad_(True)
+    fr = f64.clone().requires_grad_(True)
+    loss = ((base.double().cpu() + fr @ whr + bhr - tgt.double().cpu()) ** 2).mean()
+    loss.backward()
+    o = out.double().cpu()
+    assert abs(o[0] - loss.item()) <= 1e-5 * loss.item()
+    assert (o[1:NFEAT + 1] - whr.grad).abs().max() <= 1e-5 * whr.grad.abs().max()
+    assert abs(o[NFEAT + 1] - bhr.grad[0]) <= 1e-5 * abs(bhr.grad[0]) + 1e-7
+    assert (dfeat.double().cpu() - fr.grad).abs().max() <= 1e-5 * fr.grad.abs().max()
+    # Adam
+    p0 = torch.tensor(rng.normal(size=100), dtype=torch.float32, device="cuda")
+    gr = torch.tensor(rng.normal(size=100), dtype=torch.float32, device="cuda")
+    m = torch.zeros(100, dtype=torch.float32, device="cuda")
+    v = torch.zeros(100, dtype=torch.float32, device="cuda")
+    p1 = p0.clone()
+    assert lib.tbsg_adam(_p(p1), _p(gr), _p(m), _p(v), 100, 1e-2, 0.9, 0.999, 1e-8, 0.0, 1, st) == 0
+    mh = 0.1 * gr.double() / 0.1
+    vh = 0.001 * gr.double() ** 2 / 0.001
+    want = p0.double() - 1e-2 * mh / (vh.sqrt() + 1e-8)
+    assert (p1.double() - want).abs().max() <= 1e-6
+
+
+def _net_inputs(S, B, seed):
+    rng = np.random.default_rng(seed)
+    x = rng.normal(size=(B, S, S, S, 16)).astype(np.float32)
+    base = rng.uniform(0, 1, size=(B, S, S, S)).astype(np.float32)
+    tgt = (base + 0.1 * rng.normal(size=base.shape)).astype(np.float32)
+    return x, base, tgt
+
+
+def test_network_gradient_against_oracle():
+    """Whole-network loss and per-layer gradients of the GPU path (BF16
+    activations) against the float64 oracle on the same BF16 weights/inputs."""
+    S, B = 16, 2
+    net = Surrogate(S, B, seed=3)
+    x, base, tgt = _net_inputs(S, B, 1)
+    xt = torch.tensor(x).cuda()
+    net.forward(xt, torch.tensor(base).cuda())
+    loss = net.backward(torch.tensor(tgt).cuda()).item()
+    g = net.g.double().cpu().numpy()
+    # the oracle sees the BF16-rounded weights and inputs the kernels used
+    p = net.p.double().cpu().numpy()
+    off = 0
+    for name, ci, co in LAYERS:
+        p[off:off + 27 * ci * co] = net.wb[name].double().cpu().numpy()
+        off += 27 * ci * co + co
+    xr = xt.to(torch.bfloat16).double().cpu().numpy()
+    lref, gref = nn_oracle.loss_and_grad(p, xr, base.astype(np.float64), tgt.astype(np.float64))
+    assert abs(loss - lref) <= 1e-2 * lref
+    off = 0
+    for name, ci, co in LAYERS:
+        for a, b in ((off, off + 27 * ci * co), (off + 27 * ci * co, off + 27 * ci * co + co)):
+            err = np.linalg.norm(g[a:b] - gref[a:b]) / np.linalg.norm(gref[a:b])
+            assert err < 6e-2, (name, a == off, err)
+        off += 27 * ci * co + co
+    err = np.linalg.norm(g[off:] - gref[off:]) / np.linalg.norm(gref[off:])
+    assert err < 1e-2
+
+
+def test_training_reduces_loss():
+    """A few hundred Adam steps on a small fixed set reduce the loss at least 5x."""
+    S, B, N = 16, 2, 4
+    net = Surrogate(S, B, seed=0)
+    X, BASE, Y = [], [], []
+    for i in range(N):
+        x, base, tgt = _net_inputs(S, 1, 10 + i)
+        X.append(x[0]); BASE.append(base[0]); Y.append(tgt[0])
+    X = torch.tensor(np.stack(X)).cuda().to(torch.bfloat16)
+    BASE = torch.tensor(np.stack(BASE)).cuda()
+    Y = torch.tensor(np.stack(Y)).cuda()
+    hist = train(net, X, BASE, Y, epochs=150, lr=2e-3, lr_min=1e-4)
+    assert hist[-1] < hist[0] / 5, hist[::10]

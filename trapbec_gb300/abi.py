@@ -168,6 +168,24 @@ _PROTOS = {
     "trapbec_last_error": (C.c_char_p, []),
     "trapbec_abi_version": (C.c_int, []),
     "trapbec_abi_struct_size": (C.c_int, [C.c_int]),
+    # learned warm start (include/trapbec_surrogate.h)
+    "tbsg_conv3_fwd": (C.c_int, [_VP, C.c_int, _VP, _VP, _VP, _VP, _VP, C.c_int, C.c_int, C.c_int, C.c_int,
+                                 C.c_int, C.c_int, C.c_int, C.c_float, _VP]),
+    "tbsg_conv3_wgrad_scratch_bytes": (C.c_size_t, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]),
+    "tbsg_conv3_wgrad": (C.c_int, [_VP, C.c_int, _VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _VP, _VP, _VP,
+                                   C.c_size_t, _VP]),
+    "tbsg_weight_prep": (C.c_int, [_VP, _VP, _VP, C.c_int, C.c_int, _VP]),
+    "tbsg_act_bwd": (C.c_int, [_VP, _VP, _VP, _VP, C.c_size_t, C.c_float, _VP]),
+    "tbsg_pool2_fwd": (C.c_int, [_VP, _VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _VP]),
+    "tbsg_pool2_bwd": (C.c_int, [_VP, _VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _VP]),
+    "tbsg_up2_fwd": (C.c_int, [_VP, _VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _VP]),
+    "tbsg_up2_bwd": (C.c_int, [_VP, _VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _VP]),
+    "tbsg_head_fwd": (C.c_int, [_VP, C.c_int, _VP, _VP, _VP, _VP, C.c_size_t, _VP]),
+    "tbsg_head_partials": (C.c_size_t, [C.c_size_t, C.c_int]),
+    "tbsg_head_loss": (C.c_int, [_VP, C.c_int, _VP, _VP, _VP, _VP, C.c_size_t, _VP, _VP, _VP, _VP]),
+    "tbsg_adam": (C.c_int, [_VP, _VP, _VP, _VP, C.c_size_t, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float,
+                            C.c_int, _VP]),
+    "tbsg_f32_to_bf16": (C.c_int, [_VP, _VP, C.c_size_t, _VP]),
 }
 
 _lib = None

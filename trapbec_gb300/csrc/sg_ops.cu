@@ -1,0 +1,273 @@
+// sg_ops.cu -- the memory-bound pieces of the warm-start surrogate: weight
+// preparation, activation gradient, pooling/upsampling and their gradients,
+// the FP32 output head with its loss, Adam.  Grid-stride loops over
+// 16-byte (8 x BF16) or 4 x FP32 vectors where the layout allows.
+#include "../../include/trapbec_surrogate.h"
+#include "sg_common.cuh"
+
+namespace sg {
+
+inline int grid_for(size_t n, int per_thread = 1) {
+  size_t b = (n / per_thread + 255) / 256;
+  if (b < 1) b = 1;
+  if (b > 152 * 16) b = 152 * 16;
+  return (int)b;
+}
+
+__global__ void weight_prep_kernel(const float* w32, bf16* w, bf16* wt, int cin, int cout) {
+  const size_t n = (size_t)27 * cout * cin;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int ci = (int)(i % cin);
+    const size_t r = i / cin;
+    const int co = (int)(r % cout), tap = (int)(r / cout);
+    const bf16 v = __float2bfloat16_rn(w32[i]);
+    w[i] = v;
+    wt[((size_t)(26 - tap) * cin + ci) * cout + co] = v;
+  }
+}
+
+__global__ void act_bwd_kernel(const float* dy, const bf16* y, bf16* dz, float* dskip, size_t n, float slope) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const float g = dy[i] * (__bfloat162float(y[i]) > 0.f ? 1.f : slope);
+    const bf16 gb = __float2bfloat16_rn(g);
+    dz[i] = gb;
+    if (dskip) dskip[i] += g;
+  }
+}
+
+// fine grid (D, H, W) -> coarse (D/2, H/2, W/2); one thread per coarse voxel x 8 channels
+__global__ void pool2_fwd_kernel(const bf16* x, bf16* y, int c, int B, int D, int H, int W) {
+  const int Dc = D / 2, Hc = H / 2, Wc = W / 2, c8 = c / 8;
+  const size_t n = (size_t)B * Dc * Hc * Wc * c8;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int cc = (int)(i % c8);
+    size_t r = i / c8;
+    const int w = (int)(r % Wc); r /= Wc;
+    const int h = (int)(r % Hc); r /= Hc;
+    const int d = (int)(r % Dc);
+    const size_t b = r / Dc;
+    float s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int o = 0; o < 8; ++o) {
+      const int fd = 2 * d + (o >> 2), fh = 2 * h + ((o >> 1) & 1), fw = 2 * w + (o & 1);
+      const uint4 u = *(const uint4*)(x + (((b * D + fd) * H + fh) * W + fw) * c + cc * 8);
+      const bf16* e = (const bf16*)&u;
+      for (int k = 0; k < 8; ++k) s[k] += __bfloat162float(e[k]);
+    }
+    uint4 o4;
+    bf16* e = (bf16*)&o4;
+    for (int k = 0; k < 8; ++k) e[k] = __float2bfloat16_rn(s[k] * 0.125f);
+    *(uint4*)(y + (((b * Dc + d) * Hc + h) * Wc + w) * c + cc * 8) = o4;
+  }
+}
+
+__global__ void pool2_bwd_kernel(const float* dy, float* dx, int c, int B, int D, int H, int W) {
+  const int Dc = D / 2, Hc = H / 2, Wc = W / 2;
+  const size_t n = (size_t)B * D * H * W * c;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int cc = (int)(i % c);
+    size_t r = i / c;
+    const int w = (int)(r % W); r /= W;
+    const int h = (int)(r % H); r /= H;
+    const int d = (int)(r % D);
+    const size_t b = r / D;
+    dx[i] += 0.125f * dy[(((b * Dc + d / 2) * Hc + h / 2) * Wc + w / 2) * c + cc];
+  }
+}
+
+// coarse (D, H, W) -> fine (2D, 2H, 2W)
+__global__ void up2_fwd_kernel(const bf16* x, bf16* y, int c, int B, int D, int H, int W) {
+  const int c8 = c / 8, Df = 2 * D, Hf = 2 * H, Wf = 2 * W;
+  const size_t n = (size_t)B * Df * Hf * Wf * c8;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int cc = (int)(i % c8);
+    size_t r = i / c8;
+    const int w = (int)(r % Wf); r /= Wf;
+    const int h = (int)(r % Hf); r /= Hf;
+    const int d = (int)(r % Df);
+    const size_t b = r / Df;
+    *(uint4*)(y + i * 8) = *(const uint4*)(x + (((b * D + d / 2) * H + h / 2) * W + w / 2) * c + cc * 8);
+  }
+}
+
+__global__ void up2_bwd_kernel(const float* dy, float* dx, int c, int B, int D, int H, int W) {
+  const int Hf = 2 * H, Wf = 2 * W, Df = 2 * D;
+  const size_t n = (size_t)B * D * H * W * c;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int cc = (int)(i % c);
+    size_t r = i / c;
+    const int w = (int)(r % W); r /= W;
+    const int h = (int)(r % H); r /= H;
+    const int d = (int)(r % D);
+    const size_t b = r / D;
+    float s = 0.f;
+    for (int o = 0; o < 8; ++o) {
+      const int fd = 2 * d + (o >> 2), fh = 2 * h + ((o >> 1) & 1), fw = 2 * w + (o & 1);
+      s += dy[(((b * Df + fd) * Hf + fh) * Wf + fw) * c + cc];
+    }
+    dx[i] = s;
+  }
+}
+
+constexpr int HEAD_THREADS = 256;
+constexpr int HEAD_BLOCKS = 1024;
+
+__global__ void head_fwd_kernel(const bf16* feat, int c, const float* wh, const float* bh, const float* base,
+                                float* amp, size_t nvox) {
+  for (size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v < nvox; v += (size_t)gridDim.x * blockDim.x) {
+    float s = bh[0];
+    for (int k = 0; k < c; ++k) s += __bfloat162float(feat[v * c + k]) * wh[k];
+    amp[v] = base[v] + s;
+  }
+}
+
+// per-block partials [blocks][c + 2]: loss, dwh[c], dbh
+__global__ void head_loss_kernel(const bf16* feat, int c, const float* wh, const float* bh, const float* base,
+                                 const float* target, size_t nvox, float* dfeat, float* partials) {
+  extern __shared__ float red[];   // [HEAD_THREADS][c + 2]
+  const int np = c + 2;
+  float acc[130];
+  for (int k = 0; k < np; ++k) acc[k] = 0.f;
+  const float inv = 1.f / (float)nvox;
+  for (size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v < nvox; v += (size_t)gridDim.x * blockDim.x) {
+    float s = bh[0];
+    for (int k = 0; k < c; ++k) s += __bfloat162float(feat[v * c + k]) * wh[k];
+    const float diff = base[v] + s - target[v];
+    const float g = 2.f * diff * inv;
+    acc[0] += diff * diff * inv;
+    for (int k = 0; k < c; ++k) {
+      acc[1 + k] += g * __bfloat162float(feat[v * c + k]);
+      dfeat[v * c + k] = g * wh[k];
+    }
+    acc[c + 1] += g;
+  }
+  for (int k = 0; k < np; ++k) red[threadIdx.x * np + k] = acc[k];
+  __syncthreads();
+  for (int s = HEAD_THREADS / 2; s > 0; s >>= 1) {
+    if ((int)threadIdx.x < s)
+      for (int k = 0; k < np; ++k) red[threadIdx.x * np + k] += red[(threadIdx.x + s) * np + k];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int k = 0; k < np; ++k) partials[(size_t)blockIdx.x * np + k] = red[k];
+}
+
+__global__ void head_final_kernel(const float* partials, int nblk, int np, float* out) {
+  for (int k = threadIdx.x; k < np; k += blockDim.x) {
+    float s = 0.f;
+    for (int b = 0; b < nblk; ++b) s += partials[(size_t)b * np + k];
+    out[k] = s;
+  }
+}
+
+__global__ void adam_kernel(float* p, const float* g, float* m, float* v, size_t n, float lr, float b1, float b2,
+                            float eps, float wd, float bc1, float bc2) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.f - b1) * gi;
+    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    const float mh = mi / bc1, vh = vi / bc2;
+    p[i] -= lr * (mh / (sqrtf(vh) + eps) + wd * p[i]);
+  }
+}
+
+__global__ void f32_to_bf16_kernel(const float* x, bf16* y, size_t n) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    y[i] = __float2bfloat16_rn(x[i]);
+}
+
+inline int done() { return cudaGetLastError() == cudaSuccess ? TBSG_OK : TBSG_ERR_CUDA; }
+
+}  // namespace sg
+
+using namespace sg;
+
+extern "C" {
+
+int tbsg_weight_prep(const float* w32, void* w, void* wt, int cin, int cout, void* stream) {
+  if (!w32 || !w || !wt || cin <= 0 || cout <= 0) return TBSG_ERR_ARG;
+  weight_prep_kernel<<<grid_for((size_t)27 * cin * cout), 256, 0, (cudaStream_t)stream>>>(w32, (bf16*)w, (bf16*)wt,
+                                                                                          cin, cout);
+  return done();
+}
+
+int tbsg_act_bwd(const float* dy, const void* y, void* dz, float* dskip, size_t n, float slope, void* stream) {
+  if (!dy || !y || !dz) return TBSG_ERR_ARG;
+  act_bwd_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(dy, (const bf16*)y, (bf16*)dz, dskip, n, slope);
+  return done();
+}
+
+int tbsg_pool2_fwd(const void* x, void* y, int c, int batch, int D, int H, int W, void* stream) {
+  if (!x || !y || c % 8 || (D | H | W) & 1) return TBSG_ERR_ARG;
+  pool2_fwd_kernel<<<grid_for((size_t)batch * D * H * W * c / 64), 256, 0, (cudaStream_t)stream>>>(
+      (const bf16*)x, (bf16*)y, c, batch, D, H, W);
+  return done();
+}
+
+int tbsg_pool2_bwd(const float* dy, float* dx, int c, int batch, int D, int H, int W, void* stream) {
+  if (!dy || !dx || (D | H | W) & 1) return TBSG_ERR_ARG;
+  pool2_bwd_kernel<<<grid_for((size_t)batch * D * H * W * c), 256, 0, (cudaStream_t)stream>>>(dy, dx, c, batch, D,
+                                                                                              H, W);
+  return done();
+}
+
+int tbsg_up2_fwd(const void* x, void* y, int c, int batch, int D, int H, int W, void* stream) {
+  if (!x || !y || c % 8) return TBSG_ERR_ARG;
+  up2_fwd_kernel<<<grid_for((size_t)batch * D * H * W * c), 256, 0, (cudaStream_t)stream>>>(
+      (const bf16*)x, (bf16*)y, c, batch, D, H, W);
+  return done();
+}
+
+int tbsg_up2_bwd(const float* dy, float* dx, int c, int batch, int D, int H, int W, void* stream) {
+  if (!dy || !dx) return TBSG_ERR_ARG;
+  up2_bwd_kernel<<<grid_for((size_t)batch * D * H * W * c), 256, 0, (cudaStream_t)stream>>>(dy, dx, c, batch, D, H,
+                                                                                            W);
+  return done();
+}
+
+int tbsg_head_fwd(const void* feat, int c, const float* wh, const float* bh, const float* base, float* amp,
+                  size_t nvox, void* stream) {
+  if (!feat || !wh || !bh || !base || !amp || c <= 0) return TBSG_ERR_ARG;
+  head_fwd_kernel<<<grid_for(nvox), 256, 0, (cudaStream_t)stream>>>((const bf16*)feat, c, wh, bh, base, amp, nvox);
+  return done();
+}
+
+size_t tbsg_head_partials(size_t nvox, int c) {
+  (void)nvox;
+  return (size_t)HEAD_BLOCKS * (c + 2);
+}
+
+int tbsg_head_loss(const void* feat, int c, const float* wh, const float* bh, const float* base,
+                   const float* target, size_t nvox, float* dfeat, float* partials, float* out, void* stream) {
+  if (!feat || !wh || !bh || !base || !target || !dfeat || !partials || !out || c <= 0 || c > 128)
+    return TBSG_ERR_ARG;
+  const size_t smem = (size_t)HEAD_THREADS * (c + 2) * sizeof(float);
+  if (smem > 48 * 1024) {
+    if (cudaFuncSetAttribute(head_loss_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaSuccess)
+      return TBSG_ERR_CUDA;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  head_loss_kernel<<<HEAD_BLOCKS, HEAD_THREADS, smem, st>>>((const bf16*)feat, c, wh, bh, base, target, nvox, dfeat,
+                                                            partials);
+  head_final_kernel<<<1, 256, 0, st>>>(partials, HEAD_BLOCKS, c + 2, out);
+  return done();
+}
+
+int tbsg_adam(float* p, const float* g, float* m, float* v, size_t n, float lr, float beta1, float beta2, float eps,
+              float weight_decay, int t, void* stream) {
+  if (!p || !g || !m || !v || t < 1) return TBSG_ERR_ARG;
+  const float bc1 = 1.f - powf(beta1, (float)t), bc2 = 1.f - powf(beta2, (float)t);
+  adam_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(p, g, m, v, n, lr, beta1, beta2, eps, weight_decay, bc1,
+                                                            bc2);
+  return done();
+}
+
+int tbsg_f32_to_bf16(const float* x, void* y, size_t n, void* stream) {
+  if (!x || !y) return TBSG_ERR_ARG;
+  f32_to_bf16_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(x, (bf16*)y, n);
+  return done();
+}
+
+}  // extern "C"
