@@ -50,13 +50,37 @@ def unpack(p: torch.Tensor) -> dict:
     return out
 
 
-def forward(p: torch.Tensor, x: torch.Tensor, base: torch.Tensor) -> torch.Tensor:
+def _round_bf16(t: torch.Tensor) -> torch.Tensor:
+    """Forward: round to BF16 (nearest even); backward: pass the gradient."""
+    return t + (t.to(torch.bfloat16).to(t.dtype) - t).detach()
+
+
+def _grad_to_bf16(t: torch.Tensor) -> torch.Tensor:
+    """Identity whose gradient is rounded to BF16."""
+    if t.requires_grad:
+        t.register_hook(lambda g: g.to(torch.bfloat16).to(g.dtype))
+    return t
+
+
+def forward(p: torch.Tensor, x: torch.Tensor, base: torch.Tensor, bf16: bool = False) -> torch.Tensor:
+    """bf16 = True rounds where the GPU path stores BF16: every activation
+    and pooled tensor in the forward pass, and the gradient reaching each
+    convolution's output (its dz); skip and pooling gradients stay unrounded."""
     P = unpack(p)
-    c = lambda n, t, skip=None: act(conv3(t, *P[n]) + (skip if skip is not None else 0))
+    rf = _round_bf16 if bf16 else (lambda t: t)
+    rg = _grad_to_bf16 if bf16 else (lambda t: t)
+
+    def c(n, t, skip=None):
+        z = rg(conv3(t, *P[n]))
+        if skip is not None:
+            z = z + skip
+        return rf(act(z))
+
+    pool = lambda t: rf(pool2(t))
     e0 = c("e0b", c("e0a", x))
-    e1 = c("e1b", c("e1a", pool2(e0)))
-    e2 = c("e2b", c("e2a", pool2(e1)))
-    e3 = c("e3c", c("e3b", c("e3a", pool2(e2))))
+    e1 = c("e1b", c("e1a", pool(e0)))
+    e2 = c("e2b", c("e2a", pool(e1)))
+    e3 = c("e3c", c("e3b", c("e3a", pool(e2))))
     d2 = c("d2b", c("d2a", up2(e3), e2))
     d1 = c("d1b", c("d1a", up2(d2), e1))
     d0 = c("d0b", c("d0a", up2(d1), e0))
@@ -64,10 +88,10 @@ def forward(p: torch.Tensor, x: torch.Tensor, base: torch.Tensor) -> torch.Tenso
     return base + d0 @ wh + bh
 
 
-def loss_and_grad(p: np.ndarray, x: np.ndarray, base: np.ndarray, target: np.ndarray):
+def loss_and_grad(p: np.ndarray, x: np.ndarray, base: np.ndarray, target: np.ndarray, bf16: bool = False):
     """Loss mean((amp - target)^2) and its gradient w.r.t. the flat parameters (float64)."""
     pt = torch.tensor(p, dtype=torch.float64, requires_grad=True)
-    amp = forward(pt, torch.tensor(x, dtype=torch.float64), torch.tensor(base, dtype=torch.float64))
+    amp = forward(pt, torch.tensor(x, dtype=torch.float64), torch.tensor(base, dtype=torch.float64), bf16)
     loss = ((amp - torch.tensor(target, dtype=torch.float64)) ** 2).mean()
     loss.backward()
     return float(loss.detach()), pt.grad.numpy().copy()

@@ -3,9 +3,11 @@ PyTorch on the CPU, fed the same BF16-rounded operands).
 
 Tolerances: FP32-output convolutions and weight gradients accumulate exact
 BF16 products in FP32 -> 1e-5 relative to the largest value; BF16 outputs
--> one BF16 rounding (2^-8 relative); the whole network runs BF16
-activations, so its loss matches to 1e-2 and each layer's gradient to 6e-2
-(relative Frobenius norm)."""
+-> one BF16 rounding (2^-8 relative).  The whole network stores BF16
+activations: against an oracle that rounds at the same points its loss
+matches to 1e-4 and each layer's gradient to 2e-2 (relative Frobenius norm;
+what is left is FP32 accumulation order and rounding-boundary flips);
+against the unrounded float64 oracle, to 1e-2 and 1.5e-1."""
 import ctypes as C
 
 import numpy as np
@@ -181,16 +183,17 @@ def test_network_gradient_against_oracle():
         p[off:off + 27 * ci * co] = net.wb[name].double().cpu().numpy()
         off += 27 * ci * co + co
     xr = xt.to(torch.bfloat16).double().cpu().numpy()
-    lref, gref = nn_oracle.loss_and_grad(p, xr, base.astype(np.float64), tgt.astype(np.float64))
-    assert abs(loss - lref) <= 1e-2 * lref
-    off = 0
-    for name, ci, co in LAYERS:
-        for a, b in ((off, off + 27 * ci * co), (off + 27 * ci * co, off + 27 * ci * co + co)):
-            err = np.linalg.norm(g[a:b] - gref[a:b]) / np.linalg.norm(gref[a:b])
-            assert err < 6e-2, (name, a == off, err)
-        off += 27 * ci * co + co
-    err = np.linalg.norm(g[off:] - gref[off:]) / np.linalg.norm(gref[off:])
-    assert err < 1e-2
+    for bf16, tol_l, tol_g in ((True, 1e-4, 2e-2), (False, 1e-2, 1.5e-1)):
+        lref, gref = nn_oracle.loss_and_grad(p, xr, base.astype(np.float64), tgt.astype(np.float64), bf16=bf16)
+        assert abs(loss - lref) <= tol_l * lref, (bf16, loss, lref)
+        off = 0
+        for name, ci, co in LAYERS:
+            for a, b in ((off, off + 27 * ci * co), (off + 27 * ci * co, off + 27 * ci * co + co)):
+                err = np.linalg.norm(g[a:b] - gref[a:b]) / np.linalg.norm(gref[a:b])
+                assert err < tol_g, (bf16, name, a == off, err)
+            off += 27 * ci * co + co
+        err = np.linalg.norm(g[off:] - gref[off:]) / np.linalg.norm(gref[off:])
+        assert err < tol_g / 2, (bf16, "head", err)
 
 
 def test_training_reduces_loss():

@@ -440,3 +440,75 @@ def compare(net: Surrogate, draws, tol: float = 1e-10, max_steps: int = 60000, c
         "wall_ratio_device": res["tf"]["solve_ms_device"] / (res["nn"]["solve_ms_device"] + infer_ms),
         "final_energy_rel_diff_max": float(max(de)), "final_l2_rel": l2,
     }
+
+
+# ---- command line: generate, train, compare ----------------------------------------------------
+
+def main(argv=None):
+    import argparse
+    import json
+    ap = argparse.ArgumentParser(description="train the warm-start surrogate on solver ground states and compare "
+                                             "imaginary-time relaxation from its guess against the TF guess")
+    ap.add_argument("--S", type=int, default=128, help="grid (S^3)")
+    ap.add_argument("--n-train", type=int, default=192)
+    ap.add_argument("--n-test", type=int, default=16)
+    ap.add_argument("--seed", type=int, default=2024)
+    ap.add_argument("--gen-steps", type=int, default=8000, help="relaxation steps per training ground state")
+    ap.add_argument("--gen-frac", type=float, default=0.85, help="fraction of the RK3 stability limit for data")
+    ap.add_argument("--epochs", type=int, default=60)
+    ap.add_argument("--batch", type=int, default=2)
+    ap.add_argument("--lr", type=float, default=2e-3)
+    ap.add_argument("--tol", type=float, default=1e-10)
+    ap.add_argument("--max-steps", type=int, default=60000)
+    ap.add_argument("--weights", default=None, help="load weights instead of training")
+    ap.add_argument("--out", default=None, help="save the trained weights (.npz)")
+    ap.add_argument("--json", default=None)
+    a = ap.parse_args(argv)
+    torch = _torch()
+    log = lambda m: print(m, flush=True)
+    draws = units.ground_state_draws(a.n_train + a.n_test, a.seed, grids=(a.S,), precision=abi.FP32)
+    train_d, test_d = draws[:a.n_train], draws[a.n_train:]
+    net = Surrogate(a.S, a.batch, seed=a.seed)
+    rep = {"S": a.S, "n_params": net.np, "n_train": a.n_train, "n_test": a.n_test, "seed": a.seed}
+    if a.weights:
+        net.load(a.weights)
+        rep["weights"] = a.weights
+    else:
+        t0 = time.perf_counter()
+        amps, info = ground_states(train_d, max_steps=a.gen_steps, tol=1e-12, frac=a.gen_frac)
+        rep["gen_s"] = time.perf_counter() - t0
+        rep["gen_rel_dE_median"] = float(np.median([i["rel"] for i in info]))
+        log(f"generated {len(amps)} ground states in {rep['gen_s']:.1f} s, median rel dE {rep['gen_rel_dE_median']:.2e}")
+        X = torch.empty((a.n_train, a.S, a.S, a.S, NFEAT), dtype=torch.bfloat16, device=net.dev)
+        BASE = torch.empty((a.n_train, a.S, a.S, a.S), dtype=torch.float32, device=net.dev)
+        Y = torch.empty_like(BASE)
+        for i, (prob, _) in enumerate(train_d):
+            f, base = features(prob)
+            X[i].copy_(torch.from_numpy(f).to(net.dev))
+            BASE[i].copy_(torch.from_numpy(base))
+            Y[i].copy_(torch.from_numpy(amps[i]))
+        rep["tf_guess_rmse"] = float(torch.sqrt(((BASE - Y) ** 2).mean()).item())
+        t0 = time.perf_counter()
+        hist = train(net, X, BASE, Y, epochs=a.epochs, lr=a.lr, lr_min=a.lr * 1e-2, seed=a.seed, log=log)
+        torch.cuda.synchronize()
+        rep["train_s"] = time.perf_counter() - t0
+        rep["train_steps"] = net.step_t
+        rep["loss_first"], rep["loss_last"] = hist[0], hist[-1]
+        rep["train_rmse"] = math.sqrt(hist[-1])
+        del X, BASE, Y
+        if a.out:
+            net.save(a.out, {"S": a.S, "n_train": a.n_train, "seed": a.seed, "epochs": a.epochs})
+    # held-out accuracy of the guess itself, then the relaxation comparison
+    feats, bases = zip(*[features(prob) for prob, _ in test_d])
+    pred = predict(net, list(feats), list(bases))
+    cmp_ = compare(net, test_d, tol=a.tol, max_steps=a.max_steps)
+    rep["compare"] = cmp_
+    log(json.dumps({k: v for k, v in cmp_.items() if k not in ("tf", "nn")}))
+    if a.json:
+        with open(a.json, "w") as f:
+            json.dump(rep, f, indent=1)
+    return rep
+
+
+if __name__ == "__main__":
+    main()
