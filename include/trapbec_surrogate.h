@@ -74,9 +74,15 @@ size_t tbsg_head_partials(size_t nvox, int c);
 int tbsg_head_loss(const void* feat, int c, const float* wh, const float* bh, const float* base,
                    const float* target, size_t nvox, float* dfeat, float* partials, float* out, void* stream);
 
-/* Adam with decoupled weight decay on FP32 parameters (step t >= 1).       */
+/* Adam with decoupled weight decay on FP32 parameters (step t >= 1); the
+ * gradient is multiplied by grad_scale[0] (device scalar, e.g. a clipping
+ * factor from tbsg_clip_scale; NULL = 1).                                  */
 int tbsg_adam(float* p, const float* g, float* m, float* v, size_t n, float lr, float beta1, float beta2,
-              float eps, float weight_decay, int t, void* stream);
+              float eps, float weight_decay, int t, const float* grad_scale, void* stream);
+
+/* Global-norm clipping factor: out[0] = ||g||_2, out[1] = min(1, max_norm / ||g||_2),
+ * reduced in a fixed order through `partials` (1024 floats).               */
+int tbsg_clip_scale(const float* g, size_t n, float max_norm, float* partials, float* out, void* stream);
 
 /* FP32 -> BF16 conversion (inputs of the first layer).                     */
 int tbsg_f32_to_bf16(const float* x, void* y, size_t n, void* stream);

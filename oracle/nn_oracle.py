@@ -62,7 +62,7 @@ def _grad_to_bf16(t: torch.Tensor) -> torch.Tensor:
     return t
 
 
-def forward(p: torch.Tensor, x: torch.Tensor, base: torch.Tensor, bf16: bool = False) -> torch.Tensor:
+def forward(p: torch.Tensor, x: torch.Tensor, base: torch.Tensor, bf16: bool = False, keep: dict | None = None):
     """bf16 = True rounds where the GPU path stores BF16: every activation
     and pooled tensor in the forward pass, and the gradient reaching each
     convolution's output (its dz); skip and pooling gradients stay unrounded."""
@@ -74,7 +74,11 @@ def forward(p: torch.Tensor, x: torch.Tensor, base: torch.Tensor, bf16: bool = F
         z = rg(conv3(t, *P[n]))
         if skip is not None:
             z = z + skip
-        return rf(act(z))
+        y = rf(act(z))
+        if keep is not None:   # activations (and, after backward, their gradients) by layer name
+            y.retain_grad()
+            keep[n] = y
+        return y
 
     pool = lambda t: rf(pool2(t))
     e0 = c("e0b", c("e0a", x))
@@ -88,10 +92,12 @@ def forward(p: torch.Tensor, x: torch.Tensor, base: torch.Tensor, bf16: bool = F
     return base + d0 @ wh + bh
 
 
-def loss_and_grad(p: np.ndarray, x: np.ndarray, base: np.ndarray, target: np.ndarray, bf16: bool = False):
-    """Loss mean((amp - target)^2) and its gradient w.r.t. the flat parameters (float64)."""
+def loss_and_grad(p: np.ndarray, x: np.ndarray, base: np.ndarray, target: np.ndarray, bf16: bool = False,
+                  keep: dict | None = None):
+    """Loss mean((amp - target)^2) and its gradient w.r.t. the flat parameters
+    (float64); `keep` receives each layer's output tensor (with .grad)."""
     pt = torch.tensor(p, dtype=torch.float64, requires_grad=True)
-    amp = forward(pt, torch.tensor(x, dtype=torch.float64), torch.tensor(base, dtype=torch.float64), bf16)
+    amp = forward(pt, torch.tensor(x, dtype=torch.float64), torch.tensor(base, dtype=torch.float64), bf16, keep)
     loss = ((amp - torch.tensor(target, dtype=torch.float64)) ** 2).mean()
     loss.backward()
     return float(loss.detach()), pt.grad.numpy().copy()

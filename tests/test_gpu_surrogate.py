@@ -151,11 +151,17 @@ def test_pool_up_act_head_adam():
     m = torch.zeros(100, dtype=torch.float32, device="cuda")
     v = torch.zeros(100, dtype=torch.float32, device="cuda")
     p1 = p0.clone()
-    assert lib.tbsg_adam(_p(p1), _p(gr), _p(m), _p(v), 100, 1e-2, 0.9, 0.999, 1e-8, 0.0, 1, st) == 0
+    assert lib.tbsg_adam(_p(p1), _p(gr), _p(m), _p(v), 100, 1e-2, 0.9, 0.999, 1e-8, 0.0, 1, None, st) == 0
     mh = 0.1 * gr.double() / 0.1
     vh = 0.001 * gr.double() ** 2 / 0.001
     want = p0.double() - 1e-2 * mh / (vh.sqrt() + 1e-8)
     assert (p1.double() - want).abs().max() <= 1e-6
+    # global-norm clipping factor
+    part = torch.empty(1024, dtype=torch.float32, device="cuda")
+    cs = torch.empty(2, dtype=torch.float32, device="cuda")
+    assert lib.tbsg_clip_scale(_p(gr), 100, 1.0, _p(part), _p(cs), st) == 0
+    nrm = gr.double().norm().item()
+    assert abs(cs[0].item() - nrm) <= 1e-6 * nrm and abs(cs[1].item() - min(1.0, 1.0 / nrm)) <= 1e-6
 
 
 def _net_inputs(S, B, seed):
@@ -183,17 +189,32 @@ def test_network_gradient_against_oracle():
         p[off:off + 27 * ci * co] = net.wb[name].double().cpu().numpy()
         off += 27 * ci * co + co
     xr = xt.to(torch.bfloat16).double().cpu().numpy()
+    # activations and the gradients reaching them, GPU name -> oracle layer name
+    act_names = {"e0a": "e0a", "e0": "e0b", "e1a": "e1a", "e1": "e1b", "e2a": "e2a", "e2": "e2b", "e3a": "e3a",
+                 "e3b": "e3b", "e3": "e3c", "d2a": "d2a", "d2": "d2b", "d1a": "d1a", "d1": "d1b", "d0a": "d0a",
+                 "d0": "d0b"}
+    report = {}
     for bf16, tol_l, tol_g in ((True, 1e-4, 2e-2), (False, 1e-2, 1.5e-1)):
-        lref, gref = nn_oracle.loss_and_grad(p, xr, base.astype(np.float64), tgt.astype(np.float64), bf16=bf16)
-        assert abs(loss - lref) <= tol_l * lref, (bf16, loss, lref)
-        off = 0
+        keep = {}
+        lref, gref = nn_oracle.loss_and_grad(p, xr, base.astype(np.float64), tgt.astype(np.float64), bf16=bf16,
+                                             keep=keep)
+        rel = lambda a, b: float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+        errs, off = {}, 0
         for name, ci, co in LAYERS:
-            for a, b in ((off, off + 27 * ci * co), (off + 27 * ci * co, off + 27 * ci * co + co)):
-                err = np.linalg.norm(g[a:b] - gref[a:b]) / np.linalg.norm(gref[a:b])
-                assert err < tol_g, (bf16, name, a == off, err)
+            errs["w_" + name] = rel(g[off:off + 27 * ci * co], gref[off:off + 27 * ci * co])
+            errs["b_" + name] = rel(g[off + 27 * ci * co:off + 27 * ci * co + co],
+                                    gref[off + 27 * ci * co:off + 27 * ci * co + co])
             off += 27 * ci * co + co
-        err = np.linalg.norm(g[off:] - gref[off:]) / np.linalg.norm(gref[off:])
-        assert err < tol_g / 2, (bf16, "head", err)
+        errs["head"] = rel(g[off:], gref[off:])
+        for an, on in act_names.items():
+            errs["act_" + an] = rel(net.A[an].double().cpu().numpy(), keep[on].detach().numpy())
+            if an in net.G:
+                errs["grad_" + an] = rel(net.G[an].double().cpu().numpy(), keep[on].grad.numpy())
+        report[bf16] = errs
+        bad = {k: v for k, v in errs.items() if (v >= tol_g and not k.startswith("act_")) or
+               (k.startswith("act_") and v >= (2e-3 if bf16 else 3e-2))}
+        assert abs(loss - lref) <= tol_l * lref, (bf16, loss, lref)
+        assert not bad, (bf16, bad, errs)
 
 
 def test_training_reduces_loss():

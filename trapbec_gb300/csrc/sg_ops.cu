@@ -160,15 +160,42 @@ __global__ void head_final_kernel(const float* partials, int nblk, int np, float
 }
 
 __global__ void adam_kernel(float* p, const float* g, float* m, float* v, size_t n, float lr, float b1, float b2,
-                            float eps, float wd, float bc1, float bc2) {
+                            float eps, float wd, float bc1, float bc2, const float* gscale) {
+  const float gs = gscale ? gscale[0] : 1.f;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    const float gi = g[i];
+    const float gi = g[i] * gs;
     const float mi = b1 * m[i] + (1.f - b1) * gi;
     const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
     m[i] = mi;
     v[i] = vi;
     const float mh = mi / bc1, vh = vi / bc2;
     p[i] -= lr * (mh / (sqrtf(vh) + eps) + wd * p[i]);
+  }
+}
+
+constexpr int CLIP_BLOCKS = 1024;
+
+__global__ void sumsq_kernel(const float* g, size_t n, float* partials) {
+  __shared__ double red[256];
+  double s = 0.0;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    s += (double)g[i] * g[i];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int k = 128; k > 0; k >>= 1) {
+    if ((int)threadIdx.x < k) red[threadIdx.x] += red[threadIdx.x + k];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partials[blockIdx.x] = (float)red[0];
+}
+
+__global__ void clip_final_kernel(const float* partials, int nblk, float max_norm, float* out) {
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int b = 0; b < nblk; ++b) s += partials[b];
+    const double nrm = sqrt(s);
+    out[0] = (float)nrm;
+    out[1] = nrm > max_norm ? (float)(max_norm / nrm) : 1.f;
   }
 }
 
@@ -256,11 +283,19 @@ int tbsg_head_loss(const void* feat, int c, const float* wh, const float* bh, co
 }
 
 int tbsg_adam(float* p, const float* g, float* m, float* v, size_t n, float lr, float beta1, float beta2, float eps,
-              float weight_decay, int t, void* stream) {
+              float weight_decay, int t, const float* grad_scale, void* stream) {
   if (!p || !g || !m || !v || t < 1) return TBSG_ERR_ARG;
   const float bc1 = 1.f - powf(beta1, (float)t), bc2 = 1.f - powf(beta2, (float)t);
   adam_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(p, g, m, v, n, lr, beta1, beta2, eps, weight_decay, bc1,
-                                                            bc2);
+                                                            bc2, grad_scale);
+  return done();
+}
+
+int tbsg_clip_scale(const float* g, size_t n, float max_norm, float* partials, float* out, void* stream) {
+  if (!g || !partials || !out || !(max_norm > 0.f)) return TBSG_ERR_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  sumsq_kernel<<<CLIP_BLOCKS, 256, 0, st>>>(g, n, partials);
+  clip_final_kernel<<<1, 32, 0, st>>>(partials, CLIP_BLOCKS, max_norm, out);
   return done();
 }
 

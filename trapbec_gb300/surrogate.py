@@ -125,8 +125,7 @@ class Surrogate:
         for name, ci, co in LAYERS:
             w0, b0, _, _ = self.view[name]
             host[w0:b0] = rng.normal(0.0, math.sqrt(2.0 / (27 * ci)), 27 * ci * co)
-        h0, h1, _, _ = self.view["head"]
-        host[h0:h1] = rng.normal(0.0, 1e-3, NFEAT)
+        # the head starts at zero: the untrained network returns the Thomas-Fermi amplitude
         self.p.copy_(torch.from_numpy(host))
         self.wb = {n: torch.empty(27 * ci * co, dtype=torch.bfloat16, device=self.dev) for n, ci, co in LAYERS}
         self.wt = {n: torch.empty(27 * ci * co, dtype=torch.bfloat16, device=self.dev) for n, ci, co in LAYERS}
@@ -165,6 +164,8 @@ class Surrogate:
         nvox = B * self.S ** 3
         self.partials = t.empty(self.lib.tbsg_head_partials(nvox, NFEAT), dtype=t.float32, device=self.dev)
         self.head_out = t.empty(NFEAT + 2, dtype=t.float32, device=self.dev)
+        self.clip_part = t.empty(1024, dtype=t.float32, device=self.dev)
+        self.clip_out = t.zeros(2, dtype=t.float32, device=self.dev)
         self.amp = t.empty((B, self.S, self.S, self.S), dtype=t.float32, device=self.dev)
 
     # -- plumbing -------------------------------------------------------------------
@@ -286,10 +287,15 @@ class Surrogate:
         self._act_bwd(G["e0a"], A["e0a"], dz[0]); self._conv_bwd("e0a", A["x0"], dz[0], s0, None)
         return self.head_out[0:1]
 
-    def adam_step(self, lr: float, beta1=0.9, beta2=0.999, eps=1e-8, weight_decay=0.0):
+    def adam_step(self, lr: float, beta1=0.9, beta2=0.999, eps=1e-8, weight_decay=0.0, max_norm: float = 1.0):
+        """One Adam step on the gradient of the last backward(), clipped to
+        global norm `max_norm` on the device (no host round trip)."""
         self.step_t += 1
+        self._ck(self.lib.tbsg_clip_scale(self._ptr(self.g), self.np, max_norm, self._ptr(self.clip_part),
+                                          self._ptr(self.clip_out), self._st()), "clip")
         self._ck(self.lib.tbsg_adam(self._ptr(self.p), self._ptr(self.g), self._ptr(self.m), self._ptr(self.v),
-                                    self.np, lr, beta1, beta2, eps, weight_decay, self.step_t, self._st()), "adam")
+                                    self.np, lr, beta1, beta2, eps, weight_decay, self.step_t,
+                                    self._ptr(self.clip_out[1:2]), self._st()), "adam")
         self.prep()
 
     # -- weights on disk -----------------------------------------------------------------
@@ -338,10 +344,11 @@ def ground_states(draws, max_steps: int, tol: float, frac: float = 0.6, chunk: i
 
 # ---- training -----------------------------------------------------------------------------
 
-def train(net: Surrogate, X, BASE, Y, epochs: int, lr: float = 2e-3, lr_min: float = 2e-5, seed: int = 0,
-          log=None) -> list[float]:
+def train(net: Surrogate, X, BASE, Y, epochs: int, lr: float = 5e-4, lr_min: float = 5e-6, seed: int = 0,
+          warmup: int = 100, max_norm: float = 1.0, log=None) -> list[float]:
     """Adam over the resident dataset (X [N,S,S,S,16] BF16, BASE and Y
-    [N,S,S,S] FP32, all on the device), cosine-decayed learning rate."""
+    [N,S,S,S] FP32, all on the device): linear warm-up over `warmup` steps,
+    then a cosine decay to lr_min; gradients clipped to global norm max_norm."""
     t = net.t
     N = X.shape[0]
     rng = np.random.default_rng(seed)
@@ -356,8 +363,11 @@ def train(net: Surrogate, X, BASE, Y, epochs: int, lr: float = 2e-3, lr_min: flo
             idx = t.from_numpy(order[s * net.B:(s + 1) * net.B].copy()).to(net.dev)
             net.forward(X.index_select(0, idx), BASE.index_select(0, idx))
             acc += net.backward(Y.index_select(0, idx))
-            cur = lr_min + 0.5 * (lr - lr_min) * (1 + math.cos(math.pi * k / total))
-            net.adam_step(cur)
+            if k < warmup:
+                cur = lr * (k + 1) / warmup
+            else:
+                cur = lr_min + 0.5 * (lr - lr_min) * (1 + math.cos(math.pi * (k - warmup) / max(1, total - warmup)))
+            net.adam_step(cur, max_norm=max_norm)
             k += 1
         hist.append(float(acc.item()) / steps_per_epoch)
         if log:
@@ -405,6 +415,14 @@ def compare(net: Surrogate, draws, tol: float = 1e-10, max_steps: int = 60000, c
     ev1.record()
     t.cuda.synchronize()
     infer_ms = ev0.elapsed_time(ev1)
+    # the fallback: a prediction far from the Thomas-Fermi profile is not used
+    fallback = []
+    for i, (a_, base_) in enumerate(zip(amps, bases)):
+        rms = float(np.sqrt(np.mean((a_ - base_) ** 2)))
+        bad = not np.all(np.isfinite(a_)) or rms > 0.25 or a_.max() > 1.5
+        fallback.append(bad)
+        if bad:
+            amps[i] = base_
     for mode in ("tf", "nn"):
         b = BatchSolver(params)
         for i, (_, ini) in enumerate(draws):
@@ -431,14 +449,20 @@ def compare(net: Surrogate, draws, tol: float = 1e-10, max_steps: int = 60000, c
         ph = ph / abs(ph) if abs(ph) > 0 else 1.0
         l2.append(float(np.linalg.norm(a - c * ph) / np.linalg.norm(a)))
     de = [abs(x - y) / abs(x) for x, y in zip(res["tf"]["energy"], res["nn"]["energy"])]
+    # accuracy of the two guesses against the converged Thomas-Fermi-guess state
+    rms = lambda a, b: float(np.sqrt(np.mean((a - b) ** 2)))
+    guess_tf = [rms(np.abs(f), b_) for f, b_ in zip(finals["tf"], bases)]
+    guess_nn = [rms(np.abs(f), a_) for f, a_ in zip(finals["tf"], amps)]
     s_tf, s_nn = np.array(res["tf"]["steps"], float), np.array(res["nn"]["steps"], float)
     return {
         "instances": len(draws), "tol_rel_dE": tol, "dtau_trap_units": draws[0][0].dt,
+        "nn_fallback_to_tf": int(sum(fallback)),
         "tf": res["tf"], "nn": res["nn"], "nn_inference_ms": infer_ms,
         "steps_ratio_median": float(np.median(s_tf / np.maximum(s_nn, 1))),
         "steps_ratio_total": float(s_tf.sum() / max(s_nn.sum(), 1)),
         "wall_ratio_device": res["tf"]["solve_ms_device"] / (res["nn"]["solve_ms_device"] + infer_ms),
         "final_energy_rel_diff_max": float(max(de)), "final_l2_rel": l2,
+        "guess_rmse_tf": guess_tf, "guess_rmse_nn": guess_nn,
     }
 
 
@@ -457,7 +481,7 @@ def main(argv=None):
     ap.add_argument("--gen-frac", type=float, default=0.85, help="fraction of the RK3 stability limit for data")
     ap.add_argument("--epochs", type=int, default=60)
     ap.add_argument("--batch", type=int, default=2)
-    ap.add_argument("--lr", type=float, default=2e-3)
+    ap.add_argument("--lr", type=float, default=5e-4)
     ap.add_argument("--tol", type=float, default=1e-10)
     ap.add_argument("--max-steps", type=int, default=60000)
     ap.add_argument("--weights", default=None, help="load weights instead of training")
@@ -490,6 +514,7 @@ def main(argv=None):
         rep["tf_guess_rmse"] = float(torch.sqrt(((BASE - Y) ** 2).mean()).item())
         t0 = time.perf_counter()
         hist = train(net, X, BASE, Y, epochs=a.epochs, lr=a.lr, lr_min=a.lr * 1e-2, seed=a.seed, log=log)
+        rep["loss_history"] = hist
         torch.cuda.synchronize()
         rep["train_s"] = time.perf_counter() - t0
         rep["train_steps"] = net.step_t
