@@ -177,6 +177,7 @@ def test_network_gradient_against_oracle():
     activations) against the float64 oracle on the same BF16 weights/inputs."""
     S, B = 16, 2
     net = Surrogate(S, B, seed=3)
+    net.p[-(NFEAT + 1):].copy_(torch.linspace(-0.5, 0.5, NFEAT + 1))   # a non-zero head
     x, base, tgt = _net_inputs(S, B, 1)
     xt = torch.tensor(x).cuda()
     net.forward(xt, torch.tensor(base).cuda())
