@@ -431,7 +431,12 @@ def compare(net: Surrogate, draws, tol: float = 1e-10, max_steps: int = 60000, c
                 noisy = b.get_psi(i)
                 _tf_noise(b, i, ini, noise=False)
                 clean = b.get_psi(i)
-                b.set_psi(i, (amps[i] + (noisy - clean)).astype(noisy.dtype))
+                guess = amps[i] + (noisy - clean)
+                # the solver keeps the norm of its initial state: give the NN
+                # guess the norm of the Thomas-Fermi guess (the same atom number)
+                n_tf = np.sum(np.abs(noisy.astype(np.complex128)) ** 2)
+                n_nn = np.sum(np.abs(guess.astype(np.complex128)) ** 2)
+                b.set_psi(i, (guess * math.sqrt(n_tf / n_nn)).astype(noisy.dtype))
         t0 = time.perf_counter()
         out = b.solve(max_steps=max_steps, tol=tol, check_every=check_every)
         wall = time.perf_counter() - t0
