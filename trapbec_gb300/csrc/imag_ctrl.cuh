@@ -12,12 +12,22 @@
 
 namespace tb {
 
+// Energy and mu of the incoming renormalised state, taken at exactly the
+// target norm n0: the state was scaled in its own precision, so its norm
+// misses n0 by that rounding (about 1e-10 relative for FP32 grids of 1e5-1e6
+// cells), and the energy would carry the same noise into the convergence
+// test.  The sums separate the quadratic terms (kinetic, potential,
+// rotation) from the quartic one, so E(kappa psi) = kappa^2 Q + kappa^4 q4
+// with kappa^2 = n0 / N is exact in FP64.
 __device__ __forceinline__ void imag_energy_update(const double* r, ImagCtrl* c) {
   const double dV = c->dV;
-  const double E = dV * (-0.5 * r[1] + 0.5 * r[2] + 0.25 * r[3] - 0.5 * r[4]);
-  const double mu = (-0.5 * r[1] + 0.5 * r[2] + 0.5 * r[3] - 0.5 * r[4]) / r[0];
-  if (!isfinite(E) || r[8] != 0.0) { c->nonfinite = 1; return; }
+  if (r[8] != 0.0 || !(r[0] > 0.0)) { c->nonfinite = 1; return; }
   if (c->n0 <= 0.0) c->n0 = dV * r[0];   // norm target unset: keep the initial norm
+  const double k2 = c->n0 / (dV * r[0]);
+  const double Q = -0.5 * r[1] + 0.5 * r[2] - 0.5 * r[4];
+  const double E = dV * (k2 * Q + k2 * k2 * 0.25 * r[3]);
+  const double mu = (Q + k2 * 0.5 * r[3]) / r[0];
+  if (!isfinite(E)) { c->nonfinite = 1; return; }
   if (c->have_prev) {
     const double rel = fabs(E - c->e_prev) / fabs(E);
     c->rel = rel;
