@@ -394,18 +394,59 @@ def predict(net: Surrogate, feats: list[np.ndarray], bases: list[np.ndarray]) ->
 
 # ---- the comparison: NN guess against the Thomas-Fermi guess ---------------------------------------
 
-def compare(net: Surrogate, draws, tol: float = 1e-10, max_steps: int = 60000, check_every: int = 200) -> dict:
-    """Relax the held-out draws twice at the workload's step (dtau = 0.002):
-    from the Thomas-Fermi + 1e-2 noise guess (the plain method) and from the
-    surrogate amplitude + the same noise.  Reports steps and wall time to the
-    relative energy-change tolerance, the final energies and the L2 distance
-    of the final states (after aligning the global phase)."""
+def _guesses(draws, amps, nn_noise: float):
+    """Host copies of the two initial states per draw: the Thomas-Fermi guess
+    with its seeded 1e-2 noise (the plain method) and the NN amplitude with
+    the same seeded noise pattern scaled to `nn_noise`, given the TF guess's
+    norm (the solver keeps the norm of its initial state)."""
     from .batch import BatchSolver
+    b = BatchSolver([prob.to_params() for prob, _ in draws])
+    tf, nn = [], []
+    for i, (_, ini) in enumerate(draws):
+        _tf_noise(b, i, ini)
+        noisy = b.get_psi(i)
+        _tf_noise(b, i, ini, noise=False)
+        clean = b.get_psi(i)
+        scale = nn_noise / ini["noise_amp"] if ini["noise_amp"] > 0 else 0.0
+        guess = amps[i] + (noisy - clean) * scale
+        n_tf = np.sum(np.abs(noisy.astype(np.complex128)) ** 2)
+        n_nn = np.sum(np.abs(guess.astype(np.complex128)) ** 2)
+        tf.append(noisy)
+        nn.append((guess * math.sqrt(n_tf / n_nn)).astype(noisy.dtype))
+    b.close()
+    return tf, nn
+
+
+def _relax(params, states, tol, max_steps, check_every, energy_only=False):
+    from .batch import BatchSolver
+    b = BatchSolver(params)
+    for i, s in enumerate(states):
+        b.set_psi(i, s)
+    t0 = time.perf_counter()
+    out = b.solve(max_steps=1 if energy_only else max_steps, tol=0.0 if energy_only else tol,
+                  check_every=check_every)
+    wall = time.perf_counter() - t0
+    st = b.stats()
+    res = {"steps": out["steps"], "energy": out["energy"],
+           "converged": [b.status(i)["converged"] > 0 for i in range(len(states))],
+           "solve_ms_device": st["solve_ms"], "wall_s": wall}
+    finals = None if energy_only else [b.get_psi(i) for i in range(len(states))]
+    b.close()
+    return res, finals
+
+
+def compare(net: Surrogate, draws, tol: float = 1e-10, max_steps: int = 60000, check_every: int = 200,
+            nn_noise: float = 1e-2) -> dict:
+    """Relax the held-out draws twice at the workload's step (dtau = 0.002):
+    from the Thomas-Fermi + 1e-2 noise guess (the plain method) and with the
+    surrogate.  The surrogate's initial state is its amplitude plus the same
+    seeded noise pattern at `nn_noise`, unless the Thomas-Fermi guess has the
+    lower energy at the same norm (or the prediction is unreasonable), in
+    which case the Thomas-Fermi guess is the fallback.  Reports steps and
+    device time to the relative energy-change tolerance, the final energies
+    and the L2 distance of the final states (global phase aligned)."""
     t = net.t
     params = [prob.to_params() for prob, _ in draws]
-    res = {}
-    finals = {}
-    # surrogate inference, timed with events around forward passes
     feats, bases = zip(*[features(prob) for prob, _ in draws])
     predict(net, list(feats[:net.B]), list(bases[:net.B]))   # warm-up
     ev0, ev1 = t.cuda.Event(enable_timing=True), t.cuda.Event(enable_timing=True)
@@ -415,37 +456,22 @@ def compare(net: Surrogate, draws, tol: float = 1e-10, max_steps: int = 60000, c
     ev1.record()
     t.cuda.synchronize()
     infer_ms = ev0.elapsed_time(ev1)
-    # the fallback: a prediction far from the Thomas-Fermi profile is not used
-    fallback = []
+    unreasonable = []
     for i, (a_, base_) in enumerate(zip(amps, bases)):
         rms = float(np.sqrt(np.mean((a_ - base_) ** 2)))
         bad = not np.all(np.isfinite(a_)) or rms > 0.25 or a_.max() > 1.5
-        fallback.append(bad)
+        unreasonable.append(bad)
         if bad:
             amps[i] = base_
-    for mode in ("tf", "nn"):
-        b = BatchSolver(params)
-        for i, (_, ini) in enumerate(draws):
-            _tf_noise(b, i, ini)
-            if mode == "nn":
-                noisy = b.get_psi(i)
-                _tf_noise(b, i, ini, noise=False)
-                clean = b.get_psi(i)
-                guess = amps[i] + (noisy - clean)
-                # the solver keeps the norm of its initial state: give the NN
-                # guess the norm of the Thomas-Fermi guess (the same atom number)
-                n_tf = np.sum(np.abs(noisy.astype(np.complex128)) ** 2)
-                n_nn = np.sum(np.abs(guess.astype(np.complex128)) ** 2)
-                b.set_psi(i, (guess * math.sqrt(n_tf / n_nn)).astype(noisy.dtype))
-        t0 = time.perf_counter()
-        out = b.solve(max_steps=max_steps, tol=tol, check_every=check_every)
-        wall = time.perf_counter() - t0
-        st = b.stats()
-        conv = [b.status(i)["converged"] > 0 for i in range(len(draws))]
-        finals[mode] = [b.get_psi(i) for i in range(len(draws))]
-        res[mode] = {"steps": out["steps"], "energy": out["energy"], "converged": conv,
-                     "solve_ms_device": st["solve_ms"], "wall_s": wall}
-        b.close()
+    tf_states, nn_states = _guesses(draws, amps, nn_noise)
+    # the selector: the guess with the lower energy at the same norm
+    e_tf, _ = _relax(params, tf_states, tol, max_steps, check_every, energy_only=True)
+    e_nn, _ = _relax(params, nn_states, tol, max_steps, check_every, energy_only=True)
+    use_nn = [(not bad) and en < et for bad, en, et in zip(unreasonable, e_nn["energy"], e_tf["energy"])]
+    chosen = [n if u else f for n, f, u in zip(nn_states, tf_states, use_nn)]
+    res, finals = {}, {}
+    res["tf"], finals["tf"] = _relax(params, tf_states, tol, max_steps, check_every)
+    res["nn"], finals["nn"] = _relax(params, chosen, tol, max_steps, check_every)
     l2 = []
     for a, c in zip(finals["tf"], finals["nn"]):
         a = a.astype(np.complex128).ravel()
@@ -454,20 +480,24 @@ def compare(net: Surrogate, draws, tol: float = 1e-10, max_steps: int = 60000, c
         ph = ph / abs(ph) if abs(ph) > 0 else 1.0
         l2.append(float(np.linalg.norm(a - c * ph) / np.linalg.norm(a)))
     de = [abs(x - y) / abs(x) for x, y in zip(res["tf"]["energy"], res["nn"]["energy"])]
-    # accuracy of the two guesses against the converged Thomas-Fermi-guess state
     rms = lambda a, b: float(np.sqrt(np.mean((a - b) ** 2)))
-    guess_tf = [rms(np.abs(f), b_) for f, b_ in zip(finals["tf"], bases)]
-    guess_nn = [rms(np.abs(f), a_) for f, a_ in zip(finals["tf"], amps)]
     s_tf, s_nn = np.array(res["tf"]["steps"], float), np.array(res["nn"]["steps"], float)
+    both = np.array([a and b for a, b in zip(res["tf"]["converged"], res["nn"]["converged"])])
+    ratio = s_tf / np.maximum(s_nn, 1)
     return {
-        "instances": len(draws), "tol_rel_dE": tol, "dtau_trap_units": draws[0][0].dt,
-        "nn_fallback_to_tf": int(sum(fallback)),
+        "instances": len(draws), "tol_rel_dE": tol, "dtau_trap_units": draws[0][0].dt, "nn_noise": nn_noise,
+        "nn_used": int(sum(use_nn)), "nn_unreasonable": int(sum(unreasonable)),
+        "guess_energy_tf": e_tf["energy"], "guess_energy_nn": e_nn["energy"],
         "tf": res["tf"], "nn": res["nn"], "nn_inference_ms": infer_ms,
-        "steps_ratio_median": float(np.median(s_tf / np.maximum(s_nn, 1))),
+        "steps_ratio_per_instance": ratio.tolist(),
+        "steps_ratio_median": float(np.median(ratio)),
+        "steps_ratio_median_nn_used": float(np.median(ratio[np.array(use_nn)])) if any(use_nn) else None,
         "steps_ratio_total": float(s_tf.sum() / max(s_nn.sum(), 1)),
+        "steps_ratio_total_both_converged": float(s_tf[both].sum() / max(s_nn[both].sum(), 1)) if both.any() else None,
         "wall_ratio_device": res["tf"]["solve_ms_device"] / (res["nn"]["solve_ms_device"] + infer_ms),
         "final_energy_rel_diff_max": float(max(de)), "final_l2_rel": l2,
-        "guess_rmse_tf": guess_tf, "guess_rmse_nn": guess_nn,
+        "guess_rmse_tf": [rms(np.abs(f), b_) for f, b_ in zip(finals["tf"], bases)],
+        "guess_rmse_nn": [rms(np.abs(f), a_) for f, a_ in zip(finals["tf"], amps)],
     }
 
 
@@ -489,6 +519,8 @@ def main(argv=None):
     ap.add_argument("--lr", type=float, default=5e-4)
     ap.add_argument("--tol", type=float, default=1e-10)
     ap.add_argument("--max-steps", type=int, default=60000)
+    ap.add_argument("--nn-noise", type=float, nargs="+", default=[1e-2],
+                    help="noise level(s) of the NN guess (the TF guess keeps 1e-2)")
     ap.add_argument("--weights", default=None, help="load weights instead of training")
     ap.add_argument("--out", default=None, help="save the trained weights (.npz)")
     ap.add_argument("--json", default=None)
@@ -529,11 +561,13 @@ def main(argv=None):
         if a.out:
             net.save(a.out, {"S": a.S, "n_train": a.n_train, "seed": a.seed, "epochs": a.epochs})
     # held-out accuracy of the guess itself, then the relaxation comparison
-    feats, bases = zip(*[features(prob) for prob, _ in test_d])
-    pred = predict(net, list(feats), list(bases))
-    cmp_ = compare(net, test_d, tol=a.tol, max_steps=a.max_steps)
-    rep["compare"] = cmp_
-    log(json.dumps({k: v for k, v in cmp_.items() if k not in ("tf", "nn")}))
+    rep["compare"] = []
+    for nz in a.nn_noise:
+        cmp_ = compare(net, test_d, tol=a.tol, max_steps=a.max_steps, nn_noise=nz)
+        rep["compare"].append(cmp_)
+        log(json.dumps({k: cmp_[k] for k in ("nn_noise", "nn_used", "steps_ratio_median", "steps_ratio_median_nn_used",
+                                              "steps_ratio_total", "steps_ratio_total_both_converged",
+                                              "wall_ratio_device", "final_energy_rel_diff_max")}))
     if a.json:
         with open(a.json, "w") as f:
             json.dump(rep, f, indent=1)
