@@ -199,6 +199,36 @@ def imag_leg(args):
             "tile": [st["tile_z"], st["tile_y"]], "precision": "c64 state, FP64 norm/energy/test"}
 
 
+def warmstart_leg(args):
+    """Imaginary-time relaxation to |dE|/|E| <= tol at 128^3 from the
+    surrogate's guess against the Thomas-Fermi + 1e-2 noise guess, on draws
+    held out from the surrogate's training set (the committed weights were
+    trained on draws 0..191 of seed 2024; this leg uses the draws after them).
+    Both relaxations run batched; device time from events around each solve."""
+    from trapbec_gb300 import abi, units, surrogate
+    n0 = 192
+    draws = units.ground_state_draws(n0 + args.ws_count, 2024, grids=(128,), precision=abi.FP32)[n0:]
+    net = surrogate.Surrogate(128, 2, seed=0)
+    net.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "trapbec_gb300", "weights",
+                          "surrogate_128.npz"))
+    r = surrogate.compare(net, draws, tol=args.imag_tol, max_steps=args.ws_max_steps)
+    med = lambda v: float(statistics.median(v))
+    return {
+        "grid": 128, "instances": len(draws), "held_out": f"draws {n0}..{n0 + len(draws) - 1} of seed 2024",
+        "tol_rel_dE": args.imag_tol, "dtau_trap_units": 0.002, "max_steps": args.ws_max_steps,
+        "surrogate_params": net.np, "nn_used": r["nn_used"],
+        "steps_tf": r["tf"]["steps"], "steps_nn": r["nn"]["steps"],
+        "converged_tf": int(sum(r["tf"]["converged"])), "converged_nn": int(sum(r["nn"]["converged"])),
+        "steps_ratio_median": r["steps_ratio_median"], "steps_ratio_median_nn_used": r["steps_ratio_median_nn_used"],
+        "steps_ratio_total_both_converged": r["steps_ratio_total_both_converged"],
+        "device_ms_tf": r["tf"]["solve_ms_device"], "device_ms_nn": r["nn"]["solve_ms_device"],
+        "nn_inference_ms": r["nn_inference_ms"], "wall_ratio_device": r["wall_ratio_device"],
+        "final_energy_rel_diff_max": r["final_energy_rel_diff_max"],
+        "guess_rmse_median_tf": med(r["guess_rmse_tf"]), "guess_rmse_median_nn": med(r["guess_rmse_nn"]),
+        "fallback": "TF guess where its energy at the same norm is lower (rotating, vortex states)",
+    }
+
+
 def run_gpu_arm(args):
     import numpy as np
     import torch
@@ -336,6 +366,8 @@ def run_gpu_arm(args):
         line["fp64"] = fp64
     if args.imag and rank == 0:
         line["imag"] = imag_leg(args)
+    if rank == 0 and world == 1 and not args.no_warmstart:
+        line["warmstart"] = warmstart_leg(args)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:
@@ -365,6 +397,9 @@ def main():
     ap.add_argument("--imag-grids", type=int, nargs="+", default=[64, 96, 128])
     ap.add_argument("--imag-tol", type=float, default=1e-10)
     ap.add_argument("--imag-max-steps", type=int, default=20000)
+    ap.add_argument("--no-warmstart", action="store_true", help="skip the NN-vs-TF imaginary-time leg")
+    ap.add_argument("--ws-count", type=int, default=8, help="held-out draws of the NN-vs-TF leg")
+    ap.add_argument("--ws-max-steps", type=int, default=20000)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
