@@ -503,6 +503,50 @@ def compare(net: Surrogate, draws, tol: float = 1e-10, max_steps: int = 60000, c
 
 # ---- command line: generate, train, compare ----------------------------------------------------
 
+def conv_flops(S: int, batch: int) -> tuple[float, float]:
+    """FLOPs of the convolutions of one forward pass and of one backward pass
+    (input gradients for every layer but the first, weight gradients for all)."""
+    lev = [0, 0, 1, 1, 2, 2, 3, 3, 3, 2, 2, 1, 1, 0, 0]
+    fwd = sum(2.0 * 27 * ci * co * batch * (S >> l) ** 3 for (_, ci, co), l in zip(LAYERS, lev))
+    first = 2.0 * 27 * 16 * 16 * batch * S ** 3
+    return fwd, 2 * fwd - first
+
+
+def time_passes(S: int, batch: int, reps: int) -> dict:
+    """Device time of forward and forward+backward+Adam passes (random weights
+    and inputs) and the tensor-core rate of the convolutions."""
+    torch = _torch()
+    net = Surrogate(S, batch, seed=1)
+    net.p[-(NFEAT + 1):].copy_(torch.linspace(-0.5, 0.5, NFEAT + 1))
+    net.prep()
+    g = torch.Generator(device="cpu").manual_seed(0)
+    x = torch.randn((batch, S, S, S, NFEAT), generator=g).to(net.dev).to(torch.bfloat16)
+    base = torch.rand((batch, S, S, S), generator=g).to(net.dev)
+    tgt = base + 0.05
+    for _ in range(2):
+        net.forward(x, base)
+        net.backward(tgt)
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    torch.cuda.synchronize()
+    e[0].record()
+    for _ in range(reps):
+        net.forward(x, base)
+    e[1].record()
+    for _ in range(reps):
+        net.forward(x, base)
+        net.backward(tgt)
+        net.adam_step(1e-6)
+    e[2].record()
+    torch.cuda.synchronize()
+    f_ms = e[0].elapsed_time(e[1]) / reps
+    t_ms = e[1].elapsed_time(e[2]) / reps
+    ff, fb = conv_flops(S, batch)
+    return {"S": S, "batch": batch, "forward_ms": f_ms, "train_step_ms": t_ms,
+            "conv_tflops_forward": ff / (f_ms * 1e-3) / 1e12,
+            "conv_tflops_train_step": (ff + fb) / (t_ms * 1e-3) / 1e12,
+            "conv_gflop_forward": ff / 1e9, "conv_gflop_backward": fb / 1e9}
+
+
 def main(argv=None):
     import argparse
     import json
@@ -524,7 +568,16 @@ def main(argv=None):
     ap.add_argument("--weights", default=None, help="load weights instead of training")
     ap.add_argument("--out", default=None, help="save the trained weights (.npz)")
     ap.add_argument("--json", default=None)
+    ap.add_argument("--time", type=int, default=0, metavar="REPS",
+                    help="only time forward and training passes (random weights) and exit")
     a = ap.parse_args(argv)
+    if a.time:
+        r = time_passes(a.S, a.batch, a.time)
+        print(json.dumps(r), flush=True)
+        if a.json:
+            with open(a.json, "w") as f:
+                json.dump(r, f, indent=1)
+        return r
     torch = _torch()
     log = lambda m: print(m, flush=True)
     draws = units.ground_state_draws(a.n_train + a.n_test, a.seed, grids=(a.S,), precision=abi.FP32)
