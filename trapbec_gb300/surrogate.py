@@ -342,6 +342,37 @@ def ground_states(draws, max_steps: int, tol: float, frac: float = 0.6, chunk: i
     return amps, info
 
 
+def azimuthal_average(a: np.ndarray) -> np.ndarray:
+    """The amplitude averaged over rotations about the trap axis (z through
+    the grid centre), per z plane: means over rings of width one cell,
+    linearly interpolated back to the cells by radius."""
+    nx, ny, nz = a.shape
+    x = np.arange(nx) - (nx - 1) / 2.0
+    y = np.arange(ny) - (ny - 1) / 2.0
+    r = np.sqrt(x[:, None] ** 2 + y[None, :] ** 2).ravel()
+    b = np.floor(r).astype(np.int64)
+    nb = b.max() + 1
+    cnt = np.bincount(b, minlength=nb).astype(np.float64)
+    rmean = np.bincount(b, weights=r, minlength=nb) / np.maximum(cnt, 1)
+    flat = a.reshape(nx * ny, nz).astype(np.float64)
+    out = np.empty_like(flat)
+    for k in range(nz):
+        m = np.bincount(b, weights=flat[:, k], minlength=nb) / np.maximum(cnt, 1)
+        out[:, k] = np.interp(r, rmean, m)
+    return out.reshape(a.shape).astype(a.dtype)
+
+
+def training_target(amp: np.ndarray, vortex_dev: float = 0.1) -> tuple[np.ndarray, bool]:
+    """A ground-state amplitude as a training target: states that deviate
+    from their azimuthal average by more than `vortex_dev` somewhere carry
+    vortices at symmetry-broken positions no amplitude predictor can learn,
+    and are replaced by that average."""
+    av = azimuthal_average(amp)
+    if np.max(np.abs(amp - av)) > vortex_dev:
+        return av, True
+    return amp, False
+
+
 # ---- training -----------------------------------------------------------------------------
 
 def train(net: Surrogate, X, BASE, Y, epochs: int, lr: float = 5e-4, lr_min: float = 5e-6, seed: int = 0,
@@ -566,6 +597,8 @@ def main(argv=None):
     ap.add_argument("--nn-noise", type=float, nargs="+", default=[1e-2],
                     help="noise level(s) of the NN guess (the TF guess keeps 1e-2)")
     ap.add_argument("--weights", default=None, help="load weights instead of training")
+    ap.add_argument("--symmetrize", type=int, default=1,
+                    help="train vortex states on their azimuthal average (1) or as they are (0)")
     ap.add_argument("--out", default=None, help="save the trained weights (.npz)")
     ap.add_argument("--json", default=None)
     ap.add_argument("--time", type=int, default=0, metavar="REPS",
@@ -596,11 +629,15 @@ def main(argv=None):
         X = torch.empty((a.n_train, a.S, a.S, a.S, NFEAT), dtype=torch.bfloat16, device=net.dev)
         BASE = torch.empty((a.n_train, a.S, a.S, a.S), dtype=torch.float32, device=net.dev)
         Y = torch.empty_like(BASE)
+        n_vortex = 0
         for i, (prob, _) in enumerate(train_d):
             f, base = features(prob)
             X[i].copy_(torch.from_numpy(f).to(net.dev))
             BASE[i].copy_(torch.from_numpy(base))
-            Y[i].copy_(torch.from_numpy(amps[i]))
+            tgt, vort = training_target(amps[i]) if a.symmetrize else (amps[i], False)
+            n_vortex += vort
+            Y[i].copy_(torch.from_numpy(tgt))
+        rep["targets_symmetrized"] = n_vortex
         rep["tf_guess_rmse"] = float(torch.sqrt(((BASE - Y) ** 2).mean()).item())
         t0 = time.perf_counter()
         hist = train(net, X, BASE, Y, epochs=a.epochs, lr=a.lr, lr_min=a.lr * 1e-2, seed=a.seed, log=log)
