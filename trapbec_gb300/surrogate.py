@@ -597,7 +597,7 @@ def main(argv=None):
     ap.add_argument("--nn-noise", type=float, nargs="+", default=[1e-2],
                     help="noise level(s) of the NN guess (the TF guess keeps 1e-2)")
     ap.add_argument("--weights", default=None, help="load weights instead of training")
-    ap.add_argument("--symmetrize", type=int, default=1,
+    ap.add_argument("--symmetrize", type=int, default=0,
                     help="train vortex states on their azimuthal average (1) or as they are (0)")
     ap.add_argument("--out", default=None, help="save the trained weights (.npz)")
     ap.add_argument("--json", default=None)
