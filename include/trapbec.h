@@ -215,6 +215,15 @@ typedef struct trapbec_diag_out {
 } trapbec_diag_out;
 int trapbec_diag(trapbec_ctx* ctx, trapbec_diag_out* out);
 
+/* Bounded waits of the tiled stage kernels (no counterpart in the reference).
+ * Every wait of a launch for its TMA data gives up after `limit` polls
+ * (0 = the default, 2^24), records TRAPBEC_ERR_TIMEOUT, lets the copies in
+ * flight land and returns; the call then returns TRAPBEC_ERR_TIMEOUT and the
+ * context stays usable (psi is not meaningful after it).  inject = 1 is a
+ * test hook: every wait then waits for an mbarrier phase that nothing
+ * completes, so the timeout path runs without any fault.                   */
+int trapbec_set_wait_limit(trapbec_ctx* ctx, uint32_t limit, int inject);
+
 /* Forcing (force_random_points, force.f90:12-54): multiply psi by a Pade
  * vortex sqrt(r^2 (c1 + c2 r^2) / (1 + c3 r^2 + c2 r^4)) e^{i dir theta},
  * straight along z through (x0, y0); dir = +1 or -1.

@@ -133,6 +133,7 @@ _PROTOS = {
     "trapbec_step_imag": (C.c_int, [_VP, C.c_int, C.c_int, C.c_double,
                                     C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     "trapbec_diag": (C.c_int, [_VP, C.POINTER(DiagOut)]),
+    "trapbec_set_wait_limit": (C.c_int, [_VP, C.c_uint32, C.c_int]),
     "trapbec_force_vortex": (C.c_int, [_VP, C.c_double, C.c_double, C.c_double]),
     "trapbec_force_random_points": (C.c_int, [_VP, C.c_uint64, C.c_uint64, C.POINTER(C.c_double)]),
     "trapbec_get_velocity": (C.c_int, [_VP, _VP]),

@@ -20,7 +20,10 @@
 // whose rotation is resolved at compile time (the x loop is unrolled by 7).
 // FP32 complex arithmetic uses Blackwell's packed f32x2 add/mul/fma.
 // Every mbarrier wait is bounded: on timeout the kernel records an error
-// code, drains its own copies (also bounded) and returns.
+// code, lets the copies it has in flight land (a wait on each, also bounded)
+// and returns.  A test hook (inject_wait) points every wait at an extra
+// mbarrier that nothing arrives on, so the timeout path can be exercised
+// without a fault.
 #pragma once
 #include <cuda.h>
 
@@ -90,6 +93,8 @@ template <typename T> struct TiledArgs {
   int bcz;                 // boundary type along z (periodic if zper)
   int fix_y, fix_z;        // ghost fix-up needed on y / z boundary tiles
   int chunk;               // x-chunk length of the work order
+  uint32_t spin_limit;     // try_wait calls before a wait gives up (WAIT_SPIN_LIMIT by default)
+  int inject_wait;         // test hook: every wait waits for a phase that never completes
   // Packed coefficients, formed on the host so the kernel can take them from
   // the parameter (constant) bank instead of holding them in registers:
   // 0-2: (2,-27,270)/(180 hx^2), 3-5: y, 6-8: z, 9: -490*sum(1/(180 h^2)),
@@ -133,7 +138,7 @@ template <typename T, int TZ, int TY, int R, int NSLOT = 8, int MINB = 0> struct
   static constexpr int W_OFF_ELEMS = W_OFF / (int)sizeof(c_t<T>);
   static constexpr int NT = TZ * (TY / R);
   static constexpr int S = NSLOT;                   // ring slots
-  static constexpr int SMEM = S * SLOT_STRIDE + S * 8;
+  static constexpr int SMEM = S * SLOT_STRIDE + (S + 1) * 8;
   // CTAs per SM the register allocation is sized for
   static constexpr int MIN_BLOCKS = MINB > 0 ? MINB : ((sizeof(T) == 4 && NT < 512) ? 2 : 1);
 };
@@ -175,7 +180,7 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
 
   extern __shared__ __align__(128) unsigned char smem_raw[];
   V* ring = reinterpret_cast<V*>(smem_raw);
-  uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + S * G::SLOT_STRIDE);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + S * G::SLOT_STRIDE);   // S slots + 1 never-completed
 
   const int tid = threadIdx.x;
   const int lz = tid % TZ;
@@ -187,7 +192,7 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
   }
 
   if (tid == 0) {
-    for (int s = 0; s < S; ++s) mbar_init(&bars[s], 1);
+    for (int s = 0; s <= S; ++s) mbar_init(&bars[s], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
@@ -333,11 +338,11 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
     }
 
     auto wait_plane = [&](uint32_t sq) {
-      const int sl = sq % S;
-      const uint32_t par = (sq / S) & 1u;
+      const int sl = ta.inject_wait ? S : (int)(sq % S);
+      const uint32_t par = ta.inject_wait ? 0u : (sq / S) & 1u;
       uint32_t spins = 0;
       while (!mbar_try_wait(&bars[sl], par)) {
-        if (++spins > WAIT_SPIN_LIMIT) {
+        if (++spins > ta.spin_limit) {
           failed = true;
           atomicExch(ta.err, (int)TERR_WAIT_TIMEOUT);
           break;
@@ -391,7 +396,9 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
       for (int r = 0; r < R; ++r) q[j][r] = sl[qoff + r * TZP];
     }
     __syncthreads();
-    if (tid == 0) {
+    // a slot is refilled only after its previous copy was waited for: once a
+    // wait of the issuing thread gave up, nothing more is issued
+    if (tid == 0 && !failed) {
       for (int j = 0; j < 3; ++j) {
         const int p = xa - 3 + j + S;
         if (p > plast) break;
@@ -520,7 +527,7 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
         }
       }
       __syncthreads();
-      if (tid == 0 && x + S <= plast) issue(x + S);
+      if (tid == 0 && !failed && x + S <= plast) issue(x + S);
       rowbase += plane_stride;
     };
 
@@ -536,6 +543,17 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
     seq = base + (uint32_t)(xe - xa) + 6;
     failed = __syncthreads_or(failed) != 0;
     if (failed) break;
+  }
+
+  if (failed && tid == 0) {
+    // let every copy this CTA issued land before its shared memory is released:
+    // the last S sequence numbers cover all slots; completed phases return at once
+    const uint32_t first = seq_issue > (uint32_t)S ? seq_issue - (uint32_t)S : 0u;
+    for (uint32_t sq = first; sq < seq_issue; ++sq) {
+      uint32_t spins = 0;
+      while (!mbar_try_wait(&bars[sq % S], (sq / S) & 1u) && ++spins <= WAIT_SPIN_LIMIT) {
+      }
+    }
   }
 
   if (BATCH && !PLAIN && cur_inst >= 0 && cur_red) flush(cur_err);

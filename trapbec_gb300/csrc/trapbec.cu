@@ -95,6 +95,8 @@ struct trapbec_ctx {
   bool plan_valid = false;
   int shape = 0;                       // tiled-kernel shape index
   int* d_err = nullptr;                // device error flag of the tiled kernel
+  uint32_t wait_limit = 1u << 24;      // bounded-wait limit of the tiled kernel
+  int inject_wait = 0;                 // test hook of the bounded waits
   int* h_err = nullptr;                // pinned copy
   int chunk_user = 0;                  // x-chunk requested by the caller (0 = automatic)
 };
@@ -233,6 +235,8 @@ int check_device_error(trapbec_ctx* c) {
 // Launch one stage.  kind: StageKind or 4 (diagnostics).  Returns status.
 template <typename T>
 int launch_stage(trapbec_ctx* c, int kind, StageArgs<T>& a, int* nblk_out) {
+  c->plan.spin_limit = c->wait_limit;
+  c->plan.inject_wait = c->inject_wait;
   if (use_tiled<T>(c)) {
     int rc = launch_tiled<T>(c->plan, kind, a, c->st, c->red_cap, nblk_out);
     if (rc) { set_error("tiled stage launch failed (" + std::to_string(rc) + ")"); return TRAPBEC_ERR_CUDA; }
@@ -287,7 +291,7 @@ template <typename T> int run_diag(trapbec_ctx* c) {
   c->launches++;
   CK(cudaMemcpyAsync(c->host_red, c->red_out, sizeof(double) * NRED, cudaMemcpyDeviceToHost, c->st));
   CK(cudaStreamSynchronize(c->st));
-  return TRAPBEC_OK;
+  return check_device_error(c);
 }
 
 template <typename T> double cell_volume(const trapbec_ctx* c) {
@@ -449,6 +453,11 @@ template <typename T> int do_imag_rk3(trapbec_ctx* c, int nsteps, double tol, in
   ImagCtrl& h = *c->host_ctrl;
   int done = h.step;
   c->cur = (start_cur + done) & 1;
+  if ((rc = check_device_error(c))) {   // a bounded wait gave up: the sums are not meaningful
+    *steps_done = done;
+    *rel_out = NAN;
+    return rc;
+  }
   if (h.nonfinite) {
     *steps_done = done;
     *rel_out = NAN;
@@ -1003,6 +1012,13 @@ template <typename T> int field_diag_impl(trapbec_ctx* c, void* out, int which) 
 }
 }  // namespace
 extern "C" {
+
+int trapbec_set_wait_limit(trapbec_ctx* c, uint32_t limit, int inject) {
+  if (!c) return TRAPBEC_ERR_ARG;
+  c->wait_limit = limit ? limit : (1u << 24);
+  c->inject_wait = inject ? 1 : 0;
+  return TRAPBEC_OK;
+}
 
 int trapbec_force_vortex(trapbec_ctx* c, double x0, double y0, double dir) {
   if (!c) return TRAPBEC_ERR_ARG;

@@ -104,6 +104,11 @@ class Solver:
         check(self.lib.trapbec_diag(self.ctx, C.byref(d)), "trapbec_diag")
         return d.as_dict()
 
+    def set_wait_limit(self, limit: int = 0, inject: bool = False) -> None:
+        """Bounded-wait limit of the tiled kernels (0 = default); inject = True
+        makes every wait run out (test hook of the timeout path)."""
+        check(self.lib.trapbec_set_wait_limit(self.ctx, int(limit), int(bool(inject))), "trapbec_set_wait_limit")
+
     def force_vortex(self, x0: float, y0: float, direction: int) -> None:
         """psi *= pade_density(r) e^{i dir theta} about (x0, y0) (force.f90:33-44)."""
         check(self.lib.trapbec_force_vortex(self.ctx, float(x0), float(y0), float(direction)),
