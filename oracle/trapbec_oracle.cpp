@@ -108,6 +108,7 @@ template <typename T> struct Oracle {
   T eps;        // epsilon(0.)
   std::vector<Rank<T>> ranks;
   double norm_target = -1.0;
+  bool norm_user = false;   // set by orc_set_norm_target; otherwise derived from each new state
   double e_prev = std::numeric_limits<double>::quiet_NaN();
   double intpsi2_old = 1.0;
 
@@ -515,7 +516,7 @@ template <typename T> struct Oracle {
   int imag_rk3(int nsteps, double tol, int* steps_done, double* rel_de) {
     const T cf = (T)0.5 * dt.re;
     trapbec_diag_out d;
-    if (norm_target <= 0) { diag(&d); norm_target = d.norm; }
+    if (!(norm_target > 0)) { diag(&d); norm_target = d.norm; }
     diag(&d);            // energy of the incoming state: the first test is after step 1
     e_prev = d.energy;
     int s = 0;
@@ -1044,7 +1045,9 @@ int orc_max_threads(void) {
 int orc_set_psi(void* h, const void* psi) {
   return dispatch((Handle*)h, [&](auto& o) {
     using T = std::remove_reference_t<decltype(o.t)>;
-    o.set_psi((const T*)psi); return 0; });
+    o.set_psi((const T*)psi);
+    if (!o.norm_user) o.norm_target = -1.0;   // the next relaxation keeps the new state's norm
+    return 0; });
 }
 int orc_get_psi(void* h, void* psi) {
   return dispatch((Handle*)h, [&](auto& o) {
@@ -1114,7 +1117,7 @@ int orc_step_imag_rk3(void* h, int nsteps, double tol, int* steps_done, double* 
   return dispatch((Handle*)h, [&](auto& o) { return o.imag_rk3(nsteps, tol, steps_done, rel); });
 }
 int orc_set_norm_target(void* h, double n0) {
-  return dispatch((Handle*)h, [&](auto& o) { o.norm_target = n0; return 0; });
+  return dispatch((Handle*)h, [&](auto& o) { o.norm_target = n0; o.norm_user = n0 > 0; return 0; });
 }
 int orc_set_omega(void* h, double om) {
   return dispatch((Handle*)h, [&](auto& o) { o.p.omega_z = om; return 0; });
@@ -1133,7 +1136,9 @@ double orc_psi_norm_ref(void* h) {
   return (double)((Oracle<float>*)hh->o)->psi_norm_ref();
 }
 int orc_init_state(void* h, const char* name, const trapbec_init_args* a) {
-  return dispatch((Handle*)h, [&](auto& o) { return o.init_state(name, a); });
+  return dispatch((Handle*)h, [&](auto& o) {
+    if (!o.norm_user) o.norm_target = -1.0;
+    return o.init_state(name, a); });
 }
 double orc_cell_uniform(uint64_t seed, uint64_t idx, uint64_t stream) {
   return cell_uniform(seed, idx, stream);

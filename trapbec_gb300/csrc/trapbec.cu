@@ -84,6 +84,7 @@ struct trapbec_ctx {
   double t = 0.0;
   double dt_re = 0, dt_im = 0, gamma = 0, omega = 0, vx = 0;
   double norm_target = -1.0;
+  bool norm_user = false;              // norm_target set by the caller (else derived per state)
   double intpsi2_old = 1.0;    // run.f90:23 ratio state
   bool ctrl_init = false;
   int kernel_kind = 0, tile_z = 0, tile_y = 0;
@@ -387,7 +388,7 @@ template <typename T> int do_imag_rk3(trapbec_ctx* c, int nsteps, double tol, in
   int rc = apply_pending_scale<T>(c);
   if (rc) return rc;
   double dV = cell_volume<T>(c);
-  if (c->norm_target <= 0) {
+  if (!(c->norm_target > 0.0)) {   // unset (or derived from a non-finite state)
     if ((rc = run_diag<T>(c))) return rc;
     c->norm_target = dV * c->host_red[0];
   }
@@ -863,6 +864,7 @@ int trapbec_set_psi(trapbec_ctx* c, const void* psi, int layout) {
     set_error("bad layout");
     return TRAPBEC_ERR_ARG;
   }
+  if (!c->norm_user) c->norm_target = -1.0;   // the next relaxation keeps this state's norm
   if (c->ctrl_init) {  // a new state cancels any pending renormalisation
     c->host_ctrl->scale = 1.0;
     c->host_ctrl->have_prev = 0;
@@ -912,6 +914,7 @@ int trapbec_init_state(trapbec_ctx* c, const char* name, const trapbec_init_args
   if (!c || !name) return TRAPBEC_ERR_ARG;
   int rc = DISPATCH(c, init_state_impl, c, name, args);
   if (rc) return rc;
+  if (!c->norm_user) c->norm_target = -1.0;   // the next relaxation keeps the new state's norm
   if (c->ctrl_init) {
     c->host_ctrl->scale = 1.0;
     c->host_ctrl->have_prev = 0;
@@ -1065,7 +1068,7 @@ int trapbec_set_scalar(trapbec_ctx* c, int which, double v) {
     case TRAPBEC_SCALAR_GAMMA: c->gamma = v; break;
     case TRAPBEC_SCALAR_T: c->t = v; break;
     case TRAPBEC_SCALAR_ADVECTIVE_VX: c->vx = v; c->p.advective_vx = v; break;
-    case TRAPBEC_SCALAR_NORM_TARGET: c->norm_target = v; break;
+    case TRAPBEC_SCALAR_NORM_TARGET: c->norm_target = v; c->norm_user = v > 0.0; break;
     default: set_error("unknown scalar"); return TRAPBEC_ERR_ARG;
   }
   return TRAPBEC_OK;
