@@ -216,8 +216,8 @@ typedef struct trapbec_diag_out {
 int trapbec_diag(trapbec_ctx* ctx, trapbec_diag_out* out);
 
 /* Bounded waits of the tiled stage kernels (no counterpart in the reference).
- * Every wait of a launch for its TMA data gives up after `limit` polls
- * (0 = the default, 2^24), records TRAPBEC_ERR_TIMEOUT, lets the copies in
+ * Every wait of a launch for its TMA data gives up after `limit`
+ * microseconds (0 = the default, 2 s), records TRAPBEC_ERR_TIMEOUT, lets the copies in
  * flight land and returns; the call then returns TRAPBEC_ERR_TIMEOUT and the
  * context stays usable (psi is not meaningful after it).  inject = 1 is a
  * test hook: every wait then waits for an mbarrier phase that nothing

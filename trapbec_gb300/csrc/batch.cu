@@ -278,7 +278,7 @@ template <typename T> int fill_desc(trapbec_batch* b, int i, int s) {
       ta.fix_y = 0;
       ta.fix_z = 0;
       ta.chunk = p.nx;
-      ta.spin_limit = WAIT_SPIN_LIMIT;
+      ta.wait_us = WAIT_US_DEFAULT;
       ta.inject_wait = 0;
       fill_coeffs<T>(ta);
     }

@@ -73,6 +73,21 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* b, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// Wait for the phase of `parity` to complete; false if `limit_us` microseconds pass first.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* b, uint32_t parity, uint32_t limit_us) {
+  if (mbar_try_wait(b, parity)) return true;
+  const uint64_t t0 = global_ns();
+  const uint64_t lim = (uint64_t)limit_us * 1000u;
+  while (!mbar_try_wait(b, parity)) {
+    if (global_ns() - t0 > lim) return false;
+  }
+  return true;
+}
 __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* tm, int c0, int c1, int c2, uint64_t* bar) {
   asm volatile(
       "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
@@ -83,7 +98,7 @@ __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.
 
 // Error codes written to TiledArgs::err.
 enum TiledErr : int { TERR_NONE = 0, TERR_WAIT_TIMEOUT = 1, TERR_TOO_MANY_SEGMENTS = 2 };
-constexpr uint32_t WAIT_SPIN_LIMIT = 1u << 24;  // try_wait calls (each may suspend) before giving up
+constexpr uint32_t WAIT_US_DEFAULT = 2000000;  // a wait for TMA data gives up after 2 s
 
 template <typename T> struct TiledArgs {
   StageArgs<T> s;
@@ -93,7 +108,7 @@ template <typename T> struct TiledArgs {
   int bcz;                 // boundary type along z (periodic if zper)
   int fix_y, fix_z;        // ghost fix-up needed on y / z boundary tiles
   int chunk;               // x-chunk length of the work order
-  uint32_t spin_limit;     // try_wait calls before a wait gives up (WAIT_SPIN_LIMIT by default)
+  uint32_t wait_us;        // microseconds before a wait gives up (WAIT_US_DEFAULT by default)
   int inject_wait;         // test hook: every wait waits for a phase that never completes
   // Packed coefficients, formed on the host so the kernel can take them from
   // the parameter (constant) bank instead of holding them in registers:
@@ -224,14 +239,72 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
     __syncthreads();
   };
 
+  // Batched launches: each CTA takes a contiguous range of (tile, x) units.
+  // Single grids: work items (x-chunk, z-tile, y-tile) dealt round-robin, so
+  // neighbouring CTAs stream y-neighbour tiles in lockstep and the halo rows
+  // they share are still in L2 when the second one asks for them.
   const long long total = BATCH ? ba.ustart[ba.nact] : ta0.units;
-  const long long G0 = (long long)blockIdx.x * total / gridDim.x;
-  const long long G1 = (long long)(blockIdx.x + 1) * total / gridDim.x;
+  const long long G0 = BATCH ? (long long)blockIdx.x * total / gridDim.x : (long long)blockIdx.x;
+  const long long G1 = BATCH ? (long long)(blockIdx.x + 1) * total / gridDim.x : 0;
+  const int nx0 = ta0.s.nx;
+  const int L0 = ta0.chunk;
+  const long long nitems = BATCH ? 0 : (long long)((nx0 + L0 - 1) / L0) * ta0.ntz * ta0.nty;
   uint32_t seq = 0;       // load sequence number of the first plane of a segment
   uint32_t seq_issue = 0; // next sequence number to issue (thread 0)
   bool failed = false;
 
-  for (long long g0 = G0; g0 < G1;) {
+  // Single grids: thread 0 issues planes in the global order of this CTA's
+  // items, one for every slot freed, across item boundaries, so an item's
+  // first planes are in flight while the previous item finishes.
+  struct Geo { int y0, c0, cw, xa, xb, plast; };
+  auto geo_of = [&](long long item) -> Geo {
+    Geo g;
+    const int ty = (int)(item % ta0.nty);
+    const long long r = item / ta0.nty;
+    const int tz = (int)(r % ta0.ntz);
+    const int xc = (int)(r / ta0.ntz);
+    g.y0 = ty * TY;
+    g.c0 = (int)(sizeof(T) == 4 ? (tz * TZ - HZ) : 2 * (tz * TZ - HZ));
+    g.cw = (int)(sizeof(T) == 4 ? tz * TZ : 2 * tz * TZ);
+    g.xa = xc * L0;
+    g.xb = min(nx0, g.xa + L0);
+    g.plast = g.xa + 7 * ((g.xb - g.xa + 6) / 7) + 2;
+    return g;
+  };
+  auto plane_src0 = [&](int p) -> int {
+    if (p >= 0 && p < nx0) return p;
+    if (ta0.s.bc == TRAPBEC_BC_ZERO) return p;
+    return map_ghost(p, nx0, ta0.s.bc);
+  };
+  long long iss_item = G0;
+  Geo iss_geo{};
+  int iss_p = 0;
+  auto issue_next = [&]() {   // thread 0, single grids
+    if (iss_item >= nitems) return;
+    const uint32_t sq = seq_issue++;
+    const int sl = sq % S;
+    const int p = iss_p;
+    const bool with_w = READS_W && p >= iss_geo.xa && p < iss_geo.xb;
+    V* dst = ring + (size_t)sl * G::SLOT_STRIDE_ELEMS;
+    fence_proxy_async();
+    mbar_expect_tx(&bars[sl], G::SLOT_BYTES + (with_w ? G::W_BYTES : 0));
+    tma_load_3d(dst, &tm0, iss_geo.c0, iss_geo.y0 - 3, plane_src0(p), &bars[sl]);
+    if (with_w) tma_load_3d(dst + G::W_OFF_ELEMS, &tmw0, iss_geo.cw, iss_geo.y0, p, &bars[sl]);
+    if (++iss_p > iss_geo.plast) {
+      iss_item += gridDim.x;
+      if (iss_item < nitems) {
+        iss_geo = geo_of(iss_item);
+        iss_p = iss_geo.xa - 3;
+      }
+    }
+  };
+  if (!BATCH && tid == 0 && iss_item < nitems) {
+    iss_geo = geo_of(iss_item);
+    iss_p = iss_geo.xa - 3;
+    for (int k = 0; k < S; ++k) issue_next();
+  }
+
+  for (long long g0 = G0; BATCH ? (g0 < G1) : (g0 < nitems);) {
     // ---- which grid this segment belongs to -------------------------------
     const TiledArgs<T>* tap = &ta0;
     const CUtensorMap* tmp = &tm0;
@@ -279,17 +352,27 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
     // Work units are ordered (z-tile, x-chunk, y-tile, x); with the default
     // chunk = nx this is tile-major order and each CTA streams a contiguous
     // x-range of one or two tiles.
-    const long long per_tz = (long long)ta.nty * nx;
-    const int tzi = (int)(u0 / per_tz);
-    const long long rr0 = u0 - (long long)tzi * per_tz;
-    const int xc = (int)(rr0 / ((long long)ta.nty * L));
-    const long long rr1 = rr0 - (long long)xc * ta.nty * L;
-    const int Lc = min(L, nx - xc * L);
-    const int tyi = (int)(rr1 / Lc);
-    const int xa = xc * L + (int)(rr1 - (long long)tyi * Lc);
-    int xb = xc * L + Lc;
-    if (g0 + (xb - xa) > uend) xb = xa + (int)(uend - g0);
-    g0 += xb - xa;
+    int tzi, tyi, xa, xb;
+    if (BATCH) {
+      const long long per_tz = (long long)ta.nty * nx;
+      tzi = (int)(u0 / per_tz);
+      const long long rr0 = u0 - (long long)tzi * per_tz;
+      const int xc = (int)(rr0 / ((long long)ta.nty * L));
+      const long long rr1 = rr0 - (long long)xc * ta.nty * L;
+      const int Lc = min(L, nx - xc * L);
+      tyi = (int)(rr1 / Lc);
+      xa = xc * L + (int)(rr1 - (long long)tyi * Lc);
+      xb = xc * L + Lc;
+      if (g0 + (xb - xa) > uend) xb = xa + (int)(uend - g0);
+      g0 += xb - xa;
+    } else {
+      tyi = (int)(g0 % ta.nty);
+      const long long r = g0 / ta.nty;
+      tzi = (int)(r % ta.ntz);
+      xa = (int)(r / ta.ntz) * L;
+      xb = min(nx, xa + L);
+      g0 += gridDim.x;
+    }
     if (skip) continue;   // converged grid in a batch: nothing to do, nothing loaded
 
     const int z0 = tzi * TZ;
@@ -332,7 +415,7 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
       tma_load_3d(dst, tmp, c0, y0 - 3, plane_src(p), &bars[sl]);
       if (with_w) tma_load_3d(dst + G::W_OFF_ELEMS, tmwp, cw, y0, p, &bars[sl]);
     };
-    if (tid == 0) {
+    if (BATCH && tid == 0) {
       seq_issue = base;
       for (int p = xa - 3; p <= plast && p < xa - 3 + S; ++p) issue(p);
     }
@@ -340,13 +423,9 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
     auto wait_plane = [&](uint32_t sq) {
       const int sl = ta.inject_wait ? S : (int)(sq % S);
       const uint32_t par = ta.inject_wait ? 0u : (sq / S) & 1u;
-      uint32_t spins = 0;
-      while (!mbar_try_wait(&bars[sl], par)) {
-        if (++spins > ta.spin_limit) {
-          failed = true;
-          atomicExch(ta.err, (int)TERR_WAIT_TIMEOUT);
-          break;
-        }
+      if (!mbar_wait_bounded(&bars[sl], par, ta.wait_us)) {
+        failed = true;
+        atomicExch(ta.err, (int)TERR_WAIT_TIMEOUT);
       }
     };
 
@@ -398,11 +477,15 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
     __syncthreads();
     // a slot is refilled only after its previous copy was waited for: once a
     // wait of the issuing thread gave up, nothing more is issued
-    if (tid == 0 && !failed) {
-      for (int j = 0; j < 3; ++j) {
-        const int p = xa - 3 + j + S;
-        if (p > plast) break;
-        issue(p);
+    if (tid == 0 && !failed) {   // the slots of planes xa-3 .. xa-1 are free
+      if (BATCH) {
+        for (int j = 0; j < 3; ++j) {
+          const int p = xa - 3 + j + S;
+          if (p > plast) break;
+          issue(p);
+        }
+      } else {
+        issue_next(); issue_next(); issue_next();
       }
     }
 
@@ -527,7 +610,13 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
         }
       }
       __syncthreads();
-      if (tid == 0 && !failed && x + S <= plast) issue(x + S);
+      if (tid == 0 && !failed) {   // the slot of plane x is free
+        if (BATCH) {
+          if (x + S <= plast) issue(x + S);
+        } else {
+          issue_next();
+        }
+      }
       rowbase += plane_stride;
     };
 
@@ -541,6 +630,9 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
       body(std::integral_constant<int, 6>{}, x + 6);
     }
     seq = base + (uint32_t)(xe - xa) + 6;
+    if (!BATCH && tid == 0 && !failed) {   // slots of planes xe .. xe+2 are free
+      issue_next(); issue_next(); issue_next();
+    }
     failed = __syncthreads_or(failed) != 0;
     if (failed) break;
   }
@@ -549,11 +641,7 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
     // let every copy this CTA issued land before its shared memory is released:
     // the last S sequence numbers cover all slots; completed phases return at once
     const uint32_t first = seq_issue > (uint32_t)S ? seq_issue - (uint32_t)S : 0u;
-    for (uint32_t sq = first; sq < seq_issue; ++sq) {
-      uint32_t spins = 0;
-      while (!mbar_try_wait(&bars[sq % S], (sq / S) & 1u) && ++spins <= WAIT_SPIN_LIMIT) {
-      }
-    }
+    for (uint32_t sq = first; sq < seq_issue; ++sq) (void)mbar_wait_bounded(&bars[sq % S], (sq / S) & 1u, WAIT_US_DEFAULT);
   }
 
   if (BATCH && !PLAIN && cur_inst >= 0 && cur_red) flush(cur_err);

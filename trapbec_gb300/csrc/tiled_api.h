@@ -22,7 +22,7 @@ struct TiledPlan {
   CUtensorMap tm[2];
   CUtensorMap tmw;       // w (read by stages 2 and 3)
   int* err = nullptr;    // device error flag (owned by the context)
-  uint32_t spin_limit = 1u << 24;   // try_wait calls before a wait gives up
+  uint32_t wait_us = 2000000;   // microseconds before a wait gives up
   int inject_wait = 0;   // test hook: waits aim at a phase that never completes
 };
 

@@ -121,7 +121,7 @@ int launch_shape(const TiledPlan& plan, int kind, const StageArgs<T>& a, cudaStr
   ta.fix_y = plan.fix_y;
   ta.fix_z = plan.fix_z;
   ta.chunk = plan.chunk;
-  ta.spin_limit = plan.spin_limit;
+  ta.wait_us = plan.wait_us;
   ta.inject_wait = plan.inject_wait;
   fill_coeffs<T>(ta);
   const CUtensorMap* tm = nullptr;

@@ -96,7 +96,7 @@ struct trapbec_ctx {
   bool plan_valid = false;
   int shape = 0;                       // tiled-kernel shape index
   int* d_err = nullptr;                // device error flag of the tiled kernel
-  uint32_t wait_limit = 1u << 24;      // bounded-wait limit of the tiled kernel
+  uint32_t wait_us = 2000000;          // bounded-wait limit of the tiled kernel (microseconds)
   int inject_wait = 0;                 // test hook of the bounded waits
   int* h_err = nullptr;                // pinned copy
   int chunk_user = 0;                  // x-chunk requested by the caller (0 = automatic)
@@ -208,9 +208,24 @@ template <typename T> StageArgs<T> base_args(trapbec_ctx* c, double t) {
 }
 
 // Default x-chunk of the work order (the autotuner may pick another).
+// Single-grid launches deal (x-chunk, tile) items round-robin to the
+// persistent CTAs; the chunk length L balances them: the busiest CTA takes
+// ceil(items / grid) items of L planes plus about 3 planes of per-item
+// overhead (the x halo comes from L2, the pipeline runs across items).
 int auto_chunk(const trapbec_ctx* c) {
   if (c->chunk_user > 0) return std::min(c->chunk_user, c->p.nx);
-  return c->p.nx;   // tile-major: measured fastest at 512^3; the autotuner tries shorter chunks
+  if (!c->plan_valid || c->plan.grid <= 0) return c->p.nx;
+  const long long tiles = (long long)c->plan.ntz * c->plan.nty;
+  const int nx = c->p.nx;
+  int best = nx;
+  double best_cost = 1e300;
+  for (int L = 7; L <= nx; ++L) {
+    const long long items = tiles * ((nx + L - 1) / L);
+    const long long per = (items + c->plan.grid - 1) / c->plan.grid;
+    const double cost = (double)per * (L + 3);
+    if (cost < best_cost - 1e-9) { best_cost = cost; best = L; }
+  }
+  return best;
 }
 
 template <typename T> bool use_tiled(trapbec_ctx* c) {
@@ -236,7 +251,7 @@ int check_device_error(trapbec_ctx* c) {
 // Launch one stage.  kind: StageKind or 4 (diagnostics).  Returns status.
 template <typename T>
 int launch_stage(trapbec_ctx* c, int kind, StageArgs<T>& a, int* nblk_out) {
-  c->plan.spin_limit = c->wait_limit;
+  c->plan.wait_us = c->wait_us;
   c->plan.inject_wait = c->inject_wait;
   if (use_tiled<T>(c)) {
     int rc = launch_tiled<T>(c->plan, kind, a, c->st, c->red_cap, nblk_out);
@@ -1018,7 +1033,7 @@ extern "C" {
 
 int trapbec_set_wait_limit(trapbec_ctx* c, uint32_t limit, int inject) {
   if (!c) return TRAPBEC_ERR_ARG;
-  c->wait_limit = limit ? limit : (1u << 24);
+  c->wait_us = limit ? limit : 2000000u;
   c->inject_wait = inject ? 1 : 0;
   return TRAPBEC_OK;
 }

@@ -105,7 +105,7 @@ class Solver:
         return d.as_dict()
 
     def set_wait_limit(self, limit: int = 0, inject: bool = False) -> None:
-        """Bounded-wait limit of the tiled kernels (0 = default); inject = True
+        """Bounded-wait limit of the tiled kernels in microseconds (0 = default, 2 s); inject = True
         makes every wait run out (test hook of the timeout path)."""
         check(self.lib.trapbec_set_wait_limit(self.ctx, int(limit), int(bool(inject))), "trapbec_set_wait_limit")
 
