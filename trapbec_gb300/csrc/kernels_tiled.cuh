@@ -110,6 +110,7 @@ template <typename T> struct TiledArgs {
   int chunk;               // x-chunk length of the work order
   uint32_t wait_us;        // microseconds before a wait gives up (WAIT_US_DEFAULT by default)
   int inject_wait;         // test hook: every wait waits for a phase that never completes
+  int rr;                  // single grids: 1 = round-robin (x-chunk, tile) items, 0 = contiguous unit ranges
   // Packed coefficients, formed on the host so the kernel can take them from
   // the parameter (constant) bank instead of holding them in registers:
   // 0-2: (2,-27,270)/(180 hx^2), 3-5: y, 6-8: z, 9: -490*sum(1/(180 h^2)),
@@ -243,12 +244,13 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
   // Single grids: work items (x-chunk, z-tile, y-tile) dealt round-robin, so
   // neighbouring CTAs stream y-neighbour tiles in lockstep and the halo rows
   // they share are still in L2 when the second one asks for them.
+  const bool contig = BATCH || !ta0.rr;
   const long long total = BATCH ? ba.ustart[ba.nact] : ta0.units;
-  const long long G0 = BATCH ? (long long)blockIdx.x * total / gridDim.x : (long long)blockIdx.x;
-  const long long G1 = BATCH ? (long long)(blockIdx.x + 1) * total / gridDim.x : 0;
+  const long long G0 = contig ? (long long)blockIdx.x * total / gridDim.x : (long long)blockIdx.x;
+  const long long G1 = contig ? (long long)(blockIdx.x + 1) * total / gridDim.x : 0;
   const int nx0 = ta0.s.nx;
   const int L0 = ta0.chunk;
-  const long long nitems = BATCH ? 0 : (long long)((nx0 + L0 - 1) / L0) * ta0.ntz * ta0.nty;
+  const long long nitems = contig ? 0 : (long long)((nx0 + L0 - 1) / L0) * ta0.ntz * ta0.nty;
   uint32_t seq = 0;       // load sequence number of the first plane of a segment
   uint32_t seq_issue = 0; // next sequence number to issue (thread 0)
   bool failed = false;
@@ -298,13 +300,13 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
       }
     }
   };
-  if (!BATCH && tid == 0 && iss_item < nitems) {
+  if (!contig && tid == 0 && iss_item < nitems) {
     iss_geo = geo_of(iss_item);
     iss_p = iss_geo.xa - 3;
     for (int k = 0; k < S; ++k) issue_next();
   }
 
-  for (long long g0 = G0; BATCH ? (g0 < G1) : (g0 < nitems);) {
+  for (long long g0 = G0; contig ? (g0 < G1) : (g0 < nitems);) {
     // ---- which grid this segment belongs to -------------------------------
     const TiledArgs<T>* tap = &ta0;
     const CUtensorMap* tmp = &tm0;
@@ -353,7 +355,7 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
     // chunk = nx this is tile-major order and each CTA streams a contiguous
     // x-range of one or two tiles.
     int tzi, tyi, xa, xb;
-    if (BATCH) {
+    if (contig) {
       const long long per_tz = (long long)ta.nty * nx;
       tzi = (int)(u0 / per_tz);
       const long long rr0 = u0 - (long long)tzi * per_tz;
@@ -415,7 +417,7 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
       tma_load_3d(dst, tmp, c0, y0 - 3, plane_src(p), &bars[sl]);
       if (with_w) tma_load_3d(dst + G::W_OFF_ELEMS, tmwp, cw, y0, p, &bars[sl]);
     };
-    if (BATCH && tid == 0) {
+    if (contig && tid == 0) {
       seq_issue = base;
       for (int p = xa - 3; p <= plast && p < xa - 3 + S; ++p) issue(p);
     }
@@ -478,7 +480,7 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
     // a slot is refilled only after its previous copy was waited for: once a
     // wait of the issuing thread gave up, nothing more is issued
     if (tid == 0 && !failed) {   // the slots of planes xa-3 .. xa-1 are free
-      if (BATCH) {
+      if (contig) {
         for (int j = 0; j < 3; ++j) {
           const int p = xa - 3 + j + S;
           if (p > plast) break;
@@ -611,7 +613,7 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
       }
       __syncthreads();
       if (tid == 0 && !failed) {   // the slot of plane x is free
-        if (BATCH) {
+        if (contig) {
           if (x + S <= plast) issue(x + S);
         } else {
           issue_next();
@@ -630,7 +632,7 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
       body(std::integral_constant<int, 6>{}, x + 6);
     }
     seq = base + (uint32_t)(xe - xa) + 6;
-    if (!BATCH && tid == 0 && !failed) {   // slots of planes xe .. xe+2 are free
+    if (!contig && tid == 0 && !failed) {   // slots of planes xe .. xe+2 are free
       issue_next(); issue_next(); issue_next();
     }
     failed = __syncthreads_or(failed) != 0;

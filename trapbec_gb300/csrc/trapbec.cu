@@ -208,24 +208,35 @@ template <typename T> StageArgs<T> base_args(trapbec_ctx* c, double t) {
 }
 
 // Default x-chunk of the work order (the autotuner may pick another).
-// Single-grid launches deal (x-chunk, tile) items round-robin to the
-// persistent CTAs; the chunk length L balances them: the busiest CTA takes
-// ceil(items / grid) items of L planes plus about 3 planes of per-item
-// overhead (the x halo comes from L2, the pipeline runs across items).
-int auto_chunk(const trapbec_ctx* c) {
-  if (c->chunk_user > 0) return std::min(c->chunk_user, c->p.nx);
-  if (!c->plan_valid || c->plan.grid <= 0) return c->p.nx;
-  const long long tiles = (long long)c->plan.ntz * c->plan.nty;
-  const int nx = c->p.nx;
-  int best = nx;
+// Round-robin items of L planes: the busiest CTA takes ceil(items / grid)
+// items of L planes plus about 3 planes of per-item overhead; L is a multiple
+// of 7 (the kernel's x unroll) so no plane is computed without being stored.
+int rr_auto_chunk(const trapbec_params& p, const TiledPlan& plan) {
+  const long long tiles = (long long)plan.ntz * plan.nty;
+  int best = p.nx;
   double best_cost = 1e300;
-  for (int L = 7; L <= nx; ++L) {
-    const long long items = tiles * ((nx + L - 1) / L);
-    const long long per = (items + c->plan.grid - 1) / c->plan.grid;
+  for (int L = 7; L <= p.nx; L += 7) {
+    const long long items = tiles * ((p.nx + L - 1) / L);
+    const long long per = (items + plan.grid - 1) / plan.grid;
     const double cost = (double)per * (L + 3);
     if (cost < best_cost - 1e-9) { best_cost = cost; best = L; }
   }
   return best;
+}
+
+// Work order from the chunk code (trapbec_set_chunk): > 0 round-robin items,
+// < 0 contiguous ranges in x-chunks, 0 automatic.
+void apply_order(const trapbec_params& p, TiledPlan* plan, int code) {
+  if (code > 0) {
+    plan->rr = 1;
+    plan->chunk = std::min(code, p.nx);
+  } else if (code < 0) {
+    plan->rr = 0;
+    plan->chunk = std::min(-code, p.nx);
+  } else {
+    plan->rr = 0;
+    plan->chunk = p.nx;
+  }
 }
 
 template <typename T> bool use_tiled(trapbec_ctx* c) {
@@ -697,7 +708,7 @@ template <typename T> int create_impl(trapbec_ctx* c) {
   int rc = setup_tables<T>(c);
   if (rc) return rc;
   c->plan_valid = (plan_tiled<T>(c->p, c->psi, c->w, c->nsm, 0, c->d_err, &c->plan) == 0);
-  if (c->plan_valid) c->plan.chunk = auto_chunk(c);
+  if (c->plan_valid) apply_order(c->p, &c->plan, c->chunk_user);
   return TRAPBEC_OK;
 }
 
@@ -1131,7 +1142,7 @@ int trapbec_set_kernel(trapbec_ctx* c, int kind, int tile_z, int tile_y) {
     int rc = c->prec == TRAPBEC_FP64 ? plan_tiled<double>(c->p, c->psi, c->w, c->nsm, shape, c->d_err, &c->plan)
                                      : plan_tiled<float>(c->p, c->psi, c->w, c->nsm, shape, c->d_err, &c->plan);
     c->plan_valid = (rc == 0);
-    if (c->plan_valid) c->plan.chunk = auto_chunk(c);
+    if (c->plan_valid) apply_order(c->p, &c->plan, c->chunk_user);
   }
   if (kind == 2 && !c->plan_valid) {
     set_error("tiled kernel not available for this grid / tile shape");
@@ -1141,9 +1152,9 @@ int trapbec_set_kernel(trapbec_ctx* c, int kind, int tile_z, int tile_y) {
 }
 
 int trapbec_set_chunk(trapbec_ctx* c, int chunk) {
-  if (!c || chunk < 0) return TRAPBEC_ERR_ARG;
+  if (!c) return TRAPBEC_ERR_ARG;
   c->chunk_user = chunk;
-  if (c->plan_valid) c->plan.chunk = auto_chunk(c);
+  if (c->plan_valid) apply_order(c->p, &c->plan, c->chunk_user);
   return TRAPBEC_OK;
 }
 
@@ -1180,10 +1191,9 @@ template <typename T> int autotune_impl(trapbec_ctx* c, int steps, TuneVal* best
   for (int sh = 0; sh < ns && rc == TRAPBEC_OK; ++sh) {
     TiledPlan plan;
     if (plan_tiled<T>(c->p, c->psi, c->w, c->nsm, sh, c->d_err, &plan) != 0) continue;
-    std::vector<int> chunks = {16, 32, 64, c->p.nx};
+    std::vector<int> chunks = {-c->p.nx, -64, rr_auto_chunk(c->p, plan)};
     for (int L : chunks) {
-      if (L > c->p.nx) continue;
-      plan.chunk = L;
+      apply_order(c->p, &plan, L);
       c->plan = plan;
       c->plan_valid = true;
       c->kernel_kind = 2;
@@ -1205,7 +1215,7 @@ template <typename T> int autotune_impl(trapbec_ctx* c, int steps, TuneVal* best
   if (rc) return rc;
   if (bv.shape < 0) { set_error("no tiled kernel shape fits this grid"); return TRAPBEC_ERR_UNSUPPORTED; }
   if (plan_tiled<T>(c->p, c->psi, c->w, c->nsm, bv.shape, c->d_err, &c->plan) != 0) return TRAPBEC_ERR_CUDA;
-  c->plan.chunk = bv.chunk;
+  apply_order(c->p, &c->plan, bv.chunk);
   c->plan_valid = true;
   c->shape = bv.shape;
   c->chunk_user = bv.chunk;
@@ -1232,7 +1242,7 @@ int trapbec_autotune(trapbec_ctx* c, int steps, int* tile_z, int* tile_y, int* c
     c->shape = bv.shape;
   }
   c->chunk_user = bv.chunk;
-  c->plan.chunk = bv.chunk;
+  apply_order(c->p, &c->plan, bv.chunk);
   Shape sh = c->prec == TRAPBEC_FP64 ? tiled_shape<double>(bv.shape) : tiled_shape<float>(bv.shape);
   if (tile_z) *tile_z = sh.tz;
   if (tile_y) *tile_y = sh.ty;
