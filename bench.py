@@ -250,8 +250,6 @@ def run_gpu_arm(args):
     s = Solver(p)
     if args.kernel:
         s.set_kernel(*args.kernel)
-    if args.order is not None:
-        s.set_chunk(args.order)
     s.init_state(init["name"], seed=init["seed"] + rank, amp=init["amp"], r_tf2=init["r_tf2"],
                  noise_amp=init["noise_amp"])
     ramp_steps = 5000
@@ -393,8 +391,6 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--kernel", type=int, nargs=3, default=None, metavar=("KIND", "TZ", "TY"))
-    ap.add_argument("--order", type=int, default=None,
-                    help="work order of the stage kernel (trapbec_set_chunk: >0 round-robin chunk, <0 contiguous)")
     ap.add_argument("--imag", action="store_true", help="add the batched imaginary-time leg")
     ap.add_argument("--imag-count", type=int, default=16)
     ap.add_argument("--imag-seed", type=int, default=3)

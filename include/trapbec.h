@@ -257,12 +257,9 @@ int trapbec_get_scalar(trapbec_ctx* ctx, int which, double* value);
  * the default shape; tile_z = -(i+1): built shape number i).              */
 int trapbec_set_kernel(trapbec_ctx* ctx, int kind, int tile_z, int tile_y);
 
-/* Work order of the tiled kernel's persistent CTAs.
- *  chunk > 0: (x-chunk of `chunk` planes, tile) items dealt round-robin, so
- *             neighbouring CTAs stream y-adjacent tiles in lockstep;
- *  chunk < 0: each CTA takes a contiguous range of (tile, x) units, ordered
- *             in x-chunks of -chunk planes (-nx: tile by tile);
- *  chunk = 0: automatic (contiguous, tile by tile).                         */
+/* Work order of the tiled kernel: x-planes per chunk (0 = automatic).  Tiles
+ * adjacent in y are processed chunk by chunk so their shared ghost rows are
+ * served from L2.                                                          */
 int trapbec_set_chunk(trapbec_ctx* ctx, int chunk);
 
 /* Autotune the tiled kernel for this grid: time every built tile shape and a

@@ -280,7 +280,6 @@ template <typename T> int fill_desc(trapbec_batch* b, int i, int s) {
       ta.chunk = p.nx;
       ta.wait_us = WAIT_US_DEFAULT;
       ta.inject_wait = 0;
-      ta.rr = 0;
       fill_coeffs<T>(ta);
     }
   }

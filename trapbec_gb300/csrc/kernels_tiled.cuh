@@ -79,14 +79,16 @@ __device__ __forceinline__ uint64_t global_ns() {
   return t;
 }
 // Wait for the phase of `parity` to complete; false if `limit_us` microseconds pass first.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* b, uint32_t parity, uint32_t limit_us) {
-  if (mbar_try_wait(b, parity)) return true;
+__device__ __forceinline__ bool mbar_wait_slow(uint64_t* b, uint32_t parity, uint32_t limit_us) {
   const uint64_t t0 = global_ns();
   const uint64_t lim = (uint64_t)limit_us * 1000u;
   while (!mbar_try_wait(b, parity)) {
     if (global_ns() - t0 > lim) return false;
   }
   return true;
+}
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* b, uint32_t parity, uint32_t limit_us) {
+  return mbar_try_wait(b, parity) || mbar_wait_slow(b, parity, limit_us);
 }
 __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* tm, int c0, int c1, int c2, uint64_t* bar) {
   asm volatile(
@@ -110,7 +112,6 @@ template <typename T> struct TiledArgs {
   int chunk;               // x-chunk length of the work order
   uint32_t wait_us;        // microseconds before a wait gives up (WAIT_US_DEFAULT by default)
   int inject_wait;         // test hook: every wait waits for a phase that never completes
-  int rr;                  // single grids: 1 = round-robin (x-chunk, tile) items, 0 = contiguous unit ranges
   // Packed coefficients, formed on the host so the kernel can take them from
   // the parameter (constant) bank instead of holding them in registers:
   // 0-2: (2,-27,270)/(180 hx^2), 3-5: y, 6-8: z, 9: -490*sum(1/(180 h^2)),
@@ -240,73 +241,14 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
     __syncthreads();
   };
 
-  // Batched launches: each CTA takes a contiguous range of (tile, x) units.
-  // Single grids: work items (x-chunk, z-tile, y-tile) dealt round-robin, so
-  // neighbouring CTAs stream y-neighbour tiles in lockstep and the halo rows
-  // they share are still in L2 when the second one asks for them.
-  const bool contig = BATCH || !ta0.rr;
   const long long total = BATCH ? ba.ustart[ba.nact] : ta0.units;
-  const long long G0 = contig ? (long long)blockIdx.x * total / gridDim.x : (long long)blockIdx.x;
-  const long long G1 = contig ? (long long)(blockIdx.x + 1) * total / gridDim.x : 0;
-  const int nx0 = ta0.s.nx;
-  const int L0 = ta0.chunk;
-  const long long nitems = contig ? 0 : (long long)((nx0 + L0 - 1) / L0) * ta0.ntz * ta0.nty;
+  const long long G0 = (long long)blockIdx.x * total / gridDim.x;
+  const long long G1 = (long long)(blockIdx.x + 1) * total / gridDim.x;
   uint32_t seq = 0;       // load sequence number of the first plane of a segment
   uint32_t seq_issue = 0; // next sequence number to issue (thread 0)
   bool failed = false;
 
-  // Single grids: thread 0 issues planes in the global order of this CTA's
-  // items, one for every slot freed, across item boundaries, so an item's
-  // first planes are in flight while the previous item finishes.
-  struct Geo { int y0, c0, cw, xa, xb, plast; };
-  auto geo_of = [&](long long item) -> Geo {
-    Geo g;
-    const int ty = (int)(item % ta0.nty);
-    const long long r = item / ta0.nty;
-    const int tz = (int)(r % ta0.ntz);
-    const int xc = (int)(r / ta0.ntz);
-    g.y0 = ty * TY;
-    g.c0 = (int)(sizeof(T) == 4 ? (tz * TZ - HZ) : 2 * (tz * TZ - HZ));
-    g.cw = (int)(sizeof(T) == 4 ? tz * TZ : 2 * tz * TZ);
-    g.xa = xc * L0;
-    g.xb = min(nx0, g.xa + L0);
-    g.plast = g.xa + 7 * ((g.xb - g.xa + 6) / 7) + 2;
-    return g;
-  };
-  auto plane_src0 = [&](int p) -> int {
-    if (p >= 0 && p < nx0) return p;
-    if (ta0.s.bc == TRAPBEC_BC_ZERO) return p;
-    return map_ghost(p, nx0, ta0.s.bc);
-  };
-  long long iss_item = G0;
-  Geo iss_geo{};
-  int iss_p = 0;
-  auto issue_next = [&]() {   // thread 0, single grids
-    if (iss_item >= nitems) return;
-    const uint32_t sq = seq_issue++;
-    const int sl = sq % S;
-    const int p = iss_p;
-    const bool with_w = READS_W && p >= iss_geo.xa && p < iss_geo.xb;
-    V* dst = ring + (size_t)sl * G::SLOT_STRIDE_ELEMS;
-    fence_proxy_async();
-    mbar_expect_tx(&bars[sl], G::SLOT_BYTES + (with_w ? G::W_BYTES : 0));
-    tma_load_3d(dst, &tm0, iss_geo.c0, iss_geo.y0 - 3, plane_src0(p), &bars[sl]);
-    if (with_w) tma_load_3d(dst + G::W_OFF_ELEMS, &tmw0, iss_geo.cw, iss_geo.y0, p, &bars[sl]);
-    if (++iss_p > iss_geo.plast) {
-      iss_item += gridDim.x;
-      if (iss_item < nitems) {
-        iss_geo = geo_of(iss_item);
-        iss_p = iss_geo.xa - 3;
-      }
-    }
-  };
-  if (!contig && tid == 0 && iss_item < nitems) {
-    iss_geo = geo_of(iss_item);
-    iss_p = iss_geo.xa - 3;
-    for (int k = 0; k < S; ++k) issue_next();
-  }
-
-  for (long long g0 = G0; contig ? (g0 < G1) : (g0 < nitems);) {
+  for (long long g0 = G0; g0 < G1;) {
     // ---- which grid this segment belongs to -------------------------------
     const TiledArgs<T>* tap = &ta0;
     const CUtensorMap* tmp = &tm0;
@@ -354,27 +296,17 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
     // Work units are ordered (z-tile, x-chunk, y-tile, x); with the default
     // chunk = nx this is tile-major order and each CTA streams a contiguous
     // x-range of one or two tiles.
-    int tzi, tyi, xa, xb;
-    if (contig) {
-      const long long per_tz = (long long)ta.nty * nx;
-      tzi = (int)(u0 / per_tz);
-      const long long rr0 = u0 - (long long)tzi * per_tz;
-      const int xc = (int)(rr0 / ((long long)ta.nty * L));
-      const long long rr1 = rr0 - (long long)xc * ta.nty * L;
-      const int Lc = min(L, nx - xc * L);
-      tyi = (int)(rr1 / Lc);
-      xa = xc * L + (int)(rr1 - (long long)tyi * Lc);
-      xb = xc * L + Lc;
-      if (g0 + (xb - xa) > uend) xb = xa + (int)(uend - g0);
-      g0 += xb - xa;
-    } else {
-      tyi = (int)(g0 % ta.nty);
-      const long long r = g0 / ta.nty;
-      tzi = (int)(r % ta.ntz);
-      xa = (int)(r / ta.ntz) * L;
-      xb = min(nx, xa + L);
-      g0 += gridDim.x;
-    }
+    const long long per_tz = (long long)ta.nty * nx;
+    const int tzi = (int)(u0 / per_tz);
+    const long long rr0 = u0 - (long long)tzi * per_tz;
+    const int xc = (int)(rr0 / ((long long)ta.nty * L));
+    const long long rr1 = rr0 - (long long)xc * ta.nty * L;
+    const int Lc = min(L, nx - xc * L);
+    const int tyi = (int)(rr1 / Lc);
+    const int xa = xc * L + (int)(rr1 - (long long)tyi * Lc);
+    int xb = xc * L + Lc;
+    if (g0 + (xb - xa) > uend) xb = xa + (int)(uend - g0);
+    g0 += xb - xa;
     if (skip) continue;   // converged grid in a batch: nothing to do, nothing loaded
 
     const int z0 = tzi * TZ;
@@ -417,7 +349,7 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
       tma_load_3d(dst, tmp, c0, y0 - 3, plane_src(p), &bars[sl]);
       if (with_w) tma_load_3d(dst + G::W_OFF_ELEMS, tmwp, cw, y0, p, &bars[sl]);
     };
-    if (contig && tid == 0) {
+    if (tid == 0) {
       seq_issue = base;
       for (int p = xa - 3; p <= plast && p < xa - 3 + S; ++p) issue(p);
     }
@@ -479,15 +411,11 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
     __syncthreads();
     // a slot is refilled only after its previous copy was waited for: once a
     // wait of the issuing thread gave up, nothing more is issued
-    if (tid == 0 && !failed) {   // the slots of planes xa-3 .. xa-1 are free
-      if (contig) {
-        for (int j = 0; j < 3; ++j) {
-          const int p = xa - 3 + j + S;
-          if (p > plast) break;
-          issue(p);
-        }
-      } else {
-        issue_next(); issue_next(); issue_next();
+    if (tid == 0 && !failed) {
+      for (int j = 0; j < 3; ++j) {
+        const int p = xa - 3 + j + S;
+        if (p > plast) break;
+        issue(p);
       }
     }
 
@@ -612,13 +540,7 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
         }
       }
       __syncthreads();
-      if (tid == 0 && !failed) {   // the slot of plane x is free
-        if (contig) {
-          if (x + S <= plast) issue(x + S);
-        } else {
-          issue_next();
-        }
-      }
+      if (tid == 0 && !failed && x + S <= plast) issue(x + S);
       rowbase += plane_stride;
     };
 
@@ -632,9 +554,6 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
       body(std::integral_constant<int, 6>{}, x + 6);
     }
     seq = base + (uint32_t)(xe - xa) + 6;
-    if (!contig && tid == 0 && !failed) {   // slots of planes xe .. xe+2 are free
-      issue_next(); issue_next(); issue_next();
-    }
     failed = __syncthreads_or(failed) != 0;
     if (failed) break;
   }

@@ -24,7 +24,6 @@ struct TiledPlan {
   int* err = nullptr;    // device error flag (owned by the context)
   uint32_t wait_us = 2000000;   // microseconds before a wait gives up
   int inject_wait = 0;   // test hook: waits aim at a phase that never completes
-  int rr = 0;            // round-robin (x-chunk, tile) items instead of contiguous ranges
 };
 
 // Tile shapes instantiated per precision: {TZ, TY, R, ring slots, CTAs/SM}

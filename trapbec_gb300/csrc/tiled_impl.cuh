@@ -123,7 +123,6 @@ int launch_shape(const TiledPlan& plan, int kind, const StageArgs<T>& a, cudaStr
   ta.chunk = plan.chunk;
   ta.wait_us = plan.wait_us;
   ta.inject_wait = plan.inject_wait;
-  ta.rr = plan.rr;
   fill_coeffs<T>(ta);
   const CUtensorMap* tm = nullptr;
   if ((const void*)a.psi_in == plan.psi_base[0]) tm = &plan.tm[0];

@@ -208,35 +208,9 @@ template <typename T> StageArgs<T> base_args(trapbec_ctx* c, double t) {
 }
 
 // Default x-chunk of the work order (the autotuner may pick another).
-// Round-robin items of L planes: the busiest CTA takes ceil(items / grid)
-// items of L planes plus about 3 planes of per-item overhead; L is a multiple
-// of 7 (the kernel's x unroll) so no plane is computed without being stored.
-int rr_auto_chunk(const trapbec_params& p, const TiledPlan& plan) {
-  const long long tiles = (long long)plan.ntz * plan.nty;
-  int best = p.nx;
-  double best_cost = 1e300;
-  for (int L = 7; L <= p.nx; L += 7) {
-    const long long items = tiles * ((p.nx + L - 1) / L);
-    const long long per = (items + plan.grid - 1) / plan.grid;
-    const double cost = (double)per * (L + 3);
-    if (cost < best_cost - 1e-9) { best_cost = cost; best = L; }
-  }
-  return best;
-}
-
-// Work order from the chunk code (trapbec_set_chunk): > 0 round-robin items,
-// < 0 contiguous ranges in x-chunks, 0 automatic.
-void apply_order(const trapbec_params& p, TiledPlan* plan, int code) {
-  if (code > 0) {
-    plan->rr = 1;
-    plan->chunk = std::min(code, p.nx);
-  } else if (code < 0) {
-    plan->rr = 0;
-    plan->chunk = std::min(-code, p.nx);
-  } else {
-    plan->rr = 0;
-    plan->chunk = p.nx;
-  }
+int auto_chunk(const trapbec_ctx* c) {
+  if (c->chunk_user > 0) return std::min(c->chunk_user, c->p.nx);
+  return c->p.nx;   // tile-major: measured fastest at 512^3; the autotuner tries shorter chunks
 }
 
 template <typename T> bool use_tiled(trapbec_ctx* c) {
@@ -708,7 +682,7 @@ template <typename T> int create_impl(trapbec_ctx* c) {
   int rc = setup_tables<T>(c);
   if (rc) return rc;
   c->plan_valid = (plan_tiled<T>(c->p, c->psi, c->w, c->nsm, 0, c->d_err, &c->plan) == 0);
-  if (c->plan_valid) apply_order(c->p, &c->plan, c->chunk_user);
+  if (c->plan_valid) c->plan.chunk = auto_chunk(c);
   return TRAPBEC_OK;
 }
 
@@ -1142,7 +1116,7 @@ int trapbec_set_kernel(trapbec_ctx* c, int kind, int tile_z, int tile_y) {
     int rc = c->prec == TRAPBEC_FP64 ? plan_tiled<double>(c->p, c->psi, c->w, c->nsm, shape, c->d_err, &c->plan)
                                      : plan_tiled<float>(c->p, c->psi, c->w, c->nsm, shape, c->d_err, &c->plan);
     c->plan_valid = (rc == 0);
-    if (c->plan_valid) apply_order(c->p, &c->plan, c->chunk_user);
+    if (c->plan_valid) c->plan.chunk = auto_chunk(c);
   }
   if (kind == 2 && !c->plan_valid) {
     set_error("tiled kernel not available for this grid / tile shape");
@@ -1152,9 +1126,9 @@ int trapbec_set_kernel(trapbec_ctx* c, int kind, int tile_z, int tile_y) {
 }
 
 int trapbec_set_chunk(trapbec_ctx* c, int chunk) {
-  if (!c) return TRAPBEC_ERR_ARG;
+  if (!c || chunk < 0) return TRAPBEC_ERR_ARG;
   c->chunk_user = chunk;
-  if (c->plan_valid) apply_order(c->p, &c->plan, c->chunk_user);
+  if (c->plan_valid) c->plan.chunk = auto_chunk(c);
   return TRAPBEC_OK;
 }
 
@@ -1191,9 +1165,10 @@ template <typename T> int autotune_impl(trapbec_ctx* c, int steps, TuneVal* best
   for (int sh = 0; sh < ns && rc == TRAPBEC_OK; ++sh) {
     TiledPlan plan;
     if (plan_tiled<T>(c->p, c->psi, c->w, c->nsm, sh, c->d_err, &plan) != 0) continue;
-    std::vector<int> chunks = {-c->p.nx, -64, rr_auto_chunk(c->p, plan)};
+    std::vector<int> chunks = {16, 32, 64, c->p.nx};
     for (int L : chunks) {
-      apply_order(c->p, &plan, L);
+      if (L > c->p.nx) continue;
+      plan.chunk = L;
       c->plan = plan;
       c->plan_valid = true;
       c->kernel_kind = 2;
@@ -1215,7 +1190,7 @@ template <typename T> int autotune_impl(trapbec_ctx* c, int steps, TuneVal* best
   if (rc) return rc;
   if (bv.shape < 0) { set_error("no tiled kernel shape fits this grid"); return TRAPBEC_ERR_UNSUPPORTED; }
   if (plan_tiled<T>(c->p, c->psi, c->w, c->nsm, bv.shape, c->d_err, &c->plan) != 0) return TRAPBEC_ERR_CUDA;
-  apply_order(c->p, &c->plan, bv.chunk);
+  c->plan.chunk = bv.chunk;
   c->plan_valid = true;
   c->shape = bv.shape;
   c->chunk_user = bv.chunk;
@@ -1242,7 +1217,7 @@ int trapbec_autotune(trapbec_ctx* c, int steps, int* tile_z, int* tile_y, int* c
     c->shape = bv.shape;
   }
   c->chunk_user = bv.chunk;
-  apply_order(c->p, &c->plan, bv.chunk);
+  c->plan.chunk = bv.chunk;
   Shape sh = c->prec == TRAPBEC_FP64 ? tiled_shape<double>(bv.shape) : tiled_shape<float>(bv.shape);
   if (tile_z) *tile_z = sh.tz;
   if (tile_y) *tile_y = sh.ty;
