@@ -305,14 +305,14 @@ def run_gpu_arm(args):
             s.set_scalar(abi.SCALAR_OMEGA_Z, omega_of_step(args.warmup + args.steps + r * shots))
             s.step_rt(shots)                                       # RK3 steps
             dd = s.diag()                                          # FP64 diagnostics (Psi_info/Psi_norm, E)
-            got = s.get_psi()                                      # D2H of the state
-            host_out[:] = got.reshape(-1)
+            s.get_psi(out=host_out)                                # D2H of the state into pinned memory
         torch.cuda.synchronize()
         et = time.perf_counter() - t0
         e2e = {"value": world * cells * shots * reps / et, "unit": UNIT,
                "h2d_bytes_per_step": int(cells * host.itemsize / shots),
                "d2h_bytes_per_step": int(cells * host.itemsize / shots),
-               "shots": shots, "note": "per call: set_psi (H2D) + shots RK3 steps + diag + get_psi (D2H)"}
+               "shots": shots, "host_buffers": "pinned (page-locked) input and output arrays",
+               "note": "per call: set_psi (H2D) + shots RK3 steps + diag + get_psi (D2H)"}
 
     # ---- FP64 comparison line (same workload, same kernel family) ------------
     fp64 = None

@@ -55,11 +55,18 @@ class Solver:
             a = a.reshape(want)
         check(self.lib.trapbec_set_psi(self.ctx, a.ctypes.data, layout), "trapbec_set_psi")
 
-    def get_psi(self, layout: int = abi.LAYOUT_INTERIOR) -> np.ndarray:
+    def get_psi(self, layout: int = abi.LAYOUT_INTERIOR, out: np.ndarray | None = None) -> np.ndarray:
+        """psi as a host array; `out` (C-contiguous, the context's complex
+        dtype, e.g. a pinned buffer) receives it without another copy."""
         shp = self.shape if layout == abi.LAYOUT_INTERIOR else tuple(s + 6 for s in self.shape)
-        a = np.empty(shp, dtype=self.cdtype)
+        if out is None:
+            a = np.empty(shp, dtype=self.cdtype)
+        else:
+            if out.dtype != self.cdtype or out.size != int(np.prod(shp)) or not out.flags["C_CONTIGUOUS"]:
+                raise ValueError("get_psi: out must be a C-contiguous array of the context's dtype and size")
+            a = out
         check(self.lib.trapbec_get_psi(self.ctx, a.ctypes.data, layout), "trapbec_get_psi")
-        return a
+        return a.reshape(shp)
 
     def set_trap(self, trap: np.ndarray) -> None:
         a = np.ascontiguousarray(trap.reshape(self.shape), dtype=np.float64)
