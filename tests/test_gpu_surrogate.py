@@ -38,8 +38,20 @@ def _bf(a, dev="cuda"):
     return torch.tensor(a, dtype=torch.float32).to(torch.bfloat16).to(dev)
 
 
+@pytest.fixture(params=[0, 1], ids=["tcgen05", "mma_sync"])
+def conv_path(request):
+    """Kernel family of tbsg_conv3_fwd: 0 = tcgen05 for 16/32 -> 16/32
+    channels (mma.sync for the rest), 1 = mma.sync everywhere."""
+    lib = abi.load()
+    assert lib.tbsg_set_conv_path(request.param) == 0
+    yield request.param
+    assert lib.tbsg_set_conv_path(0) == 0
+    flag = C.c_int(-1)
+    assert lib.tbsg_tc_status(C.byref(flag)) == 0 and flag.value == 0
+
+
 @pytest.mark.parametrize("cin,cout", PAIRS)
-def test_conv3_forward_and_gradients(cin, cout):
+def test_conv3_forward_and_gradients(cin, cout, conv_path):
     lib = abi.load()
     rng = np.random.default_rng(cin * 1000 + cout)
     B, D, H, W = 2, 3, 10, 12          # partial bricks in every direction

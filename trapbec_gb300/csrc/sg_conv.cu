@@ -328,11 +328,21 @@ int wgrad_launch(const WgArgs& a, int nch, float* dw, float* db, cudaStream_t st
 // the (CIN, COUT) pairs of the network; the input gradient uses the reversed pair
 #define SG_PAIRS(X) X(16, 16) X(16, 32) X(32, 16) X(32, 32) X(32, 64) X(64, 32) X(64, 64) X(64, 128) X(128, 64) X(128, 128)
 
+int conv3_fwd_tc(const void* x, int cin, const void* w, const float* bias, const void* skip, void* y, float* yf,
+                 int yf_accumulate, int cout, int batch, int D, int H, int W, int act, float slope, cudaStream_t st);
+int g_conv_path = 0;   // 0: tcgen05 where built, else mma.sync; 1: mma.sync only
+
 }  // namespace sg
 
 using namespace sg;
 
 extern "C" {
+
+int tbsg_set_conv_path(int path) {
+  if (path < 0 || path > 1) return TBSG_ERR_ARG;
+  g_conv_path = path;
+  return TBSG_OK;
+}
 
 int tbsg_conv3_fwd(const void* x, int cin, const void* w, const float* bias, const void* skip, void* y,
                    float* yf, int yf_accumulate, int cout, int batch, int D, int H, int W, int act, float slope,
@@ -345,6 +355,10 @@ int tbsg_conv3_fwd(const void* x, int cin, const void* w, const float* bias, con
   a.act = act; a.slope = slope;
   a.mode = yf ? (yf_accumulate ? 1 : 2) : 0;
   cudaStream_t st = (cudaStream_t)stream;
+  if (g_conv_path == 0) {
+    const int rc = conv3_fwd_tc(x, cin, w, bias, skip, y, yf, yf_accumulate, cout, batch, D, H, W, act, slope, st);
+    if (rc != TBSG_ERR_SHAPE) return rc;
+  }
 #define SG_FWD(I, O) \
   if (cin == I && cout == O) return fwd_launch<I, O>(a, batch, st);
   SG_PAIRS(SG_FWD)
