@@ -15,9 +15,11 @@
 // thread issues the 27 x Cin/16 MMAs (M=128, N=Cout, K=16, FP32 accumulate),
 // commits them to an mbarrier, and four warps read the 128 x Cout
 // accumulator from TMEM (warp w owns lanes 32w..32w+31 = brick rows) for the
-// fused bias + skip + leaky-ReLU epilogue.  CTAs are persistent and loop
-// over bricks; several CTAs per SM overlap one brick's loads with another's
-// MMAs.  Waits are bounded in time; TMEM is always released.
+// fused bias + skip + leaky-ReLU epilogue.  CTAs are persistent and run a
+// two-stage pipeline over their bricks with two halo buffers and two TMEM
+// accumulators: while the tensor cores work on brick i, the halo of brick
+// i+1 is in flight and the epilogue drains brick i-1.  Waits are bounded in
+// time; TMEM is always released.
 #include "../../include/trapbec_surrogate.h"
 #include "sg_common.cuh"
 
@@ -28,15 +30,17 @@ constexpr int BH = 16, BW = 8;                  // output brick rows (h) x colum
 constexpr int XD = 3, XH = BH + 2, XW = BW + 2;
 constexpr int XV = XD * XH * XW;                // 540 halo voxels
 constexpr int NTHR = 128;
-constexpr uint32_t TMEM_COLS = 32;
+constexpr uint32_t ACC_COLS = 32;               // one accumulator: 128 lanes x Cout <= 32 columns
+constexpr uint32_t TMEM_COLS = 2 * ACC_COLS;    // double-buffered
 constexpr uint64_t WAIT_NS = 2000000000ull;     // 2 s
 
 __device__ int g_timeout = 0;                   // set when an MMA-completion wait gave up
 
 template <int CIN, int COUT> struct Cfg {
   static constexpr int KC = CIN / 8;
-  static constexpr int X_BYTES = KC * XV * 16;
-  static constexpr int W_OFF = (X_BYTES + 1023) / 1024 * 1024;
+  static constexpr int X_BYTES = KC * XV * 16;                 // one halo buffer
+  static constexpr int X_STRIDE = (X_BYTES + 1023) / 1024 * 1024;
+  static constexpr int W_OFF = 2 * X_STRIDE;
   static constexpr int W_BYTES = 27 * KC * COUT * 16;
   static constexpr int BAR_OFF = W_OFF + W_BYTES;
   static constexpr int SMEM = BAR_OFF + 64;
@@ -99,11 +103,10 @@ struct Args {
 template <int CIN, int COUT>
 __global__ void __launch_bounds__(NTHR) conv3_tc_kernel(Args a) {
   using C = Cfg<CIN, COUT>;
-  static_assert(COUT % 16 == 0 && COUT <= (int)TMEM_COLS, "accumulator columns");
+  static_assert(COUT % 16 == 0 && COUT <= (int)ACC_COLS, "accumulator columns");
   extern __shared__ __align__(1024) unsigned char smem[];
-  unsigned char* xs = smem;
   unsigned char* ws = smem + C::W_OFF;
-  const uint32_t bar = smem_u32(smem + C::BAR_OFF);
+  const uint32_t bar0 = smem_u32(smem + C::BAR_OFF);          // bars[k] at bar0 + 8k
   uint32_t* taddr_s = (uint32_t*)(smem + C::BAR_OFF + 16);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
@@ -114,9 +117,9 @@ __global__ void __launch_bounds__(NTHR) conv3_tc_kernel(Args a) {
     const int co = r % COUT, tap = r / COUT;
     cp_async16(ws + ((size_t)(tap * C::KC + kc) * COUT + co) * 16, a.w + (size_t)r * CIN + kc * 8, 16);
   }
-  cp_async_commit();
   if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0 + 8));
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
@@ -124,80 +127,57 @@ __global__ void __launch_bounds__(NTHR) conv3_tc_kernel(Args a) {
                  "r"(TMEM_COLS));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-  __syncthreads();
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  const uint32_t taddr = *taddr_s;
 
   const int nbw = (a.W + BW - 1) / BW, nbh = (a.H + BH - 1) / BH;
   const long long nbricks = (long long)a.B * a.D * nbh * nbw;
-  const uint32_t xs_a = smem_u32(xs), ws_a = smem_u32(ws);
+  const uint32_t ws_a = smem_u32(ws);
   constexpr uint32_t IDESC = idesc_bf16(128, COUT);
-  uint32_t phase = 0;
-
-  for (long long brick = blockIdx.x; brick < nbricks; brick += gridDim.x) {
+  struct Pos { int b, d, h0, w0; };
+  auto pos_of = [&](long long brick) {
+    Pos q;
     long long r = brick;
     const int bw = (int)(r % nbw); r /= nbw;
     const int bh = (int)(r % nbh); r /= nbh;
-    const int d = (int)(r % a.D);
-    const int b = (int)(r / a.D);
-    const int h0 = bh * BH, w0 = bw * BW;
-    // halo, K-chunked, zero outside the grid
+    q.d = (int)(r % a.D);
+    q.b = (int)(r / a.D);
+    q.h0 = bh * BH;
+    q.w0 = bw * BW;
+    return q;
+  };
+  // halo of a brick into buffer k, K-chunked, zero outside the grid
+  auto load_halo = [&](const Pos& q, int k) {
+    unsigned char* xs = smem + k * C::X_STRIDE;
     for (int i = tid; i < C::KC * XV; i += NTHR) {
       const int hv = i % XV, kc = i / XV;
       const int hw = hv % XW, hh = (hv / XW) % XH, hd = hv / (XW * XH);
-      const int gd = d + hd - 1, gh = h0 + hh - 1, gw = w0 + hw - 1;
+      const int gd = q.d + hd - 1, gh = q.h0 + hh - 1, gw = q.w0 + hw - 1;
       const bool in = gd >= 0 && gd < a.D && gh >= 0 && gh < a.H && gw >= 0 && gw < a.W;
-      const bf16* src = in ? a.x + ((((size_t)b * a.D + gd) * a.H + gh) * a.W + gw) * CIN + kc * 8 : a.x;
+      const bf16* src = in ? a.x + ((((size_t)q.b * a.D + gd) * a.H + gh) * a.W + gw) * CIN + kc * 8 : a.x;
       cp_async16(xs + (size_t)(kc * XV + hv) * 16, src, in ? 16 : 0);
     }
     cp_async_commit();
-    cp_async_wait<0>();
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // cp.async data -> tensor-core reads
-    __syncthreads();
-    if (tid == 0) {
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-#pragma unroll 1
-      for (int tap = 0; tap < 27; ++tap) {
-        const int kd = tap / 9, kh = (tap / 3) % 3, kw = tap % 3;
-#pragma unroll
-        for (int s = 0; s < CIN / 16; ++s) {
-          const uint32_t a_addr = xs_a + (uint32_t)((2 * s) * XV + (kd * XH + kh) * XW + kw) * 16u;
-          const uint32_t b_addr = ws_a + (uint32_t)((tap * C::KC + 2 * s) * COUT) * 16u;
-          const uint64_t ad = sdesc(a_addr, XV * 16, XW * 16);
-          const uint64_t bd = sdesc(b_addr, COUT * 16, 128);
-          const uint32_t acc = (tap | s) ? 1u : 0u;
-          asm volatile(
-              "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-              " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(taddr),
-              "l"(ad), "l"(bd), "r"(IDESC), "r"(acc));
-        }
-      }
-      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
-                   : "memory");
-    }
-    // wait for the MMAs (bounded in time)
-    bool ok = bar_try(bar, phase);
+  };
+  // bounded wait for completion number n of bars[k] (parity n & 1)
+  auto wait_bar = [&](int k, uint32_t n) -> bool {
+    const uint32_t bar = bar0 + 8u * (uint32_t)k, par = n & 1u;
+    bool ok = bar_try(bar, par);
     if (!ok) {
       const uint64_t t0 = now_ns();
-      while (!(ok = bar_try(bar, phase)))
+      while (!(ok = bar_try(bar, par)))
         if (now_ns() - t0 > WAIT_NS) break;
     }
-    phase ^= 1u;
-    if (__syncthreads_or(!ok)) {
-      if (tid == 0) atomicExch(&g_timeout, 1);
-      break;
-    }
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    // epilogue: this thread's brick row m = 32 warp + lane
+    return ok;
+  };
+  auto epilogue = [&](const Pos& q, int k) {
+    const uint32_t tacc = *taddr_s + (uint32_t)k * ACC_COLS;
     const int m = warp * 32 + lane;
-    const int gh = h0 + (m >> 3), gw = w0 + (m & 7);
+    const int gh = q.h0 + (m >> 3), gw = q.w0 + (m & 7);
     const bool store = gh < a.H && gw < a.W;
-    const size_t gv = (((size_t)b * a.D + d) * a.H + gh) * a.W + gw;
+    const size_t gv = (((size_t)q.b * a.D + q.d) * a.H + gh) * a.W + gw;
 #pragma unroll
     for (int c0 = 0; c0 < COUT; c0 += 16) {
       float v[16];
-      tmem_ld16(taddr + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+      tmem_ld16(tacc + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
       if (!store) continue;
       if (a.mode == 0) {
         if (a.bias) {
@@ -227,23 +207,86 @@ __global__ void __launch_bounds__(NTHR) conv3_tc_kernel(Args a) {
       } else {
         float4* op = (float4*)(a.yf + gv * COUT + c0);
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          float4 t = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+        for (int qq = 0; qq < 4; ++qq) {
+          float4 t = make_float4(v[4 * qq], v[4 * qq + 1], v[4 * qq + 2], v[4 * qq + 3]);
           if (a.mode == 1) {
-            const float4 o = op[q];
+            const float4 o = op[qq];
             t.x += o.x; t.y += o.y; t.z += o.z; t.w += o.w;
           }
-          op[q] = t;
+          op[qq] = t;
         }
       }
     }
-    // the next brick overwrites the halo and the accumulator
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  };
+
+  // prologue: the weights and the first halo
+  long long brick = blockIdx.x;
+  Pos cur = pos_of(brick), prev{};
+  load_halo(cur, 0);
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  bool failed = false;
+  int i = 0;
+  for (; brick < nbricks; brick += gridDim.x, ++i) {
+    const int k = i & 1;
+    // halo i (and, the first time, the weights) has landed
+    cp_async_wait<0>();
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // cp.async data -> tensor-core reads
     __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t taddr = *taddr_s;
+    if (tid == 0) {   // brick i: 27 x CIN/16 MMAs into accumulator k
+      const uint32_t xs_a = smem_u32(smem + k * C::X_STRIDE);
+      const uint32_t tacc = taddr + (uint32_t)k * ACC_COLS;
+#pragma unroll 1
+      for (int tap = 0; tap < 27; ++tap) {
+        const int kd = tap / 9, kh = (tap / 3) % 3, kw = tap % 3;
+#pragma unroll
+        for (int s = 0; s < CIN / 16; ++s) {
+          const uint32_t a_addr = xs_a + (uint32_t)((2 * s) * XV + (kd * XH + kh) * XW + kw) * 16u;
+          const uint32_t b_addr = ws_a + (uint32_t)((tap * C::KC + 2 * s) * COUT) * 16u;
+          const uint64_t ad = sdesc(a_addr, XV * 16, XW * 16);
+          const uint64_t bd = sdesc(b_addr, COUT * 16, 128);
+          const uint32_t acc = (tap | s) ? 1u : 0u;
+          asm volatile(
+              "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+              " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tacc),
+              "l"(ad), "l"(bd), "r"(IDESC), "r"(acc));
+        }
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar0 + 8u * k)
+                   : "memory");
+    }
+    // brick i-1's MMAs read the other halo buffer: wait for them, then refill it
+    if (i > 0) {
+      if (__syncthreads_or(!wait_bar(k ^ 1, (uint32_t)(i - 1) >> 1))) { failed = true; break; }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    }
+    const long long next = brick + gridDim.x;
+    Pos nxt{};
+    if (next < nbricks) {
+      nxt = pos_of(next);
+      load_halo(nxt, k ^ 1);
+    }
+    if (i > 0) epilogue(prev, k ^ 1);   // overlaps brick i's MMAs and brick i+1's loads
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    prev = cur;
+    cur = nxt;
   }
+  // drain: the last brick's accumulator
+  if (!failed && i > 0) {
+    const int k = (i - 1) & 1;
+    if (__syncthreads_or(!wait_bar(k, (uint32_t)(i - 1) >> 1))) {
+      failed = true;
+    } else {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      epilogue(prev, k);
+    }
+  }
+  if (failed && tid == 0) atomicExch(&g_timeout, 1);
+  cp_async_wait<0>();   // no copy may outlive the CTA
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
-  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(TMEM_COLS));
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(*taddr_s), "r"(TMEM_COLS));
 }
 
 template <int CIN, int COUT>
@@ -260,7 +303,7 @@ int launch(const Args& a, cudaStream_t st) {
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, conv3_tc_kernel<CIN, COUT>, NTHR, C::SMEM) != cudaSuccess ||
         nb < 1)
       return TBSG_ERR_CUDA;
-    if (nb * (int)TMEM_COLS > 512) nb = 512 / (int)TMEM_COLS;
+    if (nb * (int)TMEM_COLS > 512) nb = 512 / (int)TMEM_COLS;   // TMEM of one SM
     grid = nb * nsm;
   }
   const long long nbricks = (long long)a.B * a.D * ((a.H + BH - 1) / BH) * ((a.W + BW - 1) / BW);
