@@ -4,22 +4,25 @@
 // network's FLOPs (the 128^3 and 64^3 levels).
 //
 // Implicit GEMM per 1 x 16 x 8 output brick: M = 128 voxels, N = Cout,
-// K = 27 taps x Cin.  The halo (3 x 18 x 10 voxels) is staged K-chunked in
-// shared memory, [Cin/8][3][18][10][8 BF16]: the 8 voxels of one brick row
+// K = 27 taps x Cin.  The halo (3 x 18 x 10 voxels) lands K-chunked in shared
+// memory, one TMA box [3][18][10][8 channels] per 8-channel chunk (out-of-
+// range voxels zero-filled by the TMA unit): the 8 voxels of one brick row
 // are 8 consecutive 16-byte rows, i.e. one core matrix of the no-swizzle
 // K-major operand layout, the next brick row is 160 bytes on (the stride
 // between 8-row groups) and the next 8 channels one chunk on (the stride
-// between K core matrices).  So the A operand of every tap is the same
-// descriptor with a different start address.  The weights of the whole
-// layer stay resident in the same layout, [27][Cin/8][Cout][8 BF16].  One
-// thread issues the 27 x Cin/16 MMAs (M=128, N=Cout, K=16, FP32 accumulate),
-// commits them to an mbarrier, and four warps read the 128 x Cout
-// accumulator from TMEM (warp w owns lanes 32w..32w+31 = brick rows) for the
-// fused bias + skip + leaky-ReLU epilogue.  CTAs are persistent and run a
-// two-stage pipeline over their bricks with two halo buffers and two TMEM
-// accumulators: while the tensor cores work on brick i, the halo of brick
-// i+1 is in flight and the epilogue drains brick i-1.  Waits are bounded in
-// time; TMEM is always released.
+// between K core matrices), so the A operand of every tap is the same
+// descriptor with a different start address.  The layer's weights stay
+// resident in the same layout, [27][Cin/8][Cout][8].
+//
+// Warp-specialised persistent CTAs: warp 0 issues the TMA loads of each
+// brick's halo into a ring of stages, warp 1 issues the 27 x Cin/16 MMAs
+// (M=128, N=Cout, K=16, FP32 accumulate) into one of two TMEM accumulators
+// and commits them to mbarriers, warps 2-5 read a finished accumulator from
+// TMEM (a warp reads the 32 lanes of its quarter = 32 brick voxels), release
+// it, and run the fused bias + skip + leaky-ReLU epilogue.  All hand-offs are
+// mbarrier phases; every wait is bounded in time; TMEM is always released.
+#include <cudaTypedefs.h>
+
 #include "../../include/trapbec_surrogate.h"
 #include "sg_common.cuh"
 
@@ -29,27 +32,61 @@ namespace tc {
 constexpr int BH = 16, BW = 8;                  // output brick rows (h) x columns (w); M = 128
 constexpr int XD = 3, XH = BH + 2, XW = BW + 2;
 constexpr int XV = XD * XH * XW;                // 540 halo voxels
-constexpr int NTHR = 128;
+constexpr int CHUNK = 8704;                     // one 8-channel chunk (540 x 16 B), padded to 128 B
+constexpr int NTHR = 192;                       // 6 warps: TMA, MMA, 4 x epilogue
 constexpr uint32_t ACC_COLS = 32;               // one accumulator: 128 lanes x Cout <= 32 columns
-constexpr uint32_t TMEM_COLS = 2 * ACC_COLS;    // double-buffered
+constexpr uint32_t TMEM_COLS = 2 * ACC_COLS;    // two accumulators
 constexpr uint64_t WAIT_NS = 2000000000ull;     // 2 s
 
-__device__ int g_timeout = 0;                   // set when an MMA-completion wait gave up
+__device__ int g_timeout = 0;                   // set when a wait gave up
 
 template <int CIN, int COUT> struct Cfg {
   static constexpr int KC = CIN / 8;
-  static constexpr int X_BYTES = KC * XV * 16;                 // one halo buffer
-  static constexpr int X_STRIDE = (X_BYTES + 1023) / 1024 * 1024;
-  static constexpr int W_OFF = 2 * X_STRIDE;
+  static constexpr int STAGE = KC * CHUNK;                       // one halo
   static constexpr int W_BYTES = 27 * KC * COUT * 16;
-  static constexpr int BAR_OFF = W_OFF + W_BYTES;
-  static constexpr int SMEM = BAR_OFF + 64;
+  static constexpr int NS = (STAGE * 3 + W_BYTES <= 150 * 1024) ? 3 : 2;   // halo ring depth
+  static constexpr int W_OFF = NS * STAGE;
+  static constexpr int BAR_OFF = (W_OFF + W_BYTES + 127) / 128 * 128;
+  static constexpr int SMEM = BAR_OFF + 128;
 };
 
 __device__ __forceinline__ uint64_t now_ns() {
   uint64_t t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
+}
+__device__ __forceinline__ bool bar_try(uint32_t bar, uint32_t par) {
+  uint32_t ok;
+  asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+               : "=r"(ok)
+               : "r"(bar), "r"(par)
+               : "memory");
+  return ok != 0;
+}
+// bounded wait for the phase of parity `par`
+__device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t par) {
+  if (bar_try(bar, par)) return true;
+  const uint64_t t0 = now_ns();
+  while (!bar_try(bar, par))
+    if (now_ns() - t0 > WAIT_NS) return false;
+  return true;
+}
+__device__ __forceinline__ void bar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
+}
+__device__ __forceinline__ void bar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void bar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void tma_load_5d(uint32_t dst, const CUtensorMap* tm, int c0, int c1, int c2, int c3, int c4,
+                                            uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, %6}], "
+      "[%7];" ::"r"(dst),
+      "l"(tm), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(bar)
+      : "memory");
 }
 
 // shared-memory operand descriptor: K-major, no swizzle
@@ -66,25 +103,12 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
-__device__ __forceinline__ bool bar_try(uint32_t bar, uint32_t par) {
-  uint32_t ok;
-  asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-               : "=r"(ok)
-               : "r"(bar), "r"(par)
-               : "memory");
-  return ok != 0;
-}
-
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float v[16]) {
-  uint32_t r[16];
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t r[16]) {
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
       : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
         "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
       : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
 }
 
 struct Args {
@@ -101,13 +125,17 @@ struct Args {
 };
 
 template <int CIN, int COUT>
-__global__ void __launch_bounds__(NTHR) conv3_tc_kernel(Args a) {
+__global__ void __launch_bounds__(NTHR, 1) conv3_tc_kernel(const __grid_constant__ CUtensorMap tmx, Args a) {
   using C = Cfg<CIN, COUT>;
+  constexpr int NS = C::NS;
   static_assert(COUT % 16 == 0 && COUT <= (int)ACC_COLS, "accumulator columns");
   extern __shared__ __align__(1024) unsigned char smem[];
-  unsigned char* ws = smem + C::W_OFF;
-  const uint32_t bar0 = smem_u32(smem + C::BAR_OFF);          // bars[k] at bar0 + 8k
-  uint32_t* taddr_s = (uint32_t*)(smem + C::BAR_OFF + 16);
+  const uint32_t s0 = smem_u32(smem);
+  const uint32_t ws_a = s0 + C::W_OFF;
+  // barriers: full[NS], empty[NS], acc_full[2], acc_empty[2]; then the TMEM address
+  const uint32_t full0 = s0 + C::BAR_OFF, empty0 = full0 + 8 * NS;
+  const uint32_t afull0 = empty0 + 8 * NS, aempty0 = afull0 + 16;
+  uint32_t* taddr_s = (uint32_t*)(smem + C::BAR_OFF + 8 * (2 * NS + 4));
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
   // resident weights: [27][COUT][CIN] -> [27][KC][COUT][8]
@@ -115,178 +143,170 @@ __global__ void __launch_bounds__(NTHR) conv3_tc_kernel(Args a) {
     const int kc = i % C::KC;
     const int r = i / C::KC;   // tap * COUT + co
     const int co = r % COUT, tap = r / COUT;
-    cp_async16(ws + ((size_t)(tap * C::KC + kc) * COUT + co) * 16, a.w + (size_t)r * CIN + kc * 8, 16);
+    cp_async16(smem + C::W_OFF + ((size_t)(tap * C::KC + kc) * COUT + co) * 16, a.w + (size_t)r * CIN + kc * 8, 16);
   }
+  cp_async_commit();
   if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0));
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0 + 8));
+    for (int s = 0; s < NS; ++s) { bar_init(full0 + 8 * s, 1); bar_init(empty0 + 8 * s, 1); }
+    for (int k = 0; k < 2; ++k) { bar_init(afull0 + 8 * k, 1); bar_init(aempty0 + 8 * k, 4); }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 0) {
+  if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(taddr_s)),
                  "r"(TMEM_COLS));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
+  cp_async_wait<0>();
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // weights -> tensor-core reads
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t taddr = *taddr_s;
 
   const int nbw = (a.W + BW - 1) / BW, nbh = (a.H + BH - 1) / BH;
   const long long nbricks = (long long)a.B * a.D * nbh * nbw;
-  const uint32_t ws_a = smem_u32(ws);
-  constexpr uint32_t IDESC = idesc_bf16(128, COUT);
-  struct Pos { int b, d, h0, w0; };
-  auto pos_of = [&](long long brick) {
-    Pos q;
-    long long r = brick;
-    const int bw = (int)(r % nbw); r /= nbw;
-    const int bh = (int)(r % nbh); r /= nbh;
-    q.d = (int)(r % a.D);
-    q.b = (int)(r / a.D);
-    q.h0 = bh * BH;
-    q.w0 = bw * BW;
-    return q;
-  };
-  // halo of a brick into buffer k, K-chunked, zero outside the grid
-  auto load_halo = [&](const Pos& q, int k) {
-    unsigned char* xs = smem + k * C::X_STRIDE;
-    for (int i = tid; i < C::KC * XV; i += NTHR) {
-      const int hv = i % XV, kc = i / XV;
-      const int hw = hv % XW, hh = (hv / XW) % XH, hd = hv / (XW * XH);
-      const int gd = q.d + hd - 1, gh = q.h0 + hh - 1, gw = q.w0 + hw - 1;
-      const bool in = gd >= 0 && gd < a.D && gh >= 0 && gh < a.H && gw >= 0 && gw < a.W;
-      const bf16* src = in ? a.x + ((((size_t)q.b * a.D + gd) * a.H + gh) * a.W + gw) * CIN + kc * 8 : a.x;
-      cp_async16(xs + (size_t)(kc * XV + hv) * 16, src, in ? 16 : 0);
-    }
-    cp_async_commit();
-  };
-  // bounded wait for completion number n of bars[k] (parity n & 1)
-  auto wait_bar = [&](int k, uint32_t n) -> bool {
-    const uint32_t bar = bar0 + 8u * (uint32_t)k, par = n & 1u;
-    bool ok = bar_try(bar, par);
-    if (!ok) {
-      const uint64_t t0 = now_ns();
-      while (!(ok = bar_try(bar, par)))
-        if (now_ns() - t0 > WAIT_NS) break;
-    }
-    return ok;
-  };
-  auto epilogue = [&](const Pos& q, int k) {
-    const uint32_t tacc = *taddr_s + (uint32_t)k * ACC_COLS;
-    const int m = warp * 32 + lane;
-    const int gh = q.h0 + (m >> 3), gw = q.w0 + (m & 7);
-    const bool store = gh < a.H && gw < a.W;
-    const size_t gv = (((size_t)q.b * a.D + q.d) * a.H + gh) * a.W + gw;
-#pragma unroll
-    for (int c0 = 0; c0 < COUT; c0 += 16) {
-      float v[16];
-      tmem_ld16(tacc + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
-      if (!store) continue;
-      if (a.mode == 0) {
-        if (a.bias) {
-#pragma unroll
-          for (int j = 0; j < 16; ++j) v[j] += a.bias[c0 + j];
-        }
-        if (a.skip) {
-          const uint4* sp = (const uint4*)(a.skip + gv * COUT + c0);
-          uint4 s0 = sp[0], s1 = sp[1];
-          const bf16* e0 = (const bf16*)&s0;
-          const bf16* e1 = (const bf16*)&s1;
-#pragma unroll
-          for (int j = 0; j < 8; ++j) { v[j] += __bfloat162float(e0[j]); v[8 + j] += __bfloat162float(e1[j]); }
-        }
-        if (a.act) {
-#pragma unroll
-          for (int j = 0; j < 16; ++j) v[j] = leaky(v[j], a.slope);
-        }
-        uint4 o0, o1;
-        bf16* f0 = (bf16*)&o0;
-        bf16* f1 = (bf16*)&o1;
-#pragma unroll
-        for (int j = 0; j < 8; ++j) { f0[j] = __float2bfloat16_rn(v[j]); f1[j] = __float2bfloat16_rn(v[8 + j]); }
-        uint4* op = (uint4*)(a.y + gv * COUT + c0);
-        op[0] = o0;
-        op[1] = o1;
-      } else {
-        float4* op = (float4*)(a.yf + gv * COUT + c0);
-#pragma unroll
-        for (int qq = 0; qq < 4; ++qq) {
-          float4 t = make_float4(v[4 * qq], v[4 * qq + 1], v[4 * qq + 2], v[4 * qq + 3]);
-          if (a.mode == 1) {
-            const float4 o = op[qq];
-            t.x += o.x; t.y += o.y; t.z += o.z; t.w += o.w;
-          }
-          op[qq] = t;
-        }
-      }
-    }
-  };
+  const int nmine = blockIdx.x < nbricks ? (int)((nbricks - 1 - blockIdx.x) / gridDim.x + 1) : 0;
+  bool ok = true;
 
-  // prologue: the weights and the first halo
-  long long brick = blockIdx.x;
-  Pos cur = pos_of(brick), prev{};
-  load_halo(cur, 0);
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-  bool failed = false;
-  int i = 0;
-  for (; brick < nbricks; brick += gridDim.x, ++i) {
-    const int k = i & 1;
-    // halo i (and, the first time, the weights) has landed
-    cp_async_wait<0>();
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // cp.async data -> tensor-core reads
-    __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    const uint32_t taddr = *taddr_s;
-    if (tid == 0) {   // brick i: 27 x CIN/16 MMAs into accumulator k
-      const uint32_t xs_a = smem_u32(smem + k * C::X_STRIDE);
-      const uint32_t tacc = taddr + (uint32_t)k * ACC_COLS;
+  if (warp == 0) {
+    // ---- TMA producer --------------------------------------------------------
+    if (lane == 0) {
+      for (int j = 0; j < nmine && ok; ++j) {
+        const int s = j % NS;
+        if (j >= NS) ok = bar_wait(empty0 + 8 * s, (uint32_t)((j / NS - 1) & 1));
+        if (!ok) break;
+        long long r = blockIdx.x + (long long)j * gridDim.x;
+        const int bw = (int)(r % nbw); r /= nbw;
+        const int bh = (int)(r % nbh); r /= nbh;
+        const int d = (int)(r % a.D), b = (int)(r / a.D);
+        bar_expect_tx(full0 + 8 * s, (uint32_t)(C::KC * XV * 16));
+        for (int kc = 0; kc < C::KC; ++kc)
+          tma_load_5d(s0 + s * C::STAGE + kc * CHUNK, &tmx, kc * 8, bw * BW - 1, bh * BH - 1, d - 1, b, full0 + 8 * s);
+      }
+      // let the last loads land before the CTA can end
+      for (int j = nmine - NS > 0 ? nmine - NS : 0; j < nmine; ++j)
+        (void)bar_wait(full0 + 8 * (j % NS), (uint32_t)((j / NS) & 1));
+    }
+  } else if (warp == 1) {
+    // ---- MMA issuer ------------------------------------------------------------
+    if (lane == 0) {
+      constexpr uint32_t IDESC = idesc_bf16(128, COUT);
+      for (int j = 0; j < nmine && ok; ++j) {
+        const int s = j % NS, k = j & 1;
+        ok = bar_wait(full0 + 8 * s, (uint32_t)((j / NS) & 1));
+        if (ok && j >= 2) ok = bar_wait(aempty0 + 8 * k, (uint32_t)((j / 2 - 1) & 1));
+        if (!ok) break;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t xs_a = s0 + s * C::STAGE;
+        const uint32_t tacc = taddr + (uint32_t)k * ACC_COLS;
 #pragma unroll 1
-      for (int tap = 0; tap < 27; ++tap) {
-        const int kd = tap / 9, kh = (tap / 3) % 3, kw = tap % 3;
+        for (int tap = 0; tap < 27; ++tap) {
+          const int kd = tap / 9, kh = (tap / 3) % 3, kw = tap % 3;
 #pragma unroll
-        for (int s = 0; s < CIN / 16; ++s) {
-          const uint32_t a_addr = xs_a + (uint32_t)((2 * s) * XV + (kd * XH + kh) * XW + kw) * 16u;
-          const uint32_t b_addr = ws_a + (uint32_t)((tap * C::KC + 2 * s) * COUT) * 16u;
-          const uint64_t ad = sdesc(a_addr, XV * 16, XW * 16);
-          const uint64_t bd = sdesc(b_addr, COUT * 16, 128);
-          const uint32_t acc = (tap | s) ? 1u : 0u;
-          asm volatile(
-              "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-              " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tacc),
-              "l"(ad), "l"(bd), "r"(IDESC), "r"(acc));
+          for (int q = 0; q < CIN / 16; ++q) {
+            const uint32_t a_addr = xs_a + (uint32_t)(2 * q) * CHUNK + (uint32_t)((kd * XH + kh) * XW + kw) * 16u;
+            const uint32_t b_addr = ws_a + (uint32_t)((tap * C::KC + 2 * q) * COUT) * 16u;
+            const uint64_t ad = sdesc(a_addr, CHUNK, XW * 16);
+            const uint64_t bd = sdesc(b_addr, COUT * 16, 128);
+            const uint32_t acc = (tap | q) ? 1u : 0u;
+            asm volatile(
+                "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tacc),
+                "l"(ad), "l"(bd), "r"(IDESC), "r"(acc));
+          }
+        }
+        // the halo stage is free once these MMAs are done; so is the accumulator for reading
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(empty0 + 8 * s)
+                     : "memory");
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(afull0 + 8 * k)
+                     : "memory");
+      }
+    }
+  } else {
+    // ---- epilogue: warps 2..5, TMEM lane quarter = warp % 4 ----------------------
+    const int quarter = warp & 3;
+    const int m = quarter * 32 + lane;   // brick voxel of this thread
+    for (int j = 0; j < nmine && ok; ++j) {
+      const int k = j & 1;
+      ok = bar_wait(afull0 + 8 * k, (uint32_t)((j / 2) & 1));
+      if (!__all_sync(0xffffffffu, ok)) { ok = false; break; }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      uint32_t r[COUT];
+#pragma unroll
+      for (int c0 = 0; c0 < COUT; c0 += 16)
+        tmem_ld16(taddr + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(k * ACC_COLS + c0), r + c0);
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) bar_arrive(aempty0 + 8 * k);   // the accumulator may be overwritten
+      long long rr = blockIdx.x + (long long)j * gridDim.x;
+      const int bw = (int)(rr % nbw); rr /= nbw;
+      const int bh = (int)(rr % nbh); rr /= nbh;
+      const int d = (int)(rr % a.D), b = (int)(rr / a.D);
+      const int gh = bh * BH + (m >> 3), gw = bw * BW + (m & 7);
+      if (gh >= a.H || gw >= a.W) continue;
+      const size_t gv = (((size_t)b * a.D + d) * a.H + gh) * a.W + gw;
+#pragma unroll
+      for (int c0 = 0; c0 < COUT; c0 += 16) {
+        float v[16];
+#pragma unroll
+        for (int jj = 0; jj < 16; ++jj) v[jj] = __uint_as_float(r[c0 + jj]);
+        if (a.mode == 0) {
+          if (a.bias) {
+#pragma unroll
+            for (int jj = 0; jj < 16; ++jj) v[jj] += a.bias[c0 + jj];
+          }
+          if (a.skip) {
+            const uint4* sp = (const uint4*)(a.skip + gv * COUT + c0);
+            uint4 q0 = sp[0], q1 = sp[1];
+            const bf16* e0 = (const bf16*)&q0;
+            const bf16* e1 = (const bf16*)&q1;
+#pragma unroll
+            for (int jj = 0; jj < 8; ++jj) { v[jj] += __bfloat162float(e0[jj]); v[8 + jj] += __bfloat162float(e1[jj]); }
+          }
+          if (a.act) {
+#pragma unroll
+            for (int jj = 0; jj < 16; ++jj) v[jj] = leaky(v[jj], a.slope);
+          }
+          uint4 o0, o1;
+          bf16* f0 = (bf16*)&o0;
+          bf16* f1 = (bf16*)&o1;
+#pragma unroll
+          for (int jj = 0; jj < 8; ++jj) { f0[jj] = __float2bfloat16_rn(v[jj]); f1[jj] = __float2bfloat16_rn(v[8 + jj]); }
+          uint4* op = (uint4*)(a.y + gv * COUT + c0);
+          op[0] = o0;
+          op[1] = o1;
+        } else {
+          float4* op = (float4*)(a.yf + gv * COUT + c0);
+#pragma unroll
+          for (int qq = 0; qq < 4; ++qq) {
+            float4 t = make_float4(v[4 * qq], v[4 * qq + 1], v[4 * qq + 2], v[4 * qq + 3]);
+            if (a.mode == 1) {
+              const float4 o = op[qq];
+              t.x += o.x; t.y += o.y; t.z += o.z; t.w += o.w;
+            }
+            op[qq] = t;
+          }
         }
       }
-      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar0 + 8u * k)
-                   : "memory");
-    }
-    // brick i-1's MMAs read the other halo buffer: wait for them, then refill it
-    if (i > 0) {
-      if (__syncthreads_or(!wait_bar(k ^ 1, (uint32_t)(i - 1) >> 1))) { failed = true; break; }
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    }
-    const long long next = brick + gridDim.x;
-    Pos nxt{};
-    if (next < nbricks) {
-      nxt = pos_of(next);
-      load_halo(nxt, k ^ 1);
-    }
-    if (i > 0) epilogue(prev, k ^ 1);   // overlaps brick i's MMAs and brick i+1's loads
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    prev = cur;
-    cur = nxt;
-  }
-  // drain: the last brick's accumulator
-  if (!failed && i > 0) {
-    const int k = (i - 1) & 1;
-    if (__syncthreads_or(!wait_bar(k, (uint32_t)(i - 1) >> 1))) {
-      failed = true;
-    } else {
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      epilogue(prev, k);
     }
   }
-  if (failed && tid == 0) atomicExch(&g_timeout, 1);
-  cp_async_wait<0>();   // no copy may outlive the CTA
+  if (!ok) atomicExch(&g_timeout, 1);
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
-  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(*taddr_s), "r"(TMEM_COLS));
+  if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(TMEM_COLS));
+}
+
+inline PFN_cuTensorMapEncodeTiled_v12000 encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (PFN_cuTensorMapEncodeTiled_v12000)f;
+  }
+  return fn;
 }
 
 template <int CIN, int COUT>
@@ -306,9 +326,22 @@ int launch(const Args& a, cudaStream_t st) {
     if (nb * (int)TMEM_COLS > 512) nb = 512 / (int)TMEM_COLS;   // TMEM of one SM
     grid = nb * nsm;
   }
+  // the activation tensor [B][D][H][W][CIN] as a 5-D TMA map (innermost first)
+  auto enc = encoder();
+  if (!enc) return TBSG_ERR_CUDA;
+  CUtensorMap tm;
+  cuuint64_t dims[5] = {(cuuint64_t)CIN, (cuuint64_t)a.W, (cuuint64_t)a.H, (cuuint64_t)a.D, (cuuint64_t)a.B};
+  cuuint64_t strides[4] = {(cuuint64_t)CIN * 2, (cuuint64_t)a.W * CIN * 2, (cuuint64_t)a.H * a.W * CIN * 2,
+                           (cuuint64_t)a.D * a.H * a.W * CIN * 2};
+  cuuint32_t box[5] = {8, (cuuint32_t)XW, (cuuint32_t)XH, (cuuint32_t)XD, 1};
+  cuuint32_t es[5] = {1, 1, 1, 1, 1};
+  if (enc(&tm, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, (void*)a.x, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+          CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) !=
+      CUDA_SUCCESS)
+    return TBSG_ERR_ARG;
   const long long nbricks = (long long)a.B * a.D * ((a.H + BH - 1) / BH) * ((a.W + BW - 1) / BW);
   const int g = (int)(nbricks < grid ? nbricks : grid);
-  conv3_tc_kernel<CIN, COUT><<<g, NTHR, C::SMEM, st>>>(a);
+  conv3_tc_kernel<CIN, COUT><<<g, NTHR, C::SMEM, st>>>(tm, a);
   return cudaGetLastError() == cudaSuccess ? TBSG_OK : TBSG_ERR_CUDA;
 }
 
@@ -323,6 +356,7 @@ int conv3_fwd_tc(const void* x, int cin, const void* w, const float* bias, const
   a.B = batch; a.D = D; a.H = H; a.W = W;
   a.act = act; a.slope = slope;
   a.mode = yf ? (yf_accumulate ? 1 : 2) : 0;
+  if ((uintptr_t)x % 16) return TBSG_ERR_SHAPE;   // TMA needs a 16-byte aligned base
   if (cin == 16 && cout == 16) return tc::launch<16, 16>(a, st);
   if (cin == 16 && cout == 32) return tc::launch<16, 32>(a, st);
   if (cin == 32 && cout == 16) return tc::launch<32, 16>(a, st);
