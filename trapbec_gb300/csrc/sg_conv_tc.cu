@@ -175,10 +175,10 @@ __global__ void __launch_bounds__(NTHR, 1) conv3_tc_kernel(const __grid_constant
         const int s = j % NS;
         if (j >= NS) ok = bar_wait(empty0 + 8 * s, (uint32_t)((j / NS - 1) & 1));
         if (!ok) break;
-        long long r = blockIdx.x + (long long)j * gridDim.x;
-        const int bw = (int)(r % nbw); r /= nbw;
-        const int bh = (int)(r % nbh); r /= nbh;
-        const int d = (int)(r % a.D), b = (int)(r / a.D);
+        unsigned r = blockIdx.x + (unsigned)j * gridDim.x;
+        const int bw = (int)(r % (unsigned)nbw); r /= (unsigned)nbw;
+        const int bh = (int)(r % (unsigned)nbh); r /= (unsigned)nbh;
+        const int d = (int)(r % (unsigned)a.D), b = (int)(r / (unsigned)a.D);
         bar_expect_tx(full0 + 8 * s, (uint32_t)(C::KC * XV * 16));
         for (int kc = 0; kc < C::KC; ++kc)
           tma_load_5d(s0 + s * C::STAGE + kc * CHUNK, &tmx, kc * 8, bw * BW - 1, bh * BH - 1, d - 1, b, full0 + 8 * s);
@@ -197,17 +197,18 @@ __global__ void __launch_bounds__(NTHR, 1) conv3_tc_kernel(const __grid_constant
         if (ok && j >= 2) ok = bar_wait(aempty0 + 8 * k, (uint32_t)((j / 2 - 1) & 1));
         if (!ok) break;
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint32_t xs_a = s0 + s * C::STAGE;
         const uint32_t tacc = taddr + (uint32_t)k * ACC_COLS;
-#pragma unroll 1
+        // the start-address field counts 16-byte units: per-tap operands are
+        // the base descriptors plus compile-time offsets
+        const uint64_t ad0 = sdesc(s0 + s * C::STAGE, CHUNK, XW * 16);
+        const uint64_t bd0 = sdesc(ws_a, COUT * 16, 128);
+#pragma unroll
         for (int tap = 0; tap < 27; ++tap) {
           const int kd = tap / 9, kh = (tap / 3) % 3, kw = tap % 3;
 #pragma unroll
           for (int q = 0; q < CIN / 16; ++q) {
-            const uint32_t a_addr = xs_a + (uint32_t)(2 * q) * CHUNK + (uint32_t)((kd * XH + kh) * XW + kw) * 16u;
-            const uint32_t b_addr = ws_a + (uint32_t)((tap * C::KC + 2 * q) * COUT) * 16u;
-            const uint64_t ad = sdesc(a_addr, CHUNK, XW * 16);
-            const uint64_t bd = sdesc(b_addr, COUT * 16, 128);
+            const uint64_t ad = ad0 + (uint64_t)((2 * q) * (CHUNK / 16) + (kd * XH + kh) * XW + kw);
+            const uint64_t bd = bd0 + (uint64_t)((tap * C::KC + 2 * q) * COUT);
             const uint32_t acc = (tap | q) ? 1u : 0u;
             asm volatile(
                 "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
@@ -226,6 +227,9 @@ __global__ void __launch_bounds__(NTHR, 1) conv3_tc_kernel(const __grid_constant
     // ---- epilogue: warps 2..5, TMEM lane quarter = warp % 4 ----------------------
     const int quarter = warp & 3;
     const int m = quarter * 32 + lane;   // brick voxel of this thread
+    float bias_r[COUT];
+#pragma unroll
+    for (int c = 0; c < COUT; ++c) bias_r[c] = (a.mode == 0 && a.bias) ? a.bias[c] : 0.f;
     for (int j = 0; j < nmine && ok; ++j) {
       const int k = j & 1;
       ok = bar_wait(afull0 + 8 * k, (uint32_t)((j / 2) & 1));
@@ -239,10 +243,10 @@ __global__ void __launch_bounds__(NTHR, 1) conv3_tc_kernel(const __grid_constant
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       __syncwarp();
       if (lane == 0) bar_arrive(aempty0 + 8 * k);   // the accumulator may be overwritten
-      long long rr = blockIdx.x + (long long)j * gridDim.x;
-      const int bw = (int)(rr % nbw); rr /= nbw;
-      const int bh = (int)(rr % nbh); rr /= nbh;
-      const int d = (int)(rr % a.D), b = (int)(rr / a.D);
+      unsigned rr = blockIdx.x + (unsigned)j * gridDim.x;
+      const int bw = (int)(rr % (unsigned)nbw); rr /= (unsigned)nbw;
+      const int bh = (int)(rr % (unsigned)nbh); rr /= (unsigned)nbh;
+      const int d = (int)(rr % (unsigned)a.D), b = (int)(rr / (unsigned)a.D);
       const int gh = bh * BH + (m >> 3), gw = bw * BW + (m & 7);
       if (gh >= a.H || gw >= a.W) continue;
       const size_t gv = (((size_t)b * a.D + d) * a.H + gh) * a.W + gw;
@@ -252,10 +256,8 @@ __global__ void __launch_bounds__(NTHR, 1) conv3_tc_kernel(const __grid_constant
 #pragma unroll
         for (int jj = 0; jj < 16; ++jj) v[jj] = __uint_as_float(r[c0 + jj]);
         if (a.mode == 0) {
-          if (a.bias) {
 #pragma unroll
-            for (int jj = 0; jj < 16; ++jj) v[jj] += a.bias[c0 + jj];
-          }
+          for (int jj = 0; jj < 16; ++jj) v[jj] += bias_r[c0 + jj];
           if (a.skip) {
             const uint4* sp = (const uint4*)(a.skip + gv * COUT + c0);
             uint4 q0 = sp[0], q1 = sp[1];
@@ -340,6 +342,7 @@ int launch(const Args& a, cudaStream_t st) {
       CUDA_SUCCESS)
     return TBSG_ERR_ARG;
   const long long nbricks = (long long)a.B * a.D * ((a.H + BH - 1) / BH) * ((a.W + BW - 1) / BW);
+  if (nbricks >= (1ll << 31)) return TBSG_ERR_SHAPE;   // brick indices are 32-bit in the kernel
   const int g = (int)(nbricks < grid ? nbricks : grid);
   conv3_tc_kernel<CIN, COUT><<<g, NTHR, C::SMEM, st>>>(tm, a);
   return cudaGetLastError() == cudaSuccess ? TBSG_OK : TBSG_ERR_CUDA;
