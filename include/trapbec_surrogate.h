@@ -6,7 +6,7 @@
  * encoder-decoder that predicts the ground-state amplitude from the trap
  * potential and the instance parameters; its prediction is only ever used as
  * the initial guess of trapbec_step_imag / trapbec_batch_solve_imag, and the
- * Thomas-Fermi guess remains both the fallback and the judge.
+ * Thomas-Fermi guess remains both the fallback and the yardstick.
  *
  * Conventions: all pointers are device pointers; activations are BF16,
  * channels-last [batch][D][H][W][C] with C a multiple of 16; gradients of

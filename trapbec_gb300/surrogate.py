@@ -19,8 +19,8 @@ and nucleate vortices.  The phase is not predicted: in the axially symmetric
 traps of this workload the ground state is either real (no vortices) or
 carries a vortex lattice whose positions break the symmetry, and a smooth
 phase field can represent neither.  Relaxation from the Thomas-Fermi guess
-stays the fallback and the judge: both runs stop on the same relative energy
-change, and their final energies are compared.
+stays the fallback and the yardstick: both runs stop on the same relative
+energy change, and their final energies are compared.
 """
 from __future__ import annotations
 
