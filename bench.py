@@ -250,6 +250,9 @@ def run_gpu_arm(args):
     s = Solver(p)
     if args.kernel:
         s.set_kernel(*args.kernel)
+    tune = None
+    if args.kernel is None and not args.no_autotune:
+        tune = s.autotune(steps=8)   # tile shape and work order for this grid (state restored)
     s.init_state(init["name"], seed=init["seed"] + rank, amp=init["amp"], r_tf2=init["r_tf2"],
                  noise_amp=init["noise_amp"])
     ramp_steps = 5000
@@ -323,6 +326,8 @@ def run_gpu_arm(args):
         s64 = Solver(p64)
         s64.init_state(init["name"], seed=init["seed"] + rank, amp=init["amp"], r_tf2=init["r_tf2"],
                        noise_amp=init["noise_amp"])
+        if not args.no_autotune:
+            s64.autotune(steps=2)
         timed_steps(s64, 2, chunk, omega_of_step, 0)
         k64 = args.fp64_steps
         ms64, _ = timed_steps(s64, k64, chunk, omega_of_step, 2)
@@ -350,7 +355,7 @@ def run_gpu_arm(args):
                    "omega_ramp": "0 -> 0.8 omega_perp over 5000 steps, updated every chunk",
                    "chunk_steps": chunk, "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2_flush": "inputs larger than L2 (1 GiB per array)",
-                   "kernel": kernel_name},
+                   "kernel": kernel_name, "autotune": tune},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                      "algorithmic_bytes_per_point_step": bpc,
@@ -391,6 +396,7 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--kernel", type=int, nargs=3, default=None, metavar=("KIND", "TZ", "TY"))
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default tile shape and work order")
     ap.add_argument("--imag", action="store_true", help="add the batched imaginary-time leg")
     ap.add_argument("--imag-count", type=int, default=16)
     ap.add_argument("--imag-seed", type=int, default=3)
