@@ -652,7 +652,7 @@ def main(argv=None):
             net.save(a.out, {"S": a.S, "n_train": a.n_train, "seed": a.seed, "epochs": a.epochs})
     # held-out accuracy of the guess itself, then the relaxation comparison
     rep["compare"] = []
-    for nz in a.nn_noise:
+    for nz in (a.nn_noise if test_d else []):
         cmp_ = compare(net, test_d, tol=a.tol, max_steps=a.max_steps, nn_noise=nz)
         rep["compare"].append(cmp_)
         log(json.dumps({k: cmp_[k] for k in ("nn_noise", "nn_used", "steps_ratio_median", "steps_ratio_median_nn_used",
