@@ -203,10 +203,10 @@ def warmstart_leg(args):
     """Imaginary-time relaxation to |dE|/|E| <= tol at 128^3 from the
     surrogate's guess against the Thomas-Fermi + 1e-2 noise guess, on draws
     held out from the surrogate's training set (the committed weights were
-    trained on draws 0..191 of seed 2024; this leg uses the draws after them).
+    trained on draws 0..383 of seed 2024; this leg uses draws from 400 on).
     Both relaxations run batched; device time from events around each solve."""
     from trapbec_gb300 import abi, units, surrogate
-    n0 = 192
+    n0 = 400
     draws = units.ground_state_draws(n0 + args.ws_count, 2024, grids=(128,), precision=abi.FP32)[n0:]
     net = surrogate.Surrogate(128, 2, seed=0)
     net.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "trapbec_gb300", "weights",
@@ -404,7 +404,7 @@ def main():
     ap.add_argument("--imag-tol", type=float, default=1e-10)
     ap.add_argument("--imag-max-steps", type=int, default=20000)
     ap.add_argument("--no-warmstart", action="store_true", help="skip the NN-vs-TF imaginary-time leg")
-    ap.add_argument("--ws-count", type=int, default=8, help="held-out draws of the NN-vs-TF leg")
+    ap.add_argument("--ws-count", type=int, default=16, help="held-out draws of the NN-vs-TF leg")
     ap.add_argument("--ws-max-steps", type=int, default=20000)
     args = ap.parse_args()
     if args.warmup < 3:
