@@ -5,8 +5,8 @@
 //
 // Implicit GEMM per 1 x 16 x 8 output brick: M = 128 voxels, N = Cout,
 // K = 27 taps x Cin.  The halo (3 x 18 x 10 voxels) lands K-chunked in shared
-// memory, [Cin/8][3][18][10][8 channels] (out-of-range voxels zero-filled by
-// the copies): the 8 voxels of one brick row
+// memory, one TMA box [3][18][10][8 channels] per 8-channel chunk (out-of-
+// range voxels zero-filled by the TMA unit): the 8 voxels of one brick row
 // are 8 consecutive 16-byte rows, i.e. one core matrix of the no-swizzle
 // K-major operand layout, the next brick row is 160 bytes on (the stride
 // between 8-row groups) and the next 8 channels one chunk on (the stride
@@ -14,9 +14,8 @@
 // descriptor with a different start address.  The layer's weights stay
 // resident in the same layout, [27][Cin/8][Cout][8].
 //
-// Warp-specialised persistent CTAs: warp 0 copies each brick's halo into a
-// ring of stages with cp.async (16 bytes per copy; each lane's copies arrive
-// on the stage's mbarrier when they land), warp 1 issues the 27 x Cin/16 MMAs
+// Warp-specialised persistent CTAs: warp 0 issues the TMA loads of each
+// brick's halo into a ring of stages, warp 1 issues the 27 x Cin/16 MMAs
 // (M=128, N=Cout, K=16, FP32 accumulate) into one of two TMEM accumulators
 // and commits them to mbarriers, warps 2-5 read a finished accumulator from
 // TMEM (a warp reads the 32 lanes of its quarter = 32 brick voxels), release
@@ -126,7 +125,7 @@ struct Args {
 };
 
 template <int CIN, int COUT>
-__global__ void __launch_bounds__(NTHR, 1) conv3_tc_kernel(Args a) {
+__global__ void __launch_bounds__(NTHR, 1) conv3_tc_kernel(const __grid_constant__ CUtensorMap tmx, Args a) {
   using C = Cfg<CIN, COUT>;
   constexpr int NS = C::NS;
   static_assert(COUT % 16 == 0 && COUT <= (int)ACC_COLS, "accumulator columns");
@@ -148,7 +147,7 @@ __global__ void __launch_bounds__(NTHR, 1) conv3_tc_kernel(Args a) {
   }
   cp_async_commit();
   if (tid == 0) {
-    for (int s = 0; s < NS; ++s) { bar_init(full0 + 8 * s, 32); bar_init(empty0 + 8 * s, 1); }
+    for (int s = 0; s < NS; ++s) { bar_init(full0 + 8 * s, 1); bar_init(empty0 + 8 * s, 1); }
     for (int k = 0; k < 2; ++k) { bar_init(afull0 + 8 * k, 1); bar_init(aempty0 + 8 * k, 4); }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -170,29 +169,24 @@ __global__ void __launch_bounds__(NTHR, 1) conv3_tc_kernel(Args a) {
   bool ok = true;
 
   if (warp == 0) {
-    // ---- producer warp: the halo of each brick by cp.async, 16 bytes per copy ----
-    for (int j = 0; j < nmine && ok; ++j) {
-      const int s = j % NS;
-      if (j >= NS) ok = bar_wait(empty0 + 8 * s, (uint32_t)((j / NS - 1) & 1));
-      if (!__all_sync(0xffffffffu, ok)) { ok = false; break; }
-      unsigned r = blockIdx.x + (unsigned)j * gridDim.x;
-      const int bw = (int)(r % (unsigned)nbw); r /= (unsigned)nbw;
-      const int bh = (int)(r % (unsigned)nbh); r /= (unsigned)nbh;
-      const int d = (int)(r % (unsigned)a.D), b = (int)(r / (unsigned)a.D);
-      const int h0 = bh * BH, w0 = bw * BW;
-      unsigned char* xs = smem + s * C::STAGE;
-      for (int i = lane; i < C::KC * XV; i += 32) {
-        const int hv = i % XV, kc = i / XV;
-        const int hw = hv % XW, hh = (hv / XW) % XH, hd = hv / (XW * XH);
-        const int gd = d + hd - 1, gh = h0 + hh - 1, gw = w0 + hw - 1;
-        const bool in = gd >= 0 && gd < a.D && gh >= 0 && gh < a.H && gw >= 0 && gw < a.W;
-        const bf16* src = in ? a.x + ((((size_t)b * a.D + gd) * a.H + gh) * a.W + gw) * CIN + kc * 8 : a.x;
-        cp_async16(xs + (size_t)kc * CHUNK + (size_t)hv * 16, src, in ? 16 : 0);
+    // ---- TMA producer --------------------------------------------------------
+    if (lane == 0) {
+      for (int j = 0; j < nmine && ok; ++j) {
+        const int s = j % NS;
+        if (j >= NS) ok = bar_wait(empty0 + 8 * s, (uint32_t)((j / NS - 1) & 1));
+        if (!ok) break;
+        unsigned r = blockIdx.x + (unsigned)j * gridDim.x;
+        const int bw = (int)(r % (unsigned)nbw); r /= (unsigned)nbw;
+        const int bh = (int)(r % (unsigned)nbh); r /= (unsigned)nbh;
+        const int d = (int)(r % (unsigned)a.D), b = (int)(r / (unsigned)a.D);
+        bar_expect_tx(full0 + 8 * s, (uint32_t)(C::KC * XV * 16));
+        for (int kc = 0; kc < C::KC; ++kc)
+          tma_load_5d(s0 + s * C::STAGE + kc * CHUNK, &tmx, kc * 8, bw * BW - 1, bh * BH - 1, d - 1, b, full0 + 8 * s);
       }
-      // full[s] completes when every lane's copies have landed
-      asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(full0 + 8 * s) : "memory");
+      // let the last loads land before the CTA can end
+      for (int j = nmine - NS > 0 ? nmine - NS : 0; j < nmine; ++j)
+        (void)bar_wait(full0 + 8 * (j % NS), (uint32_t)((j / NS) & 1));
     }
-    cp_async_wait<0>();   // no copy may outlive the CTA
   } else if (warp == 1) {
     // ---- MMA issuer ------------------------------------------------------------
     if (lane == 0) {
@@ -202,7 +196,6 @@ __global__ void __launch_bounds__(NTHR, 1) conv3_tc_kernel(Args a) {
         ok = bar_wait(full0 + 8 * s, (uint32_t)((j / NS) & 1));
         if (ok && j >= 2) ok = bar_wait(aempty0 + 8 * k, (uint32_t)((j / 2 - 1) & 1));
         if (!ok) break;
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // cp.async data -> tensor-core reads
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const uint32_t tacc = taddr + (uint32_t)k * ACC_COLS;
         // the start-address field counts 16-byte units: per-tap operands are
@@ -335,10 +328,23 @@ int launch(const Args& a, cudaStream_t st) {
     if (nb * (int)TMEM_COLS > 512) nb = 512 / (int)TMEM_COLS;   // TMEM of one SM
     grid = nb * nsm;
   }
+  // the activation tensor [B][D][H][W][CIN] as a 5-D TMA map (innermost first)
+  auto enc = encoder();
+  if (!enc) return TBSG_ERR_CUDA;
+  CUtensorMap tm;
+  cuuint64_t dims[5] = {(cuuint64_t)CIN, (cuuint64_t)a.W, (cuuint64_t)a.H, (cuuint64_t)a.D, (cuuint64_t)a.B};
+  cuuint64_t strides[4] = {(cuuint64_t)CIN * 2, (cuuint64_t)a.W * CIN * 2, (cuuint64_t)a.H * a.W * CIN * 2,
+                           (cuuint64_t)a.D * a.H * a.W * CIN * 2};
+  cuuint32_t box[5] = {8, (cuuint32_t)XW, (cuuint32_t)XH, (cuuint32_t)XD, 1};
+  cuuint32_t es[5] = {1, 1, 1, 1, 1};
+  if (enc(&tm, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, (void*)a.x, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+          CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) !=
+      CUDA_SUCCESS)
+    return TBSG_ERR_ARG;
   const long long nbricks = (long long)a.B * a.D * ((a.H + BH - 1) / BH) * ((a.W + BW - 1) / BW);
   if (nbricks >= (1ll << 31)) return TBSG_ERR_SHAPE;   // brick indices are 32-bit in the kernel
   const int g = (int)(nbricks < grid ? nbricks : grid);
-  conv3_tc_kernel<CIN, COUT><<<g, NTHR, C::SMEM, st>>>(a);
+  conv3_tc_kernel<CIN, COUT><<<g, NTHR, C::SMEM, st>>>(tm, a);
   return cudaGetLastError() == cudaSuccess ? TBSG_OK : TBSG_ERR_CUDA;
 }
 
