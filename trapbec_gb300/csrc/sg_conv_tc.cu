@@ -17,10 +17,9 @@
 // Warp-specialised persistent CTAs: warp 0 issues the TMA loads of each
 // brick's halo into a ring of stages, warp 1 issues the 27 x Cin/16 MMAs
 // (M=128, N=Cout, K=16, FP32 accumulate) into one of two TMEM accumulators
-// and commits them to mbarriers, and two groups of four epilogue warps (one
-// group per accumulator, so two bricks drain at once) read a finished
-// accumulator from TMEM (a warp reads the 32 lanes of its quarter = 32 brick
-// voxels), release it, and run the fused bias + skip + leaky-ReLU epilogue.  All hand-offs are
+// and commits them to mbarriers, warps 2-5 read a finished accumulator from
+// TMEM (a warp reads the 32 lanes of its quarter = 32 brick voxels), release
+// it, and run the fused bias + skip + leaky-ReLU epilogue.  All hand-offs are
 // mbarrier phases; every wait is bounded in time; TMEM is always released.
 #include <cudaTypedefs.h>
 
@@ -34,7 +33,7 @@ constexpr int BH = 16, BW = 8;                  // output brick rows (h) x colum
 constexpr int XD = 3, XH = BH + 2, XW = BW + 2;
 constexpr int XV = XD * XH * XW;                // 540 halo voxels
 constexpr int CHUNK = 8704;                     // one 8-channel chunk (540 x 16 B), padded to 128 B
-constexpr int NTHR = 320;                       // 10 warps: TMA, MMA, 2 groups of 4 epilogue warps
+constexpr int NTHR = 192;                       // 6 warps: TMA, MMA, 4 x epilogue
 constexpr uint32_t ACC_COLS = 32;               // one accumulator: 128 lanes x Cout <= 32 columns
 constexpr uint32_t TMEM_COLS = 2 * ACC_COLS;    // two accumulators
 constexpr uint64_t WAIT_NS = 2000000000ull;     // 2 s
@@ -225,15 +224,13 @@ __global__ void __launch_bounds__(NTHR, 1) conv3_tc_kernel(const __grid_constant
       }
     }
   } else {
-    // ---- epilogue: warps 2..9 in two groups of four; group g drains the
-    // bricks of accumulator g (alternate bricks), TMEM lane quarter = warp % 4
+    // ---- epilogue: warps 2..5, TMEM lane quarter = warp % 4 ----------------------
     const int quarter = warp & 3;
-    const int group = (warp - 2) >> 2;
     const int m = quarter * 32 + lane;   // brick voxel of this thread
     float bias_r[COUT];
 #pragma unroll
     for (int c = 0; c < COUT; ++c) bias_r[c] = (a.mode == 0 && a.bias) ? a.bias[c] : 0.f;
-    for (int j = group; j < nmine && ok; j += 2) {
+    for (int j = 0; j < nmine && ok; ++j) {
       const int k = j & 1;
       ok = bar_wait(afull0 + 8 * k, (uint32_t)((j / 2) & 1));
       if (!__all_sync(0xffffffffu, ok)) { ok = false; break; }
