@@ -229,6 +229,21 @@ def warmstart_leg(args):
     }
 
 
+def aggregate_ranks(ms_local, units_local, dist, device):
+    """Whole-job figure of N replica ranks: the slowest rank's timed milliseconds
+    (max over ranks) and the units all ranks processed in that time."""
+    import torch
+    t = torch.tensor([ms_local, float(units_local)], dtype=torch.float64, device=device)
+    if dist is not None:
+        mx = t[:1].clone()
+        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+        tot = t[1:].clone()
+        dist.all_reduce(tot, op=dist.ReduceOp.SUM)
+        t = torch.cat([mx, tot])
+    ms = float(t[0].item())
+    return ms, float(t[1].item()) / (ms * 1e-3)
+
+
 def run_gpu_arm(args):
     import numpy as np
     import torch
@@ -277,12 +292,8 @@ def run_gpu_arm(args):
     if dist:
         dist.barrier()
     d1 = s.diag()
-    ms_t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-    if dist:
-        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
-    ms = float(ms_t.item())
     cells = n ** 3
-    value = world * cells * args.steps / (ms * 1e-3)
+    ms, value = aggregate_ranks(ms, cells * args.steps, dist, "cuda")
     peak, peak_kind = load_peaks()
     bpc = 80.0 if prec == abi.FP32 else 160.0   # algorithmic bytes per grid point per RK3 step
     achieved = cells * args.steps * bpc / (ms * 1e-3) / 1e9
