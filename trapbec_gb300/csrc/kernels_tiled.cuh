@@ -40,12 +40,15 @@ template <typename T> struct PK;
 template <> struct PK<float> {
   using V = float2;
   static __device__ __forceinline__ V add(V a, V b) { return __fadd2_rn(a, b); }
+  // a - b as one packed FMA (-1 * b is exact, so the result is the rounded difference)
+  static __device__ __forceinline__ V sub(V a, V b) { return __ffma2_rn(make_float2(-1.f, -1.f), b, a); }
   static __device__ __forceinline__ V mul(V a, V b) { return __fmul2_rn(a, b); }
   static __device__ __forceinline__ V fma(V a, V b, V c) { return __ffma2_rn(a, b, c); }
 };
 template <> struct PK<double> {
   using V = double2;
   static __device__ __forceinline__ V add(V a, V b) { return make_double2(a.x + b.x, a.y + b.y); }
+  static __device__ __forceinline__ V sub(V a, V b) { return make_double2(a.x - b.x, a.y - b.y); }
   static __device__ __forceinline__ V mul(V a, V b) { return make_double2(a.x * b.x, a.y * b.y); }
   static __device__ __forceinline__ V fma(V a, V b, V c) {
     return make_double2(::fma(a.x, b.x, c.x), ::fma(a.y, b.y, c.y));
@@ -481,21 +484,21 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
         V fr = mk<T>((T)0, (T)0);
         if (PLAIN || a.frame_mode != FRAME_NONE) {
           // D1 without 1/(60h): (v3 - v-3) - 9 (v2 - v-2) + 45 (v1 - v-1)
-          V dx = P::add(xp3, neg(xm3));
-          dx = P::fma(ta.k[10], P::add(xp2, neg(xm2)), dx);
-          dx = P::fma(ta.k[11], P::add(xp1, neg(xm1)), dx);
+          V dx = P::sub(xp3, xm3);
+          dx = P::fma(ta.k[10], P::sub(xp2, xm2), dx);
+          dx = P::fma(ta.k[11], P::sub(xp1, xm1), dx);
           V zc;
           if (rot) {
-            V dy = P::add(yp3, neg(ym3));
-            dy = P::fma(ta.k[10], P::add(yp2, neg(ym2)), dy);
-            dy = P::fma(ta.k[11], P::add(yp1, neg(ym1)), dy);
+            V dy = P::sub(yp3, ym3);
+            dy = P::fma(ta.k[10], P::sub(yp2, ym2), dy);
+            dy = P::fma(ta.k[11], P::sub(yp1, ym1), dy);
             // Z = x D1y - y D1x with the 1/(60h) factors folded into x and y
             zc = P::fma(myv1[r], dx, P::mul(xv1, dy));
           } else {
             zc = P::mul(splat<T>(a.ix1), dx);
           }
           // (0, omega) * Z = (-omega Z.im, omega Z.re), on the renormalised state
-          fr = mk<T>(-oms * zc.y, oms * zc.x);
+          fr = P::mul(mk<T>(zc.y, zc.x), mk<T>(-oms, oms));
         }
         V c = craw;
         if (!PLAIN) {   // everything above is linear in psi: apply the load factor once
