@@ -39,10 +39,16 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
-def profile_traffic(prec_tag: str):
+def profile_traffic(prec_tag: str, tz: int | None = None, ty: int | None = None):
     """DRAM bytes per grid point per stage launch from the committed ncu summary
-    of the full-size launch list (profiles/stage_tiled_<prec>_512.txt)."""
-    path = os.path.join(HERE, "profiles", f"stage_tiled_{prec_tag}_512.txt")
+    of the full-size launch list of the tile shape that ran
+    (profiles/stage_tiled_<prec>_512_<tz>x<ty>.txt; the 128 x 8 FP32 default is
+    profiles/stage_tiled_fp32_512.txt)."""
+    path = os.path.join(HERE, "profiles", f"stage_tiled_{prec_tag}_512_{tz}x{ty}.txt")
+    if not os.path.exists(path):
+        if (prec_tag, tz, ty) not in (("fp32", 128, 8), ("fp32", None, None)):
+            return None
+        path = os.path.join(HERE, "profiles", f"stage_tiled_{prec_tag}_512.txt")
     if not os.path.exists(path):
         return None
     m = re.search(r"dram_bytes_per_point_per_launch:\s*([0-9.eE+-]+)", open(path).read())
@@ -298,7 +304,7 @@ def run_gpu_arm(args):
     bpc = 80.0 if prec == abi.FP32 else 160.0   # algorithmic bytes per grid point per RK3 step
     achieved = cells * args.steps * bpc / (ms * 1e-3) / 1e9
     tag = "fp32" if prec == abi.FP32 else "fp64"
-    tpp = profile_traffic(tag)
+    tpp = profile_traffic(tag, tune["tile_z"] if tune else None, tune["tile_y"] if tune else None)
     traffic = tpp * cells if tpp else None
 
     kernel_name = "tiled TMA stage kernel" if args.kernel is None or args.kernel[0] != 1 else "per-cell stage kernel"
