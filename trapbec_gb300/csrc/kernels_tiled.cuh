@@ -471,33 +471,16 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
         const V ym3 = yc[r], ym2 = yc[r + 1], ym1 = yc[r + 2];
         const V yp1 = yc[r + 4], yp2 = yc[r + 5], yp3 = yc[r + 6];
         const V* zr = col + r * TZP;
-        V lap;
-        if constexpr (sizeof(T) == 4) {
-          // FP32: three independent axis sums keep the dependent chains short
-          // (the stage kernels are issue-bound, not FMA-bound)
-          V lx = P::fma(ta.k[0], P::add(xm3, xp3), P::mul(ta.k[9], craw));
-          lx = P::fma(ta.k[1], P::add(xm2, xp2), lx);
-          lx = P::fma(ta.k[2], P::add(xm1, xp1), lx);
-          V ly = P::mul(ta.k[3], P::add(ym3, yp3));
-          ly = P::fma(ta.k[4], P::add(ym2, yp2), ly);
-          ly = P::fma(ta.k[5], P::add(ym1, yp1), ly);
-          V lzz = P::mul(ta.k[6], P::add(zr[-3], zr[3]));
-          lzz = P::fma(ta.k[7], P::add(zr[-2], zr[2]), lzz);
-          lzz = P::fma(ta.k[8], P::add(zr[-1], zr[1]), lzz);
-          lap = P::add(lx, P::add(ly, lzz));
-        } else {
-          // FP64 is bound by its pipe: the shortest operation count
-          lap = P::mul(ta.k[9], craw);
-          lap = P::fma(ta.k[0], P::add(xm3, xp3), lap);
-          lap = P::fma(ta.k[1], P::add(xm2, xp2), lap);
-          lap = P::fma(ta.k[2], P::add(xm1, xp1), lap);
-          lap = P::fma(ta.k[3], P::add(ym3, yp3), lap);
-          lap = P::fma(ta.k[4], P::add(ym2, yp2), lap);
-          lap = P::fma(ta.k[5], P::add(ym1, yp1), lap);
-          lap = P::fma(ta.k[6], P::add(zr[-3], zr[3]), lap);
-          lap = P::fma(ta.k[7], P::add(zr[-2], zr[2]), lap);
-          lap = P::fma(ta.k[8], P::add(zr[-1], zr[1]), lap);
-        }
+        V lap = P::mul(ta.k[9], craw);
+        lap = P::fma(ta.k[0], P::add(xm3, xp3), lap);
+        lap = P::fma(ta.k[1], P::add(xm2, xp2), lap);
+        lap = P::fma(ta.k[2], P::add(xm1, xp1), lap);
+        lap = P::fma(ta.k[3], P::add(ym3, yp3), lap);
+        lap = P::fma(ta.k[4], P::add(ym2, yp2), lap);
+        lap = P::fma(ta.k[5], P::add(ym1, yp1), lap);
+        lap = P::fma(ta.k[6], P::add(zr[-3], zr[3]), lap);
+        lap = P::fma(ta.k[7], P::add(zr[-2], zr[2]), lap);
+        lap = P::fma(ta.k[8], P::add(zr[-1], zr[1]), lap);
         V fr = mk<T>((T)0, (T)0);
         if (PLAIN || a.frame_mode != FRAME_NONE) {
           // D1 without 1/(60h): (v3 - v-3) - 9 (v2 - v-2) + 45 (v1 - v-1)
