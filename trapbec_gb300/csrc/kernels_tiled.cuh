@@ -197,6 +197,8 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
   using V = c_t<T>;
   constexpr int HZ = G::HZ, TZP = G::TZP, S = G::S, NT = G::NT;
   constexpr bool READS_W = (KIND == ST_S2 || KIND == ST_S3);
+  // the queue preload waits for planes xa-3 .. xa+2, all issued before it
+  static_assert(S >= 6, "the ring needs at least 6 slots");
 
   extern __shared__ __align__(128) unsigned char smem_raw[];
   V* ring = reinterpret_cast<V*>(smem_raw);
