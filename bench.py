@@ -39,12 +39,20 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
-def profile_traffic(prec_tag: str, tz: int | None = None, ty: int | None = None):
+def profile_traffic(prec_tag: str, tz: int | None = None, ty: int | None = None, deferred: bool = False):
     """DRAM bytes per grid point per stage launch from the committed ncu summary
-    of the full-size launch list of the tile shape that ran
-    (profiles/stage_tiled_<prec>_512_<tz>x<ty>.txt; the 128 x 8 FP32 default is
-    profiles/stage_tiled_fp32_512.txt)."""
-    path = os.path.join(HERE, "profiles", f"stage_tiled_{prec_tag}_512_{tz}x{ty}.txt")
+    of the full-size launch list of the tile shape and RK3 form that ran
+    (profiles/stage_tiled_<prec>_512_<tz>x<ty>[_deferred].txt; the 128 x 8 FP32
+    three-stage default is profiles/stage_tiled_fp32_512.txt)."""
+    if tz is None and ty is None:
+        tz, ty = 128, 8
+    sfx = "_deferred" if deferred else ""
+    path = os.path.join(HERE, "profiles", f"stage_tiled_{prec_tag}_512_{tz}x{ty}{sfx}.txt")
+    if deferred:
+        if not os.path.exists(path):
+            return None
+        m = re.search(r"dram_bytes_per_point_per_launch:\s*([0-9.eE+-]+)", open(path).read())
+        return float(m.group(1)) if m else None
     if not os.path.exists(path):
         if (prec_tag, tz, ty) not in (("fp32", 128, 8), ("fp32", None, None)):
             return None
@@ -271,6 +279,7 @@ def run_gpu_arm(args):
     s = Solver(p)
     if args.kernel:
         s.set_kernel(*args.kernel)
+    s.set_stage_form(args.stage_form)
     tune = None
     if args.kernel is None and not args.no_autotune:
         tune = s.autotune(steps=8)   # tile shape and work order for this grid (state restored)
@@ -301,10 +310,14 @@ def run_gpu_arm(args):
     cells = n ** 3
     ms, value = aggregate_ranks(ms, cells * args.steps, dist, "cuda")
     peak, peak_kind = load_peaks()
-    bpc = 80.0 if prec == abi.FP32 else 160.0   # algorithmic bytes per grid point per RK3 step
+    # algorithmic bytes per grid point per RK3 step: S1 24 + S2 32 + S3 24 (complex FP32);
+    # the deferred form stores no psi1 (S1 16 B); FP64 doubles every figure
+    deferred = s.stage_form_deferred()
+    bpc = (72.0 if deferred else 80.0) if prec == abi.FP32 else 160.0
     achieved = cells * args.steps * bpc / (ms * 1e-3) / 1e9
     tag = "fp32" if prec == abi.FP32 else "fp64"
-    tpp = profile_traffic(tag, tune["tile_z"] if tune else None, tune["tile_y"] if tune else None)
+    tz_run, ty_run = s.tile_shape(real_time=True)
+    tpp = profile_traffic(tag, tz_run, ty_run, deferred)
     traffic = tpp * cells if tpp else None
 
     kernel_name = "tiled TMA stage kernel" if args.kernel is None or args.kernel[0] != 1 else "per-cell stage kernel"
@@ -372,7 +385,9 @@ def run_gpu_arm(args):
                    "omega_ramp": "0 -> 0.8 omega_perp over 5000 steps, updated every chunk",
                    "chunk_steps": chunk, "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2_flush": "inputs larger than L2 (1 GiB per array)",
-                   "kernel": kernel_name, "autotune": tune},
+                   "kernel": kernel_name, "tile": [tz_run, ty_run], "autotune": tune,
+                   "rk3_form": ("deferred psi1: stage 1 stores w1 only, stage 2 forms psi1 = psi0 + w1/3 "
+                                "(bit-identical)") if deferred else "three full stages"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                      "algorithmic_bytes_per_point_step": bpc,
@@ -414,6 +429,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--kernel", type=int, nargs=3, default=None, metavar=("KIND", "TZ", "TY"))
     ap.add_argument("--no-autotune", action="store_true", help="keep the default tile shape and work order")
+    ap.add_argument("--stage-form", type=int, default=0, choices=[0, 1],
+                    help="real-time RK3 form: 0 three full stages, 1 deferred psi1 (stage 1 stores w1 only)")
     ap.add_argument("--imag", action="store_true", help="add the batched imaginary-time leg")
     ap.add_argument("--imag-count", type=int, default=16)
     ap.add_argument("--imag-seed", type=int, default=3)

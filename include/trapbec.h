@@ -253,20 +253,44 @@ int trapbec_get_scalar(trapbec_ctx* ctx, int which, double* value);
 
 /* Select the stage kernel: 0 = automatic (tiled TMA kernel where the grid
  * allows it), 1 = simple per-cell kernel, 2 = tiled kernel (error if the
- * grid does not allow it).  tile_z/tile_y pick a built tile shape (0, 0:
- * the default shape; tile_z = -(i+1): built shape number i).              */
+ * grid does not allow it).  tile_z/tile_y pick a built tile shape for every
+ * launch (tile_z = -(i+1): built shape number i); 0, 0 restores the defaults:
+ * shape 0 for reductions and imaginary time, the real-time shape (64 x 32
+ * tiles in FP32) for the plain real-time stages.                           */
 int trapbec_set_kernel(trapbec_ctx* ctx, int kind, int tile_z, int tile_y);
+
+/* Tile shape the tiled kernel runs with: of the plain real-time stages
+ * (real_time = 1) or of every other launch (real_time = 0).  0, 0 when those
+ * launches use the per-cell kernel.                                         */
+int trapbec_get_tile_shape(trapbec_ctx* ctx, int real_time, int* tile_z, int* tile_y);
 
 /* Work order of the tiled kernel: x-planes per chunk (0 = automatic).  Tiles
  * adjacent in y are processed chunk by chunk so their shared ghost rows are
  * served from L2.                                                          */
 int trapbec_set_chunk(trapbec_ctx* ctx, int chunk);
 
-/* Autotune the tiled kernel for this grid: time every built tile shape and a
- * few chunk lengths over `steps` RK3 steps each on the current state (which
- * is saved and restored), keep the fastest.  *tile_z, *tile_y, *chunk (may
- * be NULL) receive the choice, *ms_per_step its time.  Results are cached
- * per process for identical grids.                                         */
+/* Form of the real-time RK3 step (run.f90:42-57) on the tiled FP32 kernel.
+ * TRAPBEC_RK3_THREE_STAGE (default): three full stages, each storing w and psi.
+ * TRAPBEC_RK3_DEFERRED: stage 1 stores w1 only and stage 2 forms
+ *   psi1 = psi0 + w1/3 from ghosted boxes of psi0 and w1 with the same FMA,
+ *   writing w2 to a second w buffer (allocated by this call): 72 instead of
+ *   80 bytes of HBM traffic per grid point and step, bit-identical results.
+ *   It applies on tile shapes whose shared memory holds both boxes and where
+ *   the plain stage variant runs (harmonic or no potential, rotation or no
+ *   frame term); elsewhere the step keeps three stages.  On GB300 it measured
+ *   slower than three stages on the best tile shape.
+ * trapbec_get_stage_form: *deferred = 1 when the next trapbec_step_rt takes
+ * the deferred form.                                                        */
+enum trapbec_rk3_form { TRAPBEC_RK3_THREE_STAGE = 0, TRAPBEC_RK3_DEFERRED = 1 };
+int trapbec_set_stage_form(trapbec_ctx* ctx, int form);
+int trapbec_get_stage_form(trapbec_ctx* ctx, int* deferred);
+
+/* Autotune the tiled kernel of the real-time stages for this grid: time every
+ * built tile shape and a few chunk lengths over `steps` RK3 steps each on the
+ * current state (which is saved and restored), keep the fastest for the plain
+ * real-time stages (reductions and imaginary time keep their shape).
+ * *tile_z, *tile_y, *chunk (may be NULL) receive the choice, *ms_per_step its
+ * time.  Results are cached per process for identical grids.               */
 int trapbec_autotune(trapbec_ctx* ctx, int steps, int* tile_z, int* tile_y, int* chunk, double* ms_per_step);
 
 /* Kernels launched by this context since creation (for launch accounting). */

@@ -9,8 +9,9 @@ from tests.helpers import params, smooth_state, rel_err
 
 pytestmark = pytest.mark.gpu
 
-# built shapes by index (FP32: (128,8), (64,8), (64,16), (64,8) with 6 slots / 3 CTAs per SM)
-SHAPES = {abi.FP32: [(128, 8, 0), (64, 8, 1), (64, 16, 2), (64, 8, 3)], abi.FP64: [(32, 8, 0), (64, 8, 1)]}
+# built shapes by index (FP32: (128,8), (64,8), (64,16), (64,8) with 6 slots / 3 CTAs per SM, (64,32) with 4 rows per thread)
+SHAPES = {abi.FP32: [(128, 8, 0), (64, 8, 1), (64, 16, 2), (64, 8, 3), (64, 32, 4)],
+          abi.FP64: [(32, 8, 0), (64, 8, 1)]}
 
 
 def _grid_for(tz, ty, bc, zper):
@@ -108,3 +109,91 @@ def test_tiled_imag_rk3(prec):
         assert np.linalg.norm(a - b) / np.linalg.norm(b) < 1e-5
         assert abs(d["energy"] - do["energy"]) < 1e-5 * abs(do["energy"])
     assert abs(d["norm"] / do["norm"] - 1) < (1e-12 if prec == abi.FP64 else 1e-6)
+
+
+DEFER_CASES = [(shp, bc, zper) for shp in SHAPES[abi.FP32]
+               for bc, zper in ((abi.BC_ZERO, 0), (abi.BC_SOLID, 0), (abi.BC_PERIODIC, 0), (abi.BC_ZERO, 1))]
+DEFER_SHAPES = (0, 1, 2)   # shapes whose shared memory holds the deferred stage's two boxes per slot
+
+
+@pytest.mark.parametrize("shape,bc,zper", DEFER_CASES, ids=lambda v: str(v))
+def test_deferred_form_bitwise_equals_three_stages(shape, bc, zper):
+    """The deferred real-time form (stage 1 stores w1 only, stage 2 forms
+    psi1 = psi0 + w1/3 from ghosted boxes of psi0 and w1) gives the same bits
+    as three full stages, including the ghost fix-ups of boundary tiles."""
+    tz, ty, idx = shape
+    n = _grid_for(tz, ty, bc, zper)
+    p = params(n=n, L=(0.5 * n[0], 0.5 * n[1], 0.5 * n[2]), prec=abi.FP32, bc=bc, periodicz=zper, pot="harmonic",
+               harm=(40.0, 50.0, 60.0), omega=0.35, dt=0.01)
+    psi = smooth_state(p, seed=31)
+    out = []
+    for form in (abi.RK3_DEFERRED, abi.RK3_THREE_STAGE):
+        s = Solver(p)
+        s.set_kernel(2, -(idx + 1), 0)
+        s.set_stage_form(form)
+        assert s.stage_form_deferred() == (form == abi.RK3_DEFERRED and idx in DEFER_SHAPES)
+        s.set_psi(psi)
+        s.step_rt(7)
+        out.append(s.get_psi())
+        s.close()
+    assert np.array_equal(out[0].view(np.uint32), out[1].view(np.uint32))
+
+
+def test_deferred_form_partial_tiles_and_long_run():
+    """Partial tiles (zero ghosts from the TMA fill) and many steps, so both w
+    buffers are reused across steps."""
+    n = (9, 13, 70)
+    p = params(n=n, L=(4.5, 6.5, 35.0), prec=abi.FP32, pot="harmonic", harm=(3.0, 4.0, 5.0), omega=0.2, dt=0.01)
+    psi = smooth_state(p, seed=6)
+    out = []
+    for form in (abi.RK3_DEFERRED, abi.RK3_THREE_STAGE):
+        s = Solver(p)
+        s.set_kernel(2, -1, 0)
+        s.set_stage_form(form)
+        assert s.stage_form_deferred() == (form == abi.RK3_DEFERRED)
+        s.set_psi(psi)
+        s.step_rt(40)
+        out.append(s.get_psi())
+    assert np.array_equal(out[0].view(np.uint32), out[1].view(np.uint32))
+
+
+def test_deferred_form_applicability():
+    """Three stages by default; deferred only on request, where the plain FP32
+    tiled stages run on a shape that holds its boxes."""
+    n = (12, 32, 128)
+    base = dict(n=n, L=(6.0, 16.0, 64.0), pot="harmonic", harm=(3.0, 4.0, 5.0), dt=0.01)
+    s = Solver(params(prec=abi.FP32, omega=0.2, **base))
+    assert not s.stage_form_deferred()
+    s.set_stage_form(abi.RK3_DEFERRED)
+    assert not s.stage_form_deferred()   # the default real-time shape (64 x 32) cannot hold both boxes
+    s.set_kernel(2, -1, 0)               # shape 0 for every launch
+    assert s.stage_form_deferred()
+    s.set_kernel(1)                      # per-cell kernel
+    assert not s.stage_form_deferred()
+    s.close()
+    s = Solver(params(prec=abi.FP64, **base))
+    s.set_stage_form(abi.RK3_DEFERRED)
+    assert not s.stage_form_deferred()
+    s = Solver(params(prec=abi.FP32, vx=0.1, **base))
+    s.set_stage_form(abi.RK3_DEFERRED)
+    s.set_kernel(2, -1, 0)
+    assert not s.stage_form_deferred()   # advective frame: general variant
+
+
+def test_real_time_shape_equals_general_shape():
+    """The default plan split (64 x 32 tiles for the plain real-time stages,
+    shape 0 for the rest) against shape 0 everywhere: same bits."""
+    n = (20, 64, 128)
+    p = params(n=n, L=(10.0, 32.0, 64.0), prec=abi.FP32, bc=abi.BC_SOLID, pot="harmonic", harm=(3.0, 4.0, 5.0),
+               omega=0.3, dt=0.01)
+    psi = smooth_state(p, seed=12)
+    out = []
+    for explicit in (False, True):
+        s = Solver(p)
+        if explicit:
+            s.set_kernel(2, -1, 0)
+        s.set_psi(psi)
+        s.step_rt(9)
+        out.append((s.get_psi(), s.diag()["energy"]))
+    assert np.array_equal(out[0][0].view(np.uint32), out[1][0].view(np.uint32))
+    assert out[0][1] == out[1][1]

@@ -33,6 +33,7 @@ FP32, FP64 = 0, 1
 LAYOUT_INTERIOR, LAYOUT_GHOSTED = 0, 1
 FIELD_VELOCITY, FIELD_QPRESSURE = 0, 1
 IMAG_REF_EULER, IMAG_RK3_RENORM = 0, 1
+RK3_THREE_STAGE, RK3_DEFERRED = 0, 1
 
 SCALAR_OMEGA_Z, SCALAR_DT_RE, SCALAR_DT_IM, SCALAR_GAMMA = 0, 1, 2, 3
 SCALAR_T, SCALAR_ADVECTIVE_VX, SCALAR_NORM_TARGET = 4, 5, 6
@@ -142,6 +143,9 @@ _PROTOS = {
     "trapbec_get_scalar": (C.c_int, [_VP, C.c_int, C.POINTER(C.c_double)]),
     "trapbec_set_kernel": (C.c_int, [_VP, C.c_int, C.c_int, C.c_int]),
     "trapbec_set_chunk": (C.c_int, [_VP, C.c_int]),
+    "trapbec_set_stage_form": (C.c_int, [_VP, C.c_int]),
+    "trapbec_get_tile_shape": (C.c_int, [_VP, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "trapbec_get_stage_form": (C.c_int, [_VP, C.POINTER(C.c_int)]),
     "trapbec_autotune": (C.c_int, [_VP, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
                                    C.POINTER(C.c_double)]),
     "trapbec_launch_count": (C.c_int, [_VP, C.POINTER(C.c_int64)]),

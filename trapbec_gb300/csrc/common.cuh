@@ -26,7 +26,12 @@ enum FrameMode : int { FRAME_NONE = 0, FRAME_ROT = 1, FRAME_ADV = 2 };
 //   S3: w = A*w + c*rhs,      psi' = psi + B*w, w not stored (run.f90:52-54)
 //   EU: psi' = psi + c*rhs,   no w                           (run.f90:22)
 //   DIAG: no update, no writes; reductions of the energy set only
-enum StageKind : int { ST_S1 = 0, ST_S2 = 1, ST_S3 = 2, ST_EU = 3, ST_DIAG = 4 };
+// The deferred real-time form (tiled FP32 kernel, plain stages) splits the
+// psi' = psi + B1*w1 of S1 into the next stage, which forms it on the fly:
+//   S1W: w1 = c*rhs(psi0), only w1 stored
+//   S2D: psi1 = psi0 + B1*w1 (same FMA as S1), then S2 from psi1; w2 goes to
+//        a second w buffer because w1 is read with its ghost frame
+enum StageKind : int { ST_S1 = 0, ST_S2 = 1, ST_S3 = 2, ST_EU = 3, ST_DIAG = 4, ST_S1W = 5, ST_S2D = 6 };
 
 // Number of FP64 quantities a stage kernel may reduce (fused reductions).
 //   0: sum|psi|^2  1: sum Re psi* lap  2: sum pot|psi|^2  3: sum |psi|^4
@@ -78,6 +83,8 @@ template <typename T> struct StageArgs {
   T scale;                    // factor applied to psi_in on load (renormalisation)
   ImagCtrl* ctrl;             // imaginary-time control block (may be null)
   int use_ctrl_scale;         // take the load factor from ctrl->scale
+  const c_t<T>* __restrict__ w_in;  // S2D: w1 (ghost fix-ups read it); w receives w2
+  T B1;                       // S2D: B of stage 1 (psi1 = psi0 + B1*w1)
 };
 
 // Stage prologue: a converged imaginary-time loop turns stages into no-ops;

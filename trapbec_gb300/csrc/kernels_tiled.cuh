@@ -118,8 +118,9 @@ template <typename T> struct TiledArgs {
   // Packed coefficients, formed on the host so the kernel can take them from
   // the parameter (constant) bank instead of holding them in registers:
   // 0-2: (2,-27,270)/(180 hx^2), 3-5: y, 6-8: z, 9: -490*sum(1/(180 h^2)),
-  // 10: -9, 11: 45, 12: (c_re, c_re), 13: (-c_im, c_im), 14: (A, A), 15: (B, B)
-  c_t<T> k[16];
+  // 10: -9, 11: 45, 12: (c_re, c_re), 13: (-c_im, c_im), 14: (A, A), 15: (B, B),
+  // 16: (B1, B1) (deferred S2)
+  c_t<T> k[17];
 };
 
 // Float-float (FP32) or Neumaier (FP64) running sums for the fused reductions.
@@ -163,6 +164,19 @@ template <typename T, int TZ, int TY, int R, int NSLOT = 8, int MINB = 0> struct
   static constexpr int MIN_BLOCKS = MINB > 0 ? MINB : ((sizeof(T) == 4 && NT < 512) ? 2 : 1);
 };
 
+// Ring of one stage kind.  The deferred S2 holds a ghosted w1 box beside the
+// psi box in every slot, with as many slots as fit in the shared memory the
+// other kinds use (at least 6), so all kinds keep the same CTAs per SM.
+template <typename T, class G, int KIND> struct KindGeom {
+  static constexpr bool DEFER = (KIND == ST_S2D);
+  static constexpr int W_BYTES = DEFER ? G::SLOT_BYTES : G::W_BYTES;
+  static constexpr int SLOT_STRIDE = DEFER ? (G::W_OFF + G::SLOT_BYTES + 127) / 128 * 128 : G::SLOT_STRIDE;
+  static constexpr int SLOT_STRIDE_ELEMS = SLOT_STRIDE / (int)sizeof(c_t<T>);
+  static constexpr int FIT = (G::S * G::SLOT_STRIDE) / SLOT_STRIDE;
+  static constexpr int S = DEFER ? (FIT < 6 ? 6 : (FIT > G::S ? G::S : FIT)) : G::S;
+  static constexpr int SMEM = S * SLOT_STRIDE + (S + 1) * 8;
+};
+
 // Work description of a batched launch: the concatenated units of all active
 // instances, each instance's arguments and tensor maps in a device table.
 template <typename T> struct InstDesc {
@@ -193,16 +207,18 @@ __global__ void __launch_bounds__(TileGeom<T, TZ, TY, R, NSLOT, MINB>::NT, TileG
 stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constant__ CUtensorMap tmw0,
                    const __grid_constant__ TiledArgs<T> ta0, const __grid_constant__ BatchArgs ba) {
   using G = TileGeom<T, TZ, TY, R, NSLOT, MINB>;
+  using K = KindGeom<T, G, KIND>;
   using P = PK<T>;
   using V = c_t<T>;
-  constexpr int HZ = G::HZ, TZP = G::TZP, S = G::S, NT = G::NT;
-  constexpr bool READS_W = (KIND == ST_S2 || KIND == ST_S3);
+  constexpr int HZ = G::HZ, TZP = G::TZP, S = K::S, NT = G::NT;
+  constexpr bool READS_W = (KIND == ST_S2 || KIND == ST_S3 || KIND == ST_S2D);
+  static_assert(!K::DEFER || PLAIN, "the deferred stage has a plain variant only");
   // the queue preload waits for planes xa-3 .. xa+2, all issued before it
   static_assert(S >= 6, "the ring needs at least 6 slots");
 
   extern __shared__ __align__(128) unsigned char smem_raw[];
   V* ring = reinterpret_cast<V*>(smem_raw);
-  uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + S * G::SLOT_STRIDE);   // S slots + 1 never-completed
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + S * K::SLOT_STRIDE);   // S slots + 1 never-completed
 
   const int tid = threadIdx.x;
   const int lz = tid % TZ;
@@ -343,16 +359,18 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
     const T pzv = (zok && harm) ? a.pz[gz] : (T)0;
 
     // One ring slot = the psi box of plane p and, for stages that read w,
-    // the w tile of plane p (only planes this segment stores).
+    // the w tile of plane p (only planes this segment stores); the deferred
+    // S2 loads the ghosted w1 box of every plane instead.
     auto issue = [&](int p) {
       const uint32_t sq = seq_issue++;
       const int sl = sq % S;
-      const bool with_w = READS_W && p >= xa && p < xb;
-      V* dst = ring + (size_t)sl * G::SLOT_STRIDE_ELEMS;
+      const bool with_w = K::DEFER || (READS_W && p >= xa && p < xb);
+      V* dst = ring + (size_t)sl * K::SLOT_STRIDE_ELEMS;
       fence_proxy_async();
-      mbar_expect_tx(&bars[sl], G::SLOT_BYTES + (with_w ? G::W_BYTES : 0));
+      mbar_expect_tx(&bars[sl], G::SLOT_BYTES + (with_w ? K::W_BYTES : 0));
       tma_load_3d(dst, tmp, c0, y0 - 3, plane_src(p), &bars[sl]);
-      if (with_w) tma_load_3d(dst + G::W_OFF_ELEMS, tmwp, cw, y0, p, &bars[sl]);
+      if (K::DEFER) tma_load_3d(dst + G::W_OFF_ELEMS, tmwp, c0, y0 - 3, plane_src(p), &bars[sl]);
+      else if (with_w) tma_load_3d(dst + G::W_OFF_ELEMS, tmwp, cw, y0, p, &bars[sl]);
     };
     if (tid == 0) {
       seq_issue = base;
@@ -371,7 +389,7 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
     // Patch the y/z ghost cells of a boundary tile's slot from global memory
     // (solid mirror or periodic wrap; zero where map_ghost says so).
     auto fixup = [&](uint32_t sq, int p) {
-      V* sl = ring + (size_t)(sq % S) * G::SLOT_STRIDE_ELEMS;
+      V* sl = ring + (size_t)(sq % S) * K::SLOT_STRIDE_ELEMS;
       const int xp = plane_src(p);
       if (xp < 0 || xp >= nx) return;  // zero plane
       const size_t plane = (size_t)xp * ny;
@@ -404,15 +422,82 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
     // register queue: at plane x, q[(x - xa + j) % 7][r] holds plane x - 3 + j
     V q[7][R];
     const int qoff = (yg * R + 3) * TZP + lz + HZ;   // first cell of this thread in a slot
+
+    // Deferred S2: psi1 = psi0 + B1*w1 (the FMA stage 1 would have stored)
+    // into the psi box of slot sq (plane p): this thread's own centre cells,
+    // returned in v[], and, for a plane that will be a centre plane, its share
+    // of the y and z ghost cells.  Ghost cells of boundary tiles come from
+    // global psi0 and w1 as in fixup().  Every cell is formed by one thread
+    // and read by others only after the __syncthreads() that ends the plane.
+    auto prepare = [&](uint32_t sq, int p, bool ghosts, V* v) {
+      V* sl = ring + (size_t)(sq % S) * K::SLOT_STRIDE_ELEMS;
+      const V* swb = sl + G::W_OFF_ELEMS;
+      const V kb = ta.k[16];
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const int cell = qoff + r * TZP;
+        v[r] = P::fma(kb, swb[cell], sl[cell]);
+        sl[cell] = v[r];
+      }
+      if (!ghosts) return;
+      const int xp = plane_src(p);
+      const bool zplane = xp < 0 || xp >= nx;   // zero plane: both boxes came back zero
+      const size_t plane = (size_t)(zplane ? 0 : xp) * ny;
+      for (int e = tid; e < 6 * TZ; e += NT) {
+        const int rr = e / TZ, cz = e % TZ;
+        const int ry = rr < 3 ? rr - 3 : TY + rr - 3;
+        const int cell = (ry + 3) * TZP + cz + HZ;
+        const int gy = y0 + ry, gzz = z0 + cz;
+        V val;
+        if (bnd_y && !zplane && !(gy >= 0 && gy < ny) && gzz < nz) {
+          const int my = map_ghost(gy, ny, a.bc);
+          val = mk<T>((T)0, (T)0);
+          if (my >= 0) {
+            const size_t gi = (plane + my) * nz + gzz;
+            val = P::fma(kb, a.w_in[gi], a.psi_in[gi]);
+          }
+        } else {
+          val = P::fma(kb, swb[cell], sl[cell]);
+        }
+        sl[cell] = val;
+      }
+      for (int e = tid; e < 6 * TY; e += NT) {
+        const int ry = e / 6, m = e % 6;
+        const int cz = m < 3 ? m - 3 : TZ + m - 3;
+        const int cell = (ry + 3) * TZP + cz + HZ;
+        const int gy = y0 + ry, gzz = z0 + cz;
+        V val;
+        if (bnd_z && !zplane && !(gzz >= 0 && gzz < nz) && gy < ny) {
+          const int mz = map_ghost(gzz, nz, ta.bcz);
+          val = mk<T>((T)0, (T)0);
+          if (mz >= 0) {
+            const size_t gi = (plane + gy) * nz + mz;
+            val = P::fma(kb, a.w_in[gi], a.psi_in[gi]);
+          }
+        } else {
+          val = P::fma(kb, swb[cell], sl[cell]);
+        }
+        sl[cell] = val;
+      }
+    };
 #pragma unroll
     for (int j = 0; j < 6; ++j) {
       const uint32_t sq = base + j;
       wait_plane(sq);
-      if (j >= 3 && (bnd_y || bnd_z)) fixup(sq, xa - 3 + j);
-      const V* sl = ring + (size_t)(sq % S) * G::SLOT_STRIDE_ELEMS;
+      if (K::DEFER) {
+        V v[R];
+        prepare(sq, xa - 3 + j, j >= 3, v);
 #pragma unroll
-      for (int r = 0; r < R; ++r) q[j][r] = sl[qoff + r * TZP];
+        for (int r = 0; r < R; ++r) q[j][r] = v[r];
+      } else {
+        if (j >= 3 && (bnd_y || bnd_z)) fixup(sq, xa - 3 + j);
+        const V* sl = ring + (size_t)(sq % S) * K::SLOT_STRIDE_ELEMS;
+#pragma unroll
+        for (int r = 0; r < R; ++r) q[j][r] = sl[qoff + r * TZP];
+      }
     }
+    // generic-proxy writes of prepare() before the ring's next TMA writes
+    if (K::DEFER) fence_proxy_async();
     __syncthreads();
     // a slot is refilled only after its previous copy was waited for: once a
     // wait of the issuing thread gave up, nothing more is issued
@@ -449,13 +534,19 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
         pnext = harm ? a.px[xn] : (T)0;
       }
       wait_plane(sq3);
-      if (bnd_y || bnd_z) fixup(sq3, x + 3);
-      {
-        const V* sl3 = ring + (size_t)(sq3 % S) * G::SLOT_STRIDE_ELEMS;
+      if (K::DEFER) {
+        V v[R];
+        prepare(sq3, x + 3, true, v);
+        fence_proxy_async();
+#pragma unroll
+        for (int r = 0; r < R; ++r) q[(OFF + 6) % 7][r] = v[r];
+      } else {
+        if (bnd_y || bnd_z) fixup(sq3, x + 3);
+        const V* sl3 = ring + (size_t)(sq3 % S) * K::SLOT_STRIDE_ELEMS;
 #pragma unroll
         for (int r = 0; r < R; ++r) q[(OFF + 6) % 7][r] = sl3[qoff + r * TZP];
       }
-      const V* slx = ring + (size_t)(sqx % S) * G::SLOT_STRIDE_ELEMS;
+      const V* slx = ring + (size_t)(sqx % S) * K::SLOT_STRIDE_ELEMS;
       const V* col = slx + qoff;
       // y column: 3 ghost rows above, R centres (from the queue), 3 below
       V yc[R + 6];
@@ -519,14 +610,15 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
           pn = P::add(c, cr);
           wn = cr;
         } else {
-          const V wv = READS_W ? slx[G::W_OFF_ELEMS + (yg * R + r) * TZ + lz] : mk<T>((T)0, (T)0);
-          wn = (KIND == ST_S1) ? cr : P::fma(ta.k[14], wv, cr);
+          const V wv = K::DEFER ? slx[G::W_OFF_ELEMS + qoff + r * TZP]
+                       : READS_W ? slx[G::W_OFF_ELEMS + (yg * R + r) * TZ + lz] : mk<T>((T)0, (T)0);
+          wn = (KIND == ST_S1 || KIND == ST_S1W) ? cr : P::fma(ta.k[14], wv, cr);
           pn = P::fma(ta.k[15], wn, c);
         }
         if (store && zok && yok[r]) {
           const size_t idx = rowbase + (size_t)r * nz;
-          if (KIND == ST_S1 || KIND == ST_S2) a.w[idx] = wn;
-          if (KIND != ST_DIAG) a.psi_out[idx] = pn;
+          if (KIND == ST_S1 || KIND == ST_S2 || KIND == ST_S1W || KIND == ST_S2D) a.w[idx] = wn;
+          if (KIND != ST_DIAG && KIND != ST_S1W) a.psi_out[idx] = pn;
           if (!PLAIN) {
             if (a.reduce == 1) rN.add(pn.x * pn.x + pn.y * pn.y);
             if (KIND == ST_DIAG || a.reduce == 2) {

@@ -2,8 +2,8 @@
 #include "tiled_impl.cuh"
 
 namespace tb {
-int plan_f32_s1(const trapbec_params& p, void* const psi[2], void* w, int nsm, int* err, TiledPlan* plan) {
-  return plan_shape<float, 64, 8, 2, 8, 0>(p, psi, w, nsm, err, plan);
+int plan_f32_s1(const trapbec_params& p, void* const psi[2], void* w, void* w2, int nsm, int* err, TiledPlan* plan) {
+  return plan_shape<float, 64, 8, 2, 8, 0>(p, psi, w, w2, nsm, err, plan);
 }
 int launch_f32_s1(const TiledPlan& plan, int kind, const StageArgs<float>& a, cudaStream_t st, int red_cap, int* nblk) {
   return launch_shape<float, 64, 8, 2, 8, 0>(plan, kind, a, st, red_cap, nblk);

@@ -2,8 +2,8 @@
 #include "tiled_impl.cuh"
 
 namespace tb {
-int plan_f64_s0(const trapbec_params& p, void* const psi[2], void* w, int nsm, int* err, TiledPlan* plan) {
-  return plan_shape<double, 32, 8, 2, 8, 0>(p, psi, w, nsm, err, plan);
+int plan_f64_s0(const trapbec_params& p, void* const psi[2], void* w, void* w2, int nsm, int* err, TiledPlan* plan) {
+  return plan_shape<double, 32, 8, 2, 8, 0>(p, psi, w, w2, nsm, err, plan);
 }
 int launch_f64_s0(const TiledPlan& plan, int kind, const StageArgs<double>& a, cudaStream_t st, int red_cap, int* nblk) {
   return launch_shape<double, 32, 8, 2, 8, 0>(plan, kind, a, st, red_cap, nblk);

@@ -34,39 +34,46 @@ template <typename T> inline void fill_coeffs(TiledArgs<T>& ta) {
   ta.k[10] = pr((T)(-9)); ta.k[11] = pr((T)45);
   ta.k[12] = pr(a.c_re); ta.k[13] = mk<T>(-a.c_im, a.c_im);
   ta.k[14] = pr(a.A); ta.k[15] = pr(a.B);
+  ta.k[16] = pr(a.B1);
+}
+
+// One TMA descriptor over an (nx, ny, nz) complex array: a box with the
+// 3-deep ghost frame (ghosted) or an interior tile.
+template <typename T, int TZ, int TY, int R, int NS, int MB>
+int encode_box(const trapbec_params& p, void* base, bool ghosted, CUtensorMap* map) {
+  using G = TileGeom<T, TZ, TY, R, NS, MB>;
+  auto enc = tensor_map_encoder();
+  if (!enc) return 2;
+  cuuint64_t dims[3], strides[2];
+  cuuint32_t box[3], es[3] = {1, 1, 1};
+  // FP32: one 8-byte element = one complex float; FP64: a complex double is two doubles
+  dims[0] = sizeof(T) == 4 ? (cuuint64_t)p.nz : (cuuint64_t)p.nz * 2;
+  const int bz = ghosted ? G::TZP : TZ;
+  box[0] = sizeof(T) == 4 ? bz : 2 * bz;
+  dims[1] = (cuuint64_t)p.ny;
+  dims[2] = (cuuint64_t)p.nx;
+  strides[0] = (cuuint64_t)p.nz * sizeof(c_t<T>);
+  strides[1] = (cuuint64_t)p.ny * p.nz * sizeof(c_t<T>);
+  box[1] = ghosted ? G::ROWS : TY;
+  box[2] = 1;
+  CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, base, dims, strides, box, es,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? 0 : 3;
 }
 
 // TMA descriptors of one grid: the two psi buffers (boxes with the 3-deep
 // ghost frame) and w (interior tiles).
 template <typename T, int TZ, int TY, int R, int NS, int MB>
 int encode_maps(const trapbec_params& p, void* const psi[2], void* w, CUtensorMap* tm, CUtensorMap* tmw) {
-  using G = TileGeom<T, TZ, TY, R, NS, MB>;
-  auto enc = tensor_map_encoder();
-  if (!enc) return 2;
-  for (int b = 0; b < 3; ++b) {
-    const bool is_w = (b == 2);
-    cuuint64_t dims[3], strides[2];
-    cuuint32_t box[3], es[3] = {1, 1, 1};
-    // FP32: one 8-byte element = one complex float; FP64: a complex double is two doubles
-    dims[0] = sizeof(T) == 4 ? (cuuint64_t)p.nz : (cuuint64_t)p.nz * 2;
-    const int bz = is_w ? TZ : G::TZP;
-    box[0] = sizeof(T) == 4 ? bz : 2 * bz;
-    dims[1] = (cuuint64_t)p.ny;
-    dims[2] = (cuuint64_t)p.nx;
-    strides[0] = (cuuint64_t)p.nz * sizeof(c_t<T>);
-    strides[1] = (cuuint64_t)p.ny * p.nz * sizeof(c_t<T>);
-    box[1] = is_w ? TY : G::ROWS;
-    box[2] = 1;
-    CUresult r = enc(is_w ? tmw : &tm[b], CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, is_w ? w : psi[b], dims, strides,
-                     box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r != CUDA_SUCCESS) return 3;
-  }
-  return 0;
+  for (int b = 0; b < 2; ++b)
+    if (int rc = encode_box<T, TZ, TY, R, NS, MB>(p, psi[b], true, &tm[b])) return rc;
+  return encode_box<T, TZ, TY, R, NS, MB>(p, w, false, tmw);
 }
 
 template <typename T, int TZ, int TY, int R, int NS, int MB>
-int plan_shape(const trapbec_params& p, void* const psi[2], void* w, int nsm, int* err_flag, TiledPlan* plan) {
+int plan_shape(const trapbec_params& p, void* const psi[2], void* w, void* w2, int nsm, int* err_flag,
+               TiledPlan* plan) {
   using G = TileGeom<T, TZ, TY, R, NS, MB>;
   if (p.two_dim || p.nx < 4 || p.ny < 4 || p.nz < 8) return 1;
   if (sizeof(T) == 4 && (p.nz % 2)) return 1;  // TMA strides must be multiples of 16 bytes
@@ -80,6 +87,8 @@ int plan_shape(const trapbec_params& p, void* const psi[2], void* w, int nsm, in
   if (int rc = encode_maps<T, TZ, TY, R, NS, MB>(p, psi, w, q.tm, &q.tmw)) return rc;
   q.psi_base[0] = psi[0];
   q.psi_base[1] = psi[1];
+  q.w_base[0] = w;
+  q.w_base[1] = nullptr;
   auto k1 = stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S1, false, false>;
   auto k2 = stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S2, false, false>;
   auto k3 = stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S3, false, false>;
@@ -92,6 +101,26 @@ int plan_shape(const trapbec_params& p, void* const psi[2], void* w, int nsm, in
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM) != cudaSuccess) return 4;
   int nb = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k2, G::NT, G::SMEM) != cudaSuccess || nb < 1) return 5;
+  // the deferred real-time form (FP32): S1 stores w1 only, S2 forms psi1 from
+  // ghosted boxes of psi0 and w1 and writes w2 to the second w buffer
+  q.defer_ok = 0;
+  if constexpr (sizeof(T) == 4) {
+    if (w2) {
+      auto kw = stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S1W, true, false>;
+      auto kd = stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S2D, true, false>;
+      constexpr int SMEM_D = KindGeom<T, G, ST_S2D>::SMEM;
+      int nbd = 0;
+      if (encode_box<T, TZ, TY, R, NS, MB>(p, w, true, &q.tmwg) == 0 &&
+          encode_box<T, TZ, TY, R, NS, MB>(p, w2, false, &q.tmw1) == 0 &&
+          cudaFuncSetAttribute(kw, cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM) == cudaSuccess &&
+          cudaFuncSetAttribute(kd, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_D) == cudaSuccess &&
+          cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nbd, kd, G::NT, SMEM_D) == cudaSuccess && nbd >= nb) {
+        q.w_base[1] = w2;
+        q.defer_ok = 1;
+      }
+    }
+  }
+  cudaGetLastError();   // a refused attribute only disables the deferred form
   q.ntz = (p.nz + TZ - 1) / TZ;
   q.nty = (p.ny + TY - 1) / TY;
   q.units = (long long)q.ntz * q.nty * p.nx;
@@ -128,25 +157,42 @@ int launch_shape(const TiledPlan& plan, int kind, const StageArgs<T>& a, cudaStr
   if ((const void*)a.psi_in == plan.psi_base[0]) tm = &plan.tm[0];
   else if ((const void*)a.psi_in == plan.psi_base[1]) tm = &plan.tm[1];
   if (!tm) return 6;
+  // w tiles come from whichever w buffer a.w is
+  const CUtensorMap* tmw = &plan.tmw;
+  if (plan.defer_ok && (const void*)a.w == plan.w_base[1]) tmw = &plan.tmw1;
   int grid = plan.grid;
   if (a.red && grid > red_cap) grid = red_cap;
-  // the plain variant: no reductions, no load factor, harmonic / no potential,
-  // rotation / no frame term, not from the imaginary-time control block
-  const bool plain = a.red == nullptr && a.reduce == 0 && a.ctrl == nullptr && a.scale == (T)1 &&
-                     a.pot_mode != POT_ARR && a.frame_mode != FRAME_ADV;
+  const bool plain = tiled_plain(a);
+  if (kind == ST_S1W || kind == ST_S2D) {
+    if constexpr (sizeof(T) == 4) {
+      if (!plain || !plan.defer_ok) return 9;
+      if (kind == ST_S1W) {
+        stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S1W, true, false><<<grid, G::NT, G::SMEM, st>>>(*tm, *tmw, ta, BatchArgs{});
+      } else {
+        // w1 (ghosted boxes) in, w2 out
+        if ((const void*)a.w_in != plan.w_base[0] || (const void*)a.w != plan.w_base[1]) return 10;
+        stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S2D, true, false>
+            <<<grid, G::NT, KindGeom<T, G, ST_S2D>::SMEM, st>>>(*tm, plan.tmwg, ta, BatchArgs{});
+      }
+      if (nblk) *nblk = grid;
+      return cudaGetLastError() == cudaSuccess ? 0 : 8;
+    } else {
+      return 9;
+    }
+  }
   if (plain && kind == ST_S1) {
-    stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S1, true, false><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta, BatchArgs{});
+    stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S1, true, false><<<grid, G::NT, G::SMEM, st>>>(*tm, *tmw, ta, BatchArgs{});
   } else if (plain && kind == ST_S2) {
-    stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S2, true, false><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta, BatchArgs{});
+    stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S2, true, false><<<grid, G::NT, G::SMEM, st>>>(*tm, *tmw, ta, BatchArgs{});
   } else if (plain && kind == ST_S3) {
-    stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S3, true, false><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta, BatchArgs{});
+    stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S3, true, false><<<grid, G::NT, G::SMEM, st>>>(*tm, *tmw, ta, BatchArgs{});
   } else {
     switch (kind) {
-      case ST_S1: stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S1, false, false><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta, BatchArgs{}); break;
-      case ST_S2: stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S2, false, false><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta, BatchArgs{}); break;
-      case ST_S3: stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S3, false, false><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta, BatchArgs{}); break;
-      case ST_EU: stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_EU, false, false><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta, BatchArgs{}); break;
-      case ST_DIAG: stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_DIAG, false, false><<<grid, G::NT, G::SMEM, st>>>(*tm, plan.tmw, ta, BatchArgs{}); break;
+      case ST_S1: stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S1, false, false><<<grid, G::NT, G::SMEM, st>>>(*tm, *tmw, ta, BatchArgs{}); break;
+      case ST_S2: stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S2, false, false><<<grid, G::NT, G::SMEM, st>>>(*tm, *tmw, ta, BatchArgs{}); break;
+      case ST_S3: stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S3, false, false><<<grid, G::NT, G::SMEM, st>>>(*tm, *tmw, ta, BatchArgs{}); break;
+      case ST_EU: stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_EU, false, false><<<grid, G::NT, G::SMEM, st>>>(*tm, *tmw, ta, BatchArgs{}); break;
+      case ST_DIAG: stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_DIAG, false, false><<<grid, G::NT, G::SMEM, st>>>(*tm, *tmw, ta, BatchArgs{}); break;
       default: return 7;
     }
   }

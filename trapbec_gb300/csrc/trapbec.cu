@@ -69,6 +69,7 @@ struct trapbec_ctx {
   void* psi[2] = {nullptr, nullptr};
   int cur = 0;
   void* w = nullptr;
+  void* w2 = nullptr;                  // second w buffer of the deferred real-time form (allocated on request)
   double force_args[3] = {0.0, 0.0, 1.0};   // (x0, y0, dir) of the next forced vortex
   void *xx = nullptr, *yy = nullptr, *zz = nullptr, *px = nullptr, *py = nullptr, *pz = nullptr;
   void* trap_user = nullptr;   // Trap array set by the caller (context precision)
@@ -92,14 +93,18 @@ struct trapbec_ctx {
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   double last_ms = 0.0;
   std::vector<double> hxx, hyy, hzz;   // coordinates as double (exact copies of T values)
-  TiledPlan plan;                      // tiled-kernel plan (tensor maps, tile shape)
+  TiledPlan plan;                      // tiled-kernel plan (tensor maps, tile shape) of every launch ...
   bool plan_valid = false;
   int shape = 0;                       // tiled-kernel shape index
+  TiledPlan plan_rt;                   // ... but the plain real-time stages, which run this one
+  bool plan_rt_valid = false;
+  int shape_rt = -1;
   int* d_err = nullptr;                // device error flag of the tiled kernel
   uint32_t wait_us = 2000000;          // bounded-wait limit of the tiled kernel (microseconds)
   int inject_wait = 0;                 // test hook of the bounded waits
   int* h_err = nullptr;                // pinned copy
   int chunk_user = 0;                  // x-chunk requested by the caller (0 = automatic)
+  int stage_form = TRAPBEC_RK3_THREE_STAGE;   // real-time RK3 form (trapbec_rk3_form)
 };
 
 namespace {
@@ -218,6 +223,31 @@ template <typename T> bool use_tiled(trapbec_ctx* c) {
   return c->plan_valid;
 }
 
+// Stage kinds of the real-time step that take the real-time plan when plain.
+inline bool rt_kind(int kind) {
+  return kind == ST_S1 || kind == ST_S2 || kind == ST_S3 || kind == ST_S1W || kind == ST_S2D;
+}
+
+// The two tiled plans: `plan` (shape index `shape`) for every launch and
+// `plan_rt` for the plain real-time stages (shape_rt < 0: the default
+// real-time shape where it plans; otherwise, or if it does not plan, the
+// general plan).  Chunk lengths follow auto_chunk.
+template <typename T> void make_plans(trapbec_ctx* c, int shape, int shape_rt) {
+  c->plan_valid = (plan_tiled<T>(c->p, c->psi, c->w, c->w2, c->nsm, shape, c->d_err, &c->plan) == 0);
+  c->shape = shape;
+  if (shape_rt < 0) shape_rt = tiled_rt_shape<T>();
+  c->plan_rt_valid = false;
+  if (shape_rt != shape)
+    c->plan_rt_valid = (plan_tiled<T>(c->p, c->psi, c->w, c->w2, c->nsm, shape_rt, c->d_err, &c->plan_rt) == 0);
+  if (!c->plan_rt_valid && c->plan_valid) {
+    c->plan_rt = c->plan;
+    c->plan_rt_valid = true;
+  }
+  c->shape_rt = c->plan_rt_valid ? c->plan_rt.shape : -1;
+  if (c->plan_valid) c->plan.chunk = auto_chunk(c);
+  if (c->plan_rt_valid) c->plan_rt.chunk = auto_chunk(c);
+}
+
 // Read and clear the device error flag of the tiled kernel.
 int check_device_error(trapbec_ctx* c) {
   CK(cudaMemcpyAsync(c->h_err, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->st));
@@ -236,10 +266,17 @@ int check_device_error(trapbec_ctx* c) {
 // Launch one stage.  kind: StageKind or 4 (diagnostics).  Returns status.
 template <typename T>
 int launch_stage(trapbec_ctx* c, int kind, StageArgs<T>& a, int* nblk_out) {
-  c->plan.wait_us = c->wait_us;
-  c->plan.inject_wait = c->inject_wait;
-  if (use_tiled<T>(c)) {
-    int rc = launch_tiled<T>(c->plan, kind, a, c->st, c->red_cap, nblk_out);
+  const bool rt = rt_kind(kind) && tiled_plain(a);
+  TiledPlan& plan = rt ? c->plan_rt : c->plan;
+  const bool tiled = c->kernel_kind != 1 && (rt ? c->plan_rt_valid : c->plan_valid);
+  plan.wait_us = c->wait_us;
+  plan.inject_wait = c->inject_wait;
+  if (!tiled && (kind == ST_S1W || kind == ST_S2D)) {
+    set_error("the deferred real-time stages need the tiled kernel");
+    return TRAPBEC_ERR_UNSUPPORTED;
+  }
+  if (tiled) {
+    int rc = launch_tiled<T>(plan, kind, a, c->st, c->red_cap, nblk_out);
     if (rc) { set_error("tiled stage launch failed (" + std::to_string(rc) + ")"); return TRAPBEC_ERR_CUDA; }
     CKL();
     c->launches++;
@@ -338,6 +375,26 @@ template <typename T> int do_step_rt(trapbec_ctx* c, int nsteps) {
     StageArgs<T> a = base_args<T>(c, c->t);
     a.c_re = cre; a.c_im = cim;
     a.w = (c_t<T>*)c->w;
+    if (c->stage_form == TRAPBEC_RK3_DEFERRED && c->kernel_kind != 1 && c->plan_rt_valid && c->plan_rt.defer_ok &&
+        tiled_plain(a)) {
+      // deferred form: stage 1 stores w1 only; stage 2 forms psi1 = psi0 + w1/3
+      // from psi0 and w1 with the FMA stage 1 would have used, and writes w2
+      // to the second w buffer; stage 3 writes psi3 over psi0.  Same values.
+      a.psi_in = (const c_t<T>*)c->psi[c->cur]; a.psi_out = nullptr;
+      a.A = 0; a.B = (T)1 / (T)3;
+      if ((rc = launch_stage<T>(c, ST_S1W, a, nullptr))) return rc;
+      a.w_in = (const c_t<T>*)c->w; a.w = (c_t<T>*)c->w2;
+      a.B1 = (T)1 / (T)3;
+      a.psi_out = (c_t<T>*)c->psi[c->cur ^ 1];
+      a.A = a2; a.B = (T)1;
+      if ((rc = launch_stage<T>(c, ST_S2D, a, nullptr))) return rc;
+      a.w_in = nullptr;
+      a.psi_in = (const c_t<T>*)c->psi[c->cur ^ 1]; a.psi_out = (c_t<T>*)c->psi[c->cur];
+      a.A = (T)(-1); a.B = (T)0.5;
+      if ((rc = launch_stage<T>(c, ST_S3, a, nullptr))) return rc;
+      c->t = (double)((T)c->t + dcr);   // run.f90:55, t real
+      continue;
+    }
     // stage 1: w = c rhs; psi += w/3
     a.psi_in = (const c_t<T>*)c->psi[c->cur]; a.psi_out = (c_t<T>*)c->psi[c->cur ^ 1];
     a.A = 0; a.B = (T)1 / (T)3;
@@ -681,14 +738,13 @@ template <typename T> int create_impl(trapbec_ctx* c) {
   *c->h_err = 0;
   int rc = setup_tables<T>(c);
   if (rc) return rc;
-  c->plan_valid = (plan_tiled<T>(c->p, c->psi, c->w, c->nsm, 0, c->d_err, &c->plan) == 0);
-  if (c->plan_valid) c->plan.chunk = auto_chunk(c);
+  make_plans<T>(c, 0, -1);
   return TRAPBEC_OK;
 }
 
 void free_ctx(trapbec_ctx* c) {
   if (!c) return;
-  void* bufs[] = {c->psi[0], c->psi[1], c->w, c->xx, c->yy, c->zz, c->px, c->py, c->pz,
+  void* bufs[] = {c->psi[0], c->psi[1], c->w, c->w2, c->xx, c->yy, c->zz, c->px, c->py, c->pz,
                   c->trap_user, c->trap_eff, c->red, c->red_out, c->ctrl, c->d_err};
   for (void* b : bufs) if (b) cudaFree(b);
   if (c->host_red) cudaFreeHost(c->host_red);
@@ -1109,15 +1165,12 @@ int trapbec_set_kernel(trapbec_ctx* c, int kind, int tile_z, int tile_y) {
       return TRAPBEC_ERR_UNSUPPORTED;
     }
   }
-  if (shape != c->shape || !c->plan_valid) {
-    c->shape = shape;
-    c->tile_z = tile_z;
-    c->tile_y = tile_y;
-    int rc = c->prec == TRAPBEC_FP64 ? plan_tiled<double>(c->p, c->psi, c->w, c->nsm, shape, c->d_err, &c->plan)
-                                     : plan_tiled<float>(c->p, c->psi, c->w, c->nsm, shape, c->d_err, &c->plan);
-    c->plan_valid = (rc == 0);
-    if (c->plan_valid) c->plan.chunk = auto_chunk(c);
-  }
+  // an explicit shape serves every launch; the default keeps the real-time shape
+  const int shape_rt = (tile_z || tile_y) ? shape : -1;
+  c->tile_z = tile_z;
+  c->tile_y = tile_y;
+  if (c->prec == TRAPBEC_FP64) make_plans<double>(c, shape, shape_rt);
+  else make_plans<float>(c, shape, shape_rt);
   if (kind == 2 && !c->plan_valid) {
     set_error("tiled kernel not available for this grid / tile shape");
     return TRAPBEC_ERR_UNSUPPORTED;
@@ -1129,6 +1182,43 @@ int trapbec_set_chunk(trapbec_ctx* c, int chunk) {
   if (!c || chunk < 0) return TRAPBEC_ERR_ARG;
   c->chunk_user = chunk;
   if (c->plan_valid) c->plan.chunk = auto_chunk(c);
+  if (c->plan_rt_valid) c->plan_rt.chunk = auto_chunk(c);
+  return TRAPBEC_OK;
+}
+
+int trapbec_get_tile_shape(trapbec_ctx* c, int real_time, int* tile_z, int* tile_y) {
+  if (!c || !tile_z || !tile_y) return TRAPBEC_ERR_ARG;
+  const bool valid = c->kernel_kind != 1 && (real_time ? c->plan_rt_valid : c->plan_valid);
+  const TiledPlan& pl = real_time ? c->plan_rt : c->plan;
+  *tile_z = valid ? pl.tz : 0;
+  *tile_y = valid ? pl.ty : 0;
+  return TRAPBEC_OK;
+}
+
+int trapbec_set_stage_form(trapbec_ctx* c, int form) {
+  if (!c || (form != TRAPBEC_RK3_THREE_STAGE && form != TRAPBEC_RK3_DEFERRED)) return TRAPBEC_ERR_ARG;
+  c->stage_form = form;
+  if (form == TRAPBEC_RK3_DEFERRED && c->prec == TRAPBEC_FP32 && !c->p.two_dim && !c->w2) {
+    // the second w buffer, then plans that know it
+    CK(cudaMalloc(&c->w2, c->n * c->esz));
+    CK(cudaMemsetAsync(c->w2, 0, c->n * c->esz, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    make_plans<float>(c, c->shape, c->shape_rt);
+  }
+  return TRAPBEC_OK;
+}
+
+int trapbec_get_stage_form(trapbec_ctx* c, int* deferred) {
+  if (!c || !deferred) return TRAPBEC_ERR_ARG;
+  StageArgs<float> a;
+  std::memset(&a, 0, sizeof(a));
+  bool plain = true;
+  if (c->prec == TRAPBEC_FP32) {
+    a = base_args<float>(c, c->t);
+    plain = tiled_plain(a);
+  }
+  *deferred = (c->stage_form == TRAPBEC_RK3_DEFERRED && c->prec == TRAPBEC_FP32 && c->kernel_kind != 1 &&
+               c->plan_rt_valid && c->plan_rt.defer_ok && plain) ? 1 : 0;
   return TRAPBEC_OK;
 }
 
@@ -1164,13 +1254,13 @@ template <typename T> int autotune_impl(trapbec_ctx* c, int steps, TuneVal* best
   int rc = TRAPBEC_OK;
   for (int sh = 0; sh < ns && rc == TRAPBEC_OK; ++sh) {
     TiledPlan plan;
-    if (plan_tiled<T>(c->p, c->psi, c->w, c->nsm, sh, c->d_err, &plan) != 0) continue;
+    if (plan_tiled<T>(c->p, c->psi, c->w, c->w2, c->nsm, sh, c->d_err, &plan) != 0) continue;
     std::vector<int> chunks = {16, 32, 64, c->p.nx};
     for (int L : chunks) {
       if (L > c->p.nx) continue;
       plan.chunk = L;
-      c->plan = plan;
-      c->plan_valid = true;
+      c->plan_rt = plan;
+      c->plan_rt_valid = true;
       c->kernel_kind = 2;
       if ((rc = do_step_rt<T>(c, 1))) break;     // warm-up
       if ((rc = do_step_rt<T>(c, steps))) break;
@@ -1189,11 +1279,10 @@ template <typename T> int autotune_impl(trapbec_ctx* c, int steps, TuneVal* best
   c->kernel_kind = 0;
   if (rc) return rc;
   if (bv.shape < 0) { set_error("no tiled kernel shape fits this grid"); return TRAPBEC_ERR_UNSUPPORTED; }
-  if (plan_tiled<T>(c->p, c->psi, c->w, c->nsm, bv.shape, c->d_err, &c->plan) != 0) return TRAPBEC_ERR_CUDA;
-  c->plan.chunk = bv.chunk;
-  c->plan_valid = true;
-  c->shape = bv.shape;
-  c->chunk_user = bv.chunk;
+  if (plan_tiled<T>(c->p, c->psi, c->w, c->w2, c->nsm, bv.shape, c->d_err, &c->plan_rt) != 0) return TRAPBEC_ERR_CUDA;
+  c->plan_rt.chunk = bv.chunk;
+  c->plan_rt_valid = true;
+  c->shape_rt = bv.shape;
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     g_tune_cache.push_back({key, bv});
@@ -1209,15 +1298,14 @@ int trapbec_autotune(trapbec_ctx* c, int steps, int* tile_z, int* tile_y, int* c
   TuneVal bv;
   int rc = DISPATCH(c, autotune_impl, c, steps, &bv);
   if (rc) return rc;
-  if (!c->plan_valid || c->plan.shape != bv.shape) {
-    int r2 = c->prec == TRAPBEC_FP64 ? plan_tiled<double>(c->p, c->psi, c->w, c->nsm, bv.shape, c->d_err, &c->plan)
-                                     : plan_tiled<float>(c->p, c->psi, c->w, c->nsm, bv.shape, c->d_err, &c->plan);
+  if (!c->plan_rt_valid || c->plan_rt.shape != bv.shape) {   // a cached choice
+    int r2 = c->prec == TRAPBEC_FP64 ? plan_tiled<double>(c->p, c->psi, c->w, c->w2, c->nsm, bv.shape, c->d_err, &c->plan_rt)
+                                     : plan_tiled<float>(c->p, c->psi, c->w, c->w2, c->nsm, bv.shape, c->d_err, &c->plan_rt);
     if (r2) return TRAPBEC_ERR_CUDA;
-    c->plan_valid = true;
-    c->shape = bv.shape;
+    c->plan_rt_valid = true;
+    c->shape_rt = bv.shape;
   }
-  c->chunk_user = bv.chunk;
-  c->plan.chunk = bv.chunk;
+  c->plan_rt.chunk = bv.chunk;
   Shape sh = c->prec == TRAPBEC_FP64 ? tiled_shape<double>(bv.shape) : tiled_shape<float>(bv.shape);
   if (tile_z) *tile_z = sh.tz;
   if (tile_y) *tile_y = sh.ty;

@@ -167,6 +167,24 @@ class Solver:
     def set_chunk(self, chunk: int) -> None:
         check(self.lib.trapbec_set_chunk(self.ctx, int(chunk)), "trapbec_set_chunk")
 
+    def tile_shape(self, real_time: bool = True) -> tuple[int, int]:
+        """(tile_z, tile_y) of the plain real-time stages (or of every other launch); (0, 0) = per-cell kernel."""
+        tz, ty = C.c_int(0), C.c_int(0)
+        check(self.lib.trapbec_get_tile_shape(self.ctx, int(bool(real_time)), C.byref(tz), C.byref(ty)),
+              "trapbec_get_tile_shape")
+        return tz.value, ty.value
+
+    def set_stage_form(self, form: int) -> None:
+        """Real-time RK3 form: abi.RK3_THREE_STAGE (default) or abi.RK3_DEFERRED
+        (stage 1 stores w1 only; allocates a second w buffer)."""
+        check(self.lib.trapbec_set_stage_form(self.ctx, int(form)), "trapbec_set_stage_form")
+
+    def stage_form_deferred(self) -> bool:
+        """True when the next step_rt takes the deferred form."""
+        v = C.c_int(0)
+        check(self.lib.trapbec_get_stage_form(self.ctx, C.byref(v)), "trapbec_get_stage_form")
+        return bool(v.value)
+
     def autotune(self, steps: int = 3) -> dict:
         tz, ty, ch, ms = C.c_int(0), C.c_int(0), C.c_int(0), C.c_double(0)
         check(self.lib.trapbec_autotune(self.ctx, int(steps), C.byref(tz), C.byref(ty), C.byref(ch),
