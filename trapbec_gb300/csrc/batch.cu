@@ -164,32 +164,16 @@ template <typename T> int shape_encode(int s, const trapbec_params& p, void* con
 // order (fixed partition per thread, fixed tree) and updates ctrl[i].
 __device__ void gather_instance(const double* __restrict__ part, const int* __restrict__ tag, int nslots, int inst,
                                 double* out /* shared NRED */) {
-  __shared__ double sh[FIN_THREADS];
-  for (int q = 0; q < NRED; ++q) {
-    double x;
-    if (q < 6) {
-      Acc s;
-      s.init();
-      for (int b = threadIdx.x; b < nslots; b += FIN_THREADS)
-        if (tag[b] == inst) s.add(part[(size_t)b * NRED + q]);
-      x = s.val();
-    } else {
-      x = (q == 7) ? 1.0e300 : 0.0;
-      for (int b = threadIdx.x; b < nslots; b += FIN_THREADS)
-        if (tag[b] == inst) x = (q == 7) ? fmin(x, part[(size_t)b * NRED + q]) : fmax(x, part[(size_t)b * NRED + q]);
-    }
-    sh[threadIdx.x] = x;
-    __syncthreads();
-    for (int s2 = FIN_THREADS / 2; s2 > 0; s2 >>= 1) {
-      if ((int)threadIdx.x < s2) {
-        const double y = sh[threadIdx.x + s2], z = sh[threadIdx.x];
-        sh[threadIdx.x] = (q == 6 || q == 8) ? fmax(z, y) : (q == 7 ? fmin(z, y) : z + y);
-      }
-      __syncthreads();
-    }
-    if (threadIdx.x == 0) out[q] = sh[0];
-    __syncthreads();
+  FinAcc a;
+  a.init();
+  for (int b = threadIdx.x; b < nslots; b += FIN_THREADS) {
+    if (tag[b] != inst) continue;
+    double v[NRED];
+#pragma unroll
+    for (int q = 0; q < NRED; ++q) v[q] = part[(size_t)b * NRED + q];
+    a.add(v);
   }
+  fin_tree(a, out);
 }
 
 __global__ void __launch_bounds__(FIN_THREADS) batch_fin_energy_kernel(const double* __restrict__ part,

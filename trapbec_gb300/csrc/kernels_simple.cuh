@@ -140,34 +140,79 @@ __global__ void __launch_bounds__(SIMPLE_THREADS) stage_simple_kernel(StageArgs<
 // Reduce the [NRED][nblk] partials to NRED values, in a fixed order so the
 // result is bitwise reproducible run to run.
 constexpr int FIN_THREADS = 512;
-// Called by all FIN_THREADS threads of one block; out[] is written by thread 0.
-__device__ __forceinline__ void finalize_partials(const double* __restrict__ red, int nblk, double* out) {
-  __shared__ double sh[FIN_THREADS];
-  for (int q = 0; q < NRED; ++q) {
-    const double* r = red + (size_t)q * nblk;
-    double x;
-    if (q < 6) {
-      Acc s;
-      s.init();
-      for (int b = threadIdx.x; b < nblk; b += FIN_THREADS) s.add(r[b]);
-      x = s.val();
-    } else {
-      x = (q == 7) ? 1.0e300 : 0.0;
-      for (int b = threadIdx.x; b < nblk; b += FIN_THREADS) x = (q == 7) ? fmin(x, r[b]) : fmax(x, r[b]);
+
+// Combination rule of reduction slot q: sums (0-5), max (6, 8), min (7).
+__device__ __forceinline__ double fin_op(int q, double z, double y) {
+  return (q == 6 || q == 8) ? fmax(z, y) : (q == 7 ? fmin(z, y) : z + y);
+}
+
+// One thread's running values of the NRED quantities.
+struct FinAcc {
+  Acc s[6];
+  double mx6, mn7, mx8;
+  __device__ __forceinline__ void init() {
+#pragma unroll
+    for (int q = 0; q < 6; ++q) s[q].init();
+    mx6 = 0.0; mn7 = 1.0e300; mx8 = 0.0;
+  }
+  __device__ __forceinline__ void add(const double* v) {   // v[NRED] of one partial
+#pragma unroll
+    for (int q = 0; q < 6; ++q) s[q].add(v[q]);
+    mx6 = fmax(mx6, v[6]);
+    mn7 = fmin(mn7, v[7]);
+    mx8 = fmax(mx8, v[8]);
+  }
+};
+
+// Combine the FIN_THREADS threads' values with a fixed pairwise tree (thread
+// t takes t + s at every level s = 256 ... 1: shared memory down to 32, warp
+// shuffles below, the same pairs either way); out[] is written by thread 0.
+__device__ __forceinline__ void fin_tree(const FinAcc& a, double* out) {
+  __shared__ double sh[NRED][FIN_THREADS];
+  const int t = threadIdx.x;
+#pragma unroll
+  for (int q = 0; q < 6; ++q) sh[q][t] = a.s[q].val();
+  sh[6][t] = a.mx6;
+  sh[7][t] = a.mn7;
+  sh[8][t] = a.mx8;
+  __syncthreads();
+  for (int s = FIN_THREADS / 2; s >= 32; s >>= 1) {
+    if (t < s) {
+#pragma unroll
+      for (int q = 0; q < NRED; ++q) sh[q][t] = fin_op(q, sh[q][t], sh[q][t + s]);
     }
-    sh[threadIdx.x] = x;
-    __syncthreads();
-    for (int s = FIN_THREADS / 2; s > 0; s >>= 1) {
-      if (threadIdx.x < s) {
-        double y = sh[threadIdx.x + s];
-        double z = sh[threadIdx.x];
-        sh[threadIdx.x] = (q == 6 || q == 8) ? fmax(z, y) : (q == 7 ? fmin(z, y) : z + y);
-      }
-      __syncthreads();
-    }
-    if (threadIdx.x == 0) out[q] = sh[0];
     __syncthreads();
   }
+  if (t < 32) {
+    double x[NRED];
+#pragma unroll
+    for (int q = 0; q < NRED; ++q) x[q] = sh[q][t];
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) {
+#pragma unroll
+      for (int q = 0; q < NRED; ++q) x[q] = fin_op(q, x[q], __shfl_down_sync(0xffffffffu, x[q], s));
+    }
+    if (t == 0) {
+#pragma unroll
+      for (int q = 0; q < NRED; ++q) out[q] = x[q];
+    }
+  }
+  __syncthreads();
+}
+
+// Called by all FIN_THREADS threads of one block: combines the block partials
+// red[q * nblk + b] (thread t takes b = t, t + FIN_THREADS, ... in order, then
+// the fixed tree); out[] is written by thread 0.
+__device__ __forceinline__ void finalize_partials(const double* __restrict__ red, int nblk, double* out) {
+  FinAcc a;
+  a.init();
+  for (int b = threadIdx.x; b < nblk; b += FIN_THREADS) {
+    double v[NRED];
+#pragma unroll
+    for (int q = 0; q < NRED; ++q) v[q] = red[(size_t)q * nblk + b];
+    a.add(v);
+  }
+  fin_tree(a, out);
 }
 
 static __global__ void __launch_bounds__(FIN_THREADS) reduce_finalize_kernel(const double* __restrict__ red,
