@@ -107,12 +107,15 @@ template <> struct BShapeF32<0> { static constexpr int TZ = 64, TY = 8, R = 2; }
 template <> struct BShapeF32<1> { static constexpr int TZ = 128, TY = 8, R = 2; };
 struct BShapeF64 { static constexpr int TZ = 32, TY = 8, R = 2; };
 
+// The batch runs the imaginary-time variant of the stage kernel: every
+// instance has a harmonic or no potential, a rotating or no frame and the
+// fixed reductions of the imaginary-time loop (fill_desc).
 template <typename T, int TZ, int TY, int R> struct BK {
   using G = TileGeom<T, TZ, TY, R, 8, 0>;
   static int prepare(int nsm, int* grid) {
-    auto k1 = stage_tiled_kernel<T, TZ, TY, R, 8, 0, ST_S1, false, true>;
-    auto k2 = stage_tiled_kernel<T, TZ, TY, R, 8, 0, ST_S2, false, true>;
-    auto k3 = stage_tiled_kernel<T, TZ, TY, R, 8, 0, ST_S3, false, true>;
+    auto k1 = stage_tiled_kernel<T, TZ, TY, R, 8, 0, ST_S1, VAR_IMAG, true>;
+    auto k2 = stage_tiled_kernel<T, TZ, TY, R, 8, 0, ST_S2, VAR_IMAG, true>;
+    auto k3 = stage_tiled_kernel<T, TZ, TY, R, 8, 0, ST_S3, VAR_IMAG, true>;
     for (auto k : {k1, k2, k3})
       if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM) != cudaSuccess) return 1;
     int nb = 0;
@@ -125,9 +128,9 @@ template <typename T, int TZ, int TY, int R> struct BK {
     std::memset(&dummy, 0, sizeof(dummy));
     CUtensorMap dm;
     std::memset(&dm, 0, sizeof(dm));
-    if (kind == ST_S1) stage_tiled_kernel<T, TZ, TY, R, 8, 0, ST_S1, false, true><<<grid, G::NT, G::SMEM, st>>>(dm, dm, dummy, ba);
-    else if (kind == ST_S2) stage_tiled_kernel<T, TZ, TY, R, 8, 0, ST_S2, false, true><<<grid, G::NT, G::SMEM, st>>>(dm, dm, dummy, ba);
-    else stage_tiled_kernel<T, TZ, TY, R, 8, 0, ST_S3, false, true><<<grid, G::NT, G::SMEM, st>>>(dm, dm, dummy, ba);
+    if (kind == ST_S1) stage_tiled_kernel<T, TZ, TY, R, 8, 0, ST_S1, VAR_IMAG, true><<<grid, G::NT, G::SMEM, st>>>(dm, dm, dummy, ba);
+    else if (kind == ST_S2) stage_tiled_kernel<T, TZ, TY, R, 8, 0, ST_S2, VAR_IMAG, true><<<grid, G::NT, G::SMEM, st>>>(dm, dm, dummy, ba);
+    else stage_tiled_kernel<T, TZ, TY, R, 8, 0, ST_S3, VAR_IMAG, true><<<grid, G::NT, G::SMEM, st>>>(dm, dm, dummy, ba);
   }
   static int encode(const trapbec_params& p, void* const psi[2], void* w, CUtensorMap* tm, CUtensorMap* tmw) {
     return encode_maps<T, TZ, TY, R, 8, 0>(p, psi, w, tm, tmw);

@@ -27,6 +27,8 @@
 #pragma once
 #include <cuda.h>
 
+#include <type_traits>
+
 #include "common.cuh"
 #include "kernels_simple.cuh"
 #include "tiled_api.h"
@@ -196,13 +198,23 @@ struct BatchArgs {
   int par;                 // step parity of this launch (selects TiledArgs)
 };
 
-// PLAIN: the real-time / get_rhs fast path -- no fused reductions, no load
-// factor, harmonic or no potential, rotation or no frame term (the rotation
-// algebra runs with omega = 0 when the frame is off).  Everything else goes
-// through the general variant (PLAIN = false) with run-time switches.
+// Variants (VAR):
+// VAR_PLAIN: the real-time / get_rhs fast path -- no fused reductions, no load
+//   factor, harmonic or no potential, rotation or no frame term (the rotation
+//   algebra runs with omega = 0 when the frame is off).
+// VAR_IMAG: the imaginary-time RK3 stages -- the same compile-time physics,
+//   plus the load factor, the converged-loop skip and the reductions fixed by
+//   the stage (stage 1 the energy set of the incoming state, stage 3 the norm
+//   of the new state, stage 2 none).  Same states, energies and norms as the
+//   general variant; the |psi| statistics of Psi_info (partials 5-7), which
+//   only diagnostics read, are left at their initial values.
+// VAR_GEN: everything else, with run-time switches (array potential,
+//   advective frame, diagnostics, any reduction).
 // BATCH: the units of many independent grids in one launch (batched
 // imaginary-time solves); arguments are read per segment from the table.
-template <typename T, int TZ, int TY, int R, int NSLOT, int MINB, int KIND, bool PLAIN, bool BATCH>
+enum StageVar : int { VAR_GEN = 0, VAR_PLAIN = 1, VAR_IMAG = 2 };
+
+template <typename T, int TZ, int TY, int R, int NSLOT, int MINB, int KIND, int VAR, bool BATCH>
 __global__ void __launch_bounds__(TileGeom<T, TZ, TY, R, NSLOT, MINB>::NT, TileGeom<T, TZ, TY, R, NSLOT, MINB>::MIN_BLOCKS)
 stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constant__ CUtensorMap tmw0,
                    const __grid_constant__ TiledArgs<T> ta0, const __grid_constant__ BatchArgs ba) {
@@ -212,11 +224,16 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
   using V = c_t<T>;
   constexpr int HZ = G::HZ, TZP = G::TZP, S = K::S, NT = G::NT;
   constexpr bool READS_W = (KIND == ST_S2 || KIND == ST_S3 || KIND == ST_S2D);
+  constexpr bool PLAIN = (VAR == VAR_PLAIN), IMAG = (VAR == VAR_IMAG), GEN = (VAR == VAR_GEN);
+  constexpr bool ANALYTIC = PLAIN || IMAG;   // harmonic / no potential, rotation / no frame
   static_assert(!K::DEFER || PLAIN, "the deferred stage has a plain variant only");
+  static_assert(!IMAG || KIND == ST_S1 || KIND == ST_S2 || KIND == ST_S3, "imaginary-time variant: RK3 stages only");
   // the queue preload waits for planes xa-3 .. xa+2, all issued before it
   static_assert(S >= 6, "the ring needs at least 6 slots");
 
   extern __shared__ __align__(128) unsigned char smem_raw[];
+  // batched launches: the current grid's arguments, staged from the device table
+  __shared__ typename std::conditional<BATCH, TiledArgs<T>, char>::type targs_s;
   V* ring = reinterpret_cast<V*>(smem_raw);
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + S * K::SLOT_STRIDE);   // S slots + 1 never-completed
 
@@ -286,6 +303,16 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
       tmwp = &d->tmw;
       ubase = ba.ustart[k];
       uend = ba.ustart[k + 1] < G1 ? ba.ustart[k + 1] : G1;
+      if constexpr (BATCH) {
+        // read the arguments from shared memory: they are reloaded after each
+        // barrier instead of holding ~40 registers for the whole segment (the
+        // previous segment ended with a barrier, so nobody reads the old copy)
+        const int* src = reinterpret_cast<const int*>(tap);
+        int* dst = reinterpret_cast<int*>(&targs_s);
+        for (int e = tid; e < (int)(sizeof(TiledArgs<T>) / 4); e += NT) dst[e] = src[e];
+        __syncthreads();
+        tap = &targs_s;
+      }
     }
     const TiledArgs<T>& ta = *tap;
     const StageArgs<T>& a = ta.s;
@@ -293,7 +320,7 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
     if (BATCH && !PLAIN && inst != cur_inst) {       // new grid: hand over the previous grid's sums
       if (cur_inst >= 0 && cur_red) flush(cur_err);
       cur_inst = inst;
-      cur_red = (a.reduce != 0 || KIND == ST_DIAG);
+      cur_red = IMAG ? (KIND == ST_S1 || KIND == ST_S3) : (a.reduce != 0 || KIND == ST_DIAG);
       cur_err = ta.err;
     }
     T scale = (T)1;
@@ -304,8 +331,8 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
     const int L = ta.chunk;
 
     const V vscale = splat<T>(scale);
-    const T oms = (PLAIN && a.frame_mode == FRAME_NONE) ? (T)0 : a.omega * scale;
-    const bool rot = PLAIN || a.frame_mode == FRAME_ROT;
+    const T oms = (ANALYTIC && a.frame_mode == FRAME_NONE) ? (T)0 : a.omega * scale;
+    const bool rot = ANALYTIC || a.frame_mode == FRAME_ROT;
     const bool harm = a.pot_mode == POT_HARM;
 
     auto plane_src = [&](int p) -> int {  // x coordinate the TMA reads for plane p
@@ -524,7 +551,7 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
 #pragma unroll
       for (int r = 0; r < R; ++r) {
         tv[r] = (T)0;
-        if (!PLAIN && a.pot_mode == POT_ARR && store && zok && yok[r]) tv[r] = a.trap[rowbase + (size_t)r * nz];
+        if (GEN && a.pot_mode == POT_ARR && store && zok && yok[r]) tv[r] = a.trap[rowbase + (size_t)r * nz];
       }
       const V xv1 = splat<T>(xnext);
       const T pxv = pnext;
@@ -575,7 +602,7 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
         lap = P::fma(ta.k[7], P::add(zr[-2], zr[2]), lap);
         lap = P::fma(ta.k[8], P::add(zr[-1], zr[1]), lap);
         V fr = mk<T>((T)0, (T)0);
-        if (PLAIN || a.frame_mode != FRAME_NONE) {
+        if (ANALYTIC || a.frame_mode != FRAME_NONE) {
           // D1 without 1/(60h): (v3 - v-3) - 9 (v2 - v-2) + 45 (v1 - v-1)
           V dx = P::sub(xp3, xm3);
           dx = P::fma(ta.k[10], P::sub(xp2, xm2), dx);
@@ -599,7 +626,7 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
           lap = P::mul(vscale, lap);
         }
         T pot = pxv + pyv[r] + pzv;
-        if (!PLAIN && a.pot_mode == POT_ARR) pot = tv[r];
+        if (GEN && a.pot_mode == POT_ARR) pot = tv[r];
         const T a2 = c.x * c.x + c.y * c.y;
         const T rho = (T)1 - a2 - pot;
         const V rhs = P::fma(splat<T>(rho), c, P::add(lap, fr));
@@ -620,17 +647,19 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
           if (KIND == ST_S1 || KIND == ST_S2 || KIND == ST_S1W || KIND == ST_S2D) a.w[idx] = wn;
           if (KIND != ST_DIAG && KIND != ST_S1W) a.psi_out[idx] = pn;
           if (!PLAIN) {
-            if (a.reduce == 1) rN.add(pn.x * pn.x + pn.y * pn.y);
-            if (KIND == ST_DIAG || a.reduce == 2) {
+            if (GEN ? a.reduce == 1 : KIND == ST_S3) rN.add(pn.x * pn.x + pn.y * pn.y);
+            if (GEN ? (KIND == ST_DIAG || a.reduce == 2) : KIND == ST_S1) {
               rN.add(a2);
               rK.add(c.x * lap.x + c.y * lap.y);
               rP.add(pot * a2);
               rQ.add(a2 * a2);
               rR.add(c.x * fr.x + c.y * fr.y);
-              const T am = sqrt(a2);
-              rA.add(am);
-              mx = fmax(mx, am);
-              mn = fmin(mn, am);
+              if (GEN) {   // |psi| statistics of Psi_info: diagnostics only, not the imaginary-time loop
+                const T am = sqrt(a2);
+                rA.add(am);
+                mx = fmax(mx, am);
+                mn = fmin(mn, am);
+              }
               nf |= !isfinite(a2);
             }
           }
@@ -663,7 +692,7 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
   }
 
   if (BATCH && !PLAIN && cur_inst >= 0 && cur_red) flush(cur_err);
-  if (!BATCH && !PLAIN && ta0.s.red != nullptr) {
+  if (!BATCH && (GEN || (IMAG && KIND != ST_S2)) && ta0.s.red != nullptr) {
     double acc[NRED];
     acc[0] = rN.val(); acc[1] = rK.val(); acc[2] = rP.val(); acc[3] = rQ.val();
     acc[4] = rR.val(); acc[5] = rA.val(); acc[6] = (double)mx; acc[7] = (double)mn; acc[8] = nf ? 1.0 : 0.0;

@@ -62,6 +62,15 @@ template <typename T> inline bool tiled_plain(const StageArgs<T>& a) {
          a.frame_mode != FRAME_ADV;
 }
 
+// Stage arguments the imaginary-time variant covers: an RK3 stage of the
+// on-device imaginary-time loop (control block set) with harmonic or no
+// potential, rotation or no frame term, and the reduction that stage makes
+// in that loop (stage 1 the energy set, stage 2 none, stage 3 the norm).
+template <typename T> inline bool tiled_imag(const StageArgs<T>& a, int kind) {
+  return a.ctrl != nullptr && a.pot_mode != POT_ARR && a.frame_mode != FRAME_ADV &&
+         ((kind == ST_S1 && a.reduce == 2) || (kind == ST_S2 && a.reduce == 0) || (kind == ST_S3 && a.reduce == 1));
+}
+
 // Launch one stage.  kind: StageKind.  a.psi_in must be one of the two psi
 // buffers of the plan.  *nblk_out receives the grid size (reduction partials).
 template <typename T>

@@ -97,7 +97,10 @@ int plan_shape(const trapbec_params& p, void* const psi[2], void* w, void* w2, i
   auto k6 = stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S1, true, false>;
   auto k7 = stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S2, true, false>;
   auto k8 = stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S3, true, false>;
-  for (auto k : {k1, k2, k3, k4, k5, k6, k7, k8})
+  auto k9 = stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S1, VAR_IMAG, false>;
+  auto k10 = stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S2, VAR_IMAG, false>;
+  auto k11 = stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S3, VAR_IMAG, false>;
+  for (auto k : {k1, k2, k3, k4, k5, k6, k7, k8, k9, k10, k11})
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM) != cudaSuccess) return 4;
   int nb = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k2, G::NT, G::SMEM) != cudaSuccess || nb < 1) return 5;
@@ -180,7 +183,11 @@ int launch_shape(const TiledPlan& plan, int kind, const StageArgs<T>& a, cudaStr
       return 9;
     }
   }
-  if (plain && kind == ST_S1) {
+  if (tiled_imag(a, kind)) {
+    if (kind == ST_S1) stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S1, VAR_IMAG, false><<<grid, G::NT, G::SMEM, st>>>(*tm, *tmw, ta, BatchArgs{});
+    else if (kind == ST_S2) stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S2, VAR_IMAG, false><<<grid, G::NT, G::SMEM, st>>>(*tm, *tmw, ta, BatchArgs{});
+    else stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S3, VAR_IMAG, false><<<grid, G::NT, G::SMEM, st>>>(*tm, *tmw, ta, BatchArgs{});
+  } else if (plain && kind == ST_S1) {
     stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S1, true, false><<<grid, G::NT, G::SMEM, st>>>(*tm, *tmw, ta, BatchArgs{});
   } else if (plain && kind == ST_S2) {
     stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S2, true, false><<<grid, G::NT, G::SMEM, st>>>(*tm, *tmw, ta, BatchArgs{});
