@@ -94,6 +94,15 @@ int tbsg_clip_scale(const float* g, size_t n, float max_norm, float* partials, f
 /* FP32 -> BF16 conversion (inputs of the first layer).                     */
 int tbsg_f32_to_bf16(const float* x, void* y, size_t n, void* stream);
 
+/* Input features of one instance on the device: x receives [nx][ny][nz][16]
+ * BF16 channels (0: harmonic potential wx X^2 + wy Y^2 + wz Z^2 of the scaled
+ * coordinates X = x/Lx ..., clipped at 2; 1: Thomas-Fermi amplitude
+ * sqrt(max(0, 1 - potential)); 2-9: consts[0..7] (host memory); 10-15: 0),
+ * base receives the FP32 amplitude [nx][ny][nz].  Equal to the host recipe
+ * computed in FP64, rounded to FP32 and then to BF16.                      */
+int tbsg_features(void* x, float* base, int nx, int ny, int nz, double lx, double ly, double lz, double wx, double wy,
+                  double wz, const float* consts, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -288,3 +288,22 @@ def test_training_reduces_loss():
     Y = torch.tensor(np.stack(Y)).cuda()
     hist = train(net, X, BASE, Y, epochs=150, lr=2e-3, lr_min=1e-4)
     assert hist[-1] < hist[0] / 5, hist[::10]
+
+
+def test_device_features_equal_host_features():
+    """tbsg_features (the inference and training input path) writes the host
+    recipe's channels rounded to BF16, bit for bit, and the FP32 base exactly."""
+    import torch
+    from trapbec_gb300 import units
+    from trapbec_gb300.surrogate import features, features_device
+    lib = abi.load()
+    for prob, _ in units.ground_state_draws(3, 11, grids=(64, 96), precision=abi.FP32):
+        f, base = features(prob)
+        n = prob.n
+        x = torch.empty(n + (NFEAT,), dtype=torch.bfloat16, device="cuda")
+        b = torch.empty(n, dtype=torch.float32, device="cuda")
+        features_device(lib, prob, x, b)
+        torch.cuda.synchronize()
+        want = torch.from_numpy(f).to(torch.bfloat16)
+        assert torch.equal(x.cpu().view(torch.int16), want.view(torch.int16))
+        assert np.array_equal(b.cpu().numpy().view(np.uint32), base.view(np.uint32))

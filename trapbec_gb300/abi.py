@@ -194,6 +194,8 @@ _PROTOS = {
                             C.c_int, _VP, _VP]),
     "tbsg_clip_scale": (C.c_int, [_VP, C.c_size_t, C.c_float, _VP, _VP, _VP]),
     "tbsg_f32_to_bf16": (C.c_int, [_VP, _VP, C.c_size_t, _VP]),
+    "tbsg_features": (C.c_int, [_VP, _VP, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
+                                C.c_double, C.c_double, C.c_double, _VP, _VP]),
 }
 
 _lib = None

@@ -204,6 +204,40 @@ __global__ void f32_to_bf16_kernel(const float* x, bf16* y, size_t n) {
     y[i] = __float2bfloat16_rn(x[i]);
 }
 
+// Input channels of one instance: one thread per voxel writes the 16 BF16
+// channels (channels-last) and the FP32 Thomas-Fermi amplitude.  Coordinates,
+// harmonic potential and amplitude follow the host recipe operation by
+// operation in FP64 with explicit rounding (no contraction), then round to
+// FP32 and from FP32 to BF16, so the result equals the converted host arrays.
+struct FeatConsts { float c[8]; };   // channels 2-9 (constant over the grid)
+
+__device__ __forceinline__ double feat_coord(int idx, int m, double L) {   // ((2(idx+1)-1)/(2m) L - L/2) / L
+  const double q = __ddiv_rn((double)(2 * idx + 1), 2.0 * (double)m);
+  return __ddiv_rn(__dsub_rn(__dmul_rn(q, L), L / 2.0), L);
+}
+
+__global__ void features_kernel(bf16* __restrict__ x, float* __restrict__ base, int nx, int ny, int nz, double lx,
+                                double ly, double lz, double wx, double wy, double wz, FeatConsts fc) {
+  const size_t n = (size_t)nx * ny * nz;
+  for (size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (size_t)gridDim.x * blockDim.x) {
+    const int k = (int)(v % nz);
+    const int j = (int)((v / nz) % ny);
+    const int i = (int)(v / ((size_t)ny * nz));
+    const double X = feat_coord(i, nx, lx), Y = feat_coord(j, ny, ly), Z = feat_coord(k, nz, lz);
+    const double pot = __dadd_rn(__dadd_rn(__dmul_rn(wx, __dmul_rn(X, X)), __dmul_rn(wy, __dmul_rn(Y, Y))),
+                                 __dmul_rn(wz, __dmul_rn(Z, Z)));
+    const float b = __double2float_rn(sqrt(fmax(0.0, __dsub_rn(1.0, pot))));
+    bf16* o = x + v * 16;
+    o[0] = __float2bfloat16_rn(__double2float_rn(fmin(pot, 2.0)));
+    o[1] = __float2bfloat16_rn(b);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) o[2 + q] = __float2bfloat16_rn(fc.c[q]);
+#pragma unroll
+    for (int q = 10; q < 16; ++q) o[q] = __float2bfloat16_rn(0.0f);
+    base[v] = b;
+  }
+}
+
 inline int done() { return cudaGetLastError() == cudaSuccess ? TBSG_OK : TBSG_ERR_CUDA; }
 
 }  // namespace sg
@@ -296,6 +330,16 @@ int tbsg_clip_scale(const float* g, size_t n, float max_norm, float* partials, f
   cudaStream_t st = (cudaStream_t)stream;
   sumsq_kernel<<<CLIP_BLOCKS, 256, 0, st>>>(g, n, partials);
   clip_final_kernel<<<1, 32, 0, st>>>(partials, CLIP_BLOCKS, max_norm, out);
+  return done();
+}
+
+int tbsg_features(void* x, float* base, int nx, int ny, int nz, double lx, double ly, double lz, double wx, double wy,
+                  double wz, const float* consts, void* stream) {
+  if (!x || !base || !consts || nx <= 0 || ny <= 0 || nz <= 0 || !(lx > 0) || !(ly > 0) || !(lz > 0)) return TBSG_ERR_ARG;
+  FeatConsts fc;
+  for (int q = 0; q < 8; ++q) fc.c[q] = consts[q];
+  const size_t n = (size_t)nx * ny * nz;
+  features_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>((bf16*)x, base, nx, ny, nz, lx, ly, lz, wx, wy, wz, fc);
   return done();
 }
 

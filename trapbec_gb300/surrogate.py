@@ -73,16 +73,28 @@ def features(prob: units.TrapProblem) -> tuple[np.ndarray, np.ndarray]:
     f = np.zeros(n + (NFEAT,), dtype=np.float32)
     f[..., 0] = np.minimum(pot, 2.0)
     f[..., 1] = base
-    wp, wz = prob.omega[0], prob.omega[2]
-    f[..., 2] = math.log10(prob.g) / 3.0
-    f[..., 3] = prob.Omega / (0.7 * wp)
-    f[..., 4] = (wz / wp - 0.5) / 3.5
-    f[..., 5] = p.lx / p.nx
-    f[..., 6] = p.ly / p.ny
-    f[..., 7] = p.lz / p.nz
-    f[..., 8] = prob.Omega / prob.mu
-    f[..., 9] = math.log10(prob.mu / wp) / 3.0
+    f[..., 2:10] = feature_consts(prob)
     return f, base.astype(np.float32)
+
+
+def feature_consts(prob: units.TrapProblem) -> np.ndarray:
+    """Channels 2-9 of `features` (constant over the grid), FP32."""
+    p = prob.to_params()
+    wp, wz = prob.omega[0], prob.omega[2]
+    return np.array([math.log10(prob.g) / 3.0, prob.Omega / (0.7 * wp), (wz / wp - 0.5) / 3.5, p.lx / p.nx,
+                     p.ly / p.ny, p.lz / p.nz, prob.Omega / prob.mu, math.log10(prob.mu / wp) / 3.0],
+                    dtype=np.float32)
+
+
+def features_device(lib, prob: units.TrapProblem, x, base, stream=None) -> None:
+    """`features(prob)` built on the device: x a [S, S, S, 16] BF16 view, base a
+    [S, S, S] FP32 view (CUDA tensors); equal to the host arrays rounded to BF16."""
+    p = prob.to_params()
+    c = feature_consts(prob)
+    rc = lib.tbsg_features(x.data_ptr(), base.data_ptr(), p.nx, p.ny, p.nz, p.lx, p.ly, p.lz, p.harm_wx, p.harm_wy,
+                           p.harm_wz, c.ctypes.data, stream)
+    if rc:
+        raise RuntimeError(f"tbsg_features failed ({rc})")
 
 
 def stable_dtau(prob: units.TrapProblem, frac: float = 0.6) -> float:
@@ -423,6 +435,30 @@ def predict(net: Surrogate, feats: list[np.ndarray], bases: list[np.ndarray]) ->
     return out
 
 
+def predict_problems(net: Surrogate, probs) -> tuple[list[np.ndarray], list[np.ndarray]]:
+    """Predicted amplitudes (host, clipped at 0) and Thomas-Fermi bases (host)
+    of the problems, with the input features built on the device."""
+    t = net.t
+    S = net.S
+    x = t.empty((net.B, S, S, S, NFEAT), dtype=t.bfloat16, device=net.dev)
+    base = t.empty((net.B, S, S, S), dtype=t.float32, device=net.dev)
+    st = net._st()
+    amps, bases = [], []
+    for i in range(0, len(probs), net.B):
+        pb = list(probs[i:i + net.B])
+        while len(pb) < net.B:   # pad the last batch
+            pb.append(pb[-1])
+        for j, prob in enumerate(pb):
+            features_device(net.lib, prob, x[j], base[j], st)
+        amp = net.forward(x, base)
+        res = amp.cpu().numpy()
+        bh = base.cpu().numpy()
+        k = min(net.B, len(probs) - i)
+        amps.extend([np.maximum(res[j], 0.0) for j in range(k)])
+        bases.extend([bh[j].copy() for j in range(k)])
+    return amps, bases
+
+
 # ---- the comparison: NN guess against the Thomas-Fermi guess ---------------------------------------
 
 def _guesses(draws, amps, nn_noise: float):
@@ -478,12 +514,12 @@ def compare(net: Surrogate, draws, tol: float = 1e-10, max_steps: int = 60000, c
     and the L2 distance of the final states (global phase aligned)."""
     t = net.t
     params = [prob.to_params() for prob, _ in draws]
-    feats, bases = zip(*[features(prob) for prob, _ in draws])
-    predict(net, list(feats[:net.B]), list(bases[:net.B]))   # warm-up
+    probs = [prob for prob, _ in draws]
+    predict_problems(net, probs[:net.B])   # warm-up
     ev0, ev1 = t.cuda.Event(enable_timing=True), t.cuda.Event(enable_timing=True)
     t.cuda.synchronize()
     ev0.record()
-    amps = predict(net, list(feats), list(bases))
+    amps, bases = predict_problems(net, probs)   # features on the device, amplitudes back on the host
     ev1.record()
     t.cuda.synchronize()
     infer_ms = ev0.elapsed_time(ev1)
@@ -631,9 +667,7 @@ def main(argv=None):
         Y = torch.empty_like(BASE)
         n_vortex = 0
         for i, (prob, _) in enumerate(train_d):
-            f, base = features(prob)
-            X[i].copy_(torch.from_numpy(f).to(net.dev))
-            BASE[i].copy_(torch.from_numpy(base))
+            features_device(net.lib, prob, X[i], BASE[i])
             tgt, vort = training_target(amps[i]) if a.symmetrize else (amps[i], False)
             n_vortex += vort
             Y[i].copy_(torch.from_numpy(tgt))
