@@ -81,6 +81,13 @@ class ClockSampler:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}",
                                           "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=self.f, stderr=subprocess.DEVNULL)
+            # let nvidia-smi finish starting (its driver initialisation stalls this
+            # process's launches) before the timed region begins: wait for a sample
+            t0 = time.perf_counter()
+            while time.perf_counter() - t0 < 5.0 and self.proc.poll() is None:
+                if os.path.getsize(self.path) > 0:
+                    break
+                time.sleep(0.02)
         except Exception:
             self.proc = None
         return self

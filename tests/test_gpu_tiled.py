@@ -197,3 +197,37 @@ def test_real_time_shape_equals_general_shape():
         out.append((s.get_psi(), s.diag()["energy"]))
     assert np.array_equal(out[0][0].view(np.uint32), out[1][0].view(np.uint32))
     assert out[0][1] == out[1][1]
+
+
+IMAG_VARIANT_CASES = [("harmonic", 0.3, 0.0), ("zero", 0.0, 0.0), ("array", 0.2, 0.0), ("harmonic", 0.0, 0.15)]
+
+
+@pytest.mark.parametrize("prec", [abi.FP64, abi.FP32])
+@pytest.mark.parametrize("pot,omega,vx", IMAG_VARIANT_CASES, ids=lambda v: str(v))
+def test_tiled_imag_rk3_variants(prec, pot, omega, vx):
+    """Imaginary-time RK3 through both kernel variants against the oracle:
+    harmonic / no potential with rotation / no frame take the imaginary-time
+    variant, an array potential or the advective frame the general one."""
+    n = (12, 16, 64)
+    p = params(n=n, L=(6.0, 8.0, 32.0), prec=prec, pot="harmonic" if pot == "harmonic" else pot,
+               harm=(40.0, 50.0, 60.0), omega=omega, vx=vx, dt=0.005)
+    psi = smooth_state(p, seed=17)
+    s, o = Solver(p), Oracle(p)
+    s.set_kernel(2)
+    if pot == "array":
+        trap = np.random.default_rng(5).uniform(0, 1, size=n)
+        s.set_trap(trap)
+        o.set_trap(trap)
+    s.set_psi(psi)
+    o.set_psi(s.get_psi())
+    sg, _ = s.step_imag(80, abi.IMAG_RK3_RENORM, 0.0)
+    so, _ = o.step_imag_rk3(80, 0.0)
+    assert sg == so == 80
+    a, b = s.get_psi().astype(np.complex128), o.get_psi().astype(np.complex128)
+    d, do = s.diag(), o.diag()
+    if prec == abi.FP64:
+        assert rel_err(a, b) < 1e-11
+        assert abs(d["energy"] - do["energy"]) < 1e-12 * abs(do["energy"])
+    else:
+        assert np.linalg.norm(a - b) / np.linalg.norm(b) < 1e-5
+        assert abs(d["energy"] - do["energy"]) < 1e-5 * abs(do["energy"])
