@@ -116,7 +116,9 @@ template <typename T, int TZ, int TY, int R> struct BK {
     auto k1 = stage_tiled_kernel<T, TZ, TY, R, 8, 0, ST_S1, VAR_IMAG, true>;
     auto k2 = stage_tiled_kernel<T, TZ, TY, R, 8, 0, ST_S2, VAR_IMAG, true>;
     auto k3 = stage_tiled_kernel<T, TZ, TY, R, 8, 0, ST_S3, VAR_IMAG, true>;
-    for (auto k : {k1, k2, k3})
+    if (cudaFuncSetAttribute(k1, cudaFuncAttributeMaxDynamicSharedMemorySize, KindGeom<T, G, ST_S1>::SMEM) != cudaSuccess)
+      return 1;
+    for (auto k : {k2, k3})
       if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM) != cudaSuccess) return 1;
     int nb = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k2, G::NT, G::SMEM) != cudaSuccess || nb < 1) return 1;
@@ -128,9 +130,9 @@ template <typename T, int TZ, int TY, int R> struct BK {
     std::memset(&dummy, 0, sizeof(dummy));
     CUtensorMap dm;
     std::memset(&dm, 0, sizeof(dm));
-    if (kind == ST_S1) stage_tiled_kernel<T, TZ, TY, R, 8, 0, ST_S1, VAR_IMAG, true><<<grid, G::NT, G::SMEM, st>>>(dm, dm, dummy, ba);
-    else if (kind == ST_S2) stage_tiled_kernel<T, TZ, TY, R, 8, 0, ST_S2, VAR_IMAG, true><<<grid, G::NT, G::SMEM, st>>>(dm, dm, dummy, ba);
-    else stage_tiled_kernel<T, TZ, TY, R, 8, 0, ST_S3, VAR_IMAG, true><<<grid, G::NT, G::SMEM, st>>>(dm, dm, dummy, ba);
+    if (kind == ST_S1) stage_tiled_kernel<T, TZ, TY, R, 8, 0, ST_S1, VAR_IMAG, true><<<grid, G::NT, KindGeom<T, G, ST_S1>::SMEM, st>>>(dm, dm, dummy, ba);
+    else if (kind == ST_S2) stage_tiled_kernel<T, TZ, TY, R, 8, 0, ST_S2, VAR_IMAG, true><<<grid, G::NT, KindGeom<T, G, ST_S2>::SMEM, st>>>(dm, dm, dummy, ba);
+    else stage_tiled_kernel<T, TZ, TY, R, 8, 0, ST_S3, VAR_IMAG, true><<<grid, G::NT, KindGeom<T, G, ST_S3>::SMEM, st>>>(dm, dm, dummy, ba);
   }
   static int encode(const trapbec_params& p, void* const psi[2], void* w, CUtensorMap* tm, CUtensorMap* tmw) {
     return encode_maps<T, TZ, TY, R, 8, 0>(p, psi, w, tm, tmw);

@@ -166,17 +166,24 @@ template <typename T, int TZ, int TY, int R, int NSLOT = 8, int MINB = 0> struct
   static constexpr int MIN_BLOCKS = MINB > 0 ? MINB : ((sizeof(T) == 4 && NT < 512) ? 2 : 1);
 };
 
-// Ring of one stage kind.  The deferred S2 holds a ghosted w1 box beside the
-// psi box in every slot, with as many slots as fit in the shared memory the
-// other kinds use (at least 6), so all kinds keep the same CTAs per SM.
+// Ring of one stage kind, in the shared memory of the shape (G::SMEM) so all
+// kinds keep the same CTAs per SM.  Stages 2 and 3 use the shape's slots (psi
+// box + w tile).  Kinds that read no w (stage 1, Euler, diagnostics) keep the
+// psi box only and as many slots as fit (up to 12): a deeper prefetch.  The
+// deferred S2 holds a ghosted w1 box beside the psi box (at least 6 slots).
 template <typename T, class G, int KIND> struct KindGeom {
   static constexpr bool DEFER = (KIND == ST_S2D);
-  static constexpr int W_BYTES = DEFER ? G::SLOT_BYTES : G::W_BYTES;
-  static constexpr int SLOT_STRIDE = DEFER ? (G::W_OFF + G::SLOT_BYTES + 127) / 128 * 128 : G::SLOT_STRIDE;
+  static constexpr bool NO_W = (KIND == ST_S1 || KIND == ST_S1W || KIND == ST_EU || KIND == ST_DIAG);
+  static constexpr int W_BYTES = DEFER ? G::SLOT_BYTES : (NO_W ? 0 : G::W_BYTES);
+  static constexpr int SLOT_STRIDE =
+      DEFER ? (G::W_OFF + G::SLOT_BYTES + 127) / 128 * 128 : (NO_W ? G::W_OFF : G::SLOT_STRIDE);
   static constexpr int SLOT_STRIDE_ELEMS = SLOT_STRIDE / (int)sizeof(c_t<T>);
-  static constexpr int FIT = (G::S * G::SLOT_STRIDE) / SLOT_STRIDE;
-  static constexpr int S = DEFER ? (FIT < 6 ? 6 : (FIT > G::S ? G::S : FIT)) : G::S;
+  static constexpr int FIT_D = (G::S * G::SLOT_STRIDE) / SLOT_STRIDE;
+  static constexpr int FIT = (G::SMEM - 8) / (SLOT_STRIDE + 8);
+  static constexpr int S = DEFER ? (FIT_D < 6 ? 6 : (FIT_D > G::S ? G::S : FIT_D))
+                                 : (NO_W ? (FIT > 12 ? 12 : FIT) : G::S);
   static constexpr int SMEM = S * SLOT_STRIDE + (S + 1) * 8;
+  static_assert(DEFER || SMEM <= G::SMEM, "a kind's ring fits the shape's shared memory");
 };
 
 // Work description of a batched launch: the concatenated units of all active

@@ -4,6 +4,7 @@
 #include <cudaTypedefs.h>
 
 #include <cstring>
+#include <utility>
 
 #include "kernels_tiled.cuh"
 
@@ -100,8 +101,16 @@ int plan_shape(const trapbec_params& p, void* const psi[2], void* w, void* w2, i
   auto k9 = stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S1, VAR_IMAG, false>;
   auto k10 = stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S2, VAR_IMAG, false>;
   auto k11 = stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S3, VAR_IMAG, false>;
-  for (auto k : {k1, k2, k3, k4, k5, k6, k7, k8, k9, k10, k11})
-    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM) != cudaSuccess) return 4;
+  const int sm_s1 = KindGeom<T, G, ST_S1>::SMEM, sm_eu = KindGeom<T, G, ST_EU>::SMEM;
+  const int sm_dg = KindGeom<T, G, ST_DIAG>::SMEM;
+  const std::pair<const void*, int> ks[] = {{(const void*)k1, sm_s1}, {(const void*)k2, G::SMEM},
+                                            {(const void*)k3, G::SMEM}, {(const void*)k4, sm_eu},
+                                            {(const void*)k5, sm_dg}, {(const void*)k6, sm_s1},
+                                            {(const void*)k7, G::SMEM}, {(const void*)k8, G::SMEM},
+                                            {(const void*)k9, sm_s1}, {(const void*)k10, G::SMEM},
+                                            {(const void*)k11, G::SMEM}};
+  for (const auto& k : ks)
+    if (cudaFuncSetAttribute(k.first, cudaFuncAttributeMaxDynamicSharedMemorySize, k.second) != cudaSuccess) return 4;
   int nb = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k2, G::NT, G::SMEM) != cudaSuccess || nb < 1) return 5;
   // the deferred real-time form (FP32): S1 stores w1 only, S2 forms psi1 from
@@ -115,7 +124,8 @@ int plan_shape(const trapbec_params& p, void* const psi[2], void* w, void* w2, i
       int nbd = 0;
       if (encode_box<T, TZ, TY, R, NS, MB>(p, w, true, &q.tmwg) == 0 &&
           encode_box<T, TZ, TY, R, NS, MB>(p, w2, false, &q.tmw1) == 0 &&
-          cudaFuncSetAttribute(kw, cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM) == cudaSuccess &&
+          cudaFuncSetAttribute(kw, cudaFuncAttributeMaxDynamicSharedMemorySize, KindGeom<T, G, ST_S1W>::SMEM) ==
+              cudaSuccess &&
           cudaFuncSetAttribute(kd, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_D) == cudaSuccess &&
           cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nbd, kd, G::NT, SMEM_D) == cudaSuccess && nbd >= nb) {
         q.w_base[1] = w2;
@@ -170,7 +180,7 @@ int launch_shape(const TiledPlan& plan, int kind, const StageArgs<T>& a, cudaStr
     if constexpr (sizeof(T) == 4) {
       if (!plain || !plan.defer_ok) return 9;
       if (kind == ST_S1W) {
-        stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S1W, true, false><<<grid, G::NT, G::SMEM, st>>>(*tm, *tmw, ta, BatchArgs{});
+        stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S1W, true, false><<<grid, G::NT, KindGeom<T, G, ST_S1W>::SMEM, st>>>(*tm, *tmw, ta, BatchArgs{});
       } else {
         // w1 (ghosted boxes) in, w2 out
         if ((const void*)a.w_in != plan.w_base[0] || (const void*)a.w != plan.w_base[1]) return 10;
@@ -184,22 +194,22 @@ int launch_shape(const TiledPlan& plan, int kind, const StageArgs<T>& a, cudaStr
     }
   }
   if (tiled_imag(a, kind)) {
-    if (kind == ST_S1) stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S1, VAR_IMAG, false><<<grid, G::NT, G::SMEM, st>>>(*tm, *tmw, ta, BatchArgs{});
-    else if (kind == ST_S2) stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S2, VAR_IMAG, false><<<grid, G::NT, G::SMEM, st>>>(*tm, *tmw, ta, BatchArgs{});
-    else stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S3, VAR_IMAG, false><<<grid, G::NT, G::SMEM, st>>>(*tm, *tmw, ta, BatchArgs{});
+    if (kind == ST_S1) stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S1, VAR_IMAG, false><<<grid, G::NT, KindGeom<T, G, ST_S1>::SMEM, st>>>(*tm, *tmw, ta, BatchArgs{});
+    else if (kind == ST_S2) stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S2, VAR_IMAG, false><<<grid, G::NT, KindGeom<T, G, ST_S2>::SMEM, st>>>(*tm, *tmw, ta, BatchArgs{});
+    else stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S3, VAR_IMAG, false><<<grid, G::NT, KindGeom<T, G, ST_S3>::SMEM, st>>>(*tm, *tmw, ta, BatchArgs{});
   } else if (plain && kind == ST_S1) {
-    stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S1, true, false><<<grid, G::NT, G::SMEM, st>>>(*tm, *tmw, ta, BatchArgs{});
+    stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S1, true, false><<<grid, G::NT, KindGeom<T, G, ST_S1>::SMEM, st>>>(*tm, *tmw, ta, BatchArgs{});
   } else if (plain && kind == ST_S2) {
-    stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S2, true, false><<<grid, G::NT, G::SMEM, st>>>(*tm, *tmw, ta, BatchArgs{});
+    stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S2, true, false><<<grid, G::NT, KindGeom<T, G, ST_S2>::SMEM, st>>>(*tm, *tmw, ta, BatchArgs{});
   } else if (plain && kind == ST_S3) {
-    stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S3, true, false><<<grid, G::NT, G::SMEM, st>>>(*tm, *tmw, ta, BatchArgs{});
+    stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S3, true, false><<<grid, G::NT, KindGeom<T, G, ST_S3>::SMEM, st>>>(*tm, *tmw, ta, BatchArgs{});
   } else {
     switch (kind) {
-      case ST_S1: stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S1, false, false><<<grid, G::NT, G::SMEM, st>>>(*tm, *tmw, ta, BatchArgs{}); break;
-      case ST_S2: stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S2, false, false><<<grid, G::NT, G::SMEM, st>>>(*tm, *tmw, ta, BatchArgs{}); break;
-      case ST_S3: stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S3, false, false><<<grid, G::NT, G::SMEM, st>>>(*tm, *tmw, ta, BatchArgs{}); break;
-      case ST_EU: stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_EU, false, false><<<grid, G::NT, G::SMEM, st>>>(*tm, *tmw, ta, BatchArgs{}); break;
-      case ST_DIAG: stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_DIAG, false, false><<<grid, G::NT, G::SMEM, st>>>(*tm, *tmw, ta, BatchArgs{}); break;
+      case ST_S1: stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S1, false, false><<<grid, G::NT, KindGeom<T, G, ST_S1>::SMEM, st>>>(*tm, *tmw, ta, BatchArgs{}); break;
+      case ST_S2: stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S2, false, false><<<grid, G::NT, KindGeom<T, G, ST_S2>::SMEM, st>>>(*tm, *tmw, ta, BatchArgs{}); break;
+      case ST_S3: stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S3, false, false><<<grid, G::NT, KindGeom<T, G, ST_S3>::SMEM, st>>>(*tm, *tmw, ta, BatchArgs{}); break;
+      case ST_EU: stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_EU, false, false><<<grid, G::NT, KindGeom<T, G, ST_EU>::SMEM, st>>>(*tm, *tmw, ta, BatchArgs{}); break;
+      case ST_DIAG: stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_DIAG, false, false><<<grid, G::NT, KindGeom<T, G, ST_DIAG>::SMEM, st>>>(*tm, *tmw, ta, BatchArgs{}); break;
       default: return 7;
     }
   }
