@@ -243,7 +243,9 @@ def warmstart_leg(args):
         "steps_ratio_median": r["steps_ratio_median"], "steps_ratio_median_nn_used": r["steps_ratio_median_nn_used"],
         "steps_ratio_total_both_converged": r["steps_ratio_total_both_converged"],
         "device_ms_tf": r["tf"]["solve_ms_device"], "device_ms_nn": r["nn"]["solve_ms_device"],
-        "nn_inference_ms": r["nn_inference_ms"], "wall_ratio_device": r["wall_ratio_device"],
+        "nn_inference_ms": r["nn_inference_ms"], "selection_ms_device": r["selection_ms_device"],
+        "wall_ratio_device": r["wall_ratio_device"],
+        "wall_ratio_note": "TF solve / (NN-arm solve + inference + the selector's energy evaluations), device times",
         "final_energy_rel_diff_max": r["final_energy_rel_diff_max"],
         "guess_rmse_median_tf": med(r["guess_rmse_tf"]), "guess_rmse_median_nn": med(r["guess_rmse_nn"]),
         "fallback": "TF guess where its energy at the same norm is lower (rotating, vortex states)",

@@ -69,3 +69,32 @@ def test_batch_fp32_relaxes_and_counts_launches():
         d = o.diag()
         assert abs(out["mu"][i] / d["mu"] - 1) < 1e-5, (i, out["mu"][i], d["mu"])
         assert out["steps"][i] < 3000
+
+
+def test_batch_stops_at_max_steps_and_one_step_reports_the_start_energy():
+    """A solve never runs past max_steps (also when it is not a multiple of
+    check_every), and a one-step solve reports the energy of the starting
+    state (the stage-1 reduction of the first step)."""
+    ps = _mixed_params(abi.FP64)
+    psis = [smooth_state(p, seed=60 + i) for i, p in enumerate(ps)]
+    b = BatchSolver(ps)
+    for i, psi in enumerate(psis):
+        b.set_psi(i, psi)
+    out = b.solve(max_steps=1, tol=0.0, check_every=200)
+    assert out["steps"] == [1, 1, 1]
+    for i, p in enumerate(ps):
+        s = Solver(p)
+        s.set_psi(psis[i])
+        e0 = s.diag()["energy"]
+        assert abs(out["energy"][i] - e0) < 1e-12 * abs(e0), i
+        s.close()
+    b2 = BatchSolver(ps)
+    for i, psi in enumerate(psis):
+        b2.set_psi(i, psi)
+    out = b2.solve(max_steps=13, tol=0.0, check_every=4)
+    assert out["steps"] == [13, 13, 13]
+    for i, p in enumerate(ps):
+        o = Oracle(p)
+        o.set_psi(psis[i])
+        o.step_imag_rk3(13, 0.0)
+        assert rel_err(b2.get_psi(i), o.get_psi()) < 1e-11, i

@@ -457,7 +457,7 @@ template <typename T> int solve_impl(trapbec_batch* b, int max_steps, double tol
   }
   BCK(cudaMemcpyAsync(b->d_ctrl, b->h_ctrl, sizeof(ImagCtrl) * b->ninst, cudaMemcpyHostToDevice, b->st));
   cudaGraphExec_t gexec = nullptr;
-  int graph_nact = -1;
+  int graph_nact = -1, graph_k = -1;
   BCK(cudaEventRecord(b->e0, b->st));
   int rc = TRAPBEC_OK;
   while (true) {
@@ -467,23 +467,29 @@ template <typename T> int solve_impl(trapbec_batch* b, int max_steps, double tol
       if (!c.converged && !c.nonfinite && b->in[i].steps < max_steps) act.push_back(i);
     }
     if (act.empty()) break;
+    // the active instances have made the same number of steps in this call; a
+    // replay never takes them past max_steps
+    int left = max_steps;
+    for (int i : act) left = std::min(left, max_steps - b->in[i].steps);
+    const int kk = std::min(k, std::max(1, left));
     if ((rc = upload_work<T>(b, s, act))) break;
-    if ((int)act.size() != graph_nact) {   // capture the K-step loop for this work-list size
+    if ((int)act.size() != graph_nact || kk != graph_k) {   // capture the kk-step loop for this work-list size
       if (gexec) cudaGraphExecDestroy(gexec);
       gexec = nullptr;
       cudaGraph_t g = nullptr;
       if (cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) { rc = TRAPBEC_ERR_CUDA; break; }
-      int erc = enqueue_steps<T>(b, s, k, (int)act.size());
+      int erc = enqueue_steps<T>(b, s, kk, (int)act.size());
       cudaError_t ce = cudaStreamEndCapture(b->st, &g);
       if (erc || ce != cudaSuccess) { set_error("batch: graph capture failed"); rc = TRAPBEC_ERR_CUDA; break; }
       ce = cudaGraphInstantiate(&gexec, g, 0);
       cudaGraphDestroy(g);
       if (ce != cudaSuccess) { set_error("batch: graph instantiation failed"); rc = TRAPBEC_ERR_CUDA; break; }
       graph_nact = (int)act.size();
-      b->launches -= 5LL * k;  // counted below per replay
+      graph_k = kk;
+      b->launches -= 5LL * kk;  // counted below per replay
     }
     if (cudaGraphLaunch(gexec, b->st) != cudaSuccess) { set_error("batch: graph launch failed"); rc = TRAPBEC_ERR_CUDA; break; }
-    b->launches += 5LL * k;
+    b->launches += 5LL * kk;
     if (cudaMemcpyAsync(b->h_ctrl, b->d_ctrl, sizeof(ImagCtrl) * b->ninst, cudaMemcpyDeviceToHost, b->st) ||
         cudaStreamSynchronize(b->st)) {
       set_error("batch: control read-back failed");

@@ -535,6 +535,7 @@ def compare(net: Surrogate, draws, tol: float = 1e-10, max_steps: int = 60000, c
     e_tf, _ = _relax(params, tf_states, tol, max_steps, check_every, energy_only=True)
     e_nn, _ = _relax(params, nn_states, tol, max_steps, check_every, energy_only=True)
     use_nn = [(not bad) and en < et for bad, en, et in zip(unreasonable, e_nn["energy"], e_tf["energy"])]
+    sel_ms = e_tf["solve_ms_device"] + e_nn["solve_ms_device"]   # the selector's energy evaluations
     chosen = [n if u else f for n, f, u in zip(nn_states, tf_states, use_nn)]
     res, finals = {}, {}
     res["tf"], finals["tf"] = _relax(params, tf_states, tol, max_steps, check_every)
@@ -561,7 +562,8 @@ def compare(net: Surrogate, draws, tol: float = 1e-10, max_steps: int = 60000, c
         "steps_ratio_median_nn_used": float(np.median(ratio[np.array(use_nn)])) if any(use_nn) else None,
         "steps_ratio_total": float(s_tf.sum() / max(s_nn.sum(), 1)),
         "steps_ratio_total_both_converged": float(s_tf[both].sum() / max(s_nn[both].sum(), 1)) if both.any() else None,
-        "wall_ratio_device": res["tf"]["solve_ms_device"] / (res["nn"]["solve_ms_device"] + infer_ms),
+        "selection_ms_device": sel_ms,
+        "wall_ratio_device": res["tf"]["solve_ms_device"] / (res["nn"]["solve_ms_device"] + infer_ms + sel_ms),
         "final_energy_rel_diff_max": float(max(de)), "final_l2_rel": l2,
         "guess_rmse_tf": [rms(np.abs(f), b_) for f, b_ in zip(finals["tf"], bases)],
         "guess_rmse_nn": [rms(np.abs(f), a_) for f, a_ in zip(finals["tf"], amps)],
