@@ -351,15 +351,18 @@ def run_gpu_arm(args):
         e2e_call(0)                                                # untimed warm-up call
         torch.cuda.synchronize()
         t0 = time.perf_counter()
+        call_ms = []
         for r in range(reps):
+            tc = time.perf_counter()
             e2e_call(r)
+            call_ms.append(1e3 * (time.perf_counter() - tc))
         torch.cuda.synchronize()
         et = time.perf_counter() - t0
         e2e = {"value": world * cells * shots * reps / et, "unit": UNIT,
                "h2d_bytes_per_step": int(cells * host.itemsize / shots),
                "d2h_bytes_per_step": int(cells * host.itemsize / shots),
                "shots": shots, "host_buffers": "pinned (page-locked) input and output arrays",
-               "calls": reps,
+               "calls": reps, "call_ms": call_ms,
                "note": "per call: set_psi (H2D) + shots RK3 steps + diag + get_psi (D2H); one untimed call first; "
                        "host<->device copies run at the link's ~200 GB/s"}
 
