@@ -132,3 +132,27 @@ def test_driver_stops_with_error_file_on_nonfinite_restart(tmp_path):
     r = _run(tmp_path, CPARAM.format(nsteps=20))
     assert r.returncode == 1
     assert "non-finite" in (tmp_path / "ERROR").read_text()
+
+
+def test_bad_arguments_return_status_and_leave_the_context_usable():
+    """Invalid arguments to the kernel-selection and form entry points are
+    error codes (never a launch), and the context keeps stepping afterwards."""
+    import ctypes as C
+    from trapbec_gb300 import Solver
+    p = params(n=(12, 32, 128), L=(6.0, 16.0, 64.0), prec=abi.FP32, pot="harmonic", harm=(3.0, 4.0, 5.0),
+               omega=0.2, dt=0.01)
+    s = Solver(p)
+    lib = s.lib
+    assert lib.trapbec_set_kernel(s.ctx, 3, 0, 0) == abi.ERR_ARG            # no such kernel kind
+    assert lib.trapbec_set_kernel(s.ctx, 2, -99, 0) == abi.ERR_UNSUPPORTED  # no such built shape
+    assert lib.trapbec_set_kernel(s.ctx, 2, 48, 48) == abi.ERR_UNSUPPORTED  # no shape of this size
+    assert lib.trapbec_set_stage_form(s.ctx, 2) == abi.ERR_ARG
+    assert lib.trapbec_set_chunk(s.ctx, -1) == abi.ERR_ARG
+    tz, ty = C.c_int(0), C.c_int(0)
+    assert lib.trapbec_get_tile_shape(s.ctx, 1, None, C.byref(ty)) == abi.ERR_ARG
+    assert lib.trapbec_get_tile_shape(s.ctx, 1, C.byref(tz), C.byref(ty)) == abi.OK
+    assert (tz.value, ty.value) == (64, 32)
+    s.set_psi(smooth_state(p, seed=3))
+    n0 = s.diag()["intpsi2"]
+    s.step_rt(5)
+    assert abs(s.diag()["intpsi2"] / n0 - 1) < 1e-4

@@ -1147,9 +1147,11 @@ int trapbec_get_scalar(trapbec_ctx* c, int which, double* v) {
 
 int trapbec_set_kernel(trapbec_ctx* c, int kind, int tile_z, int tile_y) {
   if (!c || kind < 0 || kind > 2) return TRAPBEC_ERR_ARG;
-  c->kernel_kind = kind;
-  if (kind == 1) return TRAPBEC_OK;
-  int shape = 0;
+  if (kind == 1) {
+    c->kernel_kind = 1;
+    return TRAPBEC_OK;
+  }
+  int shape = 0;   // the context changes only once the request is valid
   const int ns = c->prec == TRAPBEC_FP64 ? tiled_nshapes<double>() : tiled_nshapes<float>();
   if (tile_z < 0) {  // select a built shape by index: tile_z = -(index + 1)
     shape = -tile_z - 1;
@@ -1175,6 +1177,7 @@ int trapbec_set_kernel(trapbec_ctx* c, int kind, int tile_z, int tile_y) {
     set_error("tiled kernel not available for this grid / tile shape");
     return TRAPBEC_ERR_UNSUPPORTED;
   }
+  c->kernel_kind = kind;
   return TRAPBEC_OK;
 }
 
