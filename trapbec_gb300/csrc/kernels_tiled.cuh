@@ -12,7 +12,8 @@
 // Staging: each x-plane of a tile is copied with one TMA box of
 // (TZ + 2*HZ) x (TY + 6) complex values (the 3-deep y/z ghost planes
 // included) into an S-slot shared-memory ring; slots are guarded by
-// mbarriers and refilled S planes ahead.  Out-of-range boxes come back zero,
+// mbarriers and refilled S planes ahead (S per stage kind: KindGeom).
+// Out-of-range boxes come back zero,
 // which is the reference's 'zero' ghost fill (ghost.f90:53-55); for 'solid'
 // and periodic sides the x-plane coordinate is remapped before the copy and
 // the y/z ghost cells of boundary tiles are patched from global memory.
