@@ -13,9 +13,9 @@
 // (TZ + 2*HZ) x (TY + 6) complex values (the 3-deep y/z ghost planes
 // included) into an S-slot shared-memory ring; slots are guarded by
 // mbarriers and refilled S planes ahead (S per stage kind: KindGeom).
-// Out-of-range boxes come back zero,
-// which is the reference's 'zero' ghost fill (ghost.f90:53-55); for 'solid'
-// and periodic sides the x-plane coordinate is remapped before the copy and
+// Out-of-range boxes come back zero, which is the reference's 'zero' ghost
+// fill (ghost.f90:53-55); for 'solid' and periodic sides the x-plane
+// coordinate is remapped before the copy and
 // the y/z ghost cells of boundary tiles are patched from global memory.
 // The x-direction neighbours live in a 7-deep register queue per thread
 // whose rotation is resolved at compile time (the x loop is unrolled by 7).
