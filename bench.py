@@ -248,7 +248,9 @@ def warmstart_leg(args):
         "wall_ratio_note": "TF solve / (NN-arm solve + inference + the selector's energy evaluations), device times",
         "final_energy_rel_diff_max": r["final_energy_rel_diff_max"],
         "guess_rmse_median_tf": med(r["guess_rmse_tf"]), "guess_rmse_median_nn": med(r["guess_rmse_nn"]),
-        "fallback": "TF guess where its energy at the same norm is lower (rotating, vortex states)",
+        "fallback": "TF guess where its energy at the same norm is lower, and for Omega/omega_perp > 0.5 "
+                    "(bistable: vortex nucleation from the TF guess)",
+        "tf_kept_fast_rotation": r["tf_kept_fast_rotation"],
     }
 
 

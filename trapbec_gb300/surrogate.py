@@ -329,10 +329,17 @@ def _tf_noise(b, i, ini, noise=True):
                  noise_amp=ini["noise_amp"] if noise else 0.0)
 
 
-def ground_states(draws, max_steps: int, tol: float, frac: float = 0.6, chunk: int = 32):
+def ground_states(draws, max_steps: int, tol: float, frac: float = 0.6, chunk: int = 32, omega_zero: bool = True):
     """Relax each draw from its Thomas-Fermi + noise guess with the batched
     RK3 solver at `frac` of its own stability limit (the fixed point does not
-    depend on the step) and return the amplitudes |psi| (FP32) and stats."""
+    depend on the step) and return the amplitudes |psi| (FP32) and stats.
+
+    omega_zero: relax without the rotation term.  In these axisymmetric traps a
+    real, current-free state has <Lz> = 0, so the vortex-free stationary state
+    of the rotating frame -- the state an imaginary-time relaxation from the
+    vortex-free guesses settles in before any vortex nucleates -- is the
+    non-rotating ground state; relaxing at Omega = 0 gives that target without
+    the symmetry-broken vortex states a long rotating relaxation can reach."""
     from .batch import BatchSolver
     amps, info = [], []
     for c0 in range(0, len(draws), chunk):
@@ -340,7 +347,8 @@ def ground_states(draws, max_steps: int, tol: float, frac: float = 0.6, chunk: i
         ps = []
         for prob, _ in part:
             q = units.TrapProblem(n=prob.n, box=prob.box, omega=prob.omega, g=prob.g, mu=prob.mu,
-                                  dt=stable_dtau(prob, frac), Omega=prob.Omega, precision=prob.precision)
+                                  dt=stable_dtau(prob, frac), Omega=0.0 if omega_zero else prob.Omega,
+                                  precision=prob.precision)
             ps.append(q.to_params())
         b = BatchSolver(ps)
         for i, (_, ini) in enumerate(part):
@@ -503,13 +511,18 @@ def _relax(params, states, tol, max_steps, check_every, energy_only=False):
 
 
 def compare(net: Surrogate, draws, tol: float = 1e-10, max_steps: int = 60000, check_every: int = 200,
-            nn_noise: float = 1e-2) -> dict:
+            nn_noise: float = 1e-2, nn_omega_max: float = 0.5) -> dict:
     """Relax the held-out draws twice at the workload's step (dtau = 0.002):
     from the Thomas-Fermi + 1e-2 noise guess (the plain method) and with the
     surrogate.  The surrogate's initial state is its amplitude plus the same
     seeded noise pattern at `nn_noise`, unless the Thomas-Fermi guess has the
     lower energy at the same norm (or the prediction is unreasonable), in
-    which case the Thomas-Fermi guess is the fallback.  Reports steps and
+    which case the Thomas-Fermi guess is the fallback.  Above Omega/omega_perp
+    = `nn_omega_max` the Thomas-Fermi guess is always kept: there the
+    relaxation is bistable -- from the Thomas-Fermi guess it can nucleate
+    vortices and end in a vortex state 10-20% lower in energy, from the
+    surrogate's guess (close to the vortex-free stationary state) it stops
+    there -- so the two guesses would not lead to the same state.  Reports steps and
     device time to the relative energy-change tolerance, the final energies
     and the L2 distance of the final states (global phase aligned)."""
     t = net.t
@@ -534,7 +547,9 @@ def compare(net: Surrogate, draws, tol: float = 1e-10, max_steps: int = 60000, c
     # the selector: the guess with the lower energy at the same norm
     e_tf, _ = _relax(params, tf_states, tol, max_steps, check_every, energy_only=True)
     e_nn, _ = _relax(params, nn_states, tol, max_steps, check_every, energy_only=True)
-    use_nn = [(not bad) and en < et for bad, en, et in zip(unreasonable, e_nn["energy"], e_tf["energy"])]
+    slow_rot = [prob.Omega <= nn_omega_max * prob.omega[0] for prob, _ in draws]
+    use_nn = [(not bad) and ok and en < et
+              for bad, ok, en, et in zip(unreasonable, slow_rot, e_nn["energy"], e_tf["energy"])]
     sel_ms = e_tf["solve_ms_device"] + e_nn["solve_ms_device"]   # the selector's energy evaluations
     chosen = [n if u else f for n, f, u in zip(nn_states, tf_states, use_nn)]
     res, finals = {}, {}
@@ -555,6 +570,7 @@ def compare(net: Surrogate, draws, tol: float = 1e-10, max_steps: int = 60000, c
     return {
         "instances": len(draws), "tol_rel_dE": tol, "dtau_trap_units": draws[0][0].dt, "nn_noise": nn_noise,
         "nn_used": int(sum(use_nn)), "nn_unreasonable": int(sum(unreasonable)),
+        "nn_omega_max": nn_omega_max, "tf_kept_fast_rotation": int(len(draws) - sum(slow_rot)),
         "guess_energy_tf": e_tf["energy"], "guess_energy_nn": e_nn["energy"],
         "tf": res["tf"], "nn": res["nn"], "nn_inference_ms": infer_ms,
         "steps_ratio_per_instance": ratio.tolist(),
@@ -565,6 +581,7 @@ def compare(net: Surrogate, draws, tol: float = 1e-10, max_steps: int = 60000, c
         "selection_ms_device": sel_ms,
         "wall_ratio_device": res["tf"]["solve_ms_device"] / (res["nn"]["solve_ms_device"] + infer_ms + sel_ms),
         "final_energy_rel_diff_max": float(max(de)), "final_l2_rel": l2,
+        "same_end_state": int(sum(x <= 1e-4 for x in de)),   # |dE|/|E| <= 1e-4 between the two final states
         "guess_rmse_tf": [rms(np.abs(f), b_) for f, b_ in zip(finals["tf"], bases)],
         "guess_rmse_nn": [rms(np.abs(f), a_) for f, a_ in zip(finals["tf"], amps)],
     }
@@ -627,6 +644,9 @@ def main(argv=None):
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--gen-steps", type=int, default=8000, help="relaxation steps per training ground state")
     ap.add_argument("--gen-frac", type=float, default=0.85, help="fraction of the RK3 stability limit for data")
+    ap.add_argument("--target-omega", choices=["zero", "draw"], default="zero",
+                    help="training ground states relaxed without rotation (the vortex-free stationary state) "
+                         "or at each draw's Omega")
     ap.add_argument("--epochs", type=int, default=60)
     ap.add_argument("--batch", type=int, default=2)
     ap.add_argument("--lr", type=float, default=5e-4)
@@ -660,7 +680,9 @@ def main(argv=None):
         rep["weights"] = a.weights
     else:
         t0 = time.perf_counter()
-        amps, info = ground_states(train_d, max_steps=a.gen_steps, tol=1e-12, frac=a.gen_frac)
+        amps, info = ground_states(train_d, max_steps=a.gen_steps, tol=1e-12, frac=a.gen_frac,
+                                   omega_zero=a.target_omega == "zero")
+        rep["target_omega"] = a.target_omega
         rep["gen_s"] = time.perf_counter() - t0
         rep["gen_rel_dE_median"] = float(np.median([i["rel"] for i in info]))
         log(f"generated {len(amps)} ground states in {rep['gen_s']:.1f} s, median rel dE {rep['gen_rel_dE_median']:.2e}")
@@ -693,7 +715,8 @@ def main(argv=None):
         rep["compare"].append(cmp_)
         log(json.dumps({k: cmp_[k] for k in ("nn_noise", "nn_used", "steps_ratio_median", "steps_ratio_median_nn_used",
                                               "steps_ratio_total", "steps_ratio_total_both_converged",
-                                              "wall_ratio_device", "final_energy_rel_diff_max")}))
+                                              "wall_ratio_device", "final_energy_rel_diff_max", "same_end_state",
+                                              "tf_kept_fast_rotation")}))
     if a.json:
         with open(a.json, "w") as f:
             json.dump(rep, f, indent=1)
