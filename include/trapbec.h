@@ -255,8 +255,9 @@ int trapbec_get_scalar(trapbec_ctx* ctx, int which, double* value);
  * allows it), 1 = simple per-cell kernel, 2 = tiled kernel (error if the
  * grid does not allow it).  tile_z/tile_y pick a built tile shape for every
  * launch (tile_z = -(i+1): built shape number i); 0, 0 restores the defaults:
- * shape 0 for reductions and imaginary time, the real-time shape (64 x 32
- * tiles in FP32) for the plain real-time stages.                           */
+ * the first built shape that fits the grid (shape 0, 128 x 8 tiles in FP32,
+ * where it does) for reductions and imaginary time, the real-time shape
+ * (64 x 32 tiles in FP32) for the plain real-time stages where it fits.     */
 int trapbec_set_kernel(trapbec_ctx* ctx, int kind, int tile_z, int tile_y);
 
 /* Tile shape the tiled kernel runs with: of the plain real-time stages

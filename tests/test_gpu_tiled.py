@@ -231,3 +231,22 @@ def test_tiled_imag_rk3_variants(prec, pot, omega, vx):
     else:
         assert np.linalg.norm(a - b) / np.linalg.norm(b) < 1e-5
         assert abs(d["energy"] - do["energy"]) < 1e-5 * abs(do["energy"])
+
+
+def test_default_plan_falls_back_to_a_shape_that_fits():
+    """Solid walls need whole tiles: at nz = 64 the (128 x 8) shape cannot
+    plan, so the default plans take the first built shape that does (64 x 8)
+    instead of the per-cell kernel; results still match the oracle."""
+    n = (12, 16, 64)
+    p = params(n=n, L=(6.0, 8.0, 32.0), prec=abi.FP32, bc=abi.BC_SOLID, pot="harmonic", harm=(40.0, 50.0, 60.0),
+               omega=0.3, dt=0.01)
+    psi = smooth_state(p, seed=23)
+    s, o = Solver(p), Oracle(p)
+    assert s.tile_shape(real_time=False) == (64, 8)
+    assert s.tile_shape(real_time=True) == (64, 8)    # (64 x 32) needs ny divisible by 32 with solid walls
+    s.set_psi(psi)
+    o.set_psi(s.get_psi())
+    s.step_rt(6)
+    o.step_rt(6)
+    a, b = s.get_psi().astype(np.complex128), o.get_psi().astype(np.complex128)
+    assert np.linalg.norm(a - b) / np.linalg.norm(b) < 2e-6

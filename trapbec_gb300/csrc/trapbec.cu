@@ -228,12 +228,23 @@ inline bool rt_kind(int kind) {
   return kind == ST_S1 || kind == ST_S2 || kind == ST_S3 || kind == ST_S1W || kind == ST_S2D;
 }
 
-// The two tiled plans: `plan` (shape index `shape`) for every launch and
+// The two tiled plans: `plan` (shape index `shape`; shape < 0: the first
+// built shape that plans for this grid, in index order) for every launch and
 // `plan_rt` for the plain real-time stages (shape_rt < 0: the default
 // real-time shape where it plans; otherwise, or if it does not plan, the
 // general plan).  Chunk lengths follow auto_chunk.
 template <typename T> void make_plans(trapbec_ctx* c, int shape, int shape_rt) {
-  c->plan_valid = (plan_tiled<T>(c->p, c->psi, c->w, c->w2, c->nsm, shape, c->d_err, &c->plan) == 0);
+  if (shape >= 0) {
+    c->plan_valid = (plan_tiled<T>(c->p, c->psi, c->w, c->w2, c->nsm, shape, c->d_err, &c->plan) == 0);
+  } else {
+    c->plan_valid = false;
+    shape = 0;
+    for (int i = 0; i < tiled_nshapes<T>() && !c->plan_valid; ++i)
+      if (plan_tiled<T>(c->p, c->psi, c->w, c->w2, c->nsm, i, c->d_err, &c->plan) == 0) {
+        c->plan_valid = true;
+        shape = i;
+      }
+  }
   c->shape = shape;
   if (shape_rt < 0) shape_rt = tiled_rt_shape<T>();
   c->plan_rt_valid = false;
@@ -738,7 +749,7 @@ template <typename T> int create_impl(trapbec_ctx* c) {
   *c->h_err = 0;
   int rc = setup_tables<T>(c);
   if (rc) return rc;
-  make_plans<T>(c, 0, -1);
+  make_plans<T>(c, -1, -1);
   return TRAPBEC_OK;
 }
 
@@ -1167,8 +1178,11 @@ int trapbec_set_kernel(trapbec_ctx* c, int kind, int tile_z, int tile_y) {
       return TRAPBEC_ERR_UNSUPPORTED;
     }
   }
-  // an explicit shape serves every launch; the default keeps the real-time shape
-  const int shape_rt = (tile_z || tile_y) ? shape : -1;
+  // an explicit shape serves every launch; the default picks the first shape
+  // that plans for the general launches and the real-time shape for the rest
+  const bool expl = tile_z || tile_y;
+  const int shape_rt = expl ? shape : -1;
+  if (!expl) shape = -1;
   c->tile_z = tile_z;
   c->tile_y = tile_y;
   if (c->prec == TRAPBEC_FP64) make_plans<double>(c, shape, shape_rt);
