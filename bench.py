@@ -247,6 +247,7 @@ def warmstart_leg(args):
         "wall_ratio_device": r["wall_ratio_device"],
         "wall_ratio_note": "TF solve / (NN-arm solve + inference + the selector's energy evaluations), device times",
         "final_energy_rel_diff_max": r["final_energy_rel_diff_max"],
+        "same_end_state": r["same_end_state"],
         "guess_rmse_median_tf": med(r["guess_rmse_tf"]), "guess_rmse_median_nn": med(r["guess_rmse_nn"]),
         "fallback": "TF guess where its energy at the same norm is lower, and for Omega/omega_perp > 0.5 "
                     "(bistable: vortex nucleation from the TF guess)",
