@@ -401,7 +401,8 @@ def run_gpu_arm(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "c64 (f32)" if prec == abi.FP32 else "c128 (f64)",
-        "data": "synthetic (seeded TF cloud + 1e-2 noise)",
+        "data": ("synthetic (seeded TF cloud + 1e-2 noise standing in for the relaxed ground state: the "
+                 "stencil's throughput does not depend on the state)"),
         "config": {"workload": f"rotating-trap RK3 quench {n}^3 complex {'FP32' if prec == abi.FP32 else 'FP64'}",
                    "grid": [n, n, n], "box": [128.0, 128.0, 128.0], "dt_trap_units": 0.004,
                    "omega_ramp": "0 -> 0.8 omega_perp over 5000 steps, updated every chunk",
