@@ -146,18 +146,22 @@ __device__ __forceinline__ double fin_op(int q, double z, double y) {
   return (q == 6 || q == 8) ? fmax(z, y) : (q == 7 ? fmin(z, y) : z + y);
 }
 
-// One thread's running values of the NRED quantities.
+// One thread's running values of the NRED quantities.  A thread combines a
+// few partials (each already a CTA's compensated sum), so plain FP64 adds in
+// a fixed order lose nothing measurable, while a compensated add per partial
+// was most of a one-block finaliser's time on GB300, whose FP64 issue rate
+// is about one lane operation per SM clock.
 struct FinAcc {
-  Acc s[6];
+  double s[6];
   double mx6, mn7, mx8;
   __device__ __forceinline__ void init() {
 #pragma unroll
-    for (int q = 0; q < 6; ++q) s[q].init();
+    for (int q = 0; q < 6; ++q) s[q] = 0.0;
     mx6 = 0.0; mn7 = 1.0e300; mx8 = 0.0;
   }
   __device__ __forceinline__ void add(const double* v) {   // v[NRED] of one partial
 #pragma unroll
-    for (int q = 0; q < 6; ++q) s[q].add(v[q]);
+    for (int q = 0; q < 6; ++q) s[q] += v[q];
     mx6 = fmax(mx6, v[6]);
     mn7 = fmin(mn7, v[7]);
     mx8 = fmax(mx8, v[8]);
@@ -171,7 +175,7 @@ __device__ __forceinline__ void fin_tree(const FinAcc& a, double* out) {
   __shared__ double sh[NRED][FIN_THREADS];
   const int t = threadIdx.x;
 #pragma unroll
-  for (int q = 0; q < 6; ++q) sh[q][t] = a.s[q].val();
+  for (int q = 0; q < 6; ++q) sh[q][t] = a.s[q];
   sh[6][t] = a.mx6;
   sh[7][t] = a.mn7;
   sh[8][t] = a.mx8;

@@ -147,6 +147,85 @@ template <> struct RSum<double> {
   __device__ __forceinline__ double val() const { return a.val(); }
 };
 
+// Float-float pairs (value = hi + lo) for the block trees of the FP32
+// reductions.  GB300 issues FP64 at a small fraction of its FP32 rate (about
+// one FP64 lane operation per SM clock), so a tree of nine FP64 values over a
+// CTA costs ~10 us per flush when two CTAs share an SM; the same tree on
+// float-float pairs is FP32 work (TwoSum, renormalised with a second TwoSum,
+// ~44 significant bits) and only the CTA's final values are converted.
+struct FF {
+  float hi, lo;
+};
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+  const float s = a.hi + b.hi;
+  const float bb = s - a.hi;
+  const float e = ((a.hi - (s - bb)) + (b.hi - bb)) + (a.lo + b.lo);
+  const float h = s + e;
+  const float hb = h - s;
+  FF r;
+  r.hi = h;
+  r.lo = (s - (h - hb)) + (e - hb);
+  return r;
+}
+
+// Block reduction of the fused sums into red[q * nblk + blk] (the layout and
+// combination rules of block_reduce_store): FP64 threads go through
+// block_reduce_store; FP32 threads reduce their float-float sums with
+// shuffles and a fixed order over the warps, in FP32 arithmetic.
+template <int NT, typename T>
+__device__ __forceinline__ void block_reduce_sums(const RSum<T> (&rs)[6], T mx, T mn, bool nf, double* red, int blk,
+                                                  int nblk) {
+  if constexpr (sizeof(T) == 8) {
+    double acc[NRED];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) acc[q] = rs[q].val();
+    acc[6] = (double)mx; acc[7] = (double)mn; acc[8] = nf ? 1.0 : 0.0;
+    block_reduce_store<NT>(acc, red, blk, nblk);
+  } else {
+    constexpr int NW = NT / 32;
+    __shared__ FF shf[6][NW];
+    __shared__ float shm[3][NW];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    FF v[6];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) { v[q].hi = rs[q].hi; v[q].lo = rs[q].lo; }
+    float fmx = mx, fmn = mn, fnf = nf ? 1.f : 0.f;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+      for (int q = 0; q < 6; ++q) {
+        FF y;
+        y.hi = __shfl_down_sync(0xffffffffu, v[q].hi, o);
+        y.lo = __shfl_down_sync(0xffffffffu, v[q].lo, o);
+        v[q] = ff_add(v[q], y);
+      }
+      fmx = fmaxf(fmx, __shfl_down_sync(0xffffffffu, fmx, o));
+      fmn = fminf(fmn, __shfl_down_sync(0xffffffffu, fmn, o));
+      fnf = fmaxf(fnf, __shfl_down_sync(0xffffffffu, fnf, o));
+    }
+    if (lane == 0) {
+#pragma unroll
+      for (int q = 0; q < 6; ++q) shf[q][wid] = v[q];
+      shm[0][wid] = fmx; shm[1][wid] = fmn; shm[2][wid] = fnf;
+    }
+    __syncthreads();
+    if (threadIdx.x < NRED) {
+      const int q = threadIdx.x;
+      double out;
+      if (q < 6) {
+        FF x = shf[q][0];
+        for (int w = 1; w < NW; ++w) x = ff_add(x, shf[q][w]);
+        out = (double)x.hi + (double)x.lo;
+      } else {
+        float x = shm[q - 6][0];
+        for (int w = 1; w < NW; ++w) x = (q == 7) ? fminf(x, shm[1][w]) : fmaxf(x, shm[q - 6][w]);
+        out = (double)x;
+      }
+      red[(size_t)q * nblk + blk] = out;
+    }
+  }
+}
+
 template <typename T> constexpr int halo_z() { return sizeof(T) == 4 ? 4 : 3; }
 
 template <typename T, int TZ, int TY, int R, int NSLOT = 8, int MINB = 0> struct TileGeom {
@@ -260,7 +339,8 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
   }
   __syncthreads();
 
-  RSum<T> rN, rK, rP, rQ, rR, rA;
+  RSum<T> rs[6];   // norm, kinetic, potential, quartic, rotation, sum |psi|
+  RSum<T>&rN = rs[0], &rK = rs[1], &rP = rs[2], &rQ = rs[3], &rR = rs[4], &rA = rs[5];
   rN.init(); rK.init(); rP.init(); rQ.init(); rR.init(); rA.init();
   // max/min |psi| in the state precision (FP64 operations are slow on GB300)
   T mx = (T)0, mn = (T)3.0e38;
@@ -272,11 +352,8 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
   // Store the accumulators as one partial slot tagged with its grid, then reset.
   auto flush = [&](int* errp) {
     if (nseg < ba.smax) {
-      double acc[NRED];
-      acc[0] = rN.val(); acc[1] = rK.val(); acc[2] = rP.val(); acc[3] = rQ.val();
-      acc[4] = rR.val(); acc[5] = rA.val(); acc[6] = (double)mx; acc[7] = (double)mn; acc[8] = nf ? 1.0 : 0.0;
       const int slot = blockIdx.x * ba.smax + nseg;
-      block_reduce_store<NT>(acc, ba.part + (size_t)slot * NRED, 0, 1);
+      block_reduce_sums<NT>(rs, mx, mn, nf, ba.part + (size_t)slot * NRED, 0, 1);
       if (tid == 0) ba.part_tag[slot] = cur_inst;
     } else if (tid == 0) {
       atomicExch(errp, (int)TERR_TOO_MANY_SEGMENTS);
@@ -700,12 +777,8 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
   }
 
   if (BATCH && !PLAIN && cur_inst >= 0 && cur_red) flush(cur_err);
-  if (!BATCH && (GEN || (IMAG && KIND != ST_S2)) && ta0.s.red != nullptr) {
-    double acc[NRED];
-    acc[0] = rN.val(); acc[1] = rK.val(); acc[2] = rP.val(); acc[3] = rQ.val();
-    acc[4] = rR.val(); acc[5] = rA.val(); acc[6] = (double)mx; acc[7] = (double)mn; acc[8] = nf ? 1.0 : 0.0;
-    block_reduce_store<NT>(acc, ta0.s.red, blockIdx.x, gridDim.x);
-  }
+  if (!BATCH && (GEN || (IMAG && KIND != ST_S2)) && ta0.s.red != nullptr)
+    block_reduce_sums<NT>(rs, mx, mn, nf, ta0.s.red, blockIdx.x, gridDim.x);
 }
 
 }  // namespace tb
