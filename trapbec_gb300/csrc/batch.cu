@@ -13,8 +13,8 @@
 // instance then combines its slots in a fixed order and updates that
 // instance's control block (renormalisation factor, energy, |dE|/|E|,
 // convergence), exactly as the single-grid loop does.  A converged instance's
-// segments become no-ops.  The K-step loop (3 stage launches, 2 finalisers,
-// 2 slot-tag clears per step) is captured once in a CUDA graph and replayed;
+// segments become no-ops.  The K-step loop (3 stage launches and 2 finalisers
+// per step) is captured once in a CUDA graph and replayed;
 // between replays the host drops converged instances from the work list, so
 // the load stays balanced over the remaining ones.  The tile shape is picked
 // by timing every built shape on the actual batch (autotuner).
@@ -181,6 +181,83 @@ __device__ void gather_instance(const double* __restrict__ part, const int* __re
   fin_tree(a, out);
 }
 
+// FP32 batches: the stage kernel stores each slot's sums as float-float
+// pairs (block_reduce_sums with FFOUT), so the finaliser combines them in FP32
+// arithmetic (one fixed pairwise tree, as fin_tree) and only its nine results
+// and the control update are FP64: GB300 issues FP64 at about one lane
+// operation per SM clock, which made the FP64 finaliser a large share of a
+// small batch's step.
+__device__ void gather_instance_ff(const double* __restrict__ part, const int* __restrict__ tag, int nslots, int inst,
+                                   double* out /* shared NRED */) {
+  __shared__ FF shf[6][FIN_THREADS];
+  __shared__ float shm[3][FIN_THREADS];
+  FF acc[6];
+#pragma unroll
+  for (int q = 0; q < 6; ++q) acc[q].hi = acc[q].lo = 0.f;
+  float mx = 0.f, mn = 3.0e38f, nf = 0.f;
+  const float2* pf = reinterpret_cast<const float2*>(part);
+  for (int b = threadIdx.x; b < nslots; b += FIN_THREADS) {
+    if (tag[b] != inst) continue;
+    const float2* v = pf + (size_t)b * NRED;
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+      const float2 x = v[q];
+      FF y;
+      y.hi = x.x;
+      y.lo = x.y;
+      acc[q] = ff_add(acc[q], y);
+    }
+    mx = fmaxf(mx, v[6].x);
+    mn = fminf(mn, v[7].x);
+    nf = fmaxf(nf, v[8].x);
+  }
+  const int t = threadIdx.x;
+#pragma unroll
+  for (int q = 0; q < 6; ++q) shf[q][t] = acc[q];
+  shm[0][t] = mx;
+  shm[1][t] = mn;
+  shm[2][t] = nf;
+  __syncthreads();
+  for (int s = FIN_THREADS / 2; s >= 32; s >>= 1) {
+    if (t < s) {
+#pragma unroll
+      for (int q = 0; q < 6; ++q) shf[q][t] = ff_add(shf[q][t], shf[q][t + s]);
+      shm[0][t] = fmaxf(shm[0][t], shm[0][t + s]);
+      shm[1][t] = fminf(shm[1][t], shm[1][t + s]);
+      shm[2][t] = fmaxf(shm[2][t], shm[2][t + s]);
+    }
+    __syncthreads();
+  }
+  if (t < 32) {
+    FF x[6];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) x[q] = shf[q][t];
+    float a = shm[0][t], b = shm[1][t], c = shm[2][t];
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) {
+#pragma unroll
+      for (int q = 0; q < 6; ++q) {
+        FF y;
+        y.hi = __shfl_down_sync(0xffffffffu, x[q].hi, s);
+        y.lo = __shfl_down_sync(0xffffffffu, x[q].lo, s);
+        x[q] = ff_add(x[q], y);
+      }
+      a = fmaxf(a, __shfl_down_sync(0xffffffffu, a, s));
+      b = fminf(b, __shfl_down_sync(0xffffffffu, b, s));
+      c = fmaxf(c, __shfl_down_sync(0xffffffffu, c, s));
+    }
+    if (t == 0) {
+#pragma unroll
+      for (int q = 0; q < 6; ++q) out[q] = (double)x[q].hi + (double)x[q].lo;
+      out[6] = a;
+      out[7] = b;
+      out[8] = c;
+    }
+  }
+  __syncthreads();
+}
+
+template <typename T>
 __global__ void __launch_bounds__(FIN_THREADS) batch_fin_energy_kernel(const double* __restrict__ part,
                                                                        const int* __restrict__ tag, int nslots,
                                                                        const int* __restrict__ act, int nact,
@@ -190,10 +267,12 @@ __global__ void __launch_bounds__(FIN_THREADS) batch_fin_energy_kernel(const dou
   ImagCtrl* c = ctrl + inst;
   if (c->converged || c->nonfinite) return;
   __shared__ double r[NRED];
-  gather_instance(part, tag, nslots, inst, r);
+  if constexpr (sizeof(T) == 4) gather_instance_ff(part, tag, nslots, inst, r);
+  else gather_instance(part, tag, nslots, inst, r);
   if (threadIdx.x == 0) imag_energy_update(r, c);
 }
 
+template <typename T>
 __global__ void __launch_bounds__(FIN_THREADS) batch_fin_norm_kernel(const double* __restrict__ part,
                                                                      const int* __restrict__ tag, int nslots,
                                                                      const int* __restrict__ act, int nact,
@@ -203,7 +282,8 @@ __global__ void __launch_bounds__(FIN_THREADS) batch_fin_norm_kernel(const doubl
   ImagCtrl* c = ctrl + inst;
   if (c->converged || c->nonfinite) return;
   __shared__ double r[NRED];
-  gather_instance(part, tag, nslots, inst, r);
+  if constexpr (sizeof(T) == 4) gather_instance_ff(part, tag, nslots, inst, r);
+  else gather_instance(part, tag, nslots, inst, r);
   if (threadIdx.x == 0) imag_norm_update(r, c);
 }
 
@@ -341,13 +421,11 @@ template <typename T> int enqueue_steps(trapbec_batch* b, int s, int k, int nact
   ba.smax = BATCH_SMAX;
   for (int t = 0; t < k; ++t) {
     ba.par = t & 1;
-    BCK(cudaMemsetAsync(b->d_tag, 0xff, sizeof(int) * nslots, b->st));
     shape_launch<T>(s, ST_S1, ba, b->grid, b->st);
-    batch_fin_energy_kernel<<<nact, FIN_THREADS, 0, b->st>>>(b->d_part, b->d_tag, nslots, b->d_act, nact, b->d_ctrl);
+    batch_fin_energy_kernel<T><<<nact, FIN_THREADS, 0, b->st>>>(b->d_part, b->d_tag, nslots, b->d_act, nact, b->d_ctrl);
     shape_launch<T>(s, ST_S2, ba, b->grid, b->st);
-    BCK(cudaMemsetAsync(b->d_tag, 0xff, sizeof(int) * nslots, b->st));
     shape_launch<T>(s, ST_S3, ba, b->grid, b->st);
-    batch_fin_norm_kernel<<<nact, FIN_THREADS, 0, b->st>>>(b->d_part, b->d_tag, nslots, b->d_act, nact, b->d_ctrl);
+    batch_fin_norm_kernel<T><<<nact, FIN_THREADS, 0, b->st>>>(b->d_part, b->d_tag, nslots, b->d_act, nact, b->d_ctrl);
     b->launches += 5;
   }
   BCK(cudaGetLastError());
@@ -368,6 +446,11 @@ template <typename T> int upload_work(trapbec_batch* b, int s, const std::vector
   BCK(cudaMemcpyAsync(b->d_desc, b->h_desc.data(), b->h_desc.size(), cudaMemcpyHostToDevice, b->st));
   BCK(cudaMemcpyAsync(b->d_act, b->h_act, sizeof(int) * act.size(), cudaMemcpyHostToDevice, b->st));
   BCK(cudaMemcpyAsync(b->d_ustart, b->h_ustart, sizeof(long long) * (act.size() + 1), cudaMemcpyHostToDevice, b->st));
+  // Clear the slot tags for this work list.  Every S1 and S3 launch over one
+  // work list writes the same slots (one per CTA and grid it touches, tagged
+  // with that grid, whether or not the grid has converged), so within a graph
+  // replay no slot carries a stale tag and the steps need no clearing.
+  BCK(cudaMemsetAsync(b->d_tag, 0xff, sizeof(int) * (size_t)b->max_grid * BATCH_SMAX, b->st));
   return TRAPBEC_OK;
 }
 

@@ -171,10 +171,13 @@ __device__ __forceinline__ FF ff_add(FF a, FF b) {
 // Block reduction of the fused sums into red[q * nblk + blk] (the layout and
 // combination rules of block_reduce_store): FP64 threads go through
 // block_reduce_store; FP32 threads reduce their float-float sums with
-// shuffles and a fixed order over the warps, in FP32 arithmetic.
-template <int NT, typename T>
+// shuffles and a fixed order over the warps, in FP32 arithmetic.  With FFOUT
+// (FP32 only) each value is stored as a float-float pair (hi, lo) in the
+// eight bytes of its double word, for a finaliser that stays in FP32.
+template <int NT, bool FFOUT, typename T>
 __device__ __forceinline__ void block_reduce_sums(const RSum<T> (&rs)[6], T mx, T mn, bool nf, double* red, int blk,
                                                   int nblk) {
+  static_assert(!FFOUT || sizeof(T) == 4, "float-float output is for FP32 sums");
   if constexpr (sizeof(T) == 8) {
     double acc[NRED];
 #pragma unroll
@@ -211,17 +214,19 @@ __device__ __forceinline__ void block_reduce_sums(const RSum<T> (&rs)[6], T mx, 
     __syncthreads();
     if (threadIdx.x < NRED) {
       const int q = threadIdx.x;
-      double out;
+      FF x;
       if (q < 6) {
-        FF x = shf[q][0];
+        x = shf[q][0];
         for (int w = 1; w < NW; ++w) x = ff_add(x, shf[q][w]);
-        out = (double)x.hi + (double)x.lo;
       } else {
-        float x = shm[q - 6][0];
-        for (int w = 1; w < NW; ++w) x = (q == 7) ? fminf(x, shm[1][w]) : fmaxf(x, shm[q - 6][w]);
-        out = (double)x;
+        x.hi = shm[q - 6][0];
+        x.lo = 0.f;
+        for (int w = 1; w < NW; ++w) x.hi = (q == 7) ? fminf(x.hi, shm[1][w]) : fmaxf(x.hi, shm[q - 6][w]);
       }
-      red[(size_t)q * nblk + blk] = out;
+      if constexpr (FFOUT)
+        reinterpret_cast<float2*>(red)[(size_t)q * nblk + blk] = make_float2(x.hi, x.lo);
+      else
+        red[(size_t)q * nblk + blk] = (double)x.hi + (double)x.lo;
     }
   }
 }
@@ -353,7 +358,7 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
   auto flush = [&](int* errp) {
     if (nseg < ba.smax) {
       const int slot = blockIdx.x * ba.smax + nseg;
-      block_reduce_sums<NT>(rs, mx, mn, nf, ba.part + (size_t)slot * NRED, 0, 1);
+      block_reduce_sums<NT, BATCH && sizeof(T) == 4>(rs, mx, mn, nf, ba.part + (size_t)slot * NRED, 0, 1);
       if (tid == 0) ba.part_tag[slot] = cur_inst;
     } else if (tid == 0) {
       atomicExch(errp, (int)TERR_TOO_MANY_SEGMENTS);
@@ -778,7 +783,7 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
 
   if (BATCH && !PLAIN && cur_inst >= 0 && cur_red) flush(cur_err);
   if (!BATCH && (GEN || (IMAG && KIND != ST_S2)) && ta0.s.red != nullptr)
-    block_reduce_sums<NT>(rs, mx, mn, nf, ta0.s.red, blockIdx.x, gridDim.x);
+    block_reduce_sums<NT, false>(rs, mx, mn, nf, ta0.s.red, blockIdx.x, gridDim.x);
 }
 
 }  // namespace tb
