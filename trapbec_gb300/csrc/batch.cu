@@ -196,8 +196,7 @@ __device__ void gather_instance_ff(const double* __restrict__ part, const int* _
   for (int q = 0; q < 6; ++q) acc[q].hi = acc[q].lo = 0.f;
   float mx = 0.f, mn = 3.0e38f, nf = 0.f;
   const float2* pf = reinterpret_cast<const float2*>(part);
-  for (int b = threadIdx.x; b < nslots; b += FIN_THREADS) {
-    if (tag[b] != inst) continue;
+  auto take = [&](int b) {
     const float2* v = pf + (size_t)b * NRED;
 #pragma unroll
     for (int q = 0; q < 6; ++q) {
@@ -210,7 +209,22 @@ __device__ void gather_instance_ff(const double* __restrict__ part, const int* _
     mx = fmaxf(mx, v[6].x);
     mn = fminf(mn, v[7].x);
     nf = fmaxf(nf, v[8].x);
+  };
+  // the tags of a thread's first GATHER_UNROLL slots are loaded together
+  // (one memory latency instead of one per slot), then the matching slots
+  // are combined in slot order; slots beyond that (large grids) follow
+  constexpr int GATHER_UNROLL = 8;
+  int tg[GATHER_UNROLL];
+#pragma unroll
+  for (int i = 0; i < GATHER_UNROLL; ++i) {
+    const int b = threadIdx.x + i * FIN_THREADS;
+    tg[i] = b < nslots ? tag[b] : -1;
   }
+#pragma unroll
+  for (int i = 0; i < GATHER_UNROLL; ++i)
+    if (tg[i] == inst) take(threadIdx.x + i * FIN_THREADS);
+  for (int b = threadIdx.x + GATHER_UNROLL * FIN_THREADS; b < nslots; b += FIN_THREADS)
+    if (tag[b] == inst) take(b);
   const int t = threadIdx.x;
 #pragma unroll
   for (int q = 0; q < 6; ++q) shf[q][t] = acc[q];
