@@ -119,6 +119,20 @@ __device__ __forceinline__ c_t<T> d2raw(c_t<T> m3, c_t<T> m2, c_t<T> m1, c_t<T> 
   r.y = (T)2 * (m3.y + p3.y) - (T)27 * (m2.y + p2.y) + (T)270 * (m1.y + p1.y) - (T)490 * c0.y;
   return r;
 }
+// The same D2 in difference form, 2 ((v-3-c)+(v3-c)) - 27 (...) + 270 (...):
+// equal in exact arithmetic, but the neighbour differences of a resolved
+// field are (nearly) exact in floating point, so its rounding scales with the
+// result instead of with 490 |c|.  Used for FP32 diagnostics only.
+template <typename T>
+__device__ __forceinline__ c_t<T> d2diff(c_t<T> m3, c_t<T> m2, c_t<T> m1, c_t<T> c0, c_t<T> p1,
+                                         c_t<T> p2, c_t<T> p3) {
+  c_t<T> r;
+  r.x = (T)2 * ((m3.x - c0.x) + (p3.x - c0.x)) - (T)27 * ((m2.x - c0.x) + (p2.x - c0.x)) +
+        (T)270 * ((m1.x - c0.x) + (p1.x - c0.x));
+  r.y = (T)2 * ((m3.y - c0.y) + (p3.y - c0.y)) - (T)27 * ((m2.y - c0.y) + (p2.y - c0.y)) +
+        (T)270 * ((m1.y - c0.y) + (p1.y - c0.y));
+  return r;
+}
 // D1 without the 1/(60 h) factor (deriv.f90:12-18): (v3-v-3) - 9(v2-v-2) + 45(v1-v-1).
 template <typename T>
 __device__ __forceinline__ c_t<T> d1raw(c_t<T> m3, c_t<T> m2, c_t<T> m1, c_t<T> p1, c_t<T> p2,

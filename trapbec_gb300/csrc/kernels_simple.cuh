@@ -120,7 +120,21 @@ __global__ void __launch_bounds__(SIMPLE_THREADS) stage_simple_kernel(StageArgs<
       double re = c.x, im = c.y;
       double a2 = re * re + im * im;
       sN.add(a2);
-      sK.add(re * (double)lap.x + im * (double)lap.y);
+      c_t<T> lapk = lap;   // FP32 diagnostics: the kinetic sum takes the difference form of the stencil
+      if constexpr (sizeof(T) == 4 && KIND == 4) {
+        c_t<T> ex = d2diff<T>(xm3, xm2, xm1, c, xp1, xp2, xp3);
+        c_t<T> ey = d2diff<T>(ym3, ym2, ym1, c, yp1, yp2, yp3);
+        lapk.x = ex.x * a.ix2 + ey.x * a.iy2;
+        lapk.y = ex.y * a.ix2 + ey.y * a.iy2;
+        if (!a.two_dim) {
+          c_t<T> zm3 = ld_cell(a, scale, i, j, k - 3), zm2 = ld_cell(a, scale, i, j, k - 2), zm1 = ld_cell(a, scale, i, j, k - 1);
+          c_t<T> zp1 = ld_cell(a, scale, i, j, k + 1), zp2 = ld_cell(a, scale, i, j, k + 2), zp3 = ld_cell(a, scale, i, j, k + 3);
+          c_t<T> ez = d2diff<T>(zm3, zm2, zm1, c, zp1, zp2, zp3);
+          lapk.x += ez.x * a.iz2;
+          lapk.y += ez.y * a.iz2;
+        }
+      }
+      sK.add(re * (double)lapk.x + im * (double)lapk.y);
       sP.add((double)pot * a2);
       sQ.add(a2 * a2);
       sR.add(re * (double)fr.x + im * (double)fr.y);

@@ -190,6 +190,8 @@ def quench_checkpoints(n: int = 512, steps: int = 1000, every: int = 500, chunk:
                                   "energy_drift": b["energy"] / d32["energy"] - 1.0} for a, b in ck32]},
         "fp32_vs_fp64": {
             "l2_rel_psi_at": steps, "l2_rel_psi": l2,
+            # the same starting values evaluated by each precision's diagnostics
+            "start": {"norm_rel": d32["norm"] / d64["norm"] - 1.0, "energy_rel": d32["energy"] / d64["energy"] - 1.0},
             "checkpoints": [{"step": a, "norm_rel": ck32_at[a]["norm"] / b["norm"] - 1.0,
                              "energy_rel": ck32_at[a]["energy"] / b["energy"] - 1.0}
                             for a, b in ck64],
