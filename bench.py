@@ -217,7 +217,8 @@ def imag_leg(args):
             "dtau_trap_units": 0.002, "max_steps": args.imag_max_steps,
             "converged": int(sum(conv)), "steps_median": float(statistics.median(out["steps"])),
             "steps_max": int(max(out["steps"])), "solve_ms_device": st["solve_ms"], "wall_s": wall,
-            "tile": [st["tile_z"], st["tile_y"]], "precision": "c64 state, FP64 norm/energy/test"}
+            "tile": [st["tile_z"], st["tile_y"]], "precision": ("c64 state; norm and energy sums compensated float-float (FP32 arithmetic, ~44 bits); "
+                          "renormalisation, energy and |dE|/|E| test in FP64")}
 
 
 def warmstart_leg(args):
