@@ -14,6 +14,7 @@ GPU's FP32 path read as the algorithm's, not the kernel's."""
 import math
 
 import numpy as np
+import pytest
 
 from oracle.pyoracle import Oracle
 from trapbec_gb300 import abi, units
@@ -57,3 +58,69 @@ def test_fp32_norm_bias_follows_the_unit_scale():
     st32 = _drift(prob, psi0, mu_state, abi.FP32)
     assert tf32 > 1e-6                         # 5.5e-6 after 200 steps
     assert abs(st32) < 1e-7                    # 1.7e-8
+
+
+def _two_sum(a, b):
+    s = a + b
+    bb = s - a
+    return s, (a - (s - bb)) + (b - bb)
+
+
+def _numpy_rk3(prob, psi0, steps, compensated):
+    """The reference's 2N-storage RK3 (run.f90:44-55) in numpy FP32 around the
+    oracle's FP32 get_rhs; with `compensated`, each stage's psi update keeps
+    its rounding remainder (TwoSum) in a second FP32 array that the next update
+    adds back, so increments below half an ulp are not lost."""
+    p = prob.to_params()
+    p.precision = abi.FP32
+    o = Oracle(p)
+    cf = np.complex64(0.5j * np.float32(p.dt_re))
+    hi = psi0.copy()
+    lo = np.zeros_like(hi)
+    w = np.zeros_like(hi)
+    coef = ((np.float32(0), np.float32(1) / np.float32(3)), (np.float32(-2) / np.float32(3), np.float32(1)),
+            (np.float32(-1), np.float32(0.5)))
+    for _ in range(steps):
+        for A, B in coef:
+            o.set_psi(hi)
+            w = (A * w + cf * o.get_rhs()).astype(np.complex64)
+            inc = (B * w).astype(np.complex64)
+            if compensated:
+                inc = inc + lo
+                sr, er = _two_sum(hi.real, inc.real)
+                si, ei = _two_sum(hi.imag, inc.imag)
+                hi = (sr + 1j * si).astype(np.complex64)
+                lo = (er + 1j * ei).astype(np.complex64)
+            else:
+                hi = (hi + inc).astype(np.complex64)
+    return hi.astype(np.complex128) + lo
+
+
+def test_compensated_fp32_state_keeps_the_lost_increments():
+    """A possible remedy, checked on the oracle: the same ground state in the
+    Thomas-Fermi unit scale, 200 steps.  The plain numpy FP32 loop reproduces
+    the oracle's FP32 run (norm +5.5e-6, L2 4.8e-6 against FP64); keeping each
+    update's rounding remainder brings both to ~1e-9 / 3e-8."""
+    prob, psi_ref, _ = _ground_state()
+    psi0 = psi_ref.astype(np.complex64)
+    p64 = prob.to_params()
+    o = Oracle(p64)
+    o.set_psi(psi0.astype(np.complex128))
+    n0 = o.diag()["norm"]
+    o.step_rt(200)
+    ref = o.get_psi()
+    p32 = prob.to_params()
+    p32.precision = abi.FP32
+    o32 = Oracle(p32)
+    o32.set_psi(psi0)
+    o32.step_rt(200)
+    orc32 = o32.get_psi().astype(np.complex128)
+    plain = _numpy_rk3(prob, psi0, 200, False)
+    comp = _numpy_rk3(prob, psi0, 200, True)
+    norm = lambda x: np.sum(np.abs(x) ** 2)
+    l2 = lambda x: np.linalg.norm((x - ref).ravel()) / np.linalg.norm(ref.ravel())
+    n_ref = norm(ref)
+    assert abs(norm(plain) / norm(orc32) - 1) < 1e-12 and l2(plain) == pytest.approx(l2(orc32), rel=1e-3)
+    assert norm(plain) / n_ref - 1 > 1e-6 and l2(plain) > 1e-6
+    assert abs(norm(comp) / n_ref - 1) < 1e-8 and l2(comp) < 1e-7
+    assert abs(o.diag()["norm"] / n0 - 1) < 1e-12
