@@ -327,19 +327,29 @@ int trapbec_write_timing(const trapbec_params* p, const char* datadir,
  * such as hosts that reserve a GPU's memory up front in their own pool and
  * must not have memory taken behind the pool's back or their streams stalled
  * by the device synchronisation an allocation may cause.
- *  psi       device pointer to ncells complex values of `precision`
+ *  psi       device pointer to ncells complex values of `precision`, aligned
+ *            to one complex value (8 bytes FP32, 16 bytes FP64)
  *  ncells    1 .. 268435456 (16384 blocks x 16384 cells; larger counts are
  *            rejected with TRAPBEC_ERR_ARG because the fixed scratch would
  *            not hold their partial sums)
- *  stats     device pointer to 4 doubles: intpsi2, maxpsi, minpsi, meanpsi
+ *  stats     device pointer to 4 doubles (8-byte aligned): intpsi2, maxpsi,
+ *            minpsi, meanpsi
  *  stream    cudaStream_t to launch on (NULL: the legacy default stream)
+ * Null or misaligned pointers, an unknown precision and out-of-range counts
+ * return TRAPBEC_ERR_ARG before anything touches the GPU.
  * The work is queued on `stream`; read `stats` after synchronising with it.
  * Scratch space is a 512 KiB array in the library's device memory, present on
- * every GPU that loads the library until the process exits.  The first call
- * on a device looks up that array's address on the current device; make that
- * first call before starting any stream capture.  All calls on a device share
- * the one array, so calls that overlap on the GPU (different streams, or
- * different host threads) race and must be serialised by the caller.        */
+ * every GPU that loads the library until the process exits.  The driver maps
+ * it when the library's device code is loaded into a context: by default at
+ * the first call of this function on a device (at library load under
+ * CUDA_MODULE_LOADING=EAGER), which may also synchronise the device.  A host
+ * that reserves nearly all of a GPU's memory for its own pool should make one
+ * call before reserving it.  The first call on a device (and the first after
+ * the device's context was reset or re-created) looks up that array's address
+ * in the current context; make that call before starting any stream capture.
+ * All calls on a device share the one array, so calls that overlap on the GPU
+ * (different streams, or different host threads) race and must be serialised
+ * by the caller.                                                            */
 int trapbec_psi_stats_noalloc(const void* psi, int64_t ncells, int precision, double* stats, void* stream);
 
 /* ---- batched imaginary-time ground states (new) ------------------------- */

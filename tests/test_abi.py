@@ -130,3 +130,25 @@ def test_no_device_fails_loudly(has_gpu):
     rc = lib.trapbec_create(C.byref(p), C.byref(ctx))
     assert rc in (abi.ERR_NODEVICE, abi.ERR_CUDA)
     assert not ctx.value
+
+
+def test_noalloc_rejects_bad_arguments_before_touching_the_gpu():
+    """trapbec_psi_stats_noalloc validates its pointers, precision and size on
+    the host and returns TRAPBEC_ERR_ARG without any CUDA call, so this runs
+    with no GPU: null, misaligned (psi must hold whole complex values, stats
+    doubles), oversized and empty inputs, and an unknown precision."""
+    lib = abi.load()
+    ok = C.c_void_p(256)          # aligned for both precisions; never dereferenced here
+    f = lib.trapbec_psi_stats_noalloc
+    assert f(ok, 1 << 29, abi.FP32, ok, None) == abi.ERR_ARG
+    assert b"ncells" in lib.trapbec_last_error()
+    assert f(ok, 0, abi.FP32, ok, None) == abi.ERR_ARG
+    assert f(None, 10, abi.FP32, ok, None) == abi.ERR_ARG
+    assert f(ok, 10, abi.FP32, None, None) == abi.ERR_ARG
+    assert f(ok, 10, 7, ok, None) == abi.ERR_ARG
+    assert f(C.c_void_p(260), 10, abi.FP32, ok, None) == abi.ERR_ARG      # 4-byte aligned psi
+    assert b"aligned" in lib.trapbec_last_error()
+    assert f(C.c_void_p(264), 10, abi.FP64, ok, None) == abi.ERR_ARG      # 8-byte aligned FP64 psi
+    assert b"16 bytes" in lib.trapbec_last_error()
+    assert f(ok, 10, abi.FP32, C.c_void_p(260), None) == abi.ERR_ARG      # 4-byte aligned stats
+    assert b"stats" in lib.trapbec_last_error()

@@ -26,31 +26,35 @@ def _device_copy(torch, a):
 
 @pytest.mark.parametrize("prec,tol", [(abi.FP64, 1e-12), (abi.FP32, 2e-6)])
 def test_noalloc_stats_match_diag_on_two_calls(prec, tol):
+    """Two calls in a row, each checked against trapbec_diag of the same state.
+    Around the second call (the first has loaded the library's device code and
+    looked up the scratch address) neither the device's free memory nor the
+    memory torch holds may change: the entry point allocates nothing."""
     torch = pytest.importorskip("torch")
     lib = abi.load()
     p = params(n=(40, 36, 48), L=(10.0, 9.0, 12.0), prec=prec, pot="harmonic", harm=(5.0, 6.0, 7.0))
     s = Solver(p)
     states = [smooth_state(p, seed=31, amp=1.3), smooth_state(p, seed=32, amp=0.7)]
     out = torch.zeros(4, dtype=torch.float64, device="cuda")
+    dev_states = []
+    refs = []
     for psi in states:
         s.set_psi(psi)
-        ref = s.diag()
-        dev_psi = _device_copy(torch, s.get_psi())
+        refs.append(s.diag())
+        dev_states.append(_device_copy(torch, s.get_psi()))
+    s.close()
+    torch.cuda.synchronize()
+    for call, (dev_psi, ref) in enumerate(zip(dev_states, refs)):
+        if call == 1:
+            free0 = torch.cuda.mem_get_info()[0]
+            held0 = torch.cuda.memory_allocated()
         rc = lib.trapbec_psi_stats_noalloc(C.c_void_p(dev_psi.data_ptr()), dev_psi.numel(), prec,
                                            C.c_void_p(out.data_ptr()), None)
         assert rc == 0, lib.trapbec_last_error()
         torch.cuda.synchronize()
+        if call == 1:
+            assert torch.cuda.mem_get_info()[0] == free0
+            assert torch.cuda.memory_allocated() == held0
         got = out.cpu().numpy()
         for v, k in zip(got, ("intpsi2", "maxpsi", "minpsi", "meanpsi")):
-            assert abs(v - ref[k]) <= tol * abs(ref[k]), (k, v, ref[k])
-    s.close()
-
-
-def test_noalloc_rejects_oversized_and_bad_arguments():
-    lib = abi.load()
-    dummy = C.c_void_p(1)
-    assert lib.trapbec_psi_stats_noalloc(dummy, 1 << 29, abi.FP32, dummy, None) == abi.ERR_ARG
-    assert b"ncells" in lib.trapbec_last_error()
-    assert lib.trapbec_psi_stats_noalloc(dummy, 0, abi.FP32, dummy, None) == abi.ERR_ARG
-    assert lib.trapbec_psi_stats_noalloc(None, 10, abi.FP32, dummy, None) == abi.ERR_ARG
-    assert lib.trapbec_psi_stats_noalloc(dummy, 10, 7, dummy, None) == abi.ERR_ARG
+            assert abs(v - ref[k]) <= tol * abs(ref[k]), (call, k, v, ref[k])

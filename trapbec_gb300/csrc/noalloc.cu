@@ -14,8 +14,10 @@
 // start-up) and must not have a library take memory behind the pool's back
 // or stall their other streams with the device synchronisation cudaMalloc
 // and cudaFree may perform.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
+#include <cstdint>
 #include <mutex>
 #include <string>
 
@@ -36,10 +38,42 @@ constexpr int NA_NQ = 4;  // sum|psi|^2, max|psi|, min|psi|, sum|psi|
 // never read.
 static __device__ __align__(256) double g_noalloc_scratch[NA_MAX_BLOCKS * NA_NQ];
 
-// Per-device address of g_noalloc_scratch, looked up once per device.
+// Per-device address of g_noalloc_scratch and the unique id of the CUDA
+// context it was looked up in.  The array is part of the library's module,
+// which is loaded into each context separately: after the caller resets the
+// device (cudaDeviceReset) or releases and re-creates its primary context,
+// the module is loaded again and the array can sit at another address, so
+// the address is looked up again whenever the current context's id changes.
 constexpr int NA_MAX_DEVICES = 64;
 void* g_scratch_addr[NA_MAX_DEVICES] = {nullptr};
+unsigned long long g_scratch_ctx[NA_MAX_DEVICES] = {0};
 std::mutex g_scratch_mu;
+
+// cuCtxGetCurrent / cuCtxGetId through the runtime's driver entry points
+// (the library links the static runtime, not libcuda).
+using PFN_ctx_get_current = CUresult (*)(CUcontext*);
+using PFN_ctx_get_id = CUresult (*)(CUcontext, unsigned long long*);
+
+template <typename F> F driver_fn(const char* name) {
+  void* f = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion(name, &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess)
+    return nullptr;
+  return reinterpret_cast<F>(f);
+}
+
+// Unique id of the calling thread's current context (0 if it cannot be read).
+unsigned long long current_ctx_id() {
+  static PFN_ctx_get_current get_cur = driver_fn<PFN_ctx_get_current>("cuCtxGetCurrent");
+  static PFN_ctx_get_id get_id = driver_fn<PFN_ctx_get_id>("cuCtxGetId");
+  if (!get_cur || !get_id) return 0;
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_cur(&ctx) != CUDA_SUCCESS || ctx == nullptr) return 0;
+  if (get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
 
 template <typename T> struct C2;
 template <> struct C2<float> { using t = float2; };
@@ -121,7 +155,8 @@ __global__ void __launch_bounds__(NA_THREADS) stats_final_kernel(const double* _
 }
 
 // Device address of the scratch array for the current device; looked up the
-// first time this device is used and remembered afterwards.
+// first time this device is used (with the device current) and again when the
+// device's context has changed since, remembered otherwise.
 int scratch_for_current_device(double** out) {
   int dev = -1;
   cudaError_t e = cudaGetDevice(&dev);
@@ -134,14 +169,18 @@ int scratch_for_current_device(double** out) {
     return TRAPBEC_ERR_ARG;
   }
   std::lock_guard<std::mutex> lk(g_scratch_mu);
-  if (g_scratch_addr[dev] == nullptr) {
+  unsigned long long ctx = current_ctx_id();
+  if (g_scratch_addr[dev] == nullptr || ctx == 0 || ctx != g_scratch_ctx[dev]) {
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess || p == nullptr) {
       tbh::set_error(std::string("trapbec_psi_stats_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
       return TRAPBEC_ERR_CUDA;
     }
+    // the lookup made the device's primary context current if none was
+    if (ctx == 0) ctx = current_ctx_id();
     g_scratch_addr[dev] = p;
+    g_scratch_ctx[dev] = ctx;
   }
   *out = static_cast<double*>(g_scratch_addr[dev]);
   return TRAPBEC_OK;
@@ -157,6 +196,18 @@ extern "C" int trapbec_psi_stats_noalloc(const void* psi, int64_t ncells, int pr
   }
   if (precision != TRAPBEC_FP32 && precision != TRAPBEC_FP64) {
     tbh::set_error("trapbec_psi_stats_noalloc: precision must be TRAPBEC_FP32 or TRAPBEC_FP64");
+    return TRAPBEC_ERR_ARG;
+  }
+  // the kernels read psi as float2 / double2 and write stats as doubles: a
+  // pointer off that alignment would fault on the device, so refuse it here
+  const uintptr_t palign = precision == TRAPBEC_FP64 ? 16u : 8u;
+  if (reinterpret_cast<uintptr_t>(psi) % palign != 0) {
+    tbh::set_error("trapbec_psi_stats_noalloc: psi must be aligned to " + std::to_string((unsigned)palign) +
+                   " bytes (one complex value of the precision)");
+    return TRAPBEC_ERR_ARG;
+  }
+  if (reinterpret_cast<uintptr_t>(stats) % 8u != 0) {
+    tbh::set_error("trapbec_psi_stats_noalloc: stats must be aligned to 8 bytes (double)");
     return TRAPBEC_ERR_ARG;
   }
   const long long max_cells = NA_CELLS_PER_BLOCK * (long long)NA_MAX_BLOCKS;
