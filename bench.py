@@ -5,9 +5,18 @@ FP64 diagnostics, on [-64,64]^3, omega_perp = 0.02, omega_z = 0.04, g = 1,
 dt = 0.004, Omega ramped linearly towards 0.8 omega_perp.  One bench step is
 one full low-storage RK3 step (three fused stage kernels) over the whole
 grid.  The metric is grid-point updates per second (one grid point advanced
-by one RK3 step).  Synthetic seeded initial state: a Thomas-Fermi cloud with
-1e-2 noise standing in for a relaxed ground state.  Each array is 1 GiB, far
-larger than the 129 MB L2, so no flush is needed between steps.
+by one RK3 step).  The run starts from the ground state of the trap at
+Omega = 0: the seeded Thomas-Fermi cloud with 1e-2 noise relaxed in
+imaginary time on the GPU (FP32 state, FP64 renormalisation and energy).
+Each array is 1 GiB, far larger than the 129 MB L2, so no flush is needed
+between steps.
+
+Beside the timed FP32 run the line carries: the same start advanced in FP64
+and in the compensated FP32 form over a fixed number of steps, with each FP32
+form's norm, energy and L2 error against FP64 (fp32_vs_fp64); the end-to-end
+rate through the C ABI with host buffers; the CPU restatement's rate on the
+host cores; the batched imaginary-time ground states (64 instances) and the
+surrogate-against-Thomas-Fermi warm start.
 
 Output: one JSON line (see the keys below); `--impl reference` times the CPU
 restatement of the reference's algorithm on the host cores instead.
@@ -39,16 +48,16 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
-def profile_traffic(prec_tag: str, tz: int | None = None, ty: int | None = None, deferred: bool = False):
+def profile_traffic(prec_tag: str, tz: int | None = None, ty: int | None = None, form: str = ""):
     """DRAM bytes per grid point per stage launch from the committed ncu summary
     of the full-size launch list of the tile shape and RK3 form that ran
-    (profiles/stage_tiled_<prec>_512_<tz>x<ty>[_deferred].txt; the 128 x 8 FP32
+    (profiles/stage_tiled_<prec>_512_<tz>x<ty>[_<form>].txt; the 128 x 8 FP32
     three-stage default is profiles/stage_tiled_fp32_512.txt)."""
     if tz is None and ty is None:
         tz, ty = 128, 8
-    sfx = "_deferred" if deferred else ""
+    sfx = f"_{form}" if form else ""
     path = os.path.join(HERE, "profiles", f"stage_tiled_{prec_tag}_512_{tz}x{ty}{sfx}.txt")
-    if deferred:
+    if form:
         if not os.path.exists(path):
             return None
         m = re.search(r"dram_bytes_per_point_per_launch:\s*([0-9.eE+-]+)", open(path).read())
@@ -127,6 +136,25 @@ def make_problem(n: int, prec):
     from trapbec_gb300 import abi, units
     prob, init = units.rotating_quench_512(prec, n=n)
     return prob, init
+
+
+def fp64_fma_peak():
+    """FP64 FMA instructions per second of the GPU (libtrapbec's peak kernel: long
+    independent FMA chains on every SM, CUDA events)."""
+    import ctypes as C
+    from trapbec_gb300 import abi
+    v = C.c_double(0)
+    abi.check(abi.load().trapbec_fp64_fma_rate(C.byref(v)), "trapbec_fp64_fma_rate")
+    return v.value
+
+
+# FP64 pipe instructions (DADD, DMUL, DFMA) per grid point of the three stage
+# kernels' plain variant with the rotating frame (kernels_tiled.cuh, counted
+# per complex operation: add/sub/mul/fma of a pair = 2): Laplacian 38, the two
+# first derivatives 20, the frame term 6, potential sum 2, |psi|^2 2, the
+# nonlinear rhs 6, the complex multiplier 4, the w update 0/2/2 and the psi
+# update 2 -> 80 + 82 + 82.
+FP64_OPS_PER_POINT_STEP = 244
 
 
 def cpu_reference(n: int, steps: int, threads: int | None):
@@ -304,6 +332,12 @@ def run_gpu_arm(args):
     def omega_of_step(k):
         return prob.omega_z_for(om_final * min(1.0, k / ramp_steps))
 
+    # the start: the ground state at Omega = 0 (imaginary time on the GPU)
+    ground = None
+    if args.start == "ground":
+        from trapbec_gb300 import reports
+        ground = reports.quench_ground_state(n, seed=init["seed"] + rank)
+        s.set_psi(ground[0])
     chunk = args.chunk
     d0 = s.diag()
     # warm-up (untimed)
@@ -330,7 +364,7 @@ def run_gpu_arm(args):
     achieved = cells * args.steps * bpc / (ms * 1e-3) / 1e9
     tag = "fp32" if prec == abi.FP32 else "fp64"
     tz_run, ty_run = s.tile_shape(real_time=True)
-    tpp = profile_traffic(tag, tz_run, ty_run, deferred)
+    tpp = profile_traffic(tag, tz_run, ty_run, form="deferred" if deferred else "")
     traffic = tpp * cells if tpp else None
 
     kernel_name = "tiled TMA stage kernel" if args.kernel is None or args.kernel[0] != 1 else "per-cell stage kernel"
@@ -345,14 +379,24 @@ def run_gpu_arm(args):
         host[:] = s.get_psi().reshape(-1)
         reps = max(1, args.e2e_reps)
 
+        parts = []
+
         def e2e_call(r):
-            s.set_psi(host.reshape(s.shape))                       # H2D of the state
+            ta = time.perf_counter()
+            s.set_psi(host.reshape(s.shape))                       # H2D of the state (queued on the stream)
             s.set_scalar(abi.SCALAR_OMEGA_Z, omega_of_step(args.warmup + args.steps + r * shots))
-            s.step_rt(shots)                                       # RK3 steps
+            s.step_rt(shots)                                       # RK3 steps (waits for the H2D and the steps)
+            tb = time.perf_counter()
+            steps_ms = s.last_kernel_ms()
             s.diag()                                               # FP64 diagnostics (Psi_info/Psi_norm, E)
+            tc = time.perf_counter()
             s.get_psi(out=host_out)                                # D2H of the state into pinned memory
+            td = time.perf_counter()
+            parts.append({"set_psi_and_steps_ms": 1e3 * (tb - ta), "steps_device_ms": steps_ms,
+                          "diag_ms": 1e3 * (tc - tb), "get_psi_ms": 1e3 * (td - tc)})
 
         e2e_call(0)                                                # untimed warm-up call
+        parts.clear()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         call_ms = []
@@ -366,30 +410,93 @@ def run_gpu_arm(args):
                "h2d_bytes_per_step": int(cells * host.itemsize / shots),
                "d2h_bytes_per_step": int(cells * host.itemsize / shots),
                "shots": shots, "host_buffers": "pinned (page-locked) input and output arrays",
-               "calls": reps, "call_ms": call_ms,
+               "calls": reps, "call_ms": call_ms, "call_parts": parts,
                "note": "per call: set_psi (H2D) + shots RK3 steps + diag + get_psi (D2H); one untimed call first; "
                        "host<->device copies run at the link's ~200 GB/s"}
 
-    # ---- FP64 comparison line (same workload, same kernel family) ------------
+    # ---- precision: FP32 (three stages and compensated) against FP64 -----------
+    # The same start advanced `precision_steps` steps with the same Omega ramp in
+    # the plain FP32 form, the compensated FP32 form and FP64; the FP64 run is
+    # also the FP64 throughput line.
     fp64 = None
+    comp = None
+    precision = None
     if not args.no_fp64 and prec == abi.FP32:
+        import numpy as np
+        start = ground[0] if ground is not None else None
+        if start is None:
+            s.init_state(init["name"], seed=init["seed"] + rank, amp=init["amp"], r_tf2=init["r_tf2"],
+                         noise_amp=init["noise_amp"])
+            start = s.get_psi()
+        P = args.precision_steps
+        runs = {}
+
+        def run_form(sol, form_tag):
+            sol.set_psi(start if form_tag != "fp64" else start.astype(np.complex128))
+            sol.set_scalar(abi.SCALAR_T, 0.0)
+            dstart = sol.diag()
+            timed_steps(sol, 2, chunk, omega_of_step, 0)          # warm-up, then the same start again
+            sol.set_psi(start if form_tag != "fp64" else start.astype(np.complex128))
+            sol.set_scalar(abi.SCALAR_T, 0.0)
+            ms_, _ = timed_steps(sol, P, chunk, omega_of_step, 0)
+            runs[form_tag] = (dstart, sol.diag(), sol.get_psi().astype(np.complex128), ms_)
+
+        run_form(s, "fp32")
+        s.set_stage_form(abi.RK3_COMPENSATED)
+        tune_c = None if args.no_autotune else s.autotune(steps=4)
+        run_form(s, "fp32_compensated")
+        tzc, tyc = s.tile_shape(real_time=True)
         s.close()
         prob64, _ = make_problem(n, abi.FP64)
-        p64 = prob64.to_params()
-        s64 = Solver(p64)
-        s64.init_state(init["name"], seed=init["seed"] + rank, amp=init["amp"], r_tf2=init["r_tf2"],
-                       noise_amp=init["noise_amp"])
+        s64 = Solver(prob64.to_params())
         if not args.no_autotune:
             s64.autotune(steps=2)
-        timed_steps(s64, 2, chunk, omega_of_step, 0)
-        k64 = args.fp64_steps
-        ms64, _ = timed_steps(s64, k64, chunk, omega_of_step, 2)
-        v64 = cells * k64 / (ms64 * 1e-3)
-        fp64 = {"value": v64, "unit": UNIT, "ms_per_step": ms64 / k64,
-                "hbm_gbs_alg": cells * k64 * 160.0 / (ms64 * 1e-3) / 1e9,
-                "hbm_frac": cells * k64 * 160.0 / (ms64 * 1e-3) / 1e9 / peak,
-                "note": "FP64 stage kernels are bound by GB300's FP64 pipe, not HBM"}
+        run_form(s64, "fp64")
         s64.close()
+        d64s, d64e, psi64, ms64 = runs["fp64"]
+
+        # States are compared through the raw sums (no cell volume): an FP32
+        # context forms h, and so dV, in FP32 as the reference's FP32 build
+        # does, which alone puts ~6e-8 between the two precisions' norms.
+        def raw_energy(d):
+            return -0.5 * d["kinetic"] + 0.5 * d["potential"] + 0.25 * d["interaction"] - 0.5 * d["rotation"]
+
+        def versus(tag):
+            ds, de, psi, _ = runs[tag]
+            return {"norm_rel": de["intpsi2"] / d64e["intpsi2"] - 1.0,
+                    "energy_rel": raw_energy(de) / raw_energy(d64e) - 1.0,
+                    "l2_rel_psi": float(np.linalg.norm((psi - psi64).ravel()) / np.linalg.norm(psi64.ravel())),
+                    "norm_drift": de["norm"] / ds["norm"] - 1.0, "energy_drift": de["energy"] / ds["energy"] - 1.0}
+
+        precision = {
+            "steps": P, "start": ("ground state at Omega = 0 (imaginary time, FP32 state, FP64 renormalisation)"
+                                  if ground is not None else "TF cloud + 1e-2 noise"),
+            "unit_scale": "Thomas-Fermi mu = 0.4608 (the state's own mu differs by ~0.8%: it turns slowly in phase)",
+            "compared": "sum |psi|^2 and the energy's raw sums (no cell volume) after `steps` steps, FP32 / FP64 - 1; "
+                        "L2 of psi relative to FP64; drifts relative to each run's own start",
+            "fp32": versus("fp32"), "fp32_compensated": versus("fp32_compensated"),
+            "fp64_drift": {"norm": d64e["norm"] / d64s["norm"] - 1.0, "energy": d64e["energy"] / d64s["energy"] - 1.0},
+        }
+        msc = runs["fp32_compensated"][3]
+        vc = cells * P / (msc * 1e-3)
+        ach_c = cells * P * 128.0 / (msc * 1e-3) / 1e9
+        comp = {"value": vc, "unit": UNIT, "ms_per_step": msc / P, "tile": [tzc, tyc], "autotune": tune_c,
+                "roofline": {"bound": "hbm", "achieved": ach_c, "peak": peak, "unit": "GB/s", "frac": ach_c / peak,
+                             "algorithmic_bytes_per_point_step": 128.0,
+                             "traffic": (lambda t: t * cells if t else None)(
+                                 profile_traffic("fp32", tzc, tyc, form="compensated"))},
+                "note": "each stage also reads and rewrites the remainder array (48 B more per point and step)"}
+        v64 = cells * P / (ms64 * 1e-3)
+        fma = fp64_fma_peak()
+        fp64 = {"value": v64, "unit": UNIT, "ms_per_step": ms64 / P,
+                "hbm_gbs_alg": cells * P * 160.0 / (ms64 * 1e-3) / 1e9,
+                "hbm_frac": cells * P * 160.0 / (ms64 * 1e-3) / 1e9 / peak,
+                "compute_roofline": {"bound": "fp64", "ops_per_point_step": FP64_OPS_PER_POINT_STEP,
+                                     "achieved": v64 * FP64_OPS_PER_POINT_STEP / 1e12,
+                                     "peak": fma / 1e12, "unit": "T FP64 instructions/s",
+                                     "frac": v64 * FP64_OPS_PER_POINT_STEP / fma,
+                                     "peak_kind": "measured: trapbec_fp64_fma_rate (FMA chains on every SM)"},
+                "note": "FP64 stage kernels are bound by GB300's FP64 pipe, not HBM"}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -402,8 +509,9 @@ def run_gpu_arm(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "c64 (f32)" if prec == abi.FP32 else "c128 (f64)",
-        "data": ("synthetic (seeded TF cloud + 1e-2 noise standing in for the relaxed ground state: the "
-                 "stencil's throughput does not depend on the state)"),
+        "data": ("synthetic: the seeded TF cloud + 1e-2 noise relaxed to the ground state at Omega = 0 in "
+                 "imaginary time on the GPU" if ground is not None else
+                 "synthetic (seeded TF cloud + 1e-2 noise standing in for the relaxed ground state)"),
         "config": {"workload": f"rotating-trap RK3 quench {n}^3 complex {'FP32' if prec == abi.FP32 else 'FP64'}",
                    "grid": [n, n, n], "box": [128.0, 128.0, 128.0], "dt_trap_units": 0.004,
                    "omega_ramp": "0 -> 0.8 omega_perp over 5000 steps, updated every chunk",
@@ -421,11 +529,19 @@ def run_gpu_arm(args):
         "gpu_launches": launches,
         "clocks": clk.summary(),
         "wall_s_timed": wall,
-        "drift": {"norm_rel": d1["norm"] / d0["norm"] - 1.0, "energy_rel": d1["energy"] / d0["energy"] - 1.0},
+        "drift": {"norm_rel": d1["norm"] / d0["norm"] - 1.0, "energy_rel": d1["energy"] / d0["energy"] - 1.0,
+                  "steps": args.warmup + args.steps, "note": "the FP32 run's own change over its warm-up and timed steps"},
     }
+    if ground is not None:
+        line["start"] = {"imag_steps": ground[1], "imag_rel_dE": ground[2], "imag_ms_device": ground[3],
+                         "dtau_trap_units": ground[4]}
+    if precision:
+        line["fp32_vs_fp64"] = precision
+    if comp:
+        line["compensated"] = comp
     if fp64:
         line["fp64"] = fp64
-    if args.imag and rank == 0:
+    if not args.no_imag and rank == 0 and world == 1:
         line["imag"] = imag_leg(args)
     if rank == 0 and world == 1 and not args.no_warmstart:
         line["warmstart"] = warmstart_leg(args)
@@ -445,7 +561,10 @@ def main():
     ap.add_argument("--chunk", type=int, default=20, help="RK3 steps per C-ABI call (Omega updated per call)")
     ap.add_argument("--shots", type=int, default=100, help="RK3 steps per end-to-end call")
     ap.add_argument("--e2e-reps", type=int, default=3, help="timed end-to-end calls (after one untimed call)")
-    ap.add_argument("--fp64-steps", type=int, default=6)
+    ap.add_argument("--precision-steps", type=int, default=500,
+                    help="steps of the FP32 / compensated FP32 / FP64 comparison from the same start")
+    ap.add_argument("--start", default="ground", choices=["ground", "tf"],
+                    help="start of the 512^3 run: the imaginary-time ground state or the TF + noise cloud")
     ap.add_argument("--cpu-steps", type=int, default=12, help="RK3 steps of the CPU baseline sample")
     ap.add_argument("--fp64-only", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -453,10 +572,11 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--kernel", type=int, nargs=3, default=None, metavar=("KIND", "TZ", "TY"))
     ap.add_argument("--no-autotune", action="store_true", help="keep the default tile shape and work order")
-    ap.add_argument("--stage-form", type=int, default=0, choices=[0, 1],
-                    help="real-time RK3 form: 0 three full stages, 1 deferred psi1 (stage 1 stores w1 only)")
-    ap.add_argument("--imag", action="store_true", help="add the batched imaginary-time leg")
-    ap.add_argument("--imag-count", type=int, default=16)
+    ap.add_argument("--stage-form", type=int, default=0, choices=[0, 1, 2],
+                    help="real-time RK3 form of the timed run: 0 three full stages, 1 deferred psi1 "
+                         "(stage 1 stores w1 only), 2 compensated state")
+    ap.add_argument("--no-imag", action="store_true", help="skip the batched imaginary-time leg")
+    ap.add_argument("--imag-count", type=int, default=64)
     ap.add_argument("--imag-seed", type=int, default=3)
     ap.add_argument("--imag-grids", type=int, nargs="+", default=[64, 96, 128])
     ap.add_argument("--imag-tol", type=float, default=1e-10)

@@ -192,11 +192,27 @@ int trapbec_step_rt(trapbec_ctx* ctx, int nsteps, double* t_inout);
  *              receives the last norm ratio intPsi2/intPsi2_old (run.f90:23).
  *  RK3_RENORM: up to nsteps RK3 steps with real step Re(dt); after each step
  *              psi is renormalised to the norm target (FP64) and the FP64
- *              energy is formed; stops when |E_n - E_{n-1}| <= tol*|E_n|.
- *              *stat_out receives the last |dE|/|E|.
+ *              energy is formed; stops when |E_n - E_{n-1}| <= tol*|E_n|
+ *              (or on the absolute test of trapbec_set_imag_stop).
+ *              *stat_out receives the last |dE|/|E| (absolute test: the last
+ *              |dE| times the energy scale).  Every energy the test compares
+ *              comes from the same fused evaluation (the incoming state's
+ *              energy reduced in stage 1), including the final state's.
  * *steps_done receives the number of steps taken.                          */
 int trapbec_step_imag(trapbec_ctx* ctx, int nsteps, int variant, double tol,
                       int* steps_done, double* stat_out);
+
+/* Stop test of the RK3_RENORM relaxation (new; the reference relaxes a fixed
+ * number of steps, run.f90:20-33).
+ *  TRAPBEC_STOP_REL (default): |E_n - E_{n-1}| <= tol * |E_n|
+ *  TRAPBEC_STOP_ABS:           |E_n - E_{n-1}| * energy_scale < tol
+ * E is the energy trapbec_diag reports (reference units); energy_scale > 0
+ * converts it into the unit the tolerance is stated in (for a trap-units
+ * problem mapped as in the header comment of trapbec_params: (mu/g) a^3 2 mu
+ * for the total energy, that divided by the trap-units norm for the energy
+ * per particle).  Applies to later trapbec_step_imag calls.                */
+enum trapbec_imag_stop { TRAPBEC_STOP_REL = 0, TRAPBEC_STOP_ABS = 1 };
+int trapbec_set_imag_stop(trapbec_ctx* ctx, int mode, double energy_scale);
 
 /* Diagnostics of the current psi.  intpsi2/maxpsi/minpsi/meanpsi follow
  * Psi_norm and Psi_info (diagnostic.f90:7-25) but are summed in FP64 with
@@ -272,6 +288,20 @@ int trapbec_set_chunk(trapbec_ctx* ctx, int chunk);
 
 /* Form of the real-time RK3 step (run.f90:42-57) on the tiled FP32 kernel.
  * TRAPBEC_RK3_THREE_STAGE (default): three full stages, each storing w and psi.
+ * TRAPBEC_RK3_COMPENSATED (FP32 contexts): the three stages with a
+ *   compensated state.  Each stage's update psi' = psi + B w is formed as an
+ *   exact two-term sum psi' + lo' = psi + (B w + lo), where lo is a second
+ *   complex FP32 array (allocated by this call) holding the rounding
+ *   remainder of the previous update.  Increments below half an FP32 ulp of
+ *   psi, which the plain FP32 update loses (a nearly stationary state drifts
+ *   in norm by ~1e-6-1e-5 over 1000 steps), accumulate in lo instead.  The
+ *   stencil reads psi alone; get_psi and trapbec_diag report psi.  Costs 48
+ *   more bytes of HBM traffic per grid point and step (128 instead of 80).
+ *   Runs on two-row tile shapes with harmonic or no potential and a rotating
+ *   or no frame; other set-ups make trapbec_step_rt return
+ *   TRAPBEC_ERR_UNSUPPORTED.  lo restarts from zero whenever psi is changed
+ *   by anything other than a compensated step (set_psi, init_state,
+ *   imaginary time, forcing, another form).
  * TRAPBEC_RK3_DEFERRED: stage 1 stores w1 only and stage 2 forms
  *   psi1 = psi0 + w1/3 from ghosted boxes of psi0 and w1 with the same FMA,
  *   writing w2 to a second w buffer (allocated by this call): 72 instead of
@@ -280,11 +310,11 @@ int trapbec_set_chunk(trapbec_ctx* ctx, int chunk);
  *   the plain stage variant runs (harmonic or no potential, rotation or no
  *   frame term); elsewhere the step keeps three stages.  On GB300 it measured
  *   slower than three stages on the best tile shape.
- * trapbec_get_stage_form: *deferred = 1 when the next trapbec_step_rt takes
- * the deferred form.                                                        */
-enum trapbec_rk3_form { TRAPBEC_RK3_THREE_STAGE = 0, TRAPBEC_RK3_DEFERRED = 1 };
+ * trapbec_get_stage_form: *form = the form the next trapbec_step_rt takes
+ * (THREE_STAGE where a requested deferred form cannot run).                 */
+enum trapbec_rk3_form { TRAPBEC_RK3_THREE_STAGE = 0, TRAPBEC_RK3_DEFERRED = 1, TRAPBEC_RK3_COMPENSATED = 2 };
 int trapbec_set_stage_form(trapbec_ctx* ctx, int form);
-int trapbec_get_stage_form(trapbec_ctx* ctx, int* deferred);
+int trapbec_get_stage_form(trapbec_ctx* ctx, int* form);
 
 /* Autotune the tiled kernel of the real-time stages for this grid: time every
  * built tile shape and a few chunk lengths over `steps` RK3 steps each on the
@@ -362,10 +392,16 @@ void trapbec_batch_destroy(trapbec_batch* b);
 int trapbec_batch_set_psi(trapbec_batch* b, int inst, const void* psi);
 int trapbec_batch_get_psi(trapbec_batch* b, int inst, void* psi);
 /* Relax all instances: up to max_steps steps each, convergence when
- * |dE|/|E| <= tol.  check_every = steps per graph replay between host checks.
+ * |dE|/|E| <= tol (or the absolute test of trapbec_batch_set_imag_stop).
+ * check_every = steps per graph replay between host checks.
  * steps_out[ninst], energy_out[ninst], mu_out[ninst] (may be NULL).        */
 int trapbec_batch_solve_imag(trapbec_batch* b, int max_steps, double tol, int check_every,
                              int* steps_out, double* energy_out, double* mu_out);
+/* Stop test of later solves (trapbec_imag_stop, as trapbec_set_imag_stop):
+ * TRAPBEC_STOP_ABS stops instance i when |E_n - E_{n-1}| * energy_scale[i]
+ * < tol; energy_scale may be NULL (a scale of 1 for every instance), and
+ * TRAPBEC_STOP_REL ignores it.                                             */
+int trapbec_batch_set_imag_stop(trapbec_batch* b, int mode, const double* energy_scale);
 /* Fill instance `inst` with a Thomas-Fermi state ("thomas_fermi", from the
  * instance's harm_w*) or a workload state ("tf_noise", "tf_vortex_line",
  * "tf_vortex_ring"; see trapbec_init_state).                                */
@@ -377,6 +413,14 @@ int trapbec_batch_stats(trapbec_batch* b, double* solve_ms, int* tile_z, int* ti
  * pending, previous energy, last |dE|/|E|, energy, chemical potential, norm
  * before renormalisation, norm target, steps, converged flag, non-finite flag. */
 int trapbec_batch_status(trapbec_batch* b, int inst, double* out10);
+
+/* ---- measurement helper (no counterpart in the reference) -------------- */
+/* The rate (instructions per second) at which the current GPU retires FP64
+ * fused multiply-adds: independent FMA chains on every SM, one timed launch
+ * after a warm-up, CUDA events.  The compute roofline of the FP64 stage
+ * kernels, which GB300's FP64 pipe bounds before HBM does.  Allocates and
+ * frees a small output buffer; synchronises the device.                    */
+int trapbec_fp64_fma_rate(double* ops_per_second);
 
 /* ---- errors ------------------------------------------------------------- */
 const char* trapbec_strerror(int code);

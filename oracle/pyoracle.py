@@ -51,10 +51,12 @@ def lib() -> C.CDLL:
         L.orc_coords.argtypes = [vp] + [C.POINTER(C.c_double)] * 3
         L.orc_apply_damping.argtypes = [vp]
         L.orc_step_rt.argtypes = [vp, C.c_int, C.POINTER(C.c_double)]
+        L.orc_step_rt_comp.argtypes = [vp, C.c_int, C.POINTER(C.c_double)]
         L.orc_step_imag_euler.argtypes = [vp, C.c_int, C.POINTER(C.c_double)]
         L.orc_step_imag_rk3.argtypes = [vp, C.c_int, C.c_double, C.POINTER(C.c_int),
                                         C.POINTER(C.c_double)]
         L.orc_set_norm_target.argtypes = [vp, C.c_double]
+        L.orc_set_imag_stop.argtypes = [vp, C.c_double]
         L.orc_set_omega.argtypes = [vp, C.c_double]
         L.orc_set_t.argtypes = [vp, C.c_double]
         L.orc_diag.argtypes = [vp, C.POINTER(DiagOut)]
@@ -151,6 +153,13 @@ class Oracle:
         self.t = t.value
         return self.t
 
+    def step_rt_comp(self, n: int) -> float:
+        """n RK3 steps with the compensated state (remainders restart at zero on set_psi)."""
+        t = C.c_double(self.t)
+        lib().orc_step_rt_comp(self.h, int(n), C.byref(t))
+        self.t = t.value
+        return self.t
+
     def step_imag_euler(self, n: int) -> float:
         r = C.c_double(0)
         lib().orc_step_imag_euler(self.h, int(n), C.byref(r))
@@ -162,6 +171,10 @@ class Oracle:
         if rc != 0:
             raise RuntimeError(f"oracle imag rk3 failed: {rc}")
         return s.value, r.value
+
+    def set_imag_stop(self, energy_scale: float = 0.0) -> None:
+        """0: relative stop |dE|/|E| <= tol; > 0: absolute |dE| * energy_scale < tol."""
+        lib().orc_set_imag_stop(self.h, float(energy_scale))
 
     def set_norm_target(self, n0: float) -> None:
         lib().orc_set_norm_target(self.h, float(n0))

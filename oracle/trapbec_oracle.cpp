@@ -88,6 +88,7 @@ template <typename T> struct Rank {
   std::vector<T> xx, yy, zz;  // 1-based storage: index 0 unused
   std::vector<C<T>> psi;      // (-2:nmz+3, -2:nmy+3, -2:nmx+3)
   std::vector<C<T>> rhs, w;   // (1:nmz, 1:nmy, 1:nmx)
+  std::vector<C<T>> lo;       // (1:nmz, 1:nmy, 1:nmx): remainders of the compensated RK3 (new)
   std::vector<T> trap;        // (1:nmz, 1:nmy, 1:nmx)
   size_t gz, gy;              // ghosted extents in z and y
   inline size_t g(int k, int j, int i) const {  // Psi(k,j,i), ghosted
@@ -110,6 +111,7 @@ template <typename T> struct Oracle {
   double norm_target = -1.0;
   bool norm_user = false;   // set by orc_set_norm_target; otherwise derived from each new state
   double e_prev = std::numeric_limits<double>::quiet_NaN();
+  double imag_escale = 0.0;   // stop test: 0 relative |dE|/|E| <= tol; > 0 absolute |dE| * escale < tol
   double intpsi2_old = 1.0;
 
   explicit Oracle(const trapbec_params& pp) : p(pp) {
@@ -139,6 +141,7 @@ template <typename T> struct Oracle {
       R.psi.assign(R.gz * R.gy * ((size_t)nmx + 6), C<T>{0, 0});
       R.rhs.assign((size_t)nmx * nmy * nmz, C<T>{0, 0});
       R.w.assign((size_t)nmx * nmy * nmz, C<T>{0, 0});
+      R.lo.assign((size_t)nmx * nmy * nmz, C<T>{0, 0});
       R.trap.assign((size_t)nmx * nmy * nmz, (T)0);
       R.xx.assign(nmx + 1, 0); R.yy.assign(nmy + 1, 0); R.zz.assign(nmz + 1, 0);
       // initial.f90:34-42
@@ -239,7 +242,7 @@ template <typename T> struct Oracle {
   }
 
   // ---------------------------------------------------------- deriv.f90 --
-  static inline C<T> second_deriv(const C<T>* v, ptrdiff_t s, T h) {  // deriv.f90:19-25
+  static inline C<T> second_deriv_ref(const C<T>* v, ptrdiff_t s, T h) {  // deriv.f90:19-25
     C<T> a = cscale((T)2, v[-3 * s]);
     a = csub(a, cscale((T)27, v[-2 * s]));
     a = cadd(a, cscale((T)270, v[-1 * s]));
@@ -247,6 +250,16 @@ template <typename T> struct Oracle {
     a = cadd(a, cscale((T)270, v[1 * s]));
     a = csub(a, cscale((T)27, v[2 * s]));
     a = cadd(a, cscale((T)2, v[3 * s]));
+    return cdivr(a, (T)180 * (h * h));
+  }
+  // The same D2 in difference form, 2((v-3 - c) + (v3 - c)) - 27(...) + 270(...),
+  // the stencil of the compensated real-time form (new, no counterpart in the
+  // reference): equal in exact arithmetic, smaller rounding for a resolved field.
+  static inline C<T> second_deriv_diff(const C<T>* v, ptrdiff_t s, T h) {
+    const C<T> c = v[0];
+    C<T> a = cscale((T)2, cadd(csub(v[-3 * s], c), csub(v[3 * s], c)));
+    a = csub(a, cscale((T)27, cadd(csub(v[-2 * s], c), csub(v[2 * s], c))));
+    a = cadd(a, cscale((T)270, cadd(csub(v[-1 * s], c), csub(v[1 * s], c))));
     return cdivr(a, (T)180 * (h * h));
   }
   static inline C<T> first_deriv(const C<T>* v, ptrdiff_t s, T h) {  // deriv.f90:12-18
@@ -360,9 +373,11 @@ template <typename T> struct Oracle {
   }
 
   // --------------------------------------------------- finite_diff.f90 --
+  bool diff_lap = false;   // get_rhs takes the difference-form D2 (compensated form)
   void get_rhs() {
     ghost_comm();
     const bool two = p.two_dim != 0;
+    auto second_deriv = diff_lap ? &Oracle::second_deriv_diff : &Oracle::second_deriv_ref;
     for (auto& R : ranks) {
       const ptrdiff_t sx = (ptrdiff_t)(R.gz * R.gy), sy = (ptrdiff_t)R.gz;
 #pragma omp parallel for schedule(static)
@@ -430,6 +445,59 @@ template <typename T> struct Oracle {
     t = t + dt.re;  // run.f90:55, t real
   }
 
+  // The same RK3 with a compensated state (new, no counterpart in the
+  // reference): each stage's psi update psi + (B w) is carried out as an
+  // exact two-term sum (Knuth's TwoSum) of psi and B w + lo, where lo keeps
+  // the rounding remainder of the previous update, so increments below half
+  // an ulp of psi are kept in lo instead of being lost.  get_rhs reads psi
+  // alone.  With T = double the remainders are ~1e-16 relative.
+  static void two_sum(T a, T b, T& s, T& e) {
+    s = a + b;
+    const T bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+  }
+  void comp_update(Rank<T>& R, int k, int j, int i, C<T> inc_plain) {
+    C<T>& ps = R.psi[R.g(k, j, i)];
+    C<T>& l = R.lo[R.in(k, j, i)];
+    const C<T> inc = cadd(inc_plain, l);
+    C<T> sum, rem;
+    two_sum(ps.re, inc.re, sum.re, rem.re);
+    two_sum(ps.im, inc.im, sum.im, rem.im);
+    ps = sum;
+    l = rem;
+  }
+  void rk3_step_comp() {
+    const C<T> cf = {-(T)0.5 * dt.im, (T)0.5 * dt.re};
+    struct DiffScope {   // the compensated form's get_rhs takes the difference-form D2
+      bool& f;
+      explicit DiffScope(bool& g) : f(g) { f = true; }
+      ~DiffScope() { f = false; }
+    } scope(diff_lap);
+    get_rhs();
+    for_interior([&](Rank<T>& R, int k, int j, int i) {
+      size_t q = R.in(k, j, i);
+      C<T> w = cmul(cf, R.rhs[q]);
+      R.w[q] = w;
+      comp_update(R, k, j, i, cdivr(w, (T)3));
+    });
+    get_rhs();
+    const T a2 = (T)(-2.) / (T)3.;
+    for_interior([&](Rank<T>& R, int k, int j, int i) {
+      size_t q = R.in(k, j, i);
+      C<T> w = cadd(cscale(a2, R.w[q]), cmul(cf, R.rhs[q]));
+      R.w[q] = w;
+      comp_update(R, k, j, i, w);
+    });
+    get_rhs();
+    for_interior([&](Rank<T>& R, int k, int j, int i) {
+      size_t q = R.in(k, j, i);
+      C<T> w = cadd(C<T>{-R.w[q].re, -R.w[q].im}, cmul(cf, R.rhs[q]));
+      R.w[q] = w;
+      comp_update(R, k, j, i, cscale((T)0.5, w));
+    });
+    t = t + dt.re;
+  }
+
   void imag_euler_step() {  // run.f90:21-23
     const C<T> cf = {dt.re * (T)0.5, dt.im * (T)0.5};
     get_rhs();
@@ -478,9 +546,9 @@ template <typename T> struct Oracle {
         for (int j = 1; j <= R.nmy; ++j)
           for (int k = 1; k <= R.nmz; ++k) {
             const C<T>* c = &R.psi[R.g(k, j, i)];
-            C<T> lap = second_deriv(c, sx, hx);
-            lap = cadd(lap, second_deriv(c, sy, hy));
-            if (!two) lap = cadd(lap, second_deriv(c, 1, hz));
+            C<T> lap = second_deriv_ref(c, sx, hx);
+            lap = cadd(lap, second_deriv_ref(c, sy, hy));
+            if (!two) lap = cadd(lap, second_deriv_ref(c, 1, hz));
             bool act;
             C<T> fr = frame_term(R, c, sx, sy, j, i, &act);
             double re = c->re, im = c->im;
@@ -565,9 +633,10 @@ template <typename T> struct Oracle {
         ps = cscale(sc, ps);
       });
       diag(&d);
-      rel = std::fabs(d.energy - e_prev) / std::fabs(d.energy);
+      const double dE = std::fabs(d.energy - e_prev);
+      rel = imag_escale > 0.0 ? dE * imag_escale : dE / std::fabs(d.energy);
       e_prev = d.energy;
-      if (rel <= tol) break;
+      if (imag_escale > 0.0 ? rel < tol : rel <= tol) break;
     }
     if (s > nsteps) s = nsteps;
     *steps_done = s;
@@ -1046,6 +1115,7 @@ int orc_set_psi(void* h, const void* psi) {
   return dispatch((Handle*)h, [&](auto& o) {
     using T = std::remove_reference_t<decltype(o.t)>;
     o.set_psi((const T*)psi);
+    for (auto& R : o.ranks) std::fill(R.lo.begin(), R.lo.end(), C<T>{0, 0});   // a new state: no remainder
     if (!o.norm_user) o.norm_target = -1.0;   // the next relaxation keeps the new state's norm
     return 0; });
 }
@@ -1102,6 +1172,13 @@ int orc_step_rt(void* h, int nsteps, double* t) {
     for (int s = 0; s < nsteps; ++s) o.rk3_step();
     *t = (double)o.t; return 0; });
 }
+int orc_step_rt_comp(void* h, int nsteps, double* t) {
+  return dispatch((Handle*)h, [&](auto& o) {
+    using T = std::remove_reference_t<decltype(o.t)>;
+    o.t = (T)*t;
+    for (int s = 0; s < nsteps; ++s) o.rk3_step_comp();
+    *t = (double)o.t; return 0; });
+}
 int orc_step_imag_euler(void* h, int nsteps, double* ratio) {
   return dispatch((Handle*)h, [&](auto& o) {
     double r = 0;
@@ -1115,6 +1192,9 @@ int orc_step_imag_euler(void* h, int nsteps, double* ratio) {
 }
 int orc_step_imag_rk3(void* h, int nsteps, double tol, int* steps_done, double* rel) {
   return dispatch((Handle*)h, [&](auto& o) { return o.imag_rk3(nsteps, tol, steps_done, rel); });
+}
+int orc_set_imag_stop(void* h, double escale) {
+  return dispatch((Handle*)h, [&](auto& o) { o.imag_escale = escale > 0.0 ? escale : 0.0; return 0; });
 }
 int orc_set_norm_target(void* h, double n0) {
   return dispatch((Handle*)h, [&](auto& o) { o.norm_target = n0; o.norm_user = n0 > 0; return 0; });

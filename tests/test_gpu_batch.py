@@ -98,3 +98,30 @@ def test_batch_stops_at_max_steps_and_one_step_reports_the_start_energy():
         o.set_psi(psis[i])
         o.step_imag_rk3(13, 0.0)
         assert rel_err(b2.get_psi(i), o.get_psi()) < 1e-11, i
+
+
+def test_batch_absolute_stop_per_instance_scale_fp64():
+    """trapbec_batch_set_imag_stop(ABS): instance i stops when |dE| * scale[i]
+    < tol, at the step the single-grid loop with the same scale stops (one
+    apart at the threshold); a larger scale means more steps."""
+    ps = _mixed_params(abi.FP64)
+    psis = [smooth_state(p, seed=70 + i) for i, p in enumerate(ps)]
+    scales = [1.0, 10.0, 100.0]   # thresholds |dE| < 1e-8, 1e-9, 1e-10: well above the FP64 noise floor
+    tol = 1e-8
+    b = BatchSolver(ps)
+    for i, psi in enumerate(psis):
+        b.set_psi(i, psi)
+    b.set_imag_stop(abi.STOP_ABS, scales)
+    out = b.solve(max_steps=20000, tol=tol, check_every=32)
+    for i, p in enumerate(ps):
+        st = b.status(i)
+        assert st["converged"] == 1 and st["rel"] < tol
+        s = Solver(p)
+        s.set_psi(psis[i])
+        s.set_imag_stop(abi.STOP_ABS, scales[i])
+        steps, rel = s.step_imag(20000, abi.IMAG_RK3_RENORM, tol)
+        assert abs(out["steps"][i] - steps) <= 1, (i, out["steps"][i], steps)
+        s.close()
+    b.set_imag_stop(abi.STOP_REL)
+    with pytest.raises(abi.TrapbecError):
+        b.set_imag_stop(abi.STOP_ABS, [1.0, 0.0, 1.0])

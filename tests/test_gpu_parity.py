@@ -124,6 +124,31 @@ def test_time_dependent_potential_and_damping():
     assert abs(s.t - o.t) < 1e-14
 
 
+@pytest.mark.slow
+def test_vortex_ring_256_fp64_parity():
+    """The 256^3 vortex-ring workload (TF background x ring of radius 8 in
+    z = 0, 1e-3 phase noise, trap (0.05, 0.05, 0.1), g = 1, dt = 0.005) in
+    FP64: 60 RK3 steps on the GPU against the oracle from the same state, psi,
+    norm and energy to 1e-12 relative."""
+    prob, init = units.vortex_ring_256(abi.FP64)
+    p = prob.to_params()
+    s = Solver(p)
+    _solver_init(s, init)
+    psi0 = s.get_psi()
+    o = Oracle(p)
+    o.set_psi(psi0)
+    steps = 60
+    s.step_rt(steps)
+    o.step_rt(steps)
+    a, b = s.get_psi(), o.get_psi()
+    assert rel_err(a, b) < FP64_TOL
+    assert np.linalg.norm((a - b).ravel()) / np.linalg.norm(b.ravel()) < FP64_TOL
+    dg, do = s.diag(), o.diag()
+    for k in ("norm", "energy", "mu", "intpsi2", "maxpsi", "meanpsi"):
+        assert abs(dg[k] - do[k]) <= FP64_TOL * abs(do[k]), (k, dg[k], do[k])
+    s.close()
+
+
 def test_fp32_against_fp32_oracle():
     prob, init = units.vortex_line_64(abi.FP32)
     p = prob.to_params()
@@ -202,6 +227,50 @@ def test_imag_rk3_renorm_matches_oracle():
     so2, ro2 = o.step_imag_rk3(5000, 1e-10)
     assert abs(sg2 - so2) <= 1 and rg2 <= 1e-10 and ro2 <= 1e-10
     assert rel_err(s.get_psi(), o.get_psi()) < 1e-8
+
+
+def test_imag_rk3_absolute_stop_matches_oracle():
+    """The absolute stop |E_n - E_{n-1}| * scale < tol (the workload's |dE| <
+    tol with the energy in the caller's unit): the same stopping step as the
+    oracle's loop (one apart at the threshold); stat_out is |dE| * scale."""
+    p = params(n=(20, 20, 20), L=(10.0, 10.0, 10.0), pot="harmonic", harm=(100.0, 120.0, 90.0), dt=0.01,
+               omega=0.2)
+    psi = smooth_state(p, seed=13)
+    scale, tol = 37.5, 3e-9
+    s, o = Solver(p), Oracle(p)
+    s.set_psi(psi)
+    o.set_psi(psi)
+    s.set_imag_stop(abi.STOP_ABS, scale)
+    o.set_imag_stop(scale)
+    sg, rg = s.step_imag(5000, abi.IMAG_RK3_RENORM, tol)
+    so, ro = o.step_imag_rk3(5000, tol)
+    assert 10 < sg < 5000 and abs(sg - so) <= 1, (sg, so)
+    assert rg < tol and ro < tol
+    assert rel_err(s.get_psi(), o.get_psi()) < 1e-8
+    # back to the relative test: from the converged state it stops within a few steps
+    s.set_imag_stop(abi.STOP_REL)
+    sg2, rg2 = s.step_imag(100, abi.IMAG_RK3_RENORM, 1e-6)
+    assert sg2 <= 3 and rg2 <= 1e-6
+    with pytest.raises(abi.TrapbecError):
+        s.set_imag_stop(abi.STOP_ABS, -1.0)
+
+
+def test_imag_rk3_split_calls_report_the_same_last_change():
+    """A relaxation split over two calls ends on the same |dE|/|E| as one call
+    over the same steps: the energy of a call's final state comes from the same
+    stage-1 evaluation as every other energy the loop compares."""
+    p = params(n=(20, 20, 20), L=(10.0, 10.0, 10.0), pot="harmonic", harm=(100.0, 120.0, 90.0), dt=0.01,
+               omega=0.2)
+    psi = smooth_state(p, seed=14)
+    one, two = Solver(p), Solver(p)
+    one.set_psi(psi)
+    two.set_psi(psi)
+    n1, r1 = one.step_imag(100, abi.IMAG_RK3_RENORM, 0.0)
+    na, ra = two.step_imag(60, abi.IMAG_RK3_RENORM, 0.0)
+    nb, rb = two.step_imag(40, abi.IMAG_RK3_RENORM, 0.0)
+    assert n1 == 100 and na == 60 and nb == 40
+    assert rel_err(one.get_psi(), two.get_psi()) < 1e-13
+    assert abs(rb - r1) <= 1e-3 * r1, (rb, r1)
 
 
 INIT_STATES = ["constant", "thomas_fermi", "soliton", "single_vortex", "sausage", "crow", "random_points",

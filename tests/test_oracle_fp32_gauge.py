@@ -124,3 +124,39 @@ def test_compensated_fp32_state_keeps_the_lost_increments():
     assert norm(plain) / n_ref - 1 > 1e-6 and l2(plain) > 1e-6
     assert abs(norm(comp) / n_ref - 1) < 1e-8 and l2(comp) < 1e-7
     assert abs(o.diag()["norm"] / n0 - 1) < 1e-12
+
+
+def test_oracle_compensated_rk3_matches_the_numpy_loop():
+    """The oracle's compensated RK3 (the CPU reference of the GPU's
+    TRAPBEC_RK3_COMPENSATED form) keeps the increments the plain FP32 loop
+    loses: on the same ground state in the Thomas-Fermi unit scale it stays
+    within the numpy study's figures of the FP64 run, and agrees with the
+    numpy compensated loop at FP32 rounding level.  In FP64 it is the plain
+    RK3 to rounding."""
+    prob, psi_ref, _ = _ground_state()
+    psi0 = psi_ref.astype(np.complex64)
+    steps = 200
+    p64 = prob.to_params()
+    o = Oracle(p64)
+    o.set_psi(psi0.astype(np.complex128))
+    o.step_rt(steps)
+    ref = o.get_psi()
+    p32 = prob.to_params()
+    p32.precision = abi.FP32
+    oc = Oracle(p32)
+    oc.set_psi(psi0)
+    oc.step_rt_comp(steps)
+    comp = oc.get_psi().astype(np.complex128)
+    study = _numpy_rk3(prob, psi0, steps, True)
+    norm = lambda x: np.sum(np.abs(x) ** 2)
+    l2 = lambda x, y: np.linalg.norm((x - y).ravel()) / np.linalg.norm(y.ravel())
+    assert abs(norm(comp) / norm(ref) - 1) < 1e-7
+    assert l2(comp, ref) < 1e-7
+    assert l2(comp, study) < 1e-7
+    o2 = Oracle(p64)
+    o2.set_psi(psi0.astype(np.complex128))
+    o2.step_rt_comp(20)
+    o3 = Oracle(p64)
+    o3.set_psi(psi0.astype(np.complex128))
+    o3.step_rt(20)
+    assert l2(o2.get_psi(), o3.get_psi()) < 1e-14

@@ -33,7 +33,8 @@ FP32, FP64 = 0, 1
 LAYOUT_INTERIOR, LAYOUT_GHOSTED = 0, 1
 FIELD_VELOCITY, FIELD_QPRESSURE = 0, 1
 IMAG_REF_EULER, IMAG_RK3_RENORM = 0, 1
-RK3_THREE_STAGE, RK3_DEFERRED = 0, 1
+STOP_REL, STOP_ABS = 0, 1
+RK3_THREE_STAGE, RK3_DEFERRED, RK3_COMPENSATED = 0, 1, 2
 
 SCALAR_OMEGA_Z, SCALAR_DT_RE, SCALAR_DT_IM, SCALAR_GAMMA = 0, 1, 2, 3
 SCALAR_T, SCALAR_ADVECTIVE_VX, SCALAR_NORM_TARGET = 4, 5, 6
@@ -133,6 +134,7 @@ _PROTOS = {
     "trapbec_step_rt": (C.c_int, [_VP, C.c_int, C.POINTER(C.c_double)]),
     "trapbec_step_imag": (C.c_int, [_VP, C.c_int, C.c_int, C.c_double,
                                     C.POINTER(C.c_int), C.POINTER(C.c_double)]),
+    "trapbec_set_imag_stop": (C.c_int, [_VP, C.c_int, C.c_double]),
     "trapbec_diag": (C.c_int, [_VP, C.POINTER(DiagOut)]),
     "trapbec_set_wait_limit": (C.c_int, [_VP, C.c_uint32, C.c_int]),
     "trapbec_force_vortex": (C.c_int, [_VP, C.c_double, C.c_double, C.c_double]),
@@ -165,10 +167,12 @@ _PROTOS = {
     "trapbec_batch_solve_imag": (C.c_int, [_VP, C.c_int, C.c_double, C.c_int,
                                            C.POINTER(C.c_int), C.POINTER(C.c_double),
                                            C.POINTER(C.c_double)]),
+    "trapbec_batch_set_imag_stop": (C.c_int, [_VP, C.c_int, C.POINTER(C.c_double)]),
     "trapbec_batch_init_state": (C.c_int, [_VP, C.c_int, C.c_char_p, C.POINTER(InitArgs)]),
     "trapbec_batch_stats": (C.c_int, [_VP, C.POINTER(C.c_double), C.POINTER(C.c_int), C.POINTER(C.c_int),
                                       C.POINTER(C.c_int64)]),
     "trapbec_batch_status": (C.c_int, [_VP, C.c_int, C.POINTER(C.c_double)]),
+    "trapbec_fp64_fma_rate": (C.c_int, [C.POINTER(C.c_double)]),
     "trapbec_strerror": (C.c_char_p, [C.c_int]),
     "trapbec_last_error": (C.c_char_p, []),
     "trapbec_abi_version": (C.c_int, []),

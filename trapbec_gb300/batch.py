@@ -1,9 +1,10 @@
 """Batched imaginary-time ground states over libtrapbec (trapbec_batch_*).
 
 Many independent grids (own size, box, trap, rotation and step) are relaxed
-together by the RK3 imaginary-time loop with FP64 renormalisation and the
-relative energy-change stop; each RK3 stage is one persistent launch over the
-work of all unconverged grids and the step loop is replayed from a CUDA graph.
+together by the RK3 imaginary-time loop with FP64 renormalisation and an
+energy-change stop (relative by default, absolute per set_imag_stop); each RK3
+stage is one persistent launch over the work of all unconverged grids and the
+step loop is replayed from a CUDA graph.
 """
 from __future__ import annotations
 
@@ -61,6 +62,14 @@ class BatchSolver:
             a.r_tf2[k] = float(r_tf2[k])
         check(self.lib.trapbec_batch_init_state(self.h, int(i), name.encode(), C.byref(a)),
               "trapbec_batch_init_state")
+
+    def set_imag_stop(self, mode: int = abi.STOP_REL, energy_scale=None) -> None:
+        """abi.STOP_REL: instance i stops at |dE|/|E| <= tol (default).  abi.STOP_ABS: at
+        |dE| * energy_scale[i] < tol (energy_scale None: 1 for every instance)."""
+        arr = None
+        if energy_scale is not None:
+            arr = (C.c_double * self.n)(*[float(v) for v in energy_scale])
+        check(self.lib.trapbec_batch_set_imag_stop(self.h, int(mode), arr), "trapbec_batch_set_imag_stop")
 
     def solve(self, max_steps: int, tol: float, check_every: int = 64) -> dict:
         steps = (C.c_int * self.n)()

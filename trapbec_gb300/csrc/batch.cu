@@ -64,6 +64,7 @@ struct BInst {
   double dV = 0.0;
   long long units = 0; // work units of this instance for the current shape
   int ntz = 0, nty = 0;
+  double escale = 0.0; // stop test: 0 relative, > 0 absolute with this energy scale
 };
 
 }  // namespace
@@ -489,6 +490,7 @@ void reset_ctrl(trapbec_batch* b, int i, double tol) {
   c.n0 = -1.0;   // set from the initial state by the first energy finaliser
   c.tol = tol;
   c.dV = b->in[i].dV;
+  c.escale = b->in[i].escale;
   c.rel = INFINITY;
 }
 
@@ -755,6 +757,27 @@ int trapbec_batch_init_state(trapbec_batch* b, int inst, const char* init_cond, 
   if (!b || !init_cond || inst < 0 || inst >= b->ninst) return TRAPBEC_ERR_ARG;
   return b->prec == TRAPBEC_FP64 ? init_state_batch<double>(b, inst, init_cond, args)
                                  : init_state_batch<float>(b, inst, init_cond, args);
+}
+
+int trapbec_batch_set_imag_stop(trapbec_batch* b, int mode, const double* energy_scale) {
+  if (!b) return TRAPBEC_ERR_ARG;
+  if (mode == TRAPBEC_STOP_REL) {
+    for (auto& I : b->in) I.escale = 0.0;
+    return TRAPBEC_OK;
+  }
+  if (mode != TRAPBEC_STOP_ABS) {
+    set_error("trapbec_batch_set_imag_stop: mode must be TRAPBEC_STOP_REL or TRAPBEC_STOP_ABS");
+    return TRAPBEC_ERR_ARG;
+  }
+  for (int i = 0; i < b->ninst; ++i) {
+    const double e = energy_scale ? energy_scale[i] : 1.0;
+    if (!(e > 0.0) || !std::isfinite(e)) {
+      set_error("trapbec_batch_set_imag_stop: energy_scale[" + std::to_string(i) + "] must be finite and > 0");
+      return TRAPBEC_ERR_ARG;
+    }
+  }
+  for (int i = 0; i < b->ninst; ++i) b->in[i].escale = energy_scale ? energy_scale[i] : 1.0;
+  return TRAPBEC_OK;
 }
 
 int trapbec_batch_solve_imag(trapbec_batch* b, int max_steps, double tol, int check_every, int* steps_out,

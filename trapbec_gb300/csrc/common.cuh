@@ -49,8 +49,10 @@ struct ImagCtrl {
   double mu;        // chemical potential of the last evaluated state
   double norm;      // norm of the last state before renormalisation
   double n0;        // norm target
-  double tol;       // convergence tolerance on |dE|/|E|
+  double tol;       // convergence tolerance
   double dV;        // cell volume
+  double escale;    // 0: stop when |dE|/|E| <= tol; > 0: stop when |dE| * escale < tol
+                    // (escale converts the reference-unit energy into the caller's unit)
   int have_prev;    // e_prev is valid
   int converged;    // |dE|/|E| <= tol reached (stages become no-ops)
   int step;         // completed steps in the current call
@@ -85,6 +87,7 @@ template <typename T> struct StageArgs {
   int use_ctrl_scale;         // take the load factor from ctrl->scale
   const c_t<T>* __restrict__ w_in;  // S2D: w1 (ghost fix-ups read it); w receives w2
   T B1;                       // S2D: B of stage 1 (psi1 = psi0 + B1*w1)
+  c_t<T>* __restrict__ lo;    // compensated state: rounding remainder of psi, read and rewritten in place
 };
 
 // Stage prologue: a converged imaginary-time loop turns stages into no-ops;

@@ -5,7 +5,10 @@
 // incoming renormalised state) -> imag_fin_energy -> stage 2 -> stage 3
 // (+ norm reduction of the new state) -> imag_fin_norm.  The finalisers run
 // as one block, reduce the block partials in a fixed order (bitwise
-// reproducible), and update the control block in FP64.
+// reproducible), and update the control block in FP64.  The stop test is on
+// the energy change of consecutive states: relative, |E_n - E_{n-1}| <=
+// tol |E_n|, or absolute in the caller's energy unit, |E_n - E_{n-1}| *
+// escale < tol (ImagCtrl::escale > 0).
 #pragma once
 #include "common.cuh"
 #include "kernels_simple.cuh"
@@ -29,9 +32,11 @@ __device__ __forceinline__ void imag_energy_update(const double* r, ImagCtrl* c)
   const double mu = (Q + k2 * 0.5 * r[3]) / r[0];
   if (!isfinite(E)) { c->nonfinite = 1; return; }
   if (c->have_prev) {
-    const double rel = fabs(E - c->e_prev) / fabs(E);
+    // relative test |dE|/|E| <= tol, or the absolute |dE| * escale < tol
+    const double dE = fabs(E - c->e_prev);
+    const double rel = c->escale > 0.0 ? dE * c->escale : dE / fabs(E);
     c->rel = rel;
-    if (rel <= c->tol) c->converged = 1;
+    if (c->escale > 0.0 ? rel < c->tol : rel <= c->tol) c->converged = 1;
   }
   c->e_prev = E;
   c->have_prev = 1;

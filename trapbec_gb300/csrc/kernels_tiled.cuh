@@ -302,9 +302,16 @@ struct BatchArgs {
 //   only diagnostics read, are left at their initial values.
 // VAR_GEN: everything else, with run-time switches (array potential,
 //   advective frame, diagnostics, any reduction).
+// VAR_COMP: the plain variant with a compensated FP32 state.  The stage
+//   update psi' = psi + B w (run.f90:48,51,54) is formed as a TwoSum of psi
+//   and B w + lo, where lo (a second complex array, read and rewritten at the
+//   centre cell only) holds the rounding remainder of the previous update:
+//   psi' + lo' equals psi + lo + B w exactly, so increments smaller than half
+//   an ulp of psi accumulate in lo instead of being lost.  The stencil reads
+//   psi alone, as the reference's get_rhs reads its FP32 Psi.
 // BATCH: the units of many independent grids in one launch (batched
 // imaginary-time solves); arguments are read per segment from the table.
-enum StageVar : int { VAR_GEN = 0, VAR_PLAIN = 1, VAR_IMAG = 2 };
+enum StageVar : int { VAR_GEN = 0, VAR_PLAIN = 1, VAR_IMAG = 2, VAR_COMP = 5 };
 
 template <typename T, int TZ, int TY, int R, int NSLOT, int MINB, int KIND, int VAR, bool BATCH>
 __global__ void __launch_bounds__(TileGeom<T, TZ, TY, R, NSLOT, MINB>::NT, TileGeom<T, TZ, TY, R, NSLOT, MINB>::MIN_BLOCKS)
@@ -316,7 +323,10 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
   using V = c_t<T>;
   constexpr int HZ = G::HZ, TZP = G::TZP, S = K::S, NT = G::NT;
   constexpr bool READS_W = (KIND == ST_S2 || KIND == ST_S3 || KIND == ST_S2D);
-  constexpr bool PLAIN = (VAR == VAR_PLAIN), IMAG = (VAR == VAR_IMAG), GEN = (VAR == VAR_GEN);
+  constexpr bool COMP = (VAR == VAR_COMP);   // a plain variant whose update carries the remainder
+  constexpr bool PLAIN = (VAR == VAR_PLAIN) || COMP, IMAG = (VAR == VAR_IMAG), GEN = (VAR == VAR_GEN);
+  static_assert(!COMP || (!BATCH && (KIND == ST_S1 || KIND == ST_S2 || KIND == ST_S3)),
+                "the compensated state is for the real-time RK3 stages");
   constexpr bool ANALYTIC = PLAIN || IMAG;   // harmonic / no potential, rotation / no frame
   static_assert(!K::DEFER || PLAIN, "the deferred stage has a plain variant only");
   static_assert(!IMAG || KIND == ST_S1 || KIND == ST_S2 || KIND == ST_S3, "imaginary-time variant: RK3 stages only");
@@ -643,6 +653,14 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
         tv[r] = (T)0;
         if (GEN && a.pot_mode == POT_ARR && store && zok && yok[r]) tv[r] = a.trap[rowbase + (size_t)r * nz];
       }
+      // compensated state: this plane's remainders, loaded now and used by the
+      // update at the end of the plane (streaming: each is read once)
+      V lov[COMP ? R : 1];
+      if constexpr (COMP) {
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+          lov[r] = (store && zok && yok[r]) ? __ldcs(a.lo + rowbase + (size_t)r * nz) : mk<T>((T)0, (T)0);
+      }
       const V xv1 = splat<T>(xnext);
       const T pxv = pnext;
       {
@@ -681,16 +699,43 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
         const V ym3 = yc[r], ym2 = yc[r + 1], ym1 = yc[r + 2];
         const V yp1 = yc[r + 4], yp2 = yc[r + 5], yp3 = yc[r + 6];
         const V* zr = col + r * TZP;
-        V lap = P::mul(ta.k[9], craw);
-        lap = P::fma(ta.k[0], P::add(xm3, xp3), lap);
-        lap = P::fma(ta.k[1], P::add(xm2, xp2), lap);
-        lap = P::fma(ta.k[2], P::add(xm1, xp1), lap);
-        lap = P::fma(ta.k[3], P::add(ym3, yp3), lap);
-        lap = P::fma(ta.k[4], P::add(ym2, yp2), lap);
-        lap = P::fma(ta.k[5], P::add(ym1, yp1), lap);
-        lap = P::fma(ta.k[6], P::add(zr[-3], zr[3]), lap);
-        lap = P::fma(ta.k[7], P::add(zr[-2], zr[2]), lap);
-        lap = P::fma(ta.k[8], P::add(zr[-1], zr[1]), lap);
+        // The stencil in difference form, sum_j k_j ((v_-j - c) + (v_+j - c)):
+        // equal to the centre-weighted form in exact arithmetic, but
+        // neighbouring values of a resolved field differ by little, so the
+        // differences are exact or nearly so and the rounding scales with the
+        // Laplacian itself instead of with the partial sums (490/180 h^-2 |psi|
+        // per axis cancelling to |lap psi|).
+        auto lap_diff = [&]() {
+          V d = P::mul(ta.k[0], P::add(P::sub(xm3, craw), P::sub(xp3, craw)));
+          d = P::fma(ta.k[1], P::add(P::sub(xm2, craw), P::sub(xp2, craw)), d);
+          d = P::fma(ta.k[2], P::add(P::sub(xm1, craw), P::sub(xp1, craw)), d);
+          d = P::fma(ta.k[3], P::add(P::sub(ym3, craw), P::sub(yp3, craw)), d);
+          d = P::fma(ta.k[4], P::add(P::sub(ym2, craw), P::sub(yp2, craw)), d);
+          d = P::fma(ta.k[5], P::add(P::sub(ym1, craw), P::sub(yp1, craw)), d);
+          d = P::fma(ta.k[6], P::add(P::sub(zr[-3], craw), P::sub(zr[3], craw)), d);
+          d = P::fma(ta.k[7], P::add(P::sub(zr[-2], craw), P::sub(zr[2], craw)), d);
+          d = P::fma(ta.k[8], P::add(P::sub(zr[-1], craw), P::sub(zr[1], craw)), d);
+          return d;
+        };
+        V lap;
+        if constexpr (COMP) {
+          // the compensated form also takes the more accurate stencil: its
+          // point is FP32 results close to FP64 ones
+          lap = lap_diff();
+        } else {
+          // the reference's form (deriv.f90:19-25): the centre term and the
+          // symmetric pairs, accumulated with FMAs
+          lap = P::mul(ta.k[9], craw);
+          lap = P::fma(ta.k[0], P::add(xm3, xp3), lap);
+          lap = P::fma(ta.k[1], P::add(xm2, xp2), lap);
+          lap = P::fma(ta.k[2], P::add(xm1, xp1), lap);
+          lap = P::fma(ta.k[3], P::add(ym3, yp3), lap);
+          lap = P::fma(ta.k[4], P::add(ym2, yp2), lap);
+          lap = P::fma(ta.k[5], P::add(ym1, yp1), lap);
+          lap = P::fma(ta.k[6], P::add(zr[-3], zr[3]), lap);
+          lap = P::fma(ta.k[7], P::add(zr[-2], zr[2]), lap);
+          lap = P::fma(ta.k[8], P::add(zr[-1], zr[1]), lap);
+        }
         V fr = mk<T>((T)0, (T)0);
         if (ANALYTIC || a.frame_mode != FRAME_NONE) {
           // D1 without 1/(60h): (v3 - v-3) - 9 (v2 - v-2) + 45 (v1 - v-1)
@@ -715,23 +760,16 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
           c = P::mul(vscale, craw);
           lap = P::mul(vscale, lap);
         }
-        // FP32 diagnostics: the kinetic sum takes the same stencil in difference
-        // form, sum_j k_j ((v_-j - c) + (v_+j - c)).  Neighbouring values of a
-        // resolved field differ by little, so the differences are exact or
-        // nearly so, and the result carries FP32 rounding of the Laplacian
-        // itself instead of the ~1e4x larger rounding of the centre-weighted
-        // sum (490/180 h^-2 |psi| per axis cancelling to |lap psi|).
+        // FP32 energy sums (diagnostics and the imaginary-time loop's energy of
+        // stage 1) take the kinetic term from the difference form, which
+        // carries the FP32 rounding of the Laplacian itself instead of the
+        // ~1e4x larger rounding of the centre-weighted sum; the update keeps
+        // the reference's form.  With the centre-weighted sum the energy of a
+        // converged FP32 state scatters by a few 1e-10 relative from step to
+        // step, which is what an |dE| stop test sees.
         V lapd = lap;
-        if constexpr (KIND == ST_DIAG && sizeof(T) == 4) {
-          lapd = P::mul(ta.k[0], P::add(P::sub(xm3, craw), P::sub(xp3, craw)));
-          lapd = P::fma(ta.k[1], P::add(P::sub(xm2, craw), P::sub(xp2, craw)), lapd);
-          lapd = P::fma(ta.k[2], P::add(P::sub(xm1, craw), P::sub(xp1, craw)), lapd);
-          lapd = P::fma(ta.k[3], P::add(P::sub(ym3, craw), P::sub(yp3, craw)), lapd);
-          lapd = P::fma(ta.k[4], P::add(P::sub(ym2, craw), P::sub(yp2, craw)), lapd);
-          lapd = P::fma(ta.k[5], P::add(P::sub(ym1, craw), P::sub(yp1, craw)), lapd);
-          lapd = P::fma(ta.k[6], P::add(P::sub(zr[-3], craw), P::sub(zr[3], craw)), lapd);
-          lapd = P::fma(ta.k[7], P::add(P::sub(zr[-2], craw), P::sub(zr[2], craw)), lapd);
-          lapd = P::fma(ta.k[8], P::add(P::sub(zr[-1], craw), P::sub(zr[1], craw)), lapd);
+        if constexpr ((KIND == ST_DIAG || (IMAG && KIND == ST_S1)) && sizeof(T) == 4 && !COMP) {
+          lapd = lap_diff();
           if (!PLAIN) lapd = P::mul(vscale, lapd);
         }
         T pot = pxv + pyv[r] + pzv;
@@ -751,10 +789,20 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
           wn = (KIND == ST_S1 || KIND == ST_S1W) ? cr : P::fma(ta.k[14], wv, cr);
           pn = P::fma(ta.k[15], wn, c);
         }
+        V lon = mk<T>((T)0, (T)0);
+        if constexpr (COMP) {
+          // TwoSum of psi and the increment B w + lo: pn + lon == c + inc exactly
+          const V inc = P::fma(ta.k[15], wn, lov[r]);
+          const V sum = P::add(c, inc);
+          const V bb = P::sub(sum, c);
+          lon = P::add(P::sub(c, P::sub(sum, bb)), P::sub(inc, bb));
+          pn = sum;
+        }
         if (store && zok && yok[r]) {
           const size_t idx = rowbase + (size_t)r * nz;
           if (KIND == ST_S1 || KIND == ST_S2 || KIND == ST_S1W || KIND == ST_S2D) a.w[idx] = wn;
           if (KIND != ST_DIAG && KIND != ST_S1W) a.psi_out[idx] = pn;
+          if constexpr (COMP) __stcs(a.lo + idx, lon);
           if (!PLAIN) {
             if (GEN ? a.reduce == 1 : KIND == ST_S3) rN.add(pn.x * pn.x + pn.y * pn.y);
             if (GEN ? (KIND == ST_DIAG || a.reduce == 2) : KIND == ST_S1) {

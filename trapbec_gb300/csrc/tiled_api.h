@@ -25,6 +25,7 @@ struct TiledPlan {
   CUtensorMap tmw1;      // second w buffer, interior tiles (S3 of the deferred form)
   CUtensorMap tmwg;      // w with the ghost frame (deferred S2 reads w1 like psi)
   int defer_ok = 0;      // the deferred real-time form can run (FP32, second w buffer)
+  int comp_ok = 0;       // the compensated-state real-time stages are built for this shape
   int* err = nullptr;    // device error flag (owned by the context)
   uint32_t wait_us = 2000000;   // microseconds before a wait gives up
   int inject_wait = 0;   // test hook: waits aim at a phase that never completes

@@ -111,6 +111,17 @@ int plan_shape(const trapbec_params& p, void* const psi[2], void* w, void* w2, i
                                             {(const void*)k11, G::SMEM}};
   for (const auto& k : ks)
     if (cudaFuncSetAttribute(k.first, cudaFuncAttributeMaxDynamicSharedMemorySize, k.second) != cudaSuccess) return 4;
+  // the compensated-state real-time stages (FP32, two rows per thread: the
+  // remainders take registers that four-row tiles do not have)
+  if constexpr (sizeof(T) == 4 && R <= 2) {
+    auto kc1 = stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S1, VAR_COMP, false>;
+    auto kc2 = stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S2, VAR_COMP, false>;
+    auto kc3 = stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S3, VAR_COMP, false>;
+    if (cudaFuncSetAttribute(kc1, cudaFuncAttributeMaxDynamicSharedMemorySize, sm_s1) != cudaSuccess ||
+        cudaFuncSetAttribute(kc2, cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM) != cudaSuccess ||
+        cudaFuncSetAttribute(kc3, cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM) != cudaSuccess)
+      return 4;
+  }
   int nb = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k2, G::NT, G::SMEM) != cudaSuccess || nb < 1) return 5;
   // the deferred real-time form (FP32): S1 stores w1 only, S2 forms psi1 from
@@ -142,6 +153,7 @@ int plan_shape(const trapbec_params& p, void* const psi[2], void* w, void* w2, i
   q.smem = G::SMEM;
   q.nt = G::NT;
   q.tz = TZ; q.ty = TY; q.r = R;
+  q.comp_ok = (sizeof(T) == 4 && R <= 2) ? 1 : 0;
   q.fix_y = fix_y; q.fix_z = fix_z; q.bcz = bcz;
   q.chunk = p.nx;   // tile-major order until set_chunk chooses otherwise
   q.err = err_flag;
@@ -191,6 +203,19 @@ int launch_shape(const TiledPlan& plan, int kind, const StageArgs<T>& a, cudaStr
       return cudaGetLastError() == cudaSuccess ? 0 : 8;
     } else {
       return 9;
+    }
+  }
+  if (a.lo != nullptr) {   // compensated-state real-time stages
+    if constexpr (sizeof(T) == 4 && R <= 2) {
+      if (!plain) return 11;
+      if (kind == ST_S1) stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S1, VAR_COMP, false><<<grid, G::NT, KindGeom<T, G, ST_S1>::SMEM, st>>>(*tm, *tmw, ta, BatchArgs{});
+      else if (kind == ST_S2) stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S2, VAR_COMP, false><<<grid, G::NT, G::SMEM, st>>>(*tm, *tmw, ta, BatchArgs{});
+      else if (kind == ST_S3) stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S3, VAR_COMP, false><<<grid, G::NT, G::SMEM, st>>>(*tm, *tmw, ta, BatchArgs{});
+      else return 11;
+      if (nblk) *nblk = grid;
+      return cudaGetLastError() == cudaSuccess ? 0 : 8;
+    } else {
+      return 11;
     }
   }
   if (tiled_imag(a, kind)) {

@@ -105,11 +105,18 @@ struct trapbec_ctx {
   int* h_err = nullptr;                // pinned copy
   int chunk_user = 0;                  // x-chunk requested by the caller (0 = automatic)
   int stage_form = TRAPBEC_RK3_THREE_STAGE;   // real-time RK3 form (trapbec_rk3_form)
+  double imag_escale = 0.0;            // stop test of RK3_RENORM: 0 relative, > 0 absolute (energy scale)
+  void* lo = nullptr;                  // rounding remainder of psi (compensated form, allocated on request)
+  bool lo_valid = false;               // lo belongs to the current psi (else it is cleared before use)
 };
 
 namespace {
 
 int g_nsm_cache = 0;
+
+// psi was changed by something other than a compensated real-time step: the
+// remainder array no longer belongs to it and is cleared before its next use.
+inline void psi_changed(trapbec_ctx* c) { c->lo_valid = false; }
 
 template <typename T> T eps_of() { return std::numeric_limits<T>::epsilon(); }
 
@@ -277,9 +284,15 @@ int check_device_error(trapbec_ctx* c) {
 // Launch one stage.  kind: StageKind or 4 (diagnostics).  Returns status.
 template <typename T>
 int launch_stage(trapbec_ctx* c, int kind, StageArgs<T>& a, int* nblk_out) {
-  const bool rt = rt_kind(kind) && tiled_plain(a);
+  // plain real-time stages take the real-time plan, unless they carry the
+  // compensated state and its shape does not build that variant
+  const bool rt = rt_kind(kind) && tiled_plain(a) && !(a.lo && !(c->plan_rt_valid && c->plan_rt.comp_ok));
   TiledPlan& plan = rt ? c->plan_rt : c->plan;
   const bool tiled = c->kernel_kind != 1 && (rt ? c->plan_rt_valid : c->plan_valid);
+  if (a.lo && !(tiled && plan.comp_ok)) {
+    set_error("the compensated real-time form needs the tiled FP32 kernel on a two-row tile shape");
+    return TRAPBEC_ERR_UNSUPPORTED;
+  }
   plan.wait_us = c->wait_us;
   plan.inject_wait = c->inject_wait;
   if (!tiled && (kind == ST_S1W || kind == ST_S2D)) {
@@ -317,6 +330,7 @@ template <typename T> int apply_pending_scale(trapbec_ctx* c) {
     scale_kernel<T><<<simple_grid(c), SIMPLE_THREADS, 0, c->st>>>((c_t<T>*)c->psi[c->cur], c->n, (T)s);
     CKL();
     c->launches++;
+    psi_changed(c);
     c->host_ctrl->scale = 1.0;
     CK(cudaMemcpyAsync(c->ctrl, c->host_ctrl, sizeof(ImagCtrl), cudaMemcpyHostToDevice, c->st));
     CK(cudaStreamSynchronize(c->st));
@@ -379,6 +393,12 @@ template <typename T> int do_step_rt(trapbec_ctx* c, int nsteps) {
   // eye*0.5*dt = (0, 0.5)*dt = (-0.5*Im dt, 0.5*Re dt)  (run.f90:47)
   T cre = -(T)0.5 * dci, cim = (T)0.5 * dcr;
   const T a2 = (T)(-2.) / (T)3.;
+  const bool comp = c->stage_form == TRAPBEC_RK3_COMPENSATED;
+  if (comp) {
+    if (!c->lo) { set_error("compensated form: remainder array missing"); return TRAPBEC_ERR_STATE; }
+    if (!c->lo_valid) CK(cudaMemsetAsync(c->lo, 0, c->n * c->esz, c->st));   // a new state: no remainder yet
+  }
+  if (nsteps > 0) psi_changed(c);
   CK(cudaEventRecord(c->e0, c->st));
   for (int s = 0; s < nsteps; ++s) {
     rc = ensure_potential<T>(c, c->t);
@@ -386,6 +406,13 @@ template <typename T> int do_step_rt(trapbec_ctx* c, int nsteps) {
     StageArgs<T> a = base_args<T>(c, c->t);
     a.c_re = cre; a.c_im = cim;
     a.w = (c_t<T>*)c->w;
+    if (comp) {
+      if (!tiled_plain(a)) {
+        set_error("the compensated real-time form covers harmonic or no potential and a rotating or no frame");
+        return TRAPBEC_ERR_UNSUPPORTED;
+      }
+      a.lo = (c_t<T>*)c->lo;
+    }
     if (c->stage_form == TRAPBEC_RK3_DEFERRED && c->kernel_kind != 1 && c->plan_rt_valid && c->plan_rt.defer_ok &&
         tiled_plain(a)) {
       // deferred form: stage 1 stores w1 only; stage 2 forms psi1 = psi0 + w1/3
@@ -426,6 +453,7 @@ template <typename T> int do_step_rt(trapbec_ctx* c, int nsteps) {
   float ms = 0;
   CK(cudaEventElapsedTime(&ms, c->e0, c->e1));
   c->last_ms = ms;
+  if (comp) c->lo_valid = true;
   return check_device_error(c);
 }
 
@@ -434,6 +462,7 @@ template <typename T> int do_imag_euler(trapbec_ctx* c, int nsteps, int* steps_d
   if (rc) return rc;
   // run.f90:22: Psi = Psi + dt*0.5*rhs, with dt before the damping of run.f90:42
   T cre = (T)c->dt_re * (T)0.5, cim = (T)c->dt_im * (T)0.5;
+  psi_changed(c);
   double r = 0.0;
   for (int s = 0; s < nsteps; ++s) {
     if ((rc = ensure_potential<T>(c, c->t))) return rc;
@@ -471,6 +500,7 @@ template <typename T> int do_imag_rk3(trapbec_ctx* c, int nsteps, double tol, in
   c->host_ctrl->n0 = c->norm_target;
   c->host_ctrl->tol = tol;
   c->host_ctrl->dV = dV;
+  c->host_ctrl->escale = c->imag_escale;
   c->host_ctrl->converged = 0;
   c->host_ctrl->step = 0;
   c->host_ctrl->nonfinite = 0;
@@ -479,23 +509,34 @@ template <typename T> int do_imag_rk3(trapbec_ctx* c, int nsteps, double tol, in
   const T cf = (T)0.5 * (T)c->dt_re;
   const T a2 = (T)(-2.) / (T)3.;
   const int start_cur = c->cur;
+  psi_changed(c);
   CK(cudaEventRecord(c->e0, c->st));
   int nblk = 0;
-  for (int s = 0; s < nsteps; ++s) {
-    if ((rc = ensure_potential<T>(c, c->t))) return rc;
+  // stage 1 of the step from buffer `par`, with the energy of the incoming
+  // (renormalised) state reduced and handed to the energy finaliser
+  auto stage1_energy = [&](int par) -> int {
+    int r2 = ensure_potential<T>(c, c->t);
+    if (r2) return r2;
     StageArgs<T> a = base_args<T>(c, c->t);
     a.c_re = cf; a.c_im = 0;
     a.w = (c_t<T>*)c->w;
     a.ctrl = c->ctrl;
-    int par = (start_cur + s) & 1;
-    // stage 1 (+ energy of the incoming, renormalised state)
     a.psi_in = (const c_t<T>*)c->psi[par]; a.psi_out = (c_t<T>*)c->psi[par ^ 1];
     a.A = 0; a.B = (T)1 / (T)3;
     a.red = c->red; a.reduce = 2; a.use_ctrl_scale = 1;
-    if ((rc = launch_stage<T>(c, ST_S1, a, &nblk))) return rc;
+    if ((r2 = launch_stage<T>(c, ST_S1, a, &nblk))) return r2;
     imag_fin_energy_kernel<<<1, FIN_THREADS, 0, c->st>>>(c->red, nblk, c->ctrl);
     CKL();
     c->launches++;
+    return TRAPBEC_OK;
+  };
+  for (int s = 0; s < nsteps; ++s) {
+    int par = (start_cur + s) & 1;
+    if ((rc = stage1_energy(par))) return rc;
+    StageArgs<T> a = base_args<T>(c, c->t);
+    a.c_re = cf; a.c_im = 0;
+    a.w = (c_t<T>*)c->w;
+    a.ctrl = c->ctrl;
     a.reduce = 0; a.red = nullptr; a.use_ctrl_scale = 0;
     a.psi_in = (const c_t<T>*)c->psi[par ^ 1]; a.psi_out = (c_t<T>*)c->psi[par];
     a.A = a2; a.B = (T)1;
@@ -534,22 +575,24 @@ template <typename T> int do_imag_rk3(trapbec_ctx* c, int nsteps, double tol, in
     return TRAPBEC_ERR_NONFINITE;
   }
   if (!h.converged) {
-    // Energy of the final state (the loop forms E_n in the next step's stage 1).
-    if ((rc = apply_pending_scale<T>(c))) return rc;
-    if ((rc = run_diag<T>(c))) return rc;
-    trapbec_diag_out d;
-    fill_diag<T>(c, &d);
-    double rel = h.have_prev ? std::fabs(d.energy - h.e_prev) / std::fabs(d.energy) : INFINITY;
-    h.e_prev = d.energy;
-    h.have_prev = 1;
-    h.rel = rel;
-    h.energy = d.energy;
-    h.mu = d.mu;
-    CK(cudaMemcpyAsync(c->ctrl, c->host_ctrl, sizeof(ImagCtrl), cudaMemcpyHostToDevice, c->st));
+    // Energy of the final state, which the loop forms in the next step's
+    // stage 1: run that stage-1 evaluation once more (its psi and w outputs go
+    // to the spare buffers and are discarded; the state stays in c->cur with
+    // its renormalisation pending), so the last |dE| compares two energies of
+    // the same evaluation.  It may meet the stop test; no step is counted.
+    if ((rc = stage1_energy(c->cur))) return rc;
+    CK(cudaMemcpyAsync(c->host_ctrl, c->ctrl, sizeof(ImagCtrl), cudaMemcpyDeviceToHost, c->st));
     CK(cudaStreamSynchronize(c->st));
-  } else {
-    if ((rc = apply_pending_scale<T>(c))) return rc;
+    if ((rc = check_device_error(c))) { *steps_done = done; *rel_out = NAN; return rc; }
+    if (h.nonfinite) {
+      *steps_done = done;
+      *rel_out = NAN;
+      set_error("non-finite energy in imaginary-time relaxation");
+      return TRAPBEC_ERR_NONFINITE;
+    }
+    if (done == 0) h.rel = INFINITY;   // nothing to compare with
   }
+  if ((rc = apply_pending_scale<T>(c))) return rc;
   *steps_done = done;
   *rel_out = h.rel;
   return TRAPBEC_OK;
@@ -557,6 +600,7 @@ template <typename T> int do_imag_rk3(trapbec_ctx* c, int nsteps, double tol, in
 
 template <typename T> int init_state_impl(trapbec_ctx* c, const char* name, const trapbec_init_args* ia) {
   const trapbec_params& p = c->p;
+  psi_changed(c);
   std::string nm(name);
   InitArgsDev<T> a;
   std::memset(&a, 0, sizeof(a));
@@ -755,7 +799,7 @@ template <typename T> int create_impl(trapbec_ctx* c) {
 
 void free_ctx(trapbec_ctx* c) {
   if (!c) return;
-  void* bufs[] = {c->psi[0], c->psi[1], c->w, c->w2, c->xx, c->yy, c->zz, c->px, c->py, c->pz,
+  void* bufs[] = {c->psi[0], c->psi[1], c->w, c->w2, c->lo, c->xx, c->yy, c->zz, c->px, c->py, c->pz,
                   c->trap_user, c->trap_eff, c->red, c->red_out, c->ctrl, c->d_err};
   for (void* b : bufs) if (b) cudaFree(b);
   if (c->host_red) cudaFreeHost(c->host_red);
@@ -920,6 +964,7 @@ void trapbec_destroy(trapbec_ctx* c) {
 
 int trapbec_set_psi(trapbec_ctx* c, const void* psi, int layout) {
   if (!c || !psi) return TRAPBEC_ERR_ARG;
+  psi_changed(c);
   if (layout == TRAPBEC_LAYOUT_INTERIOR) {
     CK(cudaMemcpyAsync(c->psi[c->cur], psi, c->n * c->esz, cudaMemcpyHostToDevice, c->st));
   } else if (layout == TRAPBEC_LAYOUT_GHOSTED) {
@@ -1034,6 +1079,20 @@ int trapbec_step_imag(trapbec_ctx* c, int nsteps, int variant, double tol, int* 
   if (steps_done) *steps_done = sd;
   if (stat_out) *stat_out = st;
   return rc;
+}
+
+int trapbec_set_imag_stop(trapbec_ctx* c, int mode, double energy_scale) {
+  if (!c) return TRAPBEC_ERR_ARG;
+  if (mode == TRAPBEC_STOP_REL) {
+    c->imag_escale = 0.0;
+    return TRAPBEC_OK;
+  }
+  if (mode != TRAPBEC_STOP_ABS || !(energy_scale > 0.0) || !std::isfinite(energy_scale)) {
+    set_error("trapbec_set_imag_stop: mode must be TRAPBEC_STOP_REL or TRAPBEC_STOP_ABS with a finite energy_scale > 0");
+    return TRAPBEC_ERR_ARG;
+  }
+  c->imag_escale = energy_scale;
+  return TRAPBEC_OK;
 }
 
 }  // extern "C"
@@ -1213,7 +1272,19 @@ int trapbec_get_tile_shape(trapbec_ctx* c, int real_time, int* tile_z, int* tile
 }
 
 int trapbec_set_stage_form(trapbec_ctx* c, int form) {
-  if (!c || (form != TRAPBEC_RK3_THREE_STAGE && form != TRAPBEC_RK3_DEFERRED)) return TRAPBEC_ERR_ARG;
+  if (!c || (form != TRAPBEC_RK3_THREE_STAGE && form != TRAPBEC_RK3_DEFERRED && form != TRAPBEC_RK3_COMPENSATED))
+    return TRAPBEC_ERR_ARG;
+  if (form == TRAPBEC_RK3_COMPENSATED) {
+    if (c->prec != TRAPBEC_FP32) {
+      set_error("the compensated form is for FP32 contexts (an FP64 state keeps its increments)");
+      return TRAPBEC_ERR_UNSUPPORTED;
+    }
+    if (!c->lo) {
+      CK(cudaMalloc(&c->lo, c->n * c->esz));
+      c->lo_valid = false;
+    }
+  }
+  if (form != c->stage_form) psi_changed(c);
   c->stage_form = form;
   if (form == TRAPBEC_RK3_DEFERRED && c->prec == TRAPBEC_FP32 && !c->p.two_dim && !c->w2) {
     // the second w buffer, then plans that know it
@@ -1225,8 +1296,8 @@ int trapbec_set_stage_form(trapbec_ctx* c, int form) {
   return TRAPBEC_OK;
 }
 
-int trapbec_get_stage_form(trapbec_ctx* c, int* deferred) {
-  if (!c || !deferred) return TRAPBEC_ERR_ARG;
+int trapbec_get_stage_form(trapbec_ctx* c, int* form) {
+  if (!c || !form) return TRAPBEC_ERR_ARG;
   StageArgs<float> a;
   std::memset(&a, 0, sizeof(a));
   bool plain = true;
@@ -1234,8 +1305,12 @@ int trapbec_get_stage_form(trapbec_ctx* c, int* deferred) {
     a = base_args<float>(c, c->t);
     plain = tiled_plain(a);
   }
-  *deferred = (c->stage_form == TRAPBEC_RK3_DEFERRED && c->prec == TRAPBEC_FP32 && c->kernel_kind != 1 &&
-               c->plan_rt_valid && c->plan_rt.defer_ok && plain) ? 1 : 0;
+  if (c->stage_form == TRAPBEC_RK3_COMPENSATED) {
+    *form = TRAPBEC_RK3_COMPENSATED;   // or the step reports TRAPBEC_ERR_UNSUPPORTED
+    return TRAPBEC_OK;
+  }
+  *form = (c->stage_form == TRAPBEC_RK3_DEFERRED && c->prec == TRAPBEC_FP32 && c->kernel_kind != 1 &&
+           c->plan_rt_valid && c->plan_rt.defer_ok && plain) ? TRAPBEC_RK3_DEFERRED : TRAPBEC_RK3_THREE_STAGE;
   return TRAPBEC_OK;
 }
 
@@ -1255,6 +1330,7 @@ template <typename T> int autotune_impl(trapbec_ctx* c, int steps, TuneVal* best
   key.p.nx = c->p.nx; key.p.ny = c->p.ny; key.p.nz = c->p.nz;
   key.p.precision = c->p.precision; key.p.boundaries = c->p.boundaries; key.p.periodicz = c->p.periodicz;
   key.p.potential = c->p.potential;
+  key.p.reserved[0] = c->stage_form;   // the compensated form runs on other shapes
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     for (auto& kv : g_tune_cache)
@@ -1272,6 +1348,7 @@ template <typename T> int autotune_impl(trapbec_ctx* c, int steps, TuneVal* best
   for (int sh = 0; sh < ns && rc == TRAPBEC_OK; ++sh) {
     TiledPlan plan;
     if (plan_tiled<T>(c->p, c->psi, c->w, c->w2, c->nsm, sh, c->d_err, &plan) != 0) continue;
+    if (c->stage_form == TRAPBEC_RK3_COMPENSATED && !plan.comp_ok) continue;
     std::vector<int> chunks = {16, 32, 64, c->p.nx};
     for (int L : chunks) {
       if (L > c->p.nx) continue;
@@ -1294,6 +1371,7 @@ template <typename T> int autotune_impl(trapbec_ctx* c, int steps, TuneVal* best
   c->cur = cur_save;
   c->t = t_save;
   c->kernel_kind = 0;
+  psi_changed(c);
   if (rc) return rc;
   if (bv.shape < 0) { set_error("no tiled kernel shape fits this grid"); return TRAPBEC_ERR_UNSUPPORTED; }
   if (plan_tiled<T>(c->p, c->psi, c->w, c->w2, c->nsm, bv.shape, c->d_err, &c->plan_rt) != 0) return TRAPBEC_ERR_CUDA;

@@ -106,6 +106,12 @@ class Solver:
                                          C.byref(s), C.byref(st)), "trapbec_step_imag")
         return s.value, st.value
 
+    def set_imag_stop(self, mode: int = abi.STOP_REL, energy_scale: float = 1.0) -> None:
+        """Stop test of later RK3_RENORM relaxations: abi.STOP_REL (|dE|/|E| <= tol, the default) or
+        abi.STOP_ABS (|dE| * energy_scale < tol, energy_scale converting the reference-unit energy
+        into the tolerance's unit, e.g. TrapProblem.energy_to_trap(1.0))."""
+        check(self.lib.trapbec_set_imag_stop(self.ctx, int(mode), float(energy_scale)), "trapbec_set_imag_stop")
+
     def diag(self) -> dict:
         d = DiagOut()
         check(self.lib.trapbec_diag(self.ctx, C.byref(d)), "trapbec_diag")
@@ -175,15 +181,20 @@ class Solver:
         return tz.value, ty.value
 
     def set_stage_form(self, form: int) -> None:
-        """Real-time RK3 form: abi.RK3_THREE_STAGE (default) or abi.RK3_DEFERRED
-        (stage 1 stores w1 only; allocates a second w buffer)."""
+        """Real-time RK3 form: abi.RK3_THREE_STAGE (default), abi.RK3_DEFERRED (stage 1 stores w1
+        only; allocates a second w buffer) or abi.RK3_COMPENSATED (FP32: the update keeps its
+        rounding remainder in a second array; allocates it)."""
         check(self.lib.trapbec_set_stage_form(self.ctx, int(form)), "trapbec_set_stage_form")
+
+    def stage_form(self) -> int:
+        """The form the next step_rt takes."""
+        v = C.c_int(0)
+        check(self.lib.trapbec_get_stage_form(self.ctx, C.byref(v)), "trapbec_get_stage_form")
+        return v.value
 
     def stage_form_deferred(self) -> bool:
         """True when the next step_rt takes the deferred form."""
-        v = C.c_int(0)
-        check(self.lib.trapbec_get_stage_form(self.ctx, C.byref(v)), "trapbec_get_stage_form")
-        return bool(v.value)
+        return self.stage_form() == abi.RK3_DEFERRED
 
     def autotune(self, steps: int = 3) -> dict:
         tz, ty, ch, ms = C.c_int(0), C.c_int(0), C.c_int(0), C.c_double(0)
