@@ -222,9 +222,13 @@ def timed_steps(s, steps, chunk, omega_of_step, start_step=0):
 
 
 def imag_leg(args):
-    """Batched imaginary-time ground states from the Thomas-Fermi guess: wall
-    time (device events around the whole graph-replayed loop) until every
-    instance reaches |dE|/|E| <= tol, on a bounded set of draws."""
+    """Batched imaginary-time ground states from the Thomas-Fermi guess (the
+    64-instance workload): device time (events around the whole
+    graph-replayed loop) until every instance meets the stop test or
+    max_steps.  The stop test is the workload's |dE| < tol on the energy per
+    particle in trap units (the wave function normalised to one, as the
+    Thomas-Fermi-scaled interaction g implies): |E_n - E_{n-1}| / N * 2 mu <
+    tol, formed in FP64 on the device."""
     from trapbec_gb300 import abi, units
     from trapbec_gb300.batch import BatchSolver
     draws = units.ground_state_draws(args.imag_count, args.imag_seed, grids=tuple(args.imag_grids),
@@ -233,20 +237,28 @@ def imag_leg(args):
     for i, (p, ini) in enumerate(draws):
         b.init_state(i, ini["name"], seed=ini["seed"], amp=ini["amp"], r_tf2=ini["r_tf2"],
                      noise_amp=ini["noise_amp"])
+    b.set_imag_stop(abi.STOP_ABS_PER_NORM, [p.mu_to_trap(1.0) for p, _ in draws])
     t0 = time.perf_counter()
     out = b.solve(max_steps=args.imag_max_steps, tol=args.imag_tol, check_every=200)
     wall = time.perf_counter() - t0
     st = b.stats()
-    conv = [b.status(i)["converged"] > 0 for i in range(len(draws))]
+    stat = [b.status(i) for i in range(len(draws))]
+    conv = [x["converged"] > 0 for x in stat]
     cells = sum(p.n[0] * p.n[1] * p.n[2] for p, _ in draws)
     b.close()
+    fast = [d["Omega"] / d["omega"][0] > 0.5 for _, d in draws]
     return {"guess": "thomas_fermi+1e-2 noise", "instances": len(draws), "cells": cells,
-            "grids": sorted(set(p.n[0] for p, _ in draws)), "tol_rel_dE": args.imag_tol,
+            "grids": sorted(set(p.n[0] for p, _ in draws)),
+            "stop": "|d(E/N)| < tol, energy per particle in trap units (FP64)", "tol": args.imag_tol,
             "dtau_trap_units": 0.002, "max_steps": args.imag_max_steps,
             "converged": int(sum(conv)), "steps_median": float(statistics.median(out["steps"])),
             "steps_max": int(max(out["steps"])), "solve_ms_device": st["solve_ms"], "wall_s": wall,
-            "tile": [st["tile_z"], st["tile_y"]], "precision": ("c64 state; norm and energy sums compensated float-float (FP32 arithmetic, ~44 bits); "
-                          "renormalisation, energy and |dE|/|E| test in FP64")}
+            "not_converged_fast_rotating": int(sum(1 for c, f in zip(conv, fast) if not c and f)),
+            "not_converged_slow_rotating": int(sum(1 for c, f in zip(conv, fast) if not c and not f)),
+            "last_dE_per_particle_not_converged": [x["rel"] for x in stat if x["converged"] <= 0],
+            "tile": [st["tile_z"], st["tile_y"]],
+            "precision": ("c64 state; norm and energy sums compensated float-float (FP32 arithmetic, ~44 bits) "
+                          "with the kinetic term in difference form; renormalisation, energy and stop test in FP64")}
 
 
 def warmstart_leg(args):
@@ -261,11 +273,12 @@ def warmstart_leg(args):
     net = surrogate.Surrogate(128, 2, seed=0)
     net.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "trapbec_gb300", "weights",
                           "surrogate_128.npz"))
-    r = surrogate.compare(net, draws, tol=args.imag_tol, max_steps=args.ws_max_steps)
+    r = surrogate.compare(net, draws, tol=args.imag_tol, max_steps=args.ws_max_steps, stop="per_particle")
     med = lambda v: float(statistics.median(v))
     return {
         "grid": 128, "instances": len(draws), "held_out": f"draws {n0}..{n0 + len(draws) - 1} of seed 2024",
-        "tol_rel_dE": args.imag_tol, "dtau_trap_units": 0.002, "max_steps": args.ws_max_steps,
+        "stop": "|d(E/N)| < tol, energy per particle in trap units (FP64)", "tol": args.imag_tol,
+        "dtau_trap_units": 0.002, "max_steps": args.ws_max_steps,
         "surrogate_params": net.np, "nn_used": r["nn_used"],
         "steps_tf": r["tf"]["steps"], "steps_nn": r["nn"]["steps"],
         "converged_tf": int(sum(r["tf"]["converged"])), "converged_nn": int(sum(r["nn"]["converged"])),
@@ -359,12 +372,15 @@ def run_gpu_arm(args):
     peak, peak_kind = load_peaks()
     # algorithmic bytes per grid point per RK3 step: S1 24 + S2 32 + S3 24 (complex FP32);
     # the deferred form stores no psi1 (S1 16 B); FP64 doubles every figure
-    deferred = s.stage_form_deferred()
-    bpc = (72.0 if deferred else 80.0) if prec == abi.FP32 else 160.0
+    form_run = s.stage_form()
+    deferred = form_run == abi.RK3_DEFERRED
+    bpc = {abi.RK3_THREE_STAGE: 80.0, abi.RK3_DEFERRED: 72.0, abi.RK3_COMPENSATED: 128.0}[form_run] \
+        if prec == abi.FP32 else 160.0
     achieved = cells * args.steps * bpc / (ms * 1e-3) / 1e9
     tag = "fp32" if prec == abi.FP32 else "fp64"
     tz_run, ty_run = s.tile_shape(real_time=True)
-    tpp = profile_traffic(tag, tz_run, ty_run, form="deferred" if deferred else "")
+    tpp = profile_traffic(tag, tz_run, ty_run,
+                          form={abi.RK3_DEFERRED: "deferred", abi.RK3_COMPENSATED: "compensated"}.get(form_run, ""))
     traffic = tpp * cells if tpp else None
 
     kernel_name = "tiled TMA stage kernel" if args.kernel is None or args.kernel[0] != 1 else "per-cell stage kernel"
@@ -441,6 +457,7 @@ def run_gpu_arm(args):
             ms_, _ = timed_steps(sol, P, chunk, omega_of_step, 0)
             runs[form_tag] = (dstart, sol.diag(), sol.get_psi().astype(np.complex128), ms_)
 
+        s.set_stage_form(abi.RK3_THREE_STAGE)
         run_form(s, "fp32")
         s.set_stage_form(abi.RK3_COMPENSATED)
         tune_c = None if args.no_autotune else s.autotune(steps=4)
@@ -518,8 +535,11 @@ def run_gpu_arm(args):
                    "chunk_steps": chunk, "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2_flush": "inputs larger than L2 (1 GiB per array)",
                    "kernel": kernel_name, "tile": [tz_run, ty_run], "autotune": tune,
-                   "rk3_form": ("deferred psi1: stage 1 stores w1 only, stage 2 forms psi1 = psi0 + w1/3 "
-                                "(bit-identical)") if deferred else "three full stages"},
+                   "rk3_form": {abi.RK3_THREE_STAGE: "three full stages",
+                                abi.RK3_DEFERRED: ("deferred psi1: stage 1 stores w1 only, stage 2 forms psi1 = "
+                                                   "psi0 + w1/3 (bit-identical)"),
+                                abi.RK3_COMPENSATED: "compensated state (remainder array, difference-form stencil)"}
+                               [form_run]},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                      "algorithmic_bytes_per_point_step": bpc,

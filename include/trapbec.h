@@ -204,14 +204,16 @@ int trapbec_step_imag(trapbec_ctx* ctx, int nsteps, int variant, double tol,
 
 /* Stop test of the RK3_RENORM relaxation (new; the reference relaxes a fixed
  * number of steps, run.f90:20-33).
- *  TRAPBEC_STOP_REL (default): |E_n - E_{n-1}| <= tol * |E_n|
- *  TRAPBEC_STOP_ABS:           |E_n - E_{n-1}| * energy_scale < tol
- * E is the energy trapbec_diag reports (reference units); energy_scale > 0
- * converts it into the unit the tolerance is stated in (for a trap-units
- * problem mapped as in the header comment of trapbec_params: (mu/g) a^3 2 mu
- * for the total energy, that divided by the trap-units norm for the energy
- * per particle).  Applies to later trapbec_step_imag calls.                */
-enum trapbec_imag_stop { TRAPBEC_STOP_REL = 0, TRAPBEC_STOP_ABS = 1 };
+ *  TRAPBEC_STOP_REL (default):  |E_n - E_{n-1}| <= tol * |E_n|
+ *  TRAPBEC_STOP_ABS:            |E_n - E_{n-1}| * energy_scale < tol
+ *  TRAPBEC_STOP_ABS_PER_NORM:   |E_n - E_{n-1}| / N * energy_scale < tol
+ * E is the energy trapbec_diag reports and N the norm target (reference
+ * units); energy_scale > 0 converts into the unit the tolerance is stated
+ * in.  For a trap-units problem (x = a x', t = a^2 t', phi = sqrt(mu/g) psi,
+ * a = 1/sqrt(2 mu)) the total energy takes (mu/g) a^3 2 mu and the energy
+ * per particle (ABS_PER_NORM) takes 2 mu.  Applies to later
+ * trapbec_step_imag calls.                                                  */
+enum trapbec_imag_stop { TRAPBEC_STOP_REL = 0, TRAPBEC_STOP_ABS = 1, TRAPBEC_STOP_ABS_PER_NORM = 2 };
 int trapbec_set_imag_stop(trapbec_ctx* ctx, int mode, double energy_scale);
 
 /* Diagnostics of the current psi.  intpsi2/maxpsi/minpsi/meanpsi follow
@@ -399,8 +401,9 @@ int trapbec_batch_solve_imag(trapbec_batch* b, int max_steps, double tol, int ch
                              int* steps_out, double* energy_out, double* mu_out);
 /* Stop test of later solves (trapbec_imag_stop, as trapbec_set_imag_stop):
  * TRAPBEC_STOP_ABS stops instance i when |E_n - E_{n-1}| * energy_scale[i]
- * < tol; energy_scale may be NULL (a scale of 1 for every instance), and
- * TRAPBEC_STOP_REL ignores it.                                             */
+ * < tol, TRAPBEC_STOP_ABS_PER_NORM when |E_n - E_{n-1}| / N_i *
+ * energy_scale[i] < tol; energy_scale may be NULL (a scale of 1 for every
+ * instance), and TRAPBEC_STOP_REL ignores it.                              */
 int trapbec_batch_set_imag_stop(trapbec_batch* b, int mode, const double* energy_scale);
 /* Fill instance `inst` with a Thomas-Fermi state ("thomas_fermi", from the
  * instance's harm_w*) or a workload state ("tf_noise", "tf_vortex_line",

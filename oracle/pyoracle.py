@@ -56,7 +56,7 @@ def lib() -> C.CDLL:
         L.orc_step_imag_rk3.argtypes = [vp, C.c_int, C.c_double, C.POINTER(C.c_int),
                                         C.POINTER(C.c_double)]
         L.orc_set_norm_target.argtypes = [vp, C.c_double]
-        L.orc_set_imag_stop.argtypes = [vp, C.c_double]
+        L.orc_set_imag_stop.argtypes = [vp, C.c_int, C.c_double]
         L.orc_set_omega.argtypes = [vp, C.c_double]
         L.orc_set_t.argtypes = [vp, C.c_double]
         L.orc_diag.argtypes = [vp, C.POINTER(DiagOut)]
@@ -172,9 +172,10 @@ class Oracle:
             raise RuntimeError(f"oracle imag rk3 failed: {rc}")
         return s.value, r.value
 
-    def set_imag_stop(self, energy_scale: float = 0.0) -> None:
-        """0: relative stop |dE|/|E| <= tol; > 0: absolute |dE| * energy_scale < tol."""
-        lib().orc_set_imag_stop(self.h, float(energy_scale))
+    def set_imag_stop(self, mode: int = 0, energy_scale: float = 0.0) -> None:
+        """mode 0: relative stop |dE|/|E| <= tol; 1: absolute |dE| * energy_scale < tol;
+        2: absolute per unit norm |dE| / N0 * energy_scale < tol (the trapbec_imag_stop modes)."""
+        lib().orc_set_imag_stop(self.h, int(mode), float(energy_scale))
 
     def set_norm_target(self, n0: float) -> None:
         lib().orc_set_norm_target(self.h, float(n0))

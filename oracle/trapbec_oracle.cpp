@@ -111,7 +111,9 @@ template <typename T> struct Oracle {
   double norm_target = -1.0;
   bool norm_user = false;   // set by orc_set_norm_target; otherwise derived from each new state
   double e_prev = std::numeric_limits<double>::quiet_NaN();
-  double imag_escale = 0.0;   // stop test: 0 relative |dE|/|E| <= tol; > 0 absolute |dE| * escale < tol
+  int imag_stop = 0;          // stop test: 0 relative |dE|/|E| <= tol; 1 absolute |dE| * escale < tol;
+                              // 2 absolute per unit norm |dE| / N0 * escale < tol
+  double imag_escale = 0.0;
   double intpsi2_old = 1.0;
 
   explicit Oracle(const trapbec_params& pp) : p(pp) {
@@ -634,9 +636,9 @@ template <typename T> struct Oracle {
       });
       diag(&d);
       const double dE = std::fabs(d.energy - e_prev);
-      rel = imag_escale > 0.0 ? dE * imag_escale : dE / std::fabs(d.energy);
+      rel = imag_stop == 0 ? dE / std::fabs(d.energy) : (imag_stop == 2 ? dE / norm_target : dE) * imag_escale;
       e_prev = d.energy;
-      if (imag_escale > 0.0 ? rel < tol : rel <= tol) break;
+      if (imag_stop == 0 ? rel <= tol : rel < tol) break;
     }
     if (s > nsteps) s = nsteps;
     *steps_done = s;
@@ -1193,8 +1195,8 @@ int orc_step_imag_euler(void* h, int nsteps, double* ratio) {
 int orc_step_imag_rk3(void* h, int nsteps, double tol, int* steps_done, double* rel) {
   return dispatch((Handle*)h, [&](auto& o) { return o.imag_rk3(nsteps, tol, steps_done, rel); });
 }
-int orc_set_imag_stop(void* h, double escale) {
-  return dispatch((Handle*)h, [&](auto& o) { o.imag_escale = escale > 0.0 ? escale : 0.0; return 0; });
+int orc_set_imag_stop(void* h, int mode, double escale) {
+  return dispatch((Handle*)h, [&](auto& o) { o.imag_stop = mode; o.imag_escale = escale; return 0; });
 }
 int orc_set_norm_target(void* h, double n0) {
   return dispatch((Handle*)h, [&](auto& o) { o.norm_target = n0; o.norm_user = n0 > 0; return 0; });

@@ -241,12 +241,22 @@ def test_imag_rk3_absolute_stop_matches_oracle():
     s.set_psi(psi)
     o.set_psi(psi)
     s.set_imag_stop(abi.STOP_ABS, scale)
-    o.set_imag_stop(scale)
+    o.set_imag_stop(abi.STOP_ABS, scale)
     sg, rg = s.step_imag(5000, abi.IMAG_RK3_RENORM, tol)
     so, ro = o.step_imag_rk3(5000, tol)
     assert 10 < sg < 5000 and abs(sg - so) <= 1, (sg, so)
     assert rg < tol and ro < tol
     assert rel_err(s.get_psi(), o.get_psi()) < 1e-8
+    # the energy per unit norm: |dE| / N0 * scale < tol
+    s2, o2 = Solver(p), Oracle(p)
+    s2.set_psi(psi)
+    o2.set_psi(psi)
+    s2.set_imag_stop(abi.STOP_ABS_PER_NORM, scale)
+    o2.set_imag_stop(abi.STOP_ABS_PER_NORM, scale)
+    sn, rn = s2.step_imag(5000, abi.IMAG_RK3_RENORM, tol)
+    on, ron = o2.step_imag_rk3(5000, tol)
+    assert 10 < sn < 5000 and abs(sn - on) <= 1, (sn, on)
+    assert rn < tol and ron < tol
     # back to the relative test: from the converged state it stops within a few steps
     s.set_imag_stop(abi.STOP_REL)
     sg2, rg2 = s.step_imag(100, abi.IMAG_RK3_RENORM, 1e-6)

@@ -64,13 +64,14 @@ struct BInst {
   double dV = 0.0;
   long long units = 0; // work units of this instance for the current shape
   int ntz = 0, nty = 0;
-  double escale = 0.0; // stop test: 0 relative, > 0 absolute with this energy scale
+  double escale = 0.0; // energy scale of the absolute stop tests
 };
 
 }  // namespace
 
 struct trapbec_batch {
   int prec = TRAPBEC_FP32;
+  int stop_mode = TRAPBEC_STOP_REL;   // trapbec_imag_stop of later solves
   int ninst = 0;
   int nsm = 0;
   size_t esz = 8, rsz = 4;
@@ -491,6 +492,7 @@ void reset_ctrl(trapbec_batch* b, int i, double tol) {
   c.tol = tol;
   c.dV = b->in[i].dV;
   c.escale = b->in[i].escale;
+  c.stop_mode = b->stop_mode;
   c.rel = INFINITY;
 }
 
@@ -763,10 +765,11 @@ int trapbec_batch_set_imag_stop(trapbec_batch* b, int mode, const double* energy
   if (!b) return TRAPBEC_ERR_ARG;
   if (mode == TRAPBEC_STOP_REL) {
     for (auto& I : b->in) I.escale = 0.0;
+    b->stop_mode = mode;
     return TRAPBEC_OK;
   }
-  if (mode != TRAPBEC_STOP_ABS) {
-    set_error("trapbec_batch_set_imag_stop: mode must be TRAPBEC_STOP_REL or TRAPBEC_STOP_ABS");
+  if (mode != TRAPBEC_STOP_ABS && mode != TRAPBEC_STOP_ABS_PER_NORM) {
+    set_error("trapbec_batch_set_imag_stop: mode must be TRAPBEC_STOP_REL, TRAPBEC_STOP_ABS or TRAPBEC_STOP_ABS_PER_NORM");
     return TRAPBEC_ERR_ARG;
   }
   for (int i = 0; i < b->ninst; ++i) {
@@ -777,6 +780,7 @@ int trapbec_batch_set_imag_stop(trapbec_batch* b, int mode, const double* energy
     }
   }
   for (int i = 0; i < b->ninst; ++i) b->in[i].escale = energy_scale ? energy_scale[i] : 1.0;
+  b->stop_mode = mode;
   return TRAPBEC_OK;
 }
 

@@ -51,12 +51,13 @@ struct ImagCtrl {
   double n0;        // norm target
   double tol;       // convergence tolerance
   double dV;        // cell volume
-  double escale;    // 0: stop when |dE|/|E| <= tol; > 0: stop when |dE| * escale < tol
-                    // (escale converts the reference-unit energy into the caller's unit)
+  double escale;    // stop_mode 1: |dE| * escale < tol; 2: |dE| / n0 * escale < tol
+                    // (escale converts the reference-unit energy, or energy per norm, into the caller's unit)
   int have_prev;    // e_prev is valid
   int converged;    // |dE|/|E| <= tol reached (stages become no-ops)
   int step;         // completed steps in the current call
   int nonfinite;    // a norm or energy was NaN/Inf
+  int stop_mode;    // trapbec_imag_stop: 0 |dE|/|E| <= tol, 1 absolute, 2 absolute per unit norm
 };
 
 template <typename T> struct StageArgs {

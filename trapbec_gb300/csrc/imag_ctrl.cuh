@@ -8,7 +8,8 @@
 // reproducible), and update the control block in FP64.  The stop test is on
 // the energy change of consecutive states: relative, |E_n - E_{n-1}| <=
 // tol |E_n|, or absolute in the caller's energy unit, |E_n - E_{n-1}| *
-// escale < tol (ImagCtrl::escale > 0).
+// escale < tol, or absolute per unit norm, |E_n - E_{n-1}| / N0 * escale <
+// tol (ImagCtrl::stop_mode 0, 1, 2).
 #pragma once
 #include "common.cuh"
 #include "kernels_simple.cuh"
@@ -33,10 +34,11 @@ __device__ __forceinline__ void imag_energy_update(const double* r, ImagCtrl* c)
   if (!isfinite(E)) { c->nonfinite = 1; return; }
   if (c->have_prev) {
     // relative test |dE|/|E| <= tol, or the absolute |dE| * escale < tol
+    // (per unit norm: |dE| / n0 * escale < tol)
     const double dE = fabs(E - c->e_prev);
-    const double rel = c->escale > 0.0 ? dE * c->escale : dE / fabs(E);
+    const double rel = c->stop_mode == 0 ? dE / fabs(E) : (c->stop_mode == 2 ? dE / c->n0 : dE) * c->escale;
     c->rel = rel;
-    if (c->escale > 0.0 ? rel < c->tol : rel <= c->tol) c->converged = 1;
+    if (c->stop_mode == 0 ? rel <= c->tol : rel < c->tol) c->converged = 1;
   }
   c->e_prev = E;
   c->have_prev = 1;

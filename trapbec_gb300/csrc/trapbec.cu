@@ -105,7 +105,8 @@ struct trapbec_ctx {
   int* h_err = nullptr;                // pinned copy
   int chunk_user = 0;                  // x-chunk requested by the caller (0 = automatic)
   int stage_form = TRAPBEC_RK3_THREE_STAGE;   // real-time RK3 form (trapbec_rk3_form)
-  double imag_escale = 0.0;            // stop test of RK3_RENORM: 0 relative, > 0 absolute (energy scale)
+  int imag_stop = TRAPBEC_STOP_REL;    // stop test of RK3_RENORM (trapbec_imag_stop)
+  double imag_escale = 0.0;            // its energy scale (absolute modes)
   void* lo = nullptr;                  // rounding remainder of psi (compensated form, allocated on request)
   bool lo_valid = false;               // lo belongs to the current psi (else it is cleared before use)
 };
@@ -501,6 +502,7 @@ template <typename T> int do_imag_rk3(trapbec_ctx* c, int nsteps, double tol, in
   c->host_ctrl->tol = tol;
   c->host_ctrl->dV = dV;
   c->host_ctrl->escale = c->imag_escale;
+  c->host_ctrl->stop_mode = c->imag_stop;
   c->host_ctrl->converged = 0;
   c->host_ctrl->step = 0;
   c->host_ctrl->nonfinite = 0;
@@ -1084,13 +1086,17 @@ int trapbec_step_imag(trapbec_ctx* c, int nsteps, int variant, double tol, int* 
 int trapbec_set_imag_stop(trapbec_ctx* c, int mode, double energy_scale) {
   if (!c) return TRAPBEC_ERR_ARG;
   if (mode == TRAPBEC_STOP_REL) {
+    c->imag_stop = mode;
     c->imag_escale = 0.0;
     return TRAPBEC_OK;
   }
-  if (mode != TRAPBEC_STOP_ABS || !(energy_scale > 0.0) || !std::isfinite(energy_scale)) {
-    set_error("trapbec_set_imag_stop: mode must be TRAPBEC_STOP_REL or TRAPBEC_STOP_ABS with a finite energy_scale > 0");
+  if ((mode != TRAPBEC_STOP_ABS && mode != TRAPBEC_STOP_ABS_PER_NORM) || !(energy_scale > 0.0) ||
+      !std::isfinite(energy_scale)) {
+    set_error("trapbec_set_imag_stop: mode must be TRAPBEC_STOP_REL, or TRAPBEC_STOP_ABS(_PER_NORM) with a finite "
+              "energy_scale > 0");
     return TRAPBEC_ERR_ARG;
   }
+  c->imag_stop = mode;
   c->imag_escale = energy_scale;
   return TRAPBEC_OK;
 }

@@ -492,11 +492,16 @@ def _guesses(draws, amps, nn_noise: float):
     return tf, nn
 
 
-def _relax(params, states, tol, max_steps, check_every, energy_only=False):
+def _relax(params, states, tol, max_steps, check_every, energy_only=False, escale=None):
+    """Batched RK3_RENORM relaxation of `states`; with `escale` (one per state)
+    the stop test is |dE| / N * escale < tol (trapbec_batch_set_imag_stop
+    ABS_PER_NORM), else |dE|/|E| <= tol."""
     from .batch import BatchSolver
     b = BatchSolver(params)
     for i, s in enumerate(states):
         b.set_psi(i, s)
+    if escale is not None and not energy_only:
+        b.set_imag_stop(abi.STOP_ABS_PER_NORM, escale)
     t0 = time.perf_counter()
     out = b.solve(max_steps=1 if energy_only else max_steps, tol=0.0 if energy_only else tol,
                   check_every=check_every)
@@ -511,7 +516,7 @@ def _relax(params, states, tol, max_steps, check_every, energy_only=False):
 
 
 def compare(net: Surrogate, draws, tol: float = 1e-10, max_steps: int = 60000, check_every: int = 200,
-            nn_noise: float = 1e-2, nn_omega_max: float = 0.5) -> dict:
+            nn_noise: float = 1e-2, nn_omega_max: float = 0.5, stop: str = "rel") -> dict:
     """Relax the held-out draws twice at the workload's step (dtau = 0.002):
     from the Thomas-Fermi + 1e-2 noise guess (the plain method) and with the
     surrogate.  The surrogate's initial state is its amplitude plus the same
@@ -523,9 +528,12 @@ def compare(net: Surrogate, draws, tol: float = 1e-10, max_steps: int = 60000, c
     vortices and end in a vortex state 10-20% lower in energy, from the
     surrogate's guess (close to the vortex-free stationary state) it stops
     there -- so the two guesses would not lead to the same state.  Reports steps and
-    device time to the relative energy-change tolerance, the final energies
-    and the L2 distance of the final states (global phase aligned)."""
+    device time to the energy-change tolerance -- relative, |dE|/|E| <= tol
+    (stop="rel"), or on the energy per particle in trap units, |d(E/N)| < tol
+    (stop="per_particle") -- the final energies and the L2 distance of the
+    final states (global phase aligned)."""
     t = net.t
+    escale = [prob.mu_to_trap(1.0) for prob, _ in draws] if stop == "per_particle" else None
     params = [prob.to_params() for prob, _ in draws]
     probs = [prob for prob, _ in draws]
     predict_problems(net, probs[:net.B])   # warm-up
@@ -553,8 +561,8 @@ def compare(net: Surrogate, draws, tol: float = 1e-10, max_steps: int = 60000, c
     sel_ms = e_tf["solve_ms_device"] + e_nn["solve_ms_device"]   # the selector's energy evaluations
     chosen = [n if u else f for n, f, u in zip(nn_states, tf_states, use_nn)]
     res, finals = {}, {}
-    res["tf"], finals["tf"] = _relax(params, tf_states, tol, max_steps, check_every)
-    res["nn"], finals["nn"] = _relax(params, chosen, tol, max_steps, check_every)
+    res["tf"], finals["tf"] = _relax(params, tf_states, tol, max_steps, check_every, escale=escale)
+    res["nn"], finals["nn"] = _relax(params, chosen, tol, max_steps, check_every, escale=escale)
     l2 = []
     for a, c in zip(finals["tf"], finals["nn"]):
         a = a.astype(np.complex128).ravel()
@@ -568,7 +576,7 @@ def compare(net: Surrogate, draws, tol: float = 1e-10, max_steps: int = 60000, c
     both = np.array([a and b for a, b in zip(res["tf"]["converged"], res["nn"]["converged"])])
     ratio = s_tf / np.maximum(s_nn, 1)
     return {
-        "instances": len(draws), "tol_rel_dE": tol, "dtau_trap_units": draws[0][0].dt, "nn_noise": nn_noise,
+        "instances": len(draws), "tol": tol, "stop": stop, "dtau_trap_units": draws[0][0].dt, "nn_noise": nn_noise,
         "nn_used": int(sum(use_nn)), "nn_unreasonable": int(sum(unreasonable)),
         "nn_omega_max": nn_omega_max, "tf_kept_fast_rotation": int(len(draws) - sum(slow_rot)),
         "guess_energy_tf": e_tf["energy"], "guess_energy_nn": e_nn["energy"],
