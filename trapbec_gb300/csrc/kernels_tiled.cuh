@@ -405,8 +405,12 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
       uend = ba.ustart[k + 1] < G1 ? ba.ustart[k + 1] : G1;
       if constexpr (BATCH) {
         // read the arguments from shared memory: they are reloaded after each
-        // barrier instead of holding ~40 registers for the whole segment (the
-        // previous segment ended with a barrier, so nobody reads the old copy)
+        // barrier instead of holding ~40 registers for the whole segment.  The
+        // barrier before the copy keeps it from overwriting the previous
+        // segment's copy while slower threads still read it: a segment of a
+        // converged grid is skipped right after its arguments are read, with
+        // no barrier of its own.
+        __syncthreads();
         const int* src = reinterpret_cast<const int*>(tap);
         int* dst = reinterpret_cast<int*>(&targs_s);
         for (int e = tid; e < (int)(sizeof(TiledArgs<T>) / 4); e += NT) dst[e] = src[e];
