@@ -38,10 +38,11 @@ int tbsg_conv3_fwd(const void* x, int cin, const void* w, const float* bias, con
                    float* yf, int yf_accumulate, int cout, int batch, int D, int H, int W, int act, float slope,
                    void* stream);
 
-/* Kernel family of tbsg_conv3_fwd: 0 (default) = tcgen05.mma with TMEM
- * accumulators for 16/32 -> 16/32 channels and mma.sync for the others;
- * 1 = mma.sync for all pairs.  tbsg_tc_status reports (and clears) whether a
- * tcgen05 launch gave up waiting for its MMAs (bounded, 2 s).              */
+/* Kernel family of tbsg_conv3_fwd and tbsg_conv3_wgrad: 0 (default) =
+ * tcgen05.mma with TMEM accumulators (forward: 16/32 -> 16/32 channels,
+ * mma.sync for the others; weight gradients: every pair); 1 = mma.sync for
+ * all.  tbsg_tc_status reports (and clears) whether a tcgen05 launch gave up
+ * waiting for its copies or MMAs (bounded, 2 s).                          */
 int tbsg_set_conv_path(int path);
 int tbsg_tc_status(int* timed_out);
 

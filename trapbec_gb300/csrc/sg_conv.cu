@@ -331,6 +331,9 @@ int wgrad_launch(const WgArgs& a, int nch, float* dw, float* db, cudaStream_t st
 int conv3_fwd_tc(const void* x, int cin, const void* w, const float* bias, const void* skip, void* y, float* yf,
                  int yf_accumulate, int cout, int batch, int D, int H, int W, int act, float slope, cudaStream_t st);
 int g_conv_path = 0;   // 0: tcgen05 where built, else mma.sync; 1: mma.sync only
+size_t wgrad_tc_scratch_bytes(int cin, int cout, int batch, int D, int H, int W);
+int wgrad_tc(const void* x, int cin, const void* dz, int cout, int batch, int D, int H, int W, float* dw, float* db,
+             void* scratch, cudaStream_t st);
 
 }  // namespace sg
 
@@ -368,20 +371,26 @@ int tbsg_conv3_fwd(const void* x, int cin, const void* w, const float* bias, con
 
 size_t tbsg_conv3_wgrad_scratch_bytes(int cin, int cout, int batch, int D, int H, int W) {
   const int nch = nchunks(batch, D, H, W);
-  return ((size_t)nch * 27 * cout * cin + (size_t)nch * cout) * sizeof(float);
+  const size_t ms = ((size_t)nch * 27 * cout * cin + (size_t)nch * cout) * sizeof(float);
+  const size_t tc = wgrad_tc_scratch_bytes(cin, cout, batch, D, H, W);
+  return ms > tc ? ms : tc;
 }
 
 int tbsg_conv3_wgrad(const void* x, int cin, const void* dz, int cout, int batch, int D, int H, int W,
                      float* dw, float* db, void* scratch, size_t scratch_bytes, void* stream) {
   if (!x || !dz || !dw || !scratch || batch <= 0 || D <= 0 || H <= 0 || W <= 0) return TBSG_ERR_ARG;
   if (scratch_bytes < tbsg_conv3_wgrad_scratch_bytes(cin, cout, batch, D, H, W)) return TBSG_ERR_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (g_conv_path == 0) {
+    const int rc = wgrad_tc(x, cin, dz, cout, batch, D, H, W, dw, db, scratch, st);
+    if (rc != TBSG_ERR_SHAPE) return rc;
+  }
   const int nch = nchunks(batch, D, H, W);
   WgArgs a;
   a.x = (const bf16*)x; a.dz = (const bf16*)dz;
   a.part = (float*)scratch;
   a.part_b = (float*)scratch + (size_t)nch * 27 * cout * cin;
   a.B = batch; a.D = D; a.H = H; a.W = W;
-  cudaStream_t st = (cudaStream_t)stream;
 #define SG_WG(I, O) \
   if (cin == I && cout == O) return wgrad_launch<I, O>(a, nch, dw, db, st);
   SG_PAIRS(SG_WG)

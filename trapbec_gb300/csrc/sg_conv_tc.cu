@@ -21,13 +21,13 @@
 // TMEM (a warp reads the 32 lanes of its quarter = 32 brick voxels), release
 // it, and run the fused bias + skip + leaky-ReLU epilogue.  All hand-offs are
 // mbarrier phases; every wait is bounded in time; TMEM is always released.
-#include <cudaTypedefs.h>
-
 #include "../../include/trapbec_surrogate.h"
-#include "sg_common.cuh"
+#include "sg_tc_common.cuh"
 
 namespace sg {
 namespace tc {
+
+using namespace tcc;
 
 constexpr int BH = 16, BW = 8;                  // output brick rows (h) x columns (w); M = 128
 constexpr int XD = 3, XH = BH + 2, XW = BW + 2;
@@ -36,8 +36,6 @@ constexpr int CHUNK = 8704;                     // one 8-channel chunk (540 x 16
 constexpr int NTHR = 192;                       // 6 warps: TMA, MMA, 4 x epilogue
 constexpr uint32_t ACC_COLS = 32;               // one accumulator: 128 lanes x Cout <= 32 columns
 constexpr uint32_t TMEM_COLS = 2 * ACC_COLS;    // two accumulators
-constexpr uint64_t WAIT_NS = 2000000000ull;     // 2 s
-
 __device__ int g_timeout = 0;                   // set when a wait gave up
 
 template <int CIN, int COUT> struct Cfg {
@@ -49,67 +47,6 @@ template <int CIN, int COUT> struct Cfg {
   static constexpr int BAR_OFF = (W_OFF + W_BYTES + 127) / 128 * 128;
   static constexpr int SMEM = BAR_OFF + 128;
 };
-
-__device__ __forceinline__ uint64_t now_ns() {
-  uint64_t t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-__device__ __forceinline__ bool bar_try(uint32_t bar, uint32_t par) {
-  uint32_t ok;
-  asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-               : "=r"(ok)
-               : "r"(bar), "r"(par)
-               : "memory");
-  return ok != 0;
-}
-// bounded wait for the phase of parity `par`
-__device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t par) {
-  if (bar_try(bar, par)) return true;
-  const uint64_t t0 = now_ns();
-  while (!bar_try(bar, par))
-    if (now_ns() - t0 > WAIT_NS) return false;
-  return true;
-}
-__device__ __forceinline__ void bar_init(uint32_t bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
-}
-__device__ __forceinline__ void bar_arrive(uint32_t bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
-}
-__device__ __forceinline__ void bar_expect_tx(uint32_t bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ void tma_load_5d(uint32_t dst, const CUtensorMap* tm, int c0, int c1, int c2, int c3, int c4,
-                                            uint32_t bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, %6}], "
-      "[%7];" ::"r"(dst),
-      "l"(tm), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(bar)
-      : "memory");
-}
-
-// shared-memory operand descriptor: K-major, no swizzle
-__device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
-  uint64_t d = 0;
-  d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
-  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;   // between K core matrices
-  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;   // between 8-row groups (M or N)
-  d |= (uint64_t)1 << 46;                        // descriptor version
-  return d;
-}
-// instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both K-major
-__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
-  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
-}
-
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t r[16]) {
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-}
 
 struct Args {
   const bf16* x;       // [B][D][H][W][CIN]
@@ -299,18 +236,6 @@ __global__ void __launch_bounds__(NTHR, 1) conv3_tc_kernel(const __grid_constant
   if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(TMEM_COLS));
 }
 
-inline PFN_cuTensorMapEncodeTiled_v12000 encoder() {
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  if (!fn) {
-    void* f = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = (PFN_cuTensorMapEncodeTiled_v12000)f;
-  }
-  return fn;
-}
-
 template <int CIN, int COUT>
 int launch(const Args& a, cudaStream_t st) {
   using C = Cfg<CIN, COUT>;
@@ -369,14 +294,21 @@ int conv3_fwd_tc(const void* x, int cin, const void* w, const float* bias, const
 
 }  // namespace sg
 
+namespace sg {
+int wgrad_tc_timed_out(int* v);
+}
+
 extern "C" int tbsg_tc_status(int* timed_out) {
   if (!timed_out) return TBSG_ERR_ARG;
   int v = 0;
   if (cudaMemcpyFromSymbol(&v, sg::tc::g_timeout, sizeof(int)) != cudaSuccess) return TBSG_ERR_CUDA;
-  *timed_out = v;
   if (v) {
     int z = 0;
     if (cudaMemcpyToSymbol(sg::tc::g_timeout, &z, sizeof(int)) != cudaSuccess) return TBSG_ERR_CUDA;
   }
+  int vw = 0;
+  const int rc = sg::wgrad_tc_timed_out(&vw);
+  if (rc != TBSG_OK) return rc;
+  *timed_out = v | vw;
   return TBSG_OK;
 }

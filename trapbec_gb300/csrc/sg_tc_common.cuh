@@ -1,0 +1,120 @@
+// sg_tc_common.cuh -- tcgen05 / TMA / mbarrier building blocks shared by the
+// surrogate's tensor-core kernels (sg_conv_tc.cu: forward and input-gradient
+// convolutions; sg_wgrad_tc.cu: weight gradients).
+//
+// Every mbarrier wait is bounded in time (%globaltimer); a wait that gives up
+// returns false and the kernel records a timeout flag instead of hanging.
+#pragma once
+#include <cudaTypedefs.h>
+
+#include "sg_common.cuh"
+
+namespace sg {
+namespace tcc {
+
+constexpr uint64_t WAIT_NS = 2000000000ull;   // 2 s
+
+__device__ __forceinline__ uint64_t now_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ bool bar_try(uint32_t bar, uint32_t par) {
+  uint32_t ok;
+  asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+               : "=r"(ok)
+               : "r"(bar), "r"(par)
+               : "memory");
+  return ok != 0;
+}
+// bounded wait for the phase of parity `par`
+__device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t par) {
+  if (bar_try(bar, par)) return true;
+  const uint64_t t0 = now_ns();
+  while (!bar_try(bar, par))
+    if (now_ns() - t0 > WAIT_NS) return false;
+  return true;
+}
+__device__ __forceinline__ void bar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
+}
+__device__ __forceinline__ void bar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void bar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void tma_load_5d(uint32_t dst, const CUtensorMap* tm, int c0, int c1, int c2, int c3, int c4,
+                                            uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, %6}], "
+      "[%7];" ::"r"(dst),
+      "l"(tm), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(bar)
+      : "memory");
+}
+
+// Shared-memory operand descriptor, no swizzle.  A core matrix is 8 rows of
+// 16 bytes, 128 contiguous bytes.  In both forms `lbo` is the byte stride
+// between core matrices adjacent in K and `sbo` the stride between core
+// matrices adjacent in M (or N).  K-major operands: a core-matrix row holds
+// 8 consecutive K elements, its 8 rows are 8 consecutive M (N) indices.
+// MN-major operands: a row holds 8 consecutive M (N) elements, its 8 rows
+// are 8 consecutive K indices.  (Checked on GB300 with single MMAs of small-integer
+// operands against a host product, for M = 64 and 128, N = 16..80,
+// both forms of A and B.)
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;   // descriptor version
+  return d;
+}
+// Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B;
+// a_mn / b_mn select the MN-major form of A / B (0: K-major).
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N, int a_mn = 0, int b_mn = 0) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)a_mn << 15) | ((uint32_t)b_mn << 16) |
+         ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// D (TMEM) [+]= A (shared) x B (shared)^T; acc = 0 overwrites D
+__device__ __forceinline__ void mma_bf16_ss(uint32_t tacc, uint64_t ad, uint64_t bd, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tacc),
+      "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+}
+// arrive on `bar` once the MMAs issued so far by this thread are complete
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t r[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t r[8]) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point
+inline PFN_cuTensorMapEncodeTiled_v12000 encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (PFN_cuTensorMapEncodeTiled_v12000)f;
+  }
+  return fn;
+}
+
+}  // namespace tcc
+}  // namespace sg
