@@ -22,7 +22,7 @@ ROOT = os.path.dirname(HERE)
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_SOURCES = ["trapbec.cu", "tiled_dispatch.cu", "tiled_f32_s0.cu", "tiled_f32_s1.cu", "tiled_f32_s2.cu",
                 "tiled_f32_s3.cu", "tiled_f32_s4.cu", "tiled_f64_s0.cu", "tiled_f64_s1.cu", "batch.cu", "noalloc.cu", "peaks.cu",
-                "sg_conv.cu", "sg_conv_tc.cu", "sg_wgrad_tc.cu", "sg_ops.cu"]
+                "sg_conv.cu", "sg_conv_tc.cu", "sg_conv_tcs.cu", "sg_wgrad_tc.cu", "sg_ops.cu"]
 CXX_SOURCES = ["params_io.cpp"]
 HEADERS_GLOB = (".cuh", ".h")
 

@@ -330,6 +330,8 @@ int wgrad_launch(const WgArgs& a, int nch, float* dw, float* db, cudaStream_t st
 
 int conv3_fwd_tc(const void* x, int cin, const void* w, const float* bias, const void* skip, void* y, float* yf,
                  int yf_accumulate, int cout, int batch, int D, int H, int W, int act, float slope, cudaStream_t st);
+int conv3_fwd_tcs(const void* x, int cin, const void* w, const float* bias, const void* skip, void* y, float* yf,
+                  int yf_accumulate, int cout, int batch, int D, int H, int W, int act, float slope, cudaStream_t st);
 int g_conv_path = 0;   // 0: tcgen05 where built, else mma.sync; 1: mma.sync only
 size_t wgrad_tc_scratch_bytes(int cin, int cout, int batch, int D, int H, int W);
 int wgrad_tc(const void* x, int cin, const void* dz, int cout, int batch, int D, int H, int W, float* dw, float* db,
@@ -359,7 +361,9 @@ int tbsg_conv3_fwd(const void* x, int cin, const void* w, const float* bias, con
   a.mode = yf ? (yf_accumulate ? 1 : 2) : 0;
   cudaStream_t st = (cudaStream_t)stream;
   if (g_conv_path == 0) {
-    const int rc = conv3_fwd_tc(x, cin, w, bias, skip, y, yf, yf_accumulate, cout, batch, D, H, W, act, slope, st);
+    int rc = conv3_fwd_tc(x, cin, w, bias, skip, y, yf, yf_accumulate, cout, batch, D, H, W, act, slope, st);
+    if (rc != TBSG_ERR_SHAPE) return rc;
+    rc = conv3_fwd_tcs(x, cin, w, bias, skip, y, yf, yf_accumulate, cout, batch, D, H, W, act, slope, st);
     if (rc != TBSG_ERR_SHAPE) return rc;
   }
 #define SG_FWD(I, O) \

@@ -296,6 +296,7 @@ int conv3_fwd_tc(const void* x, int cin, const void* w, const float* bias, const
 
 namespace sg {
 int wgrad_tc_timed_out(int* v);
+int conv_tcs_timed_out(int* v);
 }
 
 extern "C" int tbsg_tc_status(int* timed_out) {
@@ -306,9 +307,11 @@ extern "C" int tbsg_tc_status(int* timed_out) {
     int z = 0;
     if (cudaMemcpyToSymbol(sg::tc::g_timeout, &z, sizeof(int)) != cudaSuccess) return TBSG_ERR_CUDA;
   }
-  int vw = 0;
-  const int rc = sg::wgrad_tc_timed_out(&vw);
+  int vw = 0, vs = 0;
+  int rc = sg::wgrad_tc_timed_out(&vw);
   if (rc != TBSG_OK) return rc;
-  *timed_out = v | vw;
+  rc = sg::conv_tcs_timed_out(&vs);
+  if (rc != TBSG_OK) return rc;
+  *timed_out = v | vw | vs;
   return TBSG_OK;
 }

@@ -35,6 +35,30 @@ __global__ void act_bwd_kernel(const float* dy, const bf16* y, bf16* dz, float* 
   }
 }
 
+// the same, 8 elements per thread (n % 8 == 0, 16-byte aligned arrays)
+__global__ void act_bwd8_kernel(const float4* dy, const uint4* y, uint4* dz, float4* dskip, size_t n8, float slope) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n8; i += (size_t)gridDim.x * blockDim.x) {
+    const float4 a = dy[2 * i], b = dy[2 * i + 1];
+    const uint4 yu = y[i];
+    const bf16* ye = (const bf16*)&yu;
+    float g[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+#pragma unroll
+    for (int k = 0; k < 8; ++k) g[k] *= __bfloat162float(ye[k]) > 0.f ? 1.f : slope;
+    uint4 o;
+    bf16* oe = (bf16*)&o;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) oe[k] = __float2bfloat16_rn(g[k]);
+    dz[i] = o;
+    if (dskip) {
+      float4 s0 = dskip[2 * i], s1 = dskip[2 * i + 1];
+      s0.x += g[0]; s0.y += g[1]; s0.z += g[2]; s0.w += g[3];
+      s1.x += g[4]; s1.y += g[5]; s1.z += g[6]; s1.w += g[7];
+      dskip[2 * i] = s0;
+      dskip[2 * i + 1] = s1;
+    }
+  }
+}
+
 // fine grid (D, H, W) -> coarse (D/2, H/2, W/2); one thread per coarse voxel x 8 channels
 __global__ void pool2_fwd_kernel(const bf16* x, bf16* y, int c, int B, int D, int H, int W) {
   const int Dc = D / 2, Hc = H / 2, Wc = W / 2, c8 = c / 8;
@@ -57,6 +81,30 @@ __global__ void pool2_fwd_kernel(const bf16* x, bf16* y, int c, int B, int D, in
     bf16* e = (bf16*)&o4;
     for (int k = 0; k < 8; ++k) e[k] = __float2bfloat16_rn(s[k] * 0.125f);
     *(uint4*)(y + (((b * Dc + d) * Hc + h) * Wc + w) * c + cc * 8) = o4;
+  }
+}
+
+// one thread per coarse voxel x 4 channels: dx of its 8 fine voxels += dy / 8
+__global__ void pool2_bwd4_kernel(const float* dy, float* dx, int c, int B, int D, int H, int W) {
+  const int Dc = D / 2, Hc = H / 2, Wc = W / 2, c4 = c / 4;
+  const size_t n = (size_t)B * Dc * Hc * Wc * c4;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int cc = (int)(i % c4);
+    size_t r = i / c4;
+    const int w = (int)(r % Wc); r /= Wc;
+    const int h = (int)(r % Hc); r /= Hc;
+    const int d = (int)(r % Dc);
+    const size_t b = r / Dc;
+    float4 g = *(const float4*)(dy + i * 4);
+    g.x *= 0.125f; g.y *= 0.125f; g.z *= 0.125f; g.w *= 0.125f;
+#pragma unroll
+    for (int o = 0; o < 8; ++o) {
+      const int fd = 2 * d + (o >> 2), fh = 2 * h + ((o >> 1) & 1), fw = 2 * w + (o & 1);
+      float4* q = (float4*)(dx + (((b * D + fd) * H + fh) * W + fw) * c + cc * 4);
+      float4 t = *q;
+      t.x += g.x; t.y += g.y; t.z += g.z; t.w += g.w;
+      *q = t;
+    }
   }
 }
 
@@ -86,6 +134,28 @@ __global__ void up2_fwd_kernel(const bf16* x, bf16* y, int c, int B, int D, int 
     const int d = (int)(r % Df);
     const size_t b = r / Df;
     *(uint4*)(y + i * 8) = *(const uint4*)(x + (((b * D + d / 2) * H + h / 2) * W + w / 2) * c + cc * 8);
+  }
+}
+
+// one thread per coarse voxel x 4 channels: the sum of its 8 fine gradients
+__global__ void up2_bwd4_kernel(const float* dy, float* dx, int c, int B, int D, int H, int W) {
+  const int Hf = 2 * H, Wf = 2 * W, Df = 2 * D, c4 = c / 4;
+  const size_t n = (size_t)B * D * H * W * c4;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int cc = (int)(i % c4);
+    size_t r = i / c4;
+    const int w = (int)(r % W); r /= W;
+    const int h = (int)(r % H); r /= H;
+    const int d = (int)(r % D);
+    const size_t b = r / D;
+    float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int o = 0; o < 8; ++o) {
+      const int fd = 2 * d + (o >> 2), fh = 2 * h + ((o >> 1) & 1), fw = 2 * w + (o & 1);
+      const float4 t = *(const float4*)(dy + (((b * Df + fd) * Hf + fh) * Wf + fw) * c + cc * 4);
+      s.x += t.x; s.y += t.y; s.z += t.z; s.w += t.w;
+    }
+    *(float4*)(dx + i * 4) = s;
   }
 }
 
@@ -149,6 +219,70 @@ __global__ void head_loss_kernel(const bf16* feat, int c, const float* wh, const
   }
   if (threadIdx.x == 0)
     for (int k = 0; k < np; ++k) partials[(size_t)blockIdx.x * np + k] = red[k];
+}
+
+// 16 feature channels: one voxel per thread, the channels as two 16-byte loads
+__global__ void head_fwd16_kernel(const uint4* feat, const float* wh, const float* bh, const float* base, float* amp,
+                                  size_t nvox) {
+  float w[16];
+#pragma unroll
+  for (int k = 0; k < 16; ++k) w[k] = wh[k];
+  const float b0 = bh[0];
+  for (size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v < nvox; v += (size_t)gridDim.x * blockDim.x) {
+    const uint4 u0 = feat[2 * v], u1 = feat[2 * v + 1];
+    const bf16* e0 = (const bf16*)&u0;
+    const bf16* e1 = (const bf16*)&u1;
+    float s = b0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s += __bfloat162float(e0[k]) * w[k];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s += __bfloat162float(e1[k]) * w[8 + k];
+    amp[v] = base[v] + s;
+  }
+}
+
+__global__ void __launch_bounds__(HEAD_THREADS) head_loss16_kernel(const uint4* feat, const float* wh, const float* bh,
+                                                                   const float* base, const float* target, size_t nvox,
+                                                                   float4* dfeat, float* partials) {
+  constexpr int NP = 18;
+  __shared__ float red[HEAD_THREADS * NP];
+  float w[16], acc[NP];
+#pragma unroll
+  for (int k = 0; k < 16; ++k) w[k] = wh[k];
+#pragma unroll
+  for (int k = 0; k < NP; ++k) acc[k] = 0.f;
+  const float b0 = bh[0];
+  const float inv = 1.f / (float)nvox;
+  for (size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v < nvox; v += (size_t)gridDim.x * blockDim.x) {
+    const uint4 u0 = feat[2 * v], u1 = feat[2 * v + 1];
+    const bf16* e0 = (const bf16*)&u0;
+    const bf16* e1 = (const bf16*)&u1;
+    float f[16];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) { f[k] = __bfloat162float(e0[k]); f[8 + k] = __bfloat162float(e1[k]); }
+    float s = b0;
+#pragma unroll
+    for (int k = 0; k < 16; ++k) s += f[k] * w[k];
+    const float diff = base[v] + s - target[v];
+    const float g = 2.f * diff * inv;
+    acc[0] += diff * diff * inv;
+#pragma unroll
+    for (int k = 0; k < 16; ++k) acc[1 + k] += g * f[k];
+    acc[17] += g;
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      dfeat[4 * v + q] = make_float4(g * w[4 * q], g * w[4 * q + 1], g * w[4 * q + 2], g * w[4 * q + 3]);
+  }
+#pragma unroll
+  for (int k = 0; k < NP; ++k) red[k * HEAD_THREADS + threadIdx.x] = acc[k];
+  __syncthreads();
+  for (int h = HEAD_THREADS / 2; h > 0; h >>= 1) {
+    if ((int)threadIdx.x < h)
+#pragma unroll
+      for (int k = 0; k < NP; ++k) red[k * HEAD_THREADS + threadIdx.x] += red[k * HEAD_THREADS + threadIdx.x + h];
+    __syncthreads();
+  }
+  if ((int)threadIdx.x < NP) partials[(size_t)blockIdx.x * NP + threadIdx.x] = red[threadIdx.x * HEAD_THREADS];
 }
 
 __global__ void head_final_kernel(const float* partials, int nblk, int np, float* out) {
@@ -255,7 +389,12 @@ int tbsg_weight_prep(const float* w32, void* w, void* wt, int cin, int cout, voi
 
 int tbsg_act_bwd(const float* dy, const void* y, void* dz, float* dskip, size_t n, float slope, void* stream) {
   if (!dy || !y || !dz) return TBSG_ERR_ARG;
-  act_bwd_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(dy, (const bf16*)y, (bf16*)dz, dskip, n, slope);
+  const bool vec = n % 8 == 0 && ((uintptr_t)dy | (uintptr_t)y | (uintptr_t)dz | (uintptr_t)dskip) % 16 == 0;
+  if (vec)
+    act_bwd8_kernel<<<grid_for(n / 8), 256, 0, (cudaStream_t)stream>>>(
+        (const float4*)dy, (const uint4*)y, (uint4*)dz, (float4*)dskip, n / 8, slope);
+  else
+    act_bwd_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(dy, (const bf16*)y, (bf16*)dz, dskip, n, slope);
   return done();
 }
 
@@ -268,8 +407,12 @@ int tbsg_pool2_fwd(const void* x, void* y, int c, int batch, int D, int H, int W
 
 int tbsg_pool2_bwd(const float* dy, float* dx, int c, int batch, int D, int H, int W, void* stream) {
   if (!dy || !dx || (D | H | W) & 1) return TBSG_ERR_ARG;
-  pool2_bwd_kernel<<<grid_for((size_t)batch * D * H * W * c), 256, 0, (cudaStream_t)stream>>>(dy, dx, c, batch, D,
-                                                                                              H, W);
+  if (c % 4 == 0 && ((uintptr_t)dy | (uintptr_t)dx) % 16 == 0)
+    pool2_bwd4_kernel<<<grid_for((size_t)batch * D * H * W * c / 32), 256, 0, (cudaStream_t)stream>>>(dy, dx, c, batch,
+                                                                                                    D, H, W);
+  else
+    pool2_bwd_kernel<<<grid_for((size_t)batch * D * H * W * c), 256, 0, (cudaStream_t)stream>>>(dy, dx, c, batch, D,
+                                                                                                H, W);
   return done();
 }
 
@@ -282,15 +425,22 @@ int tbsg_up2_fwd(const void* x, void* y, int c, int batch, int D, int H, int W, 
 
 int tbsg_up2_bwd(const float* dy, float* dx, int c, int batch, int D, int H, int W, void* stream) {
   if (!dy || !dx) return TBSG_ERR_ARG;
-  up2_bwd_kernel<<<grid_for((size_t)batch * D * H * W * c), 256, 0, (cudaStream_t)stream>>>(dy, dx, c, batch, D, H,
-                                                                                            W);
+  if (c % 4 == 0 && ((uintptr_t)dy | (uintptr_t)dx) % 16 == 0)
+    up2_bwd4_kernel<<<grid_for((size_t)batch * D * H * W * c / 4), 256, 0, (cudaStream_t)stream>>>(dy, dx, c, batch, D,
+                                                                                                  H, W);
+  else
+    up2_bwd_kernel<<<grid_for((size_t)batch * D * H * W * c), 256, 0, (cudaStream_t)stream>>>(dy, dx, c, batch, D, H,
+                                                                                              W);
   return done();
 }
 
 int tbsg_head_fwd(const void* feat, int c, const float* wh, const float* bh, const float* base, float* amp,
                   size_t nvox, void* stream) {
   if (!feat || !wh || !bh || !base || !amp || c <= 0) return TBSG_ERR_ARG;
-  head_fwd_kernel<<<grid_for(nvox), 256, 0, (cudaStream_t)stream>>>((const bf16*)feat, c, wh, bh, base, amp, nvox);
+  if (c == 16 && (uintptr_t)feat % 16 == 0)
+    head_fwd16_kernel<<<grid_for(nvox), 256, 0, (cudaStream_t)stream>>>((const uint4*)feat, wh, bh, base, amp, nvox);
+  else
+    head_fwd_kernel<<<grid_for(nvox), 256, 0, (cudaStream_t)stream>>>((const bf16*)feat, c, wh, bh, base, amp, nvox);
   return done();
 }
 
@@ -310,8 +460,12 @@ int tbsg_head_loss(const void* feat, int c, const float* wh, const float* bh, co
       return TBSG_ERR_CUDA;
   }
   cudaStream_t st = (cudaStream_t)stream;
-  head_loss_kernel<<<HEAD_BLOCKS, HEAD_THREADS, smem, st>>>((const bf16*)feat, c, wh, bh, base, target, nvox, dfeat,
-                                                            partials);
+  if (c == 16 && ((uintptr_t)feat | (uintptr_t)dfeat) % 16 == 0)
+    head_loss16_kernel<<<HEAD_BLOCKS, HEAD_THREADS, 0, st>>>((const uint4*)feat, wh, bh, base, target, nvox,
+                                                             (float4*)dfeat, partials);
+  else
+    head_loss_kernel<<<HEAD_BLOCKS, HEAD_THREADS, smem, st>>>((const bf16*)feat, c, wh, bh, base, target, nvox, dfeat,
+                                                              partials);
   head_final_kernel<<<1, 256, 0, st>>>(partials, HEAD_BLOCKS, c + 2, out);
   return done();
 }
