@@ -262,21 +262,22 @@ def imag_leg(args):
 
 
 def warmstart_leg(args):
-    """Imaginary-time relaxation to |dE|/|E| <= tol at 128^3 from the
-    surrogate's guess against the Thomas-Fermi + 1e-2 noise guess, on draws
-    held out from the surrogate's training set (the committed weights were
-    trained on draws 0..383 of seed 2024; this leg uses draws from 400 on).
+    """Imaginary-time relaxation to |d(E/N)| < tol at 128^3 from the
+    surrogate's guess against the Thomas-Fermi + 1e-2 noise guess, on the
+    first draws held out from the surrogate's training set (the committed
+    weights were trained on draws 0..TRAIN_DRAWS-1 of seed TRAIN_SEED).
     Both relaxations run batched; device time from events around each solve."""
     from trapbec_gb300 import abi, units, surrogate
-    n0 = 400
-    draws = units.ground_state_draws(n0 + args.ws_count, 2024, grids=(128,), precision=abi.FP32)[n0:]
+    n0 = surrogate.TRAIN_DRAWS
+    draws = units.ground_state_draws(n0 + args.ws_count, surrogate.TRAIN_SEED, grids=(128,),
+                                     precision=abi.FP32)[n0:]
     net = surrogate.Surrogate(128, 2, seed=0)
     net.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "trapbec_gb300", "weights",
                           "surrogate_128.npz"))
     r = surrogate.compare(net, draws, tol=args.imag_tol, max_steps=args.ws_max_steps, stop="per_particle")
     med = lambda v: float(statistics.median(v))
     return {
-        "grid": 128, "instances": len(draws), "held_out": f"draws {n0}..{n0 + len(draws) - 1} of seed 2024",
+        "grid": 128, "instances": len(draws), "held_out": f"draws {n0}..{n0 + len(draws) - 1} of seed {surrogate.TRAIN_SEED}",
         "stop": "|d(E/N)| < tol, energy per particle in trap units (FP64)", "tol": args.imag_tol,
         "dtau_trap_units": 0.002, "max_steps": args.ws_max_steps,
         "surrogate_params": net.np, "nn_used": r["nn_used"],

@@ -38,6 +38,12 @@ LAYERS = [("e0a", 16, 16), ("e0b", 16, 16), ("e1a", 16, 32), ("e1b", 32, 32), ("
           ("d2b", 64, 64), ("d1a", 64, 32), ("d1b", 32, 32), ("d0a", 32, 16), ("d0b", 16, 16)]
 NFEAT = 16
 SLOPE = 0.05
+# The committed weights (weights/surrogate_128.npz, record in
+# weights/surrogate_128_train.json) were trained on draws 0..TRAIN_DRAWS-1 of
+# units.ground_state_draws(seed=TRAIN_SEED, grids=(128,)); draws from
+# TRAIN_DRAWS on are held out.
+TRAIN_SEED = 2024
+TRAIN_DRAWS = 2000
 
 
 def _torch():
@@ -329,6 +335,37 @@ def _tf_noise(b, i, ini, noise=True):
                  noise_amp=ini["noise_amp"] if noise else 0.0)
 
 
+def phase_spread(psi: np.ndarray, frac: float = 0.1) -> float:
+    """Largest deviation (rad) of the phase of psi from its global phase over
+    the cells where |psi| >= frac * max|psi|: about zero for a real state up
+    to a global phase (the vortex-free ground state), of order pi where
+    vortices wind the phase."""
+    p = psi.astype(np.complex128)
+    a = np.abs(p)
+    m = a >= frac * a.max()
+    g = np.sum(p[m] * a[m])
+    g = g / abs(g) if abs(g) > 0 else 1.0
+    return float(np.max(np.abs(np.angle(p[m] * np.conj(g)))))
+
+
+def axial_winding(psi: np.ndarray, radius_frac: float = 0.2) -> int:
+    """Phase winding number of psi around the trap axis (z through the grid
+    centre) on a circle of radius radius_frac * nx cells in the middle z
+    plane: the net number of vortex lines the circle encloses (0 for a
+    vortex-free state), from bilinear samples of psi."""
+    nx, ny, nz = psi.shape
+    pl = psi[:, :, nz // 2].astype(np.complex128)
+    cx, cy, r = (nx - 1) / 2.0, (ny - 1) / 2.0, radius_frac * nx
+    t = np.linspace(0.0, 2 * np.pi, 8 * nx, endpoint=False)
+    x, y = cx + r * np.cos(t), cy + r * np.sin(t)
+    i0, j0 = np.floor(x).astype(int), np.floor(y).astype(int)
+    fx, fy = x - i0, y - j0
+    v = (pl[i0, j0] * (1 - fx) * (1 - fy) + pl[i0 + 1, j0] * fx * (1 - fy) + pl[i0, j0 + 1] * (1 - fx) * fy +
+         pl[i0 + 1, j0 + 1] * fx * fy)
+    d = np.angle(np.roll(v, -1) * np.conj(v))
+    return int(round(float(np.sum(d)) / (2 * np.pi)))
+
+
 def ground_states(draws, max_steps: int, tol: float, frac: float = 0.6, chunk: int = 32, omega_zero: bool = True):
     """Relax each draw from its Thomas-Fermi + noise guess with the batched
     RK3 solver at `frac` of its own stability limit (the fixed point does not
@@ -355,9 +392,11 @@ def ground_states(draws, max_steps: int, tol: float, frac: float = 0.6, chunk: i
             _tf_noise(b, i, ini)
         out = b.solve(max_steps=max_steps, tol=tol, check_every=200)
         for i in range(len(part)):
-            amps.append(np.abs(b.get_psi(i)).astype(np.float32))
+            psi = b.get_psi(i)
+            amps.append(np.abs(psi).astype(np.float32))
             st = b.status(i)
-            info.append({"steps": out["steps"][i], "rel": st["rel"], "converged": st["converged"] > 0})
+            info.append({"steps": out["steps"][i], "rel": st["rel"], "converged": st["converged"] > 0,
+                         "phase_spread": phase_spread(psi)})
         b.close()
     return amps, info
 
@@ -492,7 +531,7 @@ def _guesses(draws, amps, nn_noise: float):
     return tf, nn
 
 
-def _relax(params, states, tol, max_steps, check_every, energy_only=False, escale=None):
+def _relax(params, states, tol, max_steps, check_every, energy_only=False, escale=None, keep_finals=True):
     """Batched RK3_RENORM relaxation of `states`; with `escale` (one per state)
     the stop test is |dE| / N * escale < tol (trapbec_batch_set_imag_stop
     ABS_PER_NORM), else |dE|/|E| <= tol."""
@@ -510,13 +549,13 @@ def _relax(params, states, tol, max_steps, check_every, energy_only=False, escal
     res = {"steps": out["steps"], "energy": out["energy"],
            "converged": [b.status(i)["converged"] > 0 for i in range(len(states))],
            "solve_ms_device": st["solve_ms"], "wall_s": wall}
-    finals = None if energy_only else [b.get_psi(i) for i in range(len(states))]
+    finals = None if energy_only or not keep_finals else [b.get_psi(i) for i in range(len(states))]
     b.close()
     return res, finals
 
 
 def compare(net: Surrogate, draws, tol: float = 1e-10, max_steps: int = 60000, check_every: int = 200,
-            nn_noise: float = 1e-2, nn_omega_max: float = 0.5, stop: str = "rel") -> dict:
+            nn_noise: float = 1e-2, nn_omega_max: float = 0.5, stop: str = "rel", subset_rerun: bool = False) -> dict:
     """Relax the held-out draws twice at the workload's step (dtau = 0.002):
     from the Thomas-Fermi + 1e-2 noise guess (the plain method) and with the
     surrogate.  The surrogate's initial state is its amplitude plus the same
@@ -531,7 +570,13 @@ def compare(net: Surrogate, draws, tol: float = 1e-10, max_steps: int = 60000, c
     device time to the energy-change tolerance -- relative, |dE|/|E| <= tol
     (stop="rel"), or on the energy per particle in trap units, |d(E/N)| < tol
     (stop="per_particle") -- the final energies and the L2 distance of the
-    final states (global phase aligned)."""
+    final states (global phase aligned), and the phase winding of each final
+    state around the trap axis (nonzero where the relaxation ended with
+    vortices).  With `subset_rerun`, the draws whose plain relaxation reaches
+    the tolerance are relaxed again in both arms as batches of their own, so
+    that the batch wall-time ratio of that set is not set by the draws that
+    never converge (which keep the Thomas-Fermi guess and run max_steps in
+    both arms)."""
     t = net.t
     escale = [prob.mu_to_trap(1.0) for prob, _ in draws] if stop == "per_particle" else None
     params = [prob.to_params() for prob, _ in draws]
@@ -570,6 +615,23 @@ def compare(net: Surrogate, draws, tol: float = 1e-10, max_steps: int = 60000, c
         ph = np.vdot(c, a)
         ph = ph / abs(ph) if abs(ph) > 0 else 1.0
         l2.append(float(np.linalg.norm(a - c * ph) / np.linalg.norm(a)))
+    wind_tf = [axial_winding(f) for f in finals["tf"]]
+    wind_nn = [axial_winding(f) for f in finals["nn"]]
+    subset = None
+    sub = [i for i, c in enumerate(res["tf"]["converged"]) if c]
+    if subset_rerun and sub and len(sub) < len(draws):
+        pick = lambda v: [v[i] for i in sub] if v is not None else None
+        r_tf, _ = _relax(pick(params), pick(tf_states), tol, max_steps, check_every, escale=pick(escale),
+                         keep_finals=False)
+        r_nn, _ = _relax(pick(params), pick(chosen), tol, max_steps, check_every, escale=pick(escale),
+                         keep_finals=False)
+        share = len(sub) / len(draws)   # this set's share of the inference and the selector
+        subset = {"instances": len(sub), "nn_used": int(sum(use_nn[i] for i in sub)),
+                  "converged_tf": int(sum(r_tf["converged"])), "converged_nn": int(sum(r_nn["converged"])),
+                  "device_ms_tf": r_tf["solve_ms_device"], "device_ms_nn": r_nn["solve_ms_device"],
+                  "steps_tf": r_tf["steps"], "steps_nn": r_nn["steps"],
+                  "wall_ratio_device": r_tf["solve_ms_device"] /
+                                       (r_nn["solve_ms_device"] + share * (infer_ms + sel_ms))}
     de = [abs(x - y) / abs(x) for x, y in zip(res["tf"]["energy"], res["nn"]["energy"])]
     rms = lambda a, b: float(np.sqrt(np.mean((a - b) ** 2)))
     s_tf, s_nn = np.array(res["tf"]["steps"], float), np.array(res["nn"]["steps"], float)
@@ -592,7 +654,22 @@ def compare(net: Surrogate, draws, tol: float = 1e-10, max_steps: int = 60000, c
         "same_end_state": int(sum(x <= 1e-4 for x in de)),   # |dE|/|E| <= 1e-4 between the two final states
         "guess_rmse_tf": [rms(np.abs(f), b_) for f, b_ in zip(finals["tf"], bases)],
         "guess_rmse_nn": [rms(np.abs(f), a_) for f, a_ in zip(finals["tf"], amps)],
+        "winding_tf": wind_tf, "winding_nn": wind_nn,
+        "omega_over_omega_perp": [prob.Omega / prob.omega[0] for prob, _ in draws],
+        "subset_tf_converged": subset,
     }
+
+
+def holdout_error(net: Surrogate, probs, targets) -> dict:
+    """Error of the network's amplitude (and of the Thomas-Fermi amplitude)
+    against held-out ground-state amplitudes: RMS over the grid per draw."""
+    amps, bases = predict_problems(net, probs)
+    rms = lambda x, y: float(np.sqrt(np.mean((x.astype(np.float64) - y) ** 2)))
+    e_nn = np.array([rms(x, t) for x, t in zip(amps, targets)])
+    e_tf = np.array([rms(b, t) for b, t in zip(bases, targets)])
+    return {"holdout": len(targets), "holdout_rmse_nn_median": float(np.median(e_nn)),
+            "holdout_rmse_nn_mean": float(np.mean(e_nn)), "holdout_rmse_tf_median": float(np.median(e_tf)),
+            "holdout_rmse_ratio_tf_over_nn_median": float(np.median(e_tf / np.maximum(e_nn, 1e-30)))}
 
 
 # ---- command line: generate, train, compare ----------------------------------------------------
@@ -669,6 +746,16 @@ def main(argv=None):
     ap.add_argument("--json", default=None)
     ap.add_argument("--time", type=int, default=0, metavar="REPS",
                     help="only time forward and training passes (random weights) and exit")
+    ap.add_argument("--curve", type=int, nargs="*", default=[],
+                    help="also train fresh networks on the first K training draws for the same number of optimizer "
+                         "steps and report their held-out error (a learning curve)")
+    ap.add_argument("--holdout-gs", type=int, default=0,
+                    help="relax this many held-out draws to their ground states and report the guess error on them")
+    ap.add_argument("--stop", choices=["rel", "per_particle"], default="per_particle",
+                    help="stop test of the comparison: |dE|/|E| <= tol or |d(E/N)| < tol in trap units")
+    ap.add_argument("--no-compare", action="store_true", help="skip the relaxation comparison")
+    ap.add_argument("--subset-rerun", action="store_true",
+                    help="also relax the draws whose TF relaxation converges as batches of their own")
     a = ap.parse_args(argv)
     if a.time:
         r = time_passes(a.S, a.batch, a.time)
@@ -693,7 +780,20 @@ def main(argv=None):
         rep["target_omega"] = a.target_omega
         rep["gen_s"] = time.perf_counter() - t0
         rep["gen_rel_dE_median"] = float(np.median([i["rel"] for i in info]))
-        log(f"generated {len(amps)} ground states in {rep['gen_s']:.1f} s, median rel dE {rep['gen_rel_dE_median']:.2e}")
+        ps = [i["phase_spread"] for i in info]
+        rep["gen_phase_spread_rad"] = {"median": float(np.median(ps)), "max": float(np.max(ps)),
+                                       "note": "largest phase deviation from the global phase where "
+                                               "|psi| >= 0.1 max|psi|, per training ground state"}
+        log(f"generated {len(amps)} ground states in {rep['gen_s']:.1f} s, median rel dE {rep['gen_rel_dE_median']:.2e}, "
+            f"phase spread median {rep['gen_phase_spread_rad']['median']:.1e} max {rep['gen_phase_spread_rad']['max']:.1e}")
+        hold = None
+        if a.holdout_gs and test_d:
+            hd = test_d[:a.holdout_gs]
+            hamps, hinfo = ground_states(hd, max_steps=a.gen_steps, tol=1e-12, frac=a.gen_frac,
+                                         omega_zero=a.target_omega == "zero")
+            hold = ([p for p, _ in hd], hamps)
+            rep["holdout_gs"] = {"instances": len(hd),
+                                 "phase_spread_rad_max": float(np.max([i["phase_spread"] for i in hinfo]))}
         X = torch.empty((a.n_train, a.S, a.S, a.S, NFEAT), dtype=torch.bfloat16, device=net.dev)
         BASE = torch.empty((a.n_train, a.S, a.S, a.S), dtype=torch.float32, device=net.dev)
         Y = torch.empty_like(BASE)
@@ -705,6 +805,21 @@ def main(argv=None):
             Y[i].copy_(torch.from_numpy(tgt))
         rep["targets_symmetrized"] = n_vortex
         rep["tf_guess_rmse"] = float(torch.sqrt(((BASE - Y) ** 2).mean()).item())
+        total_steps = a.epochs * max(1, a.n_train // a.batch)
+        curve = []
+        for k in sorted(set(x for x in a.curve if 0 < x < a.n_train)):
+            nk = Surrogate(a.S, a.batch, seed=a.seed)
+            ek = max(1, round(total_steps / max(1, k // a.batch)))
+            t0 = time.perf_counter()
+            hk = train(nk, X[:k], BASE[:k], Y[:k], epochs=ek, lr=a.lr, lr_min=a.lr * 1e-2, seed=a.seed)
+            torch.cuda.synchronize()
+            ent = {"n_train": k, "epochs": ek, "steps": nk.step_t, "train_s": time.perf_counter() - t0,
+                   "loss_last": hk[-1]}
+            if hold:
+                ent.update(holdout_error(nk, *hold))
+            curve.append(ent)
+            log(json.dumps(ent))
+            del nk
         t0 = time.perf_counter()
         hist = train(net, X, BASE, Y, epochs=a.epochs, lr=a.lr, lr_min=a.lr * 1e-2, seed=a.seed, log=log)
         rep["loss_history"] = hist
@@ -714,17 +829,28 @@ def main(argv=None):
         rep["loss_first"], rep["loss_last"] = hist[0], hist[-1]
         rep["train_rmse"] = math.sqrt(hist[-1])
         del X, BASE, Y
+        ent = {"n_train": a.n_train, "epochs": a.epochs, "steps": net.step_t, "train_s": rep["train_s"],
+               "loss_last": hist[-1]}
+        if hold:
+            ent.update(holdout_error(net, *hold))
+        curve.append(ent)
+        log(json.dumps(ent))
+        rep["learning_curve"] = curve
         if a.out:
             net.save(a.out, {"S": a.S, "n_train": a.n_train, "seed": a.seed, "epochs": a.epochs})
     # held-out accuracy of the guess itself, then the relaxation comparison
     rep["compare"] = []
-    for nz in (a.nn_noise if test_d else []):
-        cmp_ = compare(net, test_d, tol=a.tol, max_steps=a.max_steps, nn_noise=nz)
+    for nz in (a.nn_noise if test_d and not a.no_compare else []):
+        cmp_ = compare(net, test_d, tol=a.tol, max_steps=a.max_steps, nn_noise=nz, stop=a.stop,
+                       subset_rerun=a.subset_rerun)
         rep["compare"].append(cmp_)
         log(json.dumps({k: cmp_[k] for k in ("nn_noise", "nn_used", "steps_ratio_median", "steps_ratio_median_nn_used",
                                               "steps_ratio_total", "steps_ratio_total_both_converged",
                                               "wall_ratio_device", "final_energy_rel_diff_max", "same_end_state",
                                               "tf_kept_fast_rotation")}))
+        if cmp_["subset_tf_converged"]:
+            log(json.dumps({"subset_tf_converged": {k: v for k, v in cmp_["subset_tf_converged"].items()
+                                                    if not k.startswith("steps")}}))
     if a.json:
         with open(a.json, "w") as f:
             json.dump(rep, f, indent=1)
