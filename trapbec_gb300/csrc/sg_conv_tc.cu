@@ -38,11 +38,16 @@ constexpr uint32_t ACC_COLS = 32;               // one accumulator: 128 lanes x 
 constexpr uint32_t TMEM_COLS = 2 * ACC_COLS;    // two accumulators
 __device__ int g_timeout = 0;                   // set when a wait gave up
 
+constexpr int SM_SMEM = 232448;                 // shared memory of one SM (bytes)
+
 template <int CIN, int COUT> struct Cfg {
   static constexpr int KC = CIN / 8;
   static constexpr int STAGE = KC * CHUNK;                       // one halo
   static constexpr int W_BYTES = 27 * KC * COUT * 16;
-  static constexpr int NS = (STAGE * 3 + W_BYTES <= 150 * 1024) ? 3 : 2;   // halo ring depth
+  // CTAs per SM that a halo ring of `ns` stages leaves room for (1 KB per CTA reserved)
+  static constexpr int fit(int ns) { return SM_SMEM / (ns * STAGE + W_BYTES + 128 + 1024); }
+  // halo ring depth: 3, or 2 where that lets more CTAs (more MMA issuers) share an SM
+  static constexpr int NS = fit(2) > fit(3) ? 2 : 3;
   static constexpr int W_OFF = NS * STAGE;
   static constexpr int BAR_OFF = (W_OFF + W_BYTES + 127) / 128 * 128;
   static constexpr int SMEM = BAR_OFF + 128;
@@ -244,13 +249,25 @@ int launch(const Args& a, cudaStream_t st) {
     if (cudaFuncSetAttribute(conv3_tc_kernel<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM) !=
         cudaSuccess)
       return TBSG_ERR_CUDA;
-    int dev = 0, nsm = 0, nb = 0;
+    // CTAs per SM: as many as the SM's shared memory holds (the TMEM of one
+    // SM, 512 columns, holds 8 of them); all of the SM's shared memory is
+    // given to the carveout
+    if (cudaFuncSetAttribute(conv3_tc_kernel<CIN, COUT>, cudaFuncAttributePreferredSharedMemoryCarveout, 100) !=
+        cudaSuccess)
+      return TBSG_ERR_CUDA;
+    int dev = 0, nsm = 0, smem_sm = 0, reserved = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, conv3_tc_kernel<CIN, COUT>, NTHR, C::SMEM) != cudaSuccess ||
-        nb < 1)
-      return TBSG_ERR_CUDA;
+    cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+    int nb = smem_sm / (C::SMEM + reserved);
     if (nb * (int)TMEM_COLS > 512) nb = 512 / (int)TMEM_COLS;   // TMEM of one SM
+    if (nb * NTHR > 2048) nb = 2048 / NTHR;
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, conv3_tc_kernel<CIN, COUT>) != cudaSuccess) return TBSG_ERR_CUDA;
+    const int regs = (fa.numRegs + 7) / 8 * 8;   // allocated per thread in units of 8
+    if (regs > 0 && nb * NTHR * regs > 65536) nb = 65536 / (NTHR * regs);
+    if (nsm < 1 || nb < 1) return TBSG_ERR_CUDA;
     grid = nb * nsm;
   }
   // the activation tensor [B][D][H][W][CIN] as a 5-D TMA map (innermost first)

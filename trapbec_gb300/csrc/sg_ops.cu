@@ -285,11 +285,21 @@ __global__ void __launch_bounds__(HEAD_THREADS) head_loss16_kernel(const uint4* 
   if ((int)threadIdx.x < NP) partials[(size_t)blockIdx.x * NP + threadIdx.x] = red[threadIdx.x * HEAD_THREADS];
 }
 
-__global__ void head_final_kernel(const float* partials, int nblk, int np, float* out) {
-  for (int k = threadIdx.x; k < np; k += blockDim.x) {
+// out[k] = sum over the blocks' partials of quantity k: each of 256 threads
+// adds a fixed strided subset, then one fixed shared-memory tree per quantity
+__global__ void __launch_bounds__(256) head_final_kernel(const float* partials, int nblk, int np, float* out) {
+  __shared__ float red[256];
+  for (int k = 0; k < np; ++k) {
     float s = 0.f;
-    for (int b = 0; b < nblk; ++b) s += partials[(size_t)b * np + k];
-    out[k] = s;
+    for (int b = threadIdx.x; b < nblk; b += 256) s += partials[(size_t)b * np + k];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int h = 128; h > 0; h >>= 1) {
+      if ((int)threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) out[k] = red[0];
+    __syncthreads();
   }
 }
 
@@ -323,11 +333,20 @@ __global__ void sumsq_kernel(const float* g, size_t n, float* partials) {
   if (threadIdx.x == 0) partials[blockIdx.x] = (float)red[0];
 }
 
-__global__ void clip_final_kernel(const float* partials, int nblk, float max_norm, float* out) {
+// the block partials summed in FP64 by 256 threads (fixed strided subsets and
+// a fixed tree), then the norm and the clipping factor
+__global__ void __launch_bounds__(256) clip_final_kernel(const float* partials, int nblk, float max_norm, float* out) {
+  __shared__ double red[256];
+  double s = 0.0;
+  for (int b = threadIdx.x; b < nblk; b += 256) s += partials[b];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int h = 128; h > 0; h >>= 1) {
+    if ((int)threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+    __syncthreads();
+  }
   if (threadIdx.x == 0) {
-    double s = 0.0;
-    for (int b = 0; b < nblk; ++b) s += partials[b];
-    const double nrm = sqrt(s);
+    const double nrm = sqrt(red[0]);
     out[0] = (float)nrm;
     out[1] = nrm > max_norm ? (float)(max_norm / nrm) : 1.f;
   }
@@ -483,7 +502,7 @@ int tbsg_clip_scale(const float* g, size_t n, float max_norm, float* partials, f
   if (!g || !partials || !out || !(max_norm > 0.f)) return TBSG_ERR_ARG;
   cudaStream_t st = (cudaStream_t)stream;
   sumsq_kernel<<<CLIP_BLOCKS, 256, 0, st>>>(g, n, partials);
-  clip_final_kernel<<<1, 32, 0, st>>>(partials, CLIP_BLOCKS, max_norm, out);
+  clip_final_kernel<<<1, 256, 0, st>>>(partials, CLIP_BLOCKS, max_norm, out);
   return done();
 }
 

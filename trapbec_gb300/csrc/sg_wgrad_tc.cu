@@ -228,10 +228,20 @@ __global__ void __launch_bounds__(NTHR, 1)
   if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(512));
 }
 
+// out[i] = sum of the CTAs' partials in CTA order; the loads of eight CTAs
+// are issued together (one memory latency per eight, same summation order)
 __global__ void reduce_parts_kernel(const float* part, int nchunk, size_t n, float* out) {
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     float s = 0.f;
-    for (int c = 0; c < nchunk; ++c) s += part[(size_t)c * n + i];
+    int c = 0;
+    for (; c + 8 <= nchunk; c += 8) {
+      float v[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) v[j] = part[(size_t)(c + j) * n + i];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) s += v[j];
+    }
+    for (; c < nchunk; ++c) s += part[(size_t)c * n + i];
     out[i] = s;
   }
 }
