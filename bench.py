@@ -48,6 +48,34 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
+def load_bf16_peak():
+    """Dense BF16 TFLOP/s of this GPU as a burst (cuBLAS, measured), else the fallback figure."""
+    p = os.path.join(HERE, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        if "bf16_tflops" in d:
+            return float(d["bf16_tflops"]), "measured"
+    return 1900.0, "fallback"
+
+
+def surrogate_kernels():
+    """Tensor-core rate of the surrogate's convolutions at 128^3, batch 2:
+    one forward pass and one training step (forward, input and weight
+    gradients, clipping, Adam), device time from events, against the
+    measured BF16 burst peak."""
+    from trapbec_gb300 import surrogate
+    r = surrogate.time_passes(128, 2, 5)
+    peak, kind = load_bf16_peak()
+    return {"grid": 128, "batch": 2, "forward_ms": r["forward_ms"], "train_step_ms": r["train_step_ms"],
+            "conv_gflop_forward": r["conv_gflop_forward"], "conv_gflop_backward": r["conv_gflop_backward"],
+            "forward": {"bound": "tensor", "achieved": r["conv_tflops_forward"], "peak": peak, "unit": "TFLOP/s",
+                        "frac": r["conv_tflops_forward"] / peak, "peak_kind": kind},
+            "train_step": {"bound": "tensor", "achieved": r["conv_tflops_train_step"], "peak": peak,
+                           "unit": "TFLOP/s", "frac": r["conv_tflops_train_step"] / peak, "peak_kind": kind},
+            "kernels": "tcgen05: conv3_tc_kernel (16/32 channels), conv3_tcs_kernel (64/128, streamed weights), "
+                       "conv3_wgrad_tc_kernel (weight gradients)"}
+
+
 def profile_traffic(prec_tag: str, tz: int | None = None, ty: int | None = None, form: str = ""):
     """DRAM bytes per grid point per stage launch from the committed ncu summary
     of the full-size launch list of the tile shape and RK3 form that ran
@@ -566,6 +594,7 @@ def run_gpu_arm(args):
         line["imag"] = imag_leg(args)
     if rank == 0 and world == 1 and not args.no_warmstart:
         line["warmstart"] = warmstart_leg(args)
+        line["warmstart"]["surrogate_kernels"] = surrogate_kernels()
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:

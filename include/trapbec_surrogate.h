@@ -38,6 +38,18 @@ int tbsg_conv3_fwd(const void* x, int cin, const void* w, const float* bias, con
                    float* yf, int yf_accumulate, int cout, int batch, int D, int H, int W, int act, float slope,
                    void* stream);
 
+/* Input gradient of a convolution fused with the leaky-ReLU derivative of
+ * the activation below it: with g = conv(dz, wt) (dz [..][cout], wt the
+ * flipped, transposed weights of tbsg_weight_prep, g [..][cin] in FP32
+ * accumulation), writes dz_in = BF16(g * act'(y_in)) (act' = 1 where
+ * y_in > 0, else slope; y_in the activation's BF16 output [..][cin]) and, if
+ * dskip != NULL, dskip += g * act'(y_in) (FP32).  Equal, bit for bit, to
+ * tbsg_conv3_fwd(dz, cout, wt, .., yf = g, cin, ..) followed by
+ * tbsg_act_bwd(g, y_in, dz_in, dskip, ..), without the FP32 g in memory.
+ * y_in, dz_in and dskip must be 16-byte aligned.                          */
+int tbsg_conv3_dgrad_act(const void* dz, int cout, const void* wt, const void* y_in, void* dz_in, float* dskip,
+                         int cin, int batch, int D, int H, int W, float slope, void* stream);
+
 /* Kernel family of tbsg_conv3_fwd and tbsg_conv3_wgrad: 0 (default) =
  * tcgen05.mma with TMEM accumulators (forward: 16/32 -> 16/32 channels,
  * mma.sync for the others; weight gradients: every pair); 1 = mma.sync for

@@ -89,6 +89,16 @@ def test_conv3_forward_and_gradients(cin, cout, conv_path):
     out = nn_oracle.conv3(xr, wr, torch.zeros(cout, dtype=torch.float64, requires_grad=True))
     (out * dz64).sum().backward()
     assert (gx.double().cpu() - xr.grad).abs().max() <= 1e-5 * xr.grad.abs().max()
+    # the input gradient fused with the activation derivative below: bit for bit the two-step result
+    yin = _bf(rng.normal(size=(B, D, H, W, cin)))
+    dz_ref = torch.empty((B, D, H, W, cin), dtype=torch.bfloat16, device="cuda")
+    sk_ref = torch.tensor(rng.normal(size=(B, D, H, W, cin)), dtype=torch.float32, device="cuda")
+    sk = sk_ref.clone()
+    assert lib.tbsg_act_bwd(_p(gx), _p(yin), _p(dz_ref), _p(sk_ref), gx.numel(), 0.05, st) == 0
+    dz_in = torch.empty_like(dz_ref)
+    assert lib.tbsg_conv3_dgrad_act(_p(dzb), cout, _p(wt), _p(yin), _p(dz_in), _p(sk), cin, B, D, H, W, 0.05, st) == 0
+    assert torch.equal(dz_in.view(torch.int16), dz_ref.view(torch.int16))
+    assert torch.equal(sk, sk_ref)
     # weight and bias gradients
     dw = torch.empty((27, cout, cin), dtype=torch.float32, device="cuda")
     db = torch.empty(cout, dtype=torch.float32, device="cuda")
@@ -190,7 +200,7 @@ def _net_inputs(S, B, seed):
     return x, base, tgt
 
 
-def _net_grads(seed=3):
+def _net_grads(seed=3, fused=True):
     S, B = 16, 2
     net = Surrogate(S, B, seed=seed)
     net.p[-(NFEAT + 1):].copy_(torch.linspace(-0.5, 0.5, NFEAT + 1))   # a non-zero head
@@ -199,8 +209,19 @@ def _net_grads(seed=3):
     xt = torch.tensor(x).cuda()
     bt, tt = torch.tensor(base).cuda(), torch.tensor(tgt).cuda()
     net.forward(xt, bt)
-    loss = net.backward(tt).item()
+    loss = net.backward(tt, fused=fused).item()
     return net, xt, bt, tt, loss
+
+
+def test_fused_backward_equals_unfused():
+    """The backward pass with input gradients fused into the activation
+    derivatives (the training path) gives the parameter gradients and the
+    loss of the unfused pass bit for bit."""
+    net, xt, bt, tt, loss = _net_grads(fused=True)
+    g_fused = net.g.clone()
+    loss2 = net.backward(tt, fused=False).item()
+    assert loss2 == loss
+    assert torch.equal(net.g, g_fused)
 
 
 # (layer, input activation, output activation, gradient of the input or None, skip tensor or None)
@@ -215,7 +236,7 @@ def test_network_backward_wiring():
     """Every backward step of the network recomputed in float64 from the
     GPU's own activations and upstream gradients (exact up to FP32 sums)."""
     from trapbec_gb300.surrogate import SLOPE
-    net, xt, bt, tt, loss = _net_grads()
+    net, xt, bt, tt, loss = _net_grads(fused=False)   # every FP32 activation gradient in memory
     A = {k: v.double().cpu() for k, v in net.A.items()}
     G = {k: v.double().cpu() for k, v in net.G.items()}
     g = net.g.double().cpu()

@@ -180,6 +180,8 @@ _PROTOS = {
     # learned warm start (include/trapbec_surrogate.h)
     "tbsg_conv3_fwd": (C.c_int, [_VP, C.c_int, _VP, _VP, _VP, _VP, _VP, C.c_int, C.c_int, C.c_int, C.c_int,
                                  C.c_int, C.c_int, C.c_int, C.c_float, _VP]),
+    "tbsg_conv3_dgrad_act": (C.c_int, [_VP, C.c_int, _VP, _VP, _VP, _VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                       C.c_float, _VP]),
     "tbsg_set_conv_path": (C.c_int, [C.c_int]),
     "tbsg_tc_status": (C.c_int, [C.POINTER(C.c_int)]),
     "tbsg_conv3_wgrad_scratch_bytes": (C.c_size_t, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]),

@@ -55,4 +55,40 @@ __device__ __forceinline__ void mma_bf16(float d[4], const uint32_t a[4], uint32
 
 __device__ __forceinline__ float leaky(float v, float s) { return v > 0.f ? v : v * s; }
 
+// Input-gradient epilogue fused with the leaky ReLU's derivative (mode 3):
+// for 16 consecutive channels at element offset o, g = v * act'(y) with y
+// the activation's output, dz = BF16(g), dskip += g -- the same operations,
+// in the same order, as storing v in FP32 and running the activation-
+// gradient kernel on it.
+__device__ __forceinline__ void act_grad16(const float v[16], const bf16* yact, bf16* dz, float* dskip, size_t o,
+                                           float slope) {
+  const uint4* yp = (const uint4*)(yact + o);
+  const uint4 q0 = yp[0], q1 = yp[1];
+  const bf16* e0 = (const bf16*)&q0;
+  const bf16* e1 = (const bf16*)&q1;
+  float g[16];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    g[j] = v[j] * (__bfloat162float(e0[j]) > 0.f ? 1.f : slope);
+    g[8 + j] = v[8 + j] * (__bfloat162float(e1[j]) > 0.f ? 1.f : slope);
+  }
+  uint4 o0, o1;
+  bf16* f0 = (bf16*)&o0;
+  bf16* f1 = (bf16*)&o1;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) { f0[j] = __float2bfloat16_rn(g[j]); f1[j] = __float2bfloat16_rn(g[8 + j]); }
+  uint4* dp = (uint4*)(dz + o);
+  dp[0] = o0;
+  dp[1] = o1;
+  if (dskip) {
+    float4* sp = (float4*)(dskip + o);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      float4 t = sp[q];
+      t.x += g[4 * q]; t.y += g[4 * q + 1]; t.z += g[4 * q + 2]; t.w += g[4 * q + 3];
+      sp[q] = t;
+    }
+  }
+}
+
 }  // namespace sg

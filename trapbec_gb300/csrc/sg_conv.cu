@@ -36,12 +36,14 @@ struct FwdArgs {
   const bf16* w;       // [27][COUT][CIN]
   const float* bias;   // [COUT] or null
   const bf16* skip;    // [B][V][COUT] or null, added before the activation
-  bf16* y;             // mode 0 output
+  bf16* y;             // mode 0 output; mode 3: BF16(v act'(yact))
   float* yf;           // mode 1 (+=) / mode 2 (=) output
   int D, H, W;
   int act;
   float slope;
   int mode;
+  const bf16* yact;    // mode 3: the output of the activation whose input gradient this is
+  float* dskip;        // mode 3: optional FP32 accumulation of v act'(yact)
 };
 
 template <int CIN, int COUT>
@@ -144,6 +146,17 @@ __global__ void __launch_bounds__(NTHR, 1) conv3_fwd_kernel(FwdArgs a) {
         }
         if (a.act) { v0 = leaky(v0, a.slope); v1 = leaky(v1, a.slope); }
         *(__nv_bfloat162*)(a.y + gv * COUT + c) = __floats2bfloat162_rn(v0, v1);
+      } else if (a.mode == 3) {
+        const __nv_bfloat162 yy = *(const __nv_bfloat162*)(a.yact + gv * COUT + c);
+        const float g0 = v0 * (__bfloat162float(yy.x) > 0.f ? 1.f : a.slope);
+        const float g1 = v1 * (__bfloat162float(yy.y) > 0.f ? 1.f : a.slope);
+        *(__nv_bfloat162*)(a.y + gv * COUT + c) = __floats2bfloat162_rn(g0, g1);
+        if (a.dskip) {
+          float2* sp = (float2*)(a.dskip + gv * COUT + c);
+          float2 t = *sp;
+          t.x += g0; t.y += g1;
+          *sp = t;
+        }
       } else {
         float2* o = (float2*)(a.yf + gv * COUT + c);
         if (a.mode == 1) { float2 t = *o; t.x += v0; t.y += v1; *o = t; }
@@ -329,13 +342,45 @@ int wgrad_launch(const WgArgs& a, int nch, float* dw, float* db, cudaStream_t st
 #define SG_PAIRS(X) X(16, 16) X(16, 32) X(32, 16) X(32, 32) X(32, 64) X(64, 32) X(64, 64) X(64, 128) X(128, 64) X(128, 128)
 
 int conv3_fwd_tc(const void* x, int cin, const void* w, const float* bias, const void* skip, void* y, float* yf,
-                 int yf_accumulate, int cout, int batch, int D, int H, int W, int act, float slope, cudaStream_t st);
+                 int yf_accumulate, int cout, int batch, int D, int H, int W, int act, float slope, const void* yact,
+                 float* dskip, cudaStream_t st);
 int conv3_fwd_tcs(const void* x, int cin, const void* w, const float* bias, const void* skip, void* y, float* yf,
-                  int yf_accumulate, int cout, int batch, int D, int H, int W, int act, float slope, cudaStream_t st);
+                  int yf_accumulate, int cout, int batch, int D, int H, int W, int act, float slope, const void* yact,
+                  float* dskip, cudaStream_t st);
 int g_conv_path = 0;   // 0: tcgen05 where built, else mma.sync; 1: mma.sync only
 size_t wgrad_tc_scratch_bytes(int cin, int cout, int batch, int D, int H, int W);
 int wgrad_tc(const void* x, int cin, const void* dz, int cout, int batch, int D, int H, int W, float* dw, float* db,
              void* scratch, cudaStream_t st);
+
+}  // namespace sg
+
+namespace sg {
+
+// The convolution of tbsg_conv3_fwd / tbsg_conv3_dgrad_act: tcgen05 kernels
+// where built (path 0), else (or with path 1) the mma.sync kernels.
+int conv3_any(const void* x, int cin, const void* w, const float* bias, const void* skip, void* y, float* yf,
+              int yf_accumulate, int cout, int batch, int D, int H, int W, int act, float slope, const void* yact,
+              float* dskip, cudaStream_t st) {
+  FwdArgs a;
+  a.x = (const bf16*)x; a.w = (const bf16*)w; a.bias = bias; a.skip = (const bf16*)skip;
+  a.y = (bf16*)y; a.yf = yf;
+  a.D = D; a.H = H; a.W = W;
+  a.act = act; a.slope = slope;
+  a.mode = yact ? 3 : (yf ? (yf_accumulate ? 1 : 2) : 0);
+  a.yact = (const bf16*)yact; a.dskip = dskip;
+  if (g_conv_path == 0) {
+    int rc = conv3_fwd_tc(x, cin, w, bias, skip, y, yf, yf_accumulate, cout, batch, D, H, W, act, slope, yact, dskip,
+                          st);
+    if (rc != TBSG_ERR_SHAPE) return rc;
+    rc = conv3_fwd_tcs(x, cin, w, bias, skip, y, yf, yf_accumulate, cout, batch, D, H, W, act, slope, yact, dskip, st);
+    if (rc != TBSG_ERR_SHAPE) return rc;
+  }
+#define SG_FWD(I, O) \
+  if (cin == I && cout == O) return fwd_launch<I, O>(a, batch, st);
+  SG_PAIRS(SG_FWD)
+#undef SG_FWD
+  return TBSG_ERR_SHAPE;
+}
 
 }  // namespace sg
 
@@ -353,24 +398,16 @@ int tbsg_conv3_fwd(const void* x, int cin, const void* w, const float* bias, con
                    float* yf, int yf_accumulate, int cout, int batch, int D, int H, int W, int act, float slope,
                    void* stream) {
   if (!x || !w || (!y && !yf) || batch <= 0 || D <= 0 || H <= 0 || W <= 0) return TBSG_ERR_ARG;
-  FwdArgs a;
-  a.x = (const bf16*)x; a.w = (const bf16*)w; a.bias = bias; a.skip = (const bf16*)skip;
-  a.y = (bf16*)y; a.yf = yf;
-  a.D = D; a.H = H; a.W = W;
-  a.act = act; a.slope = slope;
-  a.mode = yf ? (yf_accumulate ? 1 : 2) : 0;
-  cudaStream_t st = (cudaStream_t)stream;
-  if (g_conv_path == 0) {
-    int rc = conv3_fwd_tc(x, cin, w, bias, skip, y, yf, yf_accumulate, cout, batch, D, H, W, act, slope, st);
-    if (rc != TBSG_ERR_SHAPE) return rc;
-    rc = conv3_fwd_tcs(x, cin, w, bias, skip, y, yf, yf_accumulate, cout, batch, D, H, W, act, slope, st);
-    if (rc != TBSG_ERR_SHAPE) return rc;
-  }
-#define SG_FWD(I, O) \
-  if (cin == I && cout == O) return fwd_launch<I, O>(a, batch, st);
-  SG_PAIRS(SG_FWD)
-#undef SG_FWD
-  return TBSG_ERR_SHAPE;
+  return conv3_any(x, cin, w, bias, skip, y, yf, yf_accumulate, cout, batch, D, H, W, act, slope, nullptr, nullptr,
+                   (cudaStream_t)stream);
+}
+
+int tbsg_conv3_dgrad_act(const void* dz, int cout, const void* wt, const void* y_in, void* dz_in, float* dskip,
+                         int cin, int batch, int D, int H, int W, float slope, void* stream) {
+  if (!dz || !wt || !y_in || !dz_in || batch <= 0 || D <= 0 || H <= 0 || W <= 0) return TBSG_ERR_ARG;
+  if (((uintptr_t)y_in | (uintptr_t)dz_in | (uintptr_t)dskip) % 16) return TBSG_ERR_ARG;
+  return conv3_any(dz, cout, wt, nullptr, nullptr, dz_in, nullptr, 0, cin, batch, D, H, W, 0, slope, y_in, dskip,
+                   (cudaStream_t)stream);
 }
 
 size_t tbsg_conv3_wgrad_scratch_bytes(int cin, int cout, int batch, int D, int H, int W) {

@@ -46,8 +46,10 @@ template <int CIN, int COUT> struct Cfg {
   static constexpr int W_BYTES = 27 * KC * COUT * 16;
   // CTAs per SM that a halo ring of `ns` stages leaves room for (1 KB per CTA reserved)
   static constexpr int fit(int ns) { return SM_SMEM / (ns * STAGE + W_BYTES + 128 + 1024); }
-  // halo ring depth: 3, or 2 where that lets more CTAs (more MMA issuers) share an SM
-  static constexpr int NS = fit(2) > fit(3) ? 2 : 3;
+  // halo ring depth: 3, or 2 where 3 leaves room for one CTA only and 2 for more (more MMA issuers
+  // per SM; measured: 32 -> 16 channels 201 -> 166 us per launch; with 2 or more CTAs already the
+  // deeper ring was as fast or faster)
+  static constexpr int NS = (fit(3) < 2 && fit(2) > fit(3)) ? 2 : 3;
   static constexpr int W_OFF = NS * STAGE;
   static constexpr int BAR_OFF = (W_OFF + W_BYTES + 127) / 128 * 128;
   static constexpr int SMEM = BAR_OFF + 128;
@@ -63,7 +65,9 @@ struct Args {
   int B, D, H, W;
   int act;
   float slope;
-  int mode;            // 0: BF16 epilogue, 1: FP32 +=, 2: FP32 =
+  int mode;            // 0: BF16 epilogue, 1: FP32 +=, 2: FP32 =, 3: y = BF16(v act'(yact)), dskip += that
+  const bf16* yact;    // mode 3: the output of the activation whose input gradient this is
+  float* dskip;        // mode 3: optional FP32 accumulation
 };
 
 template <int CIN, int COUT>
@@ -220,6 +224,8 @@ __global__ void __launch_bounds__(NTHR, 1) conv3_tc_kernel(const __grid_constant
           uint4* op = (uint4*)(a.y + gv * COUT + c0);
           op[0] = o0;
           op[1] = o1;
+        } else if (a.mode == 3) {
+          act_grad16(v, a.yact, a.y, a.dskip, gv * COUT + c0, a.slope);
         } else {
           float4* op = (float4*)(a.yf + gv * COUT + c0);
 #pragma unroll
@@ -294,13 +300,15 @@ int launch(const Args& a, cudaStream_t st) {
 
 // tcgen05 path for 16/32 -> 16/32 channels; TBSG_ERR_SHAPE for the others
 int conv3_fwd_tc(const void* x, int cin, const void* w, const float* bias, const void* skip, void* y, float* yf,
-                 int yf_accumulate, int cout, int batch, int D, int H, int W, int act, float slope, cudaStream_t st) {
+                 int yf_accumulate, int cout, int batch, int D, int H, int W, int act, float slope, const void* yact,
+                 float* dskip, cudaStream_t st) {
   tc::Args a;
   a.x = (const bf16*)x; a.w = (const bf16*)w; a.bias = bias; a.skip = (const bf16*)skip;
   a.y = (bf16*)y; a.yf = yf;
   a.B = batch; a.D = D; a.H = H; a.W = W;
   a.act = act; a.slope = slope;
-  a.mode = yf ? (yf_accumulate ? 1 : 2) : 0;
+  a.mode = yact ? 3 : (yf ? (yf_accumulate ? 1 : 2) : 0);
+  a.yact = (const bf16*)yact; a.dskip = dskip;
   if ((uintptr_t)x % 16) return TBSG_ERR_SHAPE;   // TMA needs a 16-byte aligned base
   if (cin == 16 && cout == 16) return tc::launch<16, 16>(a, st);
   if (cin == 16 && cout == 32) return tc::launch<16, 32>(a, st);

@@ -64,7 +64,9 @@ struct Args {
   int B, D, H, W;
   int act;
   float slope;
-  int mode;            // 0: BF16 epilogue, 1: FP32 +=, 2: FP32 =
+  int mode;            // 0: BF16 epilogue, 1: FP32 +=, 2: FP32 =, 3: y = BF16(v act'(yact)), dskip += that
+  const bf16* yact;
+  float* dskip;
 };
 
 template <int CIN, int COUT>
@@ -220,6 +222,8 @@ __global__ void __launch_bounds__(NTHR, 1)
           uint4* op = (uint4*)(a.y + o);
           op[0] = o0;
           op[1] = o1;
+        } else if (a.mode == 3) {
+          act_grad16(v, a.yact, a.y, a.dskip, o, a.slope);
         } else {
           float4* op = (float4*)(a.yf + o);
 #pragma unroll
@@ -302,13 +306,15 @@ int launch(const Args& a, cudaStream_t st) {
 
 // streamed-weight tcgen05 path for the 64/128-channel pairs; TBSG_ERR_SHAPE for the others
 int conv3_fwd_tcs(const void* x, int cin, const void* w, const float* bias, const void* skip, void* y, float* yf,
-                  int yf_accumulate, int cout, int batch, int D, int H, int W, int act, float slope, cudaStream_t st) {
+                  int yf_accumulate, int cout, int batch, int D, int H, int W, int act, float slope, const void* yact,
+                  float* dskip, cudaStream_t st) {
   tcs::Args a;
   a.x = (const bf16*)x; a.w = (const bf16*)w; a.bias = bias; a.skip = (const bf16*)skip;
   a.y = (bf16*)y; a.yf = yf;
   a.B = batch; a.D = D; a.H = H; a.W = W;
   a.act = act; a.slope = slope;
-  a.mode = yf ? (yf_accumulate ? 1 : 2) : 0;
+  a.mode = yact ? 3 : (yf ? (yf_accumulate ? 1 : 2) : 0);
+  a.yact = (const bf16*)yact; a.dskip = dskip;
   if ((uintptr_t)x % 16 || (uintptr_t)w % 16) return TBSG_ERR_SHAPE;   // TMA needs 16-byte aligned bases
   if (cin == 32 && cout == 64) return tcs::launch<32, 64>(a, st);
   if (cin == 64 && cout == 32) return tcs::launch<64, 32>(a, st);

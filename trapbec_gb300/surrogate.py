@@ -175,6 +175,9 @@ class Surrogate:
         self.G = G
         self.dz = {lev: t.empty((B, S[lev], S[lev], S[lev], 16 << lev), dtype=t.bfloat16, device=self.dev)
                    for lev in range(4)}
+        # the second dz buffer of a level: an input gradient fused with the activation derivative below
+        # reads one and writes the other
+        self.dz2 = {lev: t.empty_like(self.dz[lev]) for lev in range(4)}
         sb = max(self.lib.tbsg_conv3_wgrad_scratch_bytes(ci, co, B, S[lv], S[lv], S[lv])
                  for (n, ci, co), lv in zip(LAYERS, [0, 0, 1, 1, 2, 2, 3, 3, 3, 2, 2, 1, 1, 0, 0]))
         self.scratch = t.empty(sb // 4 + 1, dtype=t.float32, device=self.dev)
@@ -228,6 +231,20 @@ class Surrogate:
                                              self._ptr(g_in), 0, ci, self.B, D, D, D, 0, 0.0, self._st()),
                      f"dgrad {name}")
 
+    def _conv_bwd_act(self, name, x_in, dz, D, y_in, dz_in, dskip=None):
+        """Weight gradient of `name`, then its input gradient fused with the
+        activation derivative of the layer below (y_in its output): dz_in and,
+        optionally, dskip += the activation's input gradient."""
+        _, ci, co = next(l for l in LAYERS if l[0] == name)
+        w0, b0, _, _ = self.view[name]
+        dw, db = self.g[w0:b0], self.g[b0:b0 + co]
+        self._ck(self.lib.tbsg_conv3_wgrad(self._ptr(x_in), ci, self._ptr(dz), co, self.B, D, D, D, self._ptr(dw),
+                                           self._ptr(db), self._ptr(self.scratch), self.scratch_bytes, self._st()),
+                 f"wgrad {name}")
+        self._ck(self.lib.tbsg_conv3_dgrad_act(self._ptr(dz), co, self._ptr(self.wt[name]), self._ptr(y_in),
+                                               self._ptr(dz_in), self._ptr(dskip), ci, self.B, D, D, D, SLOPE,
+                                               self._st()), f"dgrad_act {name}")
+
     def _act_bwd(self, g, y, dz, dskip=None):
         self._ck(self.lib.tbsg_act_bwd(self._ptr(g), self._ptr(y), self._ptr(dz), self._ptr(dskip), y.numel(), SLOPE,
                                        self._st()), "act_bwd")
@@ -264,9 +281,14 @@ class Surrogate:
                                  self._ptr(base), self._ptr(self.amp), self.amp.numel(), st), "head")
         return self.amp
 
-    def backward(self, target: "torch.Tensor") -> "torch.Tensor":
+    def backward(self, target: "torch.Tensor", fused: bool = True) -> "torch.Tensor":
         """Gradients of mean((amp - target)^2) of the last forward() into
-        self.g; returns the loss (a 1-element device tensor)."""
+        self.g; returns the loss (a 1-element device tensor).  fused: input
+        gradients that feed an activation derivative directly are computed
+        with it (tbsg_conv3_dgrad_act) instead of through an FP32 gradient
+        in memory; the parameter gradients are the same, bit for bit."""
+        if fused:
+            return self._backward_fused(target)
         A, G, S, L, dz = self.A, self.G, self.S, self.lib, self.dz
         st = self._st()
         s0, s1, s2, s3 = S, S // 2, S // 4, S // 8
@@ -303,6 +325,46 @@ class Surrogate:
         self._ck(L.tbsg_pool2_bwd(self._ptr(G["p1"]), self._ptr(G["e0"]), 16, self.B, s0, s0, s0, st), "pool_bwd")
         self._act_bwd(G["e0"], A["e0"], dz[0]); self._conv_bwd("e0b", A["e0a"], dz[0], s0, G["e0a"])
         self._act_bwd(G["e0a"], A["e0a"], dz[0]); self._conv_bwd("e0a", A["x0"], dz[0], s0, None)
+        return self.head_out[0:1]
+
+    def _backward_fused(self, target):
+        A, G, S, L, dz, dz2 = self.A, self.G, self.S, self.lib, self.dz, self.dz2
+        st = self._st()
+        s0, s1, s2, s3 = S, S // 2, S // 4, S // 8
+        h0, h1, _, _ = self.view["head"]
+        self._ck(L.tbsg_head_loss(self._ptr(A["d0"]), NFEAT, self._ptr(self.p[h0:h1]), self._ptr(self.p[h1:h1 + 1]),
+                                  self._ptr(self.base), self._ptr(target), self.amp.numel(), self._ptr(G["d0"]),
+                                  self._ptr(self.partials), self._ptr(self.head_out), st), "head_loss")
+        self.g[h0:h1 + 1].copy_(self.head_out[1:NFEAT + 2])
+        for k in ("e0", "e1", "e2"):
+            G[k].zero_()
+        # decoder: level 0, 1, 2 (the skip gradients accumulate into e0, e1, e2)
+        for lev, D, (b, a_), yb, up, gnext, cn in ((0, s0, ("d0b", "d0a"), "d0", "u0", "d1", 32),
+                                                    (1, s1, ("d1b", "d1a"), "d1", "u1", "d2", 64),
+                                                    (2, s2, ("d2b", "d2a"), "d2", "u2", "e3", 128)):
+            self._act_bwd(G[yb], A[yb], dz[lev])
+            self._conv_bwd_act(b, A[a_], dz[lev], D, A[a_], dz2[lev], G["e%d" % lev])
+            self._conv_bwd(a_, A[up], dz2[lev], D, G[up])
+            Dc = D // 2
+            self._ck(L.tbsg_up2_bwd(self._ptr(G[up]), self._ptr(G[gnext]), cn, self.B, Dc, Dc, Dc, st), "up_bwd")
+        # bottleneck
+        self._act_bwd(G["e3"], A["e3"], dz[3])
+        self._conv_bwd_act("e3c", A["e3b"], dz[3], s3, A["e3b"], dz2[3])
+        self._conv_bwd_act("e3b", A["e3a"], dz2[3], s3, A["e3a"], dz[3])
+        self._conv_bwd("e3a", A["p3"], dz[3], s3, G["p3"])
+        self._ck(L.tbsg_pool2_bwd(self._ptr(G["p3"]), self._ptr(G["e2"]), 64, self.B, s2, s2, s2, st), "pool_bwd")
+        # encoder: level 2, 1, 0
+        for lev, D, (b, a_), yb, pin, cin_ in ((2, s2, ("e2b", "e2a"), "e2", "p2", 32),
+                                               (1, s1, ("e1b", "e1a"), "e1", "p1", 16),
+                                               (0, s0, ("e0b", "e0a"), "e0", "x0", None)):
+            self._act_bwd(G[yb], A[yb], dz[lev])
+            self._conv_bwd_act(b, A[a_], dz[lev], D, A[a_], dz2[lev])
+            self._conv_bwd(a_, A[pin], dz2[lev], D, G[pin] if cin_ else None)
+            if cin_:
+                Dp = D
+                fine = "e%d" % (lev - 1)
+                self._ck(L.tbsg_pool2_bwd(self._ptr(G[pin]), self._ptr(G[fine]), cin_, self.B, 2 * Dp, 2 * Dp, 2 * Dp,
+                                          st), "pool_bwd")
         return self.head_out[0:1]
 
     def adam_step(self, lr: float, beta1=0.9, beta2=0.999, eps=1e-8, weight_decay=0.0, max_norm: float = 1.0):
