@@ -10,19 +10,20 @@
 //    chunk lands as [w][h][8 ch]: 8 consecutive h of one column are one
 //    MN-major core matrix (128 contiguous bytes), the next 8 h are 128 bytes
 //    on (K-group stride), the next 8 channels one chunk (2 KB) on.
-//  - B = the input halo (3 x 18 x 10 voxels), N = (kw, kd, 8 input channels).
-//    One TMA box per 8-channel chunk, with the tensor map's dimensions ordered
-//    (c, h, d, w), lands as [w][d][h][8 ch]: for a fixed kh the nine (kw, kd)
-//    taps of a column are nine core matrices 288 bytes apart (d stride = 18 h
-//    rows; w stride = 3 d planes), so ONE descriptor covers all nine taps:
-//    N = 72 (9 x 8 channels) per MMA, and kh is a start-address shift.
-// So a brick costs 8 columns x 3 kh x 2 chunks = 48 MMAs of M x 72 x 16 into
-// six accumulator blocks that stay in TMEM for the CTA's whole brick range;
-// the epilogue reads them out once.  M is 64 for up to 64 output channels
-// (the rows beyond Cout read other shared memory of the stage and are
-// discarded) and 128 for 128 (N = 80 there, as M = 128 needs N % 16 == 0; the
-// spare group is discarded).  A pass covers two input-channel chunks (16
-// channels); the grid's y dimension takes the other passes.
+//  - B = the input halo (3 x 18 x 10 voxels) of two 8-channel chunks,
+//    N = (kw, chunk, kd, 8 channels).  One TMA box per brick, through a
+//    tensor map of one sample whose dimensions are ordered (8 channels, h, d,
+//    chunk, w), lands as [w][chunk][d][h][8 ch]: for a fixed kh the 18
+//    (kw, chunk, kd) groups of a column are 18 core matrices 288 bytes apart
+//    (d stride = 18 h rows, chunk stride = 3 d planes, w stride = 2 chunks),
+//    so ONE descriptor covers all nine taps of both chunks: N = 144 per MMA,
+//    and kh is a start-address shift.
+// So a brick costs 8 columns x 3 kh = 24 MMAs of M x 144 x 16 into three
+// accumulator blocks (432 TMEM columns) that stay in TMEM for the CTA's
+// whole brick range; the epilogue reads them out once.  M is 64 for up to 64
+// output channels (the rows beyond Cout read other shared memory of the
+// stage and are discarded) and 128 for 128.  A pass covers two input-channel
+// chunks (16 channels); the grid's y dimension takes the other passes.
 //
 // Warp roles: warp 0 issues the TMA loads into a ring of stages, warp 1 the
 // MMAs (one thread), warps 2-5 the bias gradient (sum of dZ per channel, from
@@ -30,6 +31,8 @@
 // partials go to scratch and are summed in a fixed order by a reduction
 // kernel, so gradients are bitwise reproducible.  Every wait is bounded in
 // time; TMEM is always released.
+#include <cstring>
+
 #include "../../include/trapbec_surrogate.h"
 #include "sg_tc_common.cuh"
 
@@ -40,22 +43,23 @@ using namespace tcc;
 
 constexpr int BH = 16, BW = 8;                  // brick: 16 h x 8 w voxels (one d plane)
 constexpr int XD = 3, XH = BH + 2, XW = BW + 2;
-constexpr int XCHUNK = XD * XH * XW * 16;       // 8640 bytes: one 8-channel chunk of the halo
-constexpr int XCHUNK_PAD = 8704;                // 128-byte multiple
+constexpr int XBOX = 2 * XD * XH * XW * 16;     // 17280 bytes: the halo of two 8-channel chunks
+constexpr int XBOX_PAD = 17408;                 // 128-byte multiple
 constexpr int ZCHUNK = BH * BW * 16;            // 2048 bytes: one 8-channel chunk of dZ
 constexpr int NTHR = 192;
-constexpr int NG = 9;                           // (kw, kd) groups of one MMA
+constexpr int NG = 18;                          // (kw, chunk, kd) groups of one MMA
+constexpr int NMMA = NG * 8;                    // N = 144
+constexpr int MAXB = 8;                         // samples per launch (one halo tensor map each)
 
 __device__ int g_timeout = 0;
 
 template <int CIN, int COUT> struct Cfg {
   static constexpr int KCO = COUT / 8;
   static constexpr int M = COUT > 64 ? 128 : 64;
-  static constexpr int NMMA = M == 128 ? 80 : 72;
-  static constexpr int ACC_COLS = 6 * NMMA;     // blocks (kh, chunk): 432 or 480 of 512 columns
+  static constexpr int ACC_COLS = 3 * NMMA;     // blocks kh = 0..2: 432 of 512 columns
   static constexpr int Z_BYTES = KCO * ZCHUNK;
-  static constexpr int STAGE = Z_BYTES + 2 * XCHUNK_PAD;
-  static constexpr int TAIL = 1024;             // read slack after the last stage (spare N group)
+  static constexpr int STAGE = Z_BYTES + XBOX_PAD;
+  static constexpr int TAIL = 1024;
   static constexpr int NS = (4 * STAGE + TAIL + 1024 <= 220 * 1024) ? 4 : 3;
   static constexpr int BAR_OFF = NS * STAGE + TAIL;
   static constexpr int RED_OFF = BAR_OFF + 256;
@@ -72,9 +76,14 @@ struct Args {
   int B, D, H, W;
 };
 
+// the halo tensor maps, one per sample
+struct XMaps {
+  CUtensorMap m[MAXB];
+};
+
 template <int CIN, int COUT>
 __global__ void __launch_bounds__(NTHR, 1)
-    conv3_wgrad_tc_kernel(const __grid_constant__ CUtensorMap tmx, const __grid_constant__ CUtensorMap tmz, Args a) {
+    conv3_wgrad_tc_kernel(const __grid_constant__ XMaps tmx, const __grid_constant__ CUtensorMap tmz, Args a) {
   using C = Cfg<CIN, COUT>;
   constexpr int NS = C::NS;
   extern __shared__ __align__(1024) unsigned char smem[];
@@ -119,12 +128,10 @@ __global__ void __launch_bounds__(NTHR, 1)
         const int bh = (int)(r % nbh); r /= nbh;
         const int d = (int)(r % a.D), b = (int)(r / a.D);
         const uint32_t st = s0 + s * C::STAGE;
-        bar_expect_tx(full0 + 8 * s, (uint32_t)(C::Z_BYTES + 2 * XCHUNK));
+        bar_expect_tx(full0 + 8 * s, (uint32_t)(C::Z_BYTES + XBOX));
         for (int kc = 0; kc < C::KCO; ++kc)
           tma_load_5d(st + kc * ZCHUNK, &tmz, kc * 8, bh * BH, bw * BW, d, b, full0 + 8 * s);
-        for (int c = 0; c < 2; ++c)
-          tma_load_5d(st + C::Z_BYTES + c * XCHUNK_PAD, &tmx, (2 * pass + c) * 8, bh * BH - 1, d - 1, bw * BW - 1, b,
-                      full0 + 8 * s);
+        tma_load_5d(st + C::Z_BYTES, &tmx.m[b], 0, bh * BH - 1, d - 1, 2 * pass, bw * BW - 1, full0 + 8 * s);
       }
       // let the last loads land before the CTA can end
       for (int j = nmine - NS > 0 ? nmine - NS : 0; j < nmine; ++j)
@@ -133,7 +140,7 @@ __global__ void __launch_bounds__(NTHR, 1)
   } else if (warp == 1) {
     // ---- MMA issuer -------------------------------------------------------------------
     if (lane == 0) {
-      constexpr uint32_t IDESC = idesc_bf16(C::M, C::NMMA, 1, 1);
+      constexpr uint32_t IDESC = idesc_bf16(C::M, NMMA, 1, 1);
       for (int j = 0; j < nmine && ok; ++j) {
         const int s = j % NS;
         ok = bar_wait(full0 + 8 * s, (uint32_t)((j / NS) & 1));
@@ -142,19 +149,17 @@ __global__ void __launch_bounds__(NTHR, 1)
         const uint32_t st = s0 + s * C::STAGE;
         // A: dZ column w; K groups (8 h rows) 128 bytes apart, M groups (8 channels) one chunk apart
         const uint64_t ad0 = sdesc(st, 128, ZCHUNK);
-        // B: halo rows; K groups 128 bytes apart, N groups (the (kw, kd) taps) 18 h rows = one d step apart
+        // B: halo rows; K groups 128 bytes apart, N groups (kw, chunk, kd) 18 h rows = one d step apart
         const uint64_t bd0 = sdesc(st + C::Z_BYTES, 128, XH * 16);
 #pragma unroll
         for (int w = 0; w < BW; ++w) {
           const uint64_t ad = ad0 + (uint64_t)(w * BH);   // start address in 16-byte units
 #pragma unroll
-          for (int kh = 0; kh < 3; ++kh)
-#pragma unroll
-            for (int c = 0; c < 2; ++c) {
-              const uint64_t bd = bd0 + (uint64_t)(c * (XCHUNK_PAD / 16) + w * XD * XH + kh);
-              const uint32_t acc = (j | w) ? 1u : 0u;
-              mma_bf16_ss(taddr + (uint32_t)((kh * 2 + c) * C::NMMA), ad, bd, IDESC, acc);
-            }
+          for (int kh = 0; kh < 3; ++kh) {
+            const uint64_t bd = bd0 + (uint64_t)(w * 2 * XD * XH + kh);
+            const uint32_t acc = (j | w) ? 1u : 0u;
+            mma_bf16_ss(taddr + (uint32_t)(kh * NMMA), ad, bd, IDESC, acc);
+          }
         }
         mma_commit(empty0 + 8 * s);   // the stage is free once these MMAs are done
       }
@@ -200,15 +205,14 @@ __global__ void __launch_bounds__(NTHR, 1)
       const bool mine = row >= 0 && row < COUT;
       float* out = a.part + (size_t)blockIdx.x * 27 * COUT * CIN;
 #pragma unroll 1
-      for (int blk = 0; blk < 6; ++blk) {
-        const int kh = blk >> 1, c = blk & 1;
+      for (int kh = 0; kh < 3; ++kh) {
 #pragma unroll 1
         for (int g = 0; g < NG; ++g) {
           uint32_t r[8];
-          tmem_ld8(taddr + ((uint32_t)(q * 32) << 16) + (uint32_t)(blk * C::NMMA + g * 8), r);
+          tmem_ld8(taddr + ((uint32_t)(q * 32) << 16) + (uint32_t)(kh * NMMA + g * 8), r);
           tmem_wait_ld();
           if (mine) {
-            const int kw = g / 3, kd = g % 3;
+            const int kw = g / 6, c = (g / 3) & 1, kd = g % 3;
             const int tap = (kd * 3 + kh) * 3 + kw;
             float4* o = (float4*)(out + ((size_t)tap * COUT + row) * CIN + (2 * pass + c) * 8);
             o[0] = make_float4(__uint_as_float(r[0]), __uint_as_float(r[1]), __uint_as_float(r[2]),
@@ -228,21 +232,27 @@ __global__ void __launch_bounds__(NTHR, 1)
   if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(512));
 }
 
-// out[i] = sum of the CTAs' partials in CTA order; the loads of eight CTAs
-// are issued together (one memory latency per eight, same summation order)
-__global__ void reduce_parts_kernel(const float* part, int nchunk, size_t n, float* out) {
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+// out[i] = sum of the CTAs' partials in CTA order, for the weights (i < nw)
+// and then the biases (nb more, from part_b); the loads of eight CTAs are
+// issued together (one memory latency per eight, same summation order)
+__global__ void reduce_parts_kernel(const float* part, const float* part_b, int nchunk, size_t nw, size_t nb,
+                                    float* out_w, float* out_b) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < nw + nb; i += (size_t)gridDim.x * blockDim.x) {
+    const bool w = i < nw;
+    const float* p = w ? part + i : part_b + (i - nw);
+    const size_t n = w ? nw : nb;
     float s = 0.f;
     int c = 0;
     for (; c + 8 <= nchunk; c += 8) {
       float v[8];
 #pragma unroll
-      for (int j = 0; j < 8; ++j) v[j] = part[(size_t)(c + j) * n + i];
+      for (int j = 0; j < 8; ++j) v[j] = p[(size_t)(c + j) * n];
 #pragma unroll
       for (int j = 0; j < 8; ++j) s += v[j];
     }
-    for (; c < nchunk; ++c) s += part[(size_t)c * n + i];
-    out[i] = s;
+    for (; c < nchunk; ++c) s += p[(size_t)c * n];
+    if (w) out_w[i] = s;
+    else out_b[i - nw] = s;
   }
 }
 
@@ -282,16 +292,20 @@ int launch(const bf16* x, const bf16* dz, int B, int D, int H, int W, float* dw,
   }
   auto enc = encoder();
   if (!enc) return TBSG_ERR_CUDA;
-  CUtensorMap tmx, tmz;
-  {  // X [B][D][H][W][CIN] seen as (c, h, d, w, b): boxes land [w][d][h][8 ch]
-    cuuint64_t dims[5] = {(cuuint64_t)CIN, (cuuint64_t)H, (cuuint64_t)D, (cuuint64_t)W, (cuuint64_t)B};
-    cuuint64_t strides[4] = {(cuuint64_t)W * CIN * 2, (cuuint64_t)H * W * CIN * 2, (cuuint64_t)CIN * 2,
-                             (cuuint64_t)D * H * W * CIN * 2};
-    cuuint32_t box[5] = {8, (cuuint32_t)XH, (cuuint32_t)XD, (cuuint32_t)XW, 1};
+  XMaps tmx;
+  CUtensorMap tmz;
+  std::memset(&tmx, 0, sizeof(tmx));
+  for (int b = 0; b < B; ++b) {
+    // sample b of X [B][D][H][W][CIN] seen as (8 channels, h, d, chunk, w): a box of two chunks lands
+    // [w][chunk][d][h][8 ch]
+    const bf16* xb = x + (size_t)b * D * H * W * CIN;
+    cuuint64_t dims[5] = {8, (cuuint64_t)H, (cuuint64_t)D, (cuuint64_t)(CIN / 8), (cuuint64_t)W};
+    cuuint64_t strides[4] = {(cuuint64_t)W * CIN * 2, (cuuint64_t)H * W * CIN * 2, 16, (cuuint64_t)CIN * 2};
+    cuuint32_t box[5] = {8, (cuuint32_t)XH, (cuuint32_t)XD, 2, (cuuint32_t)XW};
     cuuint32_t es[5] = {1, 1, 1, 1, 1};
-    if (enc(&tmx, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, (void*)x, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
-            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) !=
-        CUDA_SUCCESS)
+    if (enc(&tmx.m[b], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, (void*)xb, dims, strides, box, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
       return TBSG_ERR_ARG;
   }
   {  // dZ [B][D][H][W][COUT] seen as (c, h, w, d, b): boxes land [w][h][8 ch]
@@ -311,9 +325,8 @@ int launch(const bf16* x, const bf16* dz, int B, int D, int H, int W, float* dw,
   a.part_b = db ? scratch + (size_t)nch * 27 * COUT * CIN : nullptr;
   a.B = B; a.D = D; a.H = H; a.W = W;
   conv3_wgrad_tc_kernel<CIN, COUT><<<dim3(nch, CIN / 16, 1), NTHR, SMEM, st>>>(tmx, tmz, a);
-  const size_t nw = (size_t)27 * COUT * CIN;
-  reduce_parts_kernel<<<(int)((nw + 255) / 256), 256, 0, st>>>(a.part, nch, nw, dw);
-  if (db) reduce_parts_kernel<<<1, 256, 0, st>>>(a.part_b, nch, COUT, db);
+  const size_t nw = (size_t)27 * COUT * CIN, nb = db ? (size_t)COUT : 0;
+  reduce_parts_kernel<<<(int)((nw + nb + 255) / 256), 256, 0, st>>>(a.part, a.part_b, nch, nw, nb, dw, db);
   return cudaGetLastError() == cudaSuccess ? TBSG_OK : TBSG_ERR_CUDA;
 }
 
@@ -328,6 +341,7 @@ size_t wgrad_tc_scratch_bytes(int cin, int cout, int batch, int D, int H, int W)
 int wgrad_tc(const void* x, int cin, const void* dz, int cout, int batch, int D, int H, int W, float* dw, float* db,
              void* scratch, cudaStream_t st) {
   if ((uintptr_t)x % 16 || (uintptr_t)dz % 16 || (uintptr_t)scratch % 16) return TBSG_ERR_SHAPE;
+  if (batch > wtc::MAXB) return TBSG_ERR_SHAPE;   // the mma.sync kernel takes larger batches
   const bf16* xb = (const bf16*)x;
   const bf16* zb = (const bf16*)dz;
   float* s = (float*)scratch;
