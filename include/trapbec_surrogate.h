@@ -61,7 +61,9 @@ int tbsg_tc_status(int* timed_out);
 /* Weight and bias gradients of a 3x3x3 convolution:
  *  dw[tap][co][ci] = sum_{b,v} dz[b][v][co] x[b][v + tap][ci],  db[co] = sum dz[.][co]
  * (db optional).  Deterministic: per-chunk partials in `scratch` (at least
- * tbsg_conv3_wgrad_scratch_bytes bytes) reduced in a fixed order.           */
+ * tbsg_conv3_wgrad_scratch_bytes bytes) reduced in a fixed order.  The
+ * tensor-core kernel takes batches of up to 8 (one halo tensor map per
+ * sample); larger batches run on the mma.sync kernel.                      */
 size_t tbsg_conv3_wgrad_scratch_bytes(int cin, int cout, int batch, int D, int H, int W);
 int tbsg_conv3_wgrad(const void* x, int cin, const void* dz, int cout, int batch, int D, int H, int W,
                      float* dw, float* db, void* scratch, size_t scratch_bytes, void* stream);

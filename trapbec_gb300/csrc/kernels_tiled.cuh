@@ -642,6 +642,15 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
 
     const size_t plane_stride = (size_t)ny * nz;
     size_t rowbase = ((size_t)xa * ny + (y0 + yg * R)) * nz + gz;
+    // compensated state: the remainders of the next plane, loaded one plane
+    // ahead (streaming: each is read once) so that a plane's compute hides
+    // their latency
+    V lo_nx[COMP ? R : 1];
+    if constexpr (COMP) {
+#pragma unroll
+      for (int r = 0; r < R; ++r)
+        lo_nx[r] = (xa < xb && zok && yok[r]) ? __ldcs(a.lo + rowbase + (size_t)r * nz) : mk<T>((T)0, (T)0);
+    }
     // x / (60 hy) and the x part of the trap, loaded one plane ahead
     T xnext = a.xx[xa] * a.iy1;
     T pnext = harm ? a.px[xa] : (T)0;
@@ -657,13 +666,18 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
         tv[r] = (T)0;
         if (GEN && a.pot_mode == POT_ARR && store && zok && yok[r]) tv[r] = a.trap[rowbase + (size_t)r * nz];
       }
-      // compensated state: this plane's remainders, loaded now and used by the
-      // update at the end of the plane (streaming: each is read once)
+      // compensated state: this plane's remainders (loaded during the previous
+      // plane), used by the update at the end of the plane; the next plane's
+      // are requested now
       V lov[COMP ? R : 1];
       if constexpr (COMP) {
+        const bool nstore = x + 1 < xb;
 #pragma unroll
-        for (int r = 0; r < R; ++r)
-          lov[r] = (store && zok && yok[r]) ? __ldcs(a.lo + rowbase + (size_t)r * nz) : mk<T>((T)0, (T)0);
+        for (int r = 0; r < R; ++r) {
+          lov[r] = lo_nx[r];
+          lo_nx[r] = (nstore && zok && yok[r]) ? __ldcs(a.lo + rowbase + plane_stride + (size_t)r * nz)
+                                               : mk<T>((T)0, (T)0);
+        }
       }
       const V xv1 = splat<T>(xnext);
       const T pxv = pnext;

@@ -45,12 +45,15 @@ template <int CIN, int COUT> struct Cfg {
   static constexpr int WSLICE = KC * N * 16;                // one tap's weights of one unit
   static constexpr int NSH = (2 * HALO + 4 * WSLICE + 1024 <= SMEM_BUDGET) ? 2 : 1;
   static constexpr int NSW_FIT = (SMEM_BUDGET - NSH * HALO - 1024) / WSLICE;
-  static constexpr int NSW = NSW_FIT > 8 ? 8 : NSW_FIT;
+  static constexpr int NSW = NSW_FIT > 32 ? 32 : NSW_FIT;   // as deep as fits: the slices come from L2
   static constexpr int W_OFF = NSH * HALO;
   static constexpr int BAR_OFF = W_OFF + NSW * WSLICE;
-  static constexpr int SMEM = BAR_OFF + 256;
+  // hfull/hempty[NSH], wfull/wempty[NSW], afull/aempty[2], then the TMEM address
+  static constexpr int NBAR = 2 * NSH + 2 * NSW + 4;
+  static constexpr int SMEM = BAR_OFF + (NBAR * 8 + 4 + 127) / 128 * 128;
   static constexpr uint32_t TMEM_COLS = 2 * N < 32 ? 32 : 2 * N;
   static_assert(NSW >= 2, "weight ring");
+  static_assert(SMEM <= SMEM_BUDGET, "shared memory of one CTA");
   static_assert(COUT % N == 0 && N % 16 == 0, "output blocks");
 };
 
