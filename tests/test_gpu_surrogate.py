@@ -113,6 +113,34 @@ def test_conv3_forward_and_gradients(cin, cout, conv_path):
     assert torch.equal(dw, dw2)
 
 
+@pytest.mark.parametrize("cin,cout", [(32, 64), (64, 32), (64, 64), (64, 128), (128, 64), (128, 128)])
+def test_streamed_weight_kernel_two_brick_units(cin, cout):
+    """The 64/128-channel tensor-core kernel on a grid with enough bricks for
+    units of two bricks sharing each weight slice (partial bricks in h and w,
+    a pair whose second brick lies outside the grid): forward against the
+    oracle, and the fused input-gradient epilogue bit for bit against the
+    two-step result."""
+    lib = abi.load()
+    assert lib.tbsg_set_conv_path(0) == 0
+    rng = np.random.default_rng(cin + 7 * cout)
+    B, D, H, W = 2, 20, 20, 20      # 160 two-brick units (>= the SM count)
+    xb = _bf(rng.normal(size=(B, D, H, W, cin)))
+    wb = _bf(rng.normal(size=(27, cout, cin)) / np.sqrt(27 * cin))
+    st = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    yf = torch.empty((B, D, H, W, cout), dtype=torch.float32, device="cuda")
+    assert lib.tbsg_conv3_fwd(_p(xb), cin, _p(wb), None, None, None, _p(yf), 0, cout, B, D, H, W, 0, 0.0, st) == 0
+    ref = nn_oracle.conv3(xb.double().cpu(), wb.double().cpu())
+    assert (yf.double().cpu() - ref).abs().max() <= 1e-5 * ref.abs().max()
+    yact = _bf(rng.normal(size=(B, D, H, W, cout)))
+    dz_ref = torch.empty((B, D, H, W, cout), dtype=torch.bfloat16, device="cuda")
+    assert lib.tbsg_act_bwd(_p(yf), _p(yact), _p(dz_ref), None, yf.numel(), 0.05, st) == 0
+    dz = torch.empty_like(dz_ref)
+    assert lib.tbsg_conv3_dgrad_act(_p(xb), cin, _p(wb), _p(yact), _p(dz), None, cout, B, D, H, W, 0.05, st) == 0
+    assert torch.equal(dz.view(torch.int16), dz_ref.view(torch.int16))
+    flag = C.c_int(-1)
+    assert lib.tbsg_tc_status(C.byref(flag)) == 0 and flag.value == 0
+
+
 def test_unsupported_pair_is_an_error():
     lib = abi.load()
     x = torch.zeros(16 * 8, dtype=torch.bfloat16, device="cuda")
