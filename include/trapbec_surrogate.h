@@ -96,6 +96,23 @@ size_t tbsg_head_partials(size_t nvox, int c);
 int tbsg_head_loss(const void* feat, int c, const float* wh, const float* bh, const float* base,
                    const float* target, size_t nvox, float* dfeat, float* partials, float* out, void* stream);
 
+/* The activation-gradient fusions of the backward pass (act' = 1 where y > 0,
+ * else slope; y the leaky ReLU's BF16 output; results equal, bit for bit, to
+ * the unfused kernel followed by tbsg_act_bwd, without the FP32 gradient in
+ * memory; pointers 16-byte aligned, c a multiple of 8):
+ *  tbsg_head_loss_act: tbsg_head_loss for 16 feature channels, writing
+ *    dz = BF16(d loss / d feat * act'(feat)) instead of d loss / d feat;
+ *  tbsg_pool2_bwd_act: dz = BF16((g + up(dy) / 8) * act'(y)) on the fine grid
+ *    (D, H, W fine; g the fine gradient so far, dy the coarse one);
+ *  tbsg_up2_bwd_act: dz = BF16(sum of the 8 fine gradients * act'(y)) on the
+ *    coarse grid (D, H, W coarse).                                          */
+int tbsg_head_loss_act(const void* feat, const float* wh, const float* bh, const float* base, const float* target,
+                       size_t nvox, void* dz, float slope, float* partials, float* out, void* stream);
+int tbsg_pool2_bwd_act(const float* dy, const float* g, const void* y, void* dz, int c, int batch, int D, int H, int W,
+                       float slope, void* stream);
+int tbsg_up2_bwd_act(const float* dy, const void* y, void* dz, int c, int batch, int D, int H, int W, float slope,
+                     void* stream);
+
 /* Adam with decoupled weight decay on FP32 parameters (step t >= 1); the
  * gradient is multiplied by grad_scale[0] (device scalar, e.g. a clipping
  * factor from tbsg_clip_scale; NULL = 1).                                  */

@@ -201,6 +201,31 @@ def test_pool_up_act_head_adam():
     assert (o[1:NFEAT + 1] - whr.grad).abs().max() <= 1e-5 * whr.grad.abs().max()
     assert abs(o[NFEAT + 1] - bhr.grad[0]) <= 1e-5 * abs(bhr.grad[0]) + 1e-7
     assert (dfeat.double().cpu() - fr.grad).abs().max() <= 1e-5 * fr.grad.abs().max()
+    # the activation-gradient fusions: bit for bit the gradient kernel followed by act_bwd
+    dzf = torch.empty((n, NFEAT), dtype=torch.bfloat16, device="cuda")
+    dzr = torch.empty_like(dzf)
+    out2 = torch.empty_like(out)
+    assert lib.tbsg_act_bwd(_p(dfeat), _p(feat), _p(dzr), None, dfeat.numel(), 0.05, st) == 0
+    assert lib.tbsg_head_loss_act(_p(feat), _p(wh), _p(bh), _p(base), _p(tgt), n, _p(dzf), 0.05, _p(part),
+                                  _p(out2), st) == 0
+    assert torch.equal(dzf.view(torch.int16), dzr.view(torch.int16)) and torch.equal(out2, out)
+    yf_ = _bf(rng.normal(size=(B, D, D, D, c)))
+    gfine = torch.tensor(rng.normal(size=(B, D, D, D, c)), dtype=torch.float32, device="cuda")
+    acc = gfine.clone()
+    assert lib.tbsg_pool2_bwd(_p(gc), _p(acc), c, B, D, D, D, st) == 0
+    dzr = torch.empty((B, D, D, D, c), dtype=torch.bfloat16, device="cuda")
+    assert lib.tbsg_act_bwd(_p(acc), _p(yf_), _p(dzr), None, acc.numel(), 0.05, st) == 0
+    dzp = torch.empty_like(dzr)
+    assert lib.tbsg_pool2_bwd_act(_p(gc), _p(gfine), _p(yf_), _p(dzp), c, B, D, D, D, 0.05, st) == 0
+    assert torch.equal(dzp.view(torch.int16), dzr.view(torch.int16))
+    yc_ = _bf(rng.normal(size=(B, D // 2, D // 2, D // 2, c)))
+    gcs = torch.empty((B, D // 2, D // 2, D // 2, c), dtype=torch.float32, device="cuda")
+    assert lib.tbsg_up2_bwd(_p(g), _p(gcs), c, B, D // 2, D // 2, D // 2, st) == 0
+    dzr = torch.empty((B, D // 2, D // 2, D // 2, c), dtype=torch.bfloat16, device="cuda")
+    assert lib.tbsg_act_bwd(_p(gcs), _p(yc_), _p(dzr), None, gcs.numel(), 0.05, st) == 0
+    dzu = torch.empty_like(dzr)
+    assert lib.tbsg_up2_bwd_act(_p(g), _p(yc_), _p(dzu), c, B, D // 2, D // 2, D // 2, 0.05, st) == 0
+    assert torch.equal(dzu.view(torch.int16), dzr.view(torch.int16))
     # Adam
     p0 = torch.tensor(rng.normal(size=100), dtype=torch.float32, device="cuda")
     gr = torch.tensor(rng.normal(size=100), dtype=torch.float32, device="cuda")

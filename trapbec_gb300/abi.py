@@ -196,6 +196,10 @@ _PROTOS = {
     "tbsg_head_fwd": (C.c_int, [_VP, C.c_int, _VP, _VP, _VP, _VP, C.c_size_t, _VP]),
     "tbsg_head_partials": (C.c_size_t, [C.c_size_t, C.c_int]),
     "tbsg_head_loss": (C.c_int, [_VP, C.c_int, _VP, _VP, _VP, _VP, C.c_size_t, _VP, _VP, _VP, _VP]),
+    "tbsg_head_loss_act": (C.c_int, [_VP, _VP, _VP, _VP, _VP, C.c_size_t, _VP, C.c_float, _VP, _VP, _VP]),
+    "tbsg_pool2_bwd_act": (C.c_int, [_VP, _VP, _VP, _VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float,
+                                     _VP]),
+    "tbsg_up2_bwd_act": (C.c_int, [_VP, _VP, _VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float, _VP]),
     "tbsg_adam": (C.c_int, [_VP, _VP, _VP, _VP, C.c_size_t, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float,
                             C.c_int, _VP, _VP]),
     "tbsg_clip_scale": (C.c_int, [_VP, C.c_size_t, C.c_float, _VP, _VP, _VP]),

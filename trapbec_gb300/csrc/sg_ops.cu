@@ -178,6 +178,73 @@ __global__ void up2_bwd_kernel(const float* dy, float* dx, int c, int B, int D, 
   }
 }
 
+// The activation-gradient fusions of the backward pass: the same operations,
+// in the same order, as the gradient kernel followed by act_bwd, without the
+// FP32 gradient in memory.  dz = BF16(g * act'(y)), act' = 1 where y > 0,
+// else slope, for 8 channels of one voxel.
+__device__ __forceinline__ uint4 act_dz8(const float g[8], const uint4 yu, float slope) {
+  const bf16* ye = (const bf16*)&yu;
+  uint4 o;
+  bf16* oe = (bf16*)&o;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) oe[k] = __float2bfloat16_rn(g[k] * (__bfloat162float(ye[k]) > 0.f ? 1.f : slope));
+  return o;
+}
+
+// pooling gradient + activation: one thread per coarse voxel x 8 channels;
+// each of its 8 fine voxels takes g = g_fine + dy / 8, then dz_fine
+__global__ void pool2_bwd_act8_kernel(const float* dy, const float* gf, const bf16* y, bf16* dz, int c, int B, int D,
+                                      int H, int W, float slope) {
+  const int Dc = D / 2, Hc = H / 2, Wc = W / 2, c8 = c / 8;
+  const size_t n = (size_t)B * Dc * Hc * Wc * c8;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int cc = (int)(i % c8);
+    size_t r = i / c8;
+    const int w = (int)(r % Wc); r /= Wc;
+    const int h = (int)(r % Hc); r /= Hc;
+    const int d = (int)(r % Dc);
+    const size_t b = r / Dc;
+    const float4 a0 = *(const float4*)(dy + i * 8), a1 = *(const float4*)(dy + i * 8 + 4);
+    const float q[8] = {0.125f * a0.x, 0.125f * a0.y, 0.125f * a0.z, 0.125f * a0.w,
+                        0.125f * a1.x, 0.125f * a1.y, 0.125f * a1.z, 0.125f * a1.w};
+#pragma unroll
+    for (int o = 0; o < 8; ++o) {
+      const int fd = 2 * d + (o >> 2), fh = 2 * h + ((o >> 1) & 1), fw = 2 * w + (o & 1);
+      const size_t f = (((b * D + fd) * H + fh) * W + fw) * c + cc * 8;
+      const float4 g0 = *(const float4*)(gf + f), g1 = *(const float4*)(gf + f + 4);
+      const float g[8] = {g0.x + q[0], g0.y + q[1], g0.z + q[2], g0.w + q[3],
+                          g1.x + q[4], g1.y + q[5], g1.z + q[6], g1.w + q[7]};
+      *(uint4*)(dz + f) = act_dz8(g, *(const uint4*)(y + f), slope);
+    }
+  }
+}
+
+// upsampling gradient + activation: one thread per coarse voxel x 8 channels:
+// g = the sum of its 8 fine gradients (in fine-voxel order), then dz_coarse
+__global__ void up2_bwd_act8_kernel(const float* dy, const bf16* y, bf16* dz, int c, int B, int D, int H, int W,
+                                    float slope) {
+  const int Hf = 2 * H, Wf = 2 * W, Df = 2 * D, c8 = c / 8;
+  const size_t n = (size_t)B * D * H * W * c8;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int cc = (int)(i % c8);
+    size_t r = i / c8;
+    const int w = (int)(r % W); r /= W;
+    const int h = (int)(r % H); r /= H;
+    const int d = (int)(r % D);
+    const size_t b = r / D;
+    float g[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int o = 0; o < 8; ++o) {
+      const int fd = 2 * d + (o >> 2), fh = 2 * h + ((o >> 1) & 1), fw = 2 * w + (o & 1);
+      const float* src = dy + (((b * Df + fd) * Hf + fh) * Wf + fw) * c + cc * 8;
+      const float4 t0 = *(const float4*)src, t1 = *(const float4*)(src + 4);
+      g[0] += t0.x; g[1] += t0.y; g[2] += t0.z; g[3] += t0.w;
+      g[4] += t1.x; g[5] += t1.y; g[6] += t1.z; g[7] += t1.w;
+    }
+    *(uint4*)(dz + i * 8) = act_dz8(g, *(const uint4*)(y + i * 8), slope);
+  }
+}
+
 constexpr int HEAD_THREADS = 256;
 constexpr int HEAD_BLOCKS = 1024;
 
@@ -241,9 +308,11 @@ __global__ void head_fwd16_kernel(const uint4* feat, const float* wh, const floa
   }
 }
 
+template <bool ACT>
 __global__ void __launch_bounds__(HEAD_THREADS) head_loss16_kernel(const uint4* feat, const float* wh, const float* bh,
                                                                    const float* base, const float* target, size_t nvox,
-                                                                   float4* dfeat, float* partials) {
+                                                                   float4* dfeat, uint4* dz, float slope,
+                                                                   float* partials) {
   constexpr int NP = 18;
   __shared__ float red[HEAD_THREADS * NP];
   float w[16], acc[NP];
@@ -269,9 +338,19 @@ __global__ void __launch_bounds__(HEAD_THREADS) head_loss16_kernel(const uint4* 
 #pragma unroll
     for (int k = 0; k < 16; ++k) acc[1 + k] += g * f[k];
     acc[17] += g;
+    if (ACT) {   // dz = BF16(d loss/d feat * act'(feat)): the head's input is a leaky ReLU's output
+      float t[8];
 #pragma unroll
-    for (int q = 0; q < 4; ++q)
-      dfeat[4 * v + q] = make_float4(g * w[4 * q], g * w[4 * q + 1], g * w[4 * q + 2], g * w[4 * q + 3]);
+      for (int k = 0; k < 8; ++k) t[k] = g * w[k];
+      dz[2 * v] = act_dz8(t, u0, slope);
+#pragma unroll
+      for (int k = 0; k < 8; ++k) t[k] = g * w[8 + k];
+      dz[2 * v + 1] = act_dz8(t, u1, slope);
+    } else {
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        dfeat[4 * v + q] = make_float4(g * w[4 * q], g * w[4 * q + 1], g * w[4 * q + 2], g * w[4 * q + 3]);
+    }
   }
 #pragma unroll
   for (int k = 0; k < NP; ++k) red[k * HEAD_THREADS + threadIdx.x] = acc[k];
@@ -480,12 +559,41 @@ int tbsg_head_loss(const void* feat, int c, const float* wh, const float* bh, co
   }
   cudaStream_t st = (cudaStream_t)stream;
   if (c == 16 && ((uintptr_t)feat | (uintptr_t)dfeat) % 16 == 0)
-    head_loss16_kernel<<<HEAD_BLOCKS, HEAD_THREADS, 0, st>>>((const uint4*)feat, wh, bh, base, target, nvox,
-                                                             (float4*)dfeat, partials);
+    head_loss16_kernel<false><<<HEAD_BLOCKS, HEAD_THREADS, 0, st>>>((const uint4*)feat, wh, bh, base, target, nvox,
+                                                                    (float4*)dfeat, nullptr, 0.f, partials);
   else
     head_loss_kernel<<<HEAD_BLOCKS, HEAD_THREADS, smem, st>>>((const bf16*)feat, c, wh, bh, base, target, nvox, dfeat,
                                                               partials);
   head_final_kernel<<<1, 256, 0, st>>>(partials, HEAD_BLOCKS, c + 2, out);
+  return done();
+}
+
+int tbsg_head_loss_act(const void* feat, const float* wh, const float* bh, const float* base, const float* target,
+                       size_t nvox, void* dz, float slope, float* partials, float* out, void* stream) {
+  if (!feat || !wh || !bh || !base || !target || !dz || !partials || !out) return TBSG_ERR_ARG;
+  if (((uintptr_t)feat | (uintptr_t)dz) % 16) return TBSG_ERR_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  head_loss16_kernel<true><<<HEAD_BLOCKS, HEAD_THREADS, 0, st>>>((const uint4*)feat, wh, bh, base, target, nvox,
+                                                                 nullptr, (uint4*)dz, slope, partials);
+  head_final_kernel<<<1, 256, 0, st>>>(partials, HEAD_BLOCKS, 16 + 2, out);
+  return done();
+}
+
+int tbsg_pool2_bwd_act(const float* dy, const float* g, const void* y, void* dz, int c, int batch, int D, int H, int W,
+                       float slope, void* stream) {
+  if (!dy || !g || !y || !dz || (D | H | W) & 1 || c % 8) return TBSG_ERR_ARG;
+  if (((uintptr_t)dy | (uintptr_t)g | (uintptr_t)y | (uintptr_t)dz) % 16) return TBSG_ERR_ARG;
+  pool2_bwd_act8_kernel<<<grid_for((size_t)batch * D * H * W * c / 64), 256, 0, (cudaStream_t)stream>>>(
+      dy, g, (const bf16*)y, (bf16*)dz, c, batch, D, H, W, slope);
+  return done();
+}
+
+int tbsg_up2_bwd_act(const float* dy, const void* y, void* dz, int c, int batch, int D, int H, int W, float slope,
+                     void* stream) {
+  if (!dy || !y || !dz || c % 8) return TBSG_ERR_ARG;
+  if (((uintptr_t)dy | (uintptr_t)y | (uintptr_t)dz) % 16) return TBSG_ERR_ARG;
+  up2_bwd_act8_kernel<<<grid_for((size_t)batch * D * H * W * c / 8), 256, 0, (cudaStream_t)stream>>>(
+      dy, (const bf16*)y, (bf16*)dz, c, batch, D, H, W, slope);
   return done();
 }
 

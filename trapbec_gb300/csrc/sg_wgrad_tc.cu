@@ -233,8 +233,9 @@ __global__ void __launch_bounds__(NTHR, 1)
 }
 
 // out[i] = sum of the CTAs' partials in CTA order, for the weights (i < nw)
-// and then the biases (nb more, from part_b); the loads of eight CTAs are
-// issued together (one memory latency per eight, same summation order)
+// and then the biases (nb more, from part_b); the loads of sixteen CTAs are
+// issued together (one memory latency per sixteen, same summation order),
+// and 64-thread blocks spread the outputs over more SMs
 __global__ void reduce_parts_kernel(const float* part, const float* part_b, int nchunk, size_t nw, size_t nb,
                                     float* out_w, float* out_b) {
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < nw + nb; i += (size_t)gridDim.x * blockDim.x) {
@@ -243,12 +244,12 @@ __global__ void reduce_parts_kernel(const float* part, const float* part_b, int 
     const size_t n = w ? nw : nb;
     float s = 0.f;
     int c = 0;
-    for (; c + 8 <= nchunk; c += 8) {
-      float v[8];
+    for (; c + 16 <= nchunk; c += 16) {
+      float v[16];
 #pragma unroll
-      for (int j = 0; j < 8; ++j) v[j] = p[(size_t)(c + j) * n];
+      for (int j = 0; j < 16; ++j) v[j] = p[(size_t)(c + j) * n];
 #pragma unroll
-      for (int j = 0; j < 8; ++j) s += v[j];
+      for (int j = 0; j < 16; ++j) s += v[j];
     }
     for (; c < nchunk; ++c) s += p[(size_t)c * n];
     if (w) out_w[i] = s;
@@ -326,7 +327,7 @@ int launch(const bf16* x, const bf16* dz, int B, int D, int H, int W, float* dw,
   a.B = B; a.D = D; a.H = H; a.W = W;
   conv3_wgrad_tc_kernel<CIN, COUT><<<dim3(nch, CIN / 16, 1), NTHR, SMEM, st>>>(tmx, tmz, a);
   const size_t nw = (size_t)27 * COUT * CIN, nb = db ? (size_t)COUT : 0;
-  reduce_parts_kernel<<<(int)((nw + nb + 255) / 256), 256, 0, st>>>(a.part, a.part_b, nch, nw, nb, dw, db);
+  reduce_parts_kernel<<<(int)((nw + nb + 63) / 64), 64, 0, st>>>(a.part, a.part_b, nch, nw, nb, dw, db);
   return cudaGetLastError() == cudaSuccess ? TBSG_OK : TBSG_ERR_CUDA;
 }
 

@@ -328,43 +328,45 @@ class Surrogate:
         return self.head_out[0:1]
 
     def _backward_fused(self, target):
+        """backward() with every activation derivative fused into the kernel
+        that forms the gradient it multiplies: the head's loss gradient, the
+        input gradients of the convolutions above an activation, the pooling
+        and the upsampling gradients."""
         A, G, S, L, dz, dz2 = self.A, self.G, self.S, self.lib, self.dz, self.dz2
         st = self._st()
         s0, s1, s2, s3 = S, S // 2, S // 4, S // 8
         h0, h1, _, _ = self.view["head"]
-        self._ck(L.tbsg_head_loss(self._ptr(A["d0"]), NFEAT, self._ptr(self.p[h0:h1]), self._ptr(self.p[h1:h1 + 1]),
-                                  self._ptr(self.base), self._ptr(target), self.amp.numel(), self._ptr(G["d0"]),
-                                  self._ptr(self.partials), self._ptr(self.head_out), st), "head_loss")
+        self._ck(L.tbsg_head_loss_act(self._ptr(A["d0"]), self._ptr(self.p[h0:h1]), self._ptr(self.p[h1:h1 + 1]),
+                                      self._ptr(self.base), self._ptr(target), self.amp.numel(), self._ptr(dz[0]),
+                                      SLOPE, self._ptr(self.partials), self._ptr(self.head_out), st), "head_loss_act")
         self.g[h0:h1 + 1].copy_(self.head_out[1:NFEAT + 2])
         for k in ("e0", "e1", "e2"):
             G[k].zero_()
         # decoder: level 0, 1, 2 (the skip gradients accumulate into e0, e1, e2)
-        for lev, D, (b, a_), yb, up, gnext, cn in ((0, s0, ("d0b", "d0a"), "d0", "u0", "d1", 32),
-                                                    (1, s1, ("d1b", "d1a"), "d1", "u1", "d2", 64),
-                                                    (2, s2, ("d2b", "d2a"), "d2", "u2", "e3", 128)):
-            self._act_bwd(G[yb], A[yb], dz[lev])
+        for lev, D, (b, a_), up, ynext, cn in ((0, s0, ("d0b", "d0a"), "u0", "d1", 32),
+                                               (1, s1, ("d1b", "d1a"), "u1", "d2", 64),
+                                               (2, s2, ("d2b", "d2a"), "u2", "e3", 128)):
             self._conv_bwd_act(b, A[a_], dz[lev], D, A[a_], dz2[lev], G["e%d" % lev])
             self._conv_bwd(a_, A[up], dz2[lev], D, G[up])
             Dc = D // 2
-            self._ck(L.tbsg_up2_bwd(self._ptr(G[up]), self._ptr(G[gnext]), cn, self.B, Dc, Dc, Dc, st), "up_bwd")
+            self._ck(L.tbsg_up2_bwd_act(self._ptr(G[up]), self._ptr(A[ynext]), self._ptr(dz[lev + 1]), cn, self.B,
+                                        Dc, Dc, Dc, SLOPE, st), "up_bwd_act")
         # bottleneck
-        self._act_bwd(G["e3"], A["e3"], dz[3])
         self._conv_bwd_act("e3c", A["e3b"], dz[3], s3, A["e3b"], dz2[3])
         self._conv_bwd_act("e3b", A["e3a"], dz2[3], s3, A["e3a"], dz[3])
         self._conv_bwd("e3a", A["p3"], dz[3], s3, G["p3"])
-        self._ck(L.tbsg_pool2_bwd(self._ptr(G["p3"]), self._ptr(G["e2"]), 64, self.B, s2, s2, s2, st), "pool_bwd")
+        self._ck(L.tbsg_pool2_bwd_act(self._ptr(G["p3"]), self._ptr(G["e2"]), self._ptr(A["e2"]), self._ptr(dz[2]), 64,
+                                      self.B, s2, s2, s2, SLOPE, st), "pool_bwd_act")
         # encoder: level 2, 1, 0
-        for lev, D, (b, a_), yb, pin, cin_ in ((2, s2, ("e2b", "e2a"), "e2", "p2", 32),
-                                               (1, s1, ("e1b", "e1a"), "e1", "p1", 16),
-                                               (0, s0, ("e0b", "e0a"), "e0", "x0", None)):
-            self._act_bwd(G[yb], A[yb], dz[lev])
+        for lev, D, (b, a_), pin, cfine in ((2, s2, ("e2b", "e2a"), "p2", 32), (1, s1, ("e1b", "e1a"), "p1", 16),
+                                            (0, s0, ("e0b", "e0a"), "x0", None)):
             self._conv_bwd_act(b, A[a_], dz[lev], D, A[a_], dz2[lev])
-            self._conv_bwd(a_, A[pin], dz2[lev], D, G[pin] if cin_ else None)
-            if cin_:
-                Dp = D
+            self._conv_bwd(a_, A[pin], dz2[lev], D, G[pin] if cfine else None)
+            if cfine:
                 fine = "e%d" % (lev - 1)
-                self._ck(L.tbsg_pool2_bwd(self._ptr(G[pin]), self._ptr(G[fine]), cin_, self.B, 2 * Dp, 2 * Dp, 2 * Dp,
-                                          st), "pool_bwd")
+                self._ck(L.tbsg_pool2_bwd_act(self._ptr(G[pin]), self._ptr(G[fine]), self._ptr(A[fine]),
+                                              self._ptr(dz[lev - 1]), cfine, self.B, 2 * D, 2 * D, 2 * D, SLOPE, st),
+                         "pool_bwd_act")
         return self.head_out[0:1]
 
     def adam_step(self, lr: float, beta1=0.9, beta2=0.999, eps=1e-8, weight_decay=0.0, max_norm: float = 1.0):
