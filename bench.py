@@ -289,6 +289,20 @@ def imag_leg(args):
                           "with the kinetic term in difference form; renormalisation, energy and stop test in FP64")}
 
 
+def ring_leg(args, peak):
+    """The 256^3 vortex-ring workload (TF background x a ring of radius 8 in
+    z = 0 with 1e-3 seeded phase noise, trap (0.05, 0.05, 0.1), g = 1,
+    dt = 0.005): 2000 RK3 steps in complex FP64 and in complex FP32 from the
+    same start; GB/s on algorithmic bytes, HBM fraction, and the FP32 run's
+    norm/energy drift and L2 error against the FP64 run."""
+    from trapbec_gb300 import reports
+    r = reports.fp32_vs_fp64(n=256, steps=args.ring_steps, chunk=250)
+    for k in ("fp32", "fp64"):
+        r[k]["hbm_frac"] = r[k]["gbs_alg"] / peak
+    r["workload"] = "vortex ring 256^3, FP64 and FP32 from the same start"
+    return r
+
+
 def warmstart_leg(args):
     """Imaginary-time relaxation to |d(E/N)| < tol at 128^3 from the
     surrogate's guess against the Thomas-Fermi + 1e-2 noise guess, on the
@@ -590,6 +604,8 @@ def run_gpu_arm(args):
         line["compensated"] = comp
     if fp64:
         line["fp64"] = fp64
+    if not args.no_ring and rank == 0 and world == 1:
+        line["ring256"] = ring_leg(args, peak)
     if not args.no_imag and rank == 0 and world == 1:
         line["imag"] = imag_leg(args)
     if rank == 0 and world == 1 and not args.no_warmstart:
@@ -625,6 +641,8 @@ def main():
     ap.add_argument("--stage-form", type=int, default=0, choices=[0, 1, 2],
                     help="real-time RK3 form of the timed run: 0 three full stages, 1 deferred psi1 "
                          "(stage 1 stores w1 only), 2 compensated state")
+    ap.add_argument("--no-ring", action="store_true", help="skip the 256^3 vortex-ring FP32/FP64 leg")
+    ap.add_argument("--ring-steps", type=int, default=2000)
     ap.add_argument("--no-imag", action="store_true", help="skip the batched imaginary-time leg")
     ap.add_argument("--imag-count", type=int, default=64)
     ap.add_argument("--imag-seed", type=int, default=3)
