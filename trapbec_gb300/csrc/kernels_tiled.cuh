@@ -645,7 +645,7 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
     // compensated state: the remainders of the next plane, loaded one plane
     // ahead (streaming: each is read once) so that a plane's compute hides
     // their latency
-    V lo_nx[COMP ? R : 1];
+    [[maybe_unused]] V lo_nx[COMP ? R : 1];
     if constexpr (COMP) {
 #pragma unroll
       for (int r = 0; r < R; ++r)
@@ -669,7 +669,7 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
       // compensated state: this plane's remainders (loaded during the previous
       // plane), used by the update at the end of the plane; the next plane's
       // are requested now
-      V lov[COMP ? R : 1];
+      [[maybe_unused]] V lov[COMP ? R : 1];
       if constexpr (COMP) {
         const bool nstore = x + 1 < xb;
 #pragma unroll
@@ -845,14 +845,31 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
       rowbase += plane_stride;
     };
 
-    for (int x = xa; x < xe; x += 7) {
-      body(std::integral_constant<int, 0>{}, x);
-      body(std::integral_constant<int, 1>{}, x + 1);
-      body(std::integral_constant<int, 2>{}, x + 2);
-      body(std::integral_constant<int, 3>{}, x + 3);
-      body(std::integral_constant<int, 4>{}, x + 4);
-      body(std::integral_constant<int, 5>{}, x + 5);
-      body(std::integral_constant<int, 6>{}, x + 6);
+    if constexpr (IMAG && BATCH) {
+      // The batched imaginary-time stages (energy and norm sums, per-segment
+      // arguments) are long; seven unrolled copies of them overflow the
+      // instruction cache (no_instruction was the top stall of a small
+      // batch's stage 1) and spilled registers, so they run one copy and shift
+      // the x queue by register moves (4 x 128^3: 274 -> 260 us per step;
+      // the single-grid loop at 512^3 was 2% faster unrolled).
+#pragma unroll 1
+      for (int x = xa; x < xe; ++x) {
+        body(std::integral_constant<int, 0>{}, x);
+#pragma unroll
+        for (int j = 0; j < 6; ++j)
+#pragma unroll
+          for (int r = 0; r < R; ++r) q[j][r] = q[j + 1][r];
+      }
+    } else {
+      for (int x = xa; x < xe; x += 7) {
+        body(std::integral_constant<int, 0>{}, x);
+        body(std::integral_constant<int, 1>{}, x + 1);
+        body(std::integral_constant<int, 2>{}, x + 2);
+        body(std::integral_constant<int, 3>{}, x + 3);
+        body(std::integral_constant<int, 4>{}, x + 4);
+        body(std::integral_constant<int, 5>{}, x + 5);
+        body(std::integral_constant<int, 6>{}, x + 6);
+      }
     }
     seq = base + (uint32_t)(xe - xa) + 6;
     failed = __syncthreads_or(failed) != 0;
