@@ -38,6 +38,18 @@ sys.path.insert(0, HERE)
 
 METRIC = "grid-pt updates/s at 512^3 FP32 vs FP64 (HBM %); imag-time wall to dE<1e-10: NN vs TF"
 UNIT = "grid-point updates/s"
+# Algorithmic HBM bytes per grid point and RK3 step of each real-time form
+# (complex FP32; FP64 doubles them): three stages S1 24 + S2 32 + S3 24; the
+# deferred form stores no psi1 (S1 16); the compensated state reads and
+# rewrites its remainder in every stage (+48); the psi-difference form stores
+# no w (S1 16 + S2 24 + S3 24).
+FORM_BYTES = {0: 80.0, 1: 72.0, 2: 128.0, 3: 64.0}
+FORM_PROFILE = {1: "deferred", 2: "compensated", 3: "psi_diff"}
+FORM_TEXT = {0: "three full stages",
+             1: "deferred psi1: stage 1 stores w1 only, stage 2 forms psi1 = psi0 + w1/3 (bit-identical)",
+             2: "compensated state (remainder array, difference-form stencil)",
+             3: ("psi difference: no w array; stage 1 stores psi1 only, stages 2 and 3 recover the previous "
+                 "stage's w as (psi_k - psi_(k-1)) / B_(k-1) from the two psi arrays")}
 
 
 def load_peaks():
@@ -417,13 +429,11 @@ def run_gpu_arm(args):
     # the deferred form stores no psi1 (S1 16 B); FP64 doubles every figure
     form_run = s.stage_form()
     deferred = form_run == abi.RK3_DEFERRED
-    bpc = {abi.RK3_THREE_STAGE: 80.0, abi.RK3_DEFERRED: 72.0, abi.RK3_COMPENSATED: 128.0}[form_run] \
-        if prec == abi.FP32 else 160.0
+    bpc = FORM_BYTES[form_run] * (1.0 if prec == abi.FP32 else 2.0)
     achieved = cells * args.steps * bpc / (ms * 1e-3) / 1e9
     tag = "fp32" if prec == abi.FP32 else "fp64"
     tz_run, ty_run = s.tile_shape(real_time=True)
-    tpp = profile_traffic(tag, tz_run, ty_run,
-                          form={abi.RK3_DEFERRED: "deferred", abi.RK3_COMPENSATED: "compensated"}.get(form_run, ""))
+    tpp = profile_traffic(tag, tz_run, ty_run, form=FORM_PROFILE.get(form_run, ""))
     traffic = tpp * cells if tpp else None
 
     kernel_name = "tiled TMA stage kernel" if args.kernel is None or args.kernel[0] != 1 else "per-cell stage kernel"
@@ -479,6 +489,7 @@ def run_gpu_arm(args):
     # also the FP64 throughput line.
     fp64 = None
     comp = None
+    other_forms = {}
     precision = None
     if not args.no_fp64 and prec == abi.FP32:
         import numpy as np
@@ -500,12 +511,15 @@ def run_gpu_arm(args):
             ms_, _ = timed_steps(sol, P, chunk, omega_of_step, 0)
             runs[form_tag] = (dstart, sol.diag(), sol.get_psi().astype(np.complex128), ms_)
 
-        s.set_stage_form(abi.RK3_THREE_STAGE)
-        run_form(s, "fp32")
-        s.set_stage_form(abi.RK3_COMPENSATED)
-        tune_c = None if args.no_autotune else s.autotune(steps=4)
-        run_form(s, "fp32_compensated")
-        tzc, tyc = s.tile_shape(real_time=True)
+        # every FP32 form from the same start, each on its own autotuned tile shape
+        form_runs = {}
+        for form, tag in ((abi.RK3_THREE_STAGE, "fp32"), (abi.RK3_COMPENSATED, "fp32_compensated"),
+                          (abi.RK3_PSI_DIFF, "fp32_psi_diff")):
+            s.set_stage_form(form)
+            tune_f = None if args.no_autotune or args.kernel else s.autotune(steps=4)
+            run_form(s, tag)
+            form_runs[form] = {"tag": tag, "autotune": tune_f, "tile": list(s.tile_shape(real_time=True)),
+                               "ran": s.stage_form() == form}
         s.close()
         prob64, _ = make_problem(n, abi.FP64)
         s64 = Solver(prob64.to_params())
@@ -535,17 +549,26 @@ def run_gpu_arm(args):
             "compared": "sum |psi|^2 and the energy's raw sums (no cell volume) after `steps` steps, FP32 / FP64 - 1; "
                         "L2 of psi relative to FP64; drifts relative to each run's own start",
             "fp32": versus("fp32"), "fp32_compensated": versus("fp32_compensated"),
+            "fp32_psi_diff": versus("fp32_psi_diff"),
+            "headline_form": {abi.RK3_THREE_STAGE: "fp32", abi.RK3_COMPENSATED: "fp32_compensated",
+                              abi.RK3_PSI_DIFF: "fp32_psi_diff"}.get(form_run),
             "fp64_drift": {"norm": d64e["norm"] / d64s["norm"] - 1.0, "energy": d64e["energy"] / d64s["energy"] - 1.0},
         }
-        msc = runs["fp32_compensated"][3]
-        vc = cells * P / (msc * 1e-3)
-        ach_c = cells * P * 128.0 / (msc * 1e-3) / 1e9
-        comp = {"value": vc, "unit": UNIT, "ms_per_step": msc / P, "tile": [tzc, tyc], "autotune": tune_c,
-                "roofline": {"bound": "hbm", "achieved": ach_c, "peak": peak, "unit": "GB/s", "frac": ach_c / peak,
-                             "algorithmic_bytes_per_point_step": 128.0,
-                             "traffic": (lambda t: t * cells if t else None)(
-                                 profile_traffic("fp32", tzc, tyc, form="compensated"))},
-                "note": "each stage also reads and rewrites the remainder array (48 B more per point and step)"}
+        def form_line(form):
+            fr = form_runs[form]
+            msf = runs[fr["tag"]][3]
+            ach_f = cells * P * FORM_BYTES[form] / (msf * 1e-3) / 1e9
+            return {"value": cells * P / (msf * 1e-3), "unit": UNIT, "ms_per_step": msf / P, "steps": P,
+                    "tile": fr["tile"], "autotune": fr["autotune"], "ran": fr["ran"],
+                    "roofline": {"bound": "hbm", "achieved": ach_f, "peak": peak, "unit": "GB/s",
+                                 "frac": ach_f / peak, "algorithmic_bytes_per_point_step": FORM_BYTES[form],
+                                 "traffic": (lambda t: t * cells if t else None)(
+                                     profile_traffic("fp32", *fr["tile"], form=FORM_PROFILE.get(form, "")))},
+                    "rk3_form": FORM_TEXT[form]}
+
+        comp = form_line(abi.RK3_COMPENSATED)
+        # the form of the timed run is the headline; the other plain forms are reported beside it
+        other_forms = {f: form_line(f) for f in (abi.RK3_THREE_STAGE, abi.RK3_PSI_DIFF) if f != form_run}
         v64 = cells * P / (ms64 * 1e-3)
         fma = fp64_fma_peak()
         fp64 = {"value": v64, "unit": UNIT, "ms_per_step": ms64 / P,
@@ -578,11 +601,7 @@ def run_gpu_arm(args):
                    "chunk_steps": chunk, "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2_flush": "inputs larger than L2 (1 GiB per array)",
                    "kernel": kernel_name, "tile": [tz_run, ty_run], "autotune": tune,
-                   "rk3_form": {abi.RK3_THREE_STAGE: "three full stages",
-                                abi.RK3_DEFERRED: ("deferred psi1: stage 1 stores w1 only, stage 2 forms psi1 = "
-                                                   "psi0 + w1/3 (bit-identical)"),
-                                abi.RK3_COMPENSATED: "compensated state (remainder array, difference-form stencil)"}
-                               [form_run]},
+                   "rk3_form": FORM_TEXT[form_run]},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                      "algorithmic_bytes_per_point_step": bpc,
@@ -602,6 +621,8 @@ def run_gpu_arm(args):
         line["fp32_vs_fp64"] = precision
     if comp:
         line["compensated"] = comp
+    for f, v in other_forms.items():
+        line[{abi.RK3_THREE_STAGE: "three_stage", abi.RK3_PSI_DIFF: "psi_diff"}[f]] = v
     if fp64:
         line["fp64"] = fp64
     if not args.no_ring and rank == 0 and world == 1:
@@ -638,9 +659,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--kernel", type=int, nargs=3, default=None, metavar=("KIND", "TZ", "TY"))
     ap.add_argument("--no-autotune", action="store_true", help="keep the default tile shape and work order")
-    ap.add_argument("--stage-form", type=int, default=0, choices=[0, 1, 2],
+    ap.add_argument("--stage-form", type=int, default=3, choices=[0, 1, 2, 3],
                     help="real-time RK3 form of the timed run: 0 three full stages, 1 deferred psi1 "
-                         "(stage 1 stores w1 only), 2 compensated state")
+                         "(stage 1 stores w1 only), 2 compensated state, 3 psi difference (no w array)")
     ap.add_argument("--no-ring", action="store_true", help="skip the 256^3 vortex-ring FP32/FP64 leg")
     ap.add_argument("--ring-steps", type=int, default=2000)
     ap.add_argument("--no-imag", action="store_true", help="skip the batched imaginary-time leg")

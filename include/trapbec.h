@@ -288,7 +288,7 @@ int trapbec_get_tile_shape(trapbec_ctx* ctx, int real_time, int* tile_z, int* ti
  * served from L2.                                                          */
 int trapbec_set_chunk(trapbec_ctx* ctx, int chunk);
 
-/* Form of the real-time RK3 step (run.f90:42-57) on the tiled FP32 kernel.
+/* Form of the real-time RK3 step (run.f90:42-57) on the tiled kernel.
  * TRAPBEC_RK3_THREE_STAGE (default): three full stages, each storing w and psi.
  * TRAPBEC_RK3_COMPENSATED (FP32 contexts): the three stages with a
  *   compensated state.  Each stage's update psi' = psi + B w is formed as an
@@ -312,9 +312,26 @@ int trapbec_set_chunk(trapbec_ctx* ctx, int chunk);
  *   the plain stage variant runs (harmonic or no potential, rotation or no
  *   frame term); elsewhere the step keeps three stages.  On GB300 it measured
  *   slower than three stages on the best tile shape.
+ * TRAPBEC_RK3_PSI_DIFF (FP32 and FP64 contexts): no w array is stored.  The
+ *   two psi arrays hold the last two stage values, and each stage recovers
+ *   the w of the stage before it from their difference: stage 1 stores psi1
+ *   only, stage 2 takes w1 = 3 (psi1 - psi0) and writes psi2 over psi0,
+ *   stage 3 takes w2 = psi2 - psi1 and writes psi3 over psi1.  The same RK3
+ *   scheme, with w rounded differently: the recovered w carries the rounding
+ *   of the psi update it came from, so results agree with three stages to
+ *   the rounding of a few ulps per step (FP64: 1e-12 relative after hundreds
+ *   of steps), not bit for bit.  64 instead of 80 bytes of HBM traffic per
+ *   grid point and step.  It applies where the plain stage variant runs on
+ *   the tiled kernel (harmonic or no potential, rotation or no frame term);
+ *   elsewhere the step keeps three stages.
  * trapbec_get_stage_form: *form = the form the next trapbec_step_rt takes
- * (THREE_STAGE where a requested deferred form cannot run).                 */
-enum trapbec_rk3_form { TRAPBEC_RK3_THREE_STAGE = 0, TRAPBEC_RK3_DEFERRED = 1, TRAPBEC_RK3_COMPENSATED = 2 };
+ * (THREE_STAGE where a requested deferred or psi-difference form cannot run). */
+enum trapbec_rk3_form {
+  TRAPBEC_RK3_THREE_STAGE = 0,
+  TRAPBEC_RK3_DEFERRED = 1,
+  TRAPBEC_RK3_COMPENSATED = 2,
+  TRAPBEC_RK3_PSI_DIFF = 3
+};
 int trapbec_set_stage_form(trapbec_ctx* ctx, int form);
 int trapbec_get_stage_form(trapbec_ctx* ctx, int* form);
 

@@ -34,7 +34,7 @@ LAYOUT_INTERIOR, LAYOUT_GHOSTED = 0, 1
 FIELD_VELOCITY, FIELD_QPRESSURE = 0, 1
 IMAG_REF_EULER, IMAG_RK3_RENORM = 0, 1
 STOP_REL, STOP_ABS, STOP_ABS_PER_NORM = 0, 1, 2
-RK3_THREE_STAGE, RK3_DEFERRED, RK3_COMPENSATED = 0, 1, 2
+RK3_THREE_STAGE, RK3_DEFERRED, RK3_COMPENSATED, RK3_PSI_DIFF = 0, 1, 2, 3
 
 SCALAR_OMEGA_Z, SCALAR_DT_RE, SCALAR_DT_IM, SCALAR_GAMMA = 0, 1, 2, 3
 SCALAR_T, SCALAR_ADVECTIVE_VX, SCALAR_NORM_TARGET = 4, 5, 6

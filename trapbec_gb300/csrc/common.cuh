@@ -31,7 +31,20 @@ enum FrameMode : int { FRAME_NONE = 0, FRAME_ROT = 1, FRAME_ADV = 2 };
 //   S1W: w1 = c*rhs(psi0), only w1 stored
 //   S2D: psi1 = psi0 + B1*w1 (same FMA as S1), then S2 from psi1; w2 goes to
 //        a second w buffer because w1 is read with its ghost frame
-enum StageKind : int { ST_S1 = 0, ST_S2 = 1, ST_S3 = 2, ST_EU = 3, ST_DIAG = 4, ST_S1W = 5, ST_S2D = 6 };
+// The psi-difference real-time form (tiled kernel, plain stages) stores no w
+// at all: the two psi arrays hold the last two stage values, and a stage
+// recovers the w of the stage before it from their difference,
+// w_prev = (psi_k - psi_{k-1}) / B_prev (exact in exact arithmetic since
+// psi_k = psi_{k-1} + B_prev*w_prev):
+//   S1P: w1 = c*rhs(psi0), psi1 = psi0 + B1*w1, only psi1 stored
+//   S2P: w2 = A2*w1 + c*rhs(psi1) with w1 = 3*(psi1 - psi0), psi2 = psi1 + B2*w2
+//        stored over psi0 (each cell is read and written by one thread)
+//   S3P: w3 = A3*w2 + c*rhs(psi2) with w2 = (psi2 - psi1)/B2, psi3 = psi2 + B3*w3
+//        stored over psi1
+enum StageKind : int {
+  ST_S1 = 0, ST_S2 = 1, ST_S3 = 2, ST_EU = 3, ST_DIAG = 4, ST_S1W = 5, ST_S2D = 6,
+  ST_S1P = 7, ST_S2P = 8, ST_S3P = 9
+};
 
 // Number of FP64 quantities a stage kernel may reduce (fused reductions).
 //   0: sum|psi|^2  1: sum Re psi* lap  2: sum pot|psi|^2  3: sum |psi|^4
@@ -88,6 +101,8 @@ template <typename T> struct StageArgs {
   int use_ctrl_scale;         // take the load factor from ctrl->scale
   const c_t<T>* __restrict__ w_in;  // S2D: w1 (ghost fix-ups read it); w receives w2
   T B1;                       // S2D: B of stage 1 (psi1 = psi0 + B1*w1)
+  T rB;                       // S2P / S3P: 1/B of the previous stage (w_prev = rB*(psi - psi_prev));
+                              // w_in then points at the previous psi array
   c_t<T>* __restrict__ lo;    // compensated state: rounding remainder of psi, read and rewritten in place
 };
 

@@ -122,7 +122,7 @@ template <typename T> struct TiledArgs {
   // the parameter (constant) bank instead of holding them in registers:
   // 0-2: (2,-27,270)/(180 hx^2), 3-5: y, 6-8: z, 9: -490*sum(1/(180 h^2)),
   // 10: -9, 11: 45, 12: (c_re, c_re), 13: (-c_im, c_im), 14: (A, A), 15: (B, B),
-  // 16: (B1, B1) (deferred S2)
+  // 16: (B1, B1) (deferred S2) or (1/B, 1/B) of the previous stage (S2P, S3P)
   c_t<T> k[17];
 };
 
@@ -256,9 +256,10 @@ template <typename T, int TZ, int TY, int R, int NSLOT = 8, int MINB = 0> struct
 // box + w tile).  Kinds that read no w (stage 1, Euler, diagnostics) keep the
 // psi box only and as many slots as fit (up to 12): a deeper prefetch.  The
 // deferred S2 holds a ghosted w1 box beside the psi box (at least 6 slots).
+// S2P and S3P load the previous psi tile where the other stages load w.
 template <typename T, class G, int KIND> struct KindGeom {
   static constexpr bool DEFER = (KIND == ST_S2D);
-  static constexpr bool NO_W = (KIND == ST_S1 || KIND == ST_S1W || KIND == ST_EU || KIND == ST_DIAG);
+  static constexpr bool NO_W = (KIND == ST_S1 || KIND == ST_S1W || KIND == ST_S1P || KIND == ST_EU || KIND == ST_DIAG);
   static constexpr int W_BYTES = DEFER ? G::SLOT_BYTES : (NO_W ? 0 : G::W_BYTES);
   static constexpr int SLOT_STRIDE =
       DEFER ? (G::W_OFF + G::SLOT_BYTES + 127) / 128 * 128 : (NO_W ? G::W_OFF : G::SLOT_STRIDE);
@@ -322,13 +323,16 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
   using P = PK<T>;
   using V = c_t<T>;
   constexpr int HZ = G::HZ, TZP = G::TZP, S = K::S, NT = G::NT;
-  constexpr bool READS_W = (KIND == ST_S2 || KIND == ST_S3 || KIND == ST_S2D);
+  // the psi-difference stages S2P / S3P read the previous psi tile in the w slot
+  constexpr bool PDIFF = (KIND == ST_S1P || KIND == ST_S2P || KIND == ST_S3P);
+  constexpr bool READS_W = (KIND == ST_S2 || KIND == ST_S3 || KIND == ST_S2D || KIND == ST_S2P || KIND == ST_S3P);
   constexpr bool COMP = (VAR == VAR_COMP);   // a plain variant whose update carries the remainder
   constexpr bool PLAIN = (VAR == VAR_PLAIN) || COMP, IMAG = (VAR == VAR_IMAG), GEN = (VAR == VAR_GEN);
   static_assert(!COMP || (!BATCH && (KIND == ST_S1 || KIND == ST_S2 || KIND == ST_S3)),
                 "the compensated state is for the real-time RK3 stages");
   constexpr bool ANALYTIC = PLAIN || IMAG;   // harmonic / no potential, rotation / no frame
   static_assert(!K::DEFER || PLAIN, "the deferred stage has a plain variant only");
+  static_assert(!PDIFF || (VAR == VAR_PLAIN && !BATCH), "the psi-difference stages have a plain variant only");
   static_assert(!IMAG || KIND == ST_S1 || KIND == ST_S2 || KIND == ST_S3, "imaginary-time variant: RK3 stages only");
   // the queue preload waits for planes xa-3 .. xa+2, all issued before it
   static_assert(S >= 6, "the ring needs at least 6 slots");
@@ -804,7 +808,12 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
         } else {
           const V wv = K::DEFER ? slx[G::W_OFF_ELEMS + qoff + r * TZP]
                        : READS_W ? slx[G::W_OFF_ELEMS + (yg * R + r) * TZ + lz] : mk<T>((T)0, (T)0);
-          wn = (KIND == ST_S1 || KIND == ST_S1W) ? cr : P::fma(ta.k[14], wv, cr);
+          if constexpr (KIND == ST_S2P || KIND == ST_S3P) {
+            // the previous stage's w from the two psi values: (psi - psi_prev) / B_prev
+            wn = P::fma(ta.k[14], P::mul(ta.k[16], P::sub(craw, wv)), cr);
+          } else {
+            wn = (KIND == ST_S1 || KIND == ST_S1W || KIND == ST_S1P) ? cr : P::fma(ta.k[14], wv, cr);
+          }
           pn = P::fma(ta.k[15], wn, c);
         }
         V lon = mk<T>((T)0, (T)0);

@@ -24,8 +24,10 @@ struct TiledPlan {
   CUtensorMap tmw;       // w (read by stages 2 and 3)
   CUtensorMap tmw1;      // second w buffer, interior tiles (S3 of the deferred form)
   CUtensorMap tmwg;      // w with the ghost frame (deferred S2 reads w1 like psi)
+  CUtensorMap tmpi[2];   // the two psi buffers as interior tiles (psi-difference S2P / S3P)
   int defer_ok = 0;      // the deferred real-time form can run (FP32, second w buffer)
   int comp_ok = 0;       // the compensated-state real-time stages are built for this shape
+  int pdiff_ok = 0;      // the psi-difference real-time stages can run
   int* err = nullptr;    // device error flag (owned by the context)
   uint32_t wait_us = 2000000;   // microseconds before a wait gives up
   int inject_wait = 0;   // test hook: waits aim at a phase that never completes

@@ -124,6 +124,23 @@ int plan_shape(const trapbec_params& p, void* const psi[2], void* w, void* w2, i
   }
   int nb = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k2, G::NT, G::SMEM) != cudaSuccess || nb < 1) return 5;
+  // the psi-difference real-time form: no w array; S2P / S3P load the
+  // previous psi array's interior tiles where S2 / S3 load w
+  {
+    auto kp1 = stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S1P, VAR_PLAIN, false>;
+    auto kp2 = stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S2P, VAR_PLAIN, false>;
+    auto kp3 = stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S3P, VAR_PLAIN, false>;
+    int nbp = 0;
+    q.pdiff_ok = encode_box<T, TZ, TY, R, NS, MB>(p, psi[0], false, &q.tmpi[0]) == 0 &&
+                 encode_box<T, TZ, TY, R, NS, MB>(p, psi[1], false, &q.tmpi[1]) == 0 &&
+                 cudaFuncSetAttribute(kp1, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      KindGeom<T, G, ST_S1P>::SMEM) == cudaSuccess &&
+                 cudaFuncSetAttribute(kp2, cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM) == cudaSuccess &&
+                 cudaFuncSetAttribute(kp3, cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM) == cudaSuccess &&
+                 cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nbp, kp2, G::NT, G::SMEM) == cudaSuccess &&
+                 nbp >= nb;
+    cudaGetLastError();   // a refused attribute only disables this form
+  }
   // the deferred real-time form (FP32): S1 stores w1 only, S2 forms psi1 from
   // ghosted boxes of psi0 and w1 and writes w2 to the second w buffer
   q.defer_ok = 0;
@@ -188,6 +205,26 @@ int launch_shape(const TiledPlan& plan, int kind, const StageArgs<T>& a, cudaStr
   int grid = plan.grid;
   if (a.red && grid > red_cap) grid = red_cap;
   const bool plain = tiled_plain(a);
+  if (kind == ST_S1P || kind == ST_S2P || kind == ST_S3P) {
+    if (!plain || !plan.pdiff_ok) return 12;
+    if (kind == ST_S1P) {
+      stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S1P, VAR_PLAIN, false>
+          <<<grid, G::NT, KindGeom<T, G, ST_S1P>::SMEM, st>>>(*tm, *tmw, ta, BatchArgs{});
+    } else {
+      // the previous psi array (a.w_in) is read as interior tiles and receives psi_out
+      const CUtensorMap* tmp = nullptr;
+      if ((const void*)a.w_in == plan.psi_base[0]) tmp = &plan.tmpi[0];
+      else if ((const void*)a.w_in == plan.psi_base[1]) tmp = &plan.tmpi[1];
+      if (!tmp || (const void*)a.psi_out != (const void*)a.w_in || a.w_in == a.psi_in) return 12;
+      ta.k[16] = mk<T>(a.rB, a.rB);
+      if (kind == ST_S2P)
+        stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S2P, VAR_PLAIN, false><<<grid, G::NT, G::SMEM, st>>>(*tm, *tmp, ta, BatchArgs{});
+      else
+        stage_tiled_kernel<T, TZ, TY, R, NS, MB, ST_S3P, VAR_PLAIN, false><<<grid, G::NT, G::SMEM, st>>>(*tm, *tmp, ta, BatchArgs{});
+    }
+    if (nblk) *nblk = grid;
+    return cudaGetLastError() == cudaSuccess ? 0 : 8;
+  }
   if (kind == ST_S1W || kind == ST_S2D) {
     if constexpr (sizeof(T) == 4) {
       if (!plain || !plan.defer_ok) return 9;

@@ -233,7 +233,8 @@ template <typename T> bool use_tiled(trapbec_ctx* c) {
 
 // Stage kinds of the real-time step that take the real-time plan when plain.
 inline bool rt_kind(int kind) {
-  return kind == ST_S1 || kind == ST_S2 || kind == ST_S3 || kind == ST_S1W || kind == ST_S2D;
+  return kind == ST_S1 || kind == ST_S2 || kind == ST_S3 || kind == ST_S1W || kind == ST_S2D || kind == ST_S1P ||
+         kind == ST_S2P || kind == ST_S3P;
 }
 
 // The two tiled plans: `plan` (shape index `shape`; shape < 0: the first
@@ -296,8 +297,8 @@ int launch_stage(trapbec_ctx* c, int kind, StageArgs<T>& a, int* nblk_out) {
   }
   plan.wait_us = c->wait_us;
   plan.inject_wait = c->inject_wait;
-  if (!tiled && (kind == ST_S1W || kind == ST_S2D)) {
-    set_error("the deferred real-time stages need the tiled kernel");
+  if (!tiled && (kind == ST_S1W || kind == ST_S2D || kind == ST_S1P || kind == ST_S2P || kind == ST_S3P)) {
+    set_error("the deferred and psi-difference real-time stages need the tiled kernel");
     return TRAPBEC_ERR_UNSUPPORTED;
   }
   if (tiled) {
@@ -431,6 +432,28 @@ template <typename T> int do_step_rt(trapbec_ctx* c, int nsteps) {
       a.psi_in = (const c_t<T>*)c->psi[c->cur ^ 1]; a.psi_out = (c_t<T>*)c->psi[c->cur];
       a.A = (T)(-1); a.B = (T)0.5;
       if ((rc = launch_stage<T>(c, ST_S3, a, nullptr))) return rc;
+      c->t = (double)((T)c->t + dcr);   // run.f90:55, t real
+      continue;
+    }
+    if (c->stage_form == TRAPBEC_RK3_PSI_DIFF && c->kernel_kind != 1 && c->plan_rt_valid && c->plan_rt.pdiff_ok &&
+        tiled_plain(a)) {
+      // psi-difference form: no w array.  Stage 1 stores psi1 only; stage 2
+      // takes w1 = 3 (psi1 - psi0) and writes psi2 over psi0; stage 3 takes
+      // w2 = psi2 - psi1 and writes psi3 over psi1.  Same scheme, w rounded
+      // differently (the recovered w includes the rounding of the psi update).
+      c_t<T>* p0 = (c_t<T>*)c->psi[c->cur];
+      c_t<T>* p1 = (c_t<T>*)c->psi[c->cur ^ 1];
+      a.w = nullptr;
+      a.psi_in = p0; a.psi_out = p1;
+      a.A = 0; a.B = (T)1 / (T)3;
+      if ((rc = launch_stage<T>(c, ST_S1P, a, nullptr))) return rc;
+      a.psi_in = p1; a.w_in = p0; a.psi_out = p0;
+      a.A = a2; a.B = (T)1; a.rB = (T)3;
+      if ((rc = launch_stage<T>(c, ST_S2P, a, nullptr))) return rc;
+      a.psi_in = p0; a.w_in = p1; a.psi_out = p1;
+      a.A = (T)(-1); a.B = (T)0.5; a.rB = (T)1;
+      if ((rc = launch_stage<T>(c, ST_S3P, a, nullptr))) return rc;
+      c->cur ^= 1;
       c->t = (double)((T)c->t + dcr);   // run.f90:55, t real
       continue;
     }
@@ -1278,7 +1301,8 @@ int trapbec_get_tile_shape(trapbec_ctx* c, int real_time, int* tile_z, int* tile
 }
 
 int trapbec_set_stage_form(trapbec_ctx* c, int form) {
-  if (!c || (form != TRAPBEC_RK3_THREE_STAGE && form != TRAPBEC_RK3_DEFERRED && form != TRAPBEC_RK3_COMPENSATED))
+  if (!c || (form != TRAPBEC_RK3_THREE_STAGE && form != TRAPBEC_RK3_DEFERRED && form != TRAPBEC_RK3_COMPENSATED &&
+             form != TRAPBEC_RK3_PSI_DIFF))
     return TRAPBEC_ERR_ARG;
   if (form == TRAPBEC_RK3_COMPENSATED) {
     if (c->prec != TRAPBEC_FP32) {
@@ -1315,8 +1339,18 @@ int trapbec_get_stage_form(trapbec_ctx* c, int* form) {
     *form = TRAPBEC_RK3_COMPENSATED;   // or the step reports TRAPBEC_ERR_UNSUPPORTED
     return TRAPBEC_OK;
   }
-  *form = (c->stage_form == TRAPBEC_RK3_DEFERRED && c->prec == TRAPBEC_FP32 && c->kernel_kind != 1 &&
-           c->plan_rt_valid && c->plan_rt.defer_ok && plain) ? TRAPBEC_RK3_DEFERRED : TRAPBEC_RK3_THREE_STAGE;
+  if (c->prec == TRAPBEC_FP64) {
+    StageArgs<double> a64 = base_args<double>(c, c->t);
+    plain = tiled_plain(a64);
+  }
+  const bool tiled_rt = c->kernel_kind != 1 && c->plan_rt_valid && plain;
+  if (c->stage_form == TRAPBEC_RK3_PSI_DIFF && tiled_rt && c->plan_rt.pdiff_ok) {
+    *form = TRAPBEC_RK3_PSI_DIFF;
+    return TRAPBEC_OK;
+  }
+  *form = (c->stage_form == TRAPBEC_RK3_DEFERRED && c->prec == TRAPBEC_FP32 && tiled_rt && c->plan_rt.defer_ok)
+              ? TRAPBEC_RK3_DEFERRED
+              : TRAPBEC_RK3_THREE_STAGE;
   return TRAPBEC_OK;
 }
 
@@ -1336,7 +1370,7 @@ template <typename T> int autotune_impl(trapbec_ctx* c, int steps, TuneVal* best
   key.p.nx = c->p.nx; key.p.ny = c->p.ny; key.p.nz = c->p.nz;
   key.p.precision = c->p.precision; key.p.boundaries = c->p.boundaries; key.p.periodicz = c->p.periodicz;
   key.p.potential = c->p.potential;
-  key.p.reserved[0] = c->stage_form;   // the compensated form runs on other shapes
+  key.p.reserved[0] = c->stage_form;   // each form is timed on its own (the compensated one on other shapes)
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     for (auto& kv : g_tune_cache)
@@ -1355,6 +1389,7 @@ template <typename T> int autotune_impl(trapbec_ctx* c, int steps, TuneVal* best
     TiledPlan plan;
     if (plan_tiled<T>(c->p, c->psi, c->w, c->w2, c->nsm, sh, c->d_err, &plan) != 0) continue;
     if (c->stage_form == TRAPBEC_RK3_COMPENSATED && !plan.comp_ok) continue;
+    if (c->stage_form == TRAPBEC_RK3_PSI_DIFF && !plan.pdiff_ok) continue;
     std::vector<int> chunks = {16, 32, 64, c->p.nx};
     for (int L : chunks) {
       if (L > c->p.nx) continue;

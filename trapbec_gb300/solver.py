@@ -182,8 +182,9 @@ class Solver:
 
     def set_stage_form(self, form: int) -> None:
         """Real-time RK3 form: abi.RK3_THREE_STAGE (default), abi.RK3_DEFERRED (stage 1 stores w1
-        only; allocates a second w buffer) or abi.RK3_COMPENSATED (FP32: the update keeps its
-        rounding remainder in a second array; allocates it)."""
+        only; allocates a second w buffer), abi.RK3_COMPENSATED (FP32: the update keeps its
+        rounding remainder in a second array; allocates it) or abi.RK3_PSI_DIFF (no w array:
+        each stage recovers the previous stage's w from the two psi arrays)."""
         check(self.lib.trapbec_set_stage_form(self.ctx, int(form)), "trapbec_set_stage_form")
 
     def stage_form(self) -> int:
