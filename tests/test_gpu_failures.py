@@ -146,7 +146,7 @@ def test_bad_arguments_return_status_and_leave_the_context_usable():
     assert lib.trapbec_set_kernel(s.ctx, 3, 0, 0) == abi.ERR_ARG            # no such kernel kind
     assert lib.trapbec_set_kernel(s.ctx, 2, -99, 0) == abi.ERR_UNSUPPORTED  # no such built shape
     assert lib.trapbec_set_kernel(s.ctx, 2, 48, 48) == abi.ERR_UNSUPPORTED  # no shape of this size
-    assert lib.trapbec_set_stage_form(s.ctx, 3) == abi.ERR_ARG
+    assert lib.trapbec_set_stage_form(s.ctx, 4) == abi.ERR_ARG   # no such form
     assert lib.trapbec_set_chunk(s.ctx, -1) == abi.ERR_ARG
     tz, ty = C.c_int(0), C.c_int(0)
     assert lib.trapbec_get_tile_shape(s.ctx, 1, None, C.byref(ty)) == abi.ERR_ARG
