@@ -7,11 +7,16 @@
 //
 // Parity status: the reference is Fortran 90 + MPI and no Fortran compiler or
 // MPI exists in the build or GPU images, so the reference binary cannot be run
-// and the reference ships no golden vectors.  This restatement is therefore
-// pinned by known-answer tests derived from mathematics (stencil exactness on
-// polynomials, convergence order, the RK3 amplification polynomial, the Lz
-// eigenvalue, norm conservation, the harmonic-oscillator ground state) and not
-// by reference outputs ("parity unpinned" against the reference binary).
+// and the reference ships no golden vectors.  The reference's own source is
+// run instead, by the Fortran-subset interpreter oracle/fortran_subset.py
+// (gfortran -O3 x86-64 semantics, no FP contraction): the golden vectors it
+// produced (tests/golden/refsrc_cases.*, generator
+// tests/golden/make_refsrc_fixtures.py) are reproduced by this restatement
+// bit for bit for the time stepping in FP64 and FP32, on 1 rank and a 2 x 2
+// process grid (tests/test_refsrc_golden.py).  Known-answer tests derived
+// from mathematics (stencil exactness on polynomials, convergence order, the
+// RK3 amplification polynomial, the Lz eigenvalue, norm conservation, the
+// harmonic-oscillator ground state) check it as well.
 //
 // It follows the reference statement by statement, in the same evaluation
 // order, with T = float for the shipped single-precision build and

@@ -1,0 +1,91 @@
+"""The CUDA path against golden vectors of the reference's own source.
+
+The fixtures (tests/golden/refsrc_cases.{json,npz}) are the states the
+reference's `program run` wrote when its Fortran source was executed by
+oracle/fortran_subset.py; see tests/test_refsrc_golden.py.  Here the GPU runs
+the same cases through the C ABI: FP64 to 1e-12 relative in psi and the
+diagnostics (the CUDA kernels contract to FMA and order the stencil sums
+symmetrically, so not bit for bit), FP32 at FP32 rounding, in both real-time
+forms the bench uses (three stages and the psi difference)."""
+import numpy as np
+import pytest
+
+from trapbec_gb300 import Solver, abi
+from tests.test_refsrc_golden import ARRAYS, CASES, STEP_CASES, INIT_CASES, case_params, printed_output_line
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-12
+
+
+def _rel(a, b):
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def _l2(a, b):
+    return float(np.linalg.norm((a - b).ravel()) / np.linalg.norm(b.ravel()))
+
+
+@pytest.mark.parametrize("form", [abi.RK3_THREE_STAGE, abi.RK3_PSI_DIFF])
+@pytest.mark.parametrize("name", STEP_CASES)
+def test_gpu_time_stepping_matches_reference_source(name, form):
+    rec = CASES[name]
+    p = case_params(rec)
+    s = Solver(p)
+    s.set_stage_form(form)
+    s.set_psi(ARRAYS[f"{name}__psi0"])
+    s.step_rt(rec["steps"])
+    ref = ARRAYS[f"{name}__psi"].astype(np.complex128)
+    got = s.get_psi().astype(np.complex128)
+    if p.precision == abi.FP64:
+        assert _rel(got, ref) < FP64_TOL, (name, _rel(got, ref))
+    else:
+        assert _l2(got, ref) < 2e-6, (name, _l2(got, ref))
+    t, mx, mn, mean, intpsi2 = printed_output_line(rec)
+    d = s.diag()
+    tol = FP64_TOL if p.precision == abi.FP64 else 2e-6
+    assert abs(d["maxpsi"] - mx) <= tol * mx
+    assert abs(d["meanpsi"] - mean) <= tol * mean
+    assert abs(d["intpsi2"] - intpsi2) <= (FP64_TOL if p.precision == abi.FP64 else 1e-5) * intpsi2
+    assert s.t == pytest.approx(t, rel=1e-6 if p.precision == abi.FP32 else 1e-15)
+    s.close()
+
+
+@pytest.mark.parametrize("name", INIT_CASES)
+def test_gpu_initial_states_match_reference_source(name):
+    rec = CASES[name]
+    s = Solver(case_params(rec))
+    s.init_state(rec["init"])
+    if "helper" in rec:
+        s.init_state(rec["helper"])
+    s.step_rt(rec["steps"])   # dt = 0: the reference wrote the initial state after one step
+    ref = ARRAYS[f"{name}__psi"]
+    assert _rel(s.get_psi(), ref) < 1e-13, (name, _rel(s.get_psi(), ref))
+    s.close()
+
+
+def test_gpu_imaginary_time_euler_matches_reference_source():
+    name = "imag_euler_fp64"
+    rec = CASES[name]
+    s = Solver(case_params(rec))
+    s.init_state("single_vortex")
+    steps, ratio = s.step_imag(rec["imag_steps"], abi.IMAG_REF_EULER)
+    assert steps == rec["imag_steps"]
+    rows = [ln.split() for ln in rec["stdout"]]
+    ratios = [float(r[1]) for r in rows if len(r) == 2 and r[0].isdigit()]
+    assert ratio == pytest.approx(ratios[-1], rel=1e-12)
+    s.step_rt(rec["steps"])
+    assert _rel(s.get_psi(), ARRAYS[f"{name}__psi"]) < FP64_TOL
+    s.close()
+
+
+@pytest.mark.parametrize("name", [n for n, r in CASES.items() if r.get("diag")])
+def test_gpu_output_diagnostics_match_reference_source(name):
+    rec = CASES[name]
+    s = Solver(case_params(rec))
+    s.set_psi(ARRAYS[f"{name}__psi0"])
+    s.step_rt(rec["steps"])
+    for kind, got in (("vel", s.velocity()), ("qpress", s.qpressure())):
+        ref = ARRAYS[f"{name}__{kind}"]
+        assert _rel(got, ref) < 1e-11, (name, kind, _rel(got, ref))
+    s.close()
