@@ -19,6 +19,7 @@ from __future__ import annotations
 import argparse
 import json
 import os
+import platform
 import struct
 import sys
 import time
@@ -146,6 +147,8 @@ def main(argv=None) -> int:
     args = ap.parse_args(argv)
     meta = {"generator": "tests/golden/make_refsrc_fixtures.py",
             "interpreter": "oracle/fortran_subset.py (gfortran -O3 x86-64 semantics, no FP contraction)",
+            # the intrinsic functions come from this machine's libm (hypot, expf, ...)
+            "platform": {"machine": platform.machine(), "libc": " ".join(platform.libc_ver())},
             "cases": {}}
     arrays = {}
     for name, p, psi0, steps, nprocs, over, extra in cases():

@@ -13,6 +13,7 @@ bit for bit (initial states, which go through libm's transcendental
 functions, to 1e-14)."""
 import json
 import os
+import platform
 
 import numpy as np
 import pytest
@@ -27,10 +28,18 @@ GOLD = os.path.join(HERE, "golden")
 def load_cases():
     meta = json.load(open(os.path.join(GOLD, "refsrc_cases.json")))
     arrays = np.load(os.path.join(GOLD, "refsrc_cases.npz"))
-    return meta["cases"], arrays
+    return meta, arrays
 
 
-CASES, ARRAYS = load_cases()
+META, ARRAYS = load_cases()
+CASES = META["cases"]
+# The interpreter took ABS of a complex (hypot) and the other intrinsic
+# functions from the generating machine's libm, as the oracle takes them from
+# this one's: where the two libms are the same the oracle must agree bit for
+# bit; another libm (aarch64 glibc's hypot rounds differently in the last
+# place) leaves ulp-level differences.
+SAME_LIBM = (META.get("platform", {}).get("machine") == platform.machine() and
+             META.get("platform", {}).get("libc") == " ".join(platform.libc_ver()))
 
 
 def case_params(rec):
@@ -88,8 +97,12 @@ def test_oracle_reproduces_reference_time_stepping_bitwise(name):
     o, _ = oracle_run(name, rec)
     ref = ARRAYS[f"{name}__psi"]
     got = o.get_psi().astype(ref.dtype)
-    assert np.array_equal(got.view(np.uint8), ref.view(np.uint8)), \
-        (name, float(np.max(np.abs(got - ref))))
+    if SAME_LIBM:
+        assert np.array_equal(got.view(np.uint8), ref.view(np.uint8)), \
+            (name, float(np.max(np.abs(got - ref))))
+    else:
+        err = float(np.max(np.abs(got - ref)) / np.max(np.abs(ref)))
+        assert err < (1e-15 if ref.dtype == np.complex128 else 1e-6), (name, err)
     assert o.t == pytest.approx(rec["t"], rel=1e-6 if ref.dtype == np.complex64 else 1e-15)
 
 
