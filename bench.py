@@ -315,10 +315,40 @@ def ring_leg(args, peak):
     norm/energy drift and L2 error against the FP64 run."""
     from trapbec_gb300 import reports
     r = reports.fp32_vs_fp64(n=256, steps=args.ring_steps, chunk=250)
-    for k in ("fp32", "fp64"):
+    for k in ("fp32", "fp64", "fp32_psi_diff"):
         r[k]["hbm_frac"] = r[k]["gbs_alg"] / peak
     r["workload"] = "vortex ring 256^3, FP64 and FP32 from the same start"
     return r
+
+
+def stretch_leg(args, peak):
+    """The quench workload's 1024^3 stretch size in complex FP32 (25.8 GB of
+    state): the headline's form on the autotuned tile, `stretch_steps` RK3
+    steps at the mid-ramp rotation from the seeded TF cloud (no ground state:
+    its relaxation at this size would dominate the run), device time."""
+    from trapbec_gb300 import Solver, abi
+    n = 1024
+    prob, init = make_problem(n, abi.FP32)
+    s = Solver(prob.to_params())
+    s.set_stage_form(args.stage_form)
+    tune = None if args.no_autotune else s.autotune(steps=3)
+    s.init_state(init["name"], seed=init["seed"], amp=init["amp"], r_tf2=init["r_tf2"], noise_amp=init["noise_amp"])
+    s.set_scalar(abi.SCALAR_OMEGA_Z, prob.omega_z_for(0.5 * init["omega_final"]))
+    s.step_rt(3)
+    steps = args.stretch_steps
+    s.step_rt(steps)
+    ms = s.last_kernel_ms()
+    form = s.stage_form()
+    tz, ty = s.tile_shape(real_time=True)
+    s.close()
+    cells = n ** 3
+    ach = cells * steps * ALG_BYTES[form] / (ms * 1e-3) / 1e9
+    return {"grid": [n, n, n], "steps": steps, "ms_per_step": ms / steps, "value": cells * steps / (ms * 1e-3),
+            "unit": UNIT, "tile": [tz, ty], "autotune": tune, "rk3_form": FORM_TEXT[form],
+            "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                         "algorithmic_bytes_per_point_step": ALG_BYTES[form],
+                         "form_bytes_per_point_step": FORM_BYTES[form],
+                         "frac_of_form_bytes": cells * steps * FORM_BYTES[form] / (ms * 1e-3) / 1e9 / peak}}
 
 
 def warmstart_leg(args):
@@ -641,6 +671,8 @@ def run_gpu_arm(args):
         line[{abi.RK3_THREE_STAGE: "three_stage", abi.RK3_PSI_DIFF: "psi_diff"}[f]] = v
     if fp64:
         line["fp64"] = fp64
+    if not args.no_stretch and rank == 0 and world == 1 and n == 512:
+        line["stretch_1024"] = stretch_leg(args, peak)
     if not args.no_ring and rank == 0 and world == 1:
         line["ring256"] = ring_leg(args, peak)
     if not args.no_imag and rank == 0 and world == 1:
@@ -679,6 +711,8 @@ def main():
                     help="real-time RK3 form of the timed run: 0 three full stages, 1 deferred psi1 "
                          "(stage 1 stores w1 only), 2 compensated state, 3 psi difference (no w array)")
     ap.add_argument("--no-ring", action="store_true", help="skip the 256^3 vortex-ring FP32/FP64 leg")
+    ap.add_argument("--no-stretch", action="store_true", help="skip the 1024^3 stretch leg")
+    ap.add_argument("--stretch-steps", type=int, default=60)
     ap.add_argument("--ring-steps", type=int, default=2000)
     ap.add_argument("--no-imag", action="store_true", help="skip the batched imaginary-time leg")
     ap.add_argument("--imag-count", type=int, default=64)

@@ -16,9 +16,10 @@ from . import abi, units
 from .solver import Solver
 
 
-def _run(prec, n, steps, chunk, psi0=None, seed=1234):
+def _run(prec, n, steps, chunk, psi0=None, seed=1234, form=abi.RK3_THREE_STAGE):
     prob, init = units.vortex_ring_256(prec, n=n, seed=seed)
     s = Solver(prob.to_params())
+    s.set_stage_form(form)
     if psi0 is None:
         s.init_state(init["name"], seed=init["seed"], amp=init["amp"], r_tf2=init["r_tf2"],
                      ring_radius=init["ring_radius"], noise_amp=init["noise_amp"])
@@ -51,6 +52,9 @@ def fp32_vs_fp64(n: int = 256, steps: int = 2000, chunk: int = 250, seed: int = 
     s.close()
     _, d032, ck32, psi32, ms32 = _run(abi.FP32, n, steps, chunk, psi0=psi0, seed=seed)
     l2 = float(np.linalg.norm(psi32.astype(np.complex128) - psi64) / np.linalg.norm(psi64))
+    # the same FP32 run in the psi-difference form (no w array; 64 instead of 80 bytes moved)
+    _, d0p, ckp, psip, msp = _run(abi.FP32, n, steps, chunk, psi0=psi0, seed=seed, form=abi.RK3_PSI_DIFF)
+    l2p = float(np.linalg.norm(psip.astype(np.complex128) - psi64) / np.linalg.norm(psi64))
     cells = n ** 3
     out = {
         "grid": n, "steps": steps,
@@ -68,6 +72,11 @@ def fp32_vs_fp64(n: int = 256, steps: int = 2000, chunk: int = 250, seed: int = 
                              "energy_rel": b[1]["energy"] / a[1]["energy"] - 1.0}
                             for a, b in zip(ck64, ck32)],
         },
+        "fp32_psi_diff": {"ms_per_step": msp / steps, "gbs_alg": cells * steps * 80 / (msp * 1e-3) / 1e9,
+                          "norm_drift": ckp[-1][1]["norm"] / d0p["norm"] - 1.0,
+                          "energy_drift": ckp[-1][1]["energy"] / d0p["energy"] - 1.0,
+                          "vs_fp64": {"l2_rel_psi": l2p, "norm_rel": ckp[-1][1]["norm"] / ck64[-1][1]["norm"] - 1.0,
+                                      "energy_rel": ckp[-1][1]["energy"] / ck64[-1][1]["energy"] - 1.0}},
         "wall_s": time.time() - t0,
         "energy_trap_units_fp64": prob.energy_to_trap(ck64[-1][1]["energy"]),
     }
