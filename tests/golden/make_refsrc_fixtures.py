@@ -10,9 +10,11 @@ Run in a checkout where the reference's sources are present:
 Each case records the trapbec_params it was run with, the start state (where
 it came through the restart files), the state the reference wrote after the
 last step (var0001.dat, gathered over ranks), rank 0's standard output and,
-where switched on, the vel01.dat / qpress01.dat diagnostics.  The fixtures
-are read by tests/test_refsrc_golden.py (the oracle, CPU) and
-tests/test_gpu_refsrc.py (the CUDA path).
+where switched on, the vel01.dat / qpress01.dat diagnostics; for a few
+single-rank cases the raw bytes of the unformatted files the reference wrote
+(tests/golden/refsrc_files.npz).  The fixtures are read by
+tests/test_refsrc_golden.py (the oracle, CPU) and tests/test_gpu_refsrc.py
+(the CUDA path and this library's writers).
 """
 from __future__ import annotations
 
@@ -140,11 +142,42 @@ def cases():
     return out
 
 
+# Cases whose output files are also kept byte for byte (tests/golden/refsrc_files.npz):
+# the unformatted records var_print writes (src/output.f90:64-75,80-91,102-108) on 1 rank.
+FILE_CASES = {"line16_np1_fp64": ("var0001.dat", "var.dat"), "line16_np1_fp32": ("var0001.dat", "var.dat"),
+              "diag_np1_fp64": ("var0001.dat", "var.dat", "vel01.dat", "qpress01.dat")}
+
+
+def write_file_fixtures(ref_src) -> None:
+    """Run the FILE_CASES again and keep the raw bytes of the files the
+    reference wrote into data/proc000 (tests/golden/refsrc_files.npz)."""
+    import shutil
+    out = {}
+    for name, p, psi0, steps, nprocs, over, extra in cases():
+        if name not in FILE_CASES:
+            continue
+        keep = os.path.join("/tmp", f"refsrc_files_{name}")
+        shutil.rmtree(keep, ignore_errors=True)
+        os.makedirs(keep)
+        refsrc.run_reference(ref_src, p, psi0, steps, nprocs, p.precision == abi.FP64, cparam_overrides=over,
+                             keep=keep)
+        for f in FILE_CASES[name]:
+            data = open(os.path.join(keep, "data", "proc000", f), "rb").read()
+            out[f"{name}__{f}"] = np.frombuffer(data, dtype=np.uint8)
+        shutil.rmtree(keep, ignore_errors=True)
+        print(f"{name}: files kept", flush=True)
+    np.savez_compressed(os.path.join(HERE, "refsrc_files.npz"), **out)
+
+
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--ref-src", default="/root/reference/src")
     ap.add_argument("--only", default=None, help="substring of the case names to run")
+    ap.add_argument("--files-only", action="store_true", help="only refsrc_files.npz")
     args = ap.parse_args(argv)
+    if args.files_only:
+        write_file_fixtures(args.ref_src)
+        return 0
     meta = {"generator": "tests/golden/make_refsrc_fixtures.py",
             "interpreter": "oracle/fortran_subset.py (gfortran -O3 x86-64 semantics, no FP contraction)",
             # the intrinsic functions come from this machine's libm (hypot, expf, ...)
@@ -178,6 +211,7 @@ def main(argv=None) -> int:
         np.savez_compressed(os.path.join(HERE, "refsrc_cases.npz"), **arrays)
         with open(os.path.join(HERE, "refsrc_cases.json"), "w") as f:
             json.dump(meta, f, indent=1, default=float)
+        write_file_fixtures(args.ref_src)
     return 0
 
 

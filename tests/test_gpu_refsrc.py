@@ -6,7 +6,12 @@ oracle/fortran_subset.py; see tests/test_refsrc_golden.py.  Here the GPU runs
 the same cases through the C ABI: FP64 to 1e-12 relative in psi and the
 diagnostics (the CUDA kernels contract to FMA and order the stencil sums
 symmetrically, so not bit for bit), FP32 at FP32 rounding, in both real-time
-forms the bench uses (three stages and the psi difference)."""
+forms the bench uses (three stages and the psi difference); and this
+library's file writers against the bytes of the files the reference wrote
+(tests/golden/refsrc_files.npz)."""
+import os
+import struct
+
 import numpy as np
 import pytest
 
@@ -88,4 +93,51 @@ def test_gpu_output_diagnostics_match_reference_source(name):
     for kind, got in (("vel", s.velocity()), ("qpress", s.qpressure())):
         ref = ARRAYS[f"{name}__{kind}"]
         assert _rel(got, ref) < 1e-11, (name, kind, _rel(got, ref))
+    s.close()
+
+
+FILES = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "refsrc_files.npz"))
+
+
+def _records(data):
+    out, off = [], 0
+    while off < len(data):
+        n = struct.unpack("<i", data[off:off + 4])[0]
+        out.append((n, data[off + 4:off + 4 + n], struct.unpack("<i", data[off + 4 + n:off + 8 + n])[0]))
+        off += 8 + n
+    return out
+
+
+@pytest.mark.parametrize("name", sorted({k.split("__")[0] for k in FILES.files}))
+def test_writers_match_reference_files(name, tmp_path):
+    """var0001.dat and var.dat written through the C ABI for the state the
+    reference wrote are its bytes exactly (src/output.f90:64-75,102-108); the
+    vel01.dat / qpress01.dat records have its layout, and values to 1e-11."""
+    rec = CASES[name]
+    p = case_params(rec)
+    s = Solver(p)
+    s.set_psi(ARRAYS[f"{name}__psi"])
+    s.set_scalar(abi.SCALAR_T, rec["t"])
+    s.t = rec["t"]
+    steps = rec["steps"]
+    d = str(tmp_path)
+    os.makedirs(os.path.join(d, "proc000"), exist_ok=True)
+    s.write_var(d, itime=steps, shots=steps)
+    s.write_restart(d, itime=steps)
+    for f in ("var0001.dat", "var.dat"):
+        want = FILES[f"{name}__{f}"].tobytes()
+        got = open(os.path.join(d, "proc000", f), "rb").read()
+        assert got == want, (name, f, len(got), len(want))
+    for f, which in (("vel01.dat", abi.FIELD_VELOCITY), ("qpress01.dat", abi.FIELD_QPRESSURE)):
+        key = f"{name}__{f}"
+        if key not in FILES.files:
+            continue
+        s.write_field(d, itime=steps, shots=steps, which=which)
+        want = _records(FILES[key].tobytes())
+        got = _records(open(os.path.join(d, "proc000", f), "rb").read())
+        assert len(got) == len(want) == 1
+        assert got[0][0] == want[0][0] and got[0][2] == want[0][2] and got[0][1][:8] == want[0][1][:8]
+        dt = np.float64 if p.precision == abi.FP64 else np.float32
+        a, b = np.frombuffer(got[0][1][8:], dtype=dt), np.frombuffer(want[0][1][8:], dtype=dt)
+        assert float(np.max(np.abs(a - b)) / np.max(np.abs(b))) < 1e-11
     s.close()
