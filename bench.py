@@ -485,10 +485,14 @@ def run_gpu_arm(args):
     e2e = None
     if not args.no_e2e:
         shots = args.shots
-        host = torch.empty(cells, dtype=torch.complex64 if prec == abi.FP32 else torch.complex128,
-                           pin_memory=True).numpy()
-        host_out = torch.empty_like(torch.from_numpy(host)).pin_memory().numpy()
+        # both host buffers are allocated pinned (page-locked by the CUDA host allocator) and the
+        # tensors that own them are kept for the whole leg
+        cdt = torch.complex64 if prec == abi.FP32 else torch.complex128
+        host_t = torch.empty(cells, dtype=cdt, pin_memory=True)
+        host_out_t = torch.empty(cells, dtype=cdt, pin_memory=True)
+        host, host_out = host_t.numpy(), host_out_t.numpy()
         host[:] = s.get_psi().reshape(-1)
+        host_out[:] = 0
         reps = max(1, args.e2e_reps)
 
         parts = []
@@ -695,7 +699,7 @@ def main():
     ap.add_argument("--n", type=int, default=512, help="grid size per axis (profiling uses smaller cases)")
     ap.add_argument("--chunk", type=int, default=20, help="RK3 steps per C-ABI call (Omega updated per call)")
     ap.add_argument("--shots", type=int, default=100, help="RK3 steps per end-to-end call")
-    ap.add_argument("--e2e-reps", type=int, default=3, help="timed end-to-end calls (after one untimed call)")
+    ap.add_argument("--e2e-reps", type=int, default=5, help="timed end-to-end calls (after one untimed call)")
     ap.add_argument("--precision-steps", type=int, default=500,
                     help="steps of the FP32 / compensated FP32 / FP64 comparison from the same start")
     ap.add_argument("--start", default="ground", choices=["ground", "tf"],
