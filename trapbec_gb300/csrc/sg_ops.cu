@@ -137,6 +137,27 @@ __global__ void up2_fwd_kernel(const bf16* x, bf16* y, int c, int B, int D, int 
   }
 }
 
+// one thread per coarse voxel x 8 channels: its 16 bytes read once and
+// written to its 8 fine voxels (a warp's writes cover whole fine rows)
+__global__ void up2_fwd8_kernel(const bf16* x, bf16* y, int c, int B, int D, int H, int W) {
+  const int c8 = c / 8, Df = 2 * D, Hf = 2 * H, Wf = 2 * W;
+  const size_t n = (size_t)B * D * H * W * c8;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int cc = (int)(i % c8);
+    size_t r = i / c8;
+    const int w = (int)(r % W); r /= W;
+    const int h = (int)(r % H); r /= H;
+    const int d = (int)(r % D);
+    const size_t b = r / D;
+    const uint4 v = *(const uint4*)(x + i * 8);
+#pragma unroll
+    for (int o = 0; o < 8; ++o) {
+      const int fd = 2 * d + (o >> 2), fh = 2 * h + ((o >> 1) & 1), fw = 2 * w + (o & 1);
+      *(uint4*)(y + (((b * Df + fd) * Hf + fh) * Wf + fw) * c + cc * 8) = v;
+    }
+  }
+}
+
 // one thread per coarse voxel x 4 channels: the sum of its 8 fine gradients
 __global__ void up2_bwd4_kernel(const float* dy, float* dx, int c, int B, int D, int H, int W) {
   const int Hf = 2 * H, Wf = 2 * W, Df = 2 * D, c4 = c / 4;
@@ -516,8 +537,12 @@ int tbsg_pool2_bwd(const float* dy, float* dx, int c, int batch, int D, int H, i
 
 int tbsg_up2_fwd(const void* x, void* y, int c, int batch, int D, int H, int W, void* stream) {
   if (!x || !y || c % 8) return TBSG_ERR_ARG;
-  up2_fwd_kernel<<<grid_for((size_t)batch * D * H * W * c), 256, 0, (cudaStream_t)stream>>>(
-      (const bf16*)x, (bf16*)y, c, batch, D, H, W);
+  if (((uintptr_t)x | (uintptr_t)y) % 16 == 0)
+    up2_fwd8_kernel<<<grid_for((size_t)batch * D * H * W * c / 8), 256, 0, (cudaStream_t)stream>>>(
+        (const bf16*)x, (bf16*)y, c, batch, D, H, W);
+  else
+    up2_fwd_kernel<<<grid_for((size_t)batch * D * H * W * c), 256, 0, (cudaStream_t)stream>>>(
+        (const bf16*)x, (bf16*)y, c, batch, D, H, W);
   return done();
 }
 
