@@ -70,7 +70,7 @@ enum trapbec_potential {       /* cparam.local `potential`, finite_diff.f90:29-1
   TRAPBEC_POT_CHANNEL = 6,
   TRAPBEC_POT_QUARTIC = 7,
   TRAPBEC_POT_SPHERE = 8,
-  TRAPBEC_POT_MOBIUS = 9,      /* reads the Trap array (trapbec_set_trap) + marker */
+  TRAPBEC_POT_MOBIUS = 9,      /* reads the Trap array (built as mesh_init builds it, or trapbec_set_trap) + marker */
   TRAPBEC_POT_ARRAY = 10       /* plain Trap array, no marker (new)            */
 };
 
@@ -159,7 +159,11 @@ int trapbec_set_psi(trapbec_ctx* ctx, const void* psi, int layout);
 int trapbec_get_psi(trapbec_ctx* ctx, void* psi, int layout);
 
 /* Set the Trap(1:nz,1:ny,1:nx) array (cdata.f90:10) used by the 'mobius' and
- * 'array' potentials; values are FP64 and converted to the context precision. */
+ * 'array' potentials; values are FP64 and converted to the context precision.
+ * For 'mobius' without a call to this function, the first step builds the
+ * Trap on the device as mesh_init does (initial.f90:159-198: a clamped sum of
+ * 200 x 200 Gaussians of the strip table per cell, inverted about the maximum
+ * over the grid); 'array' needs this call.                                  */
 int trapbec_set_trap(trapbec_ctx* ctx, const double* trap);
 
 /* Fill psi with one of the reference's initial states (initial.f90:58-157

@@ -19,8 +19,6 @@ import os
 import shutil
 import tempfile
 
-import numpy as np
-
 from oracle import fortran_subset as fs
 from oracle import refbin_parity as rb
 

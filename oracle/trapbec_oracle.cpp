@@ -159,6 +159,62 @@ template <typename T> struct Oracle {
       for (int i = 1; i <= nmx; ++i)
         R.xx[i] = (T)(2 * i - 1) / ((T)2 * (T)nmx) * Lx / (T)px + (T)R.cx * Lx / (T)px - Lx / (T)2;
     }
+    if (p.potential == TRAPBEC_POT_MOBIUS) init_mobius_trap();
+  }
+
+  // initial.f90:159-198: mesh_init's Trap of the 'mobius' potential (a later
+  // set_trap replaces it).  The strip table mobius(200,200,3), the per-cell
+  // sum over it clamped at 3 after every term, the maximum over all ranks
+  // (MPI_REDUCE MAX + BCAST) and Trap = theta - Trap.
+  void init_mobius_trap() {
+    const int N = 200;
+    const T pi = (T)3.14159265359;   // cdata.f90:13
+    std::vector<T> m1((size_t)N * N), m2((size_t)N * N), m3((size_t)N * N);
+    for (int i = 1; i <= N; ++i)
+      for (int j = 1; j <= N; ++j) {
+        const T r = (T)(i - 1) * (T)2 / (T)200 - (T)1;
+        const T theta = (T)(j - 1) * (T)2 * pi / (T)200;
+        const size_t q = (size_t)(i - 1) + (size_t)(j - 1) * N;   // mobius(i,j,:)
+        m1[q] = ((T)25 + (T)5 * r * std::cos(theta / (T)2)) * std::cos(theta);
+        m2[q] = ((T)25 + (T)5 * r * std::cos(theta / (T)2)) * std::sin(theta);
+        m3[q] = (T)5 * r * std::sin(theta / (T)2);
+      }
+    T theta = 0;
+    bool first = true;
+    for (auto& R : ranks) {
+      T rmax = 0;
+      bool rfirst = true;
+#pragma omp parallel for schedule(static)
+      for (int i = 1; i <= R.nmx; ++i)
+        for (int j = 1; j <= R.nmy; ++j)
+          for (int k = 1; k <= R.nmz; ++k) {
+            T acc = 0;
+            for (int ii1 = 1; ii1 <= N; ++ii1)
+              for (int ii2 = 1; ii2 <= N; ++ii2) {
+                const size_t q = (size_t)(ii1 - 1) + (size_t)(ii2 - 1) * N;
+                const T dx = R.xx[i] - m1[q], dy = R.yy[j] - m2[q], dz = R.zz[k] - m3[q];
+                T e = -((T)1.5 * (dx * dx));
+                e = e - (T)1.5 * (dy * dy);
+                e = e - (T)1.5 * (dz * dz);
+                acc = acc + std::exp(e);
+                if (acc > (T)3) acc = (T)3;
+              }
+            R.trap[R.in(k, j, i)] = acc;
+          }
+      for (int i = 1; i <= R.nmx; ++i)   // r=maxval(Trap)
+        for (int j = 1; j <= R.nmy; ++j)
+          for (int k = 1; k <= R.nmz; ++k) {
+            const T v = R.trap[R.in(k, j, i)];
+            if (rfirst || v > rmax) rmax = v;
+            rfirst = false;
+          }
+      if (first || rmax > theta) theta = rmax;
+      first = false;
+    }
+    for (auto& R : ranks)
+      for (int i = 1; i <= R.nmx; ++i)
+        for (int j = 1; j <= R.nmy; ++j)
+          for (int k = 1; k <= R.nmz; ++k) R.trap[R.in(k, j, i)] = theta - R.trap[R.in(k, j, i)];
   }
 
   // global interior index (z fastest) <-> (rank, local)

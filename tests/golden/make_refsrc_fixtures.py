@@ -111,6 +111,14 @@ def cases():
         p = params(n=(12, 12, 8), L=(24.0, 24.0, 16.0), prec=abi.FP64, pot=pot, dt=dt, **kw)
         nm = f"pot_{pot}{'_lbeam' if kw.get('lbeam') else ''}_fp64"
         out.append((nm, p, smooth_state(p, seed=45), 3, 1, {}, {}))
+    # the 'mobius' potential, whose Trap array mesh_init builds (initial.f90:159-198) -- only when the
+    # run does not restart, so these start from init_cond 'constant' -- a 200 x 200 sum per cell, so a
+    # small grid; 1 rank and 2 x 2 ranks (the Trap's maximum over the ranks)
+    for nproc, prec in (((1, 1), abi.FP64), ((2, 2), abi.FP64), ((1, 1), abi.FP32)):
+        p = params(n=(8, 8, 6), L=(64.0, 64.0, 16.0), prec=prec, pot="mobius", dt=0.01, nproc=nproc)
+        tag = "fp64" if prec == abi.FP64 else "fp32"
+        out.append((f"pot_mobius_np{nproc[0] * nproc[1]}_{tag}", p, None, 2, nproc[0] * nproc[1],
+                    {"init_cond": "'constant'"}, {"init": "constant"}))
     # imaginary-time Euler (run.f90:19-35) from a reference init_cond, then one RK3 step
     p = params(n=(12, 12, 8), L=(12.0, 12.0, 8.0), prec=abi.FP64, pot="harmonic", harm=(4.0, 4.0, 4.0), dt=0.01)
     p.winding_number = 1
@@ -174,6 +182,8 @@ def main(argv=None) -> int:
     ap.add_argument("--ref-src", default="/root/reference/src")
     ap.add_argument("--only", default=None, help="substring of the case names to run")
     ap.add_argument("--files-only", action="store_true", help="only refsrc_files.npz")
+    ap.add_argument("--merge", action="store_true",
+                    help="with --only: add the selected cases to the existing fixtures instead of discarding them")
     args = ap.parse_args(argv)
     if args.files_only:
         write_file_fixtures(args.ref_src)
@@ -207,6 +217,14 @@ def main(argv=None) -> int:
         shutil.rmtree(keep, ignore_errors=True)
         meta["cases"][name] = rec
         print(f"{name}: {rec['seconds']} s", flush=True)
+    if args.only and args.merge:
+        old_meta = json.load(open(os.path.join(HERE, "refsrc_cases.json")))
+        old_arrays = dict(np.load(os.path.join(HERE, "refsrc_cases.npz")))
+        old_meta["cases"].update(meta["cases"])
+        old_arrays.update(arrays)
+        np.savez_compressed(os.path.join(HERE, "refsrc_cases.npz"), **old_arrays)
+        with open(os.path.join(HERE, "refsrc_cases.json"), "w") as f:
+            json.dump(old_meta, f, indent=1, default=float)
     if not args.only:
         np.savez_compressed(os.path.join(HERE, "refsrc_cases.npz"), **arrays)
         with open(os.path.join(HERE, "refsrc_cases.json"), "w") as f:

@@ -63,9 +63,10 @@ def test_gpu_initial_states_match_reference_source(name):
     s.init_state(rec["init"])
     if "helper" in rec:
         s.init_state(rec["helper"])
-    s.step_rt(rec["steps"])   # dt = 0: the reference wrote the initial state after one step
+    s.step_rt(rec["steps"])   # dt = 0 for the initial states: the reference wrote them after one step
     ref = ARRAYS[f"{name}__psi"]
-    assert _rel(s.get_psi(), ref) < 1e-13, (name, _rel(s.get_psi(), ref))
+    tol = 1e-13 if ref.dtype == np.complex128 else 2e-6
+    assert _rel(s.get_psi(), ref) < tol, (name, _rel(s.get_psi(), ref))
     s.close()
 
 

@@ -123,12 +123,15 @@ def test_oracle_diagnostics_match_reference_output_line(name):
 
 @pytest.mark.parametrize("name", INIT_CASES)
 def test_oracle_reproduces_reference_initial_states(name):
+    """Cases that start from the reference's init_cond (the library of initial
+    states and helpers with dt = 0; the 'mobius' potential, whose Trap
+    mesh_init builds only then, with two steps)."""
     rec = CASES[name]
     o, _ = oracle_run(name, rec)
     ref = ARRAYS[f"{name}__psi"]
     got = o.get_psi()
     err = float(np.max(np.abs(got - ref)) / max(np.max(np.abs(ref)), 1e-300))
-    assert err < 1e-14, (name, err)
+    assert err < (1e-14 if ref.dtype == np.complex128 else 1e-6), (name, err)
 
 
 def test_oracle_reproduces_reference_imaginary_time_euler():

@@ -121,6 +121,79 @@ __global__ void fill_potential_kernel(PotArgs<T> a) {
   }
 }
 
+// The Trap array of the 'mobius' potential, as mesh_init builds it
+// (initial.f90:159-198): at every cell the sum over the 200 x 200 points of
+// the strip table of exp(-1.5 dx^2 - 1.5 dy^2 - 1.5 dz^2), clamped at 3 after
+// every term -- so the terms are added in the reference's order, ii1 outer,
+// ii2 inner -- then Trap = max(Trap) - Trap.  The table tab[c][ii2][ii1]
+// (200 x 200 per coordinate c) is formed on the host; the arithmetic rounds
+// once per operation as the reference's does (no contraction to FMA).
+constexpr int MOBIUS_N = 200;
+template <typename T> struct RN;
+template <> struct RN<float> {
+  static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+  static __device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
+  static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+};
+template <> struct RN<double> {
+  static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+  static __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+  static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+};
+
+template <typename T>
+__global__ void mobius_trap_kernel(const T* __restrict__ tab, const T* __restrict__ xx, const T* __restrict__ yy,
+                                   const T* __restrict__ zz, int nx, int ny, int nz, T* __restrict__ trap,
+                                   unsigned long long* __restrict__ maxbits) {
+  using R = RN<T>;
+  const size_t n = (size_t)nx * ny * nz;
+  const T* t1 = tab;
+  const T* t2 = tab + MOBIUS_N * MOBIUS_N;
+  const T* t3 = tab + 2 * MOBIUS_N * MOBIUS_N;
+  const T c15 = (T)1.5, cap = (T)3;
+  T mx = 0;
+  for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += (size_t)gridDim.x * blockDim.x) {
+    const int k = (int)(idx % nz);
+    const size_t r = idx / nz;
+    const int j = (int)(r % ny);
+    const int i = (int)(r / ny);
+    const T x = xx[i], y = yy[j], z = zz[k];
+    T acc = 0;   // Trap=0. (initial.f90:171)
+    for (int i1 = 0; i1 < MOBIUS_N; ++i1) {
+      for (int i2 = 0; i2 < MOBIUS_N; ++i2) {
+        const int q = i2 * MOBIUS_N + i1;   // mobius(ii1, ii2, c)
+        const T dx = R::sub(x, __ldg(t1 + q)), dy = R::sub(y, __ldg(t2 + q)), dz = R::sub(z, __ldg(t3 + q));
+        // -1.5*(dx)**2 - 1.5*(dy)**2 - 1.5*(dz)**2
+        T e = -R::mul(c15, R::mul(dx, dx));
+        e = R::sub(e, R::mul(c15, R::mul(dy, dy)));
+        e = R::sub(e, R::mul(c15, R::mul(dz, dz)));
+        acc = R::add(acc, exp(e));
+        if (acc > cap) acc = cap;
+      }
+    }
+    trap[idx] = acc;
+    mx = acc > mx ? acc : mx;
+  }
+  // the Trap values are non-negative, so their bit patterns order as unsigned integers
+  unsigned long long bits = sizeof(T) == 8 ? (unsigned long long)__double_as_longlong((double)mx)
+                                           : (unsigned long long)__float_as_uint((float)mx);
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long b = __shfl_down_sync(0xffffffffu, bits, o);
+    bits = b > bits ? b : bits;
+  }
+  if ((threadIdx.x & 31) == 0) atomicMax(maxbits, bits);
+}
+
+// Trap = theta - Trap with theta the maximum over all cells (the MPI_MAX
+// reduction over the ranks of initial.f90:189-197).
+template <typename T>
+__global__ void mobius_invert_kernel(T* __restrict__ trap, size_t n, const unsigned long long* __restrict__ maxbits) {
+  const unsigned long long b = *maxbits;
+  const T theta = sizeof(T) == 8 ? (T)__longlong_as_double((long long)b) : (T)__uint_as_float((unsigned int)b);
+  for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += (size_t)gridDim.x * blockDim.x)
+    trap[idx] = theta - trap[idx];
+}
+
 // ---------------------------------------------------------------- states --
 enum InitKind : int {
   IK_CONST = 0, IK_TF = 1, IK_SOLITON_PHASE = 2, IK_VORTEX_MUL = 3, IK_SINGLE = 4,

@@ -159,12 +159,58 @@ template <typename T> int pot_mode_at(trapbec_ctx* c, double t) {
   return POT_ARR;
 }
 
+// The 'mobius' potential's Trap array, built once on the device as mesh_init
+// builds it (initial.f90:159-198): the 200 x 200 strip table is formed here
+// in the context precision with the reference's expressions (pi =
+// 3.14159265359 as in cdata.f90:13), the sums and the inversion by
+// mobius_trap_kernel / mobius_invert_kernel.  It becomes the context's Trap
+// (a later trapbec_set_trap replaces it).
+template <typename T> int build_mobius_trap(trapbec_ctx* c) {
+  const int N = MOBIUS_N;
+  std::vector<T> tab((size_t)3 * N * N);
+  const T pi = (T)3.14159265359;
+  for (int i = 1; i <= N; ++i)
+    for (int j = 1; j <= N; ++j) {
+      const T r = (T)(i - 1) * (T)2 / (T)200 - (T)1;          // r=real(i-1)*2./200-1
+      const T theta = (T)(j - 1) * (T)2 * pi / (T)200;       // theta=real(j-1)*2.*pi/200
+      const T h = theta / (T)2;
+      const T ring = (T)25 + (T)5 * r * std::cos(h);         // (25.+5*r*cos(theta/2))
+      const size_t q = (size_t)(j - 1) * N + (i - 1);
+      tab[q] = ring * std::cos(theta);
+      tab[(size_t)N * N + q] = ring * std::sin(theta);
+      tab[(size_t)2 * N * N + q] = (T)5 * r * std::sin(h);   // 5*r*sin(theta/2)
+    }
+  void* d_tab = nullptr;
+  unsigned long long* d_max = nullptr;
+  CK(cudaMalloc(&d_tab, tab.size() * sizeof(T)));
+  CK(cudaMalloc(&d_max, sizeof(unsigned long long)));
+  if (!c->trap_user) CK(cudaMalloc(&c->trap_user, c->n * sizeof(T)));
+  CK(cudaMemcpyAsync(d_tab, tab.data(), tab.size() * sizeof(T), cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemsetAsync(d_max, 0, sizeof(unsigned long long), c->st));
+  const trapbec_params& p = c->p;
+  mobius_trap_kernel<T><<<simple_grid(c), SIMPLE_THREADS, 0, c->st>>>(
+      (const T*)d_tab, (const T*)c->xx, (const T*)c->yy, (const T*)c->zz, p.nx, p.ny, p.nz, (T*)c->trap_user, d_max);
+  CKL();
+  mobius_invert_kernel<T><<<simple_grid(c), SIMPLE_THREADS, 0, c->st>>>((T*)c->trap_user, c->n, d_max);
+  CKL();
+  c->launches += 2;
+  CK(cudaStreamSynchronize(c->st));
+  cudaFree(d_tab);
+  cudaFree(d_max);
+  c->pot_valid = false;
+  return TRAPBEC_OK;
+}
+
 template <typename T> int ensure_potential(trapbec_ctx* c, double t) {
   if (pot_mode_at<T>(c, t) != POT_ARR) return TRAPBEC_OK;
   const trapbec_params& p = c->p;
   bool tdep = pot_time_dependent(p.potential);
   if (c->pot_valid && (!tdep || c->pot_t == t)) return TRAPBEC_OK;
-  if ((p.potential == TRAPBEC_POT_MOBIUS || p.potential == TRAPBEC_POT_ARRAY) && !c->trap_user) {
+  if (p.potential == TRAPBEC_POT_MOBIUS && !c->trap_user) {
+    int rc = build_mobius_trap<T>(c);   // mesh_init's Trap of the 'mobius' potential
+    if (rc) return rc;
+  }
+  if (p.potential == TRAPBEC_POT_ARRAY && !c->trap_user) {
     set_error("potential needs a Trap array: call trapbec_set_trap first");
     return TRAPBEC_ERR_STATE;
   }
