@@ -10,8 +10,8 @@ uses executed statement by statement by the interpreter, on 1 rank or on a
 process grid of virtual MPI ranks.
 
 Only the fixture generator (tests/golden/make_refsrc_fixtures.py) calls
-this, in the container where the reference's sources are present; the tests
-read the fixtures it writes.
+this, where the reference's sources are present; the tests read the
+fixtures it writes.
 """
 from __future__ import annotations
 
