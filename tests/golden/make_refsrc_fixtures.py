@@ -111,6 +111,16 @@ def cases():
         p = params(n=(12, 12, 8), L=(24.0, 24.0, 16.0), prec=abi.FP64, pot=pot, dt=dt, **kw)
         nm = f"pot_{pot}{'_lbeam' if kw.get('lbeam') else ''}_fp64"
         out.append((nm, p, smooth_state(p, seed=45), 3, 1, {}, {}))
+    # the set-up of the reference's own cparam.local (src/cparam.local:1-44): a 2D run (Nz = 1,
+    # two_dim, periodic z) in a quartic trap with the laser, FP32 as shipped and FP64; and the
+    # second ring potential
+    for prec in (abi.FP32, abi.FP64):
+        p = params(n=(16, 16, 1), L=(32.0, 32.0, 1.0), prec=prec, pot="quartic", harm=(900.0, 8.0, 6.0),
+                   periodicz=1, two_dim=1, lbeam=1, gamma=0.003, dt=0.01, nproc=(2, 2))
+        tag = "fp64" if prec == abi.FP64 else "fp32"
+        out.append((f"sample2d_np4_{tag}", p, smooth_state(p, seed=48), 4, 4, {}, {}))
+    p = params(n=(12, 12, 8), L=(24.0, 24.0, 16.0), prec=abi.FP64, pot="harmonic_ring2", dt=0.01)
+    out.append(("pot_harmonic_ring2_fp64", p, smooth_state(p, seed=49), 3, 1, {}, {}))
     # the 'mobius' potential, whose Trap array mesh_init builds (initial.f90:159-198) -- only when the
     # run does not restart, so these start from init_cond 'constant' -- a 200 x 200 sum per cell, so a
     # small grid; 1 rank and 2 x 2 ranks (the Trap's maximum over the ranks)
