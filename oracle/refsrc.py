@@ -23,17 +23,11 @@ from oracle import fortran_subset as fs
 from oracle import refbin_parity as rb
 
 
-def run_reference(ref_src: str, p, psi0, steps: int, nprocs: int, fp64: bool, shots: int | None = None,
-                  cparam_overrides: dict | None = None, keep: str | None = None) -> dict:
-    """Run the reference's `program run` for `steps` real-time RK3 steps of
-    trapbec_params `p` from the global start state `psi0[x, y, z]` (through
-    the restart files; None: the cparam's init_cond), on `nprocs` virtual
-    ranks, in the FP64 build (`-fdefault-real-8 -fdefault-double-8`) or the
-    shipped FP32 one.  Returns the gathered psi of the last output, its t,
-    and rank 0's standard output lines."""
-    shots = shots or steps
+def cparam_for(p, steps: int, shots: int, overrides: dict | None = None) -> str:
+    """The cparam.local of oracle/refbin_parity.py for trapbec_params `p`
+    with some of its values replaced (name -> Fortran literal)."""
     text = rb.cparam_text(p, nsteps=steps, shots=shots)
-    for name, value in (cparam_overrides or {}).items():
+    for name, value in (overrides or {}).items():
         lines = text.splitlines()
         for i, ln in enumerate(lines):
             if f":: {name}=" in ln:
@@ -43,6 +37,19 @@ def run_reference(ref_src: str, p, psi0, steps: int, nprocs: int, fp64: bool, sh
         else:
             raise ValueError(f"cparam.local has no {name}")
         text = "\n".join(lines) + "\n"
+    return text
+
+
+def run_reference(ref_src: str, p, psi0, steps: int, nprocs: int, fp64: bool, shots: int | None = None,
+                  cparam_overrides: dict | None = None, keep: str | None = None) -> dict:
+    """Run the reference's `program run` for `steps` real-time RK3 steps of
+    trapbec_params `p` from the global start state `psi0[x, y, z]` (through
+    the restart files; None: the cparam's init_cond), on `nprocs` virtual
+    ranks, in the FP64 build (`-fdefault-real-8 -fdefault-double-8`) or the
+    shipped FP32 one.  Returns the gathered psi of the last output, its t,
+    and rank 0's standard output lines."""
+    shots = shots or steps
+    text = cparam_for(p, steps, shots, cparam_overrides)
     work = keep or tempfile.mkdtemp(prefix="refsrc_")
     try:
         datadir = os.path.join(work, "data")

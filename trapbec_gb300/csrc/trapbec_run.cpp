@@ -74,8 +74,12 @@ bool file_exists(const std::string& p) {
   return ::stat(p.c_str(), &st) == 0;
 }
 
+// List-directed output of a real of the build's kind: 9 significant digits
+// for the shipped single-precision build, 17 for the -fdefault-real-8 one.
+void put_real(FILE* f, double v, bool f64) { std::fprintf(f, f64 ? " %25.16E" : " %16.8E", v); }
+
 // 2D_slice##.log of var_print (output.f90:92-101): x, y, |Psi(z=1)|^2 per
-// line, a blank line after each x; list-directed output written as %16.8E.
+// line, a blank line after each x; list-directed output of the build's kind.
 void write_2d_slice(trapbec_ctx* ctx, const trapbec_params& p, const std::string& datadir, int q) {
   const bool f64 = p.precision == TRAPBEC_FP64;
   const size_t n = (size_t)p.nx * p.ny * p.nz;
@@ -100,7 +104,10 @@ void write_2d_slice(trapbec_ctx* ctx, const trapbec_params& p, const std::string
       const double y = (2.0 * (j + 1) - 1) / (2.0 * p.ny) * p.ly - p.ly / 2.0;
       const size_t c = ((size_t)i * p.ny + j) * p.nz;   // k = 1
       const double a2 = psi[2 * c] * psi[2 * c] + psi[2 * c + 1] * psi[2 * c + 1];
-      std::fprintf(f, " %16.8E %16.8E %16.8E\n", x, y, a2);
+      put_real(f, x, f64);
+      put_real(f, y, f64);
+      put_real(f, a2, f64);
+      std::fprintf(f, "\n");
     }
     std::fprintf(f, "\n");
   }
@@ -187,7 +194,9 @@ int main(int argc, char** argv) {
       itime += k;
       const int last = itime - 1;
       if (last % rc.shots == 0) {
-        std::printf(" %12d %16.8E\n", last / rc.shots, ratio);
+        std::printf(" %12d", last / rc.shots);
+        put_real(stdout, ratio, p.precision == TRAPBEC_FP64);
+        std::printf("\n");
         if (rc.imaginary_output)
           check(trapbec_write_var(ctx, datadir.c_str(), last, rc.shots, t, 1), "imaginary_print");
       }
@@ -218,8 +227,9 @@ int main(int argc, char** argv) {
     if (last % rc.shots == 0) {
       trapbec_diag_out d;
       check(trapbec_diag(ctx, &d), "Psi_info/Psi_norm");
-      std::printf(" %12d %16.8E %16.8E %16.8E %16.8E %16.8E\n", last / rc.shots, t, d.maxpsi, d.minpsi, d.meanpsi,
-                  d.intpsi2);
+      std::printf(" %12d", last / rc.shots);   // run.f90:62
+      for (double v : {t, d.maxpsi, d.minpsi, d.meanpsi, d.intpsi2}) put_real(stdout, v, p.precision == TRAPBEC_FP64);
+      std::printf("\n");
       if (d.nonfinite) emergency_stop("non-finite values in Psi");
       // run.f90:64-66 computes the diagnostics, output.f90:73-91 writes them
       if (rc.full_binary_output) check(trapbec_write_var(ctx, datadir.c_str(), last, rc.shots, t, 0), "var_print");
