@@ -101,6 +101,18 @@ def cases():
         # advective frame
         p = params(n=(12, 12, 8), L=(6.0, 6.0, 4.0), prec=prec, pot="zero", periodicz=1, vx=0.25, dt=0.01)
         out.append((f"advective_{tag}", p, smooth_state(p, seed=44), 5, 1, {}, {}))
+    # other process grids: 2 ranks (MPI_DIMS_CREATE gives 2 x 1) and 8 ranks (4 x 2)
+    for nprocs in (2, 8):
+        dims = rb.mpi_dims_create(nprocs)
+        p, psi0 = _line16(abi.FP64, dims)
+        out.append((f"line16_np{nprocs}_fp64", p, psi0, 6, nprocs, {}, {}))
+    # the time switches of get_rhs: the potential off after potential_off (finite_diff.f90:124) and
+    # the rotating frame off after t_spindown (finite_diff.f90:128), both inside the run
+    p = params(n=(12, 12, 8), L=(6.0, 6.0, 4.0), prec=abi.FP64, pot="harmonic", harm=(3.0, 4.0, 5.0), omega=0.3,
+               dt=0.01)
+    p.potential_off = 0.015
+    p.t_spindown = 0.025
+    out.append(("switches_fp64", p, smooth_state(p, seed=50), 4, 1, {}, {}))
     # the potential library and the laser, FP64, 1 rank
     pots = [("barrier", dict(gamma=0.01, dt=0.02, bc=abi.BC_SOLID)), ("box_trap", {}), ("channel", {}),
             ("quartic", dict(harm=(900.0, 8.0, 6.0))), ("sphere", {}), ("harmonic_ring", dict(harm=(50.0, 0, 0))),
