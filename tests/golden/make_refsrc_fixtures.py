@@ -101,6 +101,12 @@ def cases():
         # advective frame
         p = params(n=(12, 12, 8), L=(6.0, 6.0, 4.0), prec=prec, pot="zero", periodicz=1, vx=0.25, dt=0.01)
         out.append((f"advective_{tag}", p, smooth_state(p, seed=44), 5, 1, {}, {}))
+    # the vortex-line workload at its own size (64^3 on [-16, 16]^3), 3 steps, 1 rank; only a
+    # seeded sample of 4096 cells of the final state is kept (with the printed diagnostics line)
+    prob, init = units.vortex_line_64(abi.FP64)
+    p = prob.to_params()
+    psi0 = rb.start_state(p, init)
+    out.append(("line64_np1_fp64", p, psi0, 3, 1, {}, {"sample": 4096, "start": "tf_vortex_line"}))
     # other process grids: 2 ranks (MPI_DIMS_CREATE gives 2 x 1) and 8 ranks (4 x 2)
     for nprocs in (2, 8):
         dims = rb.mpi_dims_create(nprocs)
@@ -147,6 +153,14 @@ def cases():
     out.append(("imag_euler_fp64", p, None, 1, 1,
                 {"init_cond": "'single_vortex'", "imaginary_time": ".true.", "imag_nsteps": "6"},
                 {"imag_steps": 6}))
+    # imaginary time with the phase imprint after every step (run.f90:26) and the imag_var files
+    # (output.f90:55-62), from single_vortex; checked through the program-run driver
+    p = params(n=(12, 12, 8), L=(12.0, 12.0, 8.0), prec=abi.FP64, pot="harmonic", harm=(4.0, 4.0, 4.0), dt=0.01)
+    p.winding_number = 2
+    out.append(("imag_imprint_fp64", p, None, 1, 1,
+                {"init_cond": "'single_vortex'", "imaginary_time": ".true.", "imag_nsteps": "4",
+                 "phase_imprint_on": ".true.", "imaginary_output": ".true."},
+                {"imag_steps": 4, "imag_file": True}))
     # the init_cond library: dt = 0, one step, so var0001.dat holds the initial state
     for ic, extra_p in (("constant", {}), ("soliton", {}), ("single_vortex", {"winding_number": 2}),
                         ("sausage", {}), ("crow", {}), ("leap_frog", {}), ("line_of_lines", {"ring_rad": 4.0}),
@@ -229,9 +243,21 @@ def main(argv=None) -> int:
         rec = {"params": _pdict(p), "steps": steps, "nprocs": nprocs, "dims": list(r["dims"]), "t": r["t"],
                "cparam_overrides": over, "stdout": r["stdout"], "seconds": round(time.time() - t0, 1)}
         rec.update(extra)
-        if psi0 is not None:
-            arrays[f"{name}__psi0"] = psi0.astype(np.complex128 if fp64 else np.complex64)
-        arrays[f"{name}__psi"] = r["psi"]
+        if extra.get("sample"):
+            # large grid: the start state is the workload's own (rebuilt by the tests), and the
+            # final state is kept at a seeded sample of cells
+            idx = np.sort(np.random.default_rng(7).choice(r["psi"].size, extra["sample"], replace=False))
+            arrays[f"{name}__idx"] = idx
+            arrays[f"{name}__psi_sample"] = r["psi"].ravel()[idx]
+        else:
+            if psi0 is not None:
+                arrays[f"{name}__psi0"] = psi0.astype(np.complex128 if fp64 else np.complex64)
+            arrays[f"{name}__psi"] = r["psi"]
+        if extra.get("imag_file"):
+            # the last imag_var####.dat (itime/shots = imag_steps with shots = 1), rank 0's record
+            _, _, blk = rb.read_var(os.path.join(keep, "data", "proc000", "imag_var%04d.dat" % extra["imag_steps"]),
+                                    (p.nx, p.ny, p.nz), fp64)
+            arrays[f"{name}__psi_imag"] = np.array(blk)
         if extra.get("diag"):
             n = (p.nx, p.ny, p.nz)
             arrays[f"{name}__vel"] = _read_field(os.path.join(keep, "data"), "vel01.dat", n, nprocs, fp64)

@@ -18,7 +18,7 @@ import pytest
 from oracle import refbin_parity as rb
 from oracle.refsrc import cparam_for
 from trapbec_gb300 import abi
-from tests.test_refsrc_golden import ARRAYS, CASES, case_params, printed_output_line
+from tests.test_refsrc_golden import ARRAYS, CASES, case_params, printed_output_line, reference_state, start_psi
 
 pytestmark = pytest.mark.gpu
 
@@ -41,16 +41,17 @@ def test_driver_reproduces_reference_program_run(name, tmp_path):
     (tmp_path / "cparam.local").write_text(cparam_for(p, steps, steps, rec["cparam_overrides"]))
     data = tmp_path / "data"
     os.makedirs(data / "proc000", exist_ok=True)
-    if f"{name}__psi0" in ARRAYS.files:
-        rb.write_restart(str(data), ARRAYS[f"{name}__psi0"], 1, fp64)
+    psi0 = start_psi(name, rec)
+    if psi0 is not None:
+        rb.write_restart(str(data), psi0.astype(np.complex128 if fp64 else np.complex64), 1, fp64)
     env = dict(os.environ, TRAPBEC_PRECISION="1" if fp64 else "0")
     r = subprocess.run([DRIVER, "cparam.local", "data"], cwd=tmp_path, capture_output=True, text=True, env=env,
                        timeout=600)
     assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
     n = (p.nx, p.ny, p.nz)
     psi, t = rb.gather(str(data), 1, n, 1, fp64)
-    ref = ARRAYS[f"{name}__psi"]
-    err = float(np.max(np.abs(psi.astype(np.complex128) - ref)) / np.max(np.abs(ref)))
+    got, ref = reference_state(name, psi.astype(np.complex128))
+    err = float(np.max(np.abs(got - ref)) / np.max(np.abs(ref)))
     assert err < (1e-12 if fp64 else 2e-6), (name, err)
     assert t == pytest.approx(rec["t"], rel=1e-6 if not fp64 else 1e-14)
     # the output line itime/shots, t, maxPsi, minPsi, meanPsi, intPsi2 (run.f90:62)
@@ -63,6 +64,11 @@ def test_driver_reproduces_reference_program_run(name, tmp_path):
     tols = [1e-12] * 5 if fp64 else [2e-6, 2e-6, 2e-6, 1e-5, 1e-5]
     for a, b, tol in zip(got, want, tols):
         assert abs(a - b) <= tol * max(abs(b), want[1]), (name, got, want)
+    if rec.get("imag_file"):
+        # the imag_var####.dat the imaginary loop wrote after its last step (output.f90:55-62)
+        _, _, blk = rb.read_var(str(data / "proc000" / ("imag_var%04d.dat" % rec["imag_steps"])), n, fp64)
+        want = ARRAYS[f"{name}__psi_imag"]
+        assert float(np.max(np.abs(blk - want)) / np.max(np.abs(want))) < 1e-12
     if rec.get("diag"):
         for f, kind in (("vel01.dat", "vel"), ("qpress01.dat", "qpress")):
             got_f = _field(str(data / "proc000" / f), fp64, n)

@@ -16,7 +16,8 @@ import numpy as np
 import pytest
 
 from trapbec_gb300 import Solver, abi
-from tests.test_refsrc_golden import ARRAYS, CASES, STEP_CASES, INIT_CASES, case_params, printed_output_line
+from tests.test_refsrc_golden import (ARRAYS, CASES, STEP_CASES, INIT_CASES, case_params, printed_output_line,
+                                      reference_state, start_psi)
 
 pytestmark = pytest.mark.gpu
 
@@ -38,10 +39,10 @@ def test_gpu_time_stepping_matches_reference_source(name, form):
     p = case_params(rec)
     s = Solver(p)
     s.set_stage_form(form)
-    s.set_psi(ARRAYS[f"{name}__psi0"])
+    s.set_psi(start_psi(name, rec))
     s.step_rt(rec["steps"])
-    ref = ARRAYS[f"{name}__psi"].astype(np.complex128)
-    got = s.get_psi().astype(np.complex128)
+    got, ref = reference_state(name, s.get_psi().astype(np.complex128))
+    ref = ref.astype(np.complex128)
     if p.precision == abi.FP64:
         assert _rel(got, ref) < FP64_TOL, (name, _rel(got, ref))
     else:
@@ -70,13 +71,19 @@ def test_gpu_initial_states_match_reference_source(name):
     s.close()
 
 
-def test_gpu_imaginary_time_euler_matches_reference_source():
-    name = "imag_euler_fp64"
+@pytest.mark.parametrize("name", [n for n, r in CASES.items() if "imag_steps" in r])
+def test_gpu_imaginary_time_euler_matches_reference_source(name):
     rec = CASES[name]
     s = Solver(case_params(rec))
     s.init_state("single_vortex")
-    steps, ratio = s.step_imag(rec["imag_steps"], abi.IMAG_REF_EULER)
-    assert steps == rec["imag_steps"]
+    if rec["cparam_overrides"].get("phase_imprint_on") == ".true.":
+        for _ in range(rec["imag_steps"]):   # run.f90:21-26: Euler step, Psi_norm, phase_imprint
+            steps, ratio = s.step_imag(1, abi.IMAG_REF_EULER)
+            s.init_state("phase_imprint")
+        assert _rel(s.get_psi(), ARRAYS[f"{name}__psi_imag"]) < FP64_TOL
+    else:
+        steps, ratio = s.step_imag(rec["imag_steps"], abi.IMAG_REF_EULER)
+        assert steps == rec["imag_steps"]
     rows = [ln.split() for ln in rec["stdout"]]
     ratios = [float(r[1]) for r in rows if len(r) == 2 and r[0].isdigit()]
     assert ratio == pytest.approx(ratios[-1], rel=1e-12)
