@@ -191,6 +191,33 @@ int trapbec_get_rhs(trapbec_ctx* ctx, void* rhs_out);
  * step.  Replaces run.f90:42-57 (one call per `shots` block).            */
 int trapbec_step_rt(trapbec_ctx* ctx, int nsteps, double* t_inout);
 
+/* Overlapped host copies: the state of the next `shots` block goes up and
+ * the last block's result comes back while the GPU steps, the way run.f90
+ * would overlap its restart read and its var####.dat output (run.f90:45-66,
+ * output.f90:64-75) with the next block if the copies were asynchronous.
+ * Interior layout only; the host arrays should be pinned for the copies to
+ * run concurrently with the steps.
+ *  trapbec_set_psi_async : queue `psi`: it is copied to the device at once on
+ *      a copy stream and becomes the state at the start of the next
+ *      time-stepping call (trapbec_step_rt / _async, trapbec_step_imag);
+ *      until then the current state is unchanged and may still be read.
+ *      trapbec_set_psi, trapbec_init_state and trapbec_read_restart replace a
+ *      queued state.  `psi` must stay unchanged until trapbec_synchronize.
+ *  trapbec_get_psi_async : snapshot the current state on the device (after
+ *      all queued steps) and copy the snapshot to `psi` on a copy stream;
+ *      `psi` holds it after trapbec_wait_psi or trapbec_synchronize.
+ *  trapbec_step_rt_async : trapbec_step_rt that returns once the steps are
+ *      queued (*t_inout advanced already); their kernel time and a timed-out
+ *      device wait are reported by trapbec_synchronize or by the next call
+ *      that waits (trapbec_diag, trapbec_get_psi, trapbec_step_rt, ...).
+ *  trapbec_wait_psi      : wait for the copy of the last trapbec_get_psi_async.
+ *  trapbec_synchronize   : wait for all queued steps and copies.           */
+int trapbec_set_psi_async(trapbec_ctx* ctx, const void* psi, int layout);
+int trapbec_get_psi_async(trapbec_ctx* ctx, void* psi, int layout);
+int trapbec_step_rt_async(trapbec_ctx* ctx, int nsteps, double* t_inout);
+int trapbec_wait_psi(trapbec_ctx* ctx);
+int trapbec_synchronize(trapbec_ctx* ctx);
+
 /* Imaginary-time relaxation.
  *  REF_EULER : nsteps of Psi = Psi + dt*0.5*rhs (run.f90:19-35); *stat_out
  *              receives the last norm ratio intPsi2/intPsi2_old (run.f90:23).

@@ -132,6 +132,11 @@ _PROTOS = {
     "trapbec_init_state": (C.c_int, [_VP, C.c_char_p, C.POINTER(InitArgs)]),
     "trapbec_get_rhs": (C.c_int, [_VP, _VP]),
     "trapbec_step_rt": (C.c_int, [_VP, C.c_int, C.POINTER(C.c_double)]),
+    "trapbec_set_psi_async": (C.c_int, [_VP, _VP, C.c_int]),
+    "trapbec_get_psi_async": (C.c_int, [_VP, _VP, C.c_int]),
+    "trapbec_step_rt_async": (C.c_int, [_VP, C.c_int, C.POINTER(C.c_double)]),
+    "trapbec_wait_psi": (C.c_int, [_VP]),
+    "trapbec_synchronize": (C.c_int, [_VP]),
     "trapbec_step_imag": (C.c_int, [_VP, C.c_int, C.c_int, C.c_double,
                                     C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     "trapbec_set_imag_stop": (C.c_int, [_VP, C.c_int, C.c_double]),

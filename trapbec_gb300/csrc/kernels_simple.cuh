@@ -249,4 +249,30 @@ __global__ void scale_kernel(c_t<T>* __restrict__ psi, size_t n, T s) {
   }
 }
 
+// dst = src for a state array of n16 16-byte words and, when tail8, one
+// trailing 8-byte word (a complex FP32 array of odd length): the device-side
+// half of the overlapped host copies (queued state into psi, psi into the
+// read-back snapshot).  Four independent 16-byte loads in flight per thread,
+// streaming cache hints (the arrays are far larger than L2).
+constexpr int COPY_THREADS = 512, COPY_UNROLL = 4;
+static __global__ void __launch_bounds__(COPY_THREADS) copy_state_kernel(const uint4* __restrict__ src,
+                                                                   uint4* __restrict__ dst, size_t n16, int tail8) {
+  const size_t step = (size_t)gridDim.x * COPY_THREADS * COPY_UNROLL;
+  for (size_t base = (size_t)blockIdx.x * COPY_THREADS * COPY_UNROLL + threadIdx.x; base < n16; base += step) {
+    uint4 v[COPY_UNROLL];
+#pragma unroll
+    for (int u = 0; u < COPY_UNROLL; ++u) {
+      const size_t j = base + (size_t)u * COPY_THREADS;
+      if (j < n16) v[u] = __ldcs(src + j);
+    }
+#pragma unroll
+    for (int u = 0; u < COPY_UNROLL; ++u) {
+      const size_t j = base + (size_t)u * COPY_THREADS;
+      if (j < n16) __stcs(dst + j, v[u]);
+    }
+  }
+  if (tail8 && blockIdx.x == 0 && threadIdx.x == 0)
+    *reinterpret_cast<uint2*>(dst + n16) = *reinterpret_cast<const uint2*>(src + n16);
+}
+
 }  // namespace tb

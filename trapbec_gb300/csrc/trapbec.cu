@@ -109,6 +109,24 @@ struct trapbec_ctx {
   double imag_escale = 0.0;            // its energy scale (absolute modes)
   void* lo = nullptr;                  // rounding remainder of psi (compensated form, allocated on request)
   bool lo_valid = false;               // lo belongs to the current psi (else it is cleared before use)
+  // Overlapped host copies (trapbec_set_psi_async / trapbec_get_psi_async /
+  // trapbec_step_rt_async), created on first use.  A queued state goes host ->
+  // `stage` on cs_in while earlier steps run and is copied into psi on the
+  // context stream at the next time-stepping call; a read-back copies psi into
+  // `snap` on the context stream and snap -> host on cs_out while later steps
+  // run.  The events order the two device buffers between the streams.
+  cudaStream_t cs_in = nullptr, cs_out = nullptr;
+  void* stage = nullptr;
+  void* snap = nullptr;
+  cudaEvent_t ev_staged = nullptr;      // cs_in: the queued state has landed in stage
+  cudaEvent_t ev_stage_free = nullptr;  // st: stage was copied into psi (may be overwritten)
+  cudaEvent_t ev_snap_ready = nullptr;  // st: snap holds the state to read back
+  cudaEvent_t ev_snap_drained = nullptr;   // cs_out: snap reached the host (may be overwritten)
+  bool stage_free_rec = false, snap_drained_rec = false;   // those two events have been recorded
+  bool staged_pending = false;         // a queued state replaces psi at the next time-stepping call
+  bool out_pending = false;            // a read-back is in flight
+  bool step_async = false;             // do_step_rt returns after queueing (trapbec_step_rt_async)
+  bool steps_pending = false;          // queued steps not yet waited for (timing and error flag unread)
 };
 
 namespace {
@@ -329,6 +347,63 @@ int check_device_error(trapbec_ctx* c) {
   return TRAPBEC_OK;
 }
 
+// Wait for steps queued by trapbec_step_rt_async: their kernel time and the
+// tiled kernel's error flag.
+int finish_steps(trapbec_ctx* c) {
+  if (!c->steps_pending) return TRAPBEC_OK;
+  c->steps_pending = false;
+  CK(cudaEventSynchronize(c->e1));
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, c->e0, c->e1));
+  c->last_ms = ms;
+  return check_device_error(c);
+}
+
+// Copy streams, events and the staging buffer of the overlapped host copies.
+int ensure_async(trapbec_ctx* c, bool stage, bool snap) {
+  if (!c->cs_in) {
+    CK(cudaStreamCreateWithFlags(&c->cs_in, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&c->cs_out, cudaStreamNonBlocking));
+    for (cudaEvent_t* e : {&c->ev_staged, &c->ev_stage_free, &c->ev_snap_ready, &c->ev_snap_drained})
+      CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+  }
+  if (stage && !c->stage) CK(cudaMalloc(&c->stage, c->n * c->esz));
+  if (snap && !c->snap) CK(cudaMalloc(&c->snap, c->n * c->esz));
+  return TRAPBEC_OK;
+}
+
+// dst = src (one state array) on the context stream.
+int copy_state(trapbec_ctx* c, void* dst, const void* src) {
+  const size_t bytes = c->n * c->esz;
+  copy_state_kernel<<<4 * c->nsm, COPY_THREADS, 0, c->st>>>((const uint4*)src, (uint4*)dst, bytes / 16,
+                                                            (int)((bytes % 16) != 0));
+  CKL();
+  c->launches++;
+  return TRAPBEC_OK;
+}
+
+// A state queued by trapbec_set_psi_async becomes psi: the context stream
+// waits for its host copy, copies it in, and the state's bookkeeping is that
+// of trapbec_set_psi.
+int apply_staged(trapbec_ctx* c) {
+  if (!c->staged_pending) return TRAPBEC_OK;
+  c->staged_pending = false;
+  CK(cudaStreamWaitEvent(c->st, c->ev_staged, 0));
+  int rc = copy_state(c, c->psi[c->cur], c->stage);
+  if (rc) return rc;
+  CK(cudaEventRecord(c->ev_stage_free, c->st));
+  c->stage_free_rec = true;
+  psi_changed(c);
+  if (!c->norm_user) c->norm_target = -1.0;
+  if (c->ctrl_init) {  // a new state cancels any pending renormalisation
+    c->host_ctrl->scale = 1.0;
+    c->host_ctrl->have_prev = 0;
+    CK(cudaMemcpyAsync(c->ctrl, c->host_ctrl, sizeof(ImagCtrl), cudaMemcpyHostToDevice, c->st));
+    CK(cudaStreamSynchronize(c->st));
+  }
+  return TRAPBEC_OK;
+}
+
 // Launch one stage.  kind: StageKind or 4 (diagnostics).  Returns status.
 template <typename T>
 int launch_stage(trapbec_ctx* c, int kind, StageArgs<T>& a, int* nblk_out) {
@@ -519,11 +594,16 @@ template <typename T> int do_step_rt(trapbec_ctx* c, int nsteps) {
     c->t = (double)((T)c->t + dcr);   // run.f90:55, t real
   }
   CK(cudaEventRecord(c->e1, c->st));
+  if (comp) c->lo_valid = true;
+  if (c->step_async) {   // trapbec_step_rt_async: the steps are queued; finish_steps reads the rest
+    c->steps_pending = true;
+    return TRAPBEC_OK;
+  }
+  c->steps_pending = false;
   CK(cudaEventSynchronize(c->e1));
   float ms = 0;
   CK(cudaEventElapsedTime(&ms, c->e0, c->e1));
   c->last_ms = ms;
-  if (comp) c->lo_valid = true;
   return check_device_error(c);
 }
 
@@ -870,14 +950,18 @@ template <typename T> int create_impl(trapbec_ctx* c) {
 
 void free_ctx(trapbec_ctx* c) {
   if (!c) return;
+  if (c->cs_in) cudaStreamSynchronize(c->cs_in);
+  if (c->cs_out) cudaStreamSynchronize(c->cs_out);
   void* bufs[] = {c->psi[0], c->psi[1], c->w, c->w2, c->lo, c->xx, c->yy, c->zz, c->px, c->py, c->pz,
-                  c->trap_user, c->trap_eff, c->red, c->red_out, c->ctrl, c->d_err};
+                  c->trap_user, c->trap_eff, c->red, c->red_out, c->ctrl, c->d_err, c->stage, c->snap};
   for (void* b : bufs) if (b) cudaFree(b);
   if (c->host_red) cudaFreeHost(c->host_red);
   if (c->h_err) cudaFreeHost(c->h_err);
   if (c->host_ctrl) cudaFreeHost(c->host_ctrl);
-  if (c->e0) cudaEventDestroy(c->e0);
-  if (c->e1) cudaEventDestroy(c->e1);
+  for (cudaEvent_t e : {c->e0, c->e1, c->ev_staged, c->ev_stage_free, c->ev_snap_ready, c->ev_snap_drained})
+    if (e) cudaEventDestroy(e);
+  if (c->cs_in) cudaStreamDestroy(c->cs_in);
+  if (c->cs_out) cudaStreamDestroy(c->cs_out);
   if (c->st) cudaStreamDestroy(c->st);
   delete c;
 }
@@ -1029,12 +1113,15 @@ int trapbec_create(const trapbec_params* p, trapbec_ctx** out) {
 }
 
 void trapbec_destroy(trapbec_ctx* c) {
-  if (c && c->st) cudaStreamSynchronize(c->st);
+  if (c && c->st) cudaStreamSynchronize(c->st);   // free_ctx also waits for the copy streams
   free_ctx(c);
 }
 
 int trapbec_set_psi(trapbec_ctx* c, const void* psi, int layout) {
   if (!c || !psi) return TRAPBEC_ERR_ARG;
+  int rc0 = finish_steps(c);
+  if (rc0) return rc0;
+  c->staged_pending = false;   // this state replaces a queued one
   psi_changed(c);
   if (layout == TRAPBEC_LAYOUT_INTERIOR) {
     CK(cudaMemcpyAsync(c->psi[c->cur], psi, c->n * c->esz, cudaMemcpyHostToDevice, c->st));
@@ -1059,7 +1146,9 @@ int trapbec_set_psi(trapbec_ctx* c, const void* psi, int layout) {
 
 int trapbec_get_psi(trapbec_ctx* c, void* psi, int layout) {
   if (!c || !psi) return TRAPBEC_ERR_ARG;
-  int rc = DISPATCH(c, apply_pending_scale, c);
+  int rc = finish_steps(c);
+  if (rc) return rc;
+  rc = DISPATCH(c, apply_pending_scale, c);
   if (rc) return rc;
   if (layout == TRAPBEC_LAYOUT_INTERIOR) {
     CK(cudaMemcpyAsync(psi, c->psi[c->cur], c->n * c->esz, cudaMemcpyDeviceToHost, c->st));
@@ -1095,7 +1184,10 @@ int trapbec_set_trap(trapbec_ctx* c, const double* trap) {
 
 int trapbec_init_state(trapbec_ctx* c, const char* name, const trapbec_init_args* args) {
   if (!c || !name) return TRAPBEC_ERR_ARG;
-  int rc = DISPATCH(c, init_state_impl, c, name, args);
+  int rc = finish_steps(c);
+  if (rc) return rc;
+  c->staged_pending = false;   // this state replaces a queued one
+  rc = DISPATCH(c, init_state_impl, c, name, args);
   if (rc) return rc;
   if (!c->norm_user) c->norm_target = -1.0;   // the next relaxation keeps the new state's norm
   if (c->ctrl_init) {
@@ -1133,9 +1225,78 @@ int trapbec_get_rhs(trapbec_ctx* c, void* rhs_out) {
 
 int trapbec_step_rt(trapbec_ctx* c, int nsteps, double* t_inout) {
   if (!c || nsteps < 0) return TRAPBEC_ERR_ARG;
+  int rc = finish_steps(c);
+  if (rc) return rc;
+  if ((rc = apply_staged(c))) return rc;
   if (t_inout) c->t = *t_inout;
-  int rc = DISPATCH(c, do_step_rt, c, nsteps);
+  rc = DISPATCH(c, do_step_rt, c, nsteps);
   if (t_inout) *t_inout = c->t;
+  return rc;
+}
+
+int trapbec_step_rt_async(trapbec_ctx* c, int nsteps, double* t_inout) {
+  if (!c || nsteps < 0) return TRAPBEC_ERR_ARG;
+  int rc = apply_staged(c);
+  if (rc) return rc;
+  if (t_inout) c->t = *t_inout;
+  c->step_async = true;
+  rc = DISPATCH(c, do_step_rt, c, nsteps);
+  c->step_async = false;
+  if (t_inout) *t_inout = c->t;
+  return rc;
+}
+
+int trapbec_set_psi_async(trapbec_ctx* c, const void* psi, int layout) {
+  if (!c || !psi) return TRAPBEC_ERR_ARG;
+  if (layout != TRAPBEC_LAYOUT_INTERIOR) {
+    set_error("trapbec_set_psi_async takes the interior layout");
+    return TRAPBEC_ERR_ARG;
+  }
+  int rc = ensure_async(c, true, false);
+  if (rc) return rc;
+  if (c->stage_free_rec) CK(cudaStreamWaitEvent(c->cs_in, c->ev_stage_free, 0));
+  CK(cudaMemcpyAsync(c->stage, psi, c->n * c->esz, cudaMemcpyHostToDevice, c->cs_in));
+  CK(cudaEventRecord(c->ev_staged, c->cs_in));
+  c->staged_pending = true;
+  return TRAPBEC_OK;
+}
+
+int trapbec_get_psi_async(trapbec_ctx* c, void* psi, int layout) {
+  if (!c || !psi) return TRAPBEC_ERR_ARG;
+  if (layout != TRAPBEC_LAYOUT_INTERIOR) {
+    set_error("trapbec_get_psi_async takes the interior layout");
+    return TRAPBEC_ERR_ARG;
+  }
+  int rc = ensure_async(c, false, true);
+  if (rc) return rc;
+  if ((rc = DISPATCH(c, apply_pending_scale, c))) return rc;
+  if (c->snap_drained_rec) CK(cudaStreamWaitEvent(c->st, c->ev_snap_drained, 0));
+  if ((rc = copy_state(c, c->snap, c->psi[c->cur]))) return rc;
+  CK(cudaEventRecord(c->ev_snap_ready, c->st));
+  CK(cudaStreamWaitEvent(c->cs_out, c->ev_snap_ready, 0));
+  CK(cudaMemcpyAsync(psi, c->snap, c->n * c->esz, cudaMemcpyDeviceToHost, c->cs_out));
+  CK(cudaEventRecord(c->ev_snap_drained, c->cs_out));
+  c->snap_drained_rec = true;
+  c->out_pending = true;
+  return TRAPBEC_OK;
+}
+
+int trapbec_wait_psi(trapbec_ctx* c) {
+  if (!c) return TRAPBEC_ERR_ARG;
+  if (c->out_pending) {
+    CK(cudaEventSynchronize(c->ev_snap_drained));
+    c->out_pending = false;
+  }
+  return TRAPBEC_OK;
+}
+
+int trapbec_synchronize(trapbec_ctx* c) {
+  if (!c) return TRAPBEC_ERR_ARG;
+  int rc = finish_steps(c);
+  if (c->cs_in) CK(cudaStreamSynchronize(c->cs_in));
+  if (c->cs_out) CK(cudaStreamSynchronize(c->cs_out));
+  CK(cudaStreamSynchronize(c->st));
+  c->out_pending = false;
   return rc;
 }
 
@@ -1143,7 +1304,9 @@ int trapbec_step_imag(trapbec_ctx* c, int nsteps, int variant, double tol, int* 
   if (!c || nsteps < 0) return TRAPBEC_ERR_ARG;
   int sd = 0;
   double st = 0;
-  int rc;
+  int rc = finish_steps(c);
+  if (rc) return rc;
+  if ((rc = apply_staged(c))) return rc;
   if (variant == TRAPBEC_IMAG_REF_EULER) rc = DISPATCH(c, do_imag_euler, c, nsteps, &sd, &st);
   else if (variant == TRAPBEC_IMAG_RK3_RENORM) rc = DISPATCH(c, do_imag_rk3, c, nsteps, tol, &sd, &st);
   else { set_error("bad imaginary-time variant"); return TRAPBEC_ERR_ARG; }
@@ -1184,6 +1347,8 @@ extern "C" {
 
 int trapbec_diag(trapbec_ctx* c, trapbec_diag_out* out) {
   if (!c || !out) return TRAPBEC_ERR_ARG;
+  int rc = finish_steps(c);
+  if (rc) return rc;
   return DISPATCH(c, diag_impl, c, out);
 }
 
@@ -1478,7 +1643,9 @@ extern "C" {
 int trapbec_autotune(trapbec_ctx* c, int steps, int* tile_z, int* tile_y, int* chunk, double* ms_per_step) {
   if (!c || steps < 1) return TRAPBEC_ERR_ARG;
   TuneVal bv;
-  int rc = DISPATCH(c, autotune_impl, c, steps, &bv);
+  int rc = finish_steps(c);
+  if (rc) return rc;
+  rc = DISPATCH(c, autotune_impl, c, steps, &bv);
   if (rc) return rc;
   if (!c->plan_rt_valid || c->plan_rt.shape != bv.shape) {   // a cached choice
     int r2 = c->prec == TRAPBEC_FP64 ? plan_tiled<double>(c->p, c->psi, c->w, c->w2, c->nsm, bv.shape, c->d_err, &c->plan_rt)
@@ -1504,6 +1671,8 @@ int trapbec_launch_count(trapbec_ctx* c, int64_t* count) {
 
 int trapbec_last_kernel_ms(trapbec_ctx* c, double* ms) {
   if (!c || !ms) return TRAPBEC_ERR_ARG;
+  int rc = finish_steps(c);
+  if (rc) return rc;
   *ms = c->last_ms;
   return TRAPBEC_OK;
 }
@@ -1549,6 +1718,9 @@ int trapbec_write_restart(trapbec_ctx* c, const char* datadir, int itime, double
 
 int trapbec_read_restart(trapbec_ctx* c, const char* datadir, int* nstart, double* t) {
   if (!c || !datadir || !nstart || !t) return TRAPBEC_ERR_ARG;
+  int rc0 = finish_steps(c);
+  if (rc0) return rc0;
+  c->staged_pending = false;   // the restart state replaces a queued one
   // The reference reader looks in proc%02d (initial.f90:44,800) while the
   // writer uses proc%03d (output.f90:103); accept both, proc000 first.
   std::vector<char> buf(c->n * c->esz);

@@ -28,6 +28,7 @@ class Solver:
         self.rdtype = np.float64 if fp64 else np.float32
         self.shape = (params.nx, params.ny, params.nz)
         self.t = 0.0
+        self._held_in, self._held_out = [], []   # host arrays of copies in flight (set/get_psi_async)
 
     # -- lifetime --------------------------------------------------------
     def close(self) -> None:
@@ -67,6 +68,43 @@ class Solver:
             a = out
         check(self.lib.trapbec_get_psi(self.ctx, a.ctypes.data, layout), "trapbec_get_psi")
         return a.reshape(shp)
+
+    # -- overlapped host copies ---------------------------------------------
+    def set_psi_async(self, psi: np.ndarray) -> None:
+        """Queue `psi` (interior layout; pinned memory lets the copy overlap the steps): it is
+        copied up at once and becomes the state at the next step_rt / step_rt_async / step_imag."""
+        a = np.ascontiguousarray(psi, dtype=self.cdtype)
+        if a.size != int(np.prod(self.shape)):
+            raise ValueError("set_psi_async: psi must have the grid's size")
+        check(self.lib.trapbec_set_psi_async(self.ctx, a.ctypes.data, abi.LAYOUT_INTERIOR), "trapbec_set_psi_async")
+        self._held_in.append(a)
+
+    def get_psi_async(self, out: np.ndarray) -> None:
+        """Snapshot the state after the queued steps and copy it into `out` (C-contiguous, the
+        context's dtype) in the background; `out` holds it after wait_psi() or synchronize()."""
+        if out.dtype != self.cdtype or out.size != int(np.prod(self.shape)) or not out.flags["C_CONTIGUOUS"]:
+            raise ValueError("get_psi_async: out must be a C-contiguous array of the context's dtype and size")
+        check(self.lib.trapbec_get_psi_async(self.ctx, out.ctypes.data, abi.LAYOUT_INTERIOR), "trapbec_get_psi_async")
+        self._held_out.append(out)
+
+    def step_rt_async(self, nsteps: int) -> float:
+        """step_rt that returns once the steps are queued; returns the t they reach."""
+        t = C.c_double(self.t)
+        check(self.lib.trapbec_step_rt_async(self.ctx, int(nsteps), C.byref(t)), "trapbec_step_rt_async")
+        self.t = t.value
+        return self.t
+
+    def wait_psi(self) -> None:
+        check(self.lib.trapbec_wait_psi(self.ctx), "trapbec_wait_psi")
+        self._held_out.clear()
+
+    def synchronize(self) -> None:
+        """Wait for every queued step and copy (reports a timed-out device wait of queued steps)."""
+        try:
+            check(self.lib.trapbec_synchronize(self.ctx), "trapbec_synchronize")
+        finally:
+            self._held_in.clear()
+            self._held_out.clear()
 
     def set_trap(self, trap: np.ndarray) -> None:
         a = np.ascontiguousarray(trap.reshape(self.shape), dtype=np.float64)
