@@ -495,6 +495,7 @@ def run_gpu_arm(args):
         reps = max(1, args.e2e_reps)
 
         parts = []
+        serial_diag = []
 
         def e2e_call(r):
             ta = time.perf_counter()
@@ -503,7 +504,7 @@ def run_gpu_arm(args):
             s.step_rt(shots)                                       # RK3 steps (waits for the H2D and the steps)
             tb = time.perf_counter()
             steps_ms = s.last_kernel_ms()
-            s.diag()                                               # FP64 diagnostics (Psi_info/Psi_norm, E)
+            serial_diag[:] = [s.diag()]                            # FP64 diagnostics (Psi_info/Psi_norm, E)
             tc = time.perf_counter()
             s.get_psi(out=host_out)                                # D2H of the state into pinned memory
             td = time.perf_counter()
@@ -524,43 +525,47 @@ def run_gpu_arm(args):
         serial_last = host_out.copy()
 
         def e2e_pipelined(nrep):
-            """The same calls with the host copies overlapped: call r+1's state goes up
-            (set_psi_async) while call r's steps run, and call r's result comes back
-            (get_psi_async) while call r+1's steps run; the caller takes each result
-            (wait_psi) before asking for the next."""
+            """The same calls, two deep and with the host copies overlapped: call r+1's
+            state goes up (set_psi_async) while call r's steps run, call r+1's steps are
+            queued behind call r's diagnostics before the host waits for them, and call
+            r's state comes back (get_psi_async) while call r+1's steps run.  The caller
+            takes each call's diagnostics and state before the next call's are asked for."""
             marks = []
             s.set_psi_async(host)
+            s.set_scalar(abi.SCALAR_OMEGA_Z, omega_of_step(args.warmup + args.steps))
+            s.step_rt_async(shots)                                 # call 0: its state, its steps
             for r in range(nrep):
-                s.set_scalar(abi.SCALAR_OMEGA_Z, omega_of_step(args.warmup + args.steps + r * shots))
-                s.step_rt_async(shots)                             # takes the queued state, queues the steps
+                s.get_psi_async(host_out)                          # D2H of call r's state, after its steps
+                s.diag_async()                                     # FP64 diagnostics of call r's state
                 if r + 1 < nrep:
-                    s.set_psi_async(host)                          # H2D of the next call's state
-                s.wait_psi()                                       # the previous call's result is on the host
-                s.get_psi_async(host_out)                          # D2H of this call's state, after its steps
-                s.diag()                                           # FP64 diagnostics of this call's state
+                    s.set_psi_async(host)                          # H2D of call r+1's state
+                    s.set_scalar(abi.SCALAR_OMEGA_Z, omega_of_step(args.warmup + args.steps + (r + 1) * shots))
+                    s.step_rt_async(shots)                         # call r+1's steps, queued behind them
+                diags.append(s.diag_wait())                        # call r's diagnostics on the host
+                s.wait_psi()                                       # call r's state on the host
                 marks.append(time.perf_counter())
-                steps_ms.append(s.last_kernel_ms())
             s.synchronize()
             marks.append(time.perf_counter())
             return marks
 
-        steps_ms = []
+        diags = []
 
         e2e_pipelined(1)                                           # untimed warm-up (allocates the copy buffers)
         host_out[:] = 0
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        steps_ms.clear()
+        diags.clear()
         marks = e2e_pipelined(reps)
         torch.cuda.synchronize()
         ep = time.perf_counter() - t0
         pipe_ms = [1e3 * (b - a) for a, b in zip([t0] + marks[:-2], marks[:-1])]
-        same = bool(np.array_equal(host_out.view(np.uint8), serial_last.view(np.uint8)))
+        same = bool(np.array_equal(host_out.view(np.uint8), serial_last.view(np.uint8)) and
+                    diags[-1] == serial_diag[-1])
         e2e = {"value": world * cells * shots * reps / ep, "unit": UNIT,
                "h2d_bytes_per_step": int(cells * host.itemsize / shots),
                "d2h_bytes_per_step": int(cells * host.itemsize / shots),
                "shots": shots, "host_buffers": "pinned (page-locked) input and output arrays",
-               "calls": reps, "call_ms": pipe_ms, "steps_device_ms": steps_ms,
+               "calls": reps, "call_ms": pipe_ms,
                "copies": "overlapped: set_psi_async / get_psi_async on copy streams beside the steps",
                "serial": {"value": world * cells * shots * reps / et, "call_ms": call_ms, "call_parts": parts},
                "pipelined_equals_serial": same,

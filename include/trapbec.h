@@ -22,7 +22,9 @@
  *    precision (TRAPBEC_FP32 -> float pairs, TRAPBEC_FP64 -> double pairs).
  *  - Array order is the reference's Psi(k,j,i): z fastest, then y, then x.
  *  - One host thread per context; each context owns one CUDA stream and all
- *    of its calls are ordered on it.  get/diag calls synchronise.
+ *    of its calls are ordered on it.  get/diag calls synchronise.  The
+ *    overlapped host copies (trapbec_set_psi_async, trapbec_get_psi_async)
+ *    run on two more streams of the context, ordered against it by events.
  *  - All quantities are in the reference's units (healing-length units with
  *    g = mu = 1/2 folded into the equation, finite_diff.f90:23-27,128-132).
  */
@@ -211,7 +213,12 @@ int trapbec_step_rt(trapbec_ctx* ctx, int nsteps, double* t_inout);
  *      device wait are reported by trapbec_synchronize or by the next call
  *      that waits (trapbec_diag, trapbec_get_psi, trapbec_step_rt, ...).
  *  trapbec_wait_psi      : wait for the copy of the last trapbec_get_psi_async.
- *  trapbec_synchronize   : wait for all queued steps and copies.           */
+ *  trapbec_synchronize   : wait for all queued steps and copies.
+ *  trapbec_diag_async    : queue trapbec_diag's reduction of the current state
+ *      (after all queued steps) without waiting, so that the next block of
+ *      steps can be queued behind it; trapbec_diag_wait returns its values
+ *      (TRAPBEC_ERR_STATE if none is pending, TRAPBEC_ERR_TIMEOUT if a
+ *      device wait of the steps before it timed out).                    */
 int trapbec_set_psi_async(trapbec_ctx* ctx, const void* psi, int layout);
 int trapbec_get_psi_async(trapbec_ctx* ctx, void* psi, int layout);
 int trapbec_step_rt_async(trapbec_ctx* ctx, int nsteps, double* t_inout);
@@ -263,6 +270,10 @@ typedef struct trapbec_diag_out {
   int32_t reserved;
 } trapbec_diag_out;
 int trapbec_diag(trapbec_ctx* ctx, trapbec_diag_out* out);
+/* trapbec_diag queued without waiting, and its result (see the overlapped
+ * host copies above).                                                      */
+int trapbec_diag_async(trapbec_ctx* ctx);
+int trapbec_diag_wait(trapbec_ctx* ctx, trapbec_diag_out* out);
 
 /* Bounded waits of the tiled stage kernels (no counterpart in the reference).
  * Every wait of a launch for its TMA data gives up after `limit`
@@ -388,6 +399,15 @@ int trapbec_last_kernel_ms(trapbec_ctx* ctx, double* ms);
 int trapbec_write_var(trapbec_ctx* ctx, const char* datadir, int itime, int shots,
                       double t, int imaginary);
 int trapbec_write_restart(trapbec_ctx* ctx, const char* datadir, int itime, double t);
+/* The same two files for a state already in host memory (interior layout,
+ * the precision of *p), e.g. one read back by trapbec_get_psi_async, so that
+ * the files are written while the next steps run.                         */
+int trapbec_write_var_host(const trapbec_params* p, const char* datadir, int itime, int shots, double t,
+                           int imaginary, const void* psi);
+int trapbec_write_restart_host(const trapbec_params* p, const char* datadir, int itime, double t, const void* psi);
+/* Page-locked host memory for the overlapped copies (cudaMallocHost).      */
+int trapbec_host_alloc(size_t bytes, void** out);
+void trapbec_host_free(void* p);
 /* Write data/proc000/vel##.dat or qpress##.dat (one record: coords(2) int32,
  * the field as vel(1:nz,1:ny,1:nx,3)), as var_print does when vel_print /
  * qpress_print are set (output.f90:80-91); ## is itime/shots in i2.2.      */

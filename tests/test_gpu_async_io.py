@@ -4,6 +4,8 @@ diagnostics of the plain one bit for bit, a queued state must not be seen
 before the next time-stepping call, and a timed-out device wait inside
 queued steps must still be reported (a wait pointed at an mbarrier phase
 nothing completes, as in test_gpu_failures.py; no GPU fault)."""
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -69,6 +71,29 @@ def test_pipelined_calls_match_plain_calls(prec, form):
     assert s.t == ref.t
     assert s.last_kernel_ms() > 0.0
     s.close()
+
+    # two calls deep: the second call's state and steps are queued before the
+    # first call's diagnostics and state are read back
+    s = Solver(p)
+    s.set_stage_form(form)
+    out_a[...] = 0
+    out_b[...] = 0
+    s.set_psi_async(host_a)
+    s.step_rt_async(k)
+    s.get_psi_async(out_a)
+    s.diag_async()
+    s.set_psi_async(host_b)
+    s.step_rt_async(k)
+    da = s.diag_wait()
+    s.wait_psi()
+    s.get_psi_async(out_b)
+    s.diag_async()
+    db = s.diag_wait()
+    s.synchronize()
+    assert np.array_equal(out_a.view(np.uint8), want_a.view(np.uint8))
+    assert np.array_equal(out_b.view(np.uint8), want_b.view(np.uint8))
+    assert da == want_da and db == want_db
+    s.close()
     ref.close()
 
 
@@ -130,10 +155,21 @@ def test_queued_steps_report_a_timed_out_wait():
     with pytest.raises(TrapbecError) as e:
         s.synchronize()
     assert e.value.code == abi.ERR_TIMEOUT
+    s.step_rt_async(1)                            # the queued diagnostics report it as well
+    s.diag_async()
+    with pytest.raises(TrapbecError) as e:
+        s.diag_wait()
+    assert e.value.code == abi.ERR_TIMEOUT
+    with pytest.raises(TrapbecError) as e:
+        s.synchronize()
+    assert e.value.code == abi.ERR_TIMEOUT
     s.set_wait_limit(0, inject=False)
     s.set_psi(a)
     s.step_rt(2)
     assert s.diag()["nonfinite"] == 0
+    with pytest.raises(TrapbecError) as e:        # nothing pending
+        s.diag_wait()
+    assert e.value.code == abi.ERR_STATE
     s.close()
 
 
@@ -147,4 +183,34 @@ def test_async_calls_take_the_interior_layout_only():
     assert s.lib.trapbec_wait_psi(s.ctx) == abi.OK
     assert s.lib.trapbec_synchronize(s.ctx) == abi.OK
     assert s.lib.trapbec_synchronize(None) == abi.ERR_ARG
+    s.close()
+
+
+@pytest.mark.parametrize("prec", [abi.FP32, abi.FP64])
+def test_host_state_writers_write_the_context_writers_bytes(prec, tmp_path):
+    """var####.dat and var.dat from a state read back by get_psi_async
+    (trapbec_write_var_host / _restart_host) are the bytes trapbec_write_var /
+    trapbec_write_restart write for the same state."""
+    import os
+    p = _problem(prec)
+    s = Solver(p)
+    s.set_psi(_state(p, seed=6))
+    s.step_rt(2)
+    a, b = str(tmp_path / "a"), str(tmp_path / "b")
+    for d in (a, b):
+        os.makedirs(os.path.join(d, "proc000"))
+    s.write_var(a, itime=200, shots=100)
+    s.write_restart(a, itime=200)
+    keep, host = _pinned_like(s.get_psi())
+    s.get_psi_async(host)
+    s.wait_psi()
+    lib = s.lib
+    assert lib.trapbec_write_var_host(C.byref(s.params), b.encode(), 200, 100, s.t, 0, host.ctypes.data) == abi.OK
+    assert lib.trapbec_write_restart_host(C.byref(s.params), b.encode(), 200, s.t, host.ctypes.data) == abi.OK
+    for f in ("var0002.dat", "var.dat"):
+        assert open(os.path.join(a, "proc000", f), "rb").read() == open(os.path.join(b, "proc000", f), "rb").read()
+    ptr = C.c_void_p()
+    assert lib.trapbec_host_alloc(64, C.byref(ptr)) == abi.OK and ptr.value
+    lib.trapbec_host_free(ptr)
+    assert lib.trapbec_host_alloc(0, C.byref(ptr)) == abi.ERR_ARG
     s.close()

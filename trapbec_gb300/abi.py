@@ -141,6 +141,8 @@ _PROTOS = {
                                     C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     "trapbec_set_imag_stop": (C.c_int, [_VP, C.c_int, C.c_double]),
     "trapbec_diag": (C.c_int, [_VP, C.POINTER(DiagOut)]),
+    "trapbec_diag_async": (C.c_int, [_VP]),
+    "trapbec_diag_wait": (C.c_int, [_VP, C.POINTER(DiagOut)]),
     "trapbec_set_wait_limit": (C.c_int, [_VP, C.c_uint32, C.c_int]),
     "trapbec_force_vortex": (C.c_int, [_VP, C.c_double, C.c_double, C.c_double]),
     "trapbec_force_random_points": (C.c_int, [_VP, C.c_uint64, C.c_uint64, C.POINTER(C.c_double)]),
@@ -159,6 +161,11 @@ _PROTOS = {
     "trapbec_last_kernel_ms": (C.c_int, [_VP, C.POINTER(C.c_double)]),
     "trapbec_write_var": (C.c_int, [_VP, C.c_char_p, C.c_int, C.c_int, C.c_double, C.c_int]),
     "trapbec_write_restart": (C.c_int, [_VP, C.c_char_p, C.c_int, C.c_double]),
+    "trapbec_write_var_host": (C.c_int, [C.POINTER(Params), C.c_char_p, C.c_int, C.c_int, C.c_double, C.c_int,
+                                         _VP]),
+    "trapbec_write_restart_host": (C.c_int, [C.POINTER(Params), C.c_char_p, C.c_int, C.c_double, _VP]),
+    "trapbec_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(_VP)]),
+    "trapbec_host_free": (None, [_VP]),
     "trapbec_write_field": (C.c_int, [_VP, C.c_char_p, C.c_int, C.c_int, C.c_int]),
     "trapbec_read_restart": (C.c_int, [_VP, C.c_char_p, C.POINTER(C.c_int),
                                        C.POINTER(C.c_double)]),

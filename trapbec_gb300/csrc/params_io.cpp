@@ -389,6 +389,25 @@ int trapbec_params_parse(const char* text, trapbec_params* p, char* errbuf, size
   return tbh::parse_cparam_text(text, p, nullptr, errbuf, errlen);
 }
 
+// var_print / the restart writer for a state already in host memory
+// (output.f90:64-75,102-108): the files trapbec_write_var and
+// trapbec_write_restart write for the context's state.
+int trapbec_write_var_host(const trapbec_params* p, const char* datadir, int itime, int shots, double t,
+                           int imaginary, const void* psi) {
+  if (!p || !datadir || !psi || shots <= 0) return TRAPBEC_ERR_ARG;
+  const size_t bytes = (size_t)p->nx * p->ny * p->nz * (p->precision == TRAPBEC_FP64 ? 16 : 8);
+  char name[64];
+  // output.f90:65,75: "./data/proc%03d/var%04d.dat" with itime/shots
+  std::snprintf(name, sizeof(name), "/proc%03d/%s%04d.dat", 0, imaginary ? "imag_var" : "var", itime / shots);
+  return tbh::write_var_file(std::string(datadir) + name, p, t, psi, bytes);
+}
+
+int trapbec_write_restart_host(const trapbec_params* p, const char* datadir, int itime, double t, const void* psi) {
+  if (!p || !datadir || !psi) return TRAPBEC_ERR_ARG;
+  const size_t bytes = (size_t)p->nx * p->ny * p->nz * (p->precision == TRAPBEC_FP64 ? 16 : 8);
+  return tbh::write_restart_file(std::string(datadir) + "/proc000/var.dat", p, itime, t, psi, bytes);
+}
+
 int trapbec_write_dims(const trapbec_params* p, const char* datadir) {  // output.f90:48-60
   if (!p || !datadir) return TRAPBEC_ERR_ARG;
   std::string d(datadir);

@@ -60,6 +60,23 @@ using tbh::set_error;
   } while (0)
 
 // ---------------------------------------------------------------- context --
+struct AsyncDiag {       // what trapbec_diag_async leaves in host memory
+  double red[NRED];      // the reduction's NRED values
+  int err;               // the tiled kernel's error flag at that point of the stream
+};
+
+// Store the finalised reduction and the error flag straight into the
+// page-locked slot (mapped into the device's address space): a copy-engine
+// transfer on the context stream would queue behind a large read-back on the
+// copy stream in the same direction and hold the next steps back.
+__global__ void publish_diag_kernel(const double* __restrict__ red_out, const int* __restrict__ d_err,
+                                    AsyncDiag* __restrict__ dst) {
+  const int i = threadIdx.x;
+  if (i < NRED) dst->red[i] = red_out[i];
+  if (i == NRED) dst->err = *d_err;
+  __threadfence_system();
+}
+
 struct trapbec_ctx {
   trapbec_params p;
   int prec = TRAPBEC_FP64;
@@ -127,6 +144,10 @@ struct trapbec_ctx {
   bool out_pending = false;            // a read-back is in flight
   bool step_async = false;             // do_step_rt returns after queueing (trapbec_step_rt_async)
   bool steps_pending = false;          // queued steps not yet waited for (timing and error flag unread)
+  AsyncDiag* adiag = nullptr;          // page-locked result slot of trapbec_diag_async
+  AsyncDiag* adiag_dev = nullptr;      // its device-side address
+  cudaEvent_t ev_diag = nullptr;       // st: that slot is filled
+  bool diag_pending = false;
 };
 
 namespace {
@@ -462,7 +483,8 @@ template <typename T> int apply_pending_scale(trapbec_ctx* c) {
 }
 
 // Diagnostics reduction of the current psi into c->host_red[NRED].
-template <typename T> int run_diag(trapbec_ctx* c) {
+// Queue the diagnostics reduction of the current psi into c->red_out[NRED].
+template <typename T> int enqueue_diag(trapbec_ctx* c) {
   int rc = ensure_potential<T>(c, c->t);
   if (rc) return rc;
   StageArgs<T> a = base_args<T>(c, c->t);
@@ -475,9 +497,34 @@ template <typename T> int run_diag(trapbec_ctx* c) {
   reduce_finalize_kernel<<<1, FIN_THREADS, 0, c->st>>>(c->red, nblk, c->red_out);
   CKL();
   c->launches++;
+  return TRAPBEC_OK;
+}
+
+template <typename T> int run_diag(trapbec_ctx* c) {
+  int rc = enqueue_diag<T>(c);
+  if (rc) return rc;
   CK(cudaMemcpyAsync(c->host_red, c->red_out, sizeof(double) * NRED, cudaMemcpyDeviceToHost, c->st));
   CK(cudaStreamSynchronize(c->st));
   return check_device_error(c);
+}
+
+// trapbec_diag_async: the reduction, then its values and the tiled kernel's
+// error flag into the context's page-locked slot, with no wait.
+template <typename T> int diag_async_impl(trapbec_ctx* c) {
+  int rc = apply_pending_scale<T>(c);
+  if (rc) return rc;
+  if (!c->adiag) {
+    CK(cudaHostAlloc(&c->adiag, sizeof(AsyncDiag), cudaHostAllocMapped));
+    CK(cudaHostGetDevicePointer((void**)&c->adiag_dev, c->adiag, 0));
+  }
+  if (!c->ev_diag) CK(cudaEventCreateWithFlags(&c->ev_diag, cudaEventDisableTiming));
+  if ((rc = enqueue_diag<T>(c))) return rc;
+  publish_diag_kernel<<<1, 32, 0, c->st>>>(c->red_out, c->d_err, c->adiag_dev);
+  CKL();
+  c->launches++;
+  CK(cudaEventRecord(c->ev_diag, c->st));
+  c->diag_pending = true;
+  return TRAPBEC_OK;
 }
 
 template <typename T> double cell_volume(const trapbec_ctx* c) {
@@ -486,8 +533,7 @@ template <typename T> double cell_volume(const trapbec_ctx* c) {
   return hx * hy * (p.two_dim ? 1.0 : hz);
 }
 
-template <typename T> void fill_diag(trapbec_ctx* c, trapbec_diag_out* o) {
-  const double* r = c->host_red;
+template <typename T> void fill_diag(trapbec_ctx* c, const double* r, trapbec_diag_out* o) {
   const trapbec_params& p = c->p;
   double dV = cell_volume<T>(c);
   o->intpsi2 = r[0];
@@ -958,7 +1004,9 @@ void free_ctx(trapbec_ctx* c) {
   if (c->host_red) cudaFreeHost(c->host_red);
   if (c->h_err) cudaFreeHost(c->h_err);
   if (c->host_ctrl) cudaFreeHost(c->host_ctrl);
-  for (cudaEvent_t e : {c->e0, c->e1, c->ev_staged, c->ev_stage_free, c->ev_snap_ready, c->ev_snap_drained})
+  if (c->adiag) cudaFreeHost(c->adiag);
+  for (cudaEvent_t e : {c->e0, c->e1, c->ev_staged, c->ev_stage_free, c->ev_snap_ready, c->ev_snap_drained,
+                        c->ev_diag})
     if (e) cudaEventDestroy(e);
   if (c->cs_in) cudaStreamDestroy(c->cs_in);
   if (c->cs_out) cudaStreamDestroy(c->cs_out);
@@ -1339,7 +1387,7 @@ template <typename T> int diag_impl(trapbec_ctx* c, trapbec_diag_out* o) {
   int rc = apply_pending_scale<T>(c);
   if (rc) return rc;
   if ((rc = run_diag<T>(c))) return rc;
-  fill_diag<T>(c, o);
+  fill_diag<T>(c, c->host_red, o);
   return TRAPBEC_OK;
 }
 }  // namespace
@@ -1350,6 +1398,29 @@ int trapbec_diag(trapbec_ctx* c, trapbec_diag_out* out) {
   int rc = finish_steps(c);
   if (rc) return rc;
   return DISPATCH(c, diag_impl, c, out);
+}
+
+int trapbec_diag_async(trapbec_ctx* c) {
+  if (!c) return TRAPBEC_ERR_ARG;
+  return DISPATCH(c, diag_async_impl, c);
+}
+
+int trapbec_diag_wait(trapbec_ctx* c, trapbec_diag_out* out) {
+  if (!c || !out) return TRAPBEC_ERR_ARG;
+  if (!c->diag_pending) {
+    set_error("trapbec_diag_wait: no trapbec_diag_async is pending");
+    return TRAPBEC_ERR_STATE;
+  }
+  c->diag_pending = false;
+  CK(cudaEventSynchronize(c->ev_diag));
+  if (c->adiag->err != 0) {   // the flag stays set on the device: the next waiting call reports it too
+    set_error("device-side wait timed out in the tiled stage kernel (code " + std::to_string(c->adiag->err) +
+              ") before the diagnostics");
+    return TRAPBEC_ERR_TIMEOUT;
+  }
+  if (c->prec == TRAPBEC_FP64) fill_diag<double>(c, c->adiag->red, out);
+  else fill_diag<float>(c, c->adiag->red, out);
+  return TRAPBEC_OK;
 }
 
 }  // extern "C"
@@ -1683,10 +1754,7 @@ int trapbec_write_var(trapbec_ctx* c, const char* datadir, int itime, int shots,
   std::vector<char> buf(c->n * c->esz);
   int rc = trapbec_get_psi(c, buf.data(), TRAPBEC_LAYOUT_INTERIOR);
   if (rc) return rc;
-  char name[64];
-  // output.f90:65,75: "./data/proc%03d/var%04d.dat" with itime/shots
-  std::snprintf(name, sizeof(name), "/proc%03d/%s%04d.dat", 0, imaginary ? "imag_var" : "var", itime / shots);
-  return tbh::write_var_file(std::string(datadir) + name, &c->p, t, buf.data(), buf.size());
+  return trapbec_write_var_host(&c->p, datadir, itime, shots, t, imaginary, buf.data());
 }
 
 int trapbec_write_field(trapbec_ctx* c, const char* datadir, int itime, int shots, int which) {
@@ -1712,8 +1780,18 @@ int trapbec_write_restart(trapbec_ctx* c, const char* datadir, int itime, double
   std::vector<char> buf(c->n * c->esz);
   int rc = trapbec_get_psi(c, buf.data(), TRAPBEC_LAYOUT_INTERIOR);
   if (rc) return rc;
-  return tbh::write_restart_file(std::string(datadir) + "/proc000/var.dat", &c->p, itime, t, buf.data(),
-                                 buf.size());
+  return trapbec_write_restart_host(&c->p, datadir, itime, t, buf.data());
+}
+
+int trapbec_host_alloc(size_t bytes, void** out) {
+  if (!out || bytes == 0) return TRAPBEC_ERR_ARG;
+  *out = nullptr;
+  CK(cudaMallocHost(out, bytes));
+  return TRAPBEC_OK;
+}
+
+void trapbec_host_free(void* p) {
+  if (p) cudaFreeHost(p);
 }
 
 int trapbec_read_restart(trapbec_ctx* c, const char* datadir, int* nstart, double* t) {

@@ -213,13 +213,33 @@ int main(int argc, char** argv) {
   const uint64_t force_seed = std::getenv("TRAPBEC_FORCE_SEED") ? std::strtoull(std::getenv("TRAPBEC_FORCE_SEED"), nullptr, 10) : 1;
   double tot_ms = 0.0;
   int timed_steps = 0;
+  // The state of an output step is read back into page-locked memory on a
+  // copy stream (trapbec_get_psi_async) and its var####.dat and var.dat are
+  // written from there while the next block of steps runs; the files are the
+  // ones var_print writes at that step (output.f90:64-75,102-108).
+  const size_t state_bytes = (size_t)p.nx * p.ny * p.nz * (p.precision == TRAPBEC_FP64 ? 16 : 8);
+  void* out_buf = nullptr;
+  check(trapbec_host_alloc(state_bytes, &out_buf), "output buffer");
+  bool out_pending = false;
+  int out_last = 0;
+  double out_t = 0.0;
+  auto flush_output = [&]() {
+    if (!out_pending) return;
+    out_pending = false;
+    check(trapbec_wait_psi(ctx), "var_print: read-back");
+    if (rc.full_binary_output)
+      check(trapbec_write_var_host(&p, datadir.c_str(), out_last, rc.shots, out_t, 0, out_buf), "var_print");
+    check(trapbec_write_restart_host(&p, datadir.c_str(), out_last, out_t, out_buf), "var_print: var.dat");
+  };
   for (int itime = nstart; itime <= rc.nsteps;) {   // run.f90:43-76
     int m = (itime + rc.shots - 1) / rc.shots * rc.shots;   // next output step
     if (rc.forcing) m = std::min(m, (itime + rc.force_freq - 1) / rc.force_freq * rc.force_freq);
     const int k = std::min(m - itime + 1, rc.nsteps - itime + 1);
-    check(trapbec_step_rt(ctx, k, &t), "RK3 step");
+    const int st = trapbec_step_rt_async(ctx, k, &t);
+    flush_output();   // the last output's files, written while these steps run
+    check(st, "RK3 step");
     double ms = 0;
-    trapbec_last_kernel_ms(ctx, &ms);
+    check(trapbec_last_kernel_ms(ctx, &ms), "RK3 step");   // waits for the steps
     tot_ms += ms;
     timed_steps += k;
     itime += k;
@@ -232,18 +252,22 @@ int main(int argc, char** argv) {
       std::printf("\n");
       if (d.nonfinite) emergency_stop("non-finite values in Psi");
       // run.f90:64-66 computes the diagnostics, output.f90:73-91 writes them
-      if (rc.full_binary_output) check(trapbec_write_var(ctx, datadir.c_str(), last, rc.shots, t, 0), "var_print");
       if (rc.vel_print)
         check(trapbec_write_field(ctx, datadir.c_str(), last, rc.shots, TRAPBEC_FIELD_VELOCITY), "get_phase");
       if (rc.qpress_print)
         check(trapbec_write_field(ctx, datadir.c_str(), last, rc.shots, TRAPBEC_FIELD_QPRESSURE), "get_qpressure");
       if (rc.gnuplot_2d_print) write_2d_slice(ctx, p, datadir, last / rc.shots);
-      check(trapbec_write_restart(ctx, datadir.c_str(), last, t), "var_print: var.dat");
+      check(trapbec_get_psi_async(ctx, out_buf, TRAPBEC_LAYOUT_INTERIOR), "var_print: read-back");
+      out_pending = true;
+      out_last = last;
+      out_t = t;
     }
     if (rc.forcing && last % rc.force_freq == 0)   // run.f90:70-74
       check(trapbec_force_random_points(ctx, force_seed, (uint64_t)(last / rc.force_freq), nullptr),
             "force_random_points");
   }
+  flush_output();
+  trapbec_host_free(out_buf);
   const double tpt = timed_steps ? tot_ms * 1e-3 / timed_steps : 0.0;
   check(trapbec_write_timing(&p, datadir.c_str(), tpt, 0.0), "print_timing");
   trapbec_destroy(ctx);

@@ -94,6 +94,15 @@ class Solver:
         self.t = t.value
         return self.t
 
+    def diag_async(self) -> None:
+        """Queue diag()'s reduction of the state after the queued steps; diag_wait() returns it."""
+        check(self.lib.trapbec_diag_async(self.ctx), "trapbec_diag_async")
+
+    def diag_wait(self) -> dict:
+        d = DiagOut()
+        check(self.lib.trapbec_diag_wait(self.ctx, C.byref(d)), "trapbec_diag_wait")
+        return d.as_dict()
+
     def wait_psi(self) -> None:
         check(self.lib.trapbec_wait_psi(self.ctx), "trapbec_wait_psi")
         self._held_out.clear()
