@@ -525,22 +525,29 @@ def run_gpu_arm(args):
         serial_last = host_out.copy()
 
         def e2e_pipelined(nrep):
-            """The same calls, two deep and with the host copies overlapped: call r+1's
-            state goes up (set_psi_async) while call r's steps run, call r+1's steps are
-            queued behind call r's diagnostics before the host waits for them, and call
-            r's state comes back (get_psi_async) while call r+1's steps run.  The caller
-            takes each call's diagnostics and state before the next call's are asked for."""
+            """The same calls, queued ahead with the host copies overlapped: call r+1's
+            steps are queued behind call r's diagnostics before the host waits for those,
+            call r+2's state goes up (set_psi_async) while call r+1's steps run, and call
+            r's state comes back (get_psi_async) while call r+1's steps run, so each copy
+            has a whole block of steps to hide in.  The caller takes each call's
+            diagnostics and state before the next call's are asked for."""
             marks = []
-            s.set_psi_async(host)
-            s.set_scalar(abi.SCALAR_OMEGA_Z, omega_of_step(args.warmup + args.steps))
-            s.step_rt_async(shots)                                 # call 0: its state, its steps
+
+            def queue_steps(r):
+                s.set_scalar(abi.SCALAR_OMEGA_Z, omega_of_step(args.warmup + args.steps + r * shots))
+                s.step_rt_async(shots)                             # takes call r's queued state
+
+            s.set_psi_async(host)                                  # call 0's state
+            queue_steps(0)
+            if nrep > 1:
+                s.set_psi_async(host)                              # call 1's state, during call 0's steps
             for r in range(nrep):
                 s.get_psi_async(host_out)                          # D2H of call r's state, after its steps
                 s.diag_async()                                     # FP64 diagnostics of call r's state
                 if r + 1 < nrep:
-                    s.set_psi_async(host)                          # H2D of call r+1's state
-                    s.set_scalar(abi.SCALAR_OMEGA_Z, omega_of_step(args.warmup + args.steps + (r + 1) * shots))
-                    s.step_rt_async(shots)                         # call r+1's steps, queued behind them
+                    queue_steps(r + 1)                             # call r+1's steps, queued behind them
+                if r + 2 < nrep:
+                    s.set_psi_async(host)                          # H2D of call r+2's state
                 diags.append(s.diag_wait())                        # call r's diagnostics on the host
                 s.wait_psi()                                       # call r's state on the host
                 marks.append(time.perf_counter())
@@ -742,7 +749,7 @@ def main():
     ap.add_argument("--n", type=int, default=512, help="grid size per axis (profiling uses smaller cases)")
     ap.add_argument("--chunk", type=int, default=20, help="RK3 steps per C-ABI call (Omega updated per call)")
     ap.add_argument("--shots", type=int, default=100, help="RK3 steps per end-to-end call")
-    ap.add_argument("--e2e-reps", type=int, default=5, help="timed end-to-end calls (after one untimed call)")
+    ap.add_argument("--e2e-reps", type=int, default=10, help="timed end-to-end calls (after one untimed call)")
     ap.add_argument("--precision-steps", type=int, default=500,
                     help="steps of the FP32 / compensated FP32 / FP64 comparison from the same start")
     ap.add_argument("--start", default="ground", choices=["ground", "tf"],
