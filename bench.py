@@ -392,6 +392,17 @@ def warmstart_leg(args):
     }
 
 
+def max_over_ranks(values, dist, device):
+    """Each of `values` replaced by its maximum over the ranks (the slowest rank's
+    times); unchanged on a single process."""
+    if dist is None:
+        return list(values)
+    import torch
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.tolist()]
+
+
 def aggregate_ranks(ms_local, units_local, dist, device):
     """Whole-job figure of N replica ranks: the slowest rank's timed milliseconds
     (max over ranks) and the units all ranks processed in that time."""
@@ -514,6 +525,8 @@ def run_gpu_arm(args):
         e2e_call(0)                                                # untimed warm-up call
         parts.clear()
         torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
         t0 = time.perf_counter()
         call_ms = []
         for r in range(reps):
@@ -559,12 +572,15 @@ def run_gpu_arm(args):
 
         e2e_pipelined(1)                                           # untimed warm-up (allocates the copy buffers)
         host_out[:] = 0
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
         diags.clear()
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
         marks = e2e_pipelined(reps)
         torch.cuda.synchronize()
         ep = time.perf_counter() - t0
+        et, ep = max_over_ranks([et, ep], dist, "cuda")         # the slowest rank's times for both loops
         pipe_ms = [1e3 * (b - a) for a, b in zip([t0] + marks[:-2], marks[:-1])]
         same = bool(np.array_equal(host_out.view(np.uint8), serial_last.view(np.uint8)) and
                     diags[-1] == serial_diag[-1])

@@ -18,7 +18,8 @@ def _rank(rank, world, port, out):
     sys.path.insert(0, ROOT)
     import bench
     ms, value = bench.aggregate_ranks(10.0 + 5.0 * rank, 1000 * (rank + 1), dist, "cpu")
-    out[rank] = (ms, value)
+    slowest = bench.max_over_ranks([1.0 + rank, 3.0 - rank], dist, "cpu")
+    out[rank] = (ms, value, slowest)
     dist.barrier()
     dist.destroy_process_group()
 
@@ -30,6 +31,7 @@ def test_two_replica_ranks_aggregate():
         mp.spawn(_rank, args=(2, port, out), nprocs=2, join=True)
         res = dict(out)
     for r in (0, 1):
-        ms, value = res[r]
+        ms, value, slowest = res[r]
         assert ms == 15.0                               # the slowest rank
         assert abs(value - 3000 / 15e-3) < 1e-6 * value  # all ranks' units in that time
+        assert slowest == [2.0, 3.0]                    # end-to-end times: each the slowest rank's
