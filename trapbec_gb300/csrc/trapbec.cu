@@ -1786,7 +1786,13 @@ int trapbec_write_restart(trapbec_ctx* c, const char* datadir, int itime, double
 int trapbec_host_alloc(size_t bytes, void** out) {
   if (!out || bytes == 0) return TRAPBEC_ERR_ARG;
   *out = nullptr;
-  CK(cudaMallocHost(out, bytes));
+  const cudaError_t e = cudaMallocHost(out, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    *out = nullptr;
+    set_error(std::string("trapbec_host_alloc: ") + cudaGetErrorString(e));
+    return e == cudaErrorMemoryAllocation ? TRAPBEC_ERR_NOMEM : TRAPBEC_ERR_CUDA;
+  }
   return TRAPBEC_OK;
 }
 
