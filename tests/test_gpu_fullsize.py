@@ -8,7 +8,9 @@ seeded Thomas-Fermi cloud with 1e-2 phase noise) in a rotating frame:
 - the evolution commutes with the rotation by pi about the trap axis,
   (x, y) -> (-x, -y), which maps the cell-centred grid, the harmonic trap,
   the rotating-frame term x d/dy - y d/dx and the zero boundaries onto
-  themselves.
+  themselves;
+- and, over 2 steps (the oracle's C++ restatement on all host cores, about a
+  second per step at this size), both forms match the oracle itself.
 Tolerances are relative L2 norms of the difference (FP32 rounding over the
 steps taken), and 1e-6 on the FP64 norm and energy of the diagnostics.
 Measured on a GB300: forms 2.2e-7, phase 1.9e-7, rotation 6.1e-8 (the grid's
@@ -45,10 +47,10 @@ def start():
     return psi
 
 
-def _run(psi, form):
+def _run(psi, form, steps=STEPS):
     s, _ = _solver(form)
     s.set_psi(psi)
-    s.step_rt(STEPS)
+    s.step_rt(steps)
     out, d = s.get_psi(), s.diag()
     s.close()
     return out, d
@@ -89,3 +91,46 @@ def test_rotation_by_pi_about_the_trap_axis_commutes_with_the_step(start, refere
     b, db = _run(np.ascontiguousarray(start[::-1, ::-1, :]), abi.RK3_PSI_DIFF)
     assert _l2(np.ascontiguousarray(b[::-1, ::-1, :]), a) < L2_TOL
     _same_diag(db, da)
+
+
+def test_both_forms_match_the_oracle_at_full_size(start):
+    from oracle.pyoracle import Oracle
+    Oracle.set_threads(Oracle.max_threads())
+    s, _ = _solver(abi.RK3_PSI_DIFF)
+    o = Oracle(s.params)
+    s.close()
+    o.set_psi(start)
+    o.step_rt(2)
+    want, dw = o.get_psi(), o.diag()
+    for form in (abi.RK3_PSI_DIFF, abi.RK3_THREE_STAGE):
+        got, dg = _run(start, form, steps=2)
+        assert _l2(got, want) < L2_TOL, form
+        _same_diag(dg, dw)
+
+
+def test_psi_diff_matches_the_oracle_at_the_1024_stretch_size():
+    """The workload's largest size, 1024^3 (8 GiB per complex FP32 array, so
+    byte offsets into a state run past 2^32): 2 steps of the headline form
+    against the oracle from the seeded start state."""
+    from oracle.pyoracle import Oracle
+    Oracle.set_threads(Oracle.max_threads())
+    prob, init = units.rotating_quench_512(abi.FP32, n=1024)
+    p = prob.to_params()
+    p.omega_z = prob.omega_z_for(0.5 * init["omega_final"])
+    s = Solver(p)
+    s.set_stage_form(abi.RK3_PSI_DIFF)
+    s.init_state(init["name"], seed=init["seed"], amp=init["amp"], r_tf2=init["r_tf2"],
+                 noise_amp=init["noise_amp"])
+    psi = s.get_psi()
+    s.step_rt(2)
+    got, dg = s.get_psi(), s.diag()
+    s.close()
+    assert got.shape == (1024, 1024, 1024)
+    o = Oracle(p)
+    o.set_psi(psi)
+    del psi
+    o.step_rt(2)
+    want, dw = o.get_psi(), o.diag()
+    del o
+    assert _l2(got, want) < L2_TOL
+    _same_diag(dg, dw)
