@@ -10,7 +10,9 @@ seeded Thomas-Fermi cloud with 1e-2 phase noise) in a rotating frame:
   the rotating-frame term x d/dy - y d/dx and the zero boundaries onto
   themselves;
 - and, over 2 steps (the oracle's C++ restatement on all host cores, about a
-  second per step at this size), both forms match the oracle itself.
+  second per step at this size), both forms match the oracle itself; so does
+  the headline form at the 1024^3 stretch size, and the FP64 path at the
+  vortex-ring workload's 256^3 to 1e-12.
 Tolerances are relative L2 norms of the difference (FP32 rounding over the
 steps taken), and 1e-6 on the FP64 norm and energy of the diagnostics.
 Measured on a GB300: forms 2.2e-7, phase 1.9e-7, rotation 6.1e-8 (the grid's
@@ -134,3 +136,28 @@ def test_psi_diff_matches_the_oracle_at_the_1024_stretch_size():
     del o
     assert _l2(got, want) < L2_TOL
     _same_diag(dg, dw)
+
+
+def test_fp64_matches_the_oracle_to_1e12_at_the_256_ring_size():
+    """The FP64 path at the vortex-ring workload's full size (256^3 on
+    [-32,32]^3, anisotropic trap, TF background times a ring of radius 8 with
+    1e-3 phase noise): 10 steps against the FP64 oracle, 1e-12 relative in
+    psi (max norm), norm and energy."""
+    from oracle.pyoracle import Oracle
+    Oracle.set_threads(Oracle.max_threads())
+    prob, init = units.vortex_ring_256(abi.FP64)
+    p = prob.to_params()
+    s = Solver(p)
+    s.init_state(init["name"], seed=init["seed"], amp=init["amp"], r_tf2=init["r_tf2"],
+                 ring_radius=init["ring_radius"], noise_amp=init["noise_amp"])
+    psi = s.get_psi()
+    s.step_rt(10)
+    got, dg = s.get_psi(), s.diag()
+    s.close()
+    o = Oracle(p)
+    o.set_psi(psi)
+    o.step_rt(10)
+    want, dw = o.get_psi(), o.diag()
+    assert float(np.max(np.abs(got - want)) / np.max(np.abs(want))) < 1e-12
+    for k in ("norm", "energy"):
+        assert abs(dg[k] - dw[k]) <= 1e-12 * abs(dw[k]), (k, dg[k], dw[k])
