@@ -125,3 +125,28 @@ def test_batch_absolute_stop_per_instance_scale_fp64():
     b.set_imag_stop(abi.STOP_REL)
     with pytest.raises(abi.TrapbecError):
         b.set_imag_stop(abi.STOP_ABS, [1.0, 0.0, 1.0])
+
+
+def test_batch_matches_single_grid_at_workload_sizes():
+    """Draws of the batched ground-state workload itself (uneven 64^3 / 96^3 /
+    128^3 grids, traps, g and rotation, FP32 state from the TF guess with
+    seeded noise): 20 imaginary-time RK3 steps in one batch against each draw
+    relaxed alone through the single-grid path."""
+    from trapbec_gb300 import units
+    draws = units.ground_state_draws(4, 11, grids=(64, 96, 128), precision=abi.FP32)
+    assert len({p.n for p, _ in draws}) > 1
+    b = BatchSolver([p.to_params() for p, _ in draws])
+    for i, (p, ini) in enumerate(draws):
+        b.init_state(i, ini["name"], seed=ini["seed"], amp=ini["amp"], r_tf2=ini["r_tf2"],
+                     noise_amp=ini["noise_amp"])
+    out = b.solve(max_steps=20, tol=0.0, check_every=20)
+    assert out["steps"] == [20] * len(draws)
+    for i, (p, ini) in enumerate(draws):
+        s = Solver(p.to_params())
+        s.init_state(ini["name"], seed=ini["seed"], amp=ini["amp"], r_tf2=ini["r_tf2"], noise_amp=ini["noise_amp"])
+        steps, _ = s.step_imag(20, abi.IMAG_RK3_RENORM, 0.0)
+        assert steps == 20
+        a, ref = b.get_psi(i).astype(np.complex128), s.get_psi().astype(np.complex128)
+        assert np.linalg.norm(a - ref) / np.linalg.norm(ref) < 1e-6, i
+        s.close()
+    b.close()
