@@ -443,6 +443,8 @@ def run_gpu_arm(args):
     tune = None
     if args.kernel is None and not args.no_autotune:
         tune = s.autotune(steps=8)   # tile shape and work order for this grid (state restored)
+    if args.work_chunk is not None:
+        s.set_chunk(args.work_chunk)   # a given work order (negative: the strided order)
     s.init_state(init["name"], seed=init["seed"] + rank, amp=init["amp"], r_tf2=init["r_tf2"],
                  noise_amp=init["noise_amp"])
     ramp_steps = 5000
@@ -777,6 +779,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--kernel", type=int, nargs=3, default=None, metavar=("KIND", "TZ", "TY"))
     ap.add_argument("--no-autotune", action="store_true", help="keep the default tile shape and work order")
+    ap.add_argument("--work-chunk", type=int, default=None,
+                    help="work order of the timed run's tiled kernel (trapbec_set_chunk; < 0: strided order)")
     ap.add_argument("--stage-form", type=int, default=3, choices=[0, 1, 2, 3],
                     help="real-time RK3 form of the timed run: 0 three full stages, 1 deferred psi1 "
                          "(stage 1 stores w1 only), 2 compensated state, 3 psi difference (no w array)")

@@ -325,9 +325,13 @@ int trapbec_set_kernel(trapbec_ctx* ctx, int kind, int tile_z, int tile_y);
  * launches use the per-cell kernel.                                         */
 int trapbec_get_tile_shape(trapbec_ctx* ctx, int real_time, int* tile_z, int* tile_y);
 
-/* Work order of the tiled kernel: x-planes per chunk (0 = automatic).  Tiles
- * adjacent in y are processed chunk by chunk so their shared ghost rows are
- * served from L2.                                                          */
+/* Work order of the tiled kernel (0 = automatic).  chunk > 0: each CTA takes
+ * a contiguous range of work units in (z-tile, x-chunk, y-tile, x) order with
+ * chunks of `chunk` x-planes (nx: tile-major).  chunk < 0: the strided order,
+ * segments of -chunk x-planes in (x-chunk, z-tile, y-tile) order dealt
+ * round-robin over the CTAs, so neighbouring tiles are streamed over the same
+ * x-range at the same time and their shared ghost rows are served from L2 on
+ * grids of many more tiles than CTAs.  trapbec_autotune reports either.     */
 int trapbec_set_chunk(trapbec_ctx* ctx, int chunk);
 
 /* Form of the real-time RK3 step (run.f90:42-57) on the tiled kernel.

@@ -147,7 +147,7 @@ def test_bad_arguments_return_status_and_leave_the_context_usable():
     assert lib.trapbec_set_kernel(s.ctx, 2, -99, 0) == abi.ERR_UNSUPPORTED  # no such built shape
     assert lib.trapbec_set_kernel(s.ctx, 2, 48, 48) == abi.ERR_UNSUPPORTED  # no shape of this size
     assert lib.trapbec_set_stage_form(s.ctx, 4) == abi.ERR_ARG   # no such form
-    assert lib.trapbec_set_chunk(s.ctx, -1) == abi.ERR_ARG
+    assert lib.trapbec_set_chunk(s.ctx, -2 ** 31) == abi.ERR_ARG   # negative: the strided order; INT_MIN: none
     tz, ty = C.c_int(0), C.c_int(0)
     assert lib.trapbec_get_tile_shape(s.ctx, 1, None, C.byref(ty)) == abi.ERR_ARG
     assert lib.trapbec_get_tile_shape(s.ctx, 1, C.byref(tz), C.byref(ty)) == abi.OK

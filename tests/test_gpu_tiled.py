@@ -250,3 +250,32 @@ def test_default_plan_falls_back_to_a_shape_that_fits():
     o.step_rt(6)
     a, b = s.get_psi().astype(np.complex128), o.get_psi().astype(np.complex128)
     assert np.linalg.norm(a - b) / np.linalg.norm(b) < 2e-6
+
+
+@pytest.mark.parametrize("prec", [abi.FP32, abi.FP64])
+@pytest.mark.parametrize("form", [abi.RK3_THREE_STAGE, abi.RK3_PSI_DIFF])
+@pytest.mark.parametrize("chunk", [-8, -36, -128])
+def test_strided_order_gives_the_same_states(prec, form, chunk):
+    """The strided work order (set_chunk < 0: segments dealt round-robin over
+    the CTAs) changes which CTA streams which tiles and x-range, not the
+    arithmetic of a point: the states are bit for bit those of the default
+    order.  96 x 128 x 256 has 16 tiles of (64 x 32): chunks of 8 planes make
+    192 segments (more than the CTAs), of 36 a ragged last chunk and idle
+    CTAs, of 128 (clamped to nx) one segment per tile.  The diagnostics run
+    in the same order, with their partial sums grouped by CTA differently."""
+    p = params(n=(96, 128, 256), L=(24.0, 32.0, 64.0), prec=prec, pot="harmonic", harm=(3.0, 4.0, 5.0),
+               omega=0.3, dt=0.01)
+    psi = smooth_state(p, seed=31)
+    out = {}
+    for ch in (0, chunk):
+        s = Solver(p)
+        s.set_stage_form(form)
+        s.set_chunk(ch)
+        s.set_psi(psi)
+        s.step_rt(6)
+        out[ch] = (s.get_psi(), s.diag())
+        s.close()
+    (a, da), (b, db) = out[0], out[chunk]
+    assert np.array_equal(a.view(np.uint8), b.view(np.uint8))
+    for k in ("intpsi2", "energy", "maxpsi", "minpsi"):
+        assert abs(da[k] - db[k]) <= 1e-9 * abs(da[k]), (k, da[k], db[k])

@@ -384,8 +384,17 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
   };
 
   const long long total = BATCH ? ba.ustart[ba.nact] : ta0.units;
-  const long long G0 = (long long)blockIdx.x * total / gridDim.x;
-  const long long G1 = (long long)(blockIdx.x + 1) * total / gridDim.x;
+  // Strided order (single grids, chunk < 0): segments of -chunk x-planes in
+  // (x-chunk, z-tile, y-tile) order, dealt round-robin over the CTAs, so the
+  // CTAs stream neighbouring tiles over the same x-range at the same time and
+  // the ghost rows two tiles share are read from DRAM once, then from L2.  On
+  // a grid of more tiles than CTAs the contiguous order below streams a tile's
+  // neighbours at other times, and their shared rows come from DRAM twice.
+  const bool strided = !BATCH && ta0.chunk < 0;
+  const long long nsegs =   // strided: segments of the whole grid
+      strided ? (long long)((ta0.s.nx - ta0.chunk - 1) / (-ta0.chunk)) * ta0.ntz * ta0.nty : 0;
+  const long long G0 = strided ? (long long)blockIdx.x : (long long)blockIdx.x * total / gridDim.x;
+  const long long G1 = strided ? nsegs : (long long)(blockIdx.x + 1) * total / gridDim.x;
   uint32_t seq = 0;       // load sequence number of the first plane of a segment
   uint32_t seq_issue = 0; // next sequence number to issue (thread 0)
   bool failed = false;
@@ -452,17 +461,30 @@ stage_tiled_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constan
     // Work units are ordered (z-tile, x-chunk, y-tile, x); with the default
     // chunk = nx this is tile-major order and each CTA streams a contiguous
     // x-range of one or two tiles.
-    const long long per_tz = (long long)ta.nty * nx;
-    const int tzi = (int)(u0 / per_tz);
-    const long long rr0 = u0 - (long long)tzi * per_tz;
-    const int xc = (int)(rr0 / ((long long)ta.nty * L));
-    const long long rr1 = rr0 - (long long)xc * ta.nty * L;
-    const int Lc = min(L, nx - xc * L);
-    const int tyi = (int)(rr1 / Lc);
-    const int xa = xc * L + (int)(rr1 - (long long)tyi * Lc);
-    int xb = xc * L + Lc;
-    if (g0 + (xb - xa) > uend) xb = xa + (int)(uend - g0);
-    g0 += xb - xa;
+    int tzi, tyi, xa, xb;
+    if (strided) {   // g0 is the segment index
+      const int Ls = -L;
+      const long long per_x = (long long)ta.ntz * ta.nty;
+      const int xc = (int)(g0 / per_x);
+      const long long rem = g0 - (long long)xc * per_x;
+      tzi = (int)(rem / ta.nty);
+      tyi = (int)(rem - (long long)tzi * ta.nty);
+      xa = xc * Ls;
+      xb = min(xa + Ls, nx);
+      g0 += gridDim.x;
+    } else {
+      const long long per_tz = (long long)ta.nty * nx;
+      tzi = (int)(u0 / per_tz);
+      const long long rr0 = u0 - (long long)tzi * per_tz;
+      const int xc = (int)(rr0 / ((long long)ta.nty * L));
+      const long long rr1 = rr0 - (long long)xc * ta.nty * L;
+      const int Lc = min(L, nx - xc * L);
+      tyi = (int)(rr1 / Lc);
+      xa = xc * L + (int)(rr1 - (long long)tyi * Lc);
+      xb = xc * L + Lc;
+      if (g0 + (xb - xa) > uend) xb = xa + (int)(uend - g0);
+      g0 += xb - xa;
+    }
     if (skip) continue;   // converged grid in a batch: nothing to do, nothing loaded
 
     const int z0 = tzi * TZ;

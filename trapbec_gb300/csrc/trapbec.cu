@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -308,7 +309,8 @@ template <typename T> StageArgs<T> base_args(trapbec_ctx* c, double t) {
 // Default x-chunk of the work order (the autotuner may pick another).
 int auto_chunk(const trapbec_ctx* c) {
   if (c->chunk_user > 0) return std::min(c->chunk_user, c->p.nx);
-  return c->p.nx;   // tile-major: measured fastest at 512^3; the autotuner tries shorter chunks
+  if (c->chunk_user < 0) return -std::min(-c->chunk_user, c->p.nx);   // the strided order
+  return c->p.nx;   // tile-major: measured fastest at 512^3; the autotuner tries other orders
 }
 
 template <typename T> bool use_tiled(trapbec_ctx* c) {
@@ -1566,7 +1568,7 @@ int trapbec_set_kernel(trapbec_ctx* c, int kind, int tile_z, int tile_y) {
 }
 
 int trapbec_set_chunk(trapbec_ctx* c, int chunk) {
-  if (!c || chunk < 0) return TRAPBEC_ERR_ARG;
+  if (!c || chunk == INT_MIN) return TRAPBEC_ERR_ARG;
   c->chunk_user = chunk;
   if (c->plan_valid) c->plan.chunk = auto_chunk(c);
   if (c->plan_rt_valid) c->plan_rt.chunk = auto_chunk(c);
@@ -1672,9 +1674,10 @@ template <typename T> int autotune_impl(trapbec_ctx* c, int steps, TuneVal* best
     if (plan_tiled<T>(c->p, c->psi, c->w, c->w2, c->nsm, sh, c->d_err, &plan) != 0) continue;
     if (c->stage_form == TRAPBEC_RK3_COMPENSATED && !plan.comp_ok) continue;
     if (c->stage_form == TRAPBEC_RK3_PSI_DIFF && !plan.pdiff_ok) continue;
-    std::vector<int> chunks = {16, 32, 64, c->p.nx};
+    // contiguous unit ranges per CTA (chunk > 0) and the strided order (chunk < 0)
+    std::vector<int> chunks = {16, 32, 64, c->p.nx, -64, -128, -256};
     for (int L : chunks) {
-      if (L > c->p.nx) continue;
+      if (L > c->p.nx || -L > c->p.nx) continue;
       plan.chunk = L;
       c->plan_rt = plan;
       c->plan_rt_valid = true;
