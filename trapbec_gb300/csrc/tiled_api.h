@@ -17,7 +17,8 @@ struct TiledPlan {
   int ntz = 0, nty = 0;
   long long units = 0;
   int fix_y = 0, fix_z = 0, bcz = 0;
-  int chunk = 0;         // x-chunk length of the work order (nx: tile-major)
+  int chunk = 0;         // x-chunk length of the work order (nx: tile-major; < 0: the strided order)
+  int chunk_s1 = 0;      // work order of the stage-1 kinds when it differs (0: chunk)
   const void* psi_base[2] = {nullptr, nullptr};
   const void* w_base[2] = {nullptr, nullptr};   // w, second w buffer (deferred form)
   CUtensorMap tm[2];

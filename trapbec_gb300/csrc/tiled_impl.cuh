@@ -191,7 +191,8 @@ int launch_shape(const TiledPlan& plan, int kind, const StageArgs<T>& a, cudaStr
   ta.bcz = plan.bcz;
   ta.fix_y = plan.fix_y;
   ta.fix_z = plan.fix_z;
-  ta.chunk = plan.chunk;
+  const bool stage1 = kind == ST_S1 || kind == ST_S1P || kind == ST_S1W;
+  ta.chunk = (stage1 && plan.chunk_s1 != 0) ? plan.chunk_s1 : plan.chunk;
   ta.wait_us = plan.wait_us;
   ta.inject_wait = plan.inject_wait;
   fill_coeffs<T>(ta);

@@ -1570,8 +1570,8 @@ int trapbec_set_kernel(trapbec_ctx* c, int kind, int tile_z, int tile_y) {
 int trapbec_set_chunk(trapbec_ctx* c, int chunk) {
   if (!c || chunk == INT_MIN) return TRAPBEC_ERR_ARG;
   c->chunk_user = chunk;
-  if (c->plan_valid) c->plan.chunk = auto_chunk(c);
-  if (c->plan_rt_valid) c->plan_rt.chunk = auto_chunk(c);
+  if (c->plan_valid) { c->plan.chunk = auto_chunk(c); c->plan.chunk_s1 = 0; }
+  if (c->plan_rt_valid) { c->plan_rt.chunk = auto_chunk(c); c->plan_rt.chunk_s1 = 0; }
   return TRAPBEC_OK;
 }
 
@@ -1644,7 +1644,7 @@ struct TuneKey {
   trapbec_params p;
   bool operator==(const TuneKey& o) const { return std::memcmp(&p, &o.p, sizeof(p)) == 0; }
 };
-struct TuneVal { int shape, chunk; double ms; };
+struct TuneVal { int shape, chunk, chunk_s1; double ms; };
 std::vector<std::pair<TuneKey, TuneVal>> g_tune_cache;
 std::mutex g_tune_mu;
 
@@ -1666,7 +1666,7 @@ template <typename T> int autotune_impl(trapbec_ctx* c, int steps, TuneVal* best
   CK(cudaMemcpyAsync(save, c->psi[c->cur], c->n * c->esz, cudaMemcpyDeviceToDevice, c->st));
   const double t_save = c->t;
   const int cur_save = c->cur;
-  TuneVal bv{-1, 0, 1e300};
+  TuneVal bv{-1, 0, 0, 1e300};
   const int ns = tiled_nshapes<T>();
   int rc = TRAPBEC_OK;
   for (int sh = 0; sh < ns && rc == TRAPBEC_OK; ++sh) {
@@ -1685,10 +1685,30 @@ template <typename T> int autotune_impl(trapbec_ctx* c, int steps, TuneVal* best
       if ((rc = do_step_rt<T>(c, 1))) break;     // warm-up
       if ((rc = do_step_rt<T>(c, steps))) break;
       double ms = c->last_ms / steps;
-      if (ms < bv.ms) bv = TuneVal{sh, L, ms};
+      if (ms < bv.ms) bv = TuneVal{sh, L, 0, ms};
       CK(cudaMemcpyAsync(c->psi[cur_save], save, c->n * c->esz, cudaMemcpyDeviceToDevice, c->st));
       c->cur = cur_save;
       c->t = t_save;
+    }
+  }
+  // When the strided order won, stage 1 alone in the contiguous order: the
+  // stage-1 kinds are not bound by HBM and pay for the strided order's extra
+  // segment starts more than they gain from its L2 reuse.
+  if (rc == TRAPBEC_OK && bv.shape >= 0 && bv.chunk < 0) {
+    TiledPlan plan;
+    if (plan_tiled<T>(c->p, c->psi, c->w, c->w2, c->nsm, bv.shape, c->d_err, &plan) == 0) {
+      plan.chunk = bv.chunk;
+      plan.chunk_s1 = c->p.nx;
+      c->plan_rt = plan;
+      c->plan_rt_valid = true;
+      c->kernel_kind = 2;
+      if ((rc = do_step_rt<T>(c, 1)) == TRAPBEC_OK && (rc = do_step_rt<T>(c, steps)) == TRAPBEC_OK) {
+        const double ms = c->last_ms / steps;
+        if (ms < bv.ms) {
+          bv.chunk_s1 = c->p.nx;
+          bv.ms = ms;
+        }
+      }
     }
   }
   CK(cudaMemcpyAsync(c->psi[cur_save], save, c->n * c->esz, cudaMemcpyDeviceToDevice, c->st));
@@ -1702,6 +1722,7 @@ template <typename T> int autotune_impl(trapbec_ctx* c, int steps, TuneVal* best
   if (bv.shape < 0) { set_error("no tiled kernel shape fits this grid"); return TRAPBEC_ERR_UNSUPPORTED; }
   if (plan_tiled<T>(c->p, c->psi, c->w, c->w2, c->nsm, bv.shape, c->d_err, &c->plan_rt) != 0) return TRAPBEC_ERR_CUDA;
   c->plan_rt.chunk = bv.chunk;
+  c->plan_rt.chunk_s1 = bv.chunk_s1;
   c->plan_rt_valid = true;
   c->shape_rt = bv.shape;
   {
@@ -1729,6 +1750,7 @@ int trapbec_autotune(trapbec_ctx* c, int steps, int* tile_z, int* tile_y, int* c
     c->shape_rt = bv.shape;
   }
   c->plan_rt.chunk = bv.chunk;
+  c->plan_rt.chunk_s1 = bv.chunk_s1;
   Shape sh = c->prec == TRAPBEC_FP64 ? tiled_shape<double>(bv.shape) : tiled_shape<float>(bv.shape);
   if (tile_z) *tile_z = sh.tz;
   if (tile_y) *tile_y = sh.ty;
