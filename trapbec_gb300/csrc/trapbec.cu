@@ -1691,23 +1691,26 @@ template <typename T> int autotune_impl(trapbec_ctx* c, int steps, TuneVal* best
       c->t = t_save;
     }
   }
-  // When the strided order won, stage 1 alone in the contiguous order: the
-  // stage-1 kinds are not bound by HBM and pay for the strided order's extra
-  // segment starts more than they gain from its L2 reuse.
-  if (rc == TRAPBEC_OK && bv.shape >= 0 && bv.chunk < 0) {
+  // On the best shape, the stage-1 kinds in the contiguous tile-major order
+  // and the other stages in the strided one: the stage-1 kinds are not bound
+  // by HBM and pay for the strided order's extra segment starts more than
+  // they gain from its L2 reuse.
+  if (rc == TRAPBEC_OK && bv.shape >= 0) {
     TiledPlan plan;
     if (plan_tiled<T>(c->p, c->psi, c->w, c->w2, c->nsm, bv.shape, c->d_err, &plan) == 0) {
-      plan.chunk = bv.chunk;
-      plan.chunk_s1 = c->p.nx;
-      c->plan_rt = plan;
-      c->plan_rt_valid = true;
-      c->kernel_kind = 2;
-      if ((rc = do_step_rt<T>(c, 1)) == TRAPBEC_OK && (rc = do_step_rt<T>(c, steps)) == TRAPBEC_OK) {
+      for (int L : {-64, -128, -256}) {
+        if (-L > c->p.nx) continue;
+        plan.chunk = L;
+        plan.chunk_s1 = c->p.nx;
+        c->plan_rt = plan;
+        c->plan_rt_valid = true;
+        c->kernel_kind = 2;
+        if ((rc = do_step_rt<T>(c, 1)) || (rc = do_step_rt<T>(c, steps))) break;
         const double ms = c->last_ms / steps;
-        if (ms < bv.ms) {
-          bv.chunk_s1 = c->p.nx;
-          bv.ms = ms;
-        }
+        if (ms < bv.ms) bv = TuneVal{bv.shape, L, c->p.nx, ms};
+        CK(cudaMemcpyAsync(c->psi[cur_save], save, c->n * c->esz, cudaMemcpyDeviceToDevice, c->st));
+        c->cur = cur_save;
+        c->t = t_save;
       }
     }
   }
