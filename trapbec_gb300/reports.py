@@ -25,6 +25,7 @@ def _run(prec, n, steps, chunk, psi0=None, seed=1234, form=abi.RK3_THREE_STAGE):
                      ring_radius=init["ring_radius"], noise_amp=init["noise_amp"])
     else:
         s.set_psi(psi0)
+    s.autotune(steps=3)   # tile shape and work order for this grid and form (state restored)
     d0 = s.diag()
     ms = 0.0
     done = 0
